@@ -1,0 +1,82 @@
+"""Build libcrm_gb300.so (sm_103a) in-tree with nvcc.
+
+Three translation units, compiled in parallel:
+  crm_fp64.cu  FP64 column kernel, -fmad=false (bit-identical to a CPU run)
+  crm_fp32.cu  FP32-mixed column kernel
+  crm_host.cu  the C ABI (include/crm_gb300.h), host code built with
+               -ffp-contract=off for the same reason
+"""
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.dirname(HERE)
+CSRC = os.path.join(PKG, 'csrc')
+REPO = os.path.dirname(PKG)
+LIB = os.path.join(HERE, 'libcrm_gb300.so')
+OBJ = os.path.join(PKG, '_build')
+
+ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
+COMMON = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC,-ffp-contract=off',
+          '-I' + os.path.join(REPO, 'include')]
+UNITS = {
+    'crm_fp64': ['-fmad=false'],
+    'crm_fp32': [],
+    'crm_host': [],
+}
+
+
+def _nvcc():
+    for c in (os.environ.get('NVCC'), '/usr/local/cuda/bin/nvcc', 'nvcc'):
+        if c and (os.path.isabs(c) and os.path.exists(c) or not os.path.isabs(c)):
+            return c
+    return 'nvcc'
+
+
+def _sources():
+    out = []
+    for d in (CSRC, os.path.join(REPO, 'include')):
+        out += [os.path.join(d, f) for f in os.listdir(d)
+                if f.endswith(('.cu', '.cuh', '.h'))]
+    return out
+
+
+def up_to_date():
+    if not os.path.exists(LIB):
+        return False
+    t = os.path.getmtime(LIB)
+    return all(os.path.getmtime(s) <= t for s in _sources())
+
+
+def build(force=False, verbose=False):
+    """Compile the library if any source is newer than it; returns its path."""
+    if not force and up_to_date():
+        return LIB
+    os.makedirs(OBJ, exist_ok=True)
+    nvcc = _nvcc()
+
+    def compile_unit(name):
+        obj = os.path.join(OBJ, name + '.o')
+        cmd = [nvcc] + ARCH + COMMON + UNITS[name] + ['-c', os.path.join(CSRC, name + '.cu'), '-o', obj]
+        if verbose:
+            print(' '.join(cmd), file=sys.stderr)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError('nvcc failed for %s:\n%s%s' % (name, r.stdout, r.stderr))
+        return obj
+
+    with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
+        objs = list(ex.map(compile_unit, UNITS))
+    tmp = LIB + '.tmp'
+    cmd = [nvcc] + ARCH + ['-shared', '-o', tmp] + objs
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError('nvcc link failed:\n%s%s' % (r.stdout, r.stderr))
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == '__main__':
+    print(build(force='--force' in sys.argv, verbose=True))

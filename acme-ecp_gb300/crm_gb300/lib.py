@@ -1,0 +1,116 @@
+"""ctypes binding of libcrm_gb300.so (include/crm_gb300.h).
+
+This is the binding a Python host would add; a Fortran host binds the same
+symbols through iso_c_binding.  There is no CPU fallback: if the library or
+a CUDA device is missing, CrmContext raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import types as T
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, 'libcrm_gb300.so')
+
+EXPORTS = ('crm_create', 'crm_destroy', 'crm_run', 'crm_last_launch_count',
+           'crm_last_kernel_ms', 'crm_set_stream', 'crm_status_string', 'crm_version')
+
+_lib = None
+
+
+class CrmError(RuntimeError):
+    def __init__(self, status, what=''):
+        self.status = status
+        super().__init__('%s: %s (status %d)' % (what or 'crm', status_string(status), status))
+
+
+def load(path=None, build_if_missing=False):
+    """Load the library (optionally building it first)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise OSError('libcrm_gb300.so not built: run crm_gb300.build.build()')
+        from . import build as B
+        path = B.build()
+    lib = C.CDLL(path)
+    lib.crm_create.restype = C.c_void_p
+    lib.crm_create.argtypes = [C.POINTER(T.CCrmConfig), C.POINTER(C.c_int)]
+    lib.crm_destroy.restype = None
+    lib.crm_destroy.argtypes = [C.c_void_p]
+    lib.crm_run.restype = C.c_int
+    lib.crm_run.argtypes = [C.c_void_p, C.POINTER(T.CCrmCallDesc), C.POINTER(T.CCrmInput),
+                            C.POINTER(T.CCrmState), C.POINTER(T.CCrmRad), C.POINTER(T.CCrmOutput),
+                            C.POINTER(C.c_int)]
+    lib.crm_last_launch_count.restype = C.c_int
+    lib.crm_last_launch_count.argtypes = [C.c_void_p]
+    lib.crm_last_kernel_ms.restype = C.c_double
+    lib.crm_last_kernel_ms.argtypes = [C.c_void_p]
+    lib.crm_set_stream.restype = C.c_int
+    lib.crm_set_stream.argtypes = [C.c_void_p, C.c_void_p]
+    lib.crm_status_string.restype = C.c_char_p
+    lib.crm_status_string.argtypes = [C.c_int]
+    lib.crm_version.restype = C.c_char_p
+    lib.crm_version.argtypes = []
+    _lib = lib
+    return lib
+
+
+def status_string(s):
+    try:
+        return load().crm_status_string(int(s)).decode()
+    except OSError:
+        return 'status %d' % s
+
+
+class CrmContext:
+    """One configured handle (crm_create / crm_run / crm_destroy)."""
+
+    def __init__(self, cfg: T.CrmConfig):
+        lib = load()
+        self.cfg = cfg
+        st = C.c_int(0)
+        self._c_cfg = cfg.to_c()
+        h = lib.crm_create(C.byref(self._c_cfg), C.byref(st))
+        if not h:
+            raise CrmError(st.value, 'crm_create')
+        self._h = h
+        self._lib = lib
+
+    def close(self):
+        if getattr(self, '_h', None):
+            self._lib.crm_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_ptr):
+        return self._lib.crm_set_stream(self._h, C.c_void_p(stream_ptr))
+
+    def run(self, desc, cin, state, rad, out, raise_on_error=False):
+        """crm_run on host arrays; returns the per-column status array."""
+        status = np.zeros(desc.ncrms, dtype=np.int32)
+        c_in, c_st, c_rad, c_out = cin.to_c(), state.to_c(), rad.to_c(), out.to_c()
+        rc = self._lib.crm_run(self._h, C.byref(desc), C.byref(c_in), C.byref(c_st),
+                               C.byref(c_rad), C.byref(c_out),
+                               status.ctypes.data_as(C.POINTER(C.c_int)))
+        self.last_rc = rc
+        if raise_on_error and rc != T.CRM_OK:
+            raise CrmError(rc, 'crm_run')
+        return status
+
+    @property
+    def last_kernel_ms(self):
+        return self._lib.crm_last_kernel_ms(self._h)
+
+    @property
+    def last_launch_count(self):
+        return self._lib.crm_last_launch_count(self._h)

@@ -1,0 +1,2076 @@
+// crm_kernel.cuh -- the persistent column kernel: one CTA integrates one CRM
+// column through a whole GCM step (crm/crm_module.F90:380-1594), then takes
+// the next column.  T is the bulk arithmetic type (double: plain form;
+// float: FP32-mixed form, with FP64 kept for the pressure tridiagonal solve,
+// all domain-mean / column sums and the saturation-adjustment Newton solve).
+//
+// Every phase follows the reference routine named in its comment.  Cell-wise
+// loops are spread over the CTA's threads with a barrier between phases;
+// every sum over the horizontal runs sequentially in the reference's loop
+// order (one thread per level), so the FP64 form reproduces the CPU
+// restatement bit for bit.
+#pragma once
+#include "crm_device.cuh"
+#include "crm_kernel.h"
+
+namespace crm {
+
+// physical constants (crm/params.F90:49-64, shr_const_mod.F90)
+#define C_CP 1.00464e3
+#define C_GGR 9.80616
+#define C_LCOND 2.501e6
+#define C_LFUS 3.337e5
+#define C_LSUB (C_LCOND + C_LFUS)
+#define C_RGASU (6.02214e26 * 1.38065e-23)
+#define C_RV (C_RGASU / 18.016)
+#define C_FAC_COND (C_LCOND / C_CP)
+#define C_FAC_FUS (C_LFUS / C_CP)
+#define C_FAC_SUB (C_LSUB / C_CP)
+#define C_PI R4(3.141592653589793)
+#define C_EPSV R4(0.61)
+// MICRO_SAM1MOM/micro_params.F90
+#define C_TBGMIN R4(253.16)
+#define C_TBGMAX R4(273.16)
+#define C_TPRMIN R4(268.16)
+#define C_TPRMAX R4(283.16)
+#define C_TGRMIN R4(223.16)
+#define C_TGRMAX R4(283.16)
+#define C_A_RAIN 842.
+#define C_B_RAIN R4(0.8)
+#define C_A_SNOW R4(4.84)
+#define C_B_SNOW 0.25
+#define C_A_GRAU 94.5
+#define C_B_GRAU 0.5
+#define C_QCW0 R4(1.e-3)
+#define C_QCI0 R4(1.e-4)
+#define C_ALPHAELQ R4(1.e-3)
+#define C_BETAELQ R4(1.e-3)
+#define C_ESICOEF R4(0.1)
+#define C_EGICOEF R4(0.1)
+#define C_NZEROR 8.e6
+#define C_NZEROS 3.e6
+#define C_NZEROG 4.e6
+#define C_RHOR 1000.
+#define C_RHOS 100.
+#define C_RHOG 400.
+#define C_QP_THRESHOLD R4(1.e-8)
+#define C_DIFFELQ R4(2.21e-05)
+#define C_THERCO R4(2.40e-02)
+#define C_MUELQ R4(1.717e-05)
+
+#define TID ((int)threadIdx.x)
+#define NT ((int)blockDim.x)
+#define SYNC __syncthreads()
+
+// per-CTA scalars of the column being integrated
+struct ColShared {
+  int na, nb, nc, ncycle, icycle, nprec, status, kmin, kmax, n_damp, col;
+  double dt3[3], at, bt, ct, dtn, dtfactor, dz, cfl, prec_cfl, z0;
+  double colprec0, colprecs0;
+  double cltot, clhgh, clmed, cllow;
+  int jt_min, mx_max;
+  double red_d[32];
+  int red_i[64];
+};
+
+template <typename T>
+struct ColumnKernel {
+  const KParams &p;
+  ColShared &S;
+  T *base;
+  int nx, nzm, nz, plev, icrm;
+
+  __device__ ColumnKernel(const KParams &p_, ColShared &s_, T *b, int col)
+      : p(p_), S(s_), base(b), nx(p_.L.nx), nzm(p_.L.nzm), nz(p_.L.nz), plev(p_.L.plev), icrm(col) {}
+
+  // ---------------------------------------------------------- accessors
+  __device__ __forceinline__ F2<T> fld(size_t off, XRange x, int z1 = 1) const { return F2<T>{base + off, x.x1, x.nxa, z1}; }
+  __device__ __forceinline__ F2<T> U() const { return fld(p.L.u, p.L.xu); }
+  __device__ __forceinline__ F2<T> V() const { return fld(p.L.v, p.L.xv); }
+  __device__ __forceinline__ F2<T> W() const { return fld(p.L.w, p.L.xw); }
+  __device__ __forceinline__ F2<T> TT() const { return fld(p.L.t, p.L.xs); }
+  __device__ __forceinline__ F2<T> QT() const { return fld(p.L.qt, p.L.xs); }
+  __device__ __forceinline__ F2<T> QP() const { return fld(p.L.qp, p.L.xs); }
+  __device__ __forceinline__ F2<T> TKE() const { return fld(p.L.tke, p.L.xi); }
+  __device__ __forceinline__ F2<T> TK() const { return fld(p.L.tk, p.L.xd); }
+  __device__ __forceinline__ F2<T> TKH() const { return fld(p.L.tkh, p.L.xd); }
+  __device__ __forceinline__ F2<T> PP() const { return fld(p.L.p, p.L.xp); }
+  __device__ __forceinline__ F2<T> TABS() const { return fld(p.L.tabs, p.L.xi); }
+  __device__ __forceinline__ F2<T> QV() const { return fld(p.L.qv, p.L.xi); }
+  __device__ __forceinline__ F2<T> QCL() const { return fld(p.L.qcl, p.L.xi); }
+  __device__ __forceinline__ F2<T> QCI() const { return fld(p.L.qci, p.L.xi); }
+  __device__ __forceinline__ F2<T> QPL() const { return fld(p.L.qpl, p.L.xi); }
+  __device__ __forceinline__ F2<T> QPI() const { return fld(p.L.qpi, p.L.xi); }
+  __device__ __forceinline__ F2<T> QN() const { return fld(p.L.qn, p.L.xi); }
+  __device__ __forceinline__ F2<T> DU(int l) const { return fld(p.L.du[l - 1], p.L.xdu); }
+  __device__ __forceinline__ F2<T> DV(int l) const { return fld(p.L.dv[l - 1], p.L.xi); }
+  __device__ __forceinline__ F2<T> DW(int l) const { return fld(p.L.dw[l - 1], p.L.xi); }
+  // scratch planes (x from -2, k from 0)
+  __device__ __forceinline__ F2<T> SCR(size_t off) const { return F2<T>{base + off, -2, nx + 6, 0}; }
+  __device__ __forceinline__ T *PR(int id) const { return base + p.L.prof + (size_t)id * (nz + 2); }
+  __device__ __forceinline__ T *OP(int id) const { return base + p.L.o_plev + (size_t)id * (plev + 2); }
+  __device__ __forceinline__ T &PS(int i) const { return base[p.L.precsfc + (i - 1)]; }
+  __device__ __forceinline__ T &PSS(int i) const { return base[p.L.precssfc + (i - 1)]; }
+
+  __device__ __forceinline__ double IN(const double *a, int l) const { return a[(size_t)icrm + (size_t)p.ld * (l - 1)]; }
+  __device__ __forceinline__ size_t S4(int i, int k) const {
+    return (size_t)icrm + (size_t)p.ld * ((i - 1) + (size_t)nx * (k - 1));
+  }
+
+  // ---------------------------------------------------------- reductions
+  __device__ double block_max(double v) {
+    for (int o = 16; o > 0; o >>= 1) v = mx2(v, __shfl_xor_sync(0xffffffffu, v, o));
+    SYNC;
+    if ((TID & 31) == 0) S.red_d[TID >> 5] = v;
+    SYNC;
+    if (TID == 0) {
+      double m = S.red_d[0];
+      for (int w = 1; w < NT / 32; ++w) m = mx2(m, S.red_d[w]);
+      S.red_d[0] = m;
+    }
+    SYNC;
+    double r = S.red_d[0];
+    SYNC;
+    return r;
+  }
+
+  // ---------------------------------------------------------- halos
+  // bound_exchange.F90:188-236 (2D): periodic copies in x only
+  __device__ void exch(F2<T> f, int k1, int k2, int i_1, int i_2) {
+    int i1 = i_1 - 1, i2 = i_2 - 1;
+    int nl = i1 + 1, nr = i2 + 1, per = nl + nr;
+    int n = (k2 - k1 + 1) * per;
+    for (int e = TID; e < n; e += NT) {
+      int k = k1 + e / per, r = e % per;
+      if (r < nl) { int i = -i1 + r; f(i, k) = f(i + nx, k); }
+      else { int i = nx + 1 + (r - nl); f(i, k) = f(i - nx, k); }
+    }
+  }
+  __device__ void boundaries(int flag) {      // periodic.F90:8-136
+    if (flag == 0) {
+      exch(U(), 1, nzm, 1, 1);
+      exch(V(), 1, nzm, 1, 1);
+      F2<T> w = W();
+      for (int i = TID + 1; i <= nx; i += NT) w(i, nz) = (T)0.;
+      SYNC;
+      exch(w, 1, nz, 1, 1);
+      SYNC;
+      for (int i = TID; i <= nx + 1; i += NT) w(i, nz) = (T)0.;
+    } else if (flag == 2) {
+      exch(U(), 1, nzm, 2, 3);
+      exch(V(), 1, nzm, 2, 2);
+      exch(W(), 1, nz, 2, 2);
+      exch(TT(), 1, nzm, 3, 3);
+      exch(QT(), 1, nzm, 3, 3);
+      exch(QP(), 1, nzm, 3, 3);
+    } else if (flag == 3) {
+      exch(TT(), 1, nzm, 1, 1);
+      exch(QT(), 1, nzm, 1, 1);
+      exch(QP(), 1, nzm, 1, 1);
+    } else if (flag == 4) {
+      exch(TK(), 1, nzm, 1, 1);
+      exch(TKH(), 1, nzm, 1, 1);
+    }
+    SYNC;
+  }
+
+  // ---------------------------------------------------------- micro_diagnose
+  __device__ void micro_diagnose() {          // MICRO_SAM1MOM/microphysics.F90:334-357
+    F2<T> qv = QV(), qt = QT(), qn = QN(), tabs = TABS(), qcl = QCL(), qci = QCI(), qpl = QPL(), qpi = QPI(), qp = QP();
+    const T a_bg = (T)p.a_bg, a_pr = (T)p.a_pr;
+    for (int e = TID; e < nx * nzm; e += NT) {
+      int i = 1 + e % nx, k = 1 + e / nx;
+      qv(i, k) = qt(i, k) - qn(i, k);
+      T omn = mx2((T)0., mn2((T)1., (tabs(i, k) - (T)C_TBGMIN) * a_bg));
+      qcl(i, k) = qn(i, k) * omn;
+      qci(i, k) = qn(i, k) * ((T)1. - omn);
+      T omp = mx2((T)0., mn2((T)1., (tabs(i, k) - (T)C_TPRMIN) * a_pr));
+      qpl(i, k) = qp(i, k) * omp;
+      qpi(i, k) = qp(i, k) * ((T)1. - omp);
+    }
+    SYNC;
+  }
+
+  // ---------------------------------------------------------- precip_init
+  __device__ void precip_init() {             // MICRO_SAM1MOM/precip_init.F90:54-91
+    const T pi = (T)C_PI;
+    for (int k = TID + 1; k <= nzm; k += NT) {
+      T rho = PR(P_RHO)[k], t0 = PR(P_TABS0)[k];
+      T pratio = tsqrt((T)R4(1.29) / rho);
+      T rrr1 = (T)393. / (t0 + (T)120.) * tpow(t0 / (T)273., (T)1.5);
+      T rrr2 = tpow(t0 / (T)273., (T)R4(1.94)) * ((T)1000. / PR(P_PRES)[k]);
+      T estw = (T)100. * esatw(t0);
+      T esti = (T)100. * esati(t0);
+      T coef1 = (T)0.25 * pi * (T)C_NZEROS * (T)C_A_SNOW * (T)p.gams1 * pratio /
+                tpow(pi * (T)C_RHOS * (T)C_NZEROS / rho, (T)((3 + C_B_SNOW) / 4.));
+      T coef2 = texp((T)R4(0.025) * (t0 - (T)R4(273.15)));
+      PR(P_ACCRSI)[k] = coef1 * coef2 * (T)C_ESICOEF;
+      PR(P_ACCRSC)[k] = coef1 * (T)1.0;
+      PR(P_COEFICE)[k] = coef2;
+      coef1 = ((T)C_LSUB / (t0 * (T)C_RV) - (T)1.) * (T)C_LSUB / ((T)C_THERCO * rrr1 * t0);
+      coef2 = (T)C_RV * t0 / ((T)C_DIFFELQ * rrr2 * esti);
+      PR(P_EVAPS1)[k] = (T)(double)(0.65f * 4.f) * (T)C_NZEROS / tsqrt(pi * (T)C_RHOS * (T)C_NZEROS) / (coef1 + coef2) / tsqrt(rho);
+      PR(P_EVAPS2)[k] = (T)(double)(0.49f * 4.f) * (T)C_NZEROS * (T)p.gams2 * tsqrt((T)C_A_SNOW / ((T)C_MUELQ * rrr1)) /
+                        tpow(pi * (T)C_RHOS * (T)C_NZEROS, (T)((5 + C_B_SNOW) / 8.)) / (coef1 + coef2) *
+                        tpow(rho, (T)((1 + C_B_SNOW) / 8.)) * tsqrt(pratio);
+      coef1 = (T)0.25 * pi * (T)C_NZEROG * (T)C_A_GRAU * (T)p.gamg1 * pratio /
+              tpow(pi * (T)C_RHOG * (T)C_NZEROG / rho, (T)((3 + C_B_GRAU) / 4.));
+      coef2 = texp((T)R4(0.025) * (t0 - (T)R4(273.15)));
+      PR(P_ACCRGI)[k] = coef1 * coef2 * (T)C_EGICOEF;
+      PR(P_ACCRGC)[k] = coef1 * (T)1.0;
+      coef1 = ((T)C_LSUB / (t0 * (T)C_RV) - (T)1.) * (T)C_LSUB / ((T)C_THERCO * rrr1 * t0);
+      coef2 = (T)C_RV * t0 / ((T)C_DIFFELQ * rrr2 * esti);
+      PR(P_EVAPG1)[k] = (T)(double)(0.65f * 4.f) * (T)C_NZEROG / tsqrt(pi * (T)C_RHOG * (T)C_NZEROG) / (coef1 + coef2) / tsqrt(rho);
+      PR(P_EVAPG2)[k] = (T)(double)(0.49f * 4.f) * (T)C_NZEROG * (T)p.gamg2 * tsqrt((T)C_A_GRAU / ((T)C_MUELQ * rrr1)) /
+                        tpow(pi * (T)C_RHOG * (T)C_NZEROG, (T)((5 + C_B_GRAU) / 8.)) / (coef1 + coef2) *
+                        tpow(rho, (T)((1 + C_B_GRAU) / 8.)) * tsqrt(pratio);
+      PR(P_ACCRRC)[k] = (T)0.25 * pi * (T)C_NZEROR * (T)C_A_RAIN * (T)p.gamr1 * pratio /
+                        tpow(pi * (T)C_RHOR * (T)C_NZEROR / rho, (T)((3 + C_B_RAIN) / 4.)) * (T)1.0;
+      coef1 = ((T)C_LCOND / (t0 * (T)C_RV) - (T)1.) * (T)C_LCOND / ((T)C_THERCO * rrr1 * t0);
+      coef2 = (T)C_RV * t0 / ((T)C_DIFFELQ * rrr2 * estw);
+      PR(P_EVAPR1)[k] = (T)(double)(0.78f * 2.f) * pi * (T)C_NZEROR / tsqrt(pi * (T)C_RHOR * (T)C_NZEROR) / (coef1 + coef2) / tsqrt(rho);
+      PR(P_EVAPR2)[k] = (T)(double)(0.31f * 2.f) * pi * (T)C_NZEROR * (T)p.gamr2 * (T)R4(0.89) *
+                        tsqrt((T)C_A_RAIN / ((T)C_MUELQ * rrr1)) /
+                        tpow(pi * (T)C_RHOR * (T)C_NZEROR, (T)((5 + C_B_RAIN) / 8.)) / (coef1 + coef2) *
+                        tpow(rho, (T)((1 + C_B_RAIN) / 8.)) * tsqrt(pratio);
+    }
+    SYNC;
+  }
+
+  // ---------------------------------------------------------- init
+  // crm_module.F90:320-681
+  __device__ void init_column() {
+    const int plev_ = plev;
+    // zero the slab (allocate_* zero every module array)
+    {
+      size_t n = p.L.slab;
+      for (size_t e = TID; e < n; e += NT) base[e] = (T)0.;
+    }
+    if (TID == 0) {
+      S.na = 1; S.nb = 2; S.nc = 3;
+      S.dt3[0] = S.dt3[1] = S.dt3[2] = 0.;
+      S.status = CRM_OK;
+      S.z0 = p.z0[icrm];
+    }
+    SYNC;
+    // vertical grid (crm_module.F90:341-375)
+    for (int k = TID + 1; k <= nzm; k += NT) {
+      double z = IN(p.zmid, plev_ - k + 1) - IN(p.zint, plev_ + 1);
+      PR(P_Z)[k] = (T)z;
+      PR(P_ZI)[k] = (T)(IN(p.zint, plev_ - k + 2) - IN(p.zint, plev_ + 1));
+      PR(P_PRES)[k] = (T)(IN(p.pmid, plev_ - k + 1) / 100.);
+      PR(P_PRESI)[k] = (T)(IN(p.pint, plev_ - k + 2) / 100.);
+      PR(P_BET)[k] = (T)(C_GGR / IN(p.tl, plev_ - k + 1));
+      PR(P_GAMAZ)[k] = (T)(C_GGR / C_CP * z);
+    }
+    if (TID == 0) {
+      PR(P_ZI)[nz] = (T)(IN(p.zint, plev_ - nz + 2) - IN(p.zint, plev_ + 1));
+      PR(P_PRESI)[nz] = (T)(IN(p.pint, plev_ - nz + 2) / 100.);
+    }
+    SYNC;
+    // the grid metrics are computed in double from the double inputs
+    if (TID == 0) {
+      double z1 = IN(p.zmid, plev_) - IN(p.zint, plev_ + 1);
+      double z2 = IN(p.zmid, plev_ - 1) - IN(p.zint, plev_ + 1);
+      S.dz = 0.5 * (z1 + z2);
+    }
+    SYNC;
+    const double dz = S.dz;
+    for (int k = TID + 1; k <= nzm; k += NT) {
+      double zk = IN(p.zmid, plev_ - k + 1) - IN(p.zint, plev_ + 1);
+      double adzw = 1.;
+      if (k >= 2) {
+        double zkm = IN(p.zmid, plev_ - k + 2) - IN(p.zint, plev_ + 1);
+        adzw = (zk - zkm) / dz;
+      }
+      PR(P_ADZW)[k] = (T)adzw;
+      double zi1 = IN(p.zint, plev_ - k + 1) - IN(p.zint, plev_ + 1);
+      double zi0 = IN(p.zint, plev_ - k + 2) - IN(p.zint, plev_ + 1);
+      double adz = (zi1 - zi0) / dz;
+      PR(P_ADZ)[k] = (T)adz;
+      PR(P_RHO)[k] = (T)(IN(p.pdel, plev_ - k + 1) / C_GGR / (adz * dz));
+      if (k >= 2) PR(P_RHOW)[k] = (T)((IN(p.pmid, plev_ - k + 2) - IN(p.pmid, plev_ - k + 1)) / C_GGR / (adzw * dz));
+      if (k == nzm) {
+        // adzw(nz) = adzw(nzm)
+        PR(P_ADZW)[nz] = (T)adzw;
+      }
+    }
+    SYNC;
+    if (TID == 0) {
+      // rhow(1), rhow(nz) by linear extrapolation in double
+      double zk2 = IN(p.zmid, plev_ - 1) - IN(p.zint, plev_ + 1), zk1 = IN(p.zmid, plev_) - IN(p.zint, plev_ + 1);
+      double zk3 = IN(p.zmid, plev_ - 2) - IN(p.zint, plev_ + 1);
+      double adzw2 = (zk2 - zk1) / dz, adzw3 = (zk3 - zk2) / dz;
+      double rhow2 = (IN(p.pmid, plev_ - 2 + 2) - IN(p.pmid, plev_ - 2 + 1)) / C_GGR / (adzw2 * dz);
+      double rhow3 = (IN(p.pmid, plev_ - 3 + 2) - IN(p.pmid, plev_ - 3 + 1)) / C_GGR / (adzw3 * dz);
+      PR(P_RHOW)[1] = (T)(2. * rhow2 - rhow3);
+      double zn = IN(p.zmid, plev_ - nzm + 1) - IN(p.zint, plev_ + 1), zn1 = IN(p.zmid, plev_ - nzm + 2) - IN(p.zint, plev_ + 1);
+      double zn2 = IN(p.zmid, plev_ - nzm + 3) - IN(p.zint, plev_ + 1);
+      double adzwn = (zn - zn1) / dz, adzwn1 = (zn1 - zn2) / dz;
+      double rhown = (IN(p.pmid, plev_ - nzm + 2) - IN(p.pmid, plev_ - nzm + 1)) / C_GGR / (adzwn * dz);
+      double rhown1 = (IN(p.pmid, plev_ - (nzm - 1) + 2) - IN(p.pmid, plev_ - (nzm - 1) + 1)) / C_GGR / (adzwn1 * dz);
+      PR(P_RHOW)[nz] = (T)(2. * rhown - rhown1);
+    }
+    SYNC;
+    // state in (crm_module.F90:380-397) and the first-step clamp (:400-417)
+    F2<T> u = U(), v = V(), w = W(), tabs = TABS(), qt = QT(), qp = QP(), qn = QN();
+    bool clamp;
+    if (p.batch_mode == CRM_REFERENCE_BATCH) clamp = p.clamp_batch != 0;
+    else clamp = (p.st[0][S4(1, 1)] == p.st[0][S4(2, 1)]) && (p.st[0][S4(3, 2)] == p.st[0][S4(4, 2)]);
+    const double umax = (double)(0.5f * (float)p.dx / (float)p.dt);
+    for (int e = TID; e < nx * nzm; e += NT) {
+      int i = 1 + e % nx, k = 1 + e / nx;
+      size_t o = S4(i, k);
+      double uu = p.st[0][o], vv = p.st[1][o] * 0.0;
+      if (clamp) {
+        uu = mn2(umax, mx2(-umax, uu));
+        vv = mn2(umax, mx2(-umax, vv)) * 0.0;
+      }
+      u(i, k) = (T)uu;
+      v(i, k) = (T)vv;
+      w(i, k) = (T)p.st[2][o];
+      tabs(i, k) = (T)p.st[3][o];
+      qt(i, k) = (T)p.st[4][o];
+      qp(i, k) = (T)p.st[5][o];
+      qn(i, k) = (T)p.st[6][o];
+    }
+    SYNC;
+    micro_diagnose();
+    // sgs_init grid factors (SGS_TKE/sgs.F90:213-220)
+    for (int k = TID + 1; k <= nzm; k += NT) {
+      T adzdz = PR(P_ADZ)[k] * (T)dz;
+      PR(P_GRDFX)[k] = mn2((T)16., (T)p.dx * (T)p.dx / (adzdz * adzdz));
+      PR(P_GRDFY)[k] = mn2((T)16., (T)p.dy * (T)p.dy / (adzdz * adzdz));
+      PR(P_GRDFZ)[k] = (T)1.;
+    }
+    // t from tabs (crm_module.F90:508-509)
+    F2<T> t = TT(), qcl = QCL(), qci = QCI(), qpl = QPL(), qpi = QPI(), qv = QV();
+    for (int e = TID; e < nx * nzm; e += NT) {
+      int i = 1 + e % nx, k = 1 + e / nx;
+      t(i, k) = tabs(i, k) + PR(P_GAMAZ)[k] - (T)C_FAC_COND * qcl(i, k) - (T)C_FAC_SUB * qci(i, k) -
+                (T)C_FAC_COND * qpl(i, k) - (T)C_FAC_SUB * qpi(i, k);
+    }
+    SYNC;
+    // initial domain means (crm_module.F90:500-546)
+    const double factor_xy = 1.0 / (double)nx;
+    const double idt_gl = 1.0 / p.dt_gl;
+    for (int k = TID + 1; k <= nzm; k += NT) {
+      double u0 = 0, v0 = 0, t0 = 0, t00 = 0, tabs0 = 0, q0 = 0, qv0 = 0, qn0 = 0, qp0 = 0;
+      for (int i = 1; i <= nx; ++i) {
+        u0 = u0 + (double)u(i, k);
+        v0 = v0 + (double)v(i, k);
+        t0 = t0 + (double)t(i, k);
+        t00 = t00 + (double)(t(i, k) + (T)C_FAC_COND * qpl(i, k) + (T)C_FAC_SUB * qpi(i, k));
+        tabs0 = tabs0 + (double)tabs(i, k);
+        q0 = q0 + (double)(qv(i, k) + qcl(i, k) + qci(i, k));
+        qv0 = qv0 + (double)qv(i, k);
+        qn0 = qn0 + (double)(qcl(i, k) + qci(i, k));
+        qp0 = qp0 + (double)(qpl(i, k) + qpi(i, k));
+      }
+      u0 *= factor_xy; v0 *= factor_xy; t0 *= factor_xy; t00 *= factor_xy; tabs0 *= factor_xy;
+      q0 *= factor_xy; qv0 *= factor_xy; qn0 *= factor_xy; qp0 *= factor_xy;
+      PR(P_U0)[k] = (T)u0; PR(P_V0)[k] = (T)v0; PR(P_T0)[k] = (T)t0; PR(P_T00)[k] = (T)t00;
+      PR(P_TABS0)[k] = (T)tabs0; PR(P_Q0)[k] = (T)q0; PR(P_QV0)[k] = (T)qv0; PR(P_QN0)[k] = (T)qn0;
+      PR(P_QP0)[k] = (T)qp0;
+      int l = plev_ - k + 1;
+      double uln = mn2(umax, mx2(-umax, IN(p.ul, l)));
+      double vln = mn2(umax, mx2(-umax, IN(p.vl, l))) * 0.0;
+      double tl = IN(p.tl, l), qccl = IN(p.qccl, l), qiil = IN(p.qiil, l), ql = IN(p.ql, l);
+      double gamaz = (double)PR(P_GAMAZ)[k];
+      PR(P_TTEND)[k] = (T)((tl + gamaz - C_FAC_COND * (qccl + qiil) - C_FAC_FUS * qiil - t00) * idt_gl);
+      PR(P_QTEND)[k] = (T)((ql + qccl + qiil - q0) * idt_gl);
+      PR(P_UTEND)[k] = (T)((uln - u0) * idt_gl);
+      PR(P_VTEND)[k] = (T)((vln - v0) * idt_gl);
+    }
+    // column precipitation at the start (prectend, precstend)
+    if (TID == 0) {
+      double cp = 0, cps = 0;
+      for (int k = 1; k <= nzm; ++k) {
+        double pdel = IN(p.pdel, plev_ - k + 1);
+        for (int i = 1; i <= nx; ++i) {
+          cp = cp + (double)(qpl(i, k) + qpi(i, k)) * pdel;
+          cps = cps + (double)qpi(i, k) * pdel;
+        }
+      }
+      S.colprec0 = cp;
+      S.colprecs0 = cps;
+      S.cltot = S.clhgh = S.clmed = S.cllow = 0.;
+    }
+    SYNC;
+    precip_init();
+    // setperturb (setperturb.F90:33-80) with draws precomputed on the host
+    if (p.igstep <= 1) {
+      const double fxy = 1. / (double)nx;
+      for (int k = TID + 1; k <= 5; k += NT) {
+        double scaling = (double)(5 + 1 - k) / (double)5;
+        double t02 = 0.0;
+        const double *r = p.rnd + ((size_t)icrm * 5 + (k - 1)) * nx;
+        for (int i = 1; i <= nx; ++i) {
+          t(i, k) = t(i, k) + (T)(1.0 * r[i - 1] * scaling);
+          t02 = t02 + (double)t(i, k) * fxy;
+        }
+        T t0k = PR(P_T0)[k];
+        for (int i = 1; i <= nx; ++i) t(i, k) = (T)((double)(t(i, k) * t0k) / t02);
+      }
+      SYNC;
+    }
+  }
+
+  // ---------------------------------------------------------- kurant
+  // kurant.F90:31-64 and kurant_sgs (SGS_TKE/sgs.F90:342-367); per column
+  __device__ void kurant() {
+    F2<T> u = U(), v = V(), w = W(), tkh = TKH();
+    T *wm = PR(P_TMP0), *uhm = PR(P_TMP1), *tkhm = PR(P_TMP2);
+    for (int k = TID + 1; k <= nzm; k += NT) {
+      T a = (T)0., b = (T)0., c = (T)0.;
+      for (int i = 1; i <= nx; ++i) {
+        a = mx2(a, tabs_(w(i, k)));
+        T uu = u(i, k), vv = v(i, k);
+        b = mx2(b, tsqrt(uu * uu + (T)0. * (vv * vv)));
+        c = mx2(c, tkh(i, k));
+      }
+      wm[k] = a; uhm[k] = b; tkhm[k] = c;
+    }
+    if (TID == 0) wm[nz] = (T)0.;
+    SYNC;
+    double cfl = 0.;
+    const double rdx = 1. / p.dx;
+    for (int k = TID + 1; k <= nzm; k += NT) {
+      double dza = S.dz * (double)PR(P_ADZW)[k];
+      double t1 = mx2((double)uhm[k] * p.dt * sqrt(rdx * rdx + 0. * ((1. / p.dy) * (1. / p.dy))),
+                      mx2((double)wm[k], (double)wm[k + 1]) * p.dt / dza);
+      double tk = (double)tkhm[k];
+      double t2 = mx3(0.5 * tk * (double)PR(P_GRDFZ)[k] * p.dt / (dza * dza),
+                      0.5 * tk * (double)PR(P_GRDFX)[k] * p.dt / (p.dx * p.dx),
+                      (double)(0.f * 0.5f) * tk * (double)PR(P_GRDFY)[k] * p.dt / (p.dy * p.dy));
+      cfl = mx2(cfl, mx2(t1, t2));
+    }
+    cfl = block_max(cfl);
+    if (TID == 0) {
+      S.cfl = cfl;
+      int n = (int)ceil(cfl / R4(0.7));
+      S.ncycle = n > 1 ? n : 1;
+    }
+    SYNC;
+  }
+
+  // ---------------------------------------------------------- abcoefs
+  __device__ void abcoefs(int nstep) {        // abcoefs.F90:7-31 (thread 0)
+    if (nstep >= 3) {
+      double alpha = S.dt3[S.nb - 1] / S.dt3[S.na - 1];
+      double beta = S.dt3[S.nc - 1] / S.dt3[S.na - 1];
+      S.ct = (2. + 3. * alpha) / (6. * (alpha + beta) * beta);
+      S.bt = -(1. + 2. * (alpha + beta) * S.ct) / (2. * alpha);
+      S.at = 1. - S.bt - S.ct;
+    } else if (nstep >= 2) {
+      S.at = 3. / 2.; S.bt = -1. / 2.; S.ct = 0.;
+    } else {
+      S.at = 1.; S.bt = 0.; S.ct = 0.;
+    }
+  }
+
+  // ---------------------------------------------------------- zero, buoyancy
+  __device__ void zero_and_buoyancy() {       // zero.F90:17-29, buoyancy.F90:15-37
+    F2<T> du = DU(S.na), dv = DV(S.na), dw = DW(S.na);
+    for (int e = TID; e < (nx + 1) * nzm; e += NT) { int i = 1 + e % (nx + 1), k = 1 + e / (nx + 1); du(i, k) = (T)0.; }
+    for (int e = TID; e < nx * nzm; e += NT) { int i = 1 + e % nx, k = 1 + e / nx; dv(i, k) = (T)0.; }
+    F2<T> tabs = TABS(), qv = QV(), qcl = QCL(), qci = QCI(), qpl = QPL(), qpi = QPI();
+    const T epsv = (T)C_EPSV;
+    T *adz = PR(P_ADZ), *bet = PR(P_BET), *tabs0 = PR(P_TABS0), *qv0 = PR(P_QV0), *qn0 = PR(P_QN0), *qp0 = PR(P_QP0);
+    for (int e = TID; e < nx * nz; e += NT) {
+      int i = 1 + e % nx, k = 1 + e / nx;
+      if (k >= 2 && k <= nzm) {
+        int kb = k - 1;
+        T betu = adz[kb] / (adz[k] + adz[kb]);
+        T betd = adz[k] / (adz[k] + adz[kb]);
+        dw(i, k) = (T)0. +
+            bet[k] * betu *
+                (tabs0[k] * (epsv * (qv(i, k) - qv0[k]) - (qcl(i, k) + qci(i, k) - qn0[k] + qpl(i, k) + qpi(i, k) - qp0[k])) +
+                 (tabs(i, k) - tabs0[k]) * ((T)1. + epsv * qv0[k] - qn0[k] - qp0[k])) +
+            bet[kb] * betd *
+                (tabs0[kb] * (epsv * (qv(i, kb) - qv0[kb]) - (qcl(i, kb) + qci(i, kb) - qn0[kb] + qpl(i, kb) + qpi(i, kb) - qp0[kb])) +
+                 (tabs(i, kb) - tabs0[kb]) * ((T)1. + epsv * qv0[kb] - qn0[kb] - qp0[kb]));
+      } else {
+        dw(i, k) = (T)0.;
+      }
+    }
+    SYNC;
+  }
+
+  // ---------------------------------------------------------- forcing + radiation
+  __device__ void forcing_radiation() {       // forcing.F90:31-74, crm_module.F90:766-777
+    F2<T> t = TT(), qt = QT(), du = DU(S.na), dv = DV(S.na);
+    const T dtn = (T)S.dtn;
+    T *ttend = PR(P_TTEND), *qtend = PR(P_QTEND), *utend = PR(P_UTEND), *vtend = PR(P_VTEND);
+    for (int e = TID; e < nx * nzm; e += NT) {
+      int i = 1 + e % nx, k = 1 + e / nx;
+      t(i, k) = t(i, k) + ttend[k] * dtn;
+      qt(i, k) = qt(i, k) + qtend[k] * dtn;
+      du(i, k) = du(i, k) + utend[k];
+      dv(i, k) = dv(i, k) + vtend[k];
+    }
+    SYNC;
+    // negative-vapour fixer: per-level sums in the reference's order
+    T *qneg = PR(P_TMP0), *qpoz = PR(P_TMP1), *nneg = PR(P_TMP2);
+    for (int k = TID + 1; k <= nzm; k += NT) {
+      double sn = 0., sp = 0.;
+      int cnt = 0;
+      for (int i = 1; i <= nx; ++i) {
+        T q = qt(i, k);
+        if (q < (T)0.) { cnt += 1; sn = sn + (double)q; }
+        else sp = sp + (double)q;
+      }
+      qneg[k] = (T)sn; qpoz[k] = (T)sp; nneg[k] = (T)cnt;
+    }
+    SYNC;
+    const int gx = nx / p.L.nx_rad;
+    const double *qrad = p.qrad;
+    for (int e = TID; e < nx * nzm; e += NT) {
+      int i = 1 + e % nx, k = 1 + e / nx;
+      if (nneg[k] > (T)0. && qpoz[k] + qneg[k] > (T)0.) {
+        T factor = (T)1. + qneg[k] / qpoz[k];
+        qt(i, k) = mx2((T)0., qt(i, k) * factor);
+      }
+      int i_rad = (i - 1) / gx + 1;
+      T qr = (T)qrad[(size_t)icrm + (size_t)p.ld * ((i_rad - 1) + (size_t)p.L.nx_rad * (k - 1))];
+      t(i, k) = t(i, k) + qr * dtn;
+    }
+    SYNC;
+  }
+
+  // ---------------------------------------------------------- damping
+  __device__ void damping() {                  // damping.F90:44-107
+    T *z = PR(P_Z);
+    if (TID == 0) {
+      int n_damp = 0;
+      for (int k = nzm; k >= 1; --k)
+        if (z[nzm] - z[k] < (T)R4(0.4) * z[nzm]) n_damp = nzm - k + 1;
+      S.n_damp = n_damp;
+    }
+    SYNC;
+    const int n_damp = S.n_damp;
+    F2<T> u = U(), v = V(), t = TT();
+    T *tau = PR(P_TMP0), *u0l = PR(P_TMP1), *v0l = PR(P_TMP2), *t0l = PR(P_TMP3);
+    const T nxy = (T)(double)nx;
+    for (int k = TID + 1; k <= nzm; k += NT) {
+      if (k >= nzm - n_damp) {
+        T tk = (T)60. * tpow((T)450. / (T)60., (z[nzm] - z[k]) / (z[nzm] - z[nzm - n_damp]));
+        tau[k] = (T)1. / tk;
+      }
+      double su = 0., sv = 0., st = 0.;
+      for (int i = 1; i <= nx; ++i) {
+        su = su + (double)(u(i, k) / nxy);
+        sv = sv + (double)(v(i, k) / nxy);
+        st = st + (double)(t(i, k) / nxy);
+      }
+      u0l[k] = (T)su; v0l[k] = (T)sv; t0l[k] = (T)st;
+    }
+    SYNC;
+    F2<T> w = W(), qt = QT(), qv = QV(), du = DU(S.na), dv = DV(S.na), dw = DW(S.na);
+    const T dtn = (T)S.dtn;
+    T *qv0 = PR(P_QV0);
+    for (int e = TID; e < nx * nzm; e += NT) {
+      int i = 1 + e % nx, k = 1 + e / nx;
+      if (k >= nzm - n_damp) {
+        du(i, k) = du(i, k) - (u(i, k) - u0l[k]) * tau[k];
+        dv(i, k) = dv(i, k) - (v(i, k) - v0l[k]) * tau[k];
+        dw(i, k) = dw(i, k) - w(i, k) * tau[k];
+        t(i, k) = t(i, k) - dtn * (t(i, k) - t0l[k]) * tau[k];
+        qt(i, k) = qt(i, k) - dtn * (qv(i, k) - qv0[k]) * tau[k];
+      }
+    }
+    SYNC;
+  }
+
+  // ---------------------------------------------------------- ice_fall
+  __device__ void ice_fall() {                 // ice_fall.F90:26-167
+    F2<T> qcl = QCL(), qci = QCI(), tabs = TABS();
+    int kmin = nzm + 1, kmax = 0;
+    for (int e = TID; e < nx * nzm; e += NT) {
+      int i = 1 + e % nx, k = 1 + e / nx;
+      if (qcl(i, k) + qci(i, k) > (T)0. && tabs(i, k) < (T)R4(273.15)) {
+        kmin = min(kmin, k);
+        kmax = max(kmax, k);
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      kmin = min(kmin, __shfl_xor_sync(0xffffffffu, kmin, o));
+      kmax = max(kmax, __shfl_xor_sync(0xffffffffu, kmax, o));
+    }
+    if ((TID & 31) == 0) { S.red_i[TID >> 5] = kmin; S.red_i[32 + (TID >> 5)] = kmax; }
+    SYNC;
+    if (TID == 0) {
+      int a = nzm + 1, b = 0;
+      for (int w = 0; w < NT / 32; ++w) { a = min(a, S.red_i[w]); b = max(b, S.red_i[32 + w]); }
+      S.kmin = a; S.kmax = b;
+    }
+    SYNC;
+    kmin = S.kmin; kmax = S.kmax;
+    if (kmax == 0) return;                     // no ice cloud: nothing falls
+    F2<T> fz = SCR(p.L.s_a);
+    T *adz = PR(P_ADZ), *rho = PR(P_RHO);
+    const T dtn = (T)S.dtn, dz = (T)S.dz;
+    for (int e = TID; e < nx * nz; e += NT) {
+      int i = 1 + e % nx, k = 1 + e / nx;
+      T f = (T)0.;
+      if (k >= max(1, kmin - 1) && k <= kmax) {
+        int kc = min(nzm, k + 1), kb = max(1, k - 1);
+        T coef = dtn / ((T)0.5 * (adz[kb] + adz[k]) * dz);
+        T qiu = rho[kc] * qci(i, kc);
+        T qic = rho[k] * qci(i, k);
+        T qid = rho[kb] * qci(i, kb);
+        T vt_ice = mn2((T)R4(0.4), (T)R4(8.66) * tpow(mx2((T)0., qic) + (T)R4(1.e-10), (T)R4(0.24)));
+        T tmp_phi;
+        if (tabs_(qic - qid) < (T)R4(1.0e-25)) tmp_phi = (T)0.;
+        else {
+          T tmp_theta = (qiu - qic) / (qic - qid);
+          tmp_phi = mx2((T)0., mn3((T)0.5 * ((T)1. + tmp_theta), (T)2., (T)2. * tmp_theta));
+        }
+        f = -vt_ice * (qic - (T)0.5 * ((T)1. - coef * vt_ice) * tmp_phi * (qic - qid));
+      }
+      if (k == nz) f = (T)0.;
+      fz(i, k) = f;
+    }
+    SYNC;
+    F2<T> qt = QT(), t = TT();
+    for (int e = TID; e < nx * nzm; e += NT) {
+      int i = 1 + e % nx, k = 1 + e / nx;
+      if (k >= max(1, kmin - 2) && k <= kmax) {
+        T coef = dtn / (dz * adz[k] * rho[k]);
+        T dqi = coef * (fz(i, k) - fz(i, k + 1));
+        qt(i, k) = qt(i, k) + dqi;
+        T lat_heat = (T)(C_FAC_COND + C_FAC_FUS) * dqi;
+        t(i, k) = t(i, k) - lat_heat;
+      }
+    }
+    for (int i = TID + 1; i <= nx; i += NT) {
+      T coef = dtn / dz;
+      T dqi = -coef * fz(i, 1);
+      PS(i) = PS(i) + dqi;
+      PSS(i) = PSS(i) + dqi;
+    }
+    SYNC;
+  }
+
+  // ---------------------------------------------------------- SGS TKE
+  // shear_prod2D.F90:14-95 + tke_full.F90:108-312 (dosmagor = .true.)
+  __device__ void tke_full() {
+    F2<T> u = U(), v = V(), w = W(), def2 = SCR(p.L.s_a), buoy = SCR(p.L.s_b), aprod = SCR(p.L.s_c);
+    T *u0 = PR(P_U0), *v0 = PR(P_V0), *adz = PR(P_ADZ), *adzw = PR(P_ADZW);
+    const T dz = (T)S.dz, dx = (T)p.dx;
+    const T rdx0 = (T)1. / dx;
+    for (int e = TID; e < nx * nzm; e += NT) {
+      int i = 1 + e % nx, k = 1 + e / nx;
+      int ib = i - 1, ic = i + 1;
+      T r;
+#define SQ(x) ((x) * (x))
+      if (k >= 2 && k <= nzm - 1) {
+        int kb = k - 1, kc = k + 1;
+        T rdz = (T)1. / (dz * adz[k]);
+        T rdzw_up = (T)1. / (dz * adzw[kc]);
+        T rdzw_dn = (T)1. / (dz * adzw[k]);
+        T rdx = rdx0 * tsqrt(dx * rdz);
+        T rdx_up = rdx0 * tsqrt(dx * rdzw_up);
+        T rdx_dn = rdx0 * tsqrt(dx * rdzw_dn);
+        r = (T)2. * (SQ((u(ic, k) - u(i, k)) * rdx) + SQ((w(i, kc) - w(i, k)) * rdz)) +
+            (T)0.5 * (SQ((v(ic, k) - v(i, k)) * rdx) + SQ((v(i, k) - v(ib, k)) * rdx) +
+                      SQ((u(ic, kc) - u0[kc] - u(ic, k) + u0[k]) * rdzw_up + (w(ic, kc) - w(i, kc)) * rdx_up) +
+                      SQ((u(i, kc) - u0[kc] - u(i, k) + u0[k]) * rdzw_up + (w(i, kc) - w(ib, kc)) * rdx_up) +
+                      SQ((u(ic, k) - u0[k] - u(ic, kb) + u0[kb]) * rdzw_dn + (w(ic, k) - w(i, k)) * rdx_dn) +
+                      SQ((u(i, k) - u0[k] - u(i, kb) + u0[kb]) * rdzw_dn + (w(i, k) - w(ib, k)) * rdx_dn) +
+                      SQ((v(i, kc) - v0[kc] - v(i, k) + v0[k]) * rdzw_up) +
+                      SQ((v(i, k) - v0[k] - v(i, kb) + v0[kb]) * rdzw_dn));
+      } else if (k == 1) {
+        int kc = k + 1;
+        T rdz = (T)1. / (dz * adz[k]);
+        T rdzw_up = (T)1. / (dz * adzw[kc]);
+        T rdx = rdx0 * tsqrt(dx * rdz);
+        T rdx_up = rdx0 * tsqrt(dx * rdzw_up);
+        r = (T)2. * (SQ((u(ic, k) - u(i, k)) * rdx) + SQ((w(i, kc) - w(i, k)) * rdz)) +
+            (T)0.5 * (SQ((v(ic, k) - v(i, k)) * rdx) + SQ((v(i, k) - v(ib, k)) * rdx)) +
+            SQ((v(i, kc) - v0[kc] - v(i, k) + v0[k]) * rdzw_up) +
+            (T)0.5 * (SQ((u(ic, kc) - u0[kc] - u(ic, k) + u0[k]) * rdzw_up + (w(ic, kc) - w(i, kc)) * rdx_up) +
+                      SQ((u(i, kc) - u0[kc] - u(i, k) + u0[k]) * rdzw_up + (w(i, kc) - w(ib, kc)) * rdx_up));
+      } else {
+        int kc = k + 1, kb = k - 1;
+        T rdz = (T)1. / (dz * adz[k]);
+        T rdzw_dn = (T)1. / (dz * adzw[k]);
+        T rdx = rdx0 * tsqrt(dx * rdz);
+        T rdx_dn = rdx0 * tsqrt(dx * rdzw_dn);
+        r = (T)2. * (SQ((u(ic, k) - u(i, k)) * rdx) + SQ((w(i, kc) - w(i, k)) * rdz)) +
+            (T)0.5 * (SQ((v(ic, k) - v(i, k)) * rdx) + SQ((v(i, k) - v(ib, k)) * rdx)) +
+            SQ((v(i, k) - v0[k] - v(i, kb) + v0[kb]) * rdzw_dn) +
+            (T)0.5 * (SQ((u(ic, k) - u0[k] - u(ic, kb) + u0[kb]) * rdzw_dn + (w(ic, k) - w(i, k)) * rdx_dn) +
+                      SQ((u(i, k) - u0[k] - u(i, kb) + u0[kb]) * rdzw_dn + (w(i, k) - w(ib, k)) * rdx_dn));
+      }
+      def2(i, k) = r;
+    }
+    // SGS buoyancy flux at the interfaces k+1/2, k = 1..nzm-1
+    F2<T> tabs = TABS(), qv = QV(), qcl = QCL(), qci = QCI(), qpl = QPL(), qpi = QPI(), t = TT(), tkh = TKH();
+    T *bet = PR(P_BET), *presi = PR(P_PRESI);
+    const T epsv = (T)C_EPSV, fc = (T)C_FAC_COND, fs = (T)C_FAC_SUB, ff = (T)C_FAC_FUS;
+    for (int e = TID; e < nx * (nzm + 1); e += NT) {
+      int i = 1 + e % nx, k = e / nx;     // k = 0..nzm
+      if (k == 0 || k == nzm) { buoy(i, k) = (T)0.; aprod(i, k) = (T)0.; continue; }
+      int kc = k + 1, kb = k;
+      T betdz = (T)0.5 * (bet[kc] + bet[kb]) / dz / adzw[k + 1];
+      T tabs_if = (T)0.5 * (tabs(i, kc) + fc * qcl(i, kc) + fs * qci(i, kc) + tabs(i, kb) + fc * qcl(i, kb) + fs * qci(i, kb));
+      T qtot_if = (T)0.5 * (qv(i, kc) + qcl(i, kc) + qci(i, kc) + qv(i, kb) + qcl(i, kb) + qci(i, kb));
+      T qp_if = (T)0.5 * (qpl(i, kc) + qpi(i, kc) + qpl(i, kb) + qpi(i, kb));
+      T bbb = (T)1. + epsv * qtot_if - qp_if;
+      T dqtot = qv(i, kc) + qcl(i, kc) + qci(i, kc) - qv(i, kb) - qcl(i, kb) - qci(i, kb);
+      T bs = betdz * (bbb * (t(i, kc) - t(i, kb)) + epsv * tabs_if * dqtot +
+                      (bbb * fc - tabs_if) * (qpl(i, kc) - qpl(i, kb)) + (bbb * fs - tabs_if) * (qpi(i, kc) - qpi(i, kb)));
+      T ap = (T)-0.5 * (tkh(i, kc) + tkh(i, kb) + (T)R4(0.002)) * bs;
+      T qctot = qcl(i, kc) + qci(i, kc) + qcl(i, kb) + qci(i, kb);
+      if (qctot > (T)0.) {
+        T omn = (qcl(i, kc) + qcl(i, kb)) / (qctot + (T)R4(1.e-20));
+        T qsat_check = omn * qsatw(tabs_if, presi[k + 1]) + ((T)1. - omn) * qsati(tabs_if, presi[k + 1]);
+        if (qtot_if > qsat_check) {
+          T lstarn = fc + ((T)1. - omn) * ff;
+          T tif = (T)0.5 * (tabs(i, kc) + tabs(i, kb));
+          T qpif = (T)0.5 * (qpl(i, kc) + qpi(i, kc) + qpl(i, kb) + qpi(i, kb));
+          T dqsat = omn * dtqsatw(tif, presi[k + 1]) + ((T)1. - omn) * dtqsati(tif, presi[k + 1]);
+          T qsatt = omn * qsatw(tif, presi[k + 1]) + ((T)1. - omn) * qsati(tif, presi[k + 1]);
+          T b2 = (T)1. + epsv * qsatt + qsatt - qtot_if - qpif + (T)R4(1.61) * tif * dqsat;
+          b2 = b2 / ((T)1. + lstarn * dqsat);
+          bs = betdz * (b2 * (t(i, kc) - t(i, kb)) + (b2 * lstarn - ((T)1. + lstarn * dqsat) * tif) * dqtot +
+                        (b2 * fc - ((T)1. + fc * dqsat) * tabs(i, k)) * (qpl(i, kc) - qpl(i, kb)) +
+                        (b2 * fs - ((T)1. + fs * dqsat) * tabs(i, k)) * (qpi(i, kc) - qpi(i, kb)));
+          ap = (T)-0.5 * (tkh(i, kc) + tkh(i, kb) + (T)R4(0.002)) * bs;
+        }
+      }
+      buoy(i, k) = bs;
+      aprod(i, k) = ap;
+    }
+    SYNC;
+    // eddy viscosity / conductivity (Smagorinsky), levels 1..nzm-1
+    F2<T> tk = TK(), tke = TKE();
+    const T Cs = (T)R4(0.15), Ck = (T)R4(0.1);
+    const T Ce = Ck * Ck * Ck / ((Cs * Cs) * (Cs * Cs));
+    const T Pr = (T)1.;
+    const T dt = (T)p.dt;
+    T *grdfx = PR(P_GRDFX), *grdfy = PR(P_GRDFY), *grdfz = PR(P_GRDFZ);
+    for (int e = TID; e < nx * (nzm - 1); e += NT) {
+      int i = 1 + e % nx, k = 1 + e / nx;
+      T grd = dz * adz[k];
+      T Ce1 = Ce / (T)R4(0.7) * (T)R4(0.19);
+      T Ce2 = Ce / (T)R4(0.7) * (T)R4(0.51);
+      T cx = dx * dx / dt / grdfx[k];
+      T cy = (T)p.dy * (T)p.dy / dt / grdfy[k];
+      T dzm = dz * mn2(adzw[k], adzw[k + 1]);
+      T cz = dzm * dzm / dt / grdfz[k];
+      T tkmax = (T)R4(0.09) / ((T)1. / cx + (T)1. / cy + (T)1. / cz);
+      T bs = (T)0.5 * (buoy(i, k - 1) + buoy(i, k));
+      T smix;
+      if (bs <= (T)0.) smix = grd;
+      else smix = mn2(grd, mx2((T)R4(0.1) * grd, tsqrt((T)R4(0.76) * tk(i, k) / Ck / tsqrt(bs + (T)R4(1.e-10)))));
+      T ratio = smix / grd;
+      T Cee = Ce1 + Ce2 * ratio;
+      T tkv = tsqrt(Ck * Ck * Ck / Cee * mx2((T)0., def2(i, k) - Pr * bs)) * (smix * smix);
+      T tq = tkv / (Ck * smix);
+      tke(i, k) = tq * tq;
+      tkv = mn2(tkv, tkmax);
+      tk(i, k) = tkv;
+      tkh(i, k) = Pr * tkv;
+    }
+    SYNC;
+#undef SQ
+  }
+
+  // ---------------------------------------------------------- advect_mom
+  // advect2_mom_xy.F90:60-80 (2D) and advect2_mom_z.F90:30-122
+  __device__ void advect_mom() {
+    F2<T> u = U(), v = V(), w = W(), du = DU(S.na), dv = DV(S.na), dw = DW(S.na);
+    F2<T> fuz = SCR(p.L.s_a), fvz = SCR(p.L.s_b), fwz = SCR(p.L.s_c);
+    T *rho = PR(P_RHO), *adz = PR(P_ADZ), *rhow = PR(P_RHOW), *adzw = PR(P_ADZW);
+    const T dx25 = (T)0.25 / (T)p.dx;
+    const T dz = (T)S.dz;
+    const T dz25 = (T)1. / ((T)4. * dz);
+    for (int e = TID; e < nx * nzm; e += NT) {
+      int i = 1 + e % nx, k = 1 + e / nx;
+      int kc = k + 1, kcu = min(kc, nzm);
+      T irho = (T)1. / (rhow[kc] * adzw[kc]);
+      int ic = i + 1;
+      T fu1 = dx25 * (u(ic - 1, k) + u(i - 1, k)) * (u(i - 1, k) + u(ic - 1, k));
+      T fu2 = dx25 * (u(ic, k) + u(i, k)) * (u(i, k) + u(ic, k));
+      du(i, k) = du(i, k) - (fu2 - fu1);
+      T fv1 = dx25 * (u(ic - 1, k) + u(i - 1, k)) * (v(i - 1, k) + v(ic - 1, k));
+      T fv2 = dx25 * (u(ic, k) + u(i, k)) * (v(i, k) + v(ic, k));
+      dv(i, k) = dv(i, k) - (fv2 - fv1);
+      T fw1 = dx25 * (u(ic - 1, k) * rho[k] * adz[k] + u(ic - 1, kcu) * rho[kcu] * adz[kcu]) * (w(i - 1, kc) + w(ic - 1, kc));
+      T fw2 = dx25 * (u(ic, k) * rho[k] * adz[k] + u(ic, kcu) * rho[kcu] * adz[kcu]) * (w(i, kc) + w(ic, kc));
+      dw(i, kc) = dw(i, kc) - irho * (fw2 - fw1);
+      // vertical fluxes of u, v at w level k (k = 2..nzm); 0 at 1 and nz
+      if (k >= 2) {
+        int kb = k - 1;
+        T rhoi = dz25 * rhow[k];
+        T www = rhoi * (w(i, k) + w(i - 1, k));
+        fuz(i, k) = www * (u(i, k) + u(i, kb));
+        fvz(i, k) = www * (v(i, k) + v(i, kb));
+      } else {
+        fuz(i, 1) = (T)0.; fvz(i, 1) = (T)0.;
+        fuz(i, nz) = (T)0.; fvz(i, nz) = (T)0.;
+      }
+    }
+    SYNC;
+    T *uwle = PR(P_UWLE), *vwle = PR(P_VWLE);
+    for (int k = TID + 1; k <= nz; k += NT) {
+      double su = 0., sv = 0.;
+      if (k >= 2 && k <= nzm)
+        for (int i = 1; i <= nx; ++i) { su = su + (double)fuz(i, k); sv = sv + (double)fvz(i, k); }
+      uwle[k] = (T)su; vwle[k] = (T)sv;
+    }
+    for (int e = TID; e < nx * nzm; e += NT) {
+      int i = 1 + e % nx, k = 1 + e / nx;
+      int kc = k + 1;
+      T rhoi = (T)1. / (rho[k] * adz[k]);
+      du(i, k) = du(i, k) - (fuz(i, kc) - fuz(i, k)) * rhoi;
+      dv(i, k) = dv(i, k) - (fvz(i, kc) - fvz(i, k)) * rhoi;
+      fwz(i, k) = dz25 * (w(i, kc) * rhow[kc] + w(i, k) * rhow[k]) * (w(i, kc) + w(i, k));
+    }
+    SYNC;
+    for (int e = TID; e < nx * (nzm - 1); e += NT) {
+      int i = 1 + e % nx, k = 2 + e / nx;
+      int kb = k - 1;
+      T rhoi = (T)1. / (rhow[k] * adzw[k]);
+      dw(i, k) = dw(i, k) - (fwz(i, k) - fwz(i, kb)) * rhoi;
+    }
+    SYNC;
+  }
+
+  // ---------------------------------------------------------- diffuse_mom2D
+  // SGS_TKE/diffuse_mom2D.F90:42-160
+  __device__ void diffuse_mom() {
+    F2<T> u = U(), v = V(), w = W(), tk = TK(), du = DU(S.na), dv = DV(S.na), dw = DW(S.na);
+    F2<T> fu = SCR(p.L.s_a), fv = SCR(p.L.s_b), fw = SCR(p.L.s_c);
+    T *rho = PR(P_RHO), *adz = PR(P_ADZ), *rhow = PR(P_RHOW), *adzw = PR(P_ADZW);
+    T *grdfx = PR(P_GRDFX), *grdfz = PR(P_GRDFZ);
+    const T dx = (T)p.dx, dz = (T)S.dz;
+    const T rdx2 = (T)1. / dx / dx;
+    const T rdx25 = (T)0.25 * rdx2;
+    for (int e = TID; e < (nx + 1) * nzm; e += NT) {
+      int i = e % (nx + 1), k = 1 + e / (nx + 1);
+      int kc = k + 1, kcu = min(kc, nzm);
+      T dxz = dx / (dz * adzw[kc]);
+      T rdx21 = rdx2 * grdfx[k];
+      T rdx251 = rdx25 * grdfx[k];
+      int ic = i + 1;
+      T tkx = rdx21 * tk(i, k);
+      fu(i, k) = (T)-2. * tkx * (u(ic, k) - u(i, k));
+      fv(i, k) = -tkx * (v(ic, k) - v(i, k));
+      tkx = rdx251 * (tk(i, k) + tk(ic, k) + tk(i, kcu) + tk(ic, kcu));
+      fw(i, k) = -tkx * (w(ic, kc) - w(i, kc) + (u(ic, kcu) - u(ic, k)) * dxz);
+    }
+    SYNC;
+    for (int e = TID; e < nx * nzm; e += NT) {
+      int i = 1 + e % nx, k = 1 + e / nx;
+      int kc = k + 1, ib = i - 1;
+      du(i, k) = du(i, k) - (fu(i, k) - fu(ib, k));
+      dv(i, k) = dv(i, k) - (fv(i, k) - fv(ib, k));
+      dw(i, kc) = dw(i, kc) - (fw(i, k) - fw(ib, k));
+    }
+    SYNC;
+    // vertical fluxes (reuse fu, fv, fw)
+    for (int e = TID; e < nx * nzm; e += NT) {
+      int i = 1 + e % nx, k = 1 + e / nx;
+      if (k <= nzm - 1) {
+        int kc = k + 1;
+        T rdz = (T)1. / dz;
+        T rdz2 = rdz * rdz * grdfz[k];
+        T rdz25 = (T)0.25 * rdz2;
+        T dzx = dz / dx;
+        T iadz = (T)1. / adz[k];
+        T iadzw = (T)1. / adzw[kc];
+        int ib = i - 1;
+        T tkz = rdz2 * tk(i, k);
+        fw(i, kc) = (T)-2. * tkz * (w(i, kc) - w(i, k)) * rho[k] * iadz;
+        tkz = rdz25 * (tk(i, k) + tk(ib, k) + tk(i, kc) + tk(ib, kc));
+        fu(i, kc) = -tkz * ((u(i, kc) - u(i, k)) * iadzw + (w(i, kc) - w(ib, kc)) * dzx) * rhow[kc];
+        fv(i, kc) = -tkz * (v(i, kc) - v(i, k)) * iadzw * rhow[kc];
+      } else {
+        T rdz = (T)1. / dz;
+        T rdz2 = rdz * rdz * grdfz[nzm - 1];
+        T tkz = rdz2 * grdfz[nzm] * tk(i, nzm);
+        fw(i, nz) = (T)-2. * tkz * (w(i, nz) - w(i, nzm)) / adz[nzm] * rho[nzm];
+        fu(i, 1) = (T)0.0 * rdz * rhow[1];
+        fv(i, 1) = (T)0.0 * rdz * rhow[1];
+        fu(i, nz) = (T)0.0 * rdz * rhow[nz];
+        fv(i, nz) = (T)0.0 * rdz * rhow[nz];
+      }
+    }
+    SYNC;
+    T *uwsb = PR(P_UWSB), *vwsb = PR(P_VWSB);
+    for (int k = TID + 1; k <= nzm; k += NT) {
+      double su = 0., sv = 0.;
+      for (int i = 1; i <= nx; ++i) { su = su + (double)fu(i, k); sv = sv + (double)fv(i, k); }
+      uwsb[k] = (T)su; vwsb[k] = (T)sv;
+    }
+    for (int e = TID; e < nx * nzm; e += NT) {
+      int i = 1 + e % nx, k = 1 + e / nx;
+      int kc = k + 1;
+      T rhoi = (T)1. / (rho[k] * adz[k]);
+      du(i, k) = du(i, k) - (fu(i, kc) - fu(i, k)) * rhoi;
+      dv(i, k) = dv(i, k) - (fv(i, kc) - fv(i, k)) * rhoi;
+      if (k >= 2) {
+        T rhoiw = (T)1. / (rhow[k] * adzw[k]);
+        dw(i, k) = dw(i, k) - (fw(i, k + 1) - fw(i, k)) * rhoiw;
+      }
+    }
+    SYNC;
+  }
+
+  // ---------------------------------------------------------- FFT
+  // One pass of the real/half-complex transform of crm/fft.F90
+  // (vpassm_crm :466-806, lot = 1), radix 2 and 4; twiddles are REAL*4.
+  __device__ void vpass(const T *A, T *C, int nh, int ifac, int la) const {
+    const double *trigs = p.trigs;
+    int m = nh / ifac;
+    int ngroups = m / la;
+    for (int g = 0; g < ngroups; ++g) {
+      T c1 = 1, s1 = 0, c2 = 1, s2 = 0, c3 = 1, s3 = 0;
+      int kb = 2 * g * la;
+      if (g > 0) {
+        c1 = (T)trigs[kb]; s1 = (T)trigs[kb + 1];
+        c2 = (T)trigs[2 * kb]; s2 = (T)trigs[2 * kb + 1];
+        if (ifac == 4) { c3 = (T)trigs[3 * kb]; s3 = (T)trigs[3 * kb + 1]; }
+      }
+      for (int l = 0; l < la; ++l) {
+        int pp = g * la + l, q = g * ifac * la + l;
+        T a0 = A[2 * pp], b0 = A[2 * pp + 1], a1 = A[2 * (pp + m)], b1 = A[2 * (pp + m) + 1];
+        if (ifac == 2) {
+          C[2 * q] = a0 + a1; C[2 * q + 1] = b0 + b1;
+          if (g == 0) { C[2 * (q + la)] = a0 - a1; C[2 * (q + la) + 1] = b0 - b1; }
+          else {
+            C[2 * (q + la)] = c1 * (a0 - a1) - s1 * (b0 - b1);
+            C[2 * (q + la) + 1] = s1 * (a0 - a1) + c1 * (b0 - b1);
+          }
+        } else {  // 4
+          T a2 = A[2 * (pp + 2 * m)], b2 = A[2 * (pp + 2 * m) + 1];
+          T a3 = A[2 * (pp + 3 * m)], b3 = A[2 * (pp + 3 * m) + 1];
+          T *C0 = C + 2 * q, *C1 = C + 2 * (q + la), *C2 = C + 2 * (q + 2 * la), *C3 = C + 2 * (q + 3 * la);
+          if (g == 0) {
+            C0[0] = (a0 + a2) + (a1 + a3); C2[0] = (a0 + a2) - (a1 + a3);
+            C0[1] = (b0 + b2) + (b1 + b3); C2[1] = (b0 + b2) - (b1 + b3);
+            C1[0] = (a0 - a2) - (b1 - b3); C3[0] = (a0 - a2) + (b1 - b3);
+            C1[1] = (b0 - b2) + (a1 - a3); C3[1] = (b0 - b2) - (a1 - a3);
+          } else {
+            C0[0] = (a0 + a2) + (a1 + a3); C0[1] = (b0 + b2) + (b1 + b3);
+            C2[0] = c2 * ((a0 + a2) - (a1 + a3)) - s2 * ((b0 + b2) - (b1 + b3));
+            C2[1] = s2 * ((a0 + a2) - (a1 + a3)) + c2 * ((b0 + b2) - (b1 + b3));
+            C1[0] = c1 * ((a0 - a2) - (b1 - b3)) - s1 * ((b0 - b2) + (a1 - a3));
+            C1[1] = s1 * ((a0 - a2) - (b1 - b3)) + c1 * ((b0 - b2) + (a1 - a3));
+            C3[0] = c3 * ((a0 - a2) + (b1 - b3)) - s3 * ((b0 - b2) - (a1 - a3));
+            C3[1] = s3 * ((a0 - a2) + (b1 - b3)) + c3 * ((b0 - b2) - (a1 - a3));
+          }
+        }
+      }
+    }
+  }
+  // fft991_crm (fft.F90:5-154) on a[0..n+1], lot = 1; isign -1: grid ->
+  // spectral, +1: spectral -> grid.
+  __device__ void fft991(T *a, T *work, int n, int isign) const {
+    const double *trigs = p.trigs;
+    int nfax = p.nfax, nh = n / 2;
+    bool in_work;
+    if (isign == -1) {
+      if (nfax % 2 == 1) in_work = false;
+      else { for (int m = 0; m < n; ++m) work[m] = a[m]; in_work = true; }
+    } else {
+      work[0] = a[0] + a[n];
+      work[1] = a[0] - a[n];
+      int ia = 2, ib = n - 2;
+      for (int k = 3; k <= nh; k += 2) {
+        T c = (T)trigs[n + k - 1], s = (T)trigs[n + k];
+        T ap = a[ia] + a[ib], am = a[ia] - a[ib];
+        T bp = a[ia + 1] + a[ib + 1], bm = a[ia + 1] - a[ib + 1];
+        work[ia] = ap - (s * am + c * bp);
+        work[ib] = ap + (s * am + c * bp);
+        work[ia + 1] = (c * am - s * bp) + bm;
+        work[ib + 1] = (c * am - s * bp) - bm;
+        ia += 2; ib -= 2;
+      }
+      if (ia == ib) { work[ia] = (T)2.0 * a[ia]; work[ia + 1] = (T)-2.0 * a[ia + 1]; }
+      in_work = true;
+    }
+    int la = 1;
+    for (int k = 1; k <= nfax; ++k) {
+      if (in_work) vpass(work, a, nh, p.ifax[k], la);
+      else vpass(a, work, nh, p.ifax[k], la);
+      in_work = !in_work;
+      la *= p.ifax[k];
+    }
+    if (isign == -1) {
+      float scale = (float)(1.0 / (double)n);
+      a[0] = (T)(double)scale * (work[0] + work[1]);
+      a[n] = (T)(double)scale * (work[0] - work[1]);
+      a[1] = (T)0.0;
+      a[n + 1] = (T)0.0;
+      scale = 0.5f * scale;
+      T sc = (T)(double)scale;
+      int ia = 2, ib = n - 2;
+      for (int k = 3; k <= nh; k += 2) {
+        T c = (T)trigs[n + k - 1], s = (T)trigs[n + k];
+        T wp = work[ia] + work[ib], wm = work[ia] - work[ib];
+        T vp = work[ia + 1] + work[ib + 1], vm = work[ib + 1] - work[ia + 1];
+        a[ia] = sc * (wp + (c * vp + s * wm));
+        a[ib] = sc * (wp - (c * vp + s * wm));
+        a[ia + 1] = sc * ((c * wm - s * vp) + vm);
+        a[ib + 1] = sc * ((c * wm - s * vp) - vm);
+        ia += 2; ib -= 2;
+      }
+      if (ia == ib) {
+        scale = 2.0f * scale;
+        a[ia] = (T)(double)scale * work[ia];
+        a[ia + 1] = -(T)(double)scale * work[ia + 1];
+      }
+    } else {
+      if (in_work) for (int m = 0; m < n; ++m) a[m] = work[m];
+      a[n] = (T)0.0;
+      a[n + 1] = (T)0.0;
+    }
+  }
+
+  // ---------------------------------------------------------- pressure
+  // pressure.F90:97-310, press_rhs.F90:48-101, press_grad.F90:18-72,
+  // bound_duvdt.F90 (2D)
+  __device__ void pressure() {
+    F2<T> u = U(), w = W(), pp = PP();
+    F2<T> dua = DU(S.na), dub = DU(S.nb), duc = DU(S.nc);
+    F2<T> dwa = DW(S.na), dwb = DW(S.nb), dwc = DW(S.nc);
+    T *rho = PR(P_RHO), *rhow = PR(P_RHOW), *adz = PR(P_ADZ), *adzw = PR(P_ADZW);
+    const T dz = (T)S.dz;
+    for (int k = TID + 1; k <= nzm; k += NT) dua(nx + 1, k) = dua(1, k);
+    SYNC;
+    const T rdx = (T)1. / (T)p.dx;
+    const T btat = (T)(S.bt / S.at), ctat = (T)(S.ct / S.at);
+    const T dta = (T)(1. / S.dt3[S.na - 1] / S.at);
+    const int nx2 = nx + 2, nwk = nx + 4;
+    T *fbuf = base + p.L.fft_f, *wbuf = base + p.L.fft_w;
+    for (int e = TID; e < nx * nzm; e += NT) {
+      int i = 1 + e % nx, k = 1 + e / nx;
+      int kc = k + 1, ic = i + 1;
+      T rdz = (T)1. / (adz[k] * dz);
+      T rup = rhow[kc] / rho[k] * rdz;
+      T rdn = rhow[k] / rho[k] * rdz;
+      T r = (rdx * (u(ic, k) - u(i, k)) + (w(i, kc) * rup - w(i, k) * rdn)) * dta +
+            (rdx * (dua(ic, k) - dua(i, k)) + (dwa(i, kc) * rup - dwa(i, k) * rdn)) +
+            btat * (rdx * (dub(ic, k) - dub(i, k)) + (dwb(i, kc) * rup - dwb(i, k) * rdn)) +
+            ctat * (rdx * (duc(ic, k) - duc(i, k)) + (dwc(i, kc) * rup - dwc(i, k) * rdn));
+      fbuf[(size_t)nx2 * k + (i - 1)] = r * rho[k];
+    }
+    SYNC;
+    for (int k = TID + 1; k <= nzm; k += NT) fft991(fbuf + (size_t)nx2 * k, wbuf + (size_t)nwk * k, nx, -1);
+    SYNC;
+    // vertical tridiagonal solve per Fourier coefficient, in FP64
+    double *alfa = reinterpret_cast<double *>(base + p.L.s_a);   // (nx+1) x nzm doubles
+    double *beta = reinterpret_cast<double *>(base + p.L.s_c);
+    for (int i = TID + 1; i <= nx + 1; i += NT) {
+      int id = (int)(((float)i - 0.1f) / 2.0f);
+      double eign = p.eign[i - 1];
+      auto A = [&](int k) { return (double)rhow[k] / ((double)adz[k] * (double)adzw[k] * S.dz * S.dz); };
+      auto Cc = [&](int k) { return (double)rhow[k + 1] / ((double)adz[k] * (double)adzw[k + 1] * S.dz * S.dz); };
+      auto FF = [&](int k) -> T & { return fbuf[(size_t)nx2 * k + (i - 1)]; };
+      double *al = alfa + (size_t)(i - 1) * (nzm + 1), *be = beta + (size_t)(i - 1) * (nzm + 1);
+      double b;
+      double a1 = A(1), c1 = Cc(1);
+      if (id == 0) b = 1. / (eign * (double)rho[1] - a1 - c1);
+      else b = 1. / (eign * (double)rho[1] - c1);
+      al[1] = -c1 * b;
+      be[1] = (double)FF(1) * b;
+      for (int k = 2; k <= nzm - 1; ++k) {
+        double ak = A(k), ck = Cc(k);
+        double e = 1. / (eign * (double)rho[k] - ak - ck + ak * al[k - 1]);
+        al[k] = -ck * e;
+        be[k] = ((double)FF(k) - ak * be[k - 1]) * e;
+      }
+      double an = A(nzm);
+      double fk = ((double)FF(nzm) - an * be[nzm - 1]) / (eign * (double)rho[nzm] - an + an * al[nzm - 1]);
+      FF(nzm) = (T)fk;
+      for (int k = nzm - 1; k >= 1; --k) {
+        fk = al[k] * fk + be[k];
+        FF(k) = (T)fk;
+      }
+    }
+    SYNC;
+    for (int k = TID + 1; k <= nzm; k += NT) fft991(fbuf + (size_t)nx2 * k, wbuf + (size_t)nwk * k, nx, +1);
+    SYNC;
+    for (int e = TID; e < (nx + 1) * nzm; e += NT) {
+      int i = e % (nx + 1), k = 1 + e / (nx + 1);
+      pp(i, k) = fbuf[(size_t)nx2 * k + ((i == 0 ? nx : i) - 1)];
+    }
+    SYNC;
+    F2<T> dva = DV(S.na);
+    const T rdy = (T)1. / (T)p.dy;
+    for (int e = TID; e < nx * nzm; e += NT) {
+      int i = 1 + e % nx, k = 1 + e / nx;
+      int kb = max(1, k - 1);
+      T rdz = (T)1. / (dz * adzw[k]);
+      dua(i, k) = dua(i, k) - (pp(i, k) - pp(i - 1, k)) * rdx;
+      dva(i, k) = dva(i, k) - (pp(i, k) - pp(i, k)) * rdy;
+      dwa(i, k) = dwa(i, k) - (pp(i, k) - pp(i, kb)) * rdz;
+    }
+    SYNC;
+    for (int e = TID; e < (nx + 1) * nzm; e += NT) {
+      int i = e % (nx + 1), k = 1 + e / (nx + 1);
+      pp(i, k) = pp(i, k) * rho[k];
+    }
+    for (int k = TID + 1; k <= nzm; k += NT) dua(nx + 1, k) = dua(1, k);
+    SYNC;
+  }
+
+  // ---------------------------------------------------------- adams / uvw
+  __device__ void adams() {                    // adams.F90:17-38
+    F2<T> u = U(), v = V(), w = W();
+    F2<T> dua = DU(S.na), dub = DU(S.nb), duc = DU(S.nc);
+    F2<T> dva = DV(S.na), dvb = DV(S.nb), dvc = DV(S.nc);
+    F2<T> dwa = DW(S.na), dwb = DW(S.nb), dwc = DW(S.nc);
+    const T dtdx = (T)(S.dtn / p.dx), dtdz = (T)(S.dtn / S.dz), dtdy = (T)(S.dtn / p.dy);
+    const T d3 = (T)S.dt3[S.na - 1], at = (T)S.at, bt = (T)S.bt, ct = (T)S.ct;
+    T *rho = PR(P_RHO), *rhow = PR(P_RHOW);
+    for (int e = TID; e < nx * nzm; e += NT) {
+      int i = 1 + e % nx, k = 1 + e / nx;
+      T rhox = rho[k] * dtdx, rhoy = rho[k] * dtdy, rhoz = rhow[k] * dtdz;
+      T un = u(i, k) + d3 * (at * dua(i, k) + bt * dub(i, k) + ct * duc(i, k));
+      T vn = v(i, k) + d3 * (at * dva(i, k) + bt * dvb(i, k) + ct * dvc(i, k));
+      T wn = w(i, k) + d3 * (at * dwa(i, k) + bt * dwb(i, k) + ct * dwc(i, k));
+      duc(i, k) = un; dvc(i, k) = vn; dwc(i, k) = wn;
+      u(i, k) = (T)0.5 * (u(i, k) + un) * rhox;
+      v(i, k) = (T)0.5 * (v(i, k) + vn) * rhoy;
+      w(i, k) = (T)0.5 * (w(i, k) + wn) * rhoz;
+    }
+    SYNC;
+  }
+  __device__ void uvw() {                      // uvw.F90
+    F2<T> u = U(), v = V(), w = W(), duc = DU(S.nc), dvc = DV(S.nc), dwc = DW(S.nc);
+    for (int e = TID; e < nx * nzm; e += NT) {
+      int i = 1 + e % nx, k = 1 + e / nx;
+      u(i, k) = duc(i, k); v(i, k) = dvc(i, k); w(i, k) = dwc(i, k);
+    }
+    SYNC;
+  }
+
+  // ---------------------------------------------------------- MPDATA
+  // ADV_MPDATA/advect_scalar.F90:39-72 + advect_scalar2D.F90:60-240.
+  // f is advected in place; fadv/flux (may be null) receive the per-level
+  // advective tendency sum and vertical flux sum.
+  __device__ void advect_scalar(F2<T> f, T *fadv, T *flux) {
+    F2<T> u = U(), w = W();
+    F2<T> mx = SCR(p.L.s_a), mn = SCR(p.L.s_b), uuu = SCR(p.L.s_c), www = SCR(p.L.s_d), f0 = SCR(p.L.s_e);
+    F2<T> wfl1 = SCR(p.L.s_f);
+    T *rho = PR(P_RHO), *adz = PR(P_ADZ), *rhow = PR(P_RHOW);
+    const T eps = (T)R4(1.e-10);
+    // f0, mx/mn from the initial field, upwind fluxes
+    for (int e = TID; e < (nx + 5) * nzm; e += NT) {
+      int i = -1 + e % (nx + 5), k = 1 + e / (nx + 5);   // i = -1 .. nx+3
+      int kc = min(nzm, k + 1), kb = max(1, k - 1);
+      if (i >= 0 && i <= nx + 1) {
+        int ib = i - 1, ic = i + 1;
+        mx(i, k) = mx2(mx2(mx2(mx2(f(ib, k), f(ic, k)), f(i, kb)), f(i, kc)), f(i, k));
+        mn(i, k) = mn2(mn2(mn2(mn2(f(ib, k), f(ic, k)), f(i, kb)), f(i, kc)), f(i, k));
+      }
+      if (fadv && i >= 1 && i <= nx) f0(i, k) = f(i, k);
+      uuu(i, k) = mx2((T)0., u(i, k)) * f(i - 1, k) + mn2((T)0., u(i, k)) * f(i, k);
+      if (i <= nx + 2) www(i, k) = mx2((T)0., w(i, k)) * f(i, kb) + mn2((T)0., w(i, k)) * f(i, k);
+      if (k == 1 && i <= nx + 2) www(i, nz) = (T)0.;
+    }
+    SYNC;
+    // first-pass (upwind) vertical flux sum, then the upwind update
+    if (flux)
+      for (int k = TID + 1; k <= nzm; k += NT) {
+        double s = 0.;
+        for (int i = 1; i <= nx; ++i) s = s + (double)www(i, k);
+        wfl1(0, k) = (T)s;
+      }
+    for (int e = TID; e < (nx + 4) * nzm; e += NT) {
+      int i = -1 + e % (nx + 4), k = 1 + e / (nx + 4);   // -1 .. nx+2
+      T iadz = (T)1. / adz[k], irho = (T)1. / rho[k];
+      f(i, k) = f(i, k) - (uuu(i + 1, k) - uuu(i, k) + (www(i, k + 1) - www(i, k)) * iadz) * irho;
+    }
+    SYNC;
+    // antidiffusive velocities (andiff, across)
+    for (int e = TID; e < (nx + 3) * nzm; e += NT) {
+      int i = e % (nx + 3), k = 1 + e / (nx + 3);          // 0 .. nx+2
+      int kc = min(nzm, k + 1), kb = max(1, k - 1);
+      T irho = (T)1. / rho[k];
+      T irhow = (T)1. / (rhow[k] * adz[k]);
+      T dd = (T)(double)(2.f / (float)(kc - kb)) / adz[k];
+      int ib = i - 1;
+      {
+        T a = u(i, k), x1 = f(ib, k), x2 = f(i, k);
+        T andiff = (tabs_(a) - a * a * irho) * (T)0.5 * (x2 - x1);
+        T ax1 = dd * (f(ib, kc) + f(i, kc) - f(ib, kb) - f(i, kb));
+        T a2 = w(ib, k) + w(ib, kc) + w(i, k) + w(i, kc);
+        T across = (T)0.03125 * a * a2 * ax1;
+        uuu(i, k) = andiff - across * irho;
+      }
+      if (i <= nx + 1) {
+        int ic = i + 1;
+        T a = w(i, k), x1 = f(i, kb), x2 = f(i, k);
+        T andiff = (tabs_(a) - a * a * irhow) * (T)0.5 * (x2 - x1);
+        T ax1 = f(ic, kb) + f(ic, k) - f(ib, kb) - f(ib, k);
+        T a2 = u(i, kb) + u(i, k) + u(ic, k) + u(ic, kb);
+        T across = (T)0.03125 * a * a2 * ax1;
+        www(i, k) = (k == 1) ? (T)0. : andiff - across * irho;
+      }
+    }
+    SYNC;
+    // non-oscillatory limiter
+    for (int e = TID; e < (nx + 2) * nzm; e += NT) {
+      int i = e % (nx + 2), k = 1 + e / (nx + 2);          // 0 .. nx+1
+      int kc = min(nzm, k + 1), kb = max(1, k - 1), ib = i - 1, ic = i + 1;
+      T iadz = (T)1. / adz[k];
+      T m1 = mx2(mx2(mx2(mx2(mx2(f(ib, k), f(ic, k)), f(i, kb)), f(i, kc)), f(i, k)), mx(i, k));
+      T m2 = mn2(mn2(mn2(mn2(mn2(f(ib, k), f(ic, k)), f(i, kb)), f(i, kc)), f(i, k)), mn(i, k));
+      T pu_c = -mn2((T)0., uuu(ic, k)), pu_i = mx2((T)0., uuu(i, k));
+      T pw_c = -mn2((T)0., www(i, kc)), pw_i = mx2((T)0., www(i, k));
+      mx(i, k) = rho[k] * (m1 - f(i, k)) / (pu_c + pu_i + iadz * (pw_c + pw_i) + eps);
+      T qu_c = mx2((T)0., uuu(ic, k)), qu_i = -mn2((T)0., uuu(i, k));
+      T qw_c = mx2((T)0., www(i, kc)), qw_i = -mn2((T)0., www(i, k));
+      mn(i, k) = rho[k] * (f(i, k) - m2) / (qu_c + qu_i + iadz * (qw_c + qw_i) + eps);
+    }
+    SYNC;
+    for (int e = TID; e < (nx + 1) * nzm; e += NT) {
+      int i = 1 + e % (nx + 1), k = 1 + e / (nx + 1);      // 1 .. nx+1
+      int ib = i - 1;
+      T uu = uuu(i, k);
+      uuu(i, k) = mx2((T)0., uu) * mn3((T)1., mx(i, k), mn(ib, k)) - (-mn2((T)0., uu)) * mn3((T)1., mx(ib, k), mn(i, k));
+      if (i <= nx) {
+        int kb = max(1, k - 1);
+        T ww = www(i, k);
+        www(i, k) = mx2((T)0., ww) * mn3((T)1., mx(i, k), mn(i, kb)) - (-mn2((T)0., ww)) * mn3((T)1., mx(i, kb), mn(i, k));
+      }
+    }
+    SYNC;
+    if (flux)
+      for (int k = TID + 1; k <= nzm; k += NT) {
+        double s = (double)wfl1(0, k);
+        for (int i = 1; i <= nx; ++i) s = s + (double)www(i, k);
+        flux[k] = (T)s;
+      }
+    for (int e = TID; e < nx * nzm; e += NT) {
+      int i = 1 + e % nx, k = 1 + e / nx;
+      T iadz = (T)1. / adz[k], irho = (T)1. / rho[k];
+      f(i, k) = mx2((T)0., f(i, k) - (uuu(i + 1, k) - uuu(i, k) + (www(i, k + 1) - www(i, k)) * iadz) * irho);
+    }
+    SYNC;
+    if (fadv) {
+      for (int k = TID + 1; k <= nzm; k += NT) {
+        double s = 0.;
+        for (int i = 1; i <= nx; ++i) s = s + (double)(f(i, k) - f0(i, k));
+        fadv[k] = (T)s;
+      }
+      SYNC;
+    }
+  }
+
+  // ---------------------------------------------------------- precip_fall
+  // MICRO_SAM1MOM/microphysics.F90:453-486 (term_vel_qp) and :491-833
+  __device__ T term_vel(T tabs, T rho, T qploc) const {
+    T term = (T)0.;
+    if (qploc > (T)C_QP_THRESHOLD) {
+      T omp = mx2((T)0., mn2((T)1., (tabs - (T)C_TPRMIN) * (T)p.a_pr));
+      if (omp == (T)1.) {
+        term = (T)p.vrain * tpow(rho * qploc, (T)p.crain);
+      } else if (omp == (T)0.) {
+        T omg = mx2((T)0., mn2((T)1., (tabs - (T)C_TGRMIN) * (T)p.a_gr));
+        T qgg = omg * qploc;
+        T qss = qploc - qgg;
+        term = omg * (T)p.vgrau * tpow(rho * qgg, (T)p.cgrau) + ((T)1. - omg) * (T)p.vsnow * tpow(rho * qss, (T)p.csnow);
+      } else {
+        T omg = mx2((T)0., mn2((T)1., (tabs - (T)C_TGRMIN) * (T)p.a_gr));
+        T qrr = omp * qploc;
+        T qss = qploc - qrr;
+        T qgg = omg * qss;
+        qss = qss - qgg;
+        term = omp * (T)p.vrain * tpow(rho * qrr, (T)p.crain) +
+               ((T)1. - omp) * (omg * (T)p.vgrau * tpow(rho * qgg, (T)p.cgrau) + ((T)1. - omg) * (T)p.vsnow * tpow(rho * qss, (T)p.csnow));
+      }
+    }
+    return term;
+  }
+  // part 1: terminal velocities and the column precipitation CFL number
+  __device__ void precip_fall_1() {
+    F2<T> tabs = TABS(), qp = QP();
+    F2<T> wp = SCR(p.L.s_a), omega = SCR(p.L.s_b);
+    T *rho = PR(P_RHO), *rhow = PR(P_RHOW), *adz = PR(P_ADZ);
+    T *rhofac = PR(P_TMP4), *irhoadz = PR(P_TMP5), *iwmax = PR(P_TMP6);
+    const T dtn = (T)S.dtn, dz = (T)S.dz;
+    for (int k = TID + 1; k <= nzm; k += NT) {
+      rhofac[k] = tsqrt((T)R4(1.29) / rho[k]);
+      irhoadz[k] = (T)1. / (rho[k] * adz[k]);
+      int kb = max(1, k - 1);
+      T wmax = dz * adz[kb] / dtn;
+      iwmax[k] = (T)1. / wmax;
+    }
+    SYNC;
+    double cfl = 0.;
+    for (int e = TID; e < nx * nzm; e += NT) {
+      int i = 1 + e % nx, k = 1 + e / nx;
+      omega(i, k) = mx2((T)0., mn2((T)1., (tabs(i, k) - (T)C_TPRMIN) * (T)p.a_pr));
+      T tmp = term_vel(tabs(i, k), rho[k], qp(i, k));
+      T wv = rhofac[k] * tmp;
+      cfl = mx2(cfl, (double)(wv * iwmax[k]));
+      wp(i, k) = -wv * rhow[k] * dtn / dz;
+    }
+    cfl = block_max(cfl);
+    if (TID == 0) {
+      S.prec_cfl = cfl;
+      S.nprec = (cfl > R4(0.9)) ? (int)ceil(cfl / R4(0.9)) : 1;
+    }
+    SYNC;
+  }
+  // part 2: nprec monotone flux-limited sedimentation sub-steps
+  __device__ void precip_fall_2(int nprec) {
+    F2<T> tabs = TABS(), qp = QP(), t = TT();
+    F2<T> wp = SCR(p.L.s_a), omega = SCR(p.L.s_b), tq = SCR(p.L.s_c), fz = SCR(p.L.s_d);
+    F2<T> mx = SCR(p.L.s_e), mn = SCR(p.L.s_f), www = SCR(p.L.s_g);
+    T *rho = PR(P_RHO), *rhow = PR(P_RHOW), *adz = PR(P_ADZ);
+    T *rhofac = PR(P_TMP4), *irhoadz = PR(P_TMP5);
+    T *qpfall = PR(P_QPFALL), *precflux = PR(P_PRECFLUX);
+    const T eps = (T)R4(1.e-10);
+    const T dtn = (T)S.dtn, dz = (T)S.dz;
+    const T fc = (T)C_FAC_COND, ffus = (T)C_FAC_FUS;
+    if (nprec > 1) {
+      for (int e = TID; e < nx * nzm; e += NT) {
+        int i = 1 + e % nx, k = 1 + e / nx;
+        wp(i, k) = wp(i, k) / (T)(double)nprec;
+      }
+      SYNC;
+    }
+    for (int iprec = 1; iprec <= nprec; ++iprec) {
+      for (int e = TID; e < nx * nzm; e += NT) {
+        int i = 1 + e % nx, k = 1 + e / nx;
+        int kc = min(nzm, k + 1), kb = max(1, k - 1);
+        T q0 = qp(i, k), qb = qp(i, kb), qc = qp(i, kc);
+        mx(i, k) = mx3(qb, qc, q0);
+        mn(i, k) = mn3(qb, qc, q0);
+        fz(i, k) = q0 * wp(i, k);
+        if (k == 1) { fz(i, nz) = (T)0.; www(i, nz) = (T)0.; }
+      }
+      SYNC;
+      for (int e = TID; e < nx * nzm; e += NT) {
+        int i = 1 + e % nx, k = 1 + e / nx;
+        tq(i, k) = qp(i, k) - (fz(i, k + 1) - fz(i, k)) * irhoadz[k];
+      }
+      SYNC;
+      for (int e = TID; e < nx * nzm; e += NT) {
+        int i = 1 + e % nx, k = 1 + e / nx;
+        int kb = max(1, k - 1);
+        www(i, k) = (T)0.5 * ((T)1. + wp(i, k) * irhoadz[k]) * (tq(i, kb) * wp(i, kb) - tq(i, k) * wp(i, k));
+      }
+      SYNC;
+      for (int e = TID; e < nx * nzm; e += NT) {
+        int i = 1 + e % nx, k = 1 + e / nx;
+        int kc = min(nzm, k + 1), kb = max(1, k - 1);
+        T a = mx2(mx3(tq(i, kb), tq(i, kc), tq(i, k)), mx(i, k));
+        T b = mn2(mn3(tq(i, kb), tq(i, kc), tq(i, k)), mn(i, k));
+        mx(i, k) = rho[k] * adz[k] * (a - tq(i, k)) / (-mn2((T)0., www(i, kc)) + mx2((T)0., www(i, k)) + eps);
+        mn(i, k) = rho[k] * adz[k] * (tq(i, k) - b) / (mx2((T)0., www(i, kc)) + -mn2((T)0., www(i, k)) + eps);
+      }
+      SYNC;
+      for (int e = TID; e < nx * nzm; e += NT) {
+        int i = 1 + e % nx, k = 1 + e / nx;
+        int kb = max(1, k - 1);
+        T ww = www(i, k);
+        fz(i, k) = fz(i, k) + mx2((T)0., ww) * mn3((T)1., mx(i, k), mn(i, kb)) - (-mn2((T)0., ww)) * mn3((T)1., mx(i, kb), mn(i, k));
+      }
+      SYNC;
+      // per-level budget sums in the reference's order, then the update
+      for (int k = TID + 1; k <= nzm; k += NT) {
+        double sf = (double)qpfall[k], sp = (double)precflux[k];
+        for (int i = 1; i <= nx; ++i) {
+          T d = -(fz(i, k + 1) - fz(i, k)) * irhoadz[k] * (T)1.;
+          sf = sf + (double)d;
+          sp = sp - (double)(fz(i, k) * (T)1.);
+        }
+        qpfall[k] = (T)sf; precflux[k] = (T)sp;
+      }
+      for (int e = TID; e < nx * nzm; e += NT) {
+        int i = 1 + e % nx, k = 1 + e / nx;
+        int kc = k + 1;
+        T lf_c = (kc == nz) ? (T)0. : fc + ((T)1. - omega(i, kc)) * ffus;
+        T lf_k = fc + ((T)1. - omega(i, k)) * ffus;
+        qp(i, k) = qp(i, k) - (fz(i, kc) - fz(i, k)) * irhoadz[k];
+        T lat_heat = -(lf_c * fz(i, kc) - lf_k * fz(i, k)) * irhoadz[k];
+        t(i, k) = t(i, k) - lat_heat;
+        if (k == 1) {
+          PS(i) = PS(i) - fz(i, 1) * (T)1.;
+          PSS(i) = PSS(i) - fz(i, 1) * ((T)1. - omega(i, 1)) * (T)1.;
+        }
+      }
+      SYNC;
+      if (iprec < nprec) {
+        for (int e = TID; e < nx * nzm; e += NT) {
+          int i = 1 + e % nx, k = 1 + e / nx;
+          T tmp = term_vel(tabs(i, k), rho[k], qp(i, k));
+          T wv = rhofac[k] * tmp;
+          wp(i, k) = -wv * rhow[k] * dtn / dz / (T)(double)nprec;
+        }
+        SYNC;
+      }
+    }
+  }
+
+  // ---------------------------------------------------------- SGS scalar diffusion
+  // SGS_TKE/diffuse_scalar.F90:33-72 + diffuse_scalar2D.F90:44-140
+  __device__ void diffuse_scalar(F2<T> f, T *fdiff, T *flux) {
+    F2<T> tkh = TKH(), flx = SCR(p.L.s_a), dfdt = SCR(p.L.s_b), f0 = SCR(p.L.s_c);
+    T *rho = PR(P_RHO), *rhow = PR(P_RHOW), *adz = PR(P_ADZ), *adzw = PR(P_ADZW);
+    T *grdfx = PR(P_GRDFX), *grdfz = PR(P_GRDFZ);
+    const T dx = (T)p.dx, dz = (T)S.dz, dtn = (T)S.dtn;
+    const T rdx2 = (T)1. / (dx * dx);
+    for (int e = TID; e < (nx + 1) * nzm; e += NT) {
+      int i = e % (nx + 1), k = 1 + e / (nx + 1);        // 0 .. nx
+      T rdx5 = (T)0.5 * rdx2 * grdfx[k];
+      int ic = i + 1;
+      T tkx = rdx5 * (tkh(i, k) + tkh(ic, k));
+      flx(i, k) = -tkx * (f(ic, k) - f(i, k));
+      if (fdiff && i >= 1) f0(i, k) = f(i, k);
+    }
+    SYNC;
+    for (int e = TID; e < nx * nzm; e += NT) {
+      int i = 1 + e % nx, k = 1 + e / nx;
+      dfdt(i, k) = (T)0. - (flx(i, k) - flx(i - 1, k));
+    }
+    SYNC;
+    // vertical fluxes (flx reused, levels 0..nzm)
+    for (int e = TID; e < nx * nzm; e += NT) {
+      int i = 1 + e % nx, k = 1 + e / nx;
+      if (k <= nzm - 1) {
+        int kc = k + 1;
+        T rhoi = rhow[kc] / adzw[kc];
+        T rdz2 = (T)1. / (dz * dz);
+        T rdz5 = (T)0.5 * rdz2 * grdfz[k];
+        T tkz = rdz5 * (tkh(i, k) + tkh(i, kc));
+        flx(i, k) = -tkz * (f(i, kc) - f(i, k)) * rhoi;
+      } else {
+        T tmp = (T)1. / adzw[nz];
+        T rdz = (T)1. / dz;
+        flx(i, 0) = (T)0.0 * rdz * rhow[1];
+        flx(i, nzm) = (T)0.0 * rdz * tmp * rhow[nz];
+      }
+    }
+    SYNC;
+    if (flux)
+      for (int k = TID + 1; k <= nzm; k += NT) {
+        double s = 0.;
+        if (k == 1) for (int i = 1; i <= nx; ++i) s = s + (double)flx(i, 0);
+        else for (int i = 1; i <= nx; ++i) s = s + (double)flx(i, k - 1);
+        flux[k] = (T)s;
+      }
+    for (int e = TID; e < nx * nzm; e += NT) {
+      int i = 1 + e % nx, k = 1 + e / nx;
+      int kb = k - 1;
+      T rhoi = (T)1. / (adz[k] * rho[k]);
+      T d = dtn * (dfdt(i, k) - (flx(i, k) - flx(i, kb)) * rhoi);
+      f(i, k) = f(i, k) + d;
+    }
+    SYNC;
+    if (fdiff) {
+      for (int k = TID + 1; k <= nzm; k += NT) {
+        double s = 0.;
+        for (int i = 1; i <= nx; ++i) s = s + (double)(f(i, k) - f0(i, k));
+        fdiff[k] = (T)s;
+      }
+      SYNC;
+    }
+  }
+
+  // ---------------------------------------------------------- cloud
+  // MICRO_SAM1MOM/cloud.F90:26-111: saturation adjustment, Newton in FP64
+  __device__ void cloud() {
+    F2<T> qt = QT(), qp = QP(), qn = QN(), tabs = TABS(), t = TT();
+    T *gamaz = PR(P_GAMAZ), *pres = PR(P_PRES);
+    const double an = 1. / (C_TBGMAX - C_TBGMIN), bn = C_TBGMIN * an;
+    const double ap = 1. / (C_TPRMAX - C_TPRMIN), bp = C_TPRMIN * ap;
+    const double fac1 = C_FAC_COND + (1 + bp) * C_FAC_FUS;
+    const double fac2 = C_FAC_FUS * ap;
+    for (int e = TID; e < nx * nzm; e += NT) {
+      int i = 1 + e % nx, k = 1 + e / nx;
+      double pr = (double)pres[k];
+      double q = mx2(0., (double)qt(i, k));
+      double qpv = (double)qp(i, k);
+      double tab = (double)(t(i, k) - gamaz[k]);
+      double tabs1 = (tab + fac1 * qpv) / (1. + fac2 * qpv);
+      double qsatt;
+      if (tabs1 >= C_TBGMAX) {
+        tabs1 = tab + C_FAC_COND * qpv;
+        qsatt = qsatw(tabs1, pr);
+      } else if (tabs1 <= C_TBGMIN) {
+        tabs1 = tab + C_FAC_SUB * qpv;
+        qsatt = qsati(tabs1, pr);
+      } else {
+        double om = an * tabs1 - bn;
+        qsatt = om * qsatw(tabs1, pr) + (1. - om) * qsati(tabs1, pr);
+      }
+      double qnv;
+      if (q > qsatt) {
+        int niter = 0;
+        double dtabs = 100.;
+        double dqsat = 0.;
+        while (fabs(dtabs) > R4(0.01) && niter < 10) {
+          double lstarn, dlstarn, lstarp, dlstarp;
+          if (tabs1 >= C_TBGMAX) {
+            lstarn = C_FAC_COND; dlstarn = 0.;
+            qsatt = qsatw(tabs1, pr); dqsat = dtqsatw(tabs1, pr);
+          } else if (tabs1 <= C_TBGMIN) {
+            lstarn = C_FAC_SUB; dlstarn = 0.;
+            qsatt = qsati(tabs1, pr); dqsat = dtqsati(tabs1, pr);
+          } else {
+            double om = an * tabs1 - bn;
+            lstarn = C_FAC_COND + (1. - om) * C_FAC_FUS;
+            dlstarn = an * C_FAC_FUS;
+            qsatt = om * qsatw(tabs1, pr) + (1. - om) * qsati(tabs1, pr);
+            dqsat = om * dtqsatw(tabs1, pr) + (1. - om) * dtqsati(tabs1, pr);
+          }
+          if (tabs1 >= C_TPRMAX) { lstarp = C_FAC_COND; dlstarp = 0.; }
+          else if (tabs1 <= C_TPRMIN) { lstarp = C_FAC_SUB; dlstarp = 0.; }
+          else {
+            double omp = ap * tabs1 - bp;
+            lstarp = C_FAC_COND + (1. - omp) * C_FAC_FUS;
+            dlstarp = ap * C_FAC_FUS;
+          }
+          double fff = tab - tabs1 + lstarn * (q - qsatt) + lstarp * qpv;
+          double dfff = dlstarn * (q - qsatt) + dlstarp * qpv - lstarn * dqsat - 1.;
+          dtabs = -fff / dfff;
+          niter = niter + 1;
+          tabs1 = tabs1 + dtabs;
+        }
+        qsatt = qsatt + dqsat * dtabs;
+        qnv = mx2(0., q - qsatt);
+      } else {
+        qnv = 0.;
+      }
+      qt(i, k) = (T)q;
+      qn(i, k) = (T)qnv;
+      tabs(i, k) = (T)tabs1;
+      qp(i, k) = mx2((T)0., qp(i, k));
+    }
+    SYNC;
+  }
+
+  // ---------------------------------------------------------- precip_proc
+  // MICRO_SAM1MOM/precip_proc.F90:40-148; qpsrc/qpevp summed per level in
+  // the reference's order from the per-cell contributions
+  __device__ void precip_proc() {
+    F2<T> qt = QT(), qp = QP(), qn = QN(), tabs = TABS();
+    F2<T> csrc = SCR(p.L.s_a), cevp = SCR(p.L.s_b), flag = SCR(p.L.s_c);
+    T *pres = PR(P_PRES);
+    const T powr1 = (T)((3 + C_B_RAIN) / 4.), powr2 = (T)((5 + C_B_RAIN) / 8.);
+    const T pows1 = (T)((3 + C_B_SNOW) / 4.), pows2 = (T)((5 + C_B_SNOW) / 8.);
+    const T powg1 = (T)((3 + C_B_GRAU) / 4.), powg2 = (T)((5 + C_B_GRAU) / 8.);
+    const T dtn = (T)S.dtn;
+    const T a_bg = (T)p.a_bg, a_pr = (T)p.a_pr, a_gr = (T)p.a_gr;
+    for (int e = TID; e < nx * nzm; e += NT) {
+      int i = 1 + e % nx, k = 1 + e / nx;
+      T q = qt(i, k), qpv = qp(i, k), qnv = qn(i, k), tb = tabs(i, k);
+      T src = (T)0., evp = (T)0.;
+      int fl = 0;          // bit 0: contributes to qpsrc, bit 1: to qpevp
+      if (qnv + qpv > (T)0.) {
+        T omn = mx2((T)0., mn2((T)1., (tb - (T)C_TBGMIN) * a_bg));
+        T omp = mx2((T)0., mn2((T)1., (tb - (T)C_TPRMIN) * a_pr));
+        T omg = mx2((T)0., mn2((T)1., (tb - (T)C_TGRMIN) * a_gr));
+        if (qnv > (T)0.) {
+          T qcc = qnv * omn;
+          T qii = qnv * ((T)1. - omn);
+          T autor = (qcc > (T)C_QCW0) ? (T)C_ALPHAELQ : (T)0.;
+          T autos = (qii > (T)C_QCI0) ? (T)C_BETAELQ * PR(P_COEFICE)[k] : (T)0.;
+          T accrr = (T)0.;
+          if (omp > (T)R4(0.001)) {
+            T qrr = qpv * omp;
+            accrr = PR(P_ACCRRC)[k] * tpow(qrr, powr1);
+          }
+          T accrcs = (T)0., accris = (T)0.;
+          if (omp < (T)R4(0.999) && omg < (T)R4(0.999)) {
+            T qss = qpv * ((T)1. - omp) * ((T)1. - omg);
+            T tmp = tpow(qss, pows1);
+            accrcs = PR(P_ACCRSC)[k] * tmp;
+            accris = PR(P_ACCRSI)[k] * tmp;
+          }
+          T accrcg = (T)0., accrig = (T)0.;
+          if (omp < (T)R4(0.999) && omg > (T)R4(0.001)) {
+            T qgg = qpv * ((T)1. - omp) * omg;
+            T tmp = tpow(qgg, powg1);
+            accrcg = PR(P_ACCRGC)[k] * tmp;
+            accrig = PR(P_ACCRGI)[k] * tmp;
+          }
+          qcc = (qcc + dtn * autor * (T)C_QCW0) / ((T)1. + dtn * (accrr + accrcs + accrcg + autor));
+          qii = (qii + dtn * autos * (T)C_QCI0) / ((T)1. + dtn * (accris + accrig + autos));
+          T dq = dtn * (accrr * qcc + autor * (qcc - (T)C_QCW0) + (accris + accrig) * qii +
+                        (accrcs + accrcg) * qcc + autos * (qii - (T)C_QCI0));
+          dq = mn2(dq, qnv);
+          qpv = qpv + dq;
+          q = q - dq;
+          qnv = qnv - dq;
+          src = dq; fl = 1;
+        } else if (qpv > (T)C_QP_THRESHOLD && qnv == (T)0.) {
+          T qsatt = (T)0.;
+          if (omn > (T)R4(0.001)) qsatt = qsatt + omn * qsatw(tb, pres[k]);
+          if (omn < (T)R4(0.999)) qsatt = qsatt + ((T)1. - omn) * qsati(tb, pres[k]);
+          T dq = (T)0.;
+          if (omp > (T)R4(0.001)) {
+            T qrr = qpv * omp;
+            dq = dq + PR(P_EVAPR1)[k] * tsqrt(qrr) + PR(P_EVAPR2)[k] * tpow(qrr, powr2);
+          }
+          if (omp < (T)R4(0.999) && omg < (T)R4(0.999)) {
+            T qss = qpv * ((T)1. - omp) * ((T)1. - omg);
+            dq = dq + PR(P_EVAPS1)[k] * tsqrt(qss) + PR(P_EVAPS2)[k] * tpow(qss, pows2);
+          }
+          if (omp < (T)R4(0.999) && omg > (T)R4(0.001)) {
+            T qgg = qpv * ((T)1. - omp) * omg;
+            dq = dq + PR(P_EVAPG1)[k] * tsqrt(qgg) + PR(P_EVAPG2)[k] * tpow(qgg, powg2);
+          }
+          dq = dq * dtn * (q / qsatt - (T)1.);
+          dq = mx2((T)-0.5 * qpv, dq);
+          qpv = qpv + dq;
+          q = q - dq;
+          evp = dq; fl = 2;
+        } else {
+          q = q + qpv;
+          evp = qpv; fl = 3;            // qpevp = qpevp - qp
+          qpv = (T)0.;
+        }
+      }
+      T dq = qpv;
+      qpv = mx2((T)0., qpv);
+      q = q + (dq - qpv);
+      qt(i, k) = q; qp(i, k) = qpv; qn(i, k) = qnv;
+      csrc(i, k) = src; cevp(i, k) = evp; flag(i, k) = (T)fl;
+    }
+    SYNC;
+    T *qpsrc = PR(P_QPSRC), *qpevp = PR(P_QPEVP);
+    for (int k = TID + 1; k <= nzm; k += NT) {
+      double s = 0., v = 0.;
+      for (int i = 1; i <= nx; ++i) {
+        int fl = (int)flag(i, k);
+        if (fl == 1) s = s + (double)csrc(i, k);
+        else if (fl == 2) v = v + (double)cevp(i, k);
+        else if (fl == 3) v = v - (double)cevp(i, k);
+      }
+      qpsrc[k] = (T)s; qpevp[k] = (T)v;
+    }
+    SYNC;
+  }
+
+  // ---------------------------------------------------------- diagnose
+  __device__ void diagnose() {                 // diagnose.F90:21-85
+    F2<T> t = TT(), tabs = TABS(), qcl = QCL(), qci = QCI(), qpl = QPL(), qpi = QPI(), qv = QV(), u = U(), v = V();
+    T *gamaz = PR(P_GAMAZ);
+    for (int e = TID; e < nx * nzm; e += NT) {
+      int i = 1 + e % nx, k = 1 + e / nx;
+      tabs(i, k) = t(i, k) - gamaz[k] + (T)C_FAC_COND * (qcl(i, k) + qpl(i, k)) + (T)C_FAC_SUB * (qci(i, k) + qpi(i, k));
+    }
+    SYNC;
+    const double coef = 1. / (double)nx;
+    for (int k = TID + 1; k <= nzm; k += NT) {
+      double su = 0, sv = 0, st = 0, sa = 0, sq = 0, sn = 0, sp = 0;
+      for (int i = 1; i <= nx; ++i) {
+        su = su + (double)u(i, k);
+        sv = sv + (double)v(i, k);
+        st = st + (double)t(i, k);
+        sa = sa + (double)tabs(i, k);
+        sq = sq + (double)(qv(i, k) + qcl(i, k) + qci(i, k));
+        sn = sn + (double)(qcl(i, k) + qci(i, k));
+        sp = sp + (double)(qpl(i, k) + qpi(i, k));
+      }
+      su = su * coef; sv = sv * coef; st = st * coef; sa = sa * coef; sq = sq * coef; sn = sn * coef; sp = sp * coef;
+      PR(P_U0)[k] = (T)su; PR(P_V0)[k] = (T)sv; PR(P_T0)[k] = (T)st; PR(P_TABS0)[k] = (T)sa;
+      PR(P_Q0)[k] = (T)sq; PR(P_QN0)[k] = (T)sn; PR(P_QP0)[k] = (T)sp;
+      PR(P_QV0)[k] = (T)(sq - sn);
+    }
+    SYNC;
+  }
+
+  // ---------------------------------------------------------- step statistics
+  // crm_module.F90:896-1073, accumulated every CRM step
+  __device__ void step_stats() {
+    F2<T> qcl = QCL(), qci = QCI(), qpl = QPL(), qpi = QPI(), w = W(), tabs = TABS(), qv = QV();
+    T *rho = PR(P_RHO), *adz = PR(P_ADZ), *pres = PR(P_PRES), *rhow = PR(P_RHOW);
+    T *cs = base + p.L.colstat;     // 8 x nx: cwp, cwph, cwpm, cwpl, top level
+    const T dz = (T)S.dz;
+    const T thr = (T)R4(0.001);
+    for (int i = TID + 1; i <= nx; i += NT) {
+      T cwp = (T)0., cwph = (T)0., cwpm = (T)0., cwpl = (T)0.;
+      int top = 0;
+      for (int k = 1; k <= nzm; ++k) {
+        int kk = nz - k;
+        T tmp1 = rho[kk] * adz[kk] * dz * (qcl(i, kk) + qci(i, kk));
+        cwp = cwp + tmp1;
+        if (cwp > thr && top == 0) top = k;
+        if (pres[kk] >= (T)700.) cwpl = cwpl + tmp1;
+        else if (pres[kk] < (T)400.) cwph = cwph + tmp1;
+        else cwpm = cwpm + tmp1;
+      }
+      cs[(i - 1)] = cwp; cs[nx + (i - 1)] = cwph; cs[2 * nx + (i - 1)] = cwpm; cs[3 * nx + (i - 1)] = cwpl;
+      cs[4 * nx + (i - 1)] = (T)top;
+    }
+    SYNC;
+    T *ocld = OP(O_CLD), *otop = OP(O_CLDTOP), *oice = OP(O_GICEWP), *oliq = OP(O_GLIQWP);
+    T *mcup = OP(O_MCUP), *mcdn = OP(O_MCDN), *mcuup = OP(O_MCUUP), *mcudn = OP(O_MCUDN);
+    T *mui = OP(O_MUI), *mdi = OP(O_MDI);
+    for (int k = TID + 1; k <= nz; k += NT) {
+      // interface mass fluxes at w level k (GCM interface l = plev + 2 - k)
+      {
+        int l = plev + 2 - k;
+        double su = (double)mui[l], sd = (double)mdi[l];
+        for (int i = 1; i <= nx; ++i) {
+          T wv = w(i, k);
+          if (wv > (T)0.) {
+            int kx = max(1, k - 1);
+            T qs = qsatw(tabs(i, kx), pres[kx]);
+            if (qcl(i, kx) + qci(i, kx) > mn2((T)R4(1.e-5), (T)R4(0.01) * qs)) su = su + (double)(rhow[k] * wv);
+          } else if (wv < (T)0.) {
+            int kx = min(k + 1, nzm);
+            T qs = qsatw(tabs(i, kx), pres[kx]);
+            if (qcl(i, kx) + qci(i, kx) > mn2((T)R4(1.e-5), (T)R4(0.01) * qs)) sd = sd + (double)(rhow[k] * wv);
+            else if (qpl(i, kx) + qpi(i, kx) > (T)R4(1.0e-4)) sd = sd + (double)(rhow[k] * wv);
+          }
+        }
+        mui[l] = (T)su; mdi[l] = (T)sd;
+      }
+      if (k > nzm) continue;
+      int l = plev - k + 1;
+      // cloud top counts: column i crossed the threshold at step index k
+      {
+        double c = (double)otop[l];
+        for (int i = 1; i <= nx; ++i)
+          if ((int)cs[4 * nx + (i - 1)] == k) c = c + 1.;
+        otop[l] = (T)c;
+      }
+      double scld = (double)ocld[l], sup = (double)mcup[l], sdn = (double)mcdn[l];
+      double suu = (double)mcuup[l], sud = (double)mcudn[l], sli = (double)oliq[l], sic = (double)oice[l];
+      T tmp1 = rho[k] * adz[k] * dz;
+      for (int i = 1; i <= nx; ++i) {
+        T ws = w(i, k + 1) + w(i, k);
+        if (tmp1 * (qcl(i, k) + qci(i, k)) > thr) {
+          scld = scld + 1.0;
+          if (ws > (T)4.) {
+            sup = sup + (double)(rho[k] * (T)0.5 * ws * (T)1.0);
+            suu = suu + (double)(rho[k] * (T)0.5 * ws * ((T)1.0 - (T)1.0));
+          }
+          if (ws < (T)-4.) {
+            sdn = sdn + (double)(rho[k] * (T)0.5 * ws * (T)1.0);
+            sud = sud + (double)(rho[k] * (T)0.5 * ws * ((T)1. - (T)1.0));
+          }
+        } else {
+          if (ws > (T)4.) suu = suu + (double)(rho[k] * (T)0.5 * ws);
+          if (ws < (T)-4.) sud = sud + (double)(rho[k] * (T)0.5 * ws);
+        }
+        sli = sli + (double)qcl(i, k);
+        sic = sic + (double)qci(i, k);
+      }
+      ocld[l] = (T)scld; mcup[l] = (T)sup; mcdn[l] = (T)sdn; mcuup[l] = (T)suu; mcudn[l] = (T)sud;
+      oliq[l] = (T)sli; oice[l] = (T)sic;
+    }
+    // radiation-group sums (crm_module.F90:1000-1028)
+    const int nxr = p.L.nx_rad, gx = nx / nxr;
+    T *rad = base + p.L.rad;
+    for (int e = TID; e < nxr * nzm; e += NT) {
+      int ir = 1 + e % nxr, k = 1 + e / nxr;
+      size_t o = (size_t)(k - 1) * nxr + (ir - 1);
+      double st = (double)rad[o], sq = (double)rad[(size_t)nxr * nzm + o], sc = (double)rad[(size_t)2 * nxr * nzm + o];
+      double si = (double)rad[(size_t)3 * nxr * nzm + o], sl = (double)rad[(size_t)4 * nxr * nzm + o];
+      for (int i = (ir - 1) * gx + 1; i <= ir * gx; ++i) {
+        st = st + (double)tabs(i, k);
+        sq = sq + (double)mx2((T)0., qv(i, k));
+        sc = sc + (double)qcl(i, k);
+        si = si + (double)qci(i, k);
+        if (qcl(i, k) + qci(i, k) > (T)0) sl = sl + 1.0;
+      }
+      rad[o] = (T)st; rad[(size_t)nxr * nzm + o] = (T)sq; rad[(size_t)2 * nxr * nzm + o] = (T)sc;
+      rad[(size_t)3 * nxr * nzm + o] = (T)si; rad[(size_t)4 * nxr * nzm + o] = (T)sl;
+    }
+    SYNC;
+    if (TID == 0) {
+      // shaded cloud fractions: cf3d = 1, so each temperature flag is 1
+      // wherever its layer exists (crm_module.F90:1053-1072)
+      bool anyl = false, anyh = false, anym = false;
+      for (int k = 1; k <= nzm; ++k) {
+        if (pres[k] >= (T)700.) anyl = true;
+        else if (pres[k] < (T)400.) anyh = true;
+        else anym = true;
+      }
+      for (int i = 1; i <= nx; ++i) {
+        if (cs[(i - 1)] > thr) S.cltot = S.cltot + 1.0;
+        if (cs[nx + (i - 1)] > thr) S.clhgh = S.clhgh + (anyh ? 1.0 : 0.0);
+        if (cs[2 * nx + (i - 1)] > thr) S.clmed = S.clmed + (anym ? 1.0 : 0.0);
+        if (cs[3 * nx + (i - 1)] > thr) S.cllow = S.cllow + (anyl ? 1.0 : 0.0);
+      }
+    }
+    SYNC;
+  }
+
+  // ---------------------------------------------------------- finalize
+  // crm_module.F90:1086-1594
+  __device__ void finalize() {
+    const int ld = p.ld;
+    const double factor_xy = 1.0 / (double)nx;
+    const double icrm_run_time = 1.0 / p.dt_gl;
+    const double factor_xyt = factor_xy / (double)p.nstop;
+    const int ptop = plev - nzm + 1;
+    auto O1 = [&](int f) -> double & { return p.out[f][icrm]; };
+    auto O2 = [&](int f, int l) -> double & { return p.out[f][(size_t)icrm + (size_t)ld * (l - 1)]; };
+    // zero every GCM-level output of this column first
+    for (int e = TID; e < (CRM_NOUT - CRM_OUT_FIRST_2D) * plev; e += NT) {
+      int f = CRM_OUT_FIRST_2D + e / plev, l = 1 + e % plev;
+      O2(f, l) = 0.;
+    }
+    F2<T> tabs = TABS(), qv = QV(), qcl = QCL(), qci = QCI(), qpl = QPL(), qpi = QPI(), u = U(), v = V(), w = W();
+    F2<T> qt = QT(), qp = QP(), qn = QN(), tk = TK(), tkh = TKH(), tke = TKE();
+    // radiation means
+    {
+      const int nxr = p.L.nx_rad;
+      double tmp1 = ((double)nxr / (double)nx) * ((double)1 / (double)1) / (double)p.nstop;
+      T *rad = base + p.L.rad;
+      for (int e = TID; e < nxr * nzm; e += NT) {
+        int ir = 1 + e % nxr, k = 1 + e / nxr;
+        size_t o = (size_t)icrm + (size_t)ld * ((ir - 1) + (size_t)nxr * (k - 1));
+        size_t s = (size_t)(k - 1) * nxr + (ir - 1);
+        for (int f = 0; f < 5; ++f) p.radout[f][o] = (double)rad[(size_t)f * nxr * nzm + s] * tmp1;
+      }
+    }
+    SYNC;
+    // GCM-level means of the final state and the tendencies
+    for (int l = TID + 1; l <= plev; l += NT) {
+      double tln, qln, qccln, qiiln;
+      if (l < ptop) {
+        tln = IN(p.tl, l); qln = IN(p.ql, l); qccln = IN(p.qccl, l); qiiln = IN(p.qiil, l);
+      } else {
+        int k = plev - l + 1;
+        double st = 0., sq = 0., sc = 0., si = 0.;
+        for (int i = 1; i <= nx; ++i) {
+          st = st + (double)tabs(i, k);
+          sq = sq + (double)qv(i, k);
+          sc = sc + (double)qcl(i, k);
+          si = si + (double)qci(i, k);
+        }
+        tln = st * factor_xy; qln = sq * factor_xy; qccln = sc * factor_xy; qiiln = si * factor_xy;
+      }
+      bool top2 = (l == ptop || l == ptop + 1);
+      O2(CRM_OUT_SLTEND, l) = top2 ? 0. : C_CP * (tln - IN(p.tl, l)) * icrm_run_time;
+      O2(CRM_OUT_QLTEND, l) = top2 ? 0. : (qln - IN(p.ql, l)) * icrm_run_time;
+      O2(CRM_OUT_QCLTEND, l) = top2 ? 0. : (qccln - IN(p.qccl, l)) * icrm_run_time;
+      O2(CRM_OUT_QILTEND, l) = top2 ? 0. : (qiiln - IN(p.qiil, l)) * icrm_run_time;
+      // cloud and mass-flux statistics
+      double pdel = IN(p.pdel, l);
+      O2(CRM_OUT_CLD, l) = mn2(1.0, (double)OP(O_CLD)[l] * factor_xyt);
+      O2(CRM_OUT_CLDTOP, l) = mn2(1.0, (double)OP(O_CLDTOP)[l] * factor_xyt);
+      O2(CRM_OUT_GICEWP, l) = (double)OP(O_GICEWP)[l] * pdel * 1000. / C_GGR * factor_xyt;
+      O2(CRM_OUT_GLIQWP, l) = (double)OP(O_GLIQWP)[l] * pdel * 1000. / C_GGR * factor_xyt;
+      double mcup = (double)OP(O_MCUP)[l] * factor_xyt, mcdn = (double)OP(O_MCDN)[l] * factor_xyt;
+      double mcuup = (double)OP(O_MCUUP)[l] * factor_xyt, mcudn = (double)OP(O_MCUDN)[l] * factor_xyt;
+      O2(CRM_OUT_MCUP, l) = mcup; O2(CRM_OUT_MCDN, l) = mcdn;
+      O2(CRM_OUT_MCUUP, l) = mcuup; O2(CRM_OUT_MCUDN, l) = mcudn;
+      O2(CRM_OUT_MCTOT, l) = mcup + mcdn + mcuup + mcudn;
+      double mui0 = (double)OP(O_MUI)[l], mui1 = (double)OP(O_MUI)[l + 1];
+      double mdi0 = (double)OP(O_MDI)[l], mdi1 = (double)OP(O_MDI)[l + 1];
+      double mu = 0.5 * (mui0 + mui1), md = 0.5 * (mdi0 + mdi1);
+      mu = mu * C_GGR / 100.;
+      md = md * C_GGR / 100.;
+      O2(CRM_OUT_MU_CRM, l) = mu;
+      O2(CRM_OUT_MD_CRM, l) = md;
+      if (mui0 - mui1 > 0) O2(CRM_OUT_EU_CRM, l) = (mui0 - mui1) * C_GGR / pdel;
+      else O2(CRM_OUT_DU_CRM, l) = -1.0 * (mui0 - mui1) * C_GGR / pdel;
+      if (mdi1 - mdi0 < 0) O2(CRM_OUT_ED_CRM, l) = (mdi0 - mdi1) * C_GGR / pdel;
+      bool act = fabs(mu) > R4(1.0e-15) || fabs(md) > R4(1.0e-15);
+      if (act) atomicMin(&S.jt_min, l);
+      if (act) atomicMax(&S.mx_max, l);
+    }
+    SYNC;
+    // flux and condensate profiles at CRM levels
+    for (int k = TID + 1; k <= nzm; k += NT) {
+      int l = plev - k + 1;
+      double qcm = 0, qim = 0, qrm = 0, qgm = 0, qsm = 0, u2z = 0, v2z = 0, w2z = 0, stke = 0, stk = 0;
+      T u0 = PR(P_U0)[k], v0 = PR(P_V0)[k];
+      for (int i = 1; i <= nx; ++i) {
+        qcm = qcm + (double)qcl(i, k);
+        qim = qim + (double)qci(i, k);
+        qrm = qrm + (double)qpl(i, k);
+        T omg = mx2((T)0., mn2((T)1., (tabs(i, k) - (T)C_TGRMIN) * (T)p.a_gr));
+        qgm = qgm + (double)(qpi(i, k) * omg);
+        qsm = qsm + (double)(qpi(i, k) * ((T)1. - omg));
+        T du = u(i, k) - u0, dv = v(i, k) - v0;
+        u2z = u2z + (double)(du * du);
+        v2z = v2z + (double)(dv * dv);
+        T w1 = w(i, k + 1), w0 = w(i, k);
+        w2z = w2z + (double)((T)0.5 * (w1 * w1 + w0 * w0));
+        stke = stke + (double)tke(i, k);
+        stk = stk + (double)tk(i, k);
+      }
+      O2(CRM_OUT_QC_MEAN, l) = qcm * factor_xy;
+      O2(CRM_OUT_QI_MEAN, l) = qim * factor_xy;
+      O2(CRM_OUT_QS_MEAN, l) = qsm * factor_xy;
+      O2(CRM_OUT_QG_MEAN, l) = qgm * factor_xy;
+      O2(CRM_OUT_QR_MEAN, l) = qrm * factor_xy;
+      double rhow = (double)PR(P_RHOW)[k], rho = (double)PR(P_RHO)[k];
+      double tmp1 = S.dz / rhow;
+      double tmp2 = tmp1 / S.dtn;
+      double ns = (double)p.nstop;
+      double mkwsb0 = (double)PR(P_MKWSB0)[k] * tmp1 * rhow * factor_xy / ns;
+      double mkwsb1 = (double)PR(P_MKWSB1)[k] * tmp1 * rhow * factor_xy / ns;
+      double mkwle0 = (double)PR(P_MKWLE0)[k] * tmp2 * rhow * factor_xy / ns;
+      double mkwle1 = (double)PR(P_MKWLE1)[k] * tmp2 * rhow * factor_xy / ns;
+      double mkadv0 = (double)PR(P_MKADV0)[k] * factor_xy * icrm_run_time;
+      double mkadv1 = (double)PR(P_MKADV1)[k] * factor_xy * icrm_run_time;
+      double mkdiff0 = (double)PR(P_MKDIFF0)[k] * factor_xy * icrm_run_time;
+      double mkdiff1 = (double)PR(P_MKDIFF1)[k] * factor_xy * icrm_run_time;
+      O2(CRM_OUT_FLUX_U, l) = ((double)PR(P_UWLE)[k] + (double)PR(P_UWSB)[k]) * tmp1 * factor_xy / ns;
+      O2(CRM_OUT_FLUX_V, l) = ((double)PR(P_VWLE)[k] + (double)PR(P_VWSB)[k]) * tmp1 * factor_xy / ns;
+      O2(CRM_OUT_FLUX_QT, l) = mkwle0 + mkwsb0;
+      O2(CRM_OUT_FLUXSGS_QT, l) = mkwsb0;
+      O2(CRM_OUT_FLUX_QP, l) = mkwle1 + mkwsb1;
+      O2(CRM_OUT_QT_TRANS, l) = mkadv0 + mkdiff0;
+      O2(CRM_OUT_QP_TRANS, l) = mkadv1 + mkdiff1;
+      double tkesgsz = rho * stke * factor_xy;
+      O2(CRM_OUT_TKESGSZ, l) = tkesgsz;
+      O2(CRM_OUT_TKEZ, l) = rho * 0.5 * (u2z + v2z * 0.0 + w2z) * factor_xy + tkesgsz;
+      O2(CRM_OUT_TKZ, l) = stk * factor_xy;
+      O2(CRM_OUT_PRECFLUX, l) = ((double)PR(P_PRECFLUX)[k] * factor_xy * S.dz / p.dt / ns) / 1000.;
+      O2(CRM_OUT_QP_FALL, l) = (double)PR(P_QPFALL)[k] * factor_xy * icrm_run_time;
+      O2(CRM_OUT_QP_EVP, l) = (double)PR(P_QPEVP)[k] * factor_xy * icrm_run_time;
+      O2(CRM_OUT_QP_SRC, l) = (double)PR(P_QPSRC)[k] * factor_xy * icrm_run_time;
+      O2(CRM_OUT_QT_LS, l) = (double)PR(P_QTEND)[k];
+      O2(CRM_OUT_T_LS, l) = (double)PR(P_TTEND)[k];
+    }
+    // state and 4D outputs
+    for (int e = TID; e < nx * nzm; e += NT) {
+      int i = 1 + e % nx, k = 1 + e / nx;
+      size_t o = S4(i, k);
+      p.st[0][o] = (double)u(i, k);
+      p.st[1][o] = (double)v(i, k);
+      p.st[2][o] = (double)w(i, k);
+      p.st[3][o] = (double)tabs(i, k);
+      p.st[4][o] = (double)qt(i, k);
+      p.st[5][o] = (double)qp(i, k);
+      p.st[6][o] = (double)qn(i, k);
+      p.out[CRM_OUT_TK][o] = (double)tk(i, k);
+      p.out[CRM_OUT_TKH][o] = (double)tkh(i, k);
+      p.out[CRM_OUT_QCL][o] = (double)qcl(i, k);
+      p.out[CRM_OUT_QCI][o] = (double)qci(i, k);
+      p.out[CRM_OUT_QPL][o] = (double)qpl(i, k);
+      p.out[CRM_OUT_QPI][o] = (double)qpi(i, k);
+    }
+    // scalars (thread 0): column precipitation, surface precip, cloud cover
+    if (TID == 0) {
+      double cp = 0, cps = 0;
+      for (int k = 1; k <= nzm; ++k) {
+        double pdel = IN(p.pdel, plev - k + 1);
+        for (int i = 1; i <= nx; ++i) {
+          cp = cp + (double)(qpl(i, k) + qpi(i, k)) * pdel;
+          cps = cps + (double)qpi(i, k) * pdel;
+        }
+      }
+      O1(CRM_OUT_PRECTEND) = (cp - S.colprec0) / C_GGR * factor_xy * icrm_run_time;
+      O1(CRM_OUT_PRECSTEND) = (cps - S.colprecs0) / C_GGR * factor_xy * icrm_run_time;
+      O1(CRM_OUT_Z0M) = S.z0;
+      O1(CRM_OUT_TAUX) = 0.0 / (double)p.nstop;
+      O1(CRM_OUT_TAUY) = 0.0 / (double)p.nstop;
+      double precc = 0, precl = 0, precsc = 0, precsl = 0;
+      const double thr = (double)(10.f / 86400.f);
+      for (int i = 1; i <= nx; ++i) {
+        double ps = (double)PS(i) * S.dz / p.dt / (double)p.nstop;
+        double pss = (double)PSS(i) * S.dz / p.dt / (double)p.nstop;
+        if (ps > thr) { precc = precc + ps; precsc = precsc + pss; }
+        else { precl = precl + ps; precsl = precsl + pss; }
+        p.out[CRM_OUT_PREC_CRM][(size_t)icrm + (size_t)ld * (i - 1)] = ps / 1000.;
+      }
+      O1(CRM_OUT_PRECC) = precc * factor_xy / 1000.;
+      O1(CRM_OUT_PRECL) = precl * factor_xy / 1000.;
+      O1(CRM_OUT_PRECSC) = precsc * factor_xy / 1000.;
+      O1(CRM_OUT_PRECSL) = precsl * factor_xy / 1000.;
+      O1(CRM_OUT_CLTOT) = S.cltot * factor_xyt;
+      O1(CRM_OUT_CLHGH) = S.clhgh * factor_xyt;
+      O1(CRM_OUT_CLMED) = S.clmed * factor_xyt;
+      O1(CRM_OUT_CLLOW) = S.cllow * factor_xyt;
+      int jt = S.jt_min, mx = S.mx_max;
+      O1(CRM_OUT_JT_CRM) = (jt <= plev) ? mn2((double)plev, (double)jt) : (double)plev;
+      O1(CRM_OUT_MX_CRM) = mx2(1.0, (double)mx);
+      O1(CRM_OUT_TIMING_FACTOR) = (double)p.nstop / (double)p.nstop;
+      p.col_status[icrm] = S.status;
+    }
+    SYNC;
+  }
+
+  // ---------------------------------------------------------- one column
+  __device__ void run() {
+    init_column();
+    if (TID == 0) { S.jt_min = 1 << 30; S.mx_max = 0; }
+    for (int nstep = 1; nstep <= p.nstop; ++nstep) {
+      kurant();
+      if (S.ncycle > 16) {
+        if (TID == 0) S.status = CRM_ERR_CFL;
+        SYNC;
+        break;
+      }
+      const int ncycle = S.ncycle;
+      for (int icyc = 1; icyc <= ncycle; ++icyc) {
+        if (TID == 0) {
+          S.icycle = icyc;
+          S.dtn = p.dt / ncycle;
+          S.dt3[S.na - 1] = S.dtn;
+          S.dtfactor = S.dtn / p.dt;
+          abcoefs(nstep);
+        }
+        SYNC;
+        zero_and_buoyancy();
+        forcing_radiation();
+        damping();
+        ice_fall();
+        boundaries(3);
+        boundaries(0);
+        tke_full();
+        boundaries(4);
+        advect_mom();
+        diffuse_mom();
+        pressure();
+        adams();
+        boundaries(2);
+        advect_scalar(TT(), nullptr, nullptr);
+        advect_scalar(QT(), PR(P_MKADV0), PR(P_MKWLE0));
+        advect_scalar(QP(), PR(P_MKADV1), PR(P_MKWLE1));
+        precip_fall_1();
+        precip_fall_2(S.nprec);
+        uvw();
+        boundaries(3);
+        diffuse_scalar(TT(), nullptr, nullptr);
+        diffuse_scalar(QT(), PR(P_MKDIFF0), PR(P_MKWSB0));
+        diffuse_scalar(QP(), PR(P_MKDIFF1), PR(P_MKWSB1));
+        if (S.icycle == 1) precip_init();
+        cloud();
+        precip_proc();
+        micro_diagnose();
+        diagnose();
+        if (TID == 0) { int nn = S.na; S.na = S.nc; S.nc = S.nb; S.nb = nn; }
+        SYNC;
+      }
+      step_stats();
+    }
+    finalize();
+  }
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) crm_columns_kernel(const __grid_constant__ KParams p) {
+  __shared__ ColShared S;
+  T *base = reinterpret_cast<T *>(p.slabs) + (size_t)blockIdx.x * p.L.slab;
+  for (int col = blockIdx.x; col < p.ncrms; col += gridDim.x) {
+    ColumnKernel<T> K(p, S, base, col);
+    K.run();
+    __syncthreads();
+  }
+}
+
+template <typename T>
+void launch_crm_columns(const KParams &p, int grid, int block, cudaStream_t s) {
+  crm_columns_kernel<T><<<grid, block, 0, s>>>(p);
+}
+
+template <typename T>
+int occupancy_crm_columns(int block) {
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, crm_columns_kernel<T>, block, 0) != cudaSuccess) return 0;
+  return n;
+}
+
+}  // namespace crm

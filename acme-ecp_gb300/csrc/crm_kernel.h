@@ -1,0 +1,39 @@
+// crm_kernel.h -- parameters of the column kernel (host <-> device).
+#pragma once
+#include "crm_layout.h"
+#include "../../include/crm_gb300.h"
+
+namespace crm {
+
+struct KParams {
+  Layout L;
+  int ncrms, ld, nstop, igstep, batch_mode, clamp_batch;
+  double dx, dy, dt, dt_gl;
+  // per-call constants computed on the host (gamma functions, fall speeds)
+  double gams1, gams2, gamg1, gamg2, gamr1, gamr2;
+  double vrain, vsnow, vgrau, crain, csnow, cgrau;
+  double a_bg, a_pr, a_gr;
+  int nfax;
+  int ifax[8];
+  const double *trigs;      // fft trig table (3n/2 + 2 + n), REAL*4 values
+  const double *eign;       // (nx + 1) eigenvalues of the horizontal Laplacian
+  const double *z0;         // (ncrms) roughness length
+  const double *rnd;        // (ncrms, 5, nx) setperturb draws 1 - 2 r
+  // crm_input (device, Fortran (ld, *) order)
+  const double *zmid, *zint, *tl, *ql, *qccl, *qiil, *pmid, *pint, *pdel, *ul, *vl;
+  // crm_state in/out (ld, nx, 1, nz): u, v, w, T, qt, qp, qn
+  double *st[7];
+  const double *qrad;       // (ld, nx_rad, 1, nz)
+  double *radout[5];        // temperature, qv, qc, qi, cld
+  double *out[CRM_NOUT];
+  void *slabs;              // gridDim.x slabs of L.slab elements of T
+  int *col_status;          // (ncrms)
+  int *next_col;            // dynamic column counter (zeroed before launch)
+};
+
+template <typename T>
+void launch_crm_columns(const KParams &p, int grid, int block, cudaStream_t s);
+template <typename T>
+int occupancy_crm_columns(int block);
+
+}  // namespace crm

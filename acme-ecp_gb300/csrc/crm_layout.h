@@ -1,0 +1,116 @@
+// crm_layout.h -- per-column slab layout shared by host and device code.
+//
+// The device keeps each CRM column's fields in one contiguous slab (x fastest,
+// then k), so the CTA that owns the column touches one compact block of
+// memory that stays resident in L1/L2 across the whole GCM step.  Index
+// ranges (halos included) are those of the reference's module arrays
+// (crm/grid.F90:31-46 with NADV = NADVS = 0, crm/vars.F90:200-238,
+// SGS_TKE/sgs.F90:50-60).  2D (ny = 1) only.
+#pragma once
+#include <cstddef>
+
+namespace crm {
+
+// x extents (first index, length) of the field classes
+struct XRange {
+  int x1, nxa;
+};
+
+struct Layout {
+  int nx, nzm, nz, plev, nx_rad;
+  // x ranges
+  XRange xu, xv, xw, xs, xd, xp, xi, xdu;
+  // offsets (in elements) of every array inside one column slab
+  size_t u, v, w, t, qt, qp, tke, tk, tkh, p, tabs, qv, qcl, qci, qpl, qpi, qn;
+  size_t du[3], dv[3], dw[3];
+  size_t precsfc, precssfc;
+  // scratch (per phase)
+  size_t s_a, s_b, s_c, s_d, s_e, s_f, s_g, s_h;   // nxs x (nz+1) each
+  size_t fft_f, fft_w;                             // (nx+2) x nzm, work
+  // profiles: each (nz + 2) long, indexed directly by k (0 .. nz+1)
+  size_t prof;           // first profile
+  int nprof;             // number of profiles
+  size_t o_plev;         // GCM-level accumulators, (plev + 2) each
+  int n_oplev;
+  size_t rad;            // rad accumulators 5 x (nx_rad x nzm) + qrad
+  size_t rnd;            // setperturb random numbers 5 x nx
+  size_t colstat;        // per-column scratch for step statistics, 8 x nx
+  size_t slab;           // total elements per column
+};
+
+// profile indices (each profile is (nz+2) long, indexed by k)
+enum Prof {
+  P_Z, P_ZI, P_PRES, P_PRESI, P_ADZ, P_ADZW, P_RHO, P_RHOW, P_BET, P_GAMAZ,
+  P_T0, P_Q0, P_QV0, P_TABS0, P_U0, P_V0, P_QP0, P_QN0, P_T00,
+  P_TTEND, P_QTEND, P_UTEND, P_VTEND,
+  P_GRDFX, P_GRDFY, P_GRDFZ,
+  P_ACCRSC, P_ACCRSI, P_ACCRRC, P_COEFICE, P_ACCRGC, P_ACCRGI,
+  P_EVAPS1, P_EVAPS2, P_EVAPR1, P_EVAPR2, P_EVAPG1, P_EVAPG2,
+  P_UWLE, P_VWLE, P_UWSB, P_VWSB, P_PRECFLUX, P_QPFALL, P_TLAT, P_TLATQI, P_QIFALL,
+  P_MKWLE0, P_MKWLE1, P_MKWSB0, P_MKWSB1, P_MKADV0, P_MKADV1, P_MKDIFF0, P_MKDIFF1,
+  P_QPSRC, P_QPEVP,
+  P_TMP0, P_TMP1, P_TMP2, P_TMP3, P_TMP4, P_TMP5, P_TMP6, P_TMP7,
+  P_COUNT
+};
+
+// GCM-level accumulators (plev + 2 each, indexed by l)
+enum OPlev {
+  O_CLD, O_CLDTOP, O_GICEWP, O_GLIQWP, O_MCUP, O_MCDN, O_MCUUP, O_MCUDN, O_MUI, O_MDI,
+  O_COUNT
+};
+
+inline Layout make_layout(int nx, int nzm, int plev, int nx_rad) {
+  Layout L{};
+  L.nx = nx; L.nzm = nzm; L.nz = nzm + 1; L.plev = plev; L.nx_rad = nx_rad;
+  L.xu = {-1, nx + 5};
+  L.xv = {-1, nx + 4};
+  L.xw = {-1, nx + 4};
+  L.xs = {-2, nx + 6};
+  L.xd = {0, nx + 2};
+  L.xp = {0, nx + 1};
+  L.xi = {1, nx};
+  L.xdu = {1, nx + 1};
+  size_t o = 0;
+  auto take = [&](size_t n) { size_t r = o; o += (n + 31) / 32 * 32; return r; };
+  const int nz = L.nz;
+  L.u = take((size_t)L.xu.nxa * nzm);
+  L.v = take((size_t)L.xv.nxa * nzm);
+  L.w = take((size_t)L.xw.nxa * nz);
+  L.t = take((size_t)L.xs.nxa * nzm);
+  L.qt = take((size_t)L.xs.nxa * nzm);
+  L.qp = take((size_t)L.xs.nxa * nzm);
+  L.tke = take((size_t)L.xi.nxa * nzm);
+  L.tk = take((size_t)L.xd.nxa * nzm);
+  L.tkh = take((size_t)L.xd.nxa * nzm);
+  L.p = take((size_t)L.xp.nxa * nzm);
+  L.tabs = take((size_t)nx * nzm);
+  L.qv = take((size_t)nx * nzm);
+  L.qcl = take((size_t)nx * nzm);
+  L.qci = take((size_t)nx * nzm);
+  L.qpl = take((size_t)nx * nzm);
+  L.qpi = take((size_t)nx * nzm);
+  L.qn = take((size_t)nx * nzm);
+  for (int l = 0; l < 3; ++l) {
+    L.du[l] = take((size_t)L.xdu.nxa * nzm);
+    L.dv[l] = take((size_t)nx * nzm);
+    L.dw[l] = take((size_t)nx * nz);
+  }
+  L.precsfc = take(nx);
+  L.precssfc = take(nx);
+  const size_t sc = (size_t)(nx + 6) * (nz + 1);
+  L.s_a = take(sc); L.s_b = take(sc); L.s_c = take(sc); L.s_d = take(sc);
+  L.s_e = take(sc); L.s_f = take(sc); L.s_g = take(sc); L.s_h = take(sc);
+  L.fft_f = take((size_t)(nx + 2) * (nzm + 1));
+  L.fft_w = take((size_t)(nx + 4) * (nzm + 1));
+  L.nprof = P_COUNT;
+  L.prof = take((size_t)(nz + 2) * P_COUNT);
+  L.n_oplev = O_COUNT;
+  L.o_plev = take((size_t)(plev + 2) * O_COUNT);
+  L.rad = take((size_t)6 * nx_rad * nzm);
+  L.rnd = take((size_t)5 * nx);
+  L.colstat = take((size_t)8 * nx);
+  L.slab = o;
+  return L;
+}
+
+}  // namespace crm

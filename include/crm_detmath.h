@@ -1,0 +1,155 @@
+/*
+ * crm_detmath.h -- deterministic double-precision exp, log and pow.
+ *
+ * The CRM calls exp, log and ** (pow) on the hot path: precip_init.F90:54-91
+ * (per level and step), precip_proc.F90:75-125 and microphysics.F90:453-486
+ * (per cell), ice_fall.F90:108, damping.F90:58, sat.F90:30,93 (below -80 C).
+ * CUDA's libdevice and glibc's libm round these differently in the last bit,
+ * and a one-ulp difference in a cell feeds the chaotic CRM integration.  To
+ * make the FP64 device form bit-identical to a CPU run of the same
+ * algorithm, both sides evaluate these three functions with the code below,
+ * built only from IEEE-754 +, -, *, / (correctly rounded on both sides when
+ * floating-point contraction is off: nvcc -fmad=false, gcc -ffp-contract=off).
+ *
+ * Methods (textbook, not taken from any vendor library):
+ *  - exp: Cody-Waite reduction x = n*ln2 + r, |r| <= ln2/2, with ln2 split
+ *    into a 32-bit head and a tail so n*ln2_head is exact; e^r from its
+ *    Taylor series to degree 13 (truncation < 4e-18 relative) by Horner's
+ *    rule; scaling by 2^n through the exponent field.
+ *  - log: x = 2^e * m with m in [sqrt(1/2), sqrt(2)); f = m - 1,
+ *    s = f/(2+f), log(m) = 2 atanh(s) = f - (f^2/2 - s*(f^2/2 + R)) with
+ *    R = sum_{k=1..12} 2 s^(2k)/(2k+1) (truncation < 1e-19).
+ *  - pow(x, y) = exp(y * log(x)) for x > 0; pow(0, y>0) = 0.
+ * Accuracy on the CRM's arguments is checked against the platform libm in
+ * tests/test_detmath.py (exp/log <= 2 ulp, pow <= 16 ulp).
+ */
+#ifndef CRM_DETMATH_H
+#define CRM_DETMATH_H
+
+#if defined(__CUDACC__)
+#define CRM_DM_FN __host__ __device__ __forceinline__
+#else
+#define CRM_DM_FN static inline
+#include <string.h>
+#endif
+
+#ifdef __cplusplus
+namespace crm_detmath {
+#endif
+
+CRM_DM_FN double dm_from_bits(long long b) {
+#if defined(__CUDA_ARCH__)
+  return __longlong_as_double(b);
+#else
+  double d;
+  memcpy(&d, &b, sizeof d);
+  return d;
+#endif
+}
+
+CRM_DM_FN long long dm_to_bits(double d) {
+#if defined(__CUDA_ARCH__)
+  return __double_as_longlong(d);
+#else
+  long long b;
+  memcpy(&b, &d, sizeof b);
+  return b;
+#endif
+}
+
+/* ln 2 = DM_LN2_HI + DM_LN2_LO; the head has 32 trailing zero bits. */
+#define DM_LN2_HI 6.93147180369123816490e-01
+#define DM_LN2_LO 1.90821492927058770002e-10
+#define DM_INV_LN2 1.44269504088896338700e+00
+
+/* 2^n for -1022 <= n <= 1023 */
+CRM_DM_FN double dm_pow2i(int n) {
+  return dm_from_bits((long long)(n + 1023) << 52);
+}
+
+CRM_DM_FN double det_exp(double x) {
+  if (x != x) return x;                     /* NaN */
+  if (x > 709.0) return dm_from_bits(0x7ff0000000000000LL);
+  if (x < -744.0) return 0.0;
+  double fn = x * DM_INV_LN2 + 0.5;
+#if defined(__CUDA_ARCH__)
+  fn = floor(fn);
+#else
+  fn = __builtin_floor(fn);
+#endif
+  int n = (int)fn;
+  double r = (x - fn * DM_LN2_HI) - fn * DM_LN2_LO;
+  /* Taylor coefficients 1/k!, k = 13 .. 0 */
+  double p = 1.6059043836821614599e-10;   /* 1/13! */
+  p = p * r + 2.0876756987868098979e-09;  /* 1/12! */
+  p = p * r + 2.5052108385441718775e-08;  /* 1/11! */
+  p = p * r + 2.7557319223985890653e-07;  /* 1/10! */
+  p = p * r + 2.7557319223985892511e-06;  /* 1/9!  */
+  p = p * r + 2.4801587301587301566e-05;  /* 1/8!  */
+  p = p * r + 1.9841269841269841253e-04;  /* 1/7!  */
+  p = p * r + 1.3888888888888889419e-03;  /* 1/6!  */
+  p = p * r + 8.3333333333333332177e-03;  /* 1/5!  */
+  p = p * r + 4.1666666666666664354e-02;  /* 1/4!  */
+  p = p * r + 1.6666666666666665741e-01;  /* 1/3!  */
+  p = p * r + 0.5;
+  p = p * r + 1.0;
+  p = p * r + 1.0;
+  if (n < -1021) {                          /* gradual underflow */
+    return (p * dm_pow2i(n + 600)) * dm_pow2i(-600);
+  }
+  if (n > 1023) return (p * dm_pow2i(n - 600)) * dm_pow2i(600);
+  return p * dm_pow2i(n);
+}
+
+CRM_DM_FN double det_log(double x) {
+  if (x != x || x < 0.0) return dm_from_bits(0x7ff8000000000000LL);
+  if (x == 0.0) return -dm_from_bits(0x7ff0000000000000LL);
+  long long b = dm_to_bits(x);
+  int e = 0;
+  if ((b >> 52) == 0) {                     /* subnormal: scale by 2^54 */
+    x = x * 18014398509481984.0;
+    b = dm_to_bits(x);
+    e = -54;
+  }
+  if ((b >> 52) >= 0x7ff) return x;         /* +Inf */
+  e += (int)((b >> 52) & 0x7ff) - 1023;
+  b = (b & 0x000fffffffffffffLL) | 0x3ff0000000000000LL;   /* m in [1,2) */
+  double m = dm_from_bits(b);
+  if (m > 1.4142135623730951) {
+    m = m * 0.5;
+    e += 1;
+  }
+  double f = m - 1.0;
+  double s = f / (2.0 + f);
+  double z = s * s;
+  /* R = sum_{k=1}^{12} 2 z^k / (2k+1) by Horner */
+  double R = 8.0000000000000004441e-02;     /* 2/25 */
+  R = R * z + 8.6956521739130432160e-02;    /* 2/23 */
+  R = R * z + 9.5238095238095232808e-02;    /* 2/21 */
+  R = R * z + 1.0526315789473683626e-01;    /* 2/19 */
+  R = R * z + 1.1764705882352941013e-01;    /* 2/17 */
+  R = R * z + 1.3333333333333333148e-01;    /* 2/15 */
+  R = R * z + 1.5384615384615385469e-01;    /* 2/13 */
+  R = R * z + 1.8181818181818182323e-01;    /* 2/11 */
+  R = R * z + 2.2222222222222220989e-01;    /* 2/9  */
+  R = R * z + 2.8571428571428569843e-01;    /* 2/7  */
+  R = R * z + 4.0000000000000002220e-01;    /* 2/5  */
+  R = R * z + 6.6666666666666662966e-01;    /* 2/3  */
+  R = R * z;
+  double hfsq = 0.5 * f * f;
+  double de = (double)e;
+  return de * DM_LN2_HI - ((hfsq - (s * (hfsq + R) + de * DM_LN2_LO)) - f);
+}
+
+CRM_DM_FN double det_pow(double x, double y) {
+  if (y == 0.0) return 1.0;
+  if (x == 0.0) return y > 0.0 ? 0.0 : dm_from_bits(0x7ff0000000000000LL);
+  if (x < 0.0 || x != x || y != y) return dm_from_bits(0x7ff8000000000000LL);
+  if (x == 1.0) return 1.0;
+  return det_exp(y * det_log(x));
+}
+
+#ifdef __cplusplus
+} /* namespace crm_detmath */
+#endif
+#endif /* CRM_DETMATH_H */

@@ -1,0 +1,173 @@
+/*
+ * crm_gb300.h -- C ABI of the GB300-native superparameterized CRM step.
+ *
+ * One call advances ncrms embedded 2D cloud-resolving models (one per GCM
+ * column) over one GCM timestep dt_gl, exactly like the Fortran entry
+ *
+ *   subroutine crm(lchnk, icol, ncrms, dt_gl, plev, crm_input, crm_state,
+ *                  crm_rad, crm_ecpp_output, crm_output)
+ *
+ * in components/cam/src/physics/crm/crm_module.F90:45-56 (default build:
+ * sam1mom microphysics, SGS_TKE closure, MPDATA scalar advection, no CLUBB,
+ * no MAML, no ECPP), called from crm_physics_tend in
+ * components/cam/src/physics/cam/crm_physics.F90:1145-1156.
+ *
+ * Array convention: every array argument is a plain pointer to host memory
+ * laid out in Fortran (column-major) order with the CRM column index fastest,
+ * exactly as the derived types of the reference hold them:
+ *   (ld, plev)              crm_input_module.F90:10-47
+ *   (ld, nx, ny, nz)        crm_state_module.F90:12-56, crm_output_module.F90
+ *   (ld, nx_rad, ny_rad, nz) crm_rad_module.F90:17-34
+ * where ld (= pcols in CAM) >= ncrms and only columns 0..ncrms-1 are touched
+ * (crm_module.F90:268-281).  nz here is crm_nz (the number of CRM scalar
+ * levels, nzm in the reference grid module).
+ *
+ * Errors are returned, never raised: every entry point returns a crm_status
+ * and the per-column status array (optional) receives one code per column.
+ * The reference stops the model instead (endrun / task_abort), e.g.
+ * kurant.F90:66-75 when ncycle exceeds 16.
+ */
+#ifndef CRM_GB300_H
+#define CRM_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status */
+enum crm_status {
+  CRM_OK = 0,
+  CRM_ERR_ARG = 1,          /* bad argument / unsupported configuration     */
+  CRM_ERR_CFL = 2,          /* kurant(): ncycle > 16 (kurant.F90:66-75)     */
+  CRM_ERR_NONFINITE = 3,    /* a state field became NaN/Inf                  */
+  CRM_ERR_CUDA = 4,         /* CUDA runtime error                            */
+  CRM_ERR_UNSUPPORTED = 5,  /* feature not built (e.g. m2005)                */
+  CRM_ERR_TIMEOUT = 6,      /* a bounded device wait gave up                 */
+  CRM_ERR_BUDGET = 7,       /* serving admission: HBM budget exhausted       */
+  CRM_ERR_NO_DEVICE = 8     /* no CUDA device                                */
+};
+
+enum crm_microphysics { CRM_MICRO_SAM1MOM = 0, CRM_MICRO_M2005 = 1 };
+enum crm_precision { CRM_FP64 = 0, CRM_FP32_MIXED = 1 };
+/* Subcycle count ncycle (kurant.F90:54-64) and precipitation sub-steps nprec
+ * (MICRO_SAM1MOM/microphysics.F90:602-661) are batch maxima in the
+ * reference, and the first-step velocity clamp tests only the first column
+ * (crm_module.F90:400-417).  CRM_PER_COLUMN makes each column independent of
+ * its batch-mates; CRM_REFERENCE_BATCH reproduces the batch coupling. */
+enum crm_batch_mode { CRM_PER_COLUMN = 0, CRM_REFERENCE_BATCH = 1 };
+
+/* Compile-time CPP constants of the reference (bld/configure:1883-1914,
+ * crmdims.F90, domain.F90), passed at run time. */
+typedef struct crm_config {
+  int crm_nx, crm_ny, crm_nz;   /* CRM_NX, CRM_NY, CRM_NZ (ny == 1: 2D)  */
+  int crm_nx_rad, crm_ny_rad;   /* radiation column groups               */
+  int plev;                     /* GCM levels (pver)                     */
+  double crm_dx, crm_dy;        /* CRM_DX, CRM_DY [m]                    */
+  double crm_dt;                /* CRM_DT [s]                            */
+  int microphysics;             /* enum crm_microphysics                 */
+  int precision;                /* enum crm_precision                    */
+  int batch_mode;               /* enum crm_batch_mode                   */
+  int max_ncrms;                /* largest ncrms a handle will be given  */
+} crm_config;
+
+/* crm_input_type (crm_input_module.F90:10-47); (ld, plev) unless noted. */
+typedef struct crm_input_c {
+  const double *zmid, *zint;    /* zint: (ld, plev+1)                    */
+  const double *tl, *ql, *qccl, *qiil;
+  const double *ps;             /* (ld)                                  */
+  const double *pmid, *pint, *pdel;  /* pint: (ld, plev+1)               */
+  const double *phis;           /* (ld)                                  */
+  const double *ul, *vl;
+  const double *ocnfrac, *tau00, *wndls, *bflxls;   /* (ld)              */
+  const double *fluxu00, *fluxv00, *fluxt00, *fluxq00; /* (ld)           */
+} crm_input_c;
+
+/* crm_state_type (crm_state_module.F90:12-56): (ld, nx, ny, nz), in/out. */
+typedef struct crm_state_c {
+  double *u_wind, *v_wind, *w_wind, *temperature;
+  double *qt, *qp, *qn;          /* sam1mom prognostics                   */
+} crm_state_c;
+
+/* crm_rad_type (crm_rad_module.F90:17-34): (ld, nx_rad, ny_rad, nz).
+ * qrad is read; the others are written (time means over the call). */
+typedef struct crm_rad_c {
+  double *qrad, *temperature, *qv, *qc, *qi, *cld;
+} crm_rad_c;
+
+/* crm_output_type (crm_output_module.F90:7-133), sam1mom subset.  Shapes:
+ * 4D = (ld,nx,ny,nz), 3D = (ld,nx,ny), 2D = (ld,plev), 1D = (ld). */
+enum crm_output_field {
+  /* 4D */
+  CRM_OUT_QCL, CRM_OUT_QCI, CRM_OUT_QPL, CRM_OUT_QPI, CRM_OUT_TK, CRM_OUT_TKH,
+  /* 3D */
+  CRM_OUT_PREC_CRM,
+  /* 1D */
+  CRM_OUT_CLTOT, CRM_OUT_CLHGH, CRM_OUT_CLMED, CRM_OUT_CLLOW,
+  CRM_OUT_PRECC, CRM_OUT_PRECL, CRM_OUT_PRECSC, CRM_OUT_PRECSL,
+  CRM_OUT_JT_CRM, CRM_OUT_MX_CRM, CRM_OUT_PRECTEND, CRM_OUT_PRECSTEND,
+  CRM_OUT_TAUX, CRM_OUT_TAUY, CRM_OUT_Z0M, CRM_OUT_TIMING_FACTOR,
+  /* 2D */
+  CRM_OUT_CLDTOP, CRM_OUT_QC_MEAN, CRM_OUT_QI_MEAN, CRM_OUT_QS_MEAN,
+  CRM_OUT_QG_MEAN, CRM_OUT_QR_MEAN,
+  CRM_OUT_SLTEND, CRM_OUT_QLTEND, CRM_OUT_QCLTEND, CRM_OUT_QILTEND,
+  CRM_OUT_CLD, CRM_OUT_GICEWP, CRM_OUT_GLIQWP, CRM_OUT_MCTOT, CRM_OUT_MCUP,
+  CRM_OUT_MCDN, CRM_OUT_MCUUP, CRM_OUT_MCUDN, CRM_OUT_MU_CRM, CRM_OUT_MD_CRM,
+  CRM_OUT_DU_CRM, CRM_OUT_EU_CRM, CRM_OUT_ED_CRM,
+  CRM_OUT_FLUX_QT, CRM_OUT_FLUXSGS_QT, CRM_OUT_TKEZ, CRM_OUT_TKESGSZ,
+  CRM_OUT_TKZ, CRM_OUT_FLUX_U, CRM_OUT_FLUX_V, CRM_OUT_FLUX_QP,
+  CRM_OUT_PRECFLUX, CRM_OUT_QT_LS, CRM_OUT_QT_TRANS, CRM_OUT_QP_TRANS,
+  CRM_OUT_QP_FALL, CRM_OUT_QP_SRC, CRM_OUT_QP_EVP, CRM_OUT_T_LS,
+  CRM_NOUT
+};
+#define CRM_OUT_FIRST_3D CRM_OUT_PREC_CRM
+#define CRM_OUT_FIRST_1D CRM_OUT_CLTOT
+#define CRM_OUT_FIRST_2D CRM_OUT_CLDTOP
+
+typedef struct crm_output_c {
+  double *field[CRM_NOUT];      /* indexed by enum crm_output_field      */
+} crm_output_c;
+
+/* Hidden inputs of crm() made explicit (crm_module.F90:33,286-291,679):
+ * get_gcol_p (random seed = gcol*1000), get_nstep (setperturb when
+ * igstep <= 1), get_rlat_p/get_rlon_p (only feed the Coriolis terms, which
+ * are off: docoriolis = .false.). */
+typedef struct crm_call_desc {
+  int lchnk;
+  int ncrms;                    /* columns in this call                  */
+  int ld;                       /* leading dimension (pcols) of arrays   */
+  double dt_gl;                 /* GCM timestep [s]                      */
+  int igstep;                   /* GCM step number (get_nstep())        */
+  const int *gcol;              /* (ncrms) global column ids             */
+} crm_call_desc;
+
+typedef struct crm_ctx crm_ctx;
+
+/* Create a handle for one (nx, ny, nz, dx, dt, microphysics, precision)
+ * configuration on the current CUDA device.  Replaces the CPP build-time
+ * specialisation (crmdims.F90) and the per-call allocate_* of the module
+ * globals (crm_module.F90:199-266).  Returns NULL and sets *status on error. */
+crm_ctx *crm_create(const crm_config *cfg, int *status);
+void crm_destroy(crm_ctx *ctx);
+
+/* The drop-in for subroutine crm() (crm_module.F90:45-1718): host arrays in,
+ * host arrays out; state and rad updated in place.  col_status (ncrms, may be
+ * NULL) receives a crm_status per column.  Synchronous. */
+int crm_run(crm_ctx *ctx, const crm_call_desc *desc, const crm_input_c *in,
+            crm_state_c *state, crm_rad_c *rad, crm_output_c *out,
+            int *col_status);
+
+/* Number of kernel launches issued by the last crm_run on this handle. */
+int crm_last_launch_count(const crm_ctx *ctx);
+/* Duration of the compute kernels of the last crm_run [ms] (CUDA events on
+ * the handle's stream), excluding host<->device copies. */
+double crm_last_kernel_ms(const crm_ctx *ctx);
+/* Bind the handle to a CUDA stream (cudaStream_t passed as void*). */
+int crm_set_stream(crm_ctx *ctx, void *stream);
+const char *crm_status_string(int status);
+/* Library version string. */
+const char *crm_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CRM_GB300_H */
