@@ -1,8 +1,9 @@
 """Build libcrm_gb300.so (sm_103a) in-tree with nvcc.
 
-Three translation units, compiled in parallel:
+Four translation units, compiled in parallel:
   crm_fp64.cu  FP64 column kernel, -fmad=false (bit-identical to a CPU run)
   crm_fp32.cu  FP32-mixed column kernel
+  crm_prep.cu  per-column set-up kernel (z0, setperturb draws), -fmad=false
   crm_host.cu  the C ABI (include/crm_gb300.h), host code built with
                -ffp-contract=off for the same reason
 """
@@ -24,6 +25,7 @@ COMMON = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC,-ffp-contract=o
 UNITS = {
     'crm_fp64': ['-fmad=false'],
     'crm_fp32': [],
+    'crm_prep': ['-fmad=false'],
     'crm_host': [],
 }
 

@@ -14,7 +14,7 @@ from . import types as T
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, 'libcrm_gb300.so')
 
-EXPORTS = ('crm_create', 'crm_destroy', 'crm_run', 'crm_last_launch_count',
+EXPORTS = ('crm_create', 'crm_destroy', 'crm_run', 'crm_run_device', 'crm_last_launch_count',
            'crm_last_kernel_ms', 'crm_set_stream', 'crm_status_string', 'crm_version')
 
 _lib = None
@@ -46,6 +46,10 @@ def load(path=None, build_if_missing=False):
     lib.crm_run.argtypes = [C.c_void_p, C.POINTER(T.CCrmCallDesc), C.POINTER(T.CCrmInput),
                             C.POINTER(T.CCrmState), C.POINTER(T.CCrmRad), C.POINTER(T.CCrmOutput),
                             C.POINTER(C.c_int)]
+    lib.crm_run_device.restype = C.c_int
+    lib.crm_run_device.argtypes = [C.c_void_p, C.POINTER(T.CCrmCallDesc), C.POINTER(T.CCrmInput),
+                                   C.POINTER(T.CCrmState), C.POINTER(T.CCrmRad),
+                                   C.POINTER(T.CCrmOutput), C.c_void_p, C.c_void_p]
     lib.crm_last_launch_count.restype = C.c_int
     lib.crm_last_launch_count.argtypes = [C.c_void_p]
     lib.crm_last_kernel_ms.restype = C.c_double
@@ -106,6 +110,15 @@ class CrmContext:
         if raise_on_error and rc != T.CRM_OK:
             raise CrmError(rc, 'crm_run')
         return status
+
+    def run_device(self, dev, stream=0):
+        """crm_run_device on a DeviceCrmArrays bundle (asynchronous)."""
+        rc = self._lib.crm_run_device(self._h, C.byref(dev.c_desc), C.byref(dev.c_in),
+                                      C.byref(dev.c_state), C.byref(dev.c_rad),
+                                      C.byref(dev.c_out), C.c_void_p(dev.status_ptr),
+                                      C.c_void_p(stream))
+        if rc != T.CRM_OK:
+            raise CrmError(rc, 'crm_run_device')
 
     @property
     def last_kernel_ms(self):

@@ -82,13 +82,18 @@ def sounding(plev, t_sfc, u_top=10.0, v_top=0.0, ps=1.0e5):
 
 
 def make_inputs(cfg: CrmConfig, ncrms, t_sfc, shf, lhf, dt_gl=1200.0, seed=0,
-                u_top=10.0, v_top=0.0, ld=None, gcol0=1):
+                u_top=10.0, v_top=0.0, ld=None, gcol0=1, moist=False):
     """Build (crm_input, crm_state, crm_rad, desc) for ncrms columns.
 
     t_sfc, shf, lhf: scalars or arrays of length ncrms.  Column c uses
     numpy PCG64(seed + c) for its +-0.1 K state perturbation and the
     reference's own setperturb (seed gcol*1000, gcol = gcol0 + c) runs
     inside crm() because igstep = 1.
+
+    moist=True makes a test state that exercises every microphysics branch
+    from the first step: total water 3 % above saturation between 1 and
+    4 km and between 7 and 9 km (liquid and ice cloud), precipitation
+    1e-3 kg/kg between 2 and 5 km, and GCM cloud water/ice inputs.
     """
     ld = ld or ncrms
     plev, nx, ny, nz = cfg.plev, cfg.crm_nx, cfg.crm_ny, cfg.crm_nz
@@ -110,6 +115,15 @@ def make_inputs(cfg: CrmConfig, ncrms, t_sfc, shf, lhf, dt_gl=1200.0, seed=0,
             rad.qrad[c, :, :, k] = -1.5 / 86400.0 if s['zmid'][m] < 12000.0 else 0.0
         rng = np.random.Generator(np.random.PCG64(seed + c))
         st.temperature[c, :, :, :4] += rng.uniform(-0.1, 0.1, size=(nx, ny, 4))
+        if moist:
+            for k in range(nz):
+                m = plev - 1 - k
+                z = s['zmid'][m]
+                qs = qsatw(s['t'][m], s['pmid'][m] / 100.0)
+                if 1000.0 < z < 4000.0 or 7000.0 < z < 9000.0:
+                    st.qt[c, :, :, k] = 1.03 * qs * (1.0 + 0.02 * rng.uniform(-1, 1, size=(nx, ny)))
+                if 2000.0 < z < 5000.0:
+                    st.qp[c, :, :, k] = 1.0e-3 * rng.uniform(0.5, 1.0, size=(nx, ny))
         # surface fluxes applied to the lowest GCM layer over one GCM step
         t = s['t'].copy()
         q = s['q'].copy()
@@ -120,6 +134,9 @@ def make_inputs(cfg: CrmConfig, ncrms, t_sfc, shf, lhf, dt_gl=1200.0, seed=0,
         cin.zint[c] = s['zint']
         cin.tl[c] = t
         cin.ql[c] = q
+        if moist:
+            cin.qccl[c] = np.where((s['zmid'] > 1000.0) & (s['zmid'] < 4000.0), 2.0e-5, 0.0)
+            cin.qiil[c] = np.where((s['zmid'] > 7000.0) & (s['zmid'] < 9000.0), 1.0e-5, 0.0)
         cin.ps[c] = s['ps']
         cin.pmid[c] = s['pmid']
         cin.pint[c] = s['pint']
@@ -147,17 +164,17 @@ def config1(precision=0, batch_mode=0, nx=64):
                      crm_dt=10.0, precision=precision, batch_mode=batch_mode)
 
 
-def workload0(ncrms=16, seed=0, **kw):
+def workload0(ncrms=16, seed=0, moist=False, **kw):
     """16 columns, T_sfc 300 K, SHF 10 W/m2, LHF 100 W/m2."""
     cfg = config0(**kw)
-    return (cfg,) + make_inputs(cfg, ncrms, 300.0, 10.0, 100.0, seed=seed)
+    return (cfg,) + make_inputs(cfg, ncrms, 300.0, 10.0, 100.0, seed=seed, moist=moist)
 
 
-def workload1(ncrms=1024, seed=0, nx=64, **kw):
+def workload1(ncrms=1024, seed=0, nx=64, moist=False, **kw):
     """lat ~ U[-60, 60] deg (seeded), T_sfc = 271 + 29 cos(lat), fluxes * cos(lat)."""
     cfg = config1(nx=nx, **kw)
     rng = np.random.Generator(np.random.PCG64(10_000 + seed))
     lat = rng.uniform(-60.0, 60.0, size=ncrms)
     cl = np.cos(np.deg2rad(lat))
     return (cfg,) + make_inputs(cfg, ncrms, 271.0 + 29.0 * cl, 10.0 * cl,
-                                100.0 * cl, seed=seed)
+                                100.0 * cl, seed=seed, moist=moist)

@@ -1,20 +1,18 @@
 // crm_host.cu -- the C ABI of include/crm_gb300.h: the drop-in for the
 // reference's subroutine crm() (crm/crm_module.F90:45-1718).
 //
-// Host work per call, as in the reference (whose grid setup and setperturb
-// also run on the host, crm_module.F90:320-375,677-681): the per-call
-// constants (FFT factors and REAL*4 trig tables, fft.F90:156-300; Laplacian
-// eigenvalues, pressure.F90:172-198; gamma functions, gammafff.c; fall-speed
-// coefficients, microphysics.F90:500-507), the roughness length z0
-// (crmsurface.F90:104-133) and the random draws of setperturb
-// (setperturb.F90:33-80, cam/RNG_MT.F90:52-142).  Everything else runs in
-// one launch of the persistent column kernel.
+// Host work, once per handle: the per-configuration constants (FFT factors
+// and REAL*4 trig tables, fft.F90:156-300; Laplacian eigenvalues,
+// pressure.F90:172-198; gamma functions, gammafff.c; fall-speed
+// coefficients, microphysics.F90:500-507).  Per call two kernels run: the
+// per-column set-up (z0 and the setperturb draws, crm_prep.cu) and the
+// persistent column kernel (crm_kernel.cuh).  crm_run stages host arrays
+// through the handle's device buffers; crm_run_device takes device arrays.
 #include <cuda_runtime.h>
 
 #include <cmath>
 #include <cstdint>
 #include <cstring>
-#include <mutex>
 #include <new>
 #include <vector>
 
@@ -52,7 +50,19 @@ struct crm_ctx {
   double vrain, vsnow, vgrau, crain, csnow, cgrau, a_bg, a_pr, a_gr;
   int last_launches = 0;
   double last_kernel_ms = 0.;
+  bool pending_timing = false;
 };
+
+namespace crm {
+struct PrepParams {
+  int ncrms, ld, plev, nx, igstep;
+  const double *zmid, *zint, *pdel, *tau00, *bflxls, *wndls;
+  const int *gcol;
+  double *z0;
+  double *rnd;
+};
+void launch_crm_prep(const PrepParams &p, cudaStream_t s);
+}  // namespace crm
 
 namespace {
 
@@ -100,63 +110,6 @@ void fft_trigs(std::vector<double> &trigs, int n) {
 }
 
 float gammafff(float x) { return (float)exp(lgamma((double)x)); }
-
-// MT19937 variant of cam/RNG_MT.F90:52-142 (its UMASK is 0xBB9ACA00)
-struct RngMT {
-  int32_t mt[624];
-  int mti;
-  explicit RngMT(int32_t seed) {
-    mt[0] = seed;
-    for (mti = 1; mti < 624; ++mti) mt[mti] = (int32_t)((uint32_t)69069 * (uint32_t)mt[mti - 1]);
-  }
-  double next() {
-    const int32_t UMASK = -1147483648, LMASK = 2147483647, MATA = -1727483681;
-    const int32_t TMASKB = -1658038656, TMASKC = -272236544;
-    int32_t y;
-    if (mti >= 624) {
-      int kk;
-      for (kk = 0; kk < 624 - 397; ++kk) {
-        y = (mt[kk] & UMASK) | (mt[kk + 1] & LMASK);
-        mt[kk] = mt[kk + 397] ^ (int32_t)((uint32_t)y >> 1) ^ ((y & 1) ? MATA : 0);
-      }
-      for (; kk < 623; ++kk) {
-        y = (mt[kk] & UMASK) | (mt[kk + 1] & LMASK);
-        mt[kk] = mt[kk + (397 - 624)] ^ (int32_t)((uint32_t)y >> 1) ^ ((y & 1) ? MATA : 0);
-      }
-      y = (mt[623] & UMASK) | (mt[0] & LMASK);
-      mt[623] = mt[396] ^ (int32_t)((uint32_t)y >> 1) ^ ((y & 1) ? MATA : 0);
-      mti = 0;
-    }
-    y = mt[mti++];
-    y ^= (int32_t)((uint32_t)y >> 11);
-    y ^= (int32_t)(((uint32_t)y << 7) & (uint32_t)TMASKB);
-    y ^= (int32_t)(((uint32_t)y << 15) & (uint32_t)TMASKC);
-    y ^= (int32_t)((uint32_t)y >> 18);
-    if (y < 0) return ((double)y + 4294967296.0) / 4294967296.0;
-    return ((double)y + 0.5) / 4294967296.0;
-  }
-};
-
-double dmax2(double a, double b) { return (b > a) ? b : a; }
-double dmin2(double a, double b) { return (b < a) ? b : a; }
-
-// z0_est (crmsurface.F90:104-133) with the roughness-length clamp of
-// crm_module.F90:590
-double z0_of(double z, double bflx, double wnd, double ustar) {
-  const double vonk = R4H(0.4), am = R4H(4.8), bm = R4H(19.3), eps = R4H(1.e-10);
-  double c1 = (double)(3.14159f / 2.f - 3.f * logf(2.f));
-  double rlmo = -bflx * vonk / (ustar * ustar * ustar + eps);
-  double zeta = dmin2(1., z * rlmo);
-  double psi1;
-  if (zeta >= 0.) psi1 = -am * zeta;
-  else {
-    double x = sqrt(sqrt(1.0 - bm * zeta));
-    psi1 = 2. * det_log(1.0 + x) + det_log(1.0 + x * x) - 2. * atan(x) + c1;
-  }
-  double lnz = dmax2(0., vonk * wnd / (ustar + eps) + psi1);
-  double z0 = z * det_exp(-lnz);
-  return dmax2(R4H(0.00001), dmin2(1., z0));
-}
 
 enum InField { I_ZMID, I_ZINT, I_TL, I_QL, I_QCCL, I_QIIL, I_PMID, I_PINT, I_PDEL, I_UL, I_VL, I_NIN };
 
@@ -208,6 +161,7 @@ int alloc_ctx(crm_ctx *c) {
   c->ld_cap = g.max_ncrms;
   const int ld = c->ld_cap, plev = g.plev, nx = g.crm_nx, nz = g.crm_nz;
   c->in_elems = (size_t)ld * (plev + 1);
+  // GCM profiles, then tau00, bflxls, wndls (ld each) and gcol (ld ints)
   CK(cudaMalloc(&c->d_in, sizeof(double) * c->in_elems * I_NIN + sizeof(double) * 4 * ld));
   CK(cudaMalloc(&c->d_state, sizeof(double) * (size_t)ld * nx * nz * 7));
   CK(cudaMalloc(&c->d_rad, sizeof(double) * (size_t)ld * g.crm_nx_rad * nz * 6));
@@ -269,6 +223,75 @@ void free_ctx(crm_ctx *c) {
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
 }
 
+// Enqueue the set-up and column kernels for device-resident arguments.
+int enqueue(crm_ctx *c, const crm_call_desc *d, const crm_input_c *in, crm_state_c *st, crm_rad_c *rad,
+            crm_output_c *out, int *d_status, cudaStream_t s) {
+  const crm_config &g = c->cfg;
+  const int ncrms = d->ncrms, ld = d->ld;
+  if (ncrms < 1 || ld < ncrms || ncrms > g.max_ncrms || !(d->dt_gl > 0)) return CRM_ERR_ARG;
+  if (!d->gcol && d->igstep <= 1) return CRM_ERR_ARG;
+  const double *need[] = {in->zmid, in->zint, in->tl, in->ql, in->qccl, in->qiil, in->pmid,
+                          in->pint, in->pdel, in->ul, in->vl, in->tau00, in->bflxls, in->wndls};
+  for (const double *q : need)
+    if (!q) return CRM_ERR_ARG;
+  double *sp[7] = {st->u_wind, st->v_wind, st->w_wind, st->temperature, st->qt, st->qp, st->qn};
+  for (double *q : sp)
+    if (!q) return CRM_ERR_ARG;
+  double *rp[5] = {rad->temperature, rad->qv, rad->qc, rad->qi, rad->cld};
+  if (!rad->qrad) return CRM_ERR_ARG;
+  for (double *q : rp)
+    if (!q) return CRM_ERR_ARG;
+  for (int f = 0; f < CRM_NOUT; ++f)
+    if (!out->field[f]) return CRM_ERR_ARG;
+  int nstop = (int)(d->dt_gl / g.crm_dt);       // crm_module.F90:712-713
+  if (nstop < 1) return CRM_ERR_ARG;
+  double dt = d->dt_gl / nstop;
+  if (60. < 2 * dt) return CRM_ERR_ARG;         // damping.F90:39-42
+  crm::PrepParams pp;
+  pp.ncrms = ncrms; pp.ld = ld; pp.plev = g.plev; pp.nx = g.crm_nx; pp.igstep = d->igstep;
+  pp.zmid = in->zmid; pp.zint = in->zint; pp.pdel = in->pdel;
+  pp.tau00 = in->tau00; pp.bflxls = in->bflxls; pp.wndls = in->wndls;
+  pp.gcol = d->gcol;
+  pp.z0 = c->d_colconst;
+  pp.rnd = c->d_colconst + g.max_ncrms;
+  crm::KParams p;
+  memset(&p, 0, sizeof p);
+  p.L = c->L;
+  p.ncrms = ncrms; p.ld = ld; p.nstop = nstop; p.igstep = d->igstep;
+  p.batch_mode = g.batch_mode; p.clamp_batch = 0;
+  p.dx = g.crm_dx; p.dy = g.crm_dx; p.dt = dt; p.dt_gl = d->dt_gl;
+  p.gams1 = c->gam[4]; p.gams2 = c->gam[5]; p.gamg1 = c->gam[7]; p.gamg2 = c->gam[8];
+  p.gamr1 = c->gam[1]; p.gamr2 = c->gam[2];
+  p.vrain = c->vrain; p.vsnow = c->vsnow; p.vgrau = c->vgrau;
+  p.crain = c->crain; p.csnow = c->csnow; p.cgrau = c->cgrau;
+  p.a_bg = c->a_bg; p.a_pr = c->a_pr; p.a_gr = c->a_gr;
+  p.nfax = c->ifax[0];
+  for (int k = 0; k <= c->ifax[0] && k < 8; ++k) p.ifax[k] = c->ifax[k];
+  p.trigs = c->d_consts;
+  p.eign = c->d_consts + c->trigs.size();
+  p.z0 = pp.z0;
+  p.rnd = pp.rnd;
+  p.zmid = in->zmid; p.zint = in->zint; p.tl = in->tl; p.ql = in->ql; p.qccl = in->qccl;
+  p.qiil = in->qiil; p.pmid = in->pmid; p.pint = in->pint; p.pdel = in->pdel;
+  p.ul = in->ul; p.vl = in->vl;
+  for (int f = 0; f < 7; ++f) p.st[f] = sp[f];
+  p.qrad = rad->qrad;
+  for (int f = 0; f < 5; ++f) p.radout[f] = rp[f];
+  for (int f = 0; f < CRM_NOUT; ++f) p.out[f] = out->field[f];
+  p.slabs = c->slabs;
+  p.col_status = d_status ? d_status : c->d_status;
+  int grid = ncrms < c->grid_max ? ncrms : c->grid_max;
+  CK(cudaEventRecord(c->ev0, s));
+  crm::launch_crm_prep(pp, s);
+  if (g.precision == CRM_FP64) crm::launch_crm_columns<double>(p, grid, c->block, s);
+  else crm::launch_crm_columns<float>(p, grid, c->block, s);
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(c->ev1, s));
+  c->last_launches = 2;
+  c->pending_timing = true;
+  return CRM_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -282,7 +305,10 @@ crm_ctx *crm_create(const crm_config *cfg, int *status) {
     return nullptr;
   }
   crm_ctx *c = new (std::nothrow) crm_ctx();
-  if (!c) { if (status) *status = CRM_ERR_ARG; return nullptr; }
+  if (!c) {
+    if (status) *status = CRM_ERR_ARG;
+    return nullptr;
+  }
   c->cfg = *cfg;
   rc = alloc_ctx(c);
   if (rc != CRM_OK) {
@@ -308,7 +334,17 @@ int crm_set_stream(crm_ctx *ctx, void *stream) {
 }
 
 int crm_last_launch_count(const crm_ctx *ctx) { return ctx ? ctx->last_launches : 0; }
-double crm_last_kernel_ms(const crm_ctx *ctx) { return ctx ? ctx->last_kernel_ms : 0.; }
+
+double crm_last_kernel_ms(const crm_ctx *ctx) {
+  if (!ctx) return 0.;
+  if (ctx->pending_timing) {
+    float ms = 0.f;
+    if (cudaEventSynchronize(ctx->ev1) == cudaSuccess && cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1) == cudaSuccess)
+      return ms;
+    return 0.;
+  }
+  return ctx->last_kernel_ms;
+}
 
 const char *crm_status_string(int s) {
   switch (s) {
@@ -327,108 +363,73 @@ const char *crm_status_string(int s) {
 
 const char *crm_version(void) { return "crm-gb300 0.1 (sm_103a; 2D sam1mom; fp64 plain + fp32 mixed)"; }
 
+int crm_run_device(crm_ctx *c, const crm_call_desc *d, const crm_input_c *in, crm_state_c *st, crm_rad_c *rad,
+                   crm_output_c *out, int *col_status, void *stream) {
+  if (!c || !d || !in || !st || !rad || !out) return CRM_ERR_ARG;
+  cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
+  return enqueue(c, d, in, st, rad, out, col_status, s);
+}
+
 int crm_run(crm_ctx *c, const crm_call_desc *d, const crm_input_c *in, crm_state_c *st, crm_rad_c *rad,
             crm_output_c *out, int *col_status) {
   if (!c || !d || !in || !st || !rad || !out) return CRM_ERR_ARG;
   const crm_config &g = c->cfg;
   const int ncrms = d->ncrms, ld = d->ld, plev = g.plev, nx = g.crm_nx, nz = g.crm_nz;
-  if (ncrms < 1 || ld < ncrms || ld > c->ld_cap || !(d->dt_gl > 0)) return CRM_ERR_ARG;
+  if (ncrms < 1 || ld < ncrms || ld > c->ld_cap) return CRM_ERR_ARG;
   if (!d->gcol && d->igstep <= 1) return CRM_ERR_ARG;
-  int nstop = (int)(d->dt_gl / g.crm_dt);
-  if (nstop < 1) return CRM_ERR_ARG;
-  double dt = d->dt_gl / nstop;
-  if (60. < 2 * dt) return CRM_ERR_ARG;
   cudaStream_t s = c->stream;
-  // inputs: GCM profiles (ld, plev[+1])
-  const double *src[I_NIN] = {in->zmid, in->zint, in->tl, in->ql, in->qccl, in->qiil, in->pmid, in->pint, in->pdel, in->ul, in->vl};
+  // stage the host arguments through the handle's device buffers
+  crm_input_c din;
+  memset(&din, 0, sizeof din);
+  const double *src[I_NIN] = {in->zmid, in->zint, in->tl, in->ql, in->qccl, in->qiil,
+                              in->pmid, in->pint, in->pdel, in->ul, in->vl};
+  const double **dst[I_NIN] = {&din.zmid, &din.zint, &din.tl, &din.ql, &din.qccl, &din.qiil,
+                               &din.pmid, &din.pint, &din.pdel, &din.ul, &din.vl};
   for (int f = 0; f < I_NIN; ++f) {
     if (!src[f]) return CRM_ERR_ARG;
     size_t n = (size_t)ld * ((f == I_ZINT || f == I_PINT) ? plev + 1 : plev);
-    CK(cudaMemcpyAsync(c->d_in + (size_t)f * c->in_elems, src[f], sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    double *dp = c->d_in + (size_t)f * c->in_elems;
+    CK(cudaMemcpyAsync(dp, src[f], sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    *dst[f] = dp;
   }
-  // state and qrad
+  double *scal = c->d_in + (size_t)I_NIN * c->in_elems;
+  const double *s1[3] = {in->tau00, in->bflxls, in->wndls};
+  const double **d1[3] = {&din.tau00, &din.bflxls, &din.wndls};
+  for (int f = 0; f < 3; ++f) {
+    if (!s1[f]) return CRM_ERR_ARG;
+    CK(cudaMemcpyAsync(scal + (size_t)f * c->ld_cap, s1[f], sizeof(double) * ld, cudaMemcpyHostToDevice, s));
+    *d1[f] = scal + (size_t)f * c->ld_cap;
+  }
+  int *dgcol = reinterpret_cast<int *>(scal + (size_t)3 * c->ld_cap);
+  if (d->gcol) CK(cudaMemcpyAsync(dgcol, d->gcol, sizeof(int) * ncrms, cudaMemcpyHostToDevice, s));
+  crm_call_desc dd = *d;
+  dd.gcol = d->gcol ? dgcol : nullptr;
   double *sp[7] = {st->u_wind, st->v_wind, st->w_wind, st->temperature, st->qt, st->qp, st->qn};
   const size_t n4 = (size_t)ld * nx * nz;
+  crm_state_c dst_state;
+  double **ds[7] = {&dst_state.u_wind, &dst_state.v_wind, &dst_state.w_wind, &dst_state.temperature,
+                    &dst_state.qt, &dst_state.qp, &dst_state.qn};
   for (int f = 0; f < 7; ++f) {
     if (!sp[f]) return CRM_ERR_ARG;
     CK(cudaMemcpyAsync(c->d_state + f * n4, sp[f], sizeof(double) * n4, cudaMemcpyHostToDevice, s));
+    *ds[f] = c->d_state + f * n4;
   }
   const size_t nr = (size_t)ld * g.crm_nx_rad * nz;
   if (!rad->qrad) return CRM_ERR_ARG;
   CK(cudaMemcpyAsync(c->d_rad, rad->qrad, sizeof(double) * nr, cudaMemcpyHostToDevice, s));
-  // per-column host constants: z0 and the setperturb draws
-  std::vector<double> colc((size_t)ncrms * (1 + 5 * nx));
-  for (int i = 0; i < ncrms; ++i) {
-    auto IN = [&](const double *a, int l) { return a[(size_t)i + (size_t)ld * (l - 1)]; };
-    double z1 = IN(in->zmid, plev) - IN(in->zint, plev + 1);
-    double z2 = IN(in->zmid, plev - 1) - IN(in->zint, plev + 1);
-    double dz = 0.5 * (z1 + z2);
-    double zi1 = IN(in->zint, plev + 1) - IN(in->zint, plev + 1);
-    double zi2 = IN(in->zint, plev) - IN(in->zint, plev + 1);
-    double adz1 = (zi2 - zi1) / dz;
-    double rho1 = IN(in->pdel, plev) / 9.80616 / (adz1 * dz);
-    double ustar = sqrt(in->tau00[i] / rho1);
-    colc[i] = z0_of(z1, in->bflxls[i], in->wndls[i], ustar);
-    if (d->igstep <= 1) {
-      RngMT rng((int32_t)(d->gcol[i] * 1000));
-      double *r = &colc[(size_t)ncrms + (size_t)i * 5 * nx];
-      for (int k = 0; k < 5; ++k)
-        for (int ii = 0; ii < nx; ++ii) r[(size_t)k * nx + ii] = 1. - 2. * rng.next();
-    }
+  crm_rad_c drad;
+  drad.qrad = c->d_rad;
+  double **dr[5] = {&drad.temperature, &drad.qv, &drad.qc, &drad.qi, &drad.cld};
+  for (int f = 0; f < 5; ++f) *dr[f] = c->d_rad + (f + 1) * nr;
+  crm_output_c dout;
+  size_t o = 0;
+  for (int f = 0; f < CRM_NOUT; ++f) {
+    dout.field[f] = c->d_out + o;
+    o += out_elems(g, f, ld);
   }
-  CK(cudaMemcpyAsync(c->d_colconst, colc.data(), sizeof(double) * colc.size(), cudaMemcpyHostToDevice, s));
-  // kernel parameters
-  crm::KParams p;
-  memset(&p, 0, sizeof p);
-  p.L = c->L;
-  p.ncrms = ncrms; p.ld = ld; p.nstop = nstop; p.igstep = d->igstep;
-  p.batch_mode = g.batch_mode; p.clamp_batch = 0;
-  p.dx = g.crm_dx; p.dy = g.crm_dx; p.dt = dt; p.dt_gl = d->dt_gl;
-  p.gams1 = c->gam[4]; p.gams2 = c->gam[5]; p.gamg1 = c->gam[7]; p.gamg2 = c->gam[8];
-  p.gamr1 = c->gam[1]; p.gamr2 = c->gam[2];
-  p.vrain = c->vrain; p.vsnow = c->vsnow; p.vgrau = c->vgrau;
-  p.crain = c->crain; p.csnow = c->csnow; p.cgrau = c->cgrau;
-  p.a_bg = c->a_bg; p.a_pr = c->a_pr; p.a_gr = c->a_gr;
-  p.nfax = c->ifax[0];
-  for (int k = 0; k <= c->ifax[0] && k < 8; ++k) p.ifax[k] = c->ifax[k];
-  p.trigs = c->d_consts;
-  p.eign = c->d_consts + c->trigs.size();
-  p.z0 = c->d_colconst;
-  p.rnd = c->d_colconst + ncrms;
-  double *const *inp = nullptr;
-  (void)inp;
-  p.zmid = c->d_in + (size_t)I_ZMID * c->in_elems;
-  p.zint = c->d_in + (size_t)I_ZINT * c->in_elems;
-  p.tl = c->d_in + (size_t)I_TL * c->in_elems;
-  p.ql = c->d_in + (size_t)I_QL * c->in_elems;
-  p.qccl = c->d_in + (size_t)I_QCCL * c->in_elems;
-  p.qiil = c->d_in + (size_t)I_QIIL * c->in_elems;
-  p.pmid = c->d_in + (size_t)I_PMID * c->in_elems;
-  p.pint = c->d_in + (size_t)I_PINT * c->in_elems;
-  p.pdel = c->d_in + (size_t)I_PDEL * c->in_elems;
-  p.ul = c->d_in + (size_t)I_UL * c->in_elems;
-  p.vl = c->d_in + (size_t)I_VL * c->in_elems;
-  for (int f = 0; f < 7; ++f) p.st[f] = c->d_state + f * n4;
-  p.qrad = c->d_rad;
-  for (int f = 0; f < 5; ++f) p.radout[f] = c->d_rad + (f + 1) * nr;
-  {
-    size_t o = 0;
-    for (int f = 0; f < CRM_NOUT; ++f) {
-      p.out[f] = c->d_out + o;
-      o += out_elems(g, f, ld);
-    }
-    CK(cudaMemsetAsync(c->d_out, 0, sizeof(double) * o, s));
-  }
-  p.slabs = c->slabs;
-  p.col_status = c->d_status;
-  int grid = ncrms < c->grid_max ? ncrms : c->grid_max;
-  CK(cudaEventRecord(c->ev0, s));
-  if (g.precision == CRM_FP64) crm::launch_crm_columns<double>(p, grid, c->block, s);
-  else crm::launch_crm_columns<float>(p, grid, c->block, s);
-  CK(cudaGetLastError());
-  CK(cudaEventRecord(c->ev1, s));
-  c->last_launches = 1;
-  // results back
+  CK(cudaMemsetAsync(c->d_out, 0, sizeof(double) * o, s));
+  int rc = enqueue(c, &dd, &din, &dst_state, &drad, &dout, c->d_status, s);
+  if (rc != CRM_OK) return rc;
   for (int f = 0; f < 7; ++f)
     CK(cudaMemcpyAsync(sp[f], c->d_state + f * n4, sizeof(double) * n4, cudaMemcpyDeviceToHost, s));
   double *rp[5] = {rad->temperature, rad->qv, rad->qc, rad->qi, rad->cld};
@@ -436,13 +437,14 @@ int crm_run(crm_ctx *c, const crm_call_desc *d, const crm_input_c *in, crm_state
     if (rp[f]) CK(cudaMemcpyAsync(rp[f], c->d_rad + (f + 1) * nr, sizeof(double) * nr, cudaMemcpyDeviceToHost, s));
   for (int f = 0; f < CRM_NOUT; ++f)
     if (out->field[f])
-      CK(cudaMemcpyAsync(out->field[f], p.out[f], sizeof(double) * out_elems(g, f, ld), cudaMemcpyDeviceToHost, s));
+      CK(cudaMemcpyAsync(out->field[f], dout.field[f], sizeof(double) * out_elems(g, f, ld), cudaMemcpyDeviceToHost, s));
   std::vector<int> stat(ncrms, 0);
   CK(cudaMemcpyAsync(stat.data(), c->d_status, sizeof(int) * ncrms, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   float ms = 0.f;
   CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
   c->last_kernel_ms = ms;
+  c->pending_timing = false;
   int worst = CRM_OK;
   for (int i = 0; i < ncrms; ++i) {
     if (col_status) col_status[i] = stat[i];

@@ -1,0 +1,334 @@
+"""Benchmark of the GB300 crm(): CRM column-steps/s on the 2D nx64 nz58 workload.
+
+One step = one crm() call: 1024 GCM columns, each an embedded 64 x 58 CRM
+(dx 1 km, dt 10 s) integrated over one GCM step of 1200 s (120 CRM steps),
+sam1mom microphysics, SGS TKE, MPDATA.  Throughput = ncrms * nstop /
+seconds.  Reported:
+  value   FP32-mixed form, arguments resident in HBM (crm_run_device),
+          device time from CUDA events around the K timed calls
+  e2e     the same through the host C ABI (crm_run) from pinned host
+          buffers, host<->device copies inside the timed region
+  fp64    the FP64 plain form (bit-identical to the CPU oracle), same way
+  cpu_baseline  the CPU FP64 restatement on the host cores (bounded sample)
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+For N > 1 (torchrun) every rank integrates its own 1024 columns: CRM columns
+are independent, so the work shards with no collective ("weak" scaling).
+--impl reference times the CPU restatement of the reference's crm() on the
+host cores instead (the reference itself is Fortran/OpenACC and cannot be
+built here).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, 'acme-ecp_gb300'))
+
+METRIC = 'CRM column-steps/s, nx64 nz58, FP32-mixed vs FP64 on 1 GB300; p99 chunk latency'
+UNIT = 'column-steps/s'
+NCRMS = 1024
+WORDS_PER_CELL = 27          # algorithmic HBM words per cell per CRM step
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(REPO, 'MEASURED_PEAKS.json')) as f:
+            d = json.load(f)
+        return float(d['hbm_gbs']), 'measured'
+    except Exception:
+        return 6800.0, 'fallback'
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled while the timed region runs."""
+    Q = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+         'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+         'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ['nvidia-smi', '-i', str(self.gpu), '--query-gpu=' + self.Q,
+                 '--format=csv,noheader,nounits', '-lms', '200'],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(',')])
+
+    def stop(self):
+        if self.proc is None:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['unavailable']}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                smax = float(r[2])
+                for n, v in zip(names, r[5:9]):
+                    if v.strip().lower() in ('active', '1'):
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                pass
+        return {'sm_mhz': float(np.median(sm)) if sm else None, 'sm_max_mhz': smax,
+                'reasons': sorted(reasons), 'samples': len(sm)}
+
+
+def dist_info():
+    ws = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    return ws, rank, local
+
+
+def cpu_baseline(ncols, nthreads=0):
+    """The oracle (CPU FP64 restatement) on a bounded sample of the workload."""
+    sys.path.insert(0, os.path.join(REPO, 'oracle'))
+    import oracle
+    from crm_gb300 import synthetic as S
+    oracle.build()
+    cfg, cin, st, rad, desc = S.workload1(ncrms=ncols)
+    cores = nthreads or os.cpu_count()
+    t0 = time.perf_counter()
+    rc, _, _ = oracle.run(cfg, desc, cin, st, rad, nthreads=cores)
+    dt = time.perf_counter() - t0
+    return {'value': ncols * 120 / dt, 'unit': UNIT, 'cores': cores, 'kind': 'port',
+            'sample': '%d of the %d columns, full GCM step (120 CRM steps), FP64, OpenMP over columns'
+                      % (ncols, NCRMS), 'seconds': dt, 'rc': rc}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_info()
+    if rank != 0:
+        return
+    ncols = int(os.environ.get('CRM_BENCH_CPU_COLS', '16'))
+    for _ in range(args.warmup):
+        cpu_baseline(ncols)
+    vals = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        vals.append(cpu_baseline(ncols))
+    total = time.perf_counter() - t0
+    v = ncols * 120 * args.steps / total
+    cb = dict(vals[-1])
+    cb['value'] = v
+    line = {'metric': METRIC, 'value': v, 'unit': UNIT, 'n_gpus': ws, 'steps': args.steps,
+            'warmup': args.warmup, 'ms_per_step': 1000 * total / args.steps,
+            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+            'dtype': 'f64', 'data': 'synthetic', 'impl': 'reference',
+            'config': {'workload': '2D CRM nx64 nz58 dx1km dt10s, 1 GCM step of 1200 s, sam1mom; '
+                                   '%d-column sample per step on the host cores' % ncols},
+            'cpu_baseline': {k: cb[k] for k in ('value', 'unit', 'cores', 'kind', 'sample')},
+            'e2e': {'value': v, 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=5)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    ap.add_argument('--fp64-steps', type=int, default=2)
+    ap.add_argument('--cpu-cols', type=int, default=16)
+    args = ap.parse_args()
+    if args.impl == 'reference':
+        return run_reference(args)
+
+    import torch
+    from crm_gb300 import build as B
+    from crm_gb300 import synthetic as S
+    from crm_gb300 import types as T
+    from crm_gb300.device import DeviceCrmArrays
+    from crm_gb300.lib import CrmContext
+
+    ws, rank, local = dist_info()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group('nccl')
+    else:
+        torch.cuda.set_device(0)
+    if rank == 0:
+        B.build()
+    if ws > 1:
+        dist.barrier()
+    B.build()
+
+    def barrier():
+        if ws > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # ---- synthetic workload (each rank its own columns)
+    cfg32, cin, st, rad, desc = S.workload1(ncrms=NCRMS, seed=1000 * rank, precision=T.CRM_FP32_MIXED)
+    cfg32.max_ncrms = NCRMS
+    nstop = int(desc.dt_gl / cfg32.crm_dt)
+    colsteps = NCRMS * nstop
+    cells = cfg32.crm_nx * cfg32.crm_ny * cfg32.crm_nz
+
+    def device_rate(cfg, steps, warmup):
+        ctx = CrmContext(cfg)
+        dev = DeviceCrmArrays(cfg, cin, st, rad, desc, desc._keep)
+        stream = torch.cuda.current_stream().cuda_stream
+        for _ in range(warmup):
+            dev.reset_state(st)
+            ctx.run_device(dev, stream)
+        barrier()
+        # each step restarts from the same initial state (igstep 1): the
+        # state (213 MB) is re-read from HBM every step, larger than L2
+        kms = []
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        tot = 0.0
+        for _ in range(steps):
+            dev.reset_state(st)
+            e0.record()
+            ctx.run_device(dev, stream)
+            e1.record()
+            e1.synchronize()
+            tot += e0.elapsed_time(e1)
+            kms.append(ctx.last_kernel_ms)
+        barrier()
+        t = torch.tensor([tot], device='cuda')
+        if ws > 1:
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item()) / steps
+        return ctx, dev, ms, kms
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    ctx32, dev32, ms32, kms32 = device_rate(cfg32, args.steps, args.warmup)
+    clk = clocks.stop()
+    value = ws * colsteps / (ms32 / 1000.0)
+
+    # ---- end to end through the host C ABI, pinned host buffers
+    def pinned_copy(bundle):
+        out = bundle.copy()
+        for n, a in bundle.arrays().items():
+            t = torch.empty(a.shape[::-1], dtype=torch.float64, pin_memory=True)
+            v = t.numpy().T
+            v[...] = a
+            setattr(out, n, v)
+            out._keep = getattr(out, '_keep', []) + [t]
+        return out
+
+    cin_p, st_p, rad_p = pinned_copy(cin), pinned_copy(st), pinned_copy(rad)
+    out_t = {}
+    out_p = T.CrmOutput(desc.ld, cfg32.crm_nx, cfg32.crm_ny, cfg32.crm_nz, cfg32.plev)
+    for n, a in out_p.arrays().items():
+        t = torch.empty(a.shape[::-1], dtype=torch.float64, pin_memory=True)
+        out_t[n] = t
+        setattr(out_p, n, t.numpy().T)
+    ctx32.run(desc, cin_p, st_p, rad_p, out_p)
+    barrier()
+    e2e_t = 0.0
+    for _ in range(args.steps):
+        for n, a in st.arrays().items():
+            getattr(st_p, n)[...] = a
+        t0 = time.perf_counter()
+        ctx32.run(desc, cin_p, st_p, rad_p, out_p)
+        e2e_t += time.perf_counter() - t0
+    barrier()
+    tt = torch.tensor([e2e_t], device='cuda')
+    if ws > 1:
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    e2e_ms = float(tt.item()) * 1000.0 / args.steps
+    ld = desc.ld
+    h2d = (sum(a.nbytes for a in cin.arrays().values() if a.ndim == 2) + 3 * ld * 8 + 4 * ld +
+           sum(a.nbytes for a in st.arrays().values()) + rad.qrad.nbytes)
+    d2h = (sum(a.nbytes for a in st.arrays().values()) + 5 * rad.qrad.nbytes +
+           sum(a.nbytes for a in out_p.arrays().values()) + 4 * NCRMS)
+
+    # ---- FP64 plain form
+    cfg64 = S.config1(precision=T.CRM_FP64)
+    cfg64.max_ncrms = NCRMS
+    ctx64, dev64, ms64, _ = device_rate(cfg64, args.fp64_steps, 1)
+    value64 = ws * colsteps / (ms64 / 1000.0)
+
+    # ---- accuracy of the FP32-mixed form against the FP64 form (same inputs)
+    errs = {}
+    for n in ('temperature', 'qt', 'u_wind', 'w_wind', 'qp'):
+        a = dev32.state_numpy(n)[:NCRMS].astype(np.float64)
+        b = dev64.state_numpy(n)[:NCRMS]
+        den = np.linalg.norm(b)
+        errs[n] = float(np.linalg.norm(a - b) / den) if den > 0 else float(np.linalg.norm(a - b))
+
+    if rank != 0:
+        if ws > 1:
+            dist.destroy_process_group()
+        return
+    peak, peak_kind = measured_peaks()
+    kernel_ms = float(np.median(kms32))
+    bytes_per_launch = NCRMS * nstop * cells * WORDS_PER_CELL * 4
+    achieved = bytes_per_launch / (kernel_ms / 1000.0) / 1e9
+    traffic = None
+    try:
+        with open(os.path.join(REPO, 'profiles', 'crm_columns_fp32_traffic.json')) as f:
+            tr = json.load(f)
+        traffic = tr.get('bytes_per_launch_scaled')
+    except Exception:
+        pass
+    cb = None
+    if ws == 1:
+        try:
+            c = cpu_baseline(args.cpu_cols)
+            cb = {k: c[k] for k in ('value', 'unit', 'cores', 'kind', 'sample')}
+        except Exception as e:  # the oracle needs g++; report why it is absent
+            cb = {'value': None, 'unit': UNIT, 'cores': os.cpu_count(), 'kind': 'port',
+                  'sample': 'failed: %s' % e}
+    line = {
+        'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': ws, 'steps': args.steps,
+        'warmup': args.warmup, 'ms_per_step': ms32, 'higher_is_better': True,
+        'scaling': 'weak', 'vs_baseline': None,
+        'dtype': 'f32 (f64 tridiagonal solve, domain sums, saturation Newton)',
+        'data': 'synthetic (idealised soundings, seeded)',
+        'config': {'workload': '2D CRM batch: %d columns x (64 x 1 x 58), dx 1 km, dt 10 s, '
+                               'dt_gl 1200 s (%d CRM steps), sam1mom, SGS TKE, MPDATA' % (NCRMS, nstop),
+                   'ncrms': NCRMS, 'crm_nx': 64, 'crm_nz': 58, 'plev': 72, 'nstop': nstop,
+                   'form': 'fp32-mixed', 'batch_mode': 'per-column',
+                   'l2': 'inputs larger than L2: every step re-reads the %d MB state' %
+                         (dev32.nbytes_state() // 2 ** 20)},
+        'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
+                     'frac': achieved / peak, 'traffic': traffic,
+                     'peak_kind': peak_kind, 'kernel_ms': kernel_ms,
+                     'algorithmic_bytes_per_launch': bytes_per_launch},
+        'cpu_baseline': cb,
+        'e2e': {'value': ws * colsteps / (e2e_ms / 1000.0), 'unit': UNIT,
+                'h2d_bytes_per_step': int(h2d), 'd2h_bytes_per_step': int(d2h),
+                'ms_per_step': e2e_ms},
+        'clocks': clk,
+        'gpu_launches': 2 * args.steps,
+        'fp64_plain': {'value': value64, 'unit': UNIT, 'ms_per_step': ms64, 'steps': args.fp64_steps},
+        'fp32_over_fp64': value / value64,
+        'fp32_rel_l2_vs_fp64_state': errs,
+    }
+    print(json.dumps(line))
+    if ws > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == '__main__':
+    main()

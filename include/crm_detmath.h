@@ -8,8 +8,9 @@
  * and a one-ulp difference in a cell feeds the chaotic CRM integration.  To
  * make the FP64 device form bit-identical to a CPU run of the same
  * algorithm, both sides evaluate these three functions with the code below,
- * built only from IEEE-754 +, -, *, / (correctly rounded on both sides when
- * floating-point contraction is off: nvcc -fmad=false, gcc -ffp-contract=off).
+ * built only from IEEE-754 +, -, *, /, sqrt and fma (correctly rounded on
+ * both sides when implicit contraction is off: nvcc -fmad=false, gcc
+ * -ffp-contract=off).
  *
  * Methods (textbook, not taken from any vendor library):
  *  - exp: Cody-Waite reduction x = n*ln2 + r, |r| <= ln2/2, with ln2 split
@@ -19,9 +20,15 @@
  *  - log: x = 2^e * m with m in [sqrt(1/2), sqrt(2)); f = m - 1,
  *    s = f/(2+f), log(m) = 2 atanh(s) = f - (f^2/2 - s*(f^2/2 + R)) with
  *    R = sum_{k=1..12} 2 s^(2k)/(2k+1) (truncation < 1e-19).
- *  - pow(x, y) = exp(y * log(x)) for x > 0; pow(0, y>0) = 0.
+ *  - pow(x, y) = exp(y * log(x)) for x > 0; pow(0, y>0) = 0, with log(x)
+ *    carried as an exact head e*ln2_head plus a tail and the product y*log x
+ *    split exactly by one fused multiply-add (correctly rounded on both
+ *    sides), so the result stays within a few ulp for large |y log x|.
+ *  - atan: odd symmetry, atan(x) = pi/2 - atan(1/x) above 1, then
+ *    atan(x) = pi/6 + atan((sqrt(3) x - 1)/(x + sqrt(3))) above tan(pi/12),
+ *    and the Taylor series to t^29 on |t| <= tan(pi/12) (< 1e-18).
  * Accuracy on the CRM's arguments is checked against the platform libm in
- * tests/test_detmath.py (exp/log <= 2 ulp, pow <= 16 ulp).
+ * tests/test_detmath.py (exp, log, pow <= 2 ulp, atan <= 4 ulp).
  */
 #ifndef CRM_DETMATH_H
 #define CRM_DETMATH_H
@@ -67,18 +74,20 @@ CRM_DM_FN double dm_pow2i(int n) {
   return dm_from_bits((long long)(n + 1023) << 52);
 }
 
-CRM_DM_FN double det_exp(double x) {
-  if (x != x) return x;                     /* NaN */
-  if (x > 709.0) return dm_from_bits(0x7ff0000000000000LL);
-  if (x < -744.0) return 0.0;
-  double fn = x * DM_INV_LN2 + 0.5;
+/* exp(hi + lo) for |lo| much smaller than |hi|: the tail enters the
+ * reduced argument after the exact subtraction of n*ln2_head. */
+CRM_DM_FN double det_exp2(double hi, double lo) {
+  if (hi != hi) return hi;                  /* NaN */
+  if (hi > 709.0) return dm_from_bits(0x7ff0000000000000LL);
+  if (hi < -744.0) return 0.0;
+  double fn = hi * DM_INV_LN2 + 0.5;
 #if defined(__CUDA_ARCH__)
   fn = floor(fn);
 #else
   fn = __builtin_floor(fn);
 #endif
   int n = (int)fn;
-  double r = (x - fn * DM_LN2_HI) - fn * DM_LN2_LO;
+  double r = ((hi - fn * DM_LN2_HI) + lo) - fn * DM_LN2_LO;
   /* Taylor coefficients 1/k!, k = 13 .. 0 */
   double p = 1.6059043836821614599e-10;   /* 1/13! */
   p = p * r + 2.0876756987868098979e-09;  /* 1/12! */
@@ -101,9 +110,14 @@ CRM_DM_FN double det_exp(double x) {
   return p * dm_pow2i(n);
 }
 
-CRM_DM_FN double det_log(double x) {
-  if (x != x || x < 0.0) return dm_from_bits(0x7ff8000000000000LL);
-  if (x == 0.0) return -dm_from_bits(0x7ff0000000000000LL);
+CRM_DM_FN double det_exp(double x) { return det_exp2(x, 0.0); }
+
+/* log(x) as hi + lo: hi = e*ln2_head is exact, lo = e*ln2_tail + log(m).
+ * Returns 0 and sets *hi to the special value for x <= 0, NaN and +Inf. */
+CRM_DM_FN int det_log2(double x, double *hi, double *lo) {
+  *lo = 0.0;
+  if (x != x || x < 0.0) { *hi = dm_from_bits(0x7ff8000000000000LL); return 0; }
+  if (x == 0.0) { *hi = -dm_from_bits(0x7ff0000000000000LL); return 0; }
   long long b = dm_to_bits(x);
   int e = 0;
   if ((b >> 52) == 0) {                     /* subnormal: scale by 2^54 */
@@ -111,7 +125,7 @@ CRM_DM_FN double det_log(double x) {
     b = dm_to_bits(x);
     e = -54;
   }
-  if ((b >> 52) >= 0x7ff) return x;         /* +Inf */
+  if ((b >> 52) >= 0x7ff) { *hi = x; return 0; }   /* +Inf */
   e += (int)((b >> 52) & 0x7ff) - 1023;
   b = (b & 0x000fffffffffffffLL) | 0x3ff0000000000000LL;   /* m in [1,2) */
   double m = dm_from_bits(b);
@@ -138,7 +152,23 @@ CRM_DM_FN double det_log(double x) {
   R = R * z;
   double hfsq = 0.5 * f * f;
   double de = (double)e;
-  return de * DM_LN2_HI - ((hfsq - (s * (hfsq + R) + de * DM_LN2_LO)) - f);
+  *hi = de * DM_LN2_HI;
+  *lo = de * DM_LN2_LO - ((hfsq - s * (hfsq + R)) - f);
+  return 1;
+}
+
+CRM_DM_FN double det_log(double x) {
+  double hi, lo;
+  if (!det_log2(x, &hi, &lo)) return hi;
+  return hi + lo;
+}
+
+CRM_DM_FN double dm_fma(double a, double b, double c) {
+#if defined(__CUDA_ARCH__)
+  return fma(a, b, c);
+#else
+  return __builtin_fma(a, b, c);
+#endif
 }
 
 CRM_DM_FN double det_pow(double x, double y) {
@@ -146,7 +176,45 @@ CRM_DM_FN double det_pow(double x, double y) {
   if (x == 0.0) return y > 0.0 ? 0.0 : dm_from_bits(0x7ff0000000000000LL);
   if (x < 0.0 || x != x || y != y) return dm_from_bits(0x7ff8000000000000LL);
   if (x == 1.0) return 1.0;
-  return det_exp(y * det_log(x));
+  double lh, ll;
+  det_log2(x, &lh, &ll);
+  double ph = y * lh;
+  double pl = dm_fma(y, lh, -ph) + y * ll;  /* exact product tail */
+  double h = ph + pl;                       /* renormalise the pair */
+  double t = pl - (h - ph);
+  return det_exp2(h, t);
+}
+
+CRM_DM_FN double det_atan(double x) {
+  if (x != x) return x;
+  double sgn = 1.0;
+  if (x < 0.0) { x = -x; sgn = -1.0; }
+  double base = 0.0, mul = 1.0;
+  if (x > 1.0) { x = 1.0 / x; base = 1.5707963267948966; mul = -1.0; }
+  double off = 0.0;
+  if (x > 0.2679491924311227) {             /* tan(pi/12) */
+    x = (1.7320508075688772 * x - 1.0) / (x + 1.7320508075688772);
+    off = 0.52359877559829887;               /* pi/6 */
+  }
+  double z = x * x;
+  /* sum_{k=0}^{14} (-1)^k z^k / (2k+1) */
+  double s = 1.0 / 29.0;
+  s = -s * z + 1.0 / 27.0;
+  s = -s * z + 1.0 / 25.0;
+  s = -s * z + 1.0 / 23.0;
+  s = -s * z + 1.0 / 21.0;
+  s = -s * z + 1.0 / 19.0;
+  s = -s * z + 1.0 / 17.0;
+  s = -s * z + 1.0 / 15.0;
+  s = -s * z + 1.0 / 13.0;
+  s = -s * z + 1.0 / 11.0;
+  s = -s * z + 1.0 / 9.0;
+  s = -s * z + 1.0 / 7.0;
+  s = -s * z + 1.0 / 5.0;
+  s = -s * z + 1.0 / 3.0;
+  s = -s * z + 1.0;
+  double r = off + x * s;
+  return sgn * (base + mul * r);
 }
 
 #ifdef __cplusplus

@@ -156,6 +156,16 @@ int crm_run(crm_ctx *ctx, const crm_call_desc *desc, const crm_input_c *in,
             crm_state_c *state, crm_rad_c *rad, crm_output_c *out,
             int *col_status);
 
+/* Device-resident variant of crm_run: every array pointer in desc (gcol),
+ * in, state, rad and out is a device pointer with the same layout, and
+ * col_status (ncrms ints) is a device pointer or NULL.  The work is enqueued
+ * on `stream` (a cudaStream_t, NULL for the handle's stream) and the call
+ * returns without synchronising; argument errors are returned at once.  This
+ * is the path a GCM that keeps its physics state on the GPU would call. */
+int crm_run_device(crm_ctx *ctx, const crm_call_desc *desc, const crm_input_c *in,
+                   crm_state_c *state, crm_rad_c *rad, crm_output_c *out,
+                   int *col_status, void *stream);
+
 /* Number of kernel launches issued by the last crm_run on this handle. */
 int crm_last_launch_count(const crm_ctx *ctx);
 /* Duration of the compute kernels of the last crm_run [ms] (CUDA events on

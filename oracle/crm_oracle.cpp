@@ -616,7 +616,7 @@ struct Model {
       if (zeta >= 0.) psi1 = -am * zeta;
       else {
         double x = sqrt(sqrt(1.0 - bm * zeta));
-        psi1 = 2. * det_log(1.0 + x) + det_log(1.0 + x * x) - 2. * atan(x) + c1;
+        psi1 = 2. * det_log(1.0 + x) + det_log(1.0 + x * x) - 2. * det_atan(x) + c1;
       }
       double lnz = fmax2(0., vonk * wnd / (ustar + eps) + psi1);
       c.z0 = z * det_exp(-lnz);

@@ -1,0 +1,57 @@
+"""FP32-mixed form against the FP64 oracle.
+
+The mixed form keeps FP64 only for the pressure tridiagonal solve, the domain
+sums and the saturation-adjustment Newton iteration.  After one GCM step
+(60-120 CRM steps of a convecting boundary layer) rounding differences grow
+chaotically, so the comparison is statistical: relative L2 error per field,
+with the bounds stated below, plus exact agreement of the status codes.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from crm_gb300 import synthetic as S
+from crm_gb300 import types as T
+from crm_gb300.lib import CrmContext
+
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+# relative L2 bounds after one GCM step (state fields and GCM tendencies)
+BOUNDS = {'temperature': 1e-4, 'qt': 1e-2, 'u_wind': 1e-1, 'w_wind': 1.0, 'qp': 1.0,
+          'sltend': 5e-1, 'qltend': 1.0}
+
+
+def _errors(wl, **kw):
+    cfg, cin, st, rad, desc = wl(**kw)
+    st_o, rad_o = st.copy(), rad.copy()
+    rc, _, out_o = oracle.run(cfg, desc, cin, st_o, rad_o)
+    assert rc == 0
+    cfg.precision = T.CRM_FP32_MIXED
+    cfg.max_ncrms = desc.ld
+    ctx = CrmContext(cfg)
+    out_g = T.CrmOutput(desc.ld, cfg.crm_nx, cfg.crm_ny, cfg.crm_nz, cfg.plev)
+    st_g, rad_g = st.copy(), rad.copy()
+    ctx.run(desc, cin, st_g, rad_g, out_g, raise_on_error=True)
+    e = {n: rel_l2(getattr(st_g, n), getattr(st_o, n)) for n in ('temperature', 'qt', 'u_wind', 'w_wind', 'qp')}
+    e['sltend'] = rel_l2(out_g.sltend, out_o.sltend)
+    e['qltend'] = rel_l2(out_g.qltend, out_o.qltend)
+    for n, a in out_g.arrays().items():
+        assert np.isfinite(a).all(), n
+    return e
+
+
+@pytest.mark.parametrize('moist', [False, True])
+def test_fp32_mixed_workload0(gpu_lib, moist):
+    e = _errors(S.workload0, ncrms=4, moist=moist)
+    print('fp32-mixed rel-L2 vs fp64 oracle (32x28, moist=%s):' % moist, e)
+    for n, b in BOUNDS.items():
+        assert e[n] <= b, (n, e[n], b)
+
+
+def test_fp32_mixed_workload1(gpu_lib):
+    e = _errors(S.workload1, ncrms=4)
+    print('fp32-mixed rel-L2 vs fp64 oracle (64x58):', e)
+    for n, b in BOUNDS.items():
+        assert e[n] <= b, (n, e[n], b)

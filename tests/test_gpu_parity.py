@@ -2,7 +2,8 @@
 
 Both evaluate the same IEEE operations in the same order (no FMA contraction,
 deterministic exp/log/pow, horizontal sums in the reference's loop order), so
-every state, rad and output field must agree bit for bit.
+every state, rad and output field must agree bit for bit: the tolerance of
+these tests is zero.
 """
 import numpy as np
 import pytest
@@ -14,25 +15,37 @@ from crm_gb300.lib import CrmContext
 
 pytestmark = pytest.mark.gpu
 
+_ctx = {}
 
-def _run_both(cfg, cin, st, rad, desc):
+
+def _context(cfg):
+    key = (cfg.crm_nx, cfg.crm_nz, cfg.plev, cfg.crm_dx, cfg.crm_dt, cfg.precision, cfg.max_ncrms)
+    if key not in _ctx:
+        _ctx[key] = CrmContext(cfg)
+    return _ctx[key]
+
+
+def run_gpu(cfg, cin, st, rad, desc):
+    cfg.max_ncrms = max(cfg.max_ncrms, desc.ld)
+    ctx = _context(cfg)
+    out = T.CrmOutput(desc.ld, cfg.crm_nx, cfg.crm_ny, cfg.crm_nz, cfg.plev)
+    stat = ctx.run(desc, cin, st, rad, out)
+    return ctx.last_rc, stat, out
+
+
+def run_both(cfg, cin, st, rad, desc):
     st_o, rad_o = st.copy(), rad.copy()
     rc, stat_o, out_o = oracle.run(cfg, desc, cin, st_o, rad_o)
     assert rc == 0, stat_o
-    cfg.max_ncrms = desc.ld
-    ctx = CrmContext(cfg)
     st_g, rad_g = st.copy(), rad.copy()
-    out_g = T.CrmOutput(desc.ld, cfg.crm_nx, cfg.crm_ny, cfg.crm_nz, cfg.plev)
-    stat_g = ctx.run(desc, cin, st_g, rad_g, out_g)
-    assert ctx.last_rc == 0, stat_g
+    rc_g, stat_g, out_g = run_gpu(cfg, cin, st_g, rad_g, desc)
+    assert rc_g == 0, stat_g
     return (st_o, rad_o, out_o), (st_g, rad_g, out_g)
 
 
-def _compare_exact(a, b):
-    bad = []
-    for name in ('st', 'rad', 'out'):
-        pass
+def mismatches(a, b):
     (st_o, rad_o, out_o), (st_g, rad_g, out_g) = a, b
+    bad = []
     for n, x in st_o.arrays().items():
         y = getattr(st_g, n)
         if not np.array_equal(x, y):
@@ -51,11 +64,97 @@ def _compare_exact(a, b):
 def test_fp64_bitexact_workload0_short(gpu_lib):
     cfg, cin, st, rad, desc = S.workload0(ncrms=4)
     desc.dt_gl = 200.0          # 10 CRM steps
-    a, b = _run_both(cfg, cin, st, rad, desc)
-    assert _compare_exact(a, b) == []
+    assert mismatches(*run_both(cfg, cin, st, rad, desc)) == []
 
 
 def test_fp64_bitexact_workload0_full(gpu_lib):
     cfg, cin, st, rad, desc = S.workload0(ncrms=16)
-    a, b = _run_both(cfg, cin, st, rad, desc)
-    assert _compare_exact(a, b) == []
+    assert mismatches(*run_both(cfg, cin, st, rad, desc)) == []
+
+
+def test_fp64_bitexact_workload0_moist(gpu_lib):
+    """Supersaturated layers, falling rain and ice: every microphysics branch."""
+    cfg, cin, st, rad, desc = S.workload0(ncrms=4, moist=True)
+    a, b = run_both(cfg, cin, st, rad, desc)
+    assert a[2].cltot.max() > 0 and a[2].precc.max() > 0
+    assert mismatches(a, b) == []
+
+
+def test_fp64_bitexact_workload1(gpu_lib):
+    """64 x 58 columns, dx 1 km, 120 CRM steps."""
+    cfg, cin, st, rad, desc = S.workload1(ncrms=4)
+    assert mismatches(*run_both(cfg, cin, st, rad, desc)) == []
+
+
+def test_fp64_bitexact_workload1_moist(gpu_lib):
+    cfg, cin, st, rad, desc = S.workload1(ncrms=2, moist=True)
+    assert mismatches(*run_both(cfg, cin, st, rad, desc)) == []
+
+
+def test_fp64_bitexact_three_gcm_steps(gpu_lib):
+    """State carried across three calls (igstep 1, 2, 3), as in a GCM run."""
+    cfg, cin, st, rad, desc = S.workload0(ncrms=3, moist=True)
+    st_o, rad_o, st_g, rad_g = st.copy(), rad.copy(), st.copy(), rad.copy()
+    for step in (1, 2, 3):
+        desc.igstep = step
+        rc, _, out_o = oracle.run(cfg, desc, cin, st_o, rad_o)
+        assert rc == 0
+        rc, _, out_g = run_gpu(cfg, cin, st_g, rad_g, desc)
+        assert rc == 0
+        assert mismatches((st_o, rad_o, out_o), (st_g, rad_g, out_g)) == [], step
+
+
+def test_columns_independent_and_ld_padding(gpu_lib):
+    """Per-column mode: a column's result is the same alone and in a batch,
+    and columns beyond ncrms of a padded (ld > ncrms) array are untouched."""
+    cfg, cin, st, rad, desc = S.workload0(ncrms=5, moist=True)
+    st_all = st.copy()
+    rad_all = rad.copy()
+    rc, _, out_all = run_gpu(cfg, cin, st_all, rad_all, desc)
+    assert rc == 0
+    # column 3 alone, inside an ld = 5 array with ncrms = 1 after moving it to slot 0
+    cin1, st1, rad1 = cin.copy(), st.copy(), rad.copy()
+    for b in (cin1, st1, rad1):
+        for n, a in b.arrays().items():
+            a[0] = a[3]
+    d1 = T.call_desc(1, desc.ld, desc.dt_gl, desc.igstep, [4, 0, 0, 0, 0])
+    before = st1.temperature[1:].copy()
+    rc, _, out1 = run_gpu(cfg, cin1, st1, rad1, d1)
+    assert rc == 0
+    assert np.array_equal(st1.temperature[1:], before)
+    for n, a in st_all.arrays().items():
+        assert np.array_equal(a[3], getattr(st1, n)[0]), n
+    for n, a in out_all.arrays().items():
+        assert np.array_equal(a[3], getattr(out1, n)[0]), n
+
+
+def test_cfl_violation_is_reported_per_column(gpu_lib):
+    """kurant() needs > 16 subcycles: the reference aborts the model
+    (kurant.F90:66-75); here only that column reports CRM_ERR_CFL."""
+    cfg, cin, st, rad, desc = S.workload0(ncrms=3)
+    st.w_wind[1, 5, 0, 3] = 400.0
+    st_o = st.copy()
+    rc_o, stat_o, _ = oracle.run(cfg, desc, cin, st_o, rad.copy())
+    rc, stat, _ = run_gpu(cfg, cin, st.copy(), rad.copy(), desc)
+    assert rc == T.CRM_ERR_CFL and rc_o == T.CRM_ERR_CFL
+    assert list(stat) == [0, T.CRM_ERR_CFL, 0]
+    assert list(stat_o) == [0, T.CRM_ERR_CFL, 0]
+
+
+def test_device_path_matches_host_path(gpu_lib):
+    """crm_run_device on device-resident arrays == crm_run on host arrays."""
+    import torch
+    from crm_gb300.device import DeviceCrmArrays
+    cfg, cin, st, rad, desc = S.workload0(ncrms=4, moist=True)
+    st_h, rad_h = st.copy(), rad.copy()
+    rc, _, out_h = run_gpu(cfg, cin, st_h, rad_h, desc)
+    assert rc == 0
+    ctx = _context(cfg)
+    dev = DeviceCrmArrays(cfg, cin, st, rad, desc, desc._keep)
+    ctx.run_device(dev, torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    for n in T.STATE_FIELDS:
+        assert np.array_equal(dev.state_numpy(n), getattr(st_h, n)), n
+    for n, _ in T.OUTPUT_FIELDS:
+        assert np.array_equal(dev.out_numpy(n), getattr(out_h, n)), n
+    assert int(dev.status.sum().item()) == 0
