@@ -6,7 +6,7 @@ Public API:
   CrmConfig, CrmInput, CrmState, CrmRad, CrmOutput   the derived types
   synthetic               seeded idealised GCM columns
 """
-from .types import (CrmConfig, CrmInput, CrmOutput, CrmRad, CrmState,  # noqa: F401
+from .crm_types import (CrmConfig, CrmInput, CrmOutput, CrmRad, CrmState,  # noqa: F401
                     CRM_OK, CRM_FP64, CRM_FP32_MIXED, CRM_PER_COLUMN,
                     CRM_REFERENCE_BATCH, OUTPUT_FIELDS, call_desc)
 from .lib import CrmContext, CrmError, load  # noqa: F401

@@ -17,6 +17,7 @@ PKG = os.path.dirname(HERE)
 CSRC = os.path.join(PKG, 'csrc')
 REPO = os.path.dirname(PKG)
 LIB = os.path.join(HERE, 'libcrm_gb300.so')
+LIB_PROF = os.path.join(HERE, 'libcrm_gb300_prof.so')
 OBJ = os.path.join(PKG, '_build')
 
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
@@ -45,23 +46,28 @@ def _sources():
     return out
 
 
-def up_to_date():
-    if not os.path.exists(LIB):
+def up_to_date(lib=LIB):
+    if not os.path.exists(lib):
         return False
-    t = os.path.getmtime(LIB)
+    t = os.path.getmtime(lib)
     return all(os.path.getmtime(s) <= t for s in _sources())
 
 
-def build(force=False, verbose=False):
-    """Compile the library if any source is newer than it; returns its path."""
-    if not force and up_to_date():
-        return LIB
-    os.makedirs(OBJ, exist_ok=True)
+def build(force=False, verbose=False, phase_timers=False):
+    """Compile the library if any source is newer than it; returns its path.
+    phase_timers=True builds libcrm_gb300_prof.so, whose column kernel also
+    accumulates clock64() cycles per phase (crm_debug_phase_cycles)."""
+    lib = LIB_PROF if phase_timers else LIB
+    if not force and up_to_date(lib):
+        return lib
+    odir = OBJ + ('_prof' if phase_timers else '')
+    os.makedirs(odir, exist_ok=True)
     nvcc = _nvcc()
+    extra = ['-DCRM_PHASE_TIMERS'] if phase_timers else []
 
     def compile_unit(name):
-        obj = os.path.join(OBJ, name + '.o')
-        cmd = [nvcc] + ARCH + COMMON + UNITS[name] + ['-c', os.path.join(CSRC, name + '.cu'), '-o', obj]
+        obj = os.path.join(odir, name + '.o')
+        cmd = [nvcc] + ARCH + COMMON + extra + UNITS[name] + ['-c', os.path.join(CSRC, name + '.cu'), '-o', obj]
         if verbose:
             print(' '.join(cmd), file=sys.stderr)
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -71,14 +77,14 @@ def build(force=False, verbose=False):
 
     with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
         objs = list(ex.map(compile_unit, UNITS))
-    tmp = LIB + '.tmp'
+    tmp = lib + '.tmp'
     cmd = [nvcc] + ARCH + ['-shared', '-o', tmp] + objs
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError('nvcc link failed:\n%s%s' % (r.stdout, r.stderr))
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == '__main__':
-    print(build(force='--force' in sys.argv, verbose=True))
+    print(build(force='--force' in sys.argv, verbose=True, phase_timers='--phase-timers' in sys.argv))

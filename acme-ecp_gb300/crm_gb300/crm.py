@@ -12,7 +12,7 @@ updated in place and crm_output is overwritten, as in the reference.  The
 return value is the per-column status array (all CRM_OK on success); the
 reference stops the model instead (kurant.F90:66-75).
 """
-from . import types as T
+from . import crm_types as T
 from .lib import CrmContext, CrmError
 
 _contexts = {}

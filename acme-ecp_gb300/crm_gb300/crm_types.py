@@ -49,6 +49,13 @@ OUTPUT_FIELDS = (
                          'qp_fall', 'qp_src', 'qp_evp', 't_ls')])
 CRM_NOUT = len(OUTPUT_FIELDS)
 
+# phases timed by a profiling build (enum PhaseId in csrc/crm_kernel.h)
+PHASE_NAMES = ('init', 'kurant', 'buoyancy', 'forcing', 'damping', 'ice_fall', 'bound',
+               'tke', 'adv_mom', 'diff_mom', 'press_rhs', 'fft_fwd', 'tridiag', 'fft_inv',
+               'press_grad', 'adams', 'adv_t', 'adv_qt', 'adv_qp', 'fall1', 'fall2', 'uvw',
+               'diff_t', 'diff_q', 'prec_init', 'cloud', 'prec_proc', 'micro_diag', 'diagnose',
+               'stats', 'final')
+
 INPUT_FIELDS = ('zmid', 'zint', 'tl', 'ql', 'qccl', 'qiil', 'ps', 'pmid',
                 'pint', 'pdel', 'phis', 'ul', 'vl', 'ocnfrac', 'tau00',
                 'wndls', 'bflxls', 'fluxu00', 'fluxv00', 'fluxt00', 'fluxq00')

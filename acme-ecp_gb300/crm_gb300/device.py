@@ -8,7 +8,7 @@ import ctypes as C
 
 import numpy as np
 
-from . import types as T
+from . import crm_types as T
 
 
 def _dev(a, torch, dtype=None):

@@ -9,13 +9,14 @@ import os
 
 import numpy as np
 
-from . import types as T
+from . import crm_types as T
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, 'libcrm_gb300.so')
 
 EXPORTS = ('crm_create', 'crm_destroy', 'crm_run', 'crm_run_device', 'crm_last_launch_count',
-           'crm_last_kernel_ms', 'crm_set_stream', 'crm_status_string', 'crm_version')
+           'crm_last_kernel_ms', 'crm_set_stream', 'crm_status_string', 'crm_version',
+           'crm_debug_phase_cycles')
 
 _lib = None
 
@@ -60,6 +61,8 @@ def load(path=None, build_if_missing=False):
     lib.crm_status_string.argtypes = [C.c_int]
     lib.crm_version.restype = C.c_char_p
     lib.crm_version.argtypes = []
+    lib.crm_debug_phase_cycles.restype = C.c_int
+    lib.crm_debug_phase_cycles.argtypes = [C.c_void_p, C.POINTER(C.c_ulonglong), C.c_int]
     _lib = lib
     return lib
 
@@ -119,6 +122,12 @@ class CrmContext:
                                       C.c_void_p(stream))
         if rc != T.CRM_OK:
             raise CrmError(rc, 'crm_run_device')
+
+    def phase_cycles(self, n=64):
+        """Per-phase cycle counters of a profiling build (None otherwise)."""
+        buf = (C.c_ulonglong * n)()
+        m = self._lib.crm_debug_phase_cycles(self._h, buf, n)
+        return None if m < 0 else [int(buf[i]) for i in range(m)]
 
     @property
     def last_kernel_ms(self):

@@ -24,7 +24,7 @@ import os
 
 import numpy as np
 
-from .types import CrmConfig, CrmInput, CrmRad, CrmState, call_desc
+from .crm_types import CrmConfig, CrmInput, CrmRad, CrmState, call_desc
 
 CPAIR = 1.00464e3
 GRAV = 9.80616

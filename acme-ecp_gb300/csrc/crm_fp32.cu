@@ -5,5 +5,5 @@
 
 namespace crm {
 template void launch_crm_columns<float>(const KParams &, int, int, cudaStream_t);
-template int occupancy_crm_columns<float>(int);
+template int occupancy_crm_columns<float>(int, int, int);
 }

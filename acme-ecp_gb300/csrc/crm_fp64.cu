@@ -5,5 +5,5 @@
 
 namespace crm {
 template void launch_crm_columns<double>(const KParams &, int, int, cudaStream_t);
-template int occupancy_crm_columns<double>(int);
+template int occupancy_crm_columns<double>(int, int, int);
 }

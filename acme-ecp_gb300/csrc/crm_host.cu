@@ -42,6 +42,7 @@ struct crm_ctx {
   double *d_consts = nullptr;    // trigs, eign
   double *d_colconst = nullptr;  // z0 (ncrms), rnd (ncrms * 5 * nx)
   int *d_status = nullptr;
+  unsigned long long *d_phase = nullptr;   // per-CTA phase cycle counters
   int ld_cap = 0;
   // host-side constants
   std::vector<double> trigs, eign;
@@ -149,10 +150,10 @@ int alloc_ctx(crm_ctx *c) {
   const crm_config &g = c->cfg;
   CK(cudaGetDevice(&c->device));
   CK(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, c->device));
-  c->L = crm::make_layout(g.crm_nx, g.crm_nz, g.plev, g.crm_nx_rad);
   const size_t esz = g.precision == CRM_FP64 ? sizeof(double) : sizeof(float);
-  int per_sm = g.precision == CRM_FP64 ? crm::occupancy_crm_columns<double>(c->block)
-                                       : crm::occupancy_crm_columns<float>(c->block);
+  c->L = crm::make_layout(g.crm_nx, g.crm_nz, g.plev, g.crm_nx_rad, (int)esz);
+  int per_sm = g.precision == CRM_FP64 ? crm::occupancy_crm_columns<double>(c->block, g.crm_nx, g.crm_nz)
+                                       : crm::occupancy_crm_columns<float>(c->block, g.crm_nx, g.crm_nz);
   if (per_sm < 1) per_sm = 1;
   c->grid_max = c->nsm * per_sm;
   if (c->grid_max > g.max_ncrms) c->grid_max = g.max_ncrms;
@@ -190,6 +191,10 @@ int alloc_ctx(crm_ctx *c) {
   CK(cudaMemcpy(c->d_consts + c->trigs.size(), c->eign.data(), sizeof(double) * c->eign.size(), cudaMemcpyHostToDevice));
   CK(cudaMalloc(&c->d_colconst, sizeof(double) * (size_t)ld * (1 + 5 * nx)));
   CK(cudaMalloc(&c->d_status, sizeof(int) * (size_t)ld));
+#ifdef CRM_PHASE_TIMERS
+  CK(cudaMalloc(&c->d_phase, sizeof(unsigned long long) * 64 * (size_t)c->grid_max));
+  CK(cudaMemset(c->d_phase, 0, sizeof(unsigned long long) * 64 * (size_t)c->grid_max));
+#endif
   // gamma functions and fall speeds (precip_init.F90:25-49, microphysics.F90:500-507)
   const double b_rain = R4H(0.8), b_snow = 0.25, b_grau = 0.5;
   c->gam[0] = gammafff(3.f);
@@ -218,6 +223,7 @@ void free_ctx(crm_ctx *c) {
   if (!c) return;
   cudaFree(c->slabs); cudaFree(c->d_in); cudaFree(c->d_state); cudaFree(c->d_rad);
   cudaFree(c->d_out); cudaFree(c->d_consts); cudaFree(c->d_colconst); cudaFree(c->d_status);
+  if (c->d_phase) cudaFree(c->d_phase);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -279,6 +285,7 @@ int enqueue(crm_ctx *c, const crm_call_desc *d, const crm_input_c *in, crm_state
   for (int f = 0; f < 5; ++f) p.radout[f] = rp[f];
   for (int f = 0; f < CRM_NOUT; ++f) p.out[f] = out->field[f];
   p.slabs = c->slabs;
+  p.phase_cycles = c->d_phase;
   p.col_status = d_status ? d_status : c->d_status;
   int grid = ncrms < c->grid_max ? ncrms : c->grid_max;
   CK(cudaEventRecord(c->ev0, s));
@@ -359,6 +366,23 @@ const char *crm_status_string(int s) {
     case CRM_ERR_NO_DEVICE: return "no CUDA device";
   }
   return "unknown status";
+}
+
+// Per-phase cycle counters summed over the CTAs (profiling builds only,
+// -DCRM_PHASE_TIMERS); returns the number of phases written or -1.
+int crm_debug_phase_cycles(crm_ctx *ctx, unsigned long long *out, int n) {
+  if (!ctx || !ctx->d_phase || !out) return -1;
+  std::vector<unsigned long long> h((size_t)64 * ctx->grid_max);
+  if (cudaMemcpy(h.data(), ctx->d_phase, sizeof(unsigned long long) * h.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return -1;
+  int m = n < crm::PH_COUNT ? n : crm::PH_COUNT;
+  for (int i = 0; i < m; ++i) {
+    unsigned long long s = 0;
+    for (int b = 0; b < ctx->grid_max; ++b) s += h[(size_t)b * 64 + i];
+    out[i] = s;
+  }
+  cudaMemset(ctx->d_phase, 0, sizeof(unsigned long long) * h.size());
+  return m;
 }
 
 const char *crm_version(void) { return "crm-gb300 0.1 (sm_103a; 2D sam1mom; fp64 plain + fp32 mixed)"; }

@@ -58,6 +58,21 @@ namespace crm {
 #define C_THERCO R4(2.40e-02)
 #define C_MUELQ R4(1.717e-05)
 
+#ifdef CRM_PHASE_TIMERS
+#define PHASE_MARK(id)                                                          \
+  do {                                                                          \
+    if (threadIdx.x == 0) {                                                     \
+      unsigned long long t_ = clock64();                                        \
+      p.phase_cycles[(size_t)blockIdx.x * 64 + (id)] += t_ - S.t_last;          \
+      S.t_last = t_;                                                            \
+    }                                                                           \
+  } while (0)
+#else
+#define PHASE_MARK(id) \
+  do {                 \
+  } while (0)
+#endif
+
 #define TID ((int)threadIdx.x)
 #define NT ((int)blockDim.x)
 #define SYNC __syncthreads()
@@ -69,6 +84,7 @@ struct ColShared {
   double colprec0, colprecs0;
   double cltot, clhgh, clmed, cllow;
   int jt_min, mx_max;
+  unsigned long long t_last;
   double red_d[32];
   int red_i[64];
 };
@@ -118,6 +134,55 @@ struct ColumnKernel {
   }
 
   // ---------------------------------------------------------- reductions
+  // Horizontal sums for every level k in [k0, k1] and quantity q < nq:
+  // out(q, k, s) receives s = init(q, k) + sum over i = 1..nx of term(q, i, k).
+  // FP64 form: one thread per (q, k) adding in the reference's loop order,
+  // so the result is bit-identical to a sequential CPU evaluation.
+  // FP32-mixed form: one warp per (q, k); each lane adds its (at most four)
+  // cells in FP32, groups of four lanes combine in FP32, and the FP64 tree
+  // across the eight groups accumulates into the FP64 result.
+  // Must be called by the whole CTA; results are visible after a barrier.
+  template <typename Term, typename Init, typename Out>
+  __device__ void level_sums(int nq, int k0, int k1, Term term, Init init, Out out) {
+    const int nk = k1 - k0 + 1, npairs = nq * nk;
+    if constexpr (sizeof(T) == 8) {
+      for (int e = TID; e < npairs; e += NT) {
+        int q = e / nk, k = k0 + e % nk;
+        double s = init(q, k);
+        for (int i = 1; i <= nx; ++i) s = s + (double)term(q, i, k);
+        out(q, k, s);
+      }
+    } else {
+      const int lane = TID & 31, warp = TID >> 5, nw = NT >> 5;
+      for (int e = warp; e < npairs; e += nw) {
+        int q = e / nk, k = k0 + e % nk;
+        T part = (T)0;
+        for (int i = 1 + lane; i <= nx; i += 32) part = part + term(q, i, k);
+        part = part + __shfl_xor_sync(0xffffffffu, part, 1);
+        part = part + __shfl_xor_sync(0xffffffffu, part, 2);
+        double sd = (double)part;
+        sd = sd + __shfl_xor_sync(0xffffffffu, sd, 4);
+        sd = sd + __shfl_xor_sync(0xffffffffu, sd, 8);
+        sd = sd + __shfl_xor_sync(0xffffffffu, sd, 16);
+        if (lane == 0) out(q, k, init(q, k) + sd);
+      }
+    }
+  }
+  // Horizontal maxima (order-independent, hence exact in both forms): one
+  // warp per (q, k) with a shuffle tree.
+  template <typename Term, typename Out>
+  __device__ void level_max(int nq, int k0, int k1, Term term, Out out) {
+    const int nk = k1 - k0 + 1, npairs = nq * nk;
+    const int lane = TID & 31, warp = TID >> 5, nw = NT >> 5;
+    for (int e = warp; e < npairs; e += nw) {
+      int q = e / nk, k = k0 + e % nk;
+      T m = (T)0;
+      for (int i = 1 + lane; i <= nx; i += 32) m = mx2(m, term(q, i, k));
+      for (int o = 16; o > 0; o >>= 1) m = mx2(m, __shfl_xor_sync(0xffffffffu, m, o));
+      if (lane == 0) out(q, k, m);
+    }
+  }
+
   __device__ double block_max(double v) {
     for (int o = 16; o > 0; o >>= 1) v = mx2(v, __shfl_xor_sync(0xffffffffu, v, o));
     SYNC;
@@ -343,6 +408,8 @@ struct ColumnKernel {
       PR(P_GRDFY)[k] = mn2((T)16., (T)p.dy * (T)p.dy / (adzdz * adzdz));
       PR(P_GRDFZ)[k] = (T)1.;
     }
+    SYNC;
+    tridiag_factor();
     // t from tabs (crm_module.F90:508-509)
     F2<T> t = TT(), qcl = QCL(), qci = QCI(), qpl = QPL(), qpi = QPI(), qv = QV();
     for (int e = TID; e < nx * nzm; e += NT) {
@@ -354,24 +421,33 @@ struct ColumnKernel {
     // initial domain means (crm_module.F90:500-546)
     const double factor_xy = 1.0 / (double)nx;
     const double idt_gl = 1.0 / p.dt_gl;
+    double *md = reinterpret_cast<double *>(base + p.L.s_a);   // FP64 copies of the means
+    {
+      const int ids[9] = {P_U0, P_V0, P_T0, P_T00, P_TABS0, P_Q0, P_QV0, P_QN0, P_QP0};
+      level_sums(9, 1, nzm,
+                 [&](int q, int i, int k) -> T {
+                   switch (q) {
+                     case 0: return u(i, k);
+                     case 1: return v(i, k);
+                     case 2: return t(i, k);
+                     case 3: return t(i, k) + (T)C_FAC_COND * qpl(i, k) + (T)C_FAC_SUB * qpi(i, k);
+                     case 4: return tabs(i, k);
+                     case 5: return qv(i, k) + qcl(i, k) + qci(i, k);
+                     case 6: return qv(i, k);
+                     case 7: return qcl(i, k) + qci(i, k);
+                     default: return qpl(i, k) + qpi(i, k);
+                   }
+                 },
+                 [&](int, int) { return 0.; },
+                 [&](int q, int k, double sv) {
+                   PR(ids[q])[k] = (T)(sv * factor_xy);
+                   md[(size_t)q * (nz + 2) + k] = sv * factor_xy;
+                 });
+    }
+    SYNC;
     for (int k = TID + 1; k <= nzm; k += NT) {
-      double u0 = 0, v0 = 0, t0 = 0, t00 = 0, tabs0 = 0, q0 = 0, qv0 = 0, qn0 = 0, qp0 = 0;
-      for (int i = 1; i <= nx; ++i) {
-        u0 = u0 + (double)u(i, k);
-        v0 = v0 + (double)v(i, k);
-        t0 = t0 + (double)t(i, k);
-        t00 = t00 + (double)(t(i, k) + (T)C_FAC_COND * qpl(i, k) + (T)C_FAC_SUB * qpi(i, k));
-        tabs0 = tabs0 + (double)tabs(i, k);
-        q0 = q0 + (double)(qv(i, k) + qcl(i, k) + qci(i, k));
-        qv0 = qv0 + (double)qv(i, k);
-        qn0 = qn0 + (double)(qcl(i, k) + qci(i, k));
-        qp0 = qp0 + (double)(qpl(i, k) + qpi(i, k));
-      }
-      u0 *= factor_xy; v0 *= factor_xy; t0 *= factor_xy; t00 *= factor_xy; tabs0 *= factor_xy;
-      q0 *= factor_xy; qv0 *= factor_xy; qn0 *= factor_xy; qp0 *= factor_xy;
-      PR(P_U0)[k] = (T)u0; PR(P_V0)[k] = (T)v0; PR(P_T0)[k] = (T)t0; PR(P_T00)[k] = (T)t00;
-      PR(P_TABS0)[k] = (T)tabs0; PR(P_Q0)[k] = (T)q0; PR(P_QV0)[k] = (T)qv0; PR(P_QN0)[k] = (T)qn0;
-      PR(P_QP0)[k] = (T)qp0;
+      double u0 = md[k], v0 = md[(nz + 2) + k], t00 = md[3 * (nz + 2) + k];
+      double q0 = md[5 * (nz + 2) + k];
       int l = plev_ - k + 1;
       double uln = mn2(umax, mx2(-umax, IN(p.ul, l)));
       double vln = mn2(umax, mx2(-umax, IN(p.vl, l))) * 0.0;
@@ -421,16 +497,13 @@ struct ColumnKernel {
   __device__ void kurant() {
     F2<T> u = U(), v = V(), w = W(), tkh = TKH();
     T *wm = PR(P_TMP0), *uhm = PR(P_TMP1), *tkhm = PR(P_TMP2);
-    for (int k = TID + 1; k <= nzm; k += NT) {
-      T a = (T)0., b = (T)0., c = (T)0.;
-      for (int i = 1; i <= nx; ++i) {
-        a = mx2(a, tabs_(w(i, k)));
-        T uu = u(i, k), vv = v(i, k);
-        b = mx2(b, tsqrt(uu * uu + (T)0. * (vv * vv)));
-        c = mx2(c, tkh(i, k));
-      }
-      wm[k] = a; uhm[k] = b; tkhm[k] = c;
-    }
+    level_max(3, 1, nzm,
+              [&](int q, int i, int k) -> T {
+                if (q == 0) return tabs_(w(i, k));
+                if (q == 1) { T uu = u(i, k), vv = v(i, k); return tsqrt(uu * uu + (T)0. * (vv * vv)); }
+                return tkh(i, k);
+              },
+              [&](int q, int k, T m) { (q == 0 ? wm : q == 1 ? uhm : tkhm)[k] = m; });
     if (TID == 0) wm[nz] = (T)0.;
     SYNC;
     double cfl = 0.;
@@ -510,18 +583,19 @@ struct ColumnKernel {
       dv(i, k) = dv(i, k) + vtend[k];
     }
     SYNC;
-    // negative-vapour fixer: per-level sums in the reference's order
+    // negative-vapour fixer: per-level sums (a cell outside a sum adds an
+    // exact zero, which leaves a sum that starts at +0 unchanged)
     T *qneg = PR(P_TMP0), *qpoz = PR(P_TMP1), *nneg = PR(P_TMP2);
-    for (int k = TID + 1; k <= nzm; k += NT) {
-      double sn = 0., sp = 0.;
-      int cnt = 0;
-      for (int i = 1; i <= nx; ++i) {
-        T q = qt(i, k);
-        if (q < (T)0.) { cnt += 1; sn = sn + (double)q; }
-        else sp = sp + (double)q;
-      }
-      qneg[k] = (T)sn; qpoz[k] = (T)sp; nneg[k] = (T)cnt;
-    }
+    level_sums(3, 1, nzm,
+               [&](int q, int i, int k) -> T {
+                 T v = qt(i, k);
+                 bool neg = v < (T)0.;
+                 if (q == 0) return neg ? v : (T)0.;
+                 if (q == 1) return neg ? (T)0. : v;
+                 return neg ? (T)1. : (T)0.;
+               },
+               [&](int, int) { return 0.; },
+               [&](int q, int k, double sv) { (q == 0 ? qneg : q == 1 ? qpoz : nneg)[k] = (T)sv; });
     SYNC;
     const int gx = nx / p.L.nx_rad;
     const double *qrad = p.qrad;
@@ -557,14 +631,11 @@ struct ColumnKernel {
         T tk = (T)60. * tpow((T)450. / (T)60., (z[nzm] - z[k]) / (z[nzm] - z[nzm - n_damp]));
         tau[k] = (T)1. / tk;
       }
-      double su = 0., sv = 0., st = 0.;
-      for (int i = 1; i <= nx; ++i) {
-        su = su + (double)(u(i, k) / nxy);
-        sv = sv + (double)(v(i, k) / nxy);
-        st = st + (double)(t(i, k) / nxy);
-      }
-      u0l[k] = (T)su; v0l[k] = (T)sv; t0l[k] = (T)st;
     }
+    level_sums(3, 1, nzm,
+               [&](int q, int i, int k) -> T { return (q == 0 ? u(i, k) : q == 1 ? v(i, k) : t(i, k)) / nxy; },
+               [&](int, int) { return 0.; },
+               [&](int q, int k, double sv) { (q == 0 ? u0l : q == 1 ? v0l : t0l)[k] = (T)sv; });
     SYNC;
     F2<T> w = W(), qt = QT(), qv = QV(), du = DU(S.na), dv = DV(S.na), dw = DW(S.na);
     const T dtn = (T)S.dtn;
@@ -815,12 +886,10 @@ struct ColumnKernel {
     }
     SYNC;
     T *uwle = PR(P_UWLE), *vwle = PR(P_VWLE);
-    for (int k = TID + 1; k <= nz; k += NT) {
-      double su = 0., sv = 0.;
-      if (k >= 2 && k <= nzm)
-        for (int i = 1; i <= nx; ++i) { su = su + (double)fuz(i, k); sv = sv + (double)fvz(i, k); }
-      uwle[k] = (T)su; vwle[k] = (T)sv;
-    }
+    if (TID == 0) { uwle[1] = (T)0.; vwle[1] = (T)0.; uwle[nz] = (T)0.; vwle[nz] = (T)0.; }
+    level_sums(2, 2, nzm, [&](int q, int i, int k) -> T { return q == 0 ? fuz(i, k) : fvz(i, k); },
+               [&](int, int) { return 0.; },
+               [&](int q, int k, double sv) { (q == 0 ? uwle : vwle)[k] = (T)sv; });
     for (int e = TID; e < nx * nzm; e += NT) {
       int i = 1 + e % nx, k = 1 + e / nx;
       int kc = k + 1;
@@ -901,11 +970,9 @@ struct ColumnKernel {
     }
     SYNC;
     T *uwsb = PR(P_UWSB), *vwsb = PR(P_VWSB);
-    for (int k = TID + 1; k <= nzm; k += NT) {
-      double su = 0., sv = 0.;
-      for (int i = 1; i <= nx; ++i) { su = su + (double)fu(i, k); sv = sv + (double)fv(i, k); }
-      uwsb[k] = (T)su; vwsb[k] = (T)sv;
-    }
+    level_sums(2, 1, nzm, [&](int q, int i, int k) -> T { return q == 0 ? fu(i, k) : fv(i, k); },
+               [&](int, int) { return 0.; },
+               [&](int q, int k, double sv) { (q == 0 ? uwsb : vwsb)[k] = (T)sv; });
     for (int e = TID; e < nx * nzm; e += NT) {
       int i = 1 + e % nx, k = 1 + e / nx;
       int kc = k + 1;
@@ -921,66 +988,74 @@ struct ColumnKernel {
   }
 
   // ---------------------------------------------------------- FFT
-  // One pass of the real/half-complex transform of crm/fft.F90
-  // (vpassm_crm :466-806, lot = 1), radix 2 and 4; twiddles are REAL*4.
-  __device__ void vpass(const T *A, T *C, int nh, int ifac, int la) const {
+  // Real/half-complex transform of crm/fft.F90 (fft991_crm :5-154 with
+  // fft99a/b :301-465 and vpassm_crm :466-806, radix 2 and 4, lot = 1) for
+  // one row held in shared memory, computed by one warp: within each pass
+  // every butterfly is independent, so lanes take butterflies and the warp
+  // synchronises between passes.  Each output keeps the reference's
+  // expression, so results are identical to a sequential evaluation.
+  // Twiddle factors are REAL*4 values (fft.F90 has no implicit none).
+  __device__ void vpass_warp(const T *A, T *C, int nh, int ifac, int la, int lane) const {
     const double *trigs = p.trigs;
-    int m = nh / ifac;
-    int ngroups = m / la;
-    for (int g = 0; g < ngroups; ++g) {
-      T c1 = 1, s1 = 0, c2 = 1, s2 = 0, c3 = 1, s3 = 0;
+    const int m = nh / ifac;
+    for (int bf = lane; bf < m; bf += 32) {
+      int g = bf / la, l = bf - g * la;
+      int pp = g * la + l, q = g * ifac * la + l;
       int kb = 2 * g * la;
-      if (g > 0) {
-        c1 = (T)trigs[kb]; s1 = (T)trigs[kb + 1];
-        c2 = (T)trigs[2 * kb]; s2 = (T)trigs[2 * kb + 1];
-        if (ifac == 4) { c3 = (T)trigs[3 * kb]; s3 = (T)trigs[3 * kb + 1]; }
-      }
-      for (int l = 0; l < la; ++l) {
-        int pp = g * la + l, q = g * ifac * la + l;
-        T a0 = A[2 * pp], b0 = A[2 * pp + 1], a1 = A[2 * (pp + m)], b1 = A[2 * (pp + m) + 1];
-        if (ifac == 2) {
-          C[2 * q] = a0 + a1; C[2 * q + 1] = b0 + b1;
-          if (g == 0) { C[2 * (q + la)] = a0 - a1; C[2 * (q + la) + 1] = b0 - b1; }
-          else {
-            C[2 * (q + la)] = c1 * (a0 - a1) - s1 * (b0 - b1);
-            C[2 * (q + la) + 1] = s1 * (a0 - a1) + c1 * (b0 - b1);
-          }
-        } else {  // 4
-          T a2 = A[2 * (pp + 2 * m)], b2 = A[2 * (pp + 2 * m) + 1];
-          T a3 = A[2 * (pp + 3 * m)], b3 = A[2 * (pp + 3 * m) + 1];
-          T *C0 = C + 2 * q, *C1 = C + 2 * (q + la), *C2 = C + 2 * (q + 2 * la), *C3 = C + 2 * (q + 3 * la);
-          if (g == 0) {
-            C0[0] = (a0 + a2) + (a1 + a3); C2[0] = (a0 + a2) - (a1 + a3);
-            C0[1] = (b0 + b2) + (b1 + b3); C2[1] = (b0 + b2) - (b1 + b3);
-            C1[0] = (a0 - a2) - (b1 - b3); C3[0] = (a0 - a2) + (b1 - b3);
-            C1[1] = (b0 - b2) + (a1 - a3); C3[1] = (b0 - b2) - (a1 - a3);
-          } else {
-            C0[0] = (a0 + a2) + (a1 + a3); C0[1] = (b0 + b2) + (b1 + b3);
-            C2[0] = c2 * ((a0 + a2) - (a1 + a3)) - s2 * ((b0 + b2) - (b1 + b3));
-            C2[1] = s2 * ((a0 + a2) - (a1 + a3)) + c2 * ((b0 + b2) - (b1 + b3));
-            C1[0] = c1 * ((a0 - a2) - (b1 - b3)) - s1 * ((b0 - b2) + (a1 - a3));
-            C1[1] = s1 * ((a0 - a2) - (b1 - b3)) + c1 * ((b0 - b2) + (a1 - a3));
-            C3[0] = c3 * ((a0 - a2) + (b1 - b3)) - s3 * ((b0 - b2) - (a1 - a3));
-            C3[1] = s3 * ((a0 - a2) + (b1 - b3)) + c3 * ((b0 - b2) - (a1 - a3));
-          }
+      T a0 = A[2 * pp], b0 = A[2 * pp + 1], a1 = A[2 * (pp + m)], b1 = A[2 * (pp + m) + 1];
+      if (ifac == 2) {
+        C[2 * q] = a0 + a1; C[2 * q + 1] = b0 + b1;
+        if (g == 0) { C[2 * (q + la)] = a0 - a1; C[2 * (q + la) + 1] = b0 - b1; }
+        else {
+          T c1 = (T)trigs[kb], s1 = (T)trigs[kb + 1];
+          C[2 * (q + la)] = c1 * (a0 - a1) - s1 * (b0 - b1);
+          C[2 * (q + la) + 1] = s1 * (a0 - a1) + c1 * (b0 - b1);
+        }
+      } else {  // 4
+        T a2 = A[2 * (pp + 2 * m)], b2 = A[2 * (pp + 2 * m) + 1];
+        T a3 = A[2 * (pp + 3 * m)], b3 = A[2 * (pp + 3 * m) + 1];
+        T *C0 = C + 2 * q, *C1 = C + 2 * (q + la), *C2 = C + 2 * (q + 2 * la), *C3 = C + 2 * (q + 3 * la);
+        if (g == 0) {
+          C0[0] = (a0 + a2) + (a1 + a3); C2[0] = (a0 + a2) - (a1 + a3);
+          C0[1] = (b0 + b2) + (b1 + b3); C2[1] = (b0 + b2) - (b1 + b3);
+          C1[0] = (a0 - a2) - (b1 - b3); C3[0] = (a0 - a2) + (b1 - b3);
+          C1[1] = (b0 - b2) + (a1 - a3); C3[1] = (b0 - b2) - (a1 - a3);
+        } else {
+          T c1 = (T)trigs[kb], s1 = (T)trigs[kb + 1];
+          T c2 = (T)trigs[2 * kb], s2 = (T)trigs[2 * kb + 1];
+          T c3 = (T)trigs[3 * kb], s3 = (T)trigs[3 * kb + 1];
+          C0[0] = (a0 + a2) + (a1 + a3); C0[1] = (b0 + b2) + (b1 + b3);
+          C2[0] = c2 * ((a0 + a2) - (a1 + a3)) - s2 * ((b0 + b2) - (b1 + b3));
+          C2[1] = s2 * ((a0 + a2) - (a1 + a3)) + c2 * ((b0 + b2) - (b1 + b3));
+          C1[0] = c1 * ((a0 - a2) - (b1 - b3)) - s1 * ((b0 - b2) + (a1 - a3));
+          C1[1] = s1 * ((a0 - a2) - (b1 - b3)) + c1 * ((b0 - b2) + (a1 - a3));
+          C3[0] = c3 * ((a0 - a2) + (b1 - b3)) - s3 * ((b0 - b2) - (a1 - a3));
+          C3[1] = s3 * ((a0 - a2) + (b1 - b3)) + c3 * ((b0 - b2) - (a1 - a3));
         }
       }
     }
+    __syncwarp();
   }
-  // fft991_crm (fft.F90:5-154) on a[0..n+1], lot = 1; isign -1: grid ->
-  // spectral, +1: spectral -> grid.
-  __device__ void fft991(T *a, T *work, int n, int isign) const {
+  // fft991_crm on a[0..n+1] (shared memory), work[0..n+1]; isign -1: grid
+  // point -> spectral, +1: spectral -> grid point.  Called by a whole warp.
+  __device__ void fft991_warp(T *a, T *work, int n, int isign, int lane) const {
     const double *trigs = p.trigs;
-    int nfax = p.nfax, nh = n / 2;
+    const int nfax = p.nfax, nh = n / 2, npair = (nh - 1) / 2;   // k = 3,5,..,nh
     bool in_work;
     if (isign == -1) {
       if (nfax % 2 == 1) in_work = false;
-      else { for (int m = 0; m < n; ++m) work[m] = a[m]; in_work = true; }
+      else {
+        for (int m = lane; m < n; m += 32) work[m] = a[m];
+        in_work = true;
+      }
     } else {
-      work[0] = a[0] + a[n];
-      work[1] = a[0] - a[n];
-      int ia = 2, ib = n - 2;
-      for (int k = 3; k <= nh; k += 2) {
+      // fft99a_crm: a -> work
+      if (lane == 0) {
+        work[0] = a[0] + a[n];
+        work[1] = a[0] - a[n];
+      }
+      for (int t = lane; t < npair; t += 32) {
+        int k = 3 + 2 * t, ia = 2 + 2 * t, ib = n - 2 - 2 * t;
         T c = (T)trigs[n + k - 1], s = (T)trigs[n + k];
         T ap = a[ia] + a[ib], am = a[ia] - a[ib];
         T bp = a[ia + 1] + a[ib + 1], bm = a[ia + 1] - a[ib + 1];
@@ -988,28 +1063,36 @@ struct ColumnKernel {
         work[ib] = ap + (s * am + c * bp);
         work[ia + 1] = (c * am - s * bp) + bm;
         work[ib + 1] = (c * am - s * bp) - bm;
-        ia += 2; ib -= 2;
       }
-      if (ia == ib) { work[ia] = (T)2.0 * a[ia]; work[ia + 1] = (T)-2.0 * a[ia + 1]; }
+      {
+        int ia = 2 + 2 * npair, ib = n - 2 - 2 * npair;
+        if (ia == ib && lane == 0) { work[ia] = (T)2.0 * a[ia]; work[ia + 1] = (T)-2.0 * a[ia + 1]; }
+      }
       in_work = true;
     }
+    __syncwarp();
     int la = 1;
     for (int k = 1; k <= nfax; ++k) {
-      if (in_work) vpass(work, a, nh, p.ifax[k], la);
-      else vpass(a, work, nh, p.ifax[k], la);
+      if (in_work) vpass_warp(work, a, nh, p.ifax[k], la, lane);
+      else vpass_warp(a, work, nh, p.ifax[k], la, lane);
       in_work = !in_work;
       la *= p.ifax[k];
     }
     if (isign == -1) {
+      // fft99b_crm: work -> a
       float scale = (float)(1.0 / (double)n);
-      a[0] = (T)(double)scale * (work[0] + work[1]);
-      a[n] = (T)(double)scale * (work[0] - work[1]);
-      a[1] = (T)0.0;
-      a[n + 1] = (T)0.0;
-      scale = 0.5f * scale;
-      T sc = (T)(double)scale;
-      int ia = 2, ib = n - 2;
-      for (int k = 3; k <= nh; k += 2) {
+      const T sc0 = (T)(double)scale;
+      const T sc = (T)(double)(0.5f * scale);
+      const T sc2 = (T)(double)(2.0f * (0.5f * scale));
+      if (lane == 0) {
+        T w0 = work[0], w1 = work[1];
+        a[0] = sc0 * (w0 + w1);
+        a[n] = sc0 * (w0 - w1);
+        a[1] = (T)0.0;
+        a[n + 1] = (T)0.0;
+      }
+      for (int t = lane; t < npair; t += 32) {
+        int k = 3 + 2 * t, ia = 2 + 2 * t, ib = n - 2 - 2 * t;
         T c = (T)trigs[n + k - 1], s = (T)trigs[n + k];
         T wp = work[ia] + work[ib], wm = work[ia] - work[ib];
         T vp = work[ia + 1] + work[ib + 1], vm = work[ib + 1] - work[ia + 1];
@@ -1017,24 +1100,65 @@ struct ColumnKernel {
         a[ib] = sc * (wp - (c * vp + s * wm));
         a[ia + 1] = sc * ((c * wm - s * vp) + vm);
         a[ib + 1] = sc * ((c * wm - s * vp) - vm);
-        ia += 2; ib -= 2;
       }
-      if (ia == ib) {
-        scale = 2.0f * scale;
-        a[ia] = (T)(double)scale * work[ia];
-        a[ia + 1] = -(T)(double)scale * work[ia + 1];
+      {
+        int ia = 2 + 2 * npair, ib = n - 2 - 2 * npair;
+        if (ia == ib && lane == 0) {
+          a[ia] = sc2 * work[ia];
+          a[ia + 1] = -sc2 * work[ia + 1];
+        }
       }
     } else {
-      if (in_work) for (int m = 0; m < n; ++m) a[m] = work[m];
-      a[n] = (T)0.0;
-      a[n + 1] = (T)0.0;
+      if (in_work)
+        for (int m = lane; m < n; m += 32) a[m] = work[m];
+      if (lane == 0) { a[n] = (T)0.0; a[n + 1] = (T)0.0; }
     }
+    __syncwarp();
   }
 
   // ---------------------------------------------------------- pressure
+  // Tridiagonal factors of the vertical Poisson operator per Fourier
+  // coefficient (pressure.F90:200-236).  They depend only on the column's
+  // grid and the eigenvalues, so they are formed once per call: alfa(k) and
+  // the reciprocal pivots e(k) exactly as the reference computes them every
+  // substep, the last pivot kept as a divisor.
+  __device__ double *TRI() const { return reinterpret_cast<double *>(base + p.L.tri); }
+  __device__ void tridiag_factor() {
+    const int np = nx + 1, ls = nzm + 1;
+    double *tri = TRI();        // [a(k)] + np x ([alfa(k)] [e(k)]) + np last pivots
+    double *ak = tri;
+    T *rho = PR(P_RHO), *rhow = PR(P_RHOW), *adz = PR(P_ADZ), *adzw = PR(P_ADZW);
+    const double dz = S.dz;
+    for (int k = TID + 1; k <= nzm; k += NT)
+      ak[k] = (double)rhow[k] / ((double)adz[k] * (double)adzw[k] * dz * dz);
+    SYNC;
+    for (int i = TID + 1; i <= np; i += NT) {
+      double *al = tri + (size_t)ls + (size_t)(i - 1) * 2 * ls, *e = al + ls;
+      int id = (int)(((float)i - 0.1f) / 2.0f);
+      double eign = p.eign[i - 1];
+      double a1 = ak[1];
+      double c1 = (double)rhow[2] / ((double)adz[1] * (double)adzw[2] * dz * dz);
+      double b;
+      if (id == 0) b = 1. / (eign * (double)rho[1] - a1 - c1);
+      else b = 1. / (eign * (double)rho[1] - c1);
+      al[1] = -c1 * b;
+      e[1] = b;
+      for (int k = 2; k <= nzm - 1; ++k) {
+        double a = ak[k];
+        double c = (double)rhow[k + 1] / ((double)adz[k] * (double)adzw[k + 1] * dz * dz);
+        double ee = 1. / (eign * (double)rho[k] - a - c + a * al[k - 1]);
+        al[k] = -c * ee;
+        e[k] = ee;
+      }
+      double an = ak[nzm];
+      tri[(size_t)ls + (size_t)np * 2 * ls + (i - 1)] = eign * (double)rho[nzm] - an + an * al[nzm - 1];
+    }
+    SYNC;
+  }
+
   // pressure.F90:97-310, press_rhs.F90:48-101, press_grad.F90:18-72,
-  // bound_duvdt.F90 (2D)
-  __device__ void pressure() {
+  // bound_duvdt.F90 (2D); the Fourier coefficients live in shared memory
+  __device__ void pressure(T *fsh, T *wsh) {
     F2<T> u = U(), w = W(), pp = PP();
     F2<T> dua = DU(S.na), dub = DU(S.nb), duc = DU(S.nc);
     F2<T> dwa = DW(S.na), dwb = DW(S.nb), dwc = DW(S.nc);
@@ -1045,8 +1169,7 @@ struct ColumnKernel {
     const T rdx = (T)1. / (T)p.dx;
     const T btat = (T)(S.bt / S.at), ctat = (T)(S.ct / S.at);
     const T dta = (T)(1. / S.dt3[S.na - 1] / S.at);
-    const int nx2 = nx + 2, nwk = nx + 4;
-    T *fbuf = base + p.L.fft_f, *wbuf = base + p.L.fft_w;
+    const int nx2 = nx + 2;
     for (int e = TID; e < nx * nzm; e += NT) {
       int i = 1 + e % nx, k = 1 + e / nx;
       int kc = k + 1, ic = i + 1;
@@ -1057,47 +1180,46 @@ struct ColumnKernel {
             (rdx * (dua(ic, k) - dua(i, k)) + (dwa(i, kc) * rup - dwa(i, k) * rdn)) +
             btat * (rdx * (dub(ic, k) - dub(i, k)) + (dwb(i, kc) * rup - dwb(i, k) * rdn)) +
             ctat * (rdx * (duc(ic, k) - duc(i, k)) + (dwc(i, kc) * rup - dwc(i, k) * rdn));
-      fbuf[(size_t)nx2 * k + (i - 1)] = r * rho[k];
+      fsh[(size_t)nx2 * (k - 1) + (i - 1)] = r * rho[k];
     }
     SYNC;
-    for (int k = TID + 1; k <= nzm; k += NT) fft991(fbuf + (size_t)nx2 * k, wbuf + (size_t)nwk * k, nx, -1);
+    PHASE_MARK(PH_PRESS_RHS);
+    const int warp = TID >> 5, lane = TID & 31, nwarps = NT >> 5;
+    T *wk = wsh + (size_t)warp * (nx + 4);
+    for (int k = 1 + warp; k <= nzm; k += nwarps) fft991_warp(fsh + (size_t)nx2 * (k - 1), wk, nx, -1, lane);
     SYNC;
+    PHASE_MARK(PH_FFT_FWD);
     // vertical tridiagonal solve per Fourier coefficient, in FP64
-    double *alfa = reinterpret_cast<double *>(base + p.L.s_a);   // (nx+1) x nzm doubles
-    double *beta = reinterpret_cast<double *>(base + p.L.s_c);
-    for (int i = TID + 1; i <= nx + 1; i += NT) {
-      int id = (int)(((float)i - 0.1f) / 2.0f);
-      double eign = p.eign[i - 1];
-      auto A = [&](int k) { return (double)rhow[k] / ((double)adz[k] * (double)adzw[k] * S.dz * S.dz); };
-      auto Cc = [&](int k) { return (double)rhow[k + 1] / ((double)adz[k] * (double)adzw[k + 1] * S.dz * S.dz); };
-      auto FF = [&](int k) -> T & { return fbuf[(size_t)nx2 * k + (i - 1)]; };
-      double *al = alfa + (size_t)(i - 1) * (nzm + 1), *be = beta + (size_t)(i - 1) * (nzm + 1);
-      double b;
-      double a1 = A(1), c1 = Cc(1);
-      if (id == 0) b = 1. / (eign * (double)rho[1] - a1 - c1);
-      else b = 1. / (eign * (double)rho[1] - c1);
-      al[1] = -c1 * b;
-      be[1] = (double)FF(1) * b;
-      for (int k = 2; k <= nzm - 1; ++k) {
-        double ak = A(k), ck = Cc(k);
-        double e = 1. / (eign * (double)rho[k] - ak - ck + ak * al[k - 1]);
-        al[k] = -ck * e;
-        be[k] = ((double)FF(k) - ak * be[k - 1]) * e;
-      }
-      double an = A(nzm);
-      double fk = ((double)FF(nzm) - an * be[nzm - 1]) / (eign * (double)rho[nzm] - an + an * al[nzm - 1]);
-      FF(nzm) = (T)fk;
-      for (int k = nzm - 1; k >= 1; --k) {
-        fk = al[k] * fk + be[k];
-        FF(k) = (T)fk;
+    {
+      const int np = nx + 1, ls = nzm + 1;
+      const double *tri = TRI();
+      double *beta = reinterpret_cast<double *>(base + p.L.s_a);   // np x (nzm+1) doubles
+      for (int i = TID + 1; i <= np; i += NT) {
+        const double *al = tri + (size_t)ls + (size_t)(i - 1) * 2 * ls, *e = al + ls;
+        double *be = beta + (size_t)(i - 1) * ls;
+        T *ff = fsh + (i - 1);
+        double bprev = (double)ff[0] * e[1];
+        be[1] = bprev;
+        for (int k = 2; k <= nzm - 1; ++k) {
+          bprev = ((double)ff[(size_t)nx2 * (k - 1)] - tri[k] * bprev) * e[k];
+          be[k] = bprev;
+        }
+        double fk = ((double)ff[(size_t)nx2 * (nzm - 1)] - tri[nzm] * bprev) / tri[(size_t)ls + (size_t)np * 2 * ls + (i - 1)];
+        ff[(size_t)nx2 * (nzm - 1)] = (T)fk;
+        for (int k = nzm - 1; k >= 1; --k) {
+          fk = al[k] * fk + be[k];
+          ff[(size_t)nx2 * (k - 1)] = (T)fk;
+        }
       }
     }
     SYNC;
-    for (int k = TID + 1; k <= nzm; k += NT) fft991(fbuf + (size_t)nx2 * k, wbuf + (size_t)nwk * k, nx, +1);
+    PHASE_MARK(PH_TRIDIAG);
+    for (int k = 1 + warp; k <= nzm; k += nwarps) fft991_warp(fsh + (size_t)nx2 * (k - 1), wk, nx, +1, lane);
     SYNC;
+    PHASE_MARK(PH_FFT_INV);
     for (int e = TID; e < (nx + 1) * nzm; e += NT) {
       int i = e % (nx + 1), k = 1 + e / (nx + 1);
-      pp(i, k) = fbuf[(size_t)nx2 * k + ((i == 0 ? nx : i) - 1)];
+      pp(i, k) = fsh[(size_t)nx2 * (k - 1) + ((i == 0 ? nx : i) - 1)];
     }
     SYNC;
     F2<T> dva = DV(S.na);
@@ -1117,6 +1239,7 @@ struct ColumnKernel {
     }
     for (int k = TID + 1; k <= nzm; k += NT) dua(nx + 1, k) = dua(1, k);
     SYNC;
+    PHASE_MARK(PH_PRESS_GRAD);
   }
 
   // ---------------------------------------------------------- adams / uvw
@@ -1177,11 +1300,8 @@ struct ColumnKernel {
     SYNC;
     // first-pass (upwind) vertical flux sum, then the upwind update
     if (flux)
-      for (int k = TID + 1; k <= nzm; k += NT) {
-        double s = 0.;
-        for (int i = 1; i <= nx; ++i) s = s + (double)www(i, k);
-        wfl1(0, k) = (T)s;
-      }
+      level_sums(1, 1, nzm, [&](int, int i, int k) -> T { return www(i, k); },
+                 [&](int, int) { return 0.; }, [&](int, int k, double sv) { wfl1(0, k) = (T)sv; });
     for (int e = TID; e < (nx + 4) * nzm; e += NT) {
       int i = -1 + e % (nx + 4), k = 1 + e / (nx + 4);   // -1 .. nx+2
       T iadz = (T)1. / adz[k], irho = (T)1. / rho[k];
@@ -1243,11 +1363,9 @@ struct ColumnKernel {
     }
     SYNC;
     if (flux)
-      for (int k = TID + 1; k <= nzm; k += NT) {
-        double s = (double)wfl1(0, k);
-        for (int i = 1; i <= nx; ++i) s = s + (double)www(i, k);
-        flux[k] = (T)s;
-      }
+      level_sums(1, 1, nzm, [&](int, int i, int k) -> T { return www(i, k); },
+                 [&](int, int k) { return (double)wfl1(0, k); },
+                 [&](int, int k, double sv) { flux[k] = (T)sv; });
     for (int e = TID; e < nx * nzm; e += NT) {
       int i = 1 + e % nx, k = 1 + e / nx;
       T iadz = (T)1. / adz[k], irho = (T)1. / rho[k];
@@ -1255,11 +1373,8 @@ struct ColumnKernel {
     }
     SYNC;
     if (fadv) {
-      for (int k = TID + 1; k <= nzm; k += NT) {
-        double s = 0.;
-        for (int i = 1; i <= nx; ++i) s = s + (double)(f(i, k) - f0(i, k));
-        fadv[k] = (T)s;
-      }
+      level_sums(1, 1, nzm, [&](int, int i, int k) -> T { return f(i, k) - f0(i, k); },
+                 [&](int, int) { return 0.; }, [&](int, int k, double sv) { fadv[k] = (T)sv; });
       SYNC;
     }
   }
@@ -1377,15 +1492,13 @@ struct ColumnKernel {
       }
       SYNC;
       // per-level budget sums in the reference's order, then the update
-      for (int k = TID + 1; k <= nzm; k += NT) {
-        double sf = (double)qpfall[k], sp = (double)precflux[k];
-        for (int i = 1; i <= nx; ++i) {
-          T d = -(fz(i, k + 1) - fz(i, k)) * irhoadz[k] * (T)1.;
-          sf = sf + (double)d;
-          sp = sp - (double)(fz(i, k) * (T)1.);
-        }
-        qpfall[k] = (T)sf; precflux[k] = (T)sp;
-      }
+      level_sums(2, 1, nzm,
+                 [&](int q, int i, int k) -> T {
+                   if (q == 0) return -(fz(i, k + 1) - fz(i, k)) * irhoadz[k] * (T)1.;
+                   return -(fz(i, k) * (T)1.);
+                 },
+                 [&](int q, int k) { return (double)(q == 0 ? qpfall[k] : precflux[k]); },
+                 [&](int q, int k, double sv) { (q == 0 ? qpfall : precflux)[k] = (T)sv; });
       for (int e = TID; e < nx * nzm; e += NT) {
         int i = 1 + e % nx, k = 1 + e / nx;
         int kc = k + 1;
@@ -1453,12 +1566,8 @@ struct ColumnKernel {
     }
     SYNC;
     if (flux)
-      for (int k = TID + 1; k <= nzm; k += NT) {
-        double s = 0.;
-        if (k == 1) for (int i = 1; i <= nx; ++i) s = s + (double)flx(i, 0);
-        else for (int i = 1; i <= nx; ++i) s = s + (double)flx(i, k - 1);
-        flux[k] = (T)s;
-      }
+      level_sums(1, 1, nzm, [&](int, int i, int k) -> T { return flx(i, k == 1 ? 0 : k - 1); },
+                 [&](int, int) { return 0.; }, [&](int, int k, double sv) { flux[k] = (T)sv; });
     for (int e = TID; e < nx * nzm; e += NT) {
       int i = 1 + e % nx, k = 1 + e / nx;
       int kb = k - 1;
@@ -1468,11 +1577,8 @@ struct ColumnKernel {
     }
     SYNC;
     if (fdiff) {
-      for (int k = TID + 1; k <= nzm; k += NT) {
-        double s = 0.;
-        for (int i = 1; i <= nx; ++i) s = s + (double)(f(i, k) - f0(i, k));
-        fdiff[k] = (T)s;
-      }
+      level_sums(1, 1, nzm, [&](int, int i, int k) -> T { return f(i, k) - f0(i, k); },
+                 [&](int, int) { return 0.; }, [&](int, int k, double sv) { fdiff[k] = (T)sv; });
       SYNC;
     }
   }
@@ -1555,7 +1661,7 @@ struct ColumnKernel {
   // the reference's order from the per-cell contributions
   __device__ void precip_proc() {
     F2<T> qt = QT(), qp = QP(), qn = QN(), tabs = TABS();
-    F2<T> csrc = SCR(p.L.s_a), cevp = SCR(p.L.s_b), flag = SCR(p.L.s_c);
+    F2<T> csrc = SCR(p.L.s_a), cevp = SCR(p.L.s_b);
     T *pres = PR(P_PRES);
     const T powr1 = (T)((3 + C_B_RAIN) / 4.), powr2 = (T)((5 + C_B_RAIN) / 8.);
     const T pows1 = (T)((3 + C_B_SNOW) / 4.), pows2 = (T)((5 + C_B_SNOW) / 8.);
@@ -1566,7 +1672,6 @@ struct ColumnKernel {
       int i = 1 + e % nx, k = 1 + e / nx;
       T q = qt(i, k), qpv = qp(i, k), qnv = qn(i, k), tb = tabs(i, k);
       T src = (T)0., evp = (T)0.;
-      int fl = 0;          // bit 0: contributes to qpsrc, bit 1: to qpevp
       if (qnv + qpv > (T)0.) {
         T omn = mx2((T)0., mn2((T)1., (tb - (T)C_TBGMIN) * a_bg));
         T omp = mx2((T)0., mn2((T)1., (tb - (T)C_TPRMIN) * a_pr));
@@ -1603,7 +1708,7 @@ struct ColumnKernel {
           qpv = qpv + dq;
           q = q - dq;
           qnv = qnv - dq;
-          src = dq; fl = 1;
+          src = dq;
         } else if (qpv > (T)C_QP_THRESHOLD && qnv == (T)0.) {
           T qsatt = (T)0.;
           if (omn > (T)R4(0.001)) qsatt = qsatt + omn * qsatw(tb, pres[k]);
@@ -1625,10 +1730,10 @@ struct ColumnKernel {
           dq = mx2((T)-0.5 * qpv, dq);
           qpv = qpv + dq;
           q = q - dq;
-          evp = dq; fl = 2;
+          evp = dq;
         } else {
           q = q + qpv;
-          evp = qpv; fl = 3;            // qpevp = qpevp - qp
+          evp = -qpv;                   // qpevp = qpevp - qp
           qpv = (T)0.;
         }
       }
@@ -1636,20 +1741,13 @@ struct ColumnKernel {
       qpv = mx2((T)0., qpv);
       q = q + (dq - qpv);
       qt(i, k) = q; qp(i, k) = qpv; qn(i, k) = qnv;
-      csrc(i, k) = src; cevp(i, k) = evp; flag(i, k) = (T)fl;
+      csrc(i, k) = src; cevp(i, k) = evp;
     }
     SYNC;
     T *qpsrc = PR(P_QPSRC), *qpevp = PR(P_QPEVP);
-    for (int k = TID + 1; k <= nzm; k += NT) {
-      double s = 0., v = 0.;
-      for (int i = 1; i <= nx; ++i) {
-        int fl = (int)flag(i, k);
-        if (fl == 1) s = s + (double)csrc(i, k);
-        else if (fl == 2) v = v + (double)cevp(i, k);
-        else if (fl == 3) v = v - (double)cevp(i, k);
-      }
-      qpsrc[k] = (T)s; qpevp[k] = (T)v;
-    }
+    level_sums(2, 1, nzm, [&](int q, int i, int k) -> T { return q == 0 ? csrc(i, k) : cevp(i, k); },
+               [&](int, int) { return 0.; },
+               [&](int q, int k, double sv) { (q == 0 ? qpsrc : qpevp)[k] = (T)sv; });
     SYNC;
   }
 
@@ -1663,22 +1761,30 @@ struct ColumnKernel {
     }
     SYNC;
     const double coef = 1. / (double)nx;
-    for (int k = TID + 1; k <= nzm; k += NT) {
-      double su = 0, sv = 0, st = 0, sa = 0, sq = 0, sn = 0, sp = 0;
-      for (int i = 1; i <= nx; ++i) {
-        su = su + (double)u(i, k);
-        sv = sv + (double)v(i, k);
-        st = st + (double)t(i, k);
-        sa = sa + (double)tabs(i, k);
-        sq = sq + (double)(qv(i, k) + qcl(i, k) + qci(i, k));
-        sn = sn + (double)(qcl(i, k) + qci(i, k));
-        sp = sp + (double)(qpl(i, k) + qpi(i, k));
-      }
-      su = su * coef; sv = sv * coef; st = st * coef; sa = sa * coef; sq = sq * coef; sn = sn * coef; sp = sp * coef;
-      PR(P_U0)[k] = (T)su; PR(P_V0)[k] = (T)sv; PR(P_T0)[k] = (T)st; PR(P_TABS0)[k] = (T)sa;
-      PR(P_Q0)[k] = (T)sq; PR(P_QN0)[k] = (T)sn; PR(P_QP0)[k] = (T)sp;
-      PR(P_QV0)[k] = (T)(sq - sn);
-    }
+    // domain means; q0 and qn0 are kept in FP64 in TMP0/TMP1 for qv0
+    double *q0d = reinterpret_cast<double *>(base + p.L.s_a);
+    level_sums(7, 1, nzm,
+               [&](int q, int i, int k) -> T {
+                 switch (q) {
+                   case 0: return u(i, k);
+                   case 1: return v(i, k);
+                   case 2: return t(i, k);
+                   case 3: return tabs(i, k);
+                   case 4: return qv(i, k) + qcl(i, k) + qci(i, k);
+                   case 5: return qcl(i, k) + qci(i, k);
+                   default: return qpl(i, k) + qpi(i, k);
+                 }
+               },
+               [&](int, int) { return 0.; },
+               [&](int q, int k, double sv) {
+                 sv = sv * coef;
+                 const int ids[7] = {P_U0, P_V0, P_T0, P_TABS0, P_Q0, P_QN0, P_QP0};
+                 PR(ids[q])[k] = (T)sv;
+                 if (q == 4) q0d[k] = sv;
+                 if (q == 5) q0d[nz + 1 + k] = sv;
+               });
+    SYNC;
+    for (int k = TID + 1; k <= nzm; k += NT) PR(P_QV0)[k] = (T)(q0d[k] - q0d[nz + 1 + k]);
     SYNC;
   }
 
@@ -1687,9 +1793,10 @@ struct ColumnKernel {
   __device__ void step_stats() {
     F2<T> qcl = QCL(), qci = QCI(), qpl = QPL(), qpi = QPI(), w = W(), tabs = TABS(), qv = QV();
     T *rho = PR(P_RHO), *adz = PR(P_ADZ), *pres = PR(P_PRES), *rhow = PR(P_RHOW);
-    T *cs = base + p.L.colstat;     // 8 x nx: cwp, cwph, cwpm, cwpl, top level
+    T *cs = base + p.L.colstat;     // 5 x nx: cwp, cwph, cwpm, cwpl, top level
     const T dz = (T)S.dz;
     const T thr = (T)R4(0.001);
+    // condensate paths from the top down, per CRM column (i)
     for (int i = TID + 1; i <= nx; i += NT) {
       T cwp = (T)0., cwph = (T)0., cwpm = (T)0., cwpl = (T)0.;
       int top = 0;
@@ -1705,64 +1812,48 @@ struct ColumnKernel {
       cs[(i - 1)] = cwp; cs[nx + (i - 1)] = cwph; cs[2 * nx + (i - 1)] = cwpm; cs[3 * nx + (i - 1)] = cwpl;
       cs[4 * nx + (i - 1)] = (T)top;
     }
-    SYNC;
-    T *ocld = OP(O_CLD), *otop = OP(O_CLDTOP), *oice = OP(O_GICEWP), *oliq = OP(O_GLIQWP);
-    T *mcup = OP(O_MCUP), *mcdn = OP(O_MCDN), *mcuup = OP(O_MCUUP), *mcudn = OP(O_MCUDN);
-    T *mui = OP(O_MUI), *mdi = OP(O_MDI);
-    for (int k = TID + 1; k <= nz; k += NT) {
-      // interface mass fluxes at w level k (GCM interface l = plev + 2 - k)
-      {
-        int l = plev + 2 - k;
-        double su = (double)mui[l], sd = (double)mdi[l];
-        for (int i = 1; i <= nx; ++i) {
-          T wv = w(i, k);
-          if (wv > (T)0.) {
-            int kx = max(1, k - 1);
-            T qs = qsatw(tabs(i, kx), pres[kx]);
-            if (qcl(i, kx) + qci(i, kx) > mn2((T)R4(1.e-5), (T)R4(0.01) * qs)) su = su + (double)(rhow[k] * wv);
-          } else if (wv < (T)0.) {
-            int kx = min(k + 1, nzm);
-            T qs = qsatw(tabs(i, kx), pres[kx]);
-            if (qcl(i, kx) + qci(i, kx) > mn2((T)R4(1.e-5), (T)R4(0.01) * qs)) sd = sd + (double)(rhow[k] * wv);
-            else if (qpl(i, kx) + qpi(i, kx) > (T)R4(1.0e-4)) sd = sd + (double)(rhow[k] * wv);
-          }
-        }
-        mui[l] = (T)su; mdi[l] = (T)sd;
+    // interface mass fluxes (Xu et al. 2002): per-cell contributions at w
+    // levels k = 1..nz, zero where a cell does not count
+    F2<T> cmu = SCR(p.L.s_a), cmd = SCR(p.L.s_b);
+    for (int e = TID; e < nx * nz; e += NT) {
+      int i = 1 + e % nx, k = 1 + e / nx;
+      T wv = w(i, k), cu = (T)0., cd = (T)0.;
+      if (wv > (T)0.) {
+        int kx = max(1, k - 1);
+        T qs = qsatw(tabs(i, kx), pres[kx]);
+        if (qcl(i, kx) + qci(i, kx) > mn2((T)R4(1.e-5), (T)R4(0.01) * qs)) cu = rhow[k] * wv;
+      } else if (wv < (T)0.) {
+        int kx = min(k + 1, nzm);
+        T qs = qsatw(tabs(i, kx), pres[kx]);
+        if (qcl(i, kx) + qci(i, kx) > mn2((T)R4(1.e-5), (T)R4(0.01) * qs)) cd = rhow[k] * wv;
+        else if (qpl(i, kx) + qpi(i, kx) > (T)R4(1.0e-4)) cd = rhow[k] * wv;
       }
-      if (k > nzm) continue;
-      int l = plev - k + 1;
-      // cloud top counts: column i crossed the threshold at step index k
-      {
-        double c = (double)otop[l];
-        for (int i = 1; i <= nx; ++i)
-          if ((int)cs[4 * nx + (i - 1)] == k) c = c + 1.;
-        otop[l] = (T)c;
-      }
-      double scld = (double)ocld[l], sup = (double)mcup[l], sdn = (double)mcdn[l];
-      double suu = (double)mcuup[l], sud = (double)mcudn[l], sli = (double)oliq[l], sic = (double)oice[l];
-      T tmp1 = rho[k] * adz[k] * dz;
-      for (int i = 1; i <= nx; ++i) {
-        T ws = w(i, k + 1) + w(i, k);
-        if (tmp1 * (qcl(i, k) + qci(i, k)) > thr) {
-          scld = scld + 1.0;
-          if (ws > (T)4.) {
-            sup = sup + (double)(rho[k] * (T)0.5 * ws * (T)1.0);
-            suu = suu + (double)(rho[k] * (T)0.5 * ws * ((T)1.0 - (T)1.0));
-          }
-          if (ws < (T)-4.) {
-            sdn = sdn + (double)(rho[k] * (T)0.5 * ws * (T)1.0);
-            sud = sud + (double)(rho[k] * (T)0.5 * ws * ((T)1. - (T)1.0));
-          }
-        } else {
-          if (ws > (T)4.) suu = suu + (double)(rho[k] * (T)0.5 * ws);
-          if (ws < (T)-4.) sud = sud + (double)(rho[k] * (T)0.5 * ws);
-        }
-        sli = sli + (double)qcl(i, k);
-        sic = sic + (double)qci(i, k);
-      }
-      ocld[l] = (T)scld; mcup[l] = (T)sup; mcdn[l] = (T)sdn; mcuup[l] = (T)suu; mcudn[l] = (T)sud;
-      oliq[l] = (T)sli; oice[l] = (T)sic;
+      cmu(i, k) = cu;
+      cmd(i, k) = cd;
     }
+    SYNC;
+    T *mui = OP(O_MUI), *mdi = OP(O_MDI);
+    level_sums(2, 1, nz, [&](int q, int i, int k) -> T { return q == 0 ? cmu(i, k) : cmd(i, k); },
+               [&](int q, int k) { return (double)(q == 0 ? mui : mdi)[plev + 2 - k]; },
+               [&](int q, int k, double sv) { (q == 0 ? mui : mdi)[plev + 2 - k] = (T)sv; });
+    // cloud fraction, cloud top counts, cloudy mass fluxes, water paths
+    T *acc[8] = {OP(O_CLD), OP(O_CLDTOP), OP(O_MCUP), OP(O_MCDN), OP(O_MCUUP), OP(O_MCUDN), OP(O_GLIQWP), OP(O_GICEWP)};
+    level_sums(8, 1, nzm,
+               [&](int q, int i, int k) -> T {
+                 if (q == 1) return ((int)cs[4 * nx + (i - 1)] == k) ? (T)1. : (T)0.;
+                 if (q == 6) return qcl(i, k);
+                 if (q == 7) return qci(i, k);
+                 T tmp1 = rho[k] * adz[k] * dz;
+                 bool cloudy = tmp1 * (qcl(i, k) + qci(i, k)) > thr;
+                 if (q == 0) return cloudy ? (T)1.0 : (T)0.;
+                 T ws = w(i, k + 1) + w(i, k);
+                 if (q == 2) return (cloudy && ws > (T)4.) ? rho[k] * (T)0.5 * ws * (T)1.0 : (T)0.;
+                 if (q == 3) return (cloudy && ws < (T)-4.) ? rho[k] * (T)0.5 * ws * (T)1.0 : (T)0.;
+                 if (q == 4) return (!cloudy && ws > (T)4.) ? rho[k] * (T)0.5 * ws : (T)0.;
+                 return (!cloudy && ws < (T)-4.) ? rho[k] * (T)0.5 * ws : (T)0.;
+               },
+               [&](int q, int k) { return (double)acc[q][plev - k + 1]; },
+               [&](int q, int k, double sv) { acc[q][plev - k + 1] = (T)sv; });
     // radiation-group sums (crm_module.F90:1000-1028)
     const int nxr = p.L.nx_rad, gx = nx / nxr;
     T *rad = base + p.L.rad;
@@ -1782,20 +1873,33 @@ struct ColumnKernel {
       rad[(size_t)3 * nxr * nzm + o] = (T)si; rad[(size_t)4 * nxr * nzm + o] = (T)sl;
     }
     SYNC;
-    if (TID == 0) {
-      // shaded cloud fractions: cf3d = 1, so each temperature flag is 1
-      // wherever its layer exists (crm_module.F90:1053-1072)
+    if (TID < 32) {
+      // shaded cloud fractions (counts, exact in any order): cf3d = 1, so a
+      // column counts wherever its layer class exists (crm_module.F90:1053-1072)
       bool anyl = false, anyh = false, anym = false;
       for (int k = 1; k <= nzm; ++k) {
         if (pres[k] >= (T)700.) anyl = true;
         else if (pres[k] < (T)400.) anyh = true;
         else anym = true;
       }
-      for (int i = 1; i <= nx; ++i) {
-        if (cs[(i - 1)] > thr) S.cltot = S.cltot + 1.0;
-        if (cs[nx + (i - 1)] > thr) S.clhgh = S.clhgh + (anyh ? 1.0 : 0.0);
-        if (cs[2 * nx + (i - 1)] > thr) S.clmed = S.clmed + (anym ? 1.0 : 0.0);
-        if (cs[3 * nx + (i - 1)] > thr) S.cllow = S.cllow + (anyl ? 1.0 : 0.0);
+      int ct = 0, ch = 0, cm = 0, cl = 0;
+      for (int i = 1 + TID; i <= nx; i += 32) {
+        ct += cs[(i - 1)] > thr;
+        ch += cs[nx + (i - 1)] > thr;
+        cm += cs[2 * nx + (i - 1)] > thr;
+        cl += cs[3 * nx + (i - 1)] > thr;
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        ct += __shfl_xor_sync(0xffffffffu, ct, o);
+        ch += __shfl_xor_sync(0xffffffffu, ch, o);
+        cm += __shfl_xor_sync(0xffffffffu, cm, o);
+        cl += __shfl_xor_sync(0xffffffffu, cl, o);
+      }
+      if (TID == 0) {
+        S.cltot = S.cltot + (double)ct;
+        S.clhgh = S.clhgh + (anyh ? (double)ch : 0.0);
+        S.clmed = S.clmed + (anym ? (double)cm : 0.0);
+        S.cllow = S.cllow + (anyl ? (double)cl : 0.0);
       }
     }
     SYNC;
@@ -1831,28 +1935,51 @@ struct ColumnKernel {
       }
     }
     SYNC;
-    // GCM-level means of the final state and the tendencies
+    // horizontal sums of the final state per CRM level (FP64 scratch)
+    double *hs = reinterpret_cast<double *>(base + p.L.s_a);    // 12 x (nz + 2)
+    auto HS = [&](int q, int k) -> double & { return hs[(size_t)q * (nz + 2) + k]; };
+    {
+      T *u0p = PR(P_U0), *v0p = PR(P_V0);
+      level_sums(12, 1, nzm,
+                 [&](int q, int i, int k) -> T {
+                   switch (q) {
+                     case 0: return tabs(i, k);
+                     case 1: return qv(i, k);
+                     case 2: return qcl(i, k);
+                     case 3: return qci(i, k);
+                     case 4: return qpl(i, k);
+                     case 5: {
+                       T omg = mx2((T)0., mn2((T)1., (tabs(i, k) - (T)C_TGRMIN) * (T)p.a_gr));
+                       return qpi(i, k) * omg;
+                     }
+                     case 6: {
+                       T omg = mx2((T)0., mn2((T)1., (tabs(i, k) - (T)C_TGRMIN) * (T)p.a_gr));
+                       return qpi(i, k) * ((T)1. - omg);
+                     }
+                     case 7: { T d = u(i, k) - u0p[k]; return d * d; }
+                     case 8: { T d = v(i, k) - v0p[k]; return d * d; }
+                     case 9: { T w1 = w(i, k + 1), w0 = w(i, k); return (T)0.5 * (w1 * w1 + w0 * w0); }
+                     case 10: return tke(i, k);
+                     default: return tk(i, k);
+                   }
+                 },
+                 [&](int, int) { return 0.; }, [&](int q, int k, double sv) { HS(q, k) = sv; });
+    }
+    SYNC;
+    // GCM-level tendencies and statistics
     for (int l = TID + 1; l <= plev; l += NT) {
       double tln, qln, qccln, qiiln;
       if (l < ptop) {
         tln = IN(p.tl, l); qln = IN(p.ql, l); qccln = IN(p.qccl, l); qiiln = IN(p.qiil, l);
       } else {
         int k = plev - l + 1;
-        double st = 0., sq = 0., sc = 0., si = 0.;
-        for (int i = 1; i <= nx; ++i) {
-          st = st + (double)tabs(i, k);
-          sq = sq + (double)qv(i, k);
-          sc = sc + (double)qcl(i, k);
-          si = si + (double)qci(i, k);
-        }
-        tln = st * factor_xy; qln = sq * factor_xy; qccln = sc * factor_xy; qiiln = si * factor_xy;
+        tln = HS(0, k) * factor_xy; qln = HS(1, k) * factor_xy; qccln = HS(2, k) * factor_xy; qiiln = HS(3, k) * factor_xy;
       }
       bool top2 = (l == ptop || l == ptop + 1);
       O2(CRM_OUT_SLTEND, l) = top2 ? 0. : C_CP * (tln - IN(p.tl, l)) * icrm_run_time;
       O2(CRM_OUT_QLTEND, l) = top2 ? 0. : (qln - IN(p.ql, l)) * icrm_run_time;
       O2(CRM_OUT_QCLTEND, l) = top2 ? 0. : (qccln - IN(p.qccl, l)) * icrm_run_time;
       O2(CRM_OUT_QILTEND, l) = top2 ? 0. : (qiiln - IN(p.qiil, l)) * icrm_run_time;
-      // cloud and mass-flux statistics
       double pdel = IN(p.pdel, l);
       O2(CRM_OUT_CLD, l) = mn2(1.0, (double)OP(O_CLD)[l] * factor_xyt);
       O2(CRM_OUT_CLDTOP, l) = mn2(1.0, (double)OP(O_CLDTOP)[l] * factor_xyt);
@@ -1877,27 +2004,11 @@ struct ColumnKernel {
       if (act) atomicMin(&S.jt_min, l);
       if (act) atomicMax(&S.mx_max, l);
     }
-    SYNC;
     // flux and condensate profiles at CRM levels
     for (int k = TID + 1; k <= nzm; k += NT) {
       int l = plev - k + 1;
-      double qcm = 0, qim = 0, qrm = 0, qgm = 0, qsm = 0, u2z = 0, v2z = 0, w2z = 0, stke = 0, stk = 0;
-      T u0 = PR(P_U0)[k], v0 = PR(P_V0)[k];
-      for (int i = 1; i <= nx; ++i) {
-        qcm = qcm + (double)qcl(i, k);
-        qim = qim + (double)qci(i, k);
-        qrm = qrm + (double)qpl(i, k);
-        T omg = mx2((T)0., mn2((T)1., (tabs(i, k) - (T)C_TGRMIN) * (T)p.a_gr));
-        qgm = qgm + (double)(qpi(i, k) * omg);
-        qsm = qsm + (double)(qpi(i, k) * ((T)1. - omg));
-        T du = u(i, k) - u0, dv = v(i, k) - v0;
-        u2z = u2z + (double)(du * du);
-        v2z = v2z + (double)(dv * dv);
-        T w1 = w(i, k + 1), w0 = w(i, k);
-        w2z = w2z + (double)((T)0.5 * (w1 * w1 + w0 * w0));
-        stke = stke + (double)tke(i, k);
-        stk = stk + (double)tk(i, k);
-      }
+      double qcm = HS(2, k), qim = HS(3, k), qrm = HS(4, k), qgm = HS(5, k), qsm = HS(6, k);
+      double u2z = HS(7, k), v2z = HS(8, k), w2z = HS(9, k), stke = HS(10, k), stk = HS(11, k);
       O2(CRM_OUT_QC_MEAN, l) = qcm * factor_xy;
       O2(CRM_OUT_QI_MEAN, l) = qim * factor_xy;
       O2(CRM_OUT_QS_MEAN, l) = qsm * factor_xy;
@@ -1993,11 +2104,15 @@ struct ColumnKernel {
   }
 
   // ---------------------------------------------------------- one column
-  __device__ void run() {
+  __device__ void run(T *fsh, T *wsh) {
+    if (TID == 0) S.t_last = clock64();
     init_column();
     if (TID == 0) { S.jt_min = 1 << 30; S.mx_max = 0; }
+    SYNC;
+    PHASE_MARK(PH_INIT);
     for (int nstep = 1; nstep <= p.nstop; ++nstep) {
       kurant();
+      PHASE_MARK(PH_KURANT);
       if (S.ncycle > 16) {
         if (TID == 0) S.status = CRM_ERR_CFL;
         SYNC;
@@ -2014,62 +2129,98 @@ struct ColumnKernel {
         }
         SYNC;
         zero_and_buoyancy();
+        PHASE_MARK(PH_BUOY);
         forcing_radiation();
+        PHASE_MARK(PH_FORCING);
         damping();
+        PHASE_MARK(PH_DAMPING);
         ice_fall();
+        PHASE_MARK(PH_ICEFALL);
         boundaries(3);
         boundaries(0);
+        PHASE_MARK(PH_BOUND);
         tke_full();
+        PHASE_MARK(PH_TKE);
         boundaries(4);
         advect_mom();
+        PHASE_MARK(PH_ADVMOM);
         diffuse_mom();
-        pressure();
+        PHASE_MARK(PH_DIFFMOM);
+        pressure(fsh, wsh);
         adams();
         boundaries(2);
+        PHASE_MARK(PH_ADAMS);
         advect_scalar(TT(), nullptr, nullptr);
+        PHASE_MARK(PH_ADV_T);
         advect_scalar(QT(), PR(P_MKADV0), PR(P_MKWLE0));
+        PHASE_MARK(PH_ADV_QT);
         advect_scalar(QP(), PR(P_MKADV1), PR(P_MKWLE1));
+        PHASE_MARK(PH_ADV_QP);
         precip_fall_1();
+        PHASE_MARK(PH_FALL1);
         precip_fall_2(S.nprec);
+        PHASE_MARK(PH_FALL2);
         uvw();
         boundaries(3);
+        PHASE_MARK(PH_UVW);
         diffuse_scalar(TT(), nullptr, nullptr);
+        PHASE_MARK(PH_DIFF_T);
         diffuse_scalar(QT(), PR(P_MKDIFF0), PR(P_MKWSB0));
         diffuse_scalar(QP(), PR(P_MKDIFF1), PR(P_MKWSB1));
+        PHASE_MARK(PH_DIFF_Q);
         if (S.icycle == 1) precip_init();
+        PHASE_MARK(PH_PINIT);
         cloud();
+        PHASE_MARK(PH_CLOUD);
         precip_proc();
+        PHASE_MARK(PH_PPROC);
         micro_diagnose();
+        PHASE_MARK(PH_MDIAG);
         diagnose();
         if (TID == 0) { int nn = S.na; S.na = S.nc; S.nc = S.nb; S.nb = nn; }
         SYNC;
+        PHASE_MARK(PH_DIAG);
       }
       step_stats();
+      PHASE_MARK(PH_STATS);
     }
     finalize();
+    PHASE_MARK(PH_FINAL);
   }
 };
 
 template <typename T>
+__host__ __device__ inline size_t crm_smem_bytes(int nx, int nzm, int block) {
+  return sizeof(T) * ((size_t)(nx + 2) * nzm + (size_t)(block / 32) * (nx + 4));
+}
+
+template <typename T>
 __global__ void __launch_bounds__(256) crm_columns_kernel(const __grid_constant__ KParams p) {
   __shared__ ColShared S;
+  extern __shared__ __align__(16) unsigned char crm_dsm[];
+  T *fsh = reinterpret_cast<T *>(crm_dsm);
+  T *wsh = fsh + (size_t)(p.L.nx + 2) * p.L.nzm;
   T *base = reinterpret_cast<T *>(p.slabs) + (size_t)blockIdx.x * p.L.slab;
   for (int col = blockIdx.x; col < p.ncrms; col += gridDim.x) {
     ColumnKernel<T> K(p, S, base, col);
-    K.run();
+    K.run(fsh, wsh);
     __syncthreads();
   }
 }
 
 template <typename T>
 void launch_crm_columns(const KParams &p, int grid, int block, cudaStream_t s) {
-  crm_columns_kernel<T><<<grid, block, 0, s>>>(p);
+  size_t smem = crm_smem_bytes<T>(p.L.nx, p.L.nzm, block);
+  cudaFuncSetAttribute(crm_columns_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  crm_columns_kernel<T><<<grid, block, smem, s>>>(p);
 }
 
 template <typename T>
-int occupancy_crm_columns(int block) {
+int occupancy_crm_columns(int block, int nx, int nzm) {
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, crm_columns_kernel<T>, block, 0) != cudaSuccess) return 0;
+  size_t smem = crm_smem_bytes<T>(nx, nzm, block);
+  cudaFuncSetAttribute(crm_columns_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, crm_columns_kernel<T>, block, smem) != cudaSuccess) return 0;
   return n;
 }
 

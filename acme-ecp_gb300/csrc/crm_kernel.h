@@ -29,11 +29,20 @@ struct KParams {
   void *slabs;              // gridDim.x slabs of L.slab elements of T
   int *col_status;          // (ncrms)
   int *next_col;            // dynamic column counter (zeroed before launch)
+  unsigned long long *phase_cycles;  // (gridDim.x, 64) when built with CRM_PHASE_TIMERS
+};
+
+// phase ids for the optional per-phase cycle counters
+enum PhaseId {
+  PH_INIT, PH_KURANT, PH_BUOY, PH_FORCING, PH_DAMPING, PH_ICEFALL, PH_BOUND, PH_TKE,
+  PH_ADVMOM, PH_DIFFMOM, PH_PRESS_RHS, PH_FFT_FWD, PH_TRIDIAG, PH_FFT_INV, PH_PRESS_GRAD,
+  PH_ADAMS, PH_ADV_T, PH_ADV_QT, PH_ADV_QP, PH_FALL1, PH_FALL2, PH_UVW, PH_DIFF_T,
+  PH_DIFF_Q, PH_PINIT, PH_CLOUD, PH_PPROC, PH_MDIAG, PH_DIAG, PH_STATS, PH_FINAL, PH_COUNT
 };
 
 template <typename T>
 void launch_crm_columns(const KParams &p, int grid, int block, cudaStream_t s);
 template <typename T>
-int occupancy_crm_columns(int block);
+int occupancy_crm_columns(int block, int nx, int nzm);
 
 }  // namespace crm

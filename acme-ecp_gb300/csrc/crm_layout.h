@@ -35,6 +35,7 @@ struct Layout {
   size_t rad;            // rad accumulators 5 x (nx_rad x nzm) + qrad
   size_t rnd;            // setperturb random numbers 5 x nx
   size_t colstat;        // per-column scratch for step statistics, 8 x nx
+  size_t tri;            // FP64 tridiagonal factors (see tridiag_factor)
   size_t slab;           // total elements per column
 };
 
@@ -59,7 +60,8 @@ enum OPlev {
   O_COUNT
 };
 
-inline Layout make_layout(int nx, int nzm, int plev, int nx_rad) {
+// esz: bytes per element of the bulk type (8: FP64 form, 4: FP32-mixed)
+inline Layout make_layout(int nx, int nzm, int plev, int nx_rad, int esz) {
   Layout L{};
   L.nx = nx; L.nzm = nzm; L.nz = nzm + 1; L.plev = plev; L.nx_rad = nx_rad;
   L.xu = {-1, nx + 5};
@@ -71,7 +73,7 @@ inline Layout make_layout(int nx, int nzm, int plev, int nx_rad) {
   L.xi = {1, nx};
   L.xdu = {1, nx + 1};
   size_t o = 0;
-  auto take = [&](size_t n) { size_t r = o; o += (n + 31) / 32 * 32; return r; };
+  auto take = [&](size_t n) { size_t r = o; o += (n + 63) / 64 * 64; return r; };
   const int nz = L.nz;
   L.u = take((size_t)L.xu.nxa * nzm);
   L.v = take((size_t)L.xv.nxa * nzm);
@@ -109,6 +111,10 @@ inline Layout make_layout(int nx, int nzm, int plev, int nx_rad) {
   L.rad = take((size_t)6 * nx_rad * nzm);
   L.rnd = take((size_t)5 * nx);
   L.colstat = take((size_t)8 * nx);
+  {
+    size_t nd = (size_t)(nzm + 1) + (size_t)(nx + 1) * 2 * (nzm + 1) + (size_t)(nx + 1);
+    L.tri = take(nd * 8 / esz + 2);
+  }
   L.slab = o;
   return L;
 }

@@ -160,7 +160,7 @@ def main():
     import torch
     from crm_gb300 import build as B
     from crm_gb300 import synthetic as S
-    from crm_gb300 import types as T
+    from crm_gb300 import crm_types as T
     from crm_gb300.device import DeviceCrmArrays
     from crm_gb300.lib import CrmContext
 

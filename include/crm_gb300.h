@@ -174,6 +174,12 @@ double crm_last_kernel_ms(const crm_ctx *ctx);
 /* Bind the handle to a CUDA stream (cudaStream_t passed as void*). */
 int crm_set_stream(crm_ctx *ctx, void *stream);
 const char *crm_status_string(int status);
+/* Per-phase cycle counters of the column kernel, summed over its CTAs since
+ * the last read, in a profiling build of the library (compiled with
+ * -DCRM_PHASE_TIMERS); returns the number of phases written, or -1 in a
+ * normal build.  No counterpart in the reference (its GPTL timers
+ * t_startf/t_stopf time the whole CRM call, crm_module.F90:377,1598). */
+int crm_debug_phase_cycles(crm_ctx *ctx, unsigned long long *out, int n);
 /* Library version string. */
 const char *crm_version(void);
 

@@ -21,7 +21,7 @@ SRC = [os.path.join(HERE, 'crm_oracle.cpp'), os.path.join(HERE, 'oracle_core.h')
        os.path.join(REPO, 'include', 'crm_gb300.h'), os.path.join(REPO, 'include', 'crm_detmath.h')]
 
 sys.path.insert(0, os.path.join(REPO, 'acme-ecp_gb300'))
-from crm_gb300 import types as T  # noqa: E402
+from crm_gb300 import crm_types as T  # noqa: E402
 
 _lib = None
 

@@ -11,7 +11,7 @@ import pytest
 
 import oracle
 from crm_gb300 import synthetic as S
-from crm_gb300 import types as T
+from crm_gb300 import crm_types as T
 from crm_gb300.lib import CrmContext
 
 from conftest import rel_l2

@@ -10,7 +10,7 @@ import pytest
 
 import oracle
 from crm_gb300 import synthetic as S
-from crm_gb300 import types as T
+from crm_gb300 import crm_types as T
 from crm_gb300.lib import CrmContext
 
 pytestmark = pytest.mark.gpu
