@@ -149,6 +149,17 @@ class _Bundle:
     def copy(self):
         return type(self)(**{n: a.copy(order='F') for n, a in self.arrays().items()})
 
+    def take(self, cols):
+        """A new bundle holding the given columns (leading index) in order."""
+        cols = np.asarray(cols, dtype=np.int64)
+        return type(self)(**{n: np.asfortranarray(a[cols]) for n, a in self.arrays().items()})
+
+    def put(self, cols, other):
+        """Write the columns of `other` into columns `cols` of this bundle."""
+        cols = np.asarray(cols, dtype=np.int64)
+        for n, a in self.arrays().items():
+            a[cols] = getattr(other, n)[:len(cols)]
+
     @property
     def ld(self):
         return getattr(self, self.FIELDS[0]).shape[0]

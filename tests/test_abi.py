@@ -1,0 +1,86 @@
+"""The C ABI library without a GPU: it loads, exports every function that
+include/crm_gb300.h declares, and fails loudly (a status, no fallback) when
+no CUDA device is present."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+from conftest import has_gpu
+from crm_gb300 import build
+from crm_gb300 import crm_types as T
+from crm_gb300 import lib as L
+from crm_gb300 import synthetic as S
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_functions():
+    src = open(os.path.join(REPO, 'include', 'crm_gb300.h')).read()
+    src = re.sub(r'/\*.*?\*/', '', src, flags=re.S)
+    names = re.findall(r'^[A-Za-z_][\w \*]*?\b(crm_\w+)\s*\(', src, flags=re.M)
+    return sorted(set(names))
+
+
+@pytest.fixture(scope='module')
+def lib():
+    build.build()
+    return L.load()
+
+
+def test_header_declares_the_bound_functions():
+    assert set(header_functions()) == set(L.EXPORTS)
+
+
+def test_library_exports_every_declared_symbol(lib):
+    for name in header_functions():
+        assert hasattr(lib, name), name
+
+
+def test_status_strings_and_version(lib):
+    for s in range(9):
+        assert lib.crm_status_string(s).decode() not in ('', 'unknown status'), s
+    assert lib.crm_status_string(99).decode() == 'unknown status'
+    assert b'sm_103a' in lib.crm_version()
+
+
+def test_struct_sizes_match_the_header():
+    # pointers and ints as the header lays them out (LP64)
+    assert C.sizeof(T.CCrmOutput) == C.sizeof(C.c_void_p) * len(T.OUTPUT_FIELDS)
+    assert C.sizeof(T.CCrmInput) == C.sizeof(C.c_void_p) * len(T.INPUT_FIELDS)
+    assert C.sizeof(T.CCrmState) == C.sizeof(C.c_void_p) * 7
+    assert C.sizeof(T.CCrmConfig) == 6 * 4 + 3 * 8 + 4 * 4
+
+
+@pytest.mark.skipif(has_gpu(), reason='checks the no-device path')
+def test_create_without_device_fails_loudly(lib):
+    cfg = S.config0()
+    cfg.max_ncrms = 4
+    st = C.c_int(-1)
+    h = lib.crm_create(C.byref(cfg.to_c()), C.byref(st))
+    assert not h
+    assert st.value == T.CRM_ERR_NO_DEVICE
+    with pytest.raises(L.CrmError):
+        L.CrmContext(cfg)
+
+
+def test_invalid_configurations_are_rejected(lib):
+    for kw in ({'crm_nx': 30}, {'crm_nx': 7}, {'plev': 20}, {'crm_dt': 40.0}):
+        cfg = S.config0()
+        cfg.max_ncrms = 4
+        for k, v in kw.items():
+            setattr(cfg, k, v)
+        st = C.c_int(-1)
+        h = lib.crm_create(C.byref(cfg.to_c()), C.byref(st))
+        assert not h
+        assert st.value in (T.CRM_ERR_ARG, T.CRM_ERR_UNSUPPORTED), kw
+    for kw in ({'crm_ny': 4}, {'microphysics': T.CRM_MICRO_M2005},
+               {'batch_mode': T.CRM_REFERENCE_BATCH}):
+        cfg = S.config0()
+        cfg.max_ncrms = 4
+        for k, v in kw.items():
+            setattr(cfg, k, v)
+        st = C.c_int(-1)
+        assert not lib.crm_create(C.byref(cfg.to_c()), C.byref(st))
+        assert st.value == T.CRM_ERR_UNSUPPORTED, kw

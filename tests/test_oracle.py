@@ -1,0 +1,159 @@
+"""CPU checks of the oracle (the FP64 restatement of crm()).
+
+The reference ships no golden vectors for crm(), so these checks pin the
+restatement by properties the reference's algorithm has:
+
+  * the column water budget closes: the change of column water (qt + qp,
+    weighted by pdel/g) equals the large-scale forcing minus surface
+    precipitation, to rounding (flux-form MPDATA and sedimentation with
+    closed top and bottom, mass-conserving negative-water fixer);
+  * the periodic domain is translation invariant: rolling the initial state
+    in x rolls the result (to rounding in the FFT);
+  * a horizontally uniform state stays uniform;
+  * per-column mode makes every column independent of its batch mates, and
+    equals the reference's batch coupling when no column sub-cycles;
+  * the OpenMP thread count does not change a bit;
+  * a column that breaks the CFL limit is flagged without touching the rest.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from crm_gb300 import crm_types as T
+from crm_gb300 import synthetic as S
+
+GRAV = 9.80616
+
+
+def _run(cfg, cin, st, rad, desc, nthreads=0):
+    st, rad = st.copy(), rad.copy()
+    rc, stat, out = oracle.run(cfg, desc, cin, st, rad, nthreads=nthreads)
+    return rc, stat, st, rad, out
+
+
+def _equal(a, b):
+    """Names of the fields of (state, rad, out) that differ."""
+    bad = []
+    for x, y, tag in ((a[0], b[0], 'state'), (a[1], b[1], 'rad'), (a[2], b[2], 'out')):
+        for n, v in x.arrays().items():
+            if not np.array_equal(v, getattr(y, n)):
+                bad.append(tag + '.' + n)
+    return bad
+
+
+def water_residual(cfg, cin, st0, st1, out, dt_gl):
+    """Per column: (dW - forcing + P) / W0 with W the pdel/g-weighted column water."""
+    nz, plev = cfg.crm_nz, cfg.plev
+    res = []
+    for c in range(st0.qt.shape[0]):
+        pd = np.array([cin.pdel[c, plev - 1 - k] for k in range(nz)]) / GRAV
+        w0 = np.sum(pd * (st0.qt[c, :, 0, :] + st0.qp[c, :, 0, :]).mean(axis=0))
+        w1 = np.sum(pd * (st1.qt[c, :, 0, :] + st1.qp[c, :, 0, :]).mean(axis=0))
+        forc = np.sum(pd * np.array([out.qt_ls[c, plev - 1 - k] for k in range(nz)])) * dt_gl
+        prec = (out.precc[c] + out.precl[c]) * 1000.0 * dt_gl
+        res.append((w1 - w0 - forc + prec) / w0)
+    return np.array(res)
+
+
+@pytest.mark.parametrize('moist', [False, True])
+def test_water_budget_closes_32x28(moist):
+    cfg, cin, st, rad, desc = S.workload0(ncrms=4, moist=moist)
+    rc, stat, st1, _, out = _run(cfg, cin, st, rad, desc)
+    assert rc == 0 and not stat.any()
+    r = water_residual(cfg, cin, st, st1, out, desc.dt_gl)
+    assert np.max(np.abs(r)) < 1e-13, r
+    if moist:
+        assert np.all(out.precc + out.precl > 0)
+
+
+def test_water_budget_closes_64x58():
+    cfg, cin, st, rad, desc = S.workload1(ncrms=2, moist=True)
+    desc.dt_gl = 300.0
+    rc, stat, st1, _, out = _run(cfg, cin, st, rad, desc)
+    assert rc == 0 and not stat.any()
+    r = water_residual(cfg, cin, st, st1, out, desc.dt_gl)
+    assert np.max(np.abs(r)) < 1e-13, r
+
+
+def test_thread_count_does_not_change_results():
+    cfg, cin, st, rad, desc = S.workload0(ncrms=6, moist=True)
+    desc.dt_gl = 400.0
+    a = _run(cfg, cin, st, rad, desc, nthreads=1)
+    b = _run(cfg, cin, st, rad, desc, nthreads=3)
+    assert not _equal(a[2:], b[2:])
+
+
+def test_columns_independent_of_batch_mates():
+    cfg, cin, st, rad, desc = S.workload0(ncrms=6, moist=True)
+    desc.dt_gl = 400.0
+    full = _run(cfg, cin, st, rad, desc)
+    gcol = np.asarray(desc._keep)
+    for cols in ([0, 1, 2], [5, 3]):
+        d = T.call_desc(len(cols), len(cols), desc.dt_gl, desc.igstep, gcol[cols])
+        part = _run(cfg, cin.take(cols), st.take(cols), rad.take(cols), d)
+        ref = (full[2].take(cols), full[3].take(cols))
+        for n, v in ref[0].arrays().items():
+            assert np.array_equal(v, getattr(part[2], n)), n
+        for n, v in part[4].arrays().items():
+            assert np.array_equal(v, getattr(full[4], n)[cols]), n
+
+
+def test_reference_batch_mode_equals_per_column_without_subcycling():
+    cfg, cin, st, rad, desc = S.workload0(ncrms=4, moist=True)
+    desc.dt_gl = 400.0
+    a = _run(cfg, cin, st, rad, desc)
+    cfg_b = S.config0(batch_mode=T.CRM_REFERENCE_BATCH)
+    b = _run(cfg_b, cin, st, rad, desc)
+    assert a[0] == 0 and b[0] == 0
+    assert not _equal(a[2:], b[2:])
+
+
+def test_translation_invariance():
+    # The reference's fft991 builds its twiddles in REAL*4 (implicit typing in
+    # fft.F90), so forward and inverse transforms are exact inverses, and
+    # shift-equivariant, only to ~1e-7 relative: a shifted run differs at that
+    # level in the pressure correction.  An indexing or halo error would show
+    # as an O(1) difference of the perturbation fields.
+    cfg, cin, st, rad, desc = S.workload0(ncrms=2)
+    d = T.call_desc(2, 2, 100.0, 2, desc._keep)     # igstep 2: no setperturb
+    a = _run(cfg, cin, st, rad, d)
+    sh = 5
+    st_r = st.copy()
+    for n, v in st_r.arrays().items():
+        v[...] = np.roll(v, sh, axis=1)
+    b = _run(cfg, cin, st_r, rad, d)
+    for n, v in a[2].arrays().items():
+        x = np.roll(v, sh, axis=1)
+        y = getattr(b[2], n)
+        spread = np.max(np.abs(v - v.mean(axis=1, keepdims=True)))
+        if spread == 0.0:
+            assert np.array_equal(x, y), n
+            continue
+        assert np.max(np.abs(x - y)) <= 1e-4 * spread, (n, np.max(np.abs(x - y)), spread)
+    for n in ('sltend', 'qltend'):
+        x, y = getattr(a[4], n), getattr(b[4], n)
+        assert np.max(np.abs(x - y)) <= 1e-4 * (np.max(np.abs(x)) or 1.0), n
+
+
+def test_uniform_state_stays_uniform():
+    cfg, cin, st, rad, desc = S.workload0(ncrms=2)
+    st.temperature[...] = st.temperature[:, :1]     # drop the seeded perturbation
+    d = T.call_desc(2, 2, 400.0, 2, desc._keep)     # and setperturb
+    _, stat, st1, _, _ = _run(cfg, cin, st, rad, d)
+    assert not stat.any()
+    for n, v in st1.arrays().items():
+        spread = np.max(np.abs(v - v[:, :1]))
+        assert spread <= 1e-10 * (np.max(np.abs(v)) or 1.0), (n, spread)
+
+
+def test_cfl_violation_flags_only_that_column():
+    cfg, cin, st, rad, desc = S.workload0(ncrms=3)
+    desc.dt_gl = 100.0
+    st.w_wind[1, :, :, 10] = 2000.0
+    rc, stat, st1, _, out = _run(cfg, cin, st, rad, desc)
+    assert list(stat) == [0, T.CRM_ERR_CFL, 0]
+    assert rc == T.CRM_ERR_CFL
+    ok = _run(cfg, cin.take([0, 2]), st.take([0, 2]), rad.take([0, 2]),
+              T.call_desc(2, 2, 100.0, desc.igstep, np.asarray(desc._keep)[[0, 2]]))
+    for n, v in ok[2].arrays().items():
+        assert np.array_equal(v, getattr(st1, n)[[0, 2]]), n
