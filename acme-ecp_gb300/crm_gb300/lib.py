@@ -16,7 +16,7 @@ LIB_PATH = os.path.join(HERE, 'libcrm_gb300.so')
 
 EXPORTS = ('crm_create', 'crm_destroy', 'crm_run', 'crm_run_device', 'crm_last_launch_count',
            'crm_last_kernel_ms', 'crm_set_stream', 'crm_status_string', 'crm_version',
-           'crm_debug_phase_cycles')
+           'crm_debug_phase_cycles', 'crm_run_device_noalloc')
 
 _lib = None
 
@@ -51,6 +51,11 @@ def load(path=None, build_if_missing=False):
     lib.crm_run_device.argtypes = [C.c_void_p, C.POINTER(T.CCrmCallDesc), C.POINTER(T.CCrmInput),
                                    C.POINTER(T.CCrmState), C.POINTER(T.CCrmRad),
                                    C.POINTER(T.CCrmOutput), C.c_void_p, C.c_void_p]
+    lib.crm_run_device_noalloc.restype = C.c_int
+    lib.crm_run_device_noalloc.argtypes = [C.POINTER(T.CCrmConfig), C.POINTER(T.CCrmCallDesc),
+                                           C.POINTER(T.CCrmInput), C.POINTER(T.CCrmState),
+                                           C.POINTER(T.CCrmRad), C.POINTER(T.CCrmOutput),
+                                           C.c_void_p, C.c_void_p]
     lib.crm_last_launch_count.restype = C.c_int
     lib.crm_last_launch_count.argtypes = [C.c_void_p]
     lib.crm_last_kernel_ms.restype = C.c_double
@@ -72,6 +77,18 @@ def status_string(s):
         return load().crm_status_string(int(s)).decode()
     except OSError:
         return 'status %d' % s
+
+
+def run_device_noalloc(cfg, dev, stream=0):
+    """crm_run_device_noalloc on a DeviceCrmArrays bundle: no handle and no
+    device allocation (the library's fixed 32 MiB scratch is used instead).
+    Asynchronous; returns the crm_status of the call (argument and size
+    checks; CRM_ERR_TOO_LARGE when the call does not fit the scratch)."""
+    lib = load()
+    c_cfg = cfg.to_c()
+    return lib.crm_run_device_noalloc(C.byref(c_cfg), C.byref(dev.c_desc), C.byref(dev.c_in),
+                                      C.byref(dev.c_state), C.byref(dev.c_rad), C.byref(dev.c_out),
+                                      C.c_void_p(dev.status_ptr), C.c_void_p(stream))
 
 
 class CrmContext:

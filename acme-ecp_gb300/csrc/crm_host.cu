@@ -7,12 +7,15 @@
 // coefficients, microphysics.F90:500-507).  Per call two kernels run: the
 // per-column set-up (z0 and the setperturb draws, crm_prep.cu) and the
 // persistent column kernel (crm_kernel.cuh).  crm_run stages host arrays
-// through the handle's device buffers; crm_run_device takes device arrays.
+// through the handle's device buffers; crm_run_device takes device arrays;
+// crm_run_device_noalloc takes device arrays and no handle, and keeps its
+// scratch in a fixed static device array.
 #include <cuda_runtime.h>
 
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -364,6 +367,7 @@ const char *crm_status_string(int s) {
     case CRM_ERR_TIMEOUT: return "bounded device wait timed out";
     case CRM_ERR_BUDGET: return "HBM admission budget exhausted";
     case CRM_ERR_NO_DEVICE: return "no CUDA device";
+    case CRM_ERR_TOO_LARGE: return "call exceeds the 32 MiB fixed scratch of crm_run_device_noalloc";
   }
   return "unknown status";
 }
@@ -478,3 +482,219 @@ int crm_run(crm_ctx *c, const crm_call_desc *d, const crm_input_c *in, crm_state
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// crm_run_device_noalloc: the same two kernels with their scratch in one
+// fixed static device array instead of handle buffers.  Nothing here calls
+// cudaMalloc/cudaFree or allocates host memory: the per-configuration
+// constants are built in fixed-size host arrays on the stack and copied into
+// the static array on the caller's stream.
+
+namespace {
+
+// Scratch layout: [trigs | eign] [z0 (ncrms) | rnd (ncrms * 5 * nx)] [slabs].
+static __device__ __align__(256) unsigned char crm_noalloc_scratch[CRM_NOALLOC_SCRATCH_BYTES];
+
+constexpr int kNoallocMaxDevices = 64;
+constexpr int kNoallocMaxTrigs = 3 * CRM_NOALLOC_MAX_NX / 2 + 2 + CRM_NOALLOC_MAX_NX;
+
+struct NoallocDevice {
+  unsigned char *scratch = nullptr;   // device address of crm_noalloc_scratch
+  int nsm = 0;
+};
+NoallocDevice g_noalloc[kNoallocMaxDevices];
+std::mutex g_noalloc_mu;
+
+size_t round256(size_t n) { return (n + 255) / 256 * 256; }
+
+struct NoallocPlan {
+  crm::Layout L;
+  size_t esz, const_bytes, col_bytes, slab_bytes;
+  int ntrigs, neign, nslab;
+};
+
+// Host arithmetic only: what one call needs and how many slabs fit.
+int noalloc_plan(const crm_config &g, int ncrms, NoallocPlan &q) {
+  if (g.crm_nx > CRM_NOALLOC_MAX_NX) return CRM_ERR_TOO_LARGE;
+  q.esz = g.precision == CRM_FP64 ? sizeof(double) : sizeof(float);
+  q.L = crm::make_layout(g.crm_nx, g.crm_nz, g.plev, g.crm_nx_rad, (int)q.esz);
+  q.ntrigs = 3 * g.crm_nx / 2 + 2 + g.crm_nx;
+  q.neign = g.crm_nx + 1;
+  q.const_bytes = round256(sizeof(double) * (size_t)(q.ntrigs + q.neign));
+  q.col_bytes = round256(sizeof(double) * (size_t)ncrms * (1 + 5 * (size_t)g.crm_nx));
+  q.slab_bytes = round256(q.L.slab * q.esz);
+  const size_t cap = CRM_NOALLOC_SCRATCH_BYTES;
+  if (q.const_bytes > cap || q.col_bytes > cap - q.const_bytes ||
+      q.slab_bytes > cap - q.const_bytes - q.col_bytes)
+    return CRM_ERR_TOO_LARGE;
+  size_t n = (cap - q.const_bytes - q.col_bytes) / q.slab_bytes;
+  q.nslab = n > (size_t)ncrms ? ncrms : (int)n;
+  return CRM_OK;
+}
+
+// Once per device, with that device current: the array's device address.
+int noalloc_device(NoallocDevice &out) {
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return CRM_ERR_NO_DEVICE;
+  if (dev >= kNoallocMaxDevices) return CRM_ERR_ARG;
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  NoallocDevice &d = g_noalloc[dev];
+  if (!d.scratch) {
+    void *ptr = nullptr;
+    if (cudaGetSymbolAddress(&ptr, crm_noalloc_scratch) != cudaSuccess || !ptr) return CRM_ERR_CUDA;
+    int nsm = 0;
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm < 1)
+      return CRM_ERR_CUDA;
+    d.nsm = nsm;
+    d.scratch = static_cast<unsigned char *>(ptr);
+  }
+  out = d;
+  return CRM_OK;
+}
+
+}  // namespace
+
+extern "C" int crm_run_device_noalloc(const crm_config *cfg, const crm_call_desc *d, const crm_input_c *in,
+                                      crm_state_c *st, crm_rad_c *rad, crm_output_c *out, int *col_status,
+                                      void *stream) {
+  if (!cfg) return CRM_ERR_ARG;
+  crm_config g = *cfg;
+  g.max_ncrms = 1;   // no handle: the column count is bounded by the scratch only
+  int rc = validate(&g);
+  if (rc != CRM_OK) return rc;
+  if (!d || d->ncrms < 1 || d->ld < d->ncrms || !(d->dt_gl > 0)) return CRM_ERR_ARG;
+  const int ncrms = d->ncrms, nx = g.crm_nx;
+  NoallocPlan q;
+  rc = noalloc_plan(g, ncrms, q);
+  if (rc != CRM_OK) return rc;
+  if (!in || !st || !rad || !out || !col_status) return CRM_ERR_ARG;
+  if (!d->gcol && d->igstep <= 1) return CRM_ERR_ARG;
+  const double *need[] = {in->zmid, in->zint, in->tl, in->ql, in->qccl, in->qiil, in->pmid,
+                          in->pint, in->pdel, in->ul, in->vl, in->tau00, in->bflxls, in->wndls};
+  for (const double *x : need)
+    if (!x) return CRM_ERR_ARG;
+  double *sp[7] = {st->u_wind, st->v_wind, st->w_wind, st->temperature, st->qt, st->qp, st->qn};
+  for (double *x : sp)
+    if (!x) return CRM_ERR_ARG;
+  double *rp[5] = {rad->temperature, rad->qv, rad->qc, rad->qi, rad->cld};
+  if (!rad->qrad) return CRM_ERR_ARG;
+  for (double *x : rp)
+    if (!x) return CRM_ERR_ARG;
+  for (int f = 0; f < CRM_NOUT; ++f)
+    if (!out->field[f]) return CRM_ERR_ARG;
+  const int nstop = (int)(d->dt_gl / g.crm_dt);   // crm_module.F90:712-713
+  if (nstop < 1) return CRM_ERR_ARG;
+  const double dt = d->dt_gl / nstop;
+  if (60. < 2 * dt) return CRM_ERR_ARG;           // damping.F90:39-42
+
+  NoallocDevice dv;
+  rc = noalloc_device(dv);
+  if (rc != CRM_OK) return rc;
+  const int block = 256;
+  int per_sm = g.precision == CRM_FP64 ? crm::occupancy_crm_columns<double>(block, nx, g.crm_nz)
+                                       : crm::occupancy_crm_columns<float>(block, nx, g.crm_nz);
+  if (per_sm < 1) return CRM_ERR_UNSUPPORTED;
+  int grid = dv.nsm * per_sm;
+  if (grid > q.nslab) grid = q.nslab;
+
+  // per-configuration constants (the same tables alloc_ctx builds), on the stack
+  double consts[kNoallocMaxTrigs + CRM_NOALLOC_MAX_NX + 1];
+  int ifax[20];
+  fft_factors(ifax, nx);
+  {
+    double *trigs = consts;
+    for (int i = 0; i < q.ntrigs; ++i) trigs[i] = 0.0;
+    float pi_f = (float)(2.0f * asinf(1.0f));
+    int nn = nx / 2;
+    float del = (float)((double)(pi_f + pi_f) / (double)nn);
+    for (int i = 1; i <= nn + nn; i += 2) {
+      float angle = (float)(0.5 * (double)(i - 1) * (double)del);
+      trigs[i - 1] = (double)cosf(angle);
+      trigs[i] = (double)sinf(angle);
+    }
+    del = 0.5f * del;
+    int nh = (nn + 1) / 2, l = nh + nh, la = nn + nn;
+    for (int i = 1; i <= l; i += 2) {
+      float angle = (float)(0.5 * (double)(i - 1) * (double)del);
+      trigs[la + i - 1] = (double)cosf(angle);
+      trigs[la + i] = (double)sinf(angle);
+    }
+    double *eign = consts + q.ntrigs;
+    double dx = g.crm_dx, dy = g.crm_dx;
+    double ddx2 = 1.0 / (dx * dx), ddy2 = 1.0 / (dy * dy);
+    double pii = 3.14159265358979323846;
+    double xnx = pii / nx, xny = pii / 1;
+    int jd = (int)(((float)1 - 0.1f) / 2.f);
+    double xj = jd, facty = 2.0;
+    for (int i = 1; i <= nx + 1; ++i) {
+      int id = (int)(((float)i - 0.1f) / 2.f);
+      double xi = id, factx = 2.0;
+      eign[i - 1] = (2.0 * cos(factx * xnx * xi) - 2.0) * ddx2 + (2.0 * cos(facty * xny * xj) - 2.0) * ddy2;
+    }
+  }
+  double gam[10];
+  const double b_rain = R4H(0.8), b_snow = 0.25, b_grau = 0.5;
+  gam[0] = gammafff(3.f);
+  gam[1] = gammafff((float)(3. + b_rain));
+  gam[2] = gammafff((float)((5. + b_rain) / 2.));
+  gam[3] = gammafff((float)(4. + b_rain));
+  gam[4] = gammafff((float)(3. + b_snow));
+  gam[5] = gammafff((float)((5. + b_snow) / 2.));
+  gam[6] = gammafff((float)(4. + b_snow));
+  gam[7] = gammafff((float)(3. + b_grau));
+  gam[8] = gammafff((float)((5. + b_grau) / 2.));
+  gam[9] = gammafff((float)(4. + b_grau));
+  const double crain = b_rain / 4., csnow = b_snow / 4., cgrau = b_grau / 4.;
+
+  cudaStream_t s = (cudaStream_t)stream;
+  unsigned char *base = dv.scratch;
+  double *d_consts = reinterpret_cast<double *>(base);
+  double *d_col = reinterpret_cast<double *>(base + q.const_bytes);
+  void *d_slabs = base + q.const_bytes + q.col_bytes;
+  CK(cudaMemcpyAsync(d_consts, consts, sizeof(double) * (size_t)(q.ntrigs + q.neign), cudaMemcpyHostToDevice, s));
+
+  crm::PrepParams pp;
+  pp.ncrms = ncrms; pp.ld = d->ld; pp.plev = g.plev; pp.nx = nx; pp.igstep = d->igstep;
+  pp.zmid = in->zmid; pp.zint = in->zint; pp.pdel = in->pdel;
+  pp.tau00 = in->tau00; pp.bflxls = in->bflxls; pp.wndls = in->wndls;
+  pp.gcol = d->gcol;
+  pp.z0 = d_col;
+  pp.rnd = d_col + ncrms;
+  crm::KParams p;
+  memset(&p, 0, sizeof p);
+  p.L = q.L;
+  p.ncrms = ncrms; p.ld = d->ld; p.nstop = nstop; p.igstep = d->igstep;
+  p.batch_mode = g.batch_mode; p.clamp_batch = 0;
+  p.dx = g.crm_dx; p.dy = g.crm_dx; p.dt = dt; p.dt_gl = d->dt_gl;
+  p.gams1 = gam[4]; p.gams2 = gam[5]; p.gamg1 = gam[7]; p.gamg2 = gam[8];
+  p.gamr1 = gam[1]; p.gamr2 = gam[2];
+  p.vrain = 842. * gam[3] / 6. / det_pow(kPi4 * 1000. * 8.e6, crain);
+  p.vsnow = R4H(4.84) * gam[6] / 6. / det_pow(kPi4 * 100. * 3.e6, csnow);
+  p.vgrau = 94.5 * gam[9] / 6. / det_pow(kPi4 * 400. * 4.e6, cgrau);
+  p.crain = crain; p.csnow = csnow; p.cgrau = cgrau;
+  p.a_bg = 1. / (R4H(273.16) - R4H(253.16));
+  p.a_pr = 1. / (R4H(283.16) - R4H(268.16));
+  p.a_gr = 1. / (R4H(283.16) - R4H(223.16));
+  p.nfax = ifax[0];
+  for (int k = 0; k <= ifax[0] && k < 8; ++k) p.ifax[k] = ifax[k];
+  p.trigs = d_consts;
+  p.eign = d_consts + q.ntrigs;
+  p.z0 = pp.z0;
+  p.rnd = pp.rnd;
+  p.zmid = in->zmid; p.zint = in->zint; p.tl = in->tl; p.ql = in->ql; p.qccl = in->qccl;
+  p.qiil = in->qiil; p.pmid = in->pmid; p.pint = in->pint; p.pdel = in->pdel;
+  p.ul = in->ul; p.vl = in->vl;
+  for (int f = 0; f < 7; ++f) p.st[f] = sp[f];
+  p.qrad = rad->qrad;
+  for (int f = 0; f < 5; ++f) p.radout[f] = rp[f];
+  for (int f = 0; f < CRM_NOUT; ++f) p.out[f] = out->field[f];
+  p.slabs = d_slabs;
+  p.phase_cycles = nullptr;
+  p.next_col = nullptr;
+  p.col_status = col_status;
+  crm::launch_crm_prep(pp, s);
+  if (g.precision == CRM_FP64) crm::launch_crm_columns<double>(p, grid, block, s);
+  else crm::launch_crm_columns<float>(p, grid, block, s);
+  CK(cudaGetLastError());
+  return CRM_OK;
+}

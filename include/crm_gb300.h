@@ -44,7 +44,8 @@ enum crm_status {
   CRM_ERR_UNSUPPORTED = 5,  /* feature not built (e.g. m2005)                */
   CRM_ERR_TIMEOUT = 6,      /* a bounded device wait gave up                 */
   CRM_ERR_BUDGET = 7,       /* serving admission: HBM budget exhausted       */
-  CRM_ERR_NO_DEVICE = 8     /* no CUDA device                                */
+  CRM_ERR_NO_DEVICE = 8,    /* no CUDA device                                */
+  CRM_ERR_TOO_LARGE = 9     /* exceeds crm_run_device_noalloc's fixed scratch */
 };
 
 enum crm_microphysics { CRM_MICRO_SAM1MOM = 0, CRM_MICRO_M2005 = 1 };
@@ -165,6 +166,46 @@ int crm_run(crm_ctx *ctx, const crm_call_desc *desc, const crm_input_c *in,
 int crm_run_device(crm_ctx *ctx, const crm_call_desc *desc, const crm_input_c *in,
                    crm_state_c *state, crm_rad_c *rad, crm_output_c *out,
                    int *col_status, void *stream);
+
+/* Size of the fixed device scratch used by crm_run_device_noalloc [bytes]. */
+#define CRM_NOALLOC_SCRATCH_BYTES (32u << 20)
+#define CRM_NOALLOC_MAX_NX 1024
+
+/* crm_run_device without a handle and without any device allocation.  No
+ * counterpart in the reference (its crm() allocates the module arrays on
+ * every call, crm_module.F90:199-266).
+ *
+ * For callers that cannot allocate device memory at the point of the call:
+ * a host model whose own pool allocator has reserved the GPU's memory up
+ * front (so a cudaMalloc here would fail or fragment that pool), or a time
+ * step loop that must not pay the implicit device-wide synchronisation that
+ * cudaMalloc/cudaFree can cause while other streams are busy.
+ *
+ * Arguments are those of crm_run_device with the configuration in place of
+ * the handle: every array pointer is a device pointer, col_status (ncrms ints,
+ * device) is required, and the work is enqueued on `stream` (NULL: the legacy
+ * default stream) without synchronising.  cfg->max_ncrms is ignored.
+ *
+ * Scratch: one static device array of CRM_NOALLOC_SCRATCH_BYTES (32 MiB) in
+ * the library, holding the per-configuration constants (FP64 trig tables and
+ * Laplacian eigenvalues), the per-column set-up values (8 * (1 + 5 * nx)
+ * bytes per column) and as many per-column working slabs as fit; the column
+ * kernel then runs with that many CTAs (fewer than crm_run_device uses, so
+ * it is slower).  A call whose constants, per-column values and one slab do
+ * not fit, or with crm_nx > CRM_NOALLOC_MAX_NX, returns CRM_ERR_TOO_LARGE
+ * before touching the device.
+ *
+ * The array's device address is looked up once per device, by the first call
+ * made with that device current; make that first call before any stream
+ * capture begins.  Every call on a device shares the one array and leaves its
+ * last contents behind; nothing in it needs to start at zero (the kernel
+ * clears a column's slab when it starts the column, and the set-up values and
+ * constants are rewritten by every call).  Calls that overlap in time on the
+ * same device (different streams or host threads) race on the array: order
+ * them on one stream. */
+int crm_run_device_noalloc(const crm_config *cfg, const crm_call_desc *desc,
+                           const crm_input_c *in, crm_state_c *state, crm_rad_c *rad,
+                           crm_output_c *out, int *col_status, void *stream);
 
 /* Number of kernel launches issued by the last crm_run on this handle. */
 int crm_last_launch_count(const crm_ctx *ctx);

@@ -39,7 +39,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_status_strings_and_version(lib):
-    for s in range(9):
+    for s in range(10):
         assert lib.crm_status_string(s).decode() not in ('', 'unknown status'), s
     assert lib.crm_status_string(99).decode() == 'unknown status'
     assert b'sm_103a' in lib.crm_version()
@@ -84,3 +84,19 @@ def test_invalid_configurations_are_rejected(lib):
         st = C.c_int(-1)
         assert not lib.crm_create(C.byref(cfg.to_c()), C.byref(st))
         assert st.value == T.CRM_ERR_UNSUPPORTED, kw
+
+
+def test_noalloc_rejects_oversize_before_touching_the_device(lib):
+    # set-up values of 100000 columns (257 MB) or crm_nx 2048 exceed the fixed
+    # 32 MiB scratch of crm_run_device_noalloc; the check needs no GPU
+    cfg = S.config1()
+    d = T.CCrmCallDesc(0, 100000, 100000, 100.0, 2, None)
+    rc = lib.crm_run_device_noalloc(C.byref(cfg.to_c()), C.byref(d), C.byref(T.CCrmInput()),
+                                    C.byref(T.CCrmState()), C.byref(T.CCrmRad()),
+                                    C.byref(T.CCrmOutput()), None, None)
+    assert rc == T.CRM_ERR_TOO_LARGE
+    d = T.CCrmCallDesc(0, 1, 1, 100.0, 2, None)
+    rc = lib.crm_run_device_noalloc(C.byref(S.config1(nx=2048).to_c()), C.byref(d),
+                                    C.byref(T.CCrmInput()), C.byref(T.CCrmState()),
+                                    C.byref(T.CCrmRad()), C.byref(T.CCrmOutput()), None, None)
+    assert rc == T.CRM_ERR_TOO_LARGE
