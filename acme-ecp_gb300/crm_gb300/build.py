@@ -1,11 +1,12 @@
 """Build libcrm_gb300.so (sm_103a) in-tree with nvcc.
 
-Four translation units, compiled in parallel:
-  crm_fp64.cu  FP64 column kernel, -fmad=false (bit-identical to a CPU run)
-  crm_fp32.cu  FP32-mixed column kernel
-  crm_prep.cu  per-column set-up kernel (z0, setperturb draws), -fmad=false
-  crm_host.cu  the C ABI (include/crm_gb300.h), host code built with
-               -ffp-contract=off for the same reason
+Objects, compiled in parallel:
+  crm_columns.cu  the column kernel, once per (precision, launch shape):
+                  FP64 with -fmad=false (bit-identical to a CPU run of the
+                  same algorithm), and the FP32-mixed form
+  crm_prep.cu     per-column set-up kernel (z0, setperturb draws), -fmad=false
+  crm_host.cu     the C ABI (include/crm_gb300.h), host code built with
+                  -ffp-contract=off for the same reason
 """
 import os
 import subprocess
@@ -23,12 +24,14 @@ OBJ = os.path.join(PKG, '_build')
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 COMMON = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC,-ffp-contract=off',
           '-I' + os.path.join(REPO, 'include')]
-UNITS = {
-    'crm_fp64': ['-fmad=false'],
-    'crm_fp32': [],
-    'crm_prep': ['-fmad=false'],
-    'crm_host': [],
-}
+NUM_SHAPES = 3             # crm_kernel.h kShapes
+NX_BUILT = (32, 64, 128, 0)  # crm_kernel.h kNxBuilt (0: generic nx)
+UNITS = {'crm_prep': ('crm_prep', ['-fmad=false']), 'crm_host': ('crm_host', [])}
+for _n in NX_BUILT:
+    for _s in range(NUM_SHAPES):
+        _d = ['-DCRM_INST_NX=%d' % _n, '-DCRM_INST_SHAPE=%d' % _s]
+        UNITS['crm_fp64_nx%d_s%d' % (_n, _s)] = ('crm_columns', ['-fmad=false', '-DCRM_INST_T=double'] + _d)
+        UNITS['crm_fp32_nx%d_s%d' % (_n, _s)] = ('crm_columns', ['-DCRM_INST_T=float'] + _d)
 
 
 def _nvcc():
@@ -67,7 +70,8 @@ def build(force=False, verbose=False, phase_timers=False):
 
     def compile_unit(name):
         obj = os.path.join(odir, name + '.o')
-        cmd = [nvcc] + ARCH + COMMON + extra + UNITS[name] + ['-c', os.path.join(CSRC, name + '.cu'), '-o', obj]
+        src, flags = UNITS[name]
+        cmd = [nvcc] + ARCH + COMMON + extra + flags + ['-c', os.path.join(CSRC, src + '.cu'), '-o', obj]
         if verbose:
             print(' '.join(cmd), file=sys.stderr)
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -75,7 +79,7 @@ def build(force=False, verbose=False, phase_timers=False):
             raise RuntimeError('nvcc failed for %s:\n%s%s' % (name, r.stdout, r.stderr))
         return obj
 
-    with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
+    with ThreadPoolExecutor(max_workers=min(len(UNITS), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(compile_unit, UNITS))
     tmp = lib + '.tmp'
     cmd = [nvcc] + ARCH + ['-shared', '-o', tmp] + objs

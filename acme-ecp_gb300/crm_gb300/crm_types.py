@@ -94,7 +94,7 @@ class CCrmOutput(C.Structure):
 class CCrmCallDesc(C.Structure):
     _fields_ = [('lchnk', C.c_int), ('ncrms', C.c_int), ('ld', C.c_int),
                 ('dt_gl', C.c_double), ('igstep', C.c_int),
-                ('gcol', C.POINTER(C.c_int))]
+                ('gcol', C.POINTER(C.c_int)), ('col_map', C.POINTER(C.c_int))]
 
 
 def _ptr(a):

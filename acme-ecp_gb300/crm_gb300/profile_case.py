@@ -22,9 +22,13 @@ def main():
     ap.add_argument('--precision', default='fp32', choices=['fp32', 'fp64'])
     ap.add_argument('--reps', type=int, default=2)
     ap.add_argument('--nx', type=int, default=64)
+    ap.add_argument('--shape', type=int, default=None,
+                    help='column-kernel launch shape index (crm_kernel.h kShapes)')
     ap.add_argument('--phase-timers', action='store_true',
                     help='use the profiling build and print cycles per phase')
     args = ap.parse_args()
+    if args.shape is not None:
+        os.environ['CRM_GB300_SHAPE'] = str(args.shape)
     import torch
     from crm_gb300 import build as B
     from crm_gb300 import synthetic as S
@@ -48,6 +52,11 @@ def main():
         print('rep %d: %.3f ms  (%.0f column-steps/s)' % (r, ms, args.ncrms * nstop / (ms / 1000.0)))
     torch.cuda.synchronize()
     assert int(dev.status.sum().item()) == 0
+    import hashlib
+    h = hashlib.sha256()
+    for n in sorted(dev.state):
+        h.update(dev.state[n].cpu().numpy().tobytes())
+    print('state sha256 %s' % h.hexdigest()[:16])
     if args.phase_timers:
         from crm_gb300.crm_types import PHASE_NAMES
         cyc = ctx.phase_cycles()

@@ -1,0 +1,365 @@
+"""Continuous-batching CRM service: resident column state, HBM admission,
+per-chunk latency.
+
+The reference integrates the CRMs of each GCM chunk synchronously inside
+crm_physics_tend (cam/crm_physics.F90:1145-1156) and keeps every column's CRM
+state in the physics buffer between GCM steps (pbuf 'global' fields,
+crm_physics.F90:126-191).  Here the same two facts are organised for a GPU
+that serves many chunks at once:
+
+  * each chunk (1..64 GCM columns of one CRM configuration) is *admitted*:
+    it receives slots in a device-resident pool of its configuration, if the
+    pool has room and the HBM budget allows; otherwise it waits;
+  * its CRM state stays in those slots across GCM steps; a step request
+    carries only the new GCM input profiles;
+  * the engine thread gathers every step request that is waiting, groups
+    them by configuration and launches ONE column kernel per group over the
+    union of their slots (crm_run_device with a col_map), so requests that
+    arrive while others are on the GPU join the next launch; groups of
+    different configurations and successive launches of one configuration
+    run on their own streams and overlap on the device;
+  * results (the crm_output fields a GCM step consumes) are copied back per
+    request and its future completes; latency = submit -> results on host.
+
+Per-column mode makes every column's result independent of what it is
+batched with, so a chunk gets the same bits alone and in any mix.
+"""
+import ctypes as C
+import queue
+import threading
+import time
+from concurrent.futures import Future
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import crm_types as T
+
+# crm_output fields returned to the GCM per step (what crm_physics_tend reads
+# back for ptend and the surface fluxes, crm_physics.F90:1163-1300)
+STEP_OUTPUTS = ('sltend', 'qltend', 'qcltend', 'qiltend', 'precc', 'precl', 'precsc',
+                'precsl', 'cltot', 'prectend', 'precstend', 'taux', 'tauy', 'z0m')
+
+
+class SlotPool:
+    """Free-list of column slots 0..capacity-1 (host logic only)."""
+
+    def __init__(self, capacity):
+        self.capacity = int(capacity)
+        self._free = list(range(self.capacity - 1, -1, -1))
+        self._lock = threading.Lock()
+
+    def alloc(self, n):
+        with self._lock:
+            if n > len(self._free):
+                return None
+            return [self._free.pop() for _ in range(n)]
+
+    def free(self, slots):
+        with self._lock:
+            for s in sorted(slots, reverse=True):
+                if s in self._free:
+                    raise ValueError('slot %d freed twice' % s)
+                self._free.append(s)
+
+    @property
+    def available(self):
+        return len(self._free)
+
+
+class HbmBudget:
+    """Bytes of device memory the service may hold for resident columns."""
+
+    def __init__(self, total_bytes):
+        self.total = int(total_bytes)
+        self.used = 0
+        self._lock = threading.Lock()
+
+    def reserve(self, nbytes):
+        with self._lock:
+            if self.used + nbytes > self.total:
+                return False
+            self.used += nbytes
+            return True
+
+    def release(self, nbytes):
+        with self._lock:
+            self.used -= nbytes
+            if self.used < 0:
+                raise ValueError('budget released below zero')
+
+
+def slot_bytes(cfg):
+    """Device bytes one resident column of this configuration holds."""
+    nx, nz, plev, nxr = cfg.crm_nx, cfg.crm_nz, cfg.plev, cfg.crm_nx_rad
+    state = 7 * nx * nz
+    rad = 6 * nxr * nz
+    inp = 11 * (plev + 1) + 10
+    out = 6 * nx * nz + nx + 16 + 39 * plev
+    return 8 * (state + rad + inp + out) + 8
+
+
+def config_key(cfg):
+    return (cfg.crm_nx, cfg.crm_nz, cfg.plev, cfg.crm_dx, cfg.crm_dt, cfg.precision)
+
+
+class DevicePool:
+    """Device arrays of one configuration with ld = capacity (torch tensors
+    in Fortran layout: the column slot is the fastest index), plus the C ABI
+    handles that integrate any subset of the slots."""
+
+    def __init__(self, cfg, capacity, handles=2):
+        import torch
+        from .lib import CrmContext
+        self.torch = torch
+        self.cfg = T.CrmConfig(**{**cfg.__dict__, 'max_ncrms': capacity})
+        self.capacity = capacity
+        self.slots = SlotPool(capacity)
+        dev = 'cuda'
+        ld, nx, nz, plev = capacity, cfg.crm_nx, cfg.crm_nz, cfg.plev
+        z = T.CrmInput.zeros(1, plev)
+        self.inp = {n: torch.zeros(a.shape[1:][::-1] + (ld,), dtype=torch.float64, device=dev)
+                    for n, a in z.arrays().items()}
+        self.state = {n: torch.zeros((nz, 1, nx, ld), dtype=torch.float64, device=dev)
+                      for n in T.STATE_FIELDS}
+        self.rad = {n: torch.zeros((nz, 1, cfg.crm_nx_rad, ld), dtype=torch.float64, device=dev)
+                    for n in T.RAD_FIELDS}
+        o = T.CrmOutput(1, nx, 1, nz, plev)
+        self.out = {n: torch.zeros(a.shape[1:][::-1] + (ld,), dtype=torch.float64, device=dev)
+                    for n, a in o.arrays().items()}
+        dp = lambda t: C.cast(C.c_void_p(t.data_ptr()), C.POINTER(C.c_double))
+        self.c_in = T.CCrmInput(*[dp(self.inp[n]) for n in T.INPUT_FIELDS])
+        self.c_state = T.CCrmState(*[dp(self.state[n]) for n in T.STATE_FIELDS])
+        self.c_rad = T.CCrmRad(*[dp(self.rad[n]) for n in T.RAD_FIELDS])
+        self.c_out = T.CCrmOutput()
+        for i, (n, _) in enumerate(T.OUTPUT_FIELDS):
+            self.c_out.field[i] = dp(self.out[n])
+        self.ctx = [CrmContext(self.cfg) for _ in range(handles)]
+        self.streams = [torch.cuda.Stream() for _ in range(handles)]
+        self._next = 0
+        # per-launch device scratch: col_map, gcol, status (one set per handle)
+        self.d_map = [torch.zeros(capacity, dtype=torch.int32, device=dev) for _ in range(handles)]
+        self.d_gcol = [torch.zeros(capacity, dtype=torch.int32, device=dev) for _ in range(handles)]
+        self.d_status = [torch.zeros(capacity, dtype=torch.int32, device=dev) for _ in range(handles)]
+
+    # -- host <-> slots (on a given stream)
+    def _scatter(self, dst, slots_t, host):
+        """dst[..., slots] = host, host an (n, ...) Fortran-order bundle array
+        (its transpose has the device layout: the column index last)."""
+        torch = self.torch
+        src = torch.from_numpy(np.ascontiguousarray(host.T)).pin_memory()
+        dst.index_copy_(dst.dim() - 1, slots_t, src.to(dst.device, non_blocking=True))
+
+    def load(self, slots, cin, st, rad, stream):
+        torch = self.torch
+        with torch.cuda.stream(stream):
+            s = torch.tensor(slots, dtype=torch.int64).to('cuda', non_blocking=True)
+            for n, a in st.arrays().items():
+                self._scatter(self.state[n], s, a[:len(slots)])
+            for n, a in rad.arrays().items():
+                self._scatter(self.rad[n], s, a[:len(slots)])
+            self.set_inputs(slots, cin, stream, s)
+
+    def set_inputs(self, slots, cin, stream, s=None):
+        torch = self.torch
+        with torch.cuda.stream(stream):
+            if s is None:
+                s = torch.tensor(slots, dtype=torch.int64).to('cuda', non_blocking=True)
+            for n, a in cin.arrays().items():
+                self._scatter(self.inp[n], s, a[:len(slots)])
+
+    def gather(self, slots, names, stream):
+        """{name: pinned host tensor (..., n)} for the given slots, copied
+        asynchronously on `stream` (valid once the stream reaches it)."""
+        torch = self.torch
+        res = {}
+        with torch.cuda.stream(stream):
+            s = torch.tensor(slots, dtype=torch.int64).to('cuda', non_blocking=True)
+            for n in names:
+                t = self.out[n].index_select(self.out[n].dim() - 1, s)
+                h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+                h.copy_(t, non_blocking=True)
+                res[n] = h
+        return res
+
+    def launch(self, slots, gcol, igstep, dt_gl):
+        """One column kernel over `slots`; returns (handle index, stream)."""
+        from .lib import CrmError
+        torch = self.torch
+        h = self._next
+        self._next = (self._next + 1) % len(self.ctx)
+        stream = self.streams[h]
+        n = len(slots)
+        with torch.cuda.stream(stream):
+            self.d_map[h][:n].copy_(torch.tensor(slots, dtype=torch.int32), non_blocking=True)
+            self.d_gcol[h][:n].copy_(torch.tensor(gcol, dtype=torch.int32), non_blocking=True)
+        desc = T.CCrmCallDesc(0, n, self.capacity, float(dt_gl), int(igstep),
+                              C.cast(C.c_void_p(self.d_gcol[h].data_ptr()), C.POINTER(C.c_int)),
+                              C.cast(C.c_void_p(self.d_map[h].data_ptr()), C.POINTER(C.c_int)))
+        lib = self.ctx[h]._lib
+        rc = lib.crm_run_device(self.ctx[h]._h, C.byref(desc), C.byref(self.c_in), C.byref(self.c_state),
+                                C.byref(self.c_rad), C.byref(self.c_out),
+                                C.c_void_p(self.d_status[h].data_ptr()), C.c_void_p(stream.cuda_stream))
+        if rc != T.CRM_OK:
+            raise CrmError(rc, 'crm_run_device')
+        return h, stream
+
+
+@dataclass
+class Chunk:
+    """An admitted GCM chunk: its configuration, slots and global columns."""
+    key: tuple
+    slots: list
+    gcol: list
+    nbytes: int
+    steps: int = 0
+
+
+@dataclass
+class StepRequest:
+    chunk: Chunk
+    cin: object
+    dt_gl: float
+    future: Future = field(default_factory=Future)
+    t_submit: float = 0.0
+
+
+class CrmServer:
+    """The service: open_chunk / step / close_chunk; see the module docstring."""
+
+    def __init__(self, configs, capacity=1024, hbm_budget=120 * 2 ** 30, handles=2):
+        self.configs = {config_key(c): c for c in configs}
+        self.capacity = capacity
+        self.budget = HbmBudget(hbm_budget)
+        self.handles = handles
+        self.pools = {}
+        self._q = queue.Queue()
+        self._stop = threading.Event()
+        self._pending = []
+        self.launches = 0
+        self.latencies = []
+        self._lock = threading.Lock()
+        self._thread = threading.Thread(target=self._engine, daemon=True)
+        self._thread.start()
+
+    def pool(self, key):
+        with self._lock:
+            p = self.pools.get(key)
+            if p is None:
+                p = DevicePool(self.configs[key], self.capacity, self.handles)
+                self.pools[key] = p
+            return p
+
+    # -- admission
+    def open_chunk(self, cfg, cin, st, rad, gcol, timeout=60.0):
+        """Admit a chunk: slots + budget, then its state is copied in.
+        Waits (up to timeout s) while the pool or the budget is full."""
+        key = config_key(cfg)
+        pool = self.pool(key)
+        n = len(gcol)
+        nbytes = n * slot_bytes(cfg)
+        t0 = time.perf_counter()
+        while True:
+            if self.budget.reserve(nbytes):
+                slots = pool.slots.alloc(n)
+                if slots is not None:
+                    break
+                self.budget.release(nbytes)
+            if time.perf_counter() - t0 > timeout:
+                raise TimeoutError('admission timed out')
+            time.sleep(0.001)
+        stream = pool.streams[0]
+        pool.load(slots, cin, st, rad, stream)
+        stream.synchronize()
+        return Chunk(key, slots, list(gcol), nbytes)
+
+    def close_chunk(self, chunk):
+        self.pools[chunk.key].slots.free(chunk.slots)
+        self.budget.release(chunk.nbytes)
+
+    # -- steps
+    def step(self, chunk, cin, dt_gl):
+        """Submit one GCM step of a chunk (new input profiles); returns a
+        Future of ({output name: (n, ...) array}, status array)."""
+        r = StepRequest(chunk, cin, dt_gl)
+        r.t_submit = time.perf_counter()
+        self._q.put(r)
+        return r.future
+
+    def close(self):
+        self._stop.set()
+        self._q.put(None)
+        self._thread.join(timeout=30)
+
+    def _engine(self):
+        import torch
+        torch.cuda.set_device(0)
+        inflight = []        # (requests, pool, handle, stream, event)
+        while not self._stop.is_set():
+            # take everything waiting (block briefly when idle)
+            reqs = []
+            try:
+                r = self._q.get(timeout=0.0005 if inflight else 0.05)
+                if r is not None:
+                    reqs.append(r)
+                while True:
+                    r = self._q.get_nowait()
+                    if r is not None:
+                        reqs.append(r)
+            except queue.Empty:
+                pass
+            groups = {}
+            for r in reqs:
+                groups.setdefault((r.chunk.key, r.dt_gl, r.chunk.steps == 0), []).append(r)
+            for (key, dt_gl, first), rs in groups.items():
+                pool = self.pools[key]
+                slots, gcol = [], []
+                for r in rs:
+                    slots += r.chunk.slots
+                    gcol += r.chunk.gcol
+                h = pool._next
+                stream = pool.streams[h]
+                for r in rs:
+                    pool.set_inputs(r.chunk.slots, r.cin, stream)
+                try:
+                    h, stream = pool.launch(slots, gcol, 1 if first else 2, dt_gl)
+                except Exception as e:    # argument errors: fail these requests
+                    for r in rs:
+                        r.future.set_exception(e)
+                    continue
+                outs = [(r, pool.gather(r.chunk.slots, STEP_OUTPUTS, stream)) for r in rs]
+                st = torch.empty(len(slots), dtype=torch.int32, pin_memory=True)
+                with torch.cuda.stream(stream):
+                    st.copy_(pool.d_status[h][:len(slots)], non_blocking=True)
+                ev = torch.cuda.Event()
+                ev.record(stream)
+                inflight.append((outs, st, ev))
+                self.launches += 1
+            still = []
+            for outs, st, ev in inflight:
+                if ev.query():
+                    status = st.numpy()
+                    o = 0
+                    t_done = time.perf_counter()
+                    for r, res in outs:
+                        n = len(r.chunk.slots)
+                        r.chunk.steps += 1
+                        vals = {k: v.numpy().T.copy() for k, v in res.items()}
+                        with self._lock:
+                            self.latencies.append(t_done - r.t_submit)
+                        r.future.set_result((vals, status[o:o + n].copy()))
+                        o += n
+                else:
+                    still.append((outs, st, ev))
+            inflight = still
+
+
+def apply_tendencies(cin, vals, dt_gl, cpair=1.00464e3):
+    """Advance the GCM columns by the CRM tendencies, as physics_update does
+    with ptend (state += ptend * dt): T += sltend/cp dt, q += qltend dt, ..."""
+    n = vals['sltend'].shape[0]
+    cin.tl[:n] += vals['sltend'] / cpair * dt_gl
+    cin.ql[:n] = np.maximum(cin.ql[:n] + vals['qltend'] * dt_gl, 0.0)
+    cin.qccl[:n] = np.maximum(cin.qccl[:n] + vals['qcltend'] * dt_gl, 0.0)
+    cin.qiil[:n] = np.maximum(cin.qiil[:n] + vals['qiltend'] * dt_gl, 0.0)
+    return cin

@@ -170,11 +170,11 @@ def workload0(ncrms=16, seed=0, moist=False, **kw):
     return (cfg,) + make_inputs(cfg, ncrms, 300.0, 10.0, 100.0, seed=seed, moist=moist)
 
 
-def workload1(ncrms=1024, seed=0, nx=64, moist=False, **kw):
+def workload1(ncrms=1024, seed=0, nx=64, moist=False, gcol0=1, **kw):
     """lat ~ U[-60, 60] deg (seeded), T_sfc = 271 + 29 cos(lat), fluxes * cos(lat)."""
     cfg = config1(nx=nx, **kw)
     rng = np.random.Generator(np.random.PCG64(10_000 + seed))
     lat = rng.uniform(-60.0, 60.0, size=ncrms)
     cl = np.cos(np.deg2rad(lat))
     return (cfg,) + make_inputs(cfg, ncrms, 271.0 + 29.0 * cl, 10.0 * cl,
-                                100.0 * cl, seed=seed, moist=moist)
+                                100.0 * cl, seed=seed, moist=moist, gcol0=gcol0)

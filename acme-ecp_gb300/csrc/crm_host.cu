@@ -14,6 +14,7 @@
 
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <new>
@@ -30,7 +31,7 @@ using namespace crm_detmath;
 struct crm_ctx {
   crm_config cfg;
   crm::Layout L;
-  int device = 0, nsm = 0, block = 256, grid_max = 0;
+  int device = 0, nsm = 0, shape = 0, grid_max = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -62,10 +63,58 @@ struct PrepParams {
   int ncrms, ld, plev, nx, igstep;
   const double *zmid, *zint, *pdel, *tau00, *bflxls, *wndls;
   const int *gcol;
+  const int *col_map;
   double *z0;
   double *rnd;
 };
 void launch_crm_prep(const PrepParams &p, cudaStream_t s);
+
+template <typename T, int NX>
+static void launch_tn(int shape, const KParams &p, int grid, cudaStream_t s) {
+  switch (shape) {
+    case 0: launch_crm_columns<T, NX, 0>(p, grid, s); break;
+    case 1: launch_crm_columns<T, NX, 1>(p, grid, s); break;
+    default: launch_crm_columns<T, NX, 2>(p, grid, s); break;
+  }
+}
+
+template <typename T, int NX>
+static int occupancy_tn(int shape, int nx, int nzm) {
+  switch (shape) {
+    case 0: return occupancy_crm_columns<T, NX, 0>(nx, nzm);
+    case 1: return occupancy_crm_columns<T, NX, 1>(nx, nzm);
+    default: return occupancy_crm_columns<T, NX, 2>(nx, nzm);
+  }
+}
+
+template <typename T>
+static void launch_t(int shape, const KParams &p, int grid, cudaStream_t s) {
+  switch (p.L.nx) {
+    case 32: launch_tn<T, 32>(shape, p, grid, s); break;
+    case 64: launch_tn<T, 64>(shape, p, grid, s); break;
+    case 128: launch_tn<T, 128>(shape, p, grid, s); break;
+    default: launch_tn<T, 0>(shape, p, grid, s); break;
+  }
+}
+
+template <typename T>
+static int occupancy_t(int shape, int nx, int nzm) {
+  switch (nx) {
+    case 32: return occupancy_tn<T, 32>(shape, nx, nzm);
+    case 64: return occupancy_tn<T, 64>(shape, nx, nzm);
+    case 128: return occupancy_tn<T, 128>(shape, nx, nzm);
+    default: return occupancy_tn<T, 0>(shape, nx, nzm);
+  }
+}
+
+void launch_columns(int precision, int shape, const KParams &p, int grid, cudaStream_t s) {
+  if (precision == CRM_FP64) launch_t<double>(shape, p, grid, s);
+  else launch_t<float>(shape, p, grid, s);
+}
+
+int occupancy_columns(int precision, int shape, int nx, int nzm) {
+  return precision == CRM_FP64 ? occupancy_t<double>(shape, nx, nzm) : occupancy_t<float>(shape, nx, nzm);
+}
 }  // namespace crm
 
 namespace {
@@ -130,6 +179,19 @@ size_t out_elems(const crm_config &c, int f, int ld) {
     if (e_ != cudaSuccess) return CRM_ERR_CUDA;   \
   } while (0)
 
+// Launch shape of the column kernel per precision (crm_kernel.h kShapes),
+// chosen by measurement on GB300; CRM_GB300_SHAPE=<index> overrides it.
+int default_shape(int precision) {
+  const char *e = getenv("CRM_GB300_SHAPE");
+  if (e && *e) {
+    int v = atoi(e);
+    if (v >= 0 && v < crm::kNumShapes) return v;
+  }
+  // measured, 1024 columns of 64 x 58: FP64 (256 threads, 3 CTAs/SM),
+  // FP32-mixed (256 threads, 4 CTAs/SM)
+  return precision == CRM_FP64 ? 1 : 2;
+}
+
 int validate(const crm_config *c) {
   if (!c) return CRM_ERR_ARG;
   if (c->crm_ny != 1) return CRM_ERR_UNSUPPORTED;          // 3D not built
@@ -155,9 +217,9 @@ int alloc_ctx(crm_ctx *c) {
   CK(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, c->device));
   const size_t esz = g.precision == CRM_FP64 ? sizeof(double) : sizeof(float);
   c->L = crm::make_layout(g.crm_nx, g.crm_nz, g.plev, g.crm_nx_rad, (int)esz);
-  int per_sm = g.precision == CRM_FP64 ? crm::occupancy_crm_columns<double>(c->block, g.crm_nx, g.crm_nz)
-                                       : crm::occupancy_crm_columns<float>(c->block, g.crm_nx, g.crm_nz);
-  if (per_sm < 1) per_sm = 1;
+  c->shape = default_shape(g.precision);
+  int per_sm = crm::occupancy_columns(g.precision, c->shape, g.crm_nx, g.crm_nz);
+  if (per_sm < 1) return CRM_ERR_UNSUPPORTED;
   c->grid_max = c->nsm * per_sm;
   if (c->grid_max > g.max_ncrms) c->grid_max = g.max_ncrms;
   c->slab_bytes = c->L.slab * esz;
@@ -165,7 +227,7 @@ int alloc_ctx(crm_ctx *c) {
   c->ld_cap = g.max_ncrms;
   const int ld = c->ld_cap, plev = g.plev, nx = g.crm_nx, nz = g.crm_nz;
   c->in_elems = (size_t)ld * (plev + 1);
-  // GCM profiles, then tau00, bflxls, wndls (ld each) and gcol (ld ints)
+  // GCM profiles, then tau00, bflxls, wndls (ld each), gcol and col_map (ld ints each)
   CK(cudaMalloc(&c->d_in, sizeof(double) * c->in_elems * I_NIN + sizeof(double) * 4 * ld));
   CK(cudaMalloc(&c->d_state, sizeof(double) * (size_t)ld * nx * nz * 7));
   CK(cudaMalloc(&c->d_rad, sizeof(double) * (size_t)ld * g.crm_nx_rad * nz * 6));
@@ -261,6 +323,7 @@ int enqueue(crm_ctx *c, const crm_call_desc *d, const crm_input_c *in, crm_state
   pp.zmid = in->zmid; pp.zint = in->zint; pp.pdel = in->pdel;
   pp.tau00 = in->tau00; pp.bflxls = in->bflxls; pp.wndls = in->wndls;
   pp.gcol = d->gcol;
+  pp.col_map = d->col_map;
   pp.z0 = c->d_colconst;
   pp.rnd = c->d_colconst + g.max_ncrms;
   crm::KParams p;
@@ -288,13 +351,13 @@ int enqueue(crm_ctx *c, const crm_call_desc *d, const crm_input_c *in, crm_state
   for (int f = 0; f < 5; ++f) p.radout[f] = rp[f];
   for (int f = 0; f < CRM_NOUT; ++f) p.out[f] = out->field[f];
   p.slabs = c->slabs;
+  p.col_map = d->col_map;
   p.phase_cycles = c->d_phase;
   p.col_status = d_status ? d_status : c->d_status;
   int grid = ncrms < c->grid_max ? ncrms : c->grid_max;
   CK(cudaEventRecord(c->ev0, s));
   crm::launch_crm_prep(pp, s);
-  if (g.precision == CRM_FP64) crm::launch_crm_columns<double>(p, grid, c->block, s);
-  else crm::launch_crm_columns<float>(p, grid, c->block, s);
+  crm::launch_columns(g.precision, c->shape, p, grid, s);
   CK(cudaGetLastError());
   CK(cudaEventRecord(c->ev1, s));
   c->last_launches = 2;
@@ -430,8 +493,11 @@ int crm_run(crm_ctx *c, const crm_call_desc *d, const crm_input_c *in, crm_state
   }
   int *dgcol = reinterpret_cast<int *>(scal + (size_t)3 * c->ld_cap);
   if (d->gcol) CK(cudaMemcpyAsync(dgcol, d->gcol, sizeof(int) * ncrms, cudaMemcpyHostToDevice, s));
+  int *dmap = dgcol + c->ld_cap;
+  if (d->col_map) CK(cudaMemcpyAsync(dmap, d->col_map, sizeof(int) * ncrms, cudaMemcpyHostToDevice, s));
   crm_call_desc dd = *d;
   dd.gcol = d->gcol ? dgcol : nullptr;
+  dd.col_map = d->col_map ? dmap : nullptr;
   double *sp[7] = {st->u_wind, st->v_wind, st->w_wind, st->temperature, st->qt, st->qp, st->qn};
   const size_t n4 = (size_t)ld * nx * nz;
   crm_state_c dst_state;
@@ -455,17 +521,34 @@ int crm_run(crm_ctx *c, const crm_call_desc *d, const crm_input_c *in, crm_state
     dout.field[f] = c->d_out + o;
     o += out_elems(g, f, ld);
   }
-  CK(cudaMemsetAsync(c->d_out, 0, sizeof(double) * o, s));
+  double *rp[5] = {rad->temperature, rad->qv, rad->qc, rad->qi, rad->cld};
+  // Results travel back for the columns the call integrated only: columns
+  // 0..ncrms-1 as strided rows of every (ld, ...) array, or, under a
+  // col_map, whole arrays after staging the host values of the rad means and
+  // outputs, so slots outside the map keep their host contents.
+  const bool mapped = d->col_map != nullptr;
+  if (!mapped) CK(cudaMemsetAsync(c->d_out, 0, sizeof(double) * o, s));
+  if (mapped) {
+    for (int f = 0; f < 5; ++f)
+      if (rp[f]) CK(cudaMemcpyAsync(c->d_rad + (f + 1) * nr, rp[f], sizeof(double) * nr, cudaMemcpyHostToDevice, s));
+    for (int f = 0; f < CRM_NOUT; ++f)
+      if (out->field[f])
+        CK(cudaMemcpyAsync(dout.field[f], out->field[f], sizeof(double) * out_elems(g, f, ld), cudaMemcpyHostToDevice, s));
+  }
   int rc = enqueue(c, &dd, &din, &dst_state, &drad, &dout, c->d_status, s);
   if (rc != CRM_OK) return rc;
-  for (int f = 0; f < 7; ++f)
-    CK(cudaMemcpyAsync(sp[f], c->d_state + f * n4, sizeof(double) * n4, cudaMemcpyDeviceToHost, s));
-  double *rp[5] = {rad->temperature, rad->qv, rad->qc, rad->qi, rad->cld};
+  const int cols = mapped ? ld : ncrms;
+  auto back = [&](double *dst, const double *src, size_t elems) -> cudaError_t {
+    const size_t rows = elems / (size_t)ld;
+    if (cols == ld) return cudaMemcpyAsync(dst, src, sizeof(double) * elems, cudaMemcpyDeviceToHost, s);
+    return cudaMemcpy2DAsync(dst, sizeof(double) * ld, src, sizeof(double) * ld, sizeof(double) * cols, rows,
+                             cudaMemcpyDeviceToHost, s);
+  };
+  for (int f = 0; f < 7; ++f) CK(back(sp[f], c->d_state + f * n4, n4));
   for (int f = 0; f < 5; ++f)
-    if (rp[f]) CK(cudaMemcpyAsync(rp[f], c->d_rad + (f + 1) * nr, sizeof(double) * nr, cudaMemcpyDeviceToHost, s));
+    if (rp[f]) CK(back(rp[f], c->d_rad + (f + 1) * nr, nr));
   for (int f = 0; f < CRM_NOUT; ++f)
-    if (out->field[f])
-      CK(cudaMemcpyAsync(out->field[f], dout.field[f], sizeof(double) * out_elems(g, f, ld), cudaMemcpyDeviceToHost, s));
+    if (out->field[f]) CK(back(out->field[f], dout.field[f], out_elems(g, f, ld)));
   std::vector<int> stat(ncrms, 0);
   CK(cudaMemcpyAsync(stat.data(), c->d_status, sizeof(int) * ncrms, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
@@ -562,7 +645,7 @@ extern "C" int crm_run_device_noalloc(const crm_config *cfg, const crm_call_desc
   g.max_ncrms = 1;   // no handle: the column count is bounded by the scratch only
   int rc = validate(&g);
   if (rc != CRM_OK) return rc;
-  if (!d || d->ncrms < 1 || d->ld < d->ncrms || !(d->dt_gl > 0)) return CRM_ERR_ARG;
+  if (!d || d->ncrms < 1 || d->ld < d->ncrms || !(d->dt_gl > 0) || d->col_map) return CRM_ERR_ARG;
   const int ncrms = d->ncrms, nx = g.crm_nx;
   NoallocPlan q;
   rc = noalloc_plan(g, ncrms, q);
@@ -590,9 +673,8 @@ extern "C" int crm_run_device_noalloc(const crm_config *cfg, const crm_call_desc
   NoallocDevice dv;
   rc = noalloc_device(dv);
   if (rc != CRM_OK) return rc;
-  const int block = 256;
-  int per_sm = g.precision == CRM_FP64 ? crm::occupancy_crm_columns<double>(block, nx, g.crm_nz)
-                                       : crm::occupancy_crm_columns<float>(block, nx, g.crm_nz);
+  const int shape = default_shape(g.precision);
+  int per_sm = crm::occupancy_columns(g.precision, shape, nx, g.crm_nz);
   if (per_sm < 1) return CRM_ERR_UNSUPPORTED;
   int grid = dv.nsm * per_sm;
   if (grid > q.nslab) grid = q.nslab;
@@ -658,6 +740,7 @@ extern "C" int crm_run_device_noalloc(const crm_config *cfg, const crm_call_desc
   pp.zmid = in->zmid; pp.zint = in->zint; pp.pdel = in->pdel;
   pp.tau00 = in->tau00; pp.bflxls = in->bflxls; pp.wndls = in->wndls;
   pp.gcol = d->gcol;
+  pp.col_map = nullptr;
   pp.z0 = d_col;
   pp.rnd = d_col + ncrms;
   crm::KParams p;
@@ -690,11 +773,10 @@ extern "C" int crm_run_device_noalloc(const crm_config *cfg, const crm_call_desc
   for (int f = 0; f < CRM_NOUT; ++f) p.out[f] = out->field[f];
   p.slabs = d_slabs;
   p.phase_cycles = nullptr;
-  p.next_col = nullptr;
+  p.col_map = nullptr;
   p.col_status = col_status;
   crm::launch_crm_prep(pp, s);
-  if (g.precision == CRM_FP64) crm::launch_crm_columns<double>(p, grid, block, s);
-  else crm::launch_crm_columns<float>(p, grid, block, s);
+  crm::launch_columns(g.precision, shape, p, grid, s);
   CK(cudaGetLastError());
   return CRM_OK;
 }

@@ -89,38 +89,60 @@ struct ColShared {
   int red_i[64];
 };
 
-template <typename T>
-struct ColumnKernel {
+// The CRM's horizontal size: a compile-time constant for the sizes built
+// into the library (the reference fixes it at build time too, CRM_NX in
+// crmdims.F90), so strides and the (i, k) index arithmetic of every cell loop
+// fold to constants; NX = 0 reads it from the layout at run time.
+template <int NX> struct NxDim {
+  static constexpr int nx = NX;
+  __device__ explicit NxDim(int) {}
+};
+template <> struct NxDim<0> {
+  const int nx;
+  __device__ explicit NxDim(int n) : nx(n) {}
+};
+
+template <typename T, int NX>
+struct ColumnKernel : NxDim<NX> {
+  using NxDim<NX>::nx;
   const KParams &p;
   ColShared &S;
   T *base;
-  int nx, nzm, nz, plev, icrm;
+  int nzm, nz, plev;
+  int icrm;   // slot of the column in the (ld, ...) arrays
+  int cpos;   // position of the column in the call (status index)
 
   __device__ ColumnKernel(const KParams &p_, ColShared &s_, T *b, int col)
-      : p(p_), S(s_), base(b), nx(p_.L.nx), nzm(p_.L.nzm), nz(p_.L.nz), plev(p_.L.plev), icrm(col) {}
+      : NxDim<NX>(p_.L.nx), p(p_), S(s_), base(b), nzm(p_.L.nzm), nz(p_.L.nz), plev(p_.L.plev),
+        icrm(p_.col_map ? p_.col_map[col] : col), cpos(col) {}
 
   // ---------------------------------------------------------- accessors
-  __device__ __forceinline__ F2<T> fld(size_t off, XRange x, int z1 = 1) const { return F2<T>{base + off, x.x1, x.nxa, z1}; }
-  __device__ __forceinline__ F2<T> U() const { return fld(p.L.u, p.L.xu); }
-  __device__ __forceinline__ F2<T> V() const { return fld(p.L.v, p.L.xv); }
-  __device__ __forceinline__ F2<T> W() const { return fld(p.L.w, p.L.xw); }
-  __device__ __forceinline__ F2<T> TT() const { return fld(p.L.t, p.L.xs); }
-  __device__ __forceinline__ F2<T> QT() const { return fld(p.L.qt, p.L.xs); }
-  __device__ __forceinline__ F2<T> QP() const { return fld(p.L.qp, p.L.xs); }
-  __device__ __forceinline__ F2<T> TKE() const { return fld(p.L.tke, p.L.xi); }
-  __device__ __forceinline__ F2<T> TK() const { return fld(p.L.tk, p.L.xd); }
-  __device__ __forceinline__ F2<T> TKH() const { return fld(p.L.tkh, p.L.xd); }
-  __device__ __forceinline__ F2<T> PP() const { return fld(p.L.p, p.L.xp); }
-  __device__ __forceinline__ F2<T> TABS() const { return fld(p.L.tabs, p.L.xi); }
-  __device__ __forceinline__ F2<T> QV() const { return fld(p.L.qv, p.L.xi); }
-  __device__ __forceinline__ F2<T> QCL() const { return fld(p.L.qcl, p.L.xi); }
-  __device__ __forceinline__ F2<T> QCI() const { return fld(p.L.qci, p.L.xi); }
-  __device__ __forceinline__ F2<T> QPL() const { return fld(p.L.qpl, p.L.xi); }
-  __device__ __forceinline__ F2<T> QPI() const { return fld(p.L.qpi, p.L.xi); }
-  __device__ __forceinline__ F2<T> QN() const { return fld(p.L.qn, p.L.xi); }
-  __device__ __forceinline__ F2<T> DU(int l) const { return fld(p.L.du[l - 1], p.L.xdu); }
-  __device__ __forceinline__ F2<T> DV(int l) const { return fld(p.L.dv[l - 1], p.L.xi); }
-  __device__ __forceinline__ F2<T> DW(int l) const { return fld(p.L.dw[l - 1], p.L.xi); }
+  // x extents of the field classes (first index, row length = nx + extra):
+  // the halo widths of crm/grid.F90:31-46 with NADV = NADVS = 0, as laid
+  // out by make_layout (crm_layout.h)
+  __device__ __forceinline__ F2<T> fld(size_t off, int x1, int extra, int z1 = 1) const {
+    return F2<T>{base + off, x1, nx + extra, z1};
+  }
+  __device__ __forceinline__ F2<T> U() const { return fld(p.L.u, -1, 5); }
+  __device__ __forceinline__ F2<T> V() const { return fld(p.L.v, -1, 4); }
+  __device__ __forceinline__ F2<T> W() const { return fld(p.L.w, -1, 4); }
+  __device__ __forceinline__ F2<T> TT() const { return fld(p.L.t, -2, 6); }
+  __device__ __forceinline__ F2<T> QT() const { return fld(p.L.qt, -2, 6); }
+  __device__ __forceinline__ F2<T> QP() const { return fld(p.L.qp, -2, 6); }
+  __device__ __forceinline__ F2<T> TKE() const { return fld(p.L.tke, 1, 0); }
+  __device__ __forceinline__ F2<T> TK() const { return fld(p.L.tk, 0, 2); }
+  __device__ __forceinline__ F2<T> TKH() const { return fld(p.L.tkh, 0, 2); }
+  __device__ __forceinline__ F2<T> PP() const { return fld(p.L.p, 0, 1); }
+  __device__ __forceinline__ F2<T> TABS() const { return fld(p.L.tabs, 1, 0); }
+  __device__ __forceinline__ F2<T> QV() const { return fld(p.L.qv, 1, 0); }
+  __device__ __forceinline__ F2<T> QCL() const { return fld(p.L.qcl, 1, 0); }
+  __device__ __forceinline__ F2<T> QCI() const { return fld(p.L.qci, 1, 0); }
+  __device__ __forceinline__ F2<T> QPL() const { return fld(p.L.qpl, 1, 0); }
+  __device__ __forceinline__ F2<T> QPI() const { return fld(p.L.qpi, 1, 0); }
+  __device__ __forceinline__ F2<T> QN() const { return fld(p.L.qn, 1, 0); }
+  __device__ __forceinline__ F2<T> DU(int l) const { return fld(p.L.du[l - 1], 1, 1); }
+  __device__ __forceinline__ F2<T> DV(int l) const { return fld(p.L.dv[l - 1], 1, 0); }
+  __device__ __forceinline__ F2<T> DW(int l) const { return fld(p.L.dw[l - 1], 1, 0); }
   // scratch planes (x from -2, k from 0)
   __device__ __forceinline__ F2<T> SCR(size_t off) const { return F2<T>{base + off, -2, nx + 6, 0}; }
   __device__ __forceinline__ T *PR(int id) const { return base + p.L.prof + (size_t)id * (nz + 2); }
@@ -168,6 +190,27 @@ struct ColumnKernel {
       }
     }
   }
+  // Horizontal sums that only feed statistics and diagnostics (no
+  // conservation fixer): the FP64 form is level_sums itself; the FP32-mixed
+  // form reduces the warp entirely in FP32 (pairwise, error ~log2(nx) ulp),
+  // sparing the slow FP64 pipe.
+  template <typename Term, typename Init, typename Out>
+  __device__ void level_sums_lo(int nq, int k0, int k1, Term term, Init init, Out out) {
+    if constexpr (sizeof(T) == 8) {
+      level_sums(nq, k0, k1, term, init, out);
+    } else {
+      const int nk = k1 - k0 + 1, npairs = nq * nk;
+      const int lane = TID & 31, warp = TID >> 5, nw = NT >> 5;
+      for (int e = warp; e < npairs; e += nw) {
+        int q = e / nk, k = k0 + e % nk;
+        T part = (T)0;
+        for (int i = 1 + lane; i <= nx; i += 32) part = part + term(q, i, k);
+        for (int o = 1; o < 32; o <<= 1) part = part + __shfl_xor_sync(0xffffffffu, part, o);
+        if (lane == 0) out(q, k, (double)((T)init(q, k) + part));
+      }
+    }
+  }
+
   // Horizontal maxima (order-independent, hence exact in both forms): one
   // warp per (q, k) with a shuffle tree.
   template <typename Term, typename Out>
@@ -632,7 +675,7 @@ struct ColumnKernel {
         tau[k] = (T)1. / tk;
       }
     }
-    level_sums(3, 1, nzm,
+    level_sums_lo(3, 1, nzm,
                [&](int q, int i, int k) -> T { return (q == 0 ? u(i, k) : q == 1 ? v(i, k) : t(i, k)) / nxy; },
                [&](int, int) { return 0.; },
                [&](int q, int k, double sv) { (q == 0 ? u0l : q == 1 ? v0l : t0l)[k] = (T)sv; });
@@ -887,7 +930,7 @@ struct ColumnKernel {
     SYNC;
     T *uwle = PR(P_UWLE), *vwle = PR(P_VWLE);
     if (TID == 0) { uwle[1] = (T)0.; vwle[1] = (T)0.; uwle[nz] = (T)0.; vwle[nz] = (T)0.; }
-    level_sums(2, 2, nzm, [&](int q, int i, int k) -> T { return q == 0 ? fuz(i, k) : fvz(i, k); },
+    level_sums_lo(2, 2, nzm, [&](int q, int i, int k) -> T { return q == 0 ? fuz(i, k) : fvz(i, k); },
                [&](int, int) { return 0.; },
                [&](int q, int k, double sv) { (q == 0 ? uwle : vwle)[k] = (T)sv; });
     for (int e = TID; e < nx * nzm; e += NT) {
@@ -970,7 +1013,7 @@ struct ColumnKernel {
     }
     SYNC;
     T *uwsb = PR(P_UWSB), *vwsb = PR(P_VWSB);
-    level_sums(2, 1, nzm, [&](int q, int i, int k) -> T { return q == 0 ? fu(i, k) : fv(i, k); },
+    level_sums_lo(2, 1, nzm, [&](int q, int i, int k) -> T { return q == 0 ? fu(i, k) : fv(i, k); },
                [&](int, int) { return 0.; },
                [&](int q, int k, double sv) { (q == 0 ? uwsb : vwsb)[k] = (T)sv; });
     for (int e = TID; e < nx * nzm; e += NT) {
@@ -1300,7 +1343,7 @@ struct ColumnKernel {
     SYNC;
     // first-pass (upwind) vertical flux sum, then the upwind update
     if (flux)
-      level_sums(1, 1, nzm, [&](int, int i, int k) -> T { return www(i, k); },
+      level_sums_lo(1, 1, nzm, [&](int, int i, int k) -> T { return www(i, k); },
                  [&](int, int) { return 0.; }, [&](int, int k, double sv) { wfl1(0, k) = (T)sv; });
     for (int e = TID; e < (nx + 4) * nzm; e += NT) {
       int i = -1 + e % (nx + 4), k = 1 + e / (nx + 4);   // -1 .. nx+2
@@ -1363,7 +1406,7 @@ struct ColumnKernel {
     }
     SYNC;
     if (flux)
-      level_sums(1, 1, nzm, [&](int, int i, int k) -> T { return www(i, k); },
+      level_sums_lo(1, 1, nzm, [&](int, int i, int k) -> T { return www(i, k); },
                  [&](int, int k) { return (double)wfl1(0, k); },
                  [&](int, int k, double sv) { flux[k] = (T)sv; });
     for (int e = TID; e < nx * nzm; e += NT) {
@@ -1373,7 +1416,7 @@ struct ColumnKernel {
     }
     SYNC;
     if (fadv) {
-      level_sums(1, 1, nzm, [&](int, int i, int k) -> T { return f(i, k) - f0(i, k); },
+      level_sums_lo(1, 1, nzm, [&](int, int i, int k) -> T { return f(i, k) - f0(i, k); },
                  [&](int, int) { return 0.; }, [&](int, int k, double sv) { fadv[k] = (T)sv; });
       SYNC;
     }
@@ -1419,16 +1462,18 @@ struct ColumnKernel {
       iwmax[k] = (T)1. / wmax;
     }
     SYNC;
-    double cfl = 0.;
+    // the maximum is taken in T and widened once (widening is exact and
+    // monotone, so the result equals a maximum of widened values)
+    T cflt = (T)0.;
     for (int e = TID; e < nx * nzm; e += NT) {
       int i = 1 + e % nx, k = 1 + e / nx;
       omega(i, k) = mx2((T)0., mn2((T)1., (tabs(i, k) - (T)C_TPRMIN) * (T)p.a_pr));
       T tmp = term_vel(tabs(i, k), rho[k], qp(i, k));
       T wv = rhofac[k] * tmp;
-      cfl = mx2(cfl, (double)(wv * iwmax[k]));
+      cflt = mx2(cflt, wv * iwmax[k]);
       wp(i, k) = -wv * rhow[k] * dtn / dz;
     }
-    cfl = block_max(cfl);
+    double cfl = block_max((double)cflt);
     if (TID == 0) {
       S.prec_cfl = cfl;
       S.nprec = (cfl > R4(0.9)) ? (int)ceil(cfl / R4(0.9)) : 1;
@@ -1492,7 +1537,7 @@ struct ColumnKernel {
       }
       SYNC;
       // per-level budget sums in the reference's order, then the update
-      level_sums(2, 1, nzm,
+      level_sums_lo(2, 1, nzm,
                  [&](int q, int i, int k) -> T {
                    if (q == 0) return -(fz(i, k + 1) - fz(i, k)) * irhoadz[k] * (T)1.;
                    return -(fz(i, k) * (T)1.);
@@ -1566,7 +1611,7 @@ struct ColumnKernel {
     }
     SYNC;
     if (flux)
-      level_sums(1, 1, nzm, [&](int, int i, int k) -> T { return flx(i, k == 1 ? 0 : k - 1); },
+      level_sums_lo(1, 1, nzm, [&](int, int i, int k) -> T { return flx(i, k == 1 ? 0 : k - 1); },
                  [&](int, int) { return 0.; }, [&](int, int k, double sv) { flux[k] = (T)sv; });
     for (int e = TID; e < nx * nzm; e += NT) {
       int i = 1 + e % nx, k = 1 + e / nx;
@@ -1577,7 +1622,7 @@ struct ColumnKernel {
     }
     SYNC;
     if (fdiff) {
-      level_sums(1, 1, nzm, [&](int, int i, int k) -> T { return f(i, k) - f0(i, k); },
+      level_sums_lo(1, 1, nzm, [&](int, int i, int k) -> T { return f(i, k) - f0(i, k); },
                  [&](int, int) { return 0.; }, [&](int, int k, double sv) { fdiff[k] = (T)sv; });
       SYNC;
     }
@@ -1594,6 +1639,33 @@ struct ColumnKernel {
     const double fac2 = C_FAC_FUS * ap;
     for (int e = TID; e < nx * nzm; e += NT) {
       int i = 1 + e % nx, k = 1 + e / nx;
+      if constexpr (sizeof(T) == 4) {
+        // FP32-mixed form: a cell that is clearly unsaturated (total water
+        // 0.1 % or more below saturation, far beyond FP32 rounding of qsat)
+        // takes the no-condensate branch in FP32; the FP64 path, with the
+        // Newton iteration, runs only near or above saturation.
+        const float qf = mx2(0.f, (float)qt(i, k)), qpf = (float)qp(i, k);
+        const float tabf = (float)(t(i, k) - gamaz[k]), prf = (float)pres[k];
+        float t1 = (tabf + (float)fac1 * qpf) / (1.f + (float)fac2 * qpf);
+        float qsf;
+        if (t1 >= (float)C_TBGMAX) {
+          t1 = tabf + (float)C_FAC_COND * qpf;
+          qsf = qsatw(t1, prf);
+        } else if (t1 <= (float)C_TBGMIN) {
+          t1 = tabf + (float)C_FAC_SUB * qpf;
+          qsf = qsati(t1, prf);
+        } else {
+          float om = (float)an * t1 - (float)bn;
+          qsf = om * qsatw(t1, prf) + (1.f - om) * qsati(t1, prf);
+        }
+        if (qf < 0.999f * qsf) {
+          qt(i, k) = (T)qf;
+          qn(i, k) = (T)0.;
+          tabs(i, k) = (T)t1;
+          qp(i, k) = mx2((T)0., qp(i, k));
+          continue;
+        }
+      }
       double pr = (double)pres[k];
       double q = mx2(0., (double)qt(i, k));
       double qpv = (double)qp(i, k);
@@ -1745,7 +1817,7 @@ struct ColumnKernel {
     }
     SYNC;
     T *qpsrc = PR(P_QPSRC), *qpevp = PR(P_QPEVP);
-    level_sums(2, 1, nzm, [&](int q, int i, int k) -> T { return q == 0 ? csrc(i, k) : cevp(i, k); },
+    level_sums_lo(2, 1, nzm, [&](int q, int i, int k) -> T { return q == 0 ? csrc(i, k) : cevp(i, k); },
                [&](int, int) { return 0.; },
                [&](int q, int k, double sv) { (q == 0 ? qpsrc : qpevp)[k] = (T)sv; });
     SYNC;
@@ -1763,7 +1835,7 @@ struct ColumnKernel {
     const double coef = 1. / (double)nx;
     // domain means; q0 and qn0 are kept in FP64 in TMP0/TMP1 for qv0
     double *q0d = reinterpret_cast<double *>(base + p.L.s_a);
-    level_sums(7, 1, nzm,
+    level_sums_lo(7, 1, nzm,
                [&](int q, int i, int k) -> T {
                  switch (q) {
                    case 0: return u(i, k);
@@ -1818,14 +1890,16 @@ struct ColumnKernel {
     for (int e = TID; e < nx * nz; e += NT) {
       int i = 1 + e % nx, k = 1 + e / nx;
       T wv = w(i, k), cu = (T)0., cd = (T)0.;
+      // qsat > 0, so a cell without condensate never passes the threshold:
+      // qsatw is evaluated only where condensate exists (same result)
       if (wv > (T)0.) {
         int kx = max(1, k - 1);
-        T qs = qsatw(tabs(i, kx), pres[kx]);
-        if (qcl(i, kx) + qci(i, kx) > mn2((T)R4(1.e-5), (T)R4(0.01) * qs)) cu = rhow[k] * wv;
+        T cond = qcl(i, kx) + qci(i, kx);
+        if (cond > (T)0. && cond > mn2((T)R4(1.e-5), (T)R4(0.01) * qsatw(tabs(i, kx), pres[kx]))) cu = rhow[k] * wv;
       } else if (wv < (T)0.) {
         int kx = min(k + 1, nzm);
-        T qs = qsatw(tabs(i, kx), pres[kx]);
-        if (qcl(i, kx) + qci(i, kx) > mn2((T)R4(1.e-5), (T)R4(0.01) * qs)) cd = rhow[k] * wv;
+        T cond = qcl(i, kx) + qci(i, kx);
+        if (cond > (T)0. && cond > mn2((T)R4(1.e-5), (T)R4(0.01) * qsatw(tabs(i, kx), pres[kx]))) cd = rhow[k] * wv;
         else if (qpl(i, kx) + qpi(i, kx) > (T)R4(1.0e-4)) cd = rhow[k] * wv;
       }
       cmu(i, k) = cu;
@@ -1833,12 +1907,12 @@ struct ColumnKernel {
     }
     SYNC;
     T *mui = OP(O_MUI), *mdi = OP(O_MDI);
-    level_sums(2, 1, nz, [&](int q, int i, int k) -> T { return q == 0 ? cmu(i, k) : cmd(i, k); },
+    level_sums_lo(2, 1, nz, [&](int q, int i, int k) -> T { return q == 0 ? cmu(i, k) : cmd(i, k); },
                [&](int q, int k) { return (double)(q == 0 ? mui : mdi)[plev + 2 - k]; },
                [&](int q, int k, double sv) { (q == 0 ? mui : mdi)[plev + 2 - k] = (T)sv; });
     // cloud fraction, cloud top counts, cloudy mass fluxes, water paths
     T *acc[8] = {OP(O_CLD), OP(O_CLDTOP), OP(O_MCUP), OP(O_MCDN), OP(O_MCUUP), OP(O_MCUDN), OP(O_GLIQWP), OP(O_GICEWP)};
-    level_sums(8, 1, nzm,
+    level_sums_lo(8, 1, nzm,
                [&](int q, int i, int k) -> T {
                  if (q == 1) return ((int)cs[4 * nx + (i - 1)] == k) ? (T)1. : (T)0.;
                  if (q == 6) return qcl(i, k);
@@ -1860,14 +1934,14 @@ struct ColumnKernel {
     for (int e = TID; e < nxr * nzm; e += NT) {
       int ir = 1 + e % nxr, k = 1 + e / nxr;
       size_t o = (size_t)(k - 1) * nxr + (ir - 1);
-      double st = (double)rad[o], sq = (double)rad[(size_t)nxr * nzm + o], sc = (double)rad[(size_t)2 * nxr * nzm + o];
-      double si = (double)rad[(size_t)3 * nxr * nzm + o], sl = (double)rad[(size_t)4 * nxr * nzm + o];
+      T st = rad[o], sq = rad[(size_t)nxr * nzm + o], sc = rad[(size_t)2 * nxr * nzm + o];
+      T si = rad[(size_t)3 * nxr * nzm + o], sl = rad[(size_t)4 * nxr * nzm + o];
       for (int i = (ir - 1) * gx + 1; i <= ir * gx; ++i) {
-        st = st + (double)tabs(i, k);
-        sq = sq + (double)mx2((T)0., qv(i, k));
-        sc = sc + (double)qcl(i, k);
-        si = si + (double)qci(i, k);
-        if (qcl(i, k) + qci(i, k) > (T)0) sl = sl + 1.0;
+        st = st + tabs(i, k);
+        sq = sq + mx2((T)0., qv(i, k));
+        sc = sc + qcl(i, k);
+        si = si + qci(i, k);
+        if (qcl(i, k) + qci(i, k) > (T)0) sl = sl + (T)1.0;
       }
       rad[o] = (T)st; rad[(size_t)nxr * nzm + o] = (T)sq; rad[(size_t)2 * nxr * nzm + o] = (T)sc;
       rad[(size_t)3 * nxr * nzm + o] = (T)si; rad[(size_t)4 * nxr * nzm + o] = (T)sl;
@@ -2098,13 +2172,17 @@ struct ColumnKernel {
       O1(CRM_OUT_JT_CRM) = (jt <= plev) ? mn2((double)plev, (double)jt) : (double)plev;
       O1(CRM_OUT_MX_CRM) = mx2(1.0, (double)mx);
       O1(CRM_OUT_TIMING_FACTOR) = (double)p.nstop / (double)p.nstop;
-      p.col_status[icrm] = S.status;
+      p.col_status[cpos] = S.status;
     }
     SYNC;
   }
 
   // ---------------------------------------------------------- one column
   __device__ void run(T *fsh, T *wsh) {
+    if (icrm < 0 || icrm >= p.ld) {            // bad slot in col_map: no access
+      if (TID == 0) p.col_status[cpos] = CRM_ERR_ARG;
+      return;
+    }
     if (TID == 0) S.t_last = clock64();
     init_column();
     if (TID == 0) { S.jt_min = 1 << 30; S.mx_max = 0; }
@@ -2194,33 +2272,36 @@ __host__ __device__ inline size_t crm_smem_bytes(int nx, int nzm, int block) {
   return sizeof(T) * ((size_t)(nx + 2) * nzm + (size_t)(block / 32) * (nx + 4));
 }
 
-template <typename T>
-__global__ void __launch_bounds__(256) crm_columns_kernel(const __grid_constant__ KParams p) {
+template <typename T, int NX, int NTH, int MINB>
+__global__ void __launch_bounds__(NTH, MINB) crm_columns_kernel(const __grid_constant__ KParams p) {
   __shared__ ColShared S;
   extern __shared__ __align__(16) unsigned char crm_dsm[];
   T *fsh = reinterpret_cast<T *>(crm_dsm);
   T *wsh = fsh + (size_t)(p.L.nx + 2) * p.L.nzm;
   T *base = reinterpret_cast<T *>(p.slabs) + (size_t)blockIdx.x * p.L.slab;
   for (int col = blockIdx.x; col < p.ncrms; col += gridDim.x) {
-    ColumnKernel<T> K(p, S, base, col);
+    ColumnKernel<T, NX> K(p, S, base, col);
     K.run(fsh, wsh);
     __syncthreads();
   }
 }
 
-template <typename T>
-void launch_crm_columns(const KParams &p, int grid, int block, cudaStream_t s) {
-  size_t smem = crm_smem_bytes<T>(p.L.nx, p.L.nzm, block);
-  cudaFuncSetAttribute(crm_columns_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  crm_columns_kernel<T><<<grid, block, smem, s>>>(p);
+template <typename T, int NX, int SHAPE>
+void launch_crm_columns(const KParams &p, int grid, cudaStream_t s) {
+  constexpr int nth = kShapes[SHAPE].threads, minb = kShapes[SHAPE].min_ctas;
+  size_t smem = crm_smem_bytes<T>(p.L.nx, p.L.nzm, nth);
+  cudaFuncSetAttribute(crm_columns_kernel<T, NX, nth, minb>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  crm_columns_kernel<T, NX, nth, minb><<<grid, nth, smem, s>>>(p);
 }
 
-template <typename T>
-int occupancy_crm_columns(int block, int nx, int nzm) {
+template <typename T, int NX, int SHAPE>
+int occupancy_crm_columns(int nx, int nzm) {
+  constexpr int nth = kShapes[SHAPE].threads, minb = kShapes[SHAPE].min_ctas;
   int n = 0;
-  size_t smem = crm_smem_bytes<T>(nx, nzm, block);
-  cudaFuncSetAttribute(crm_columns_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, crm_columns_kernel<T>, block, smem) != cudaSuccess) return 0;
+  size_t smem = crm_smem_bytes<T>(nx, nzm, nth);
+  cudaFuncSetAttribute(crm_columns_kernel<T, NX, nth, minb>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, crm_columns_kernel<T, NX, nth, minb>, nth, smem) != cudaSuccess)
+    return 0;
   return n;
 }
 

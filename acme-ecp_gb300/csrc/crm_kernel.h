@@ -28,7 +28,7 @@ struct KParams {
   double *out[CRM_NOUT];
   void *slabs;              // gridDim.x slabs of L.slab elements of T
   int *col_status;          // (ncrms)
-  int *next_col;            // dynamic column counter (zeroed before launch)
+  const int *col_map;       // optional (ncrms) slots: column c uses slot col_map[c]
   unsigned long long *phase_cycles;  // (gridDim.x, 64) when built with CRM_PHASE_TIMERS
 };
 
@@ -40,9 +40,31 @@ enum PhaseId {
   PH_DIFF_Q, PH_PINIT, PH_CLOUD, PH_PPROC, PH_MDIAG, PH_DIAG, PH_STATS, PH_FINAL, PH_COUNT
 };
 
-template <typename T>
-void launch_crm_columns(const KParams &p, int grid, int block, cudaStream_t s);
-template <typename T>
-int occupancy_crm_columns(int block, int nx, int nzm);
+// Launch shapes of the column kernel: threads per CTA (one CTA integrates one
+// CRM column at a time) and the CTAs per SM the register budget is sized for
+// (__launch_bounds__).  More, smaller CTAs per SM hide more latency at the
+// cost of register spills; the best shape is chosen per precision by
+// measurement (crm_host.cu).
+struct KShape {
+  int threads, min_ctas;
+};
+constexpr int kNumShapes = 3;
+constexpr KShape kShapes[kNumShapes] = {{256, 2}, {256, 3}, {256, 4}};
+
+// Horizontal sizes with a kernel specialised at compile time (the reference
+// fixes CRM_NX at build time too); any other power of two runs the generic
+// kernel (NX = 0), which reads nx from the layout.
+constexpr int kNumNx = 4;
+constexpr int kNxBuilt[kNumNx] = {32, 64, 128, 0};
+
+// One instantiation per (T, NX, shape) lives in its own object (crm_columns.cu).
+template <typename T, int NX, int SHAPE>
+void launch_crm_columns(const KParams &p, int grid, cudaStream_t s);
+template <typename T, int NX, int SHAPE>
+int occupancy_crm_columns(int nx, int nzm);
+
+// Dispatch on (precision, nx, shape) at run time.
+void launch_columns(int precision, int shape, const KParams &p, int grid, cudaStream_t s);
+int occupancy_columns(int precision, int shape, int nx, int nzm);
 
 }  // namespace crm

@@ -17,13 +17,16 @@ struct PrepParams {
   int ncrms, ld, plev, nx, igstep;
   const double *zmid, *zint, *pdel, *tau00, *bflxls, *wndls;
   const int *gcol;
-  double *z0;     // (ncrms)
-  double *rnd;    // (ncrms, 5, nx): 1 - 2 r
+  const int *col_map;   // optional (ncrms) slots
+  double *z0;     // (ld), by slot
+  double *rnd;    // (ld, 5, nx) by slot: 1 - 2 r
 };
 
 __global__ void crm_prep_kernel(const __grid_constant__ PrepParams p) {
-  int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= p.ncrms) return;
+  int pos = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pos >= p.ncrms) return;
+  const int c = p.col_map ? p.col_map[pos] : pos;   // slot
+  if (c < 0 || c >= p.ld) return;                   // reported by the column kernel
   auto IN = [&](const double *a, int l) { return a[(size_t)c + (size_t)p.ld * (l - 1)]; };
   const int plev = p.plev;
   // grid values of the lowest level (crm_module.F90:341-370)
@@ -57,7 +60,7 @@ __global__ void crm_prep_kernel(const __grid_constant__ PrepParams p) {
   if (p.igstep > 1) return;
   // RNG_MT_set_seed / RNG_MT_gen_rand
   int32_t mt[624];
-  mt[0] = (int32_t)(p.gcol[c] * 1000);
+  mt[0] = (int32_t)(p.gcol[pos] * 1000);
   for (int i = 1; i < 624; ++i) mt[i] = (int32_t)((uint32_t)69069 * (uint32_t)mt[i - 1]);
   int mti = 624;
   const int32_t UMASK = -1147483648, LMASK = 2147483647, MATA = -1727483681;

@@ -123,7 +123,7 @@ def run_reference(args):
     ws, rank, _ = dist_info()
     if rank != 0:
         return
-    ncols = int(os.environ.get('CRM_BENCH_CPU_COLS', '16'))
+    ncols = int(os.environ.get('CRM_BENCH_CPU_COLS', '128'))
     for _ in range(args.warmup):
         cpu_baseline(ncols)
     vals = []
@@ -152,7 +152,7 @@ def main():
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--fp64-steps', type=int, default=2)
-    ap.add_argument('--cpu-cols', type=int, default=16)
+    ap.add_argument('--cpu-cols', type=int, default=512)
     args = ap.parse_args()
     if args.impl == 'reference':
         return run_reference(args)
@@ -163,6 +163,7 @@ def main():
     from crm_gb300 import crm_types as T
     from crm_gb300.device import DeviceCrmArrays
     from crm_gb300.lib import CrmContext
+    from crm_gb300.shard import column_shard
 
     ws, rank, local = dist_info()
     if ws > 1:
@@ -183,7 +184,11 @@ def main():
         torch.cuda.synchronize()
 
     # ---- synthetic workload (each rank its own columns)
-    cfg32, cin, st, rad, desc = S.workload1(ncrms=NCRMS, seed=1000 * rank, precision=T.CRM_FP32_MIXED)
+    # weak scaling: NCRMS columns per rank, rank r owning global columns
+    # [r * NCRMS, (r + 1) * NCRMS) (contiguous blocks, no data exchange)
+    first, count = column_shard(ws * NCRMS, rank, ws)
+    cfg32, cin, st, rad, desc = S.workload1(ncrms=count, seed=first, gcol0=first + 1,
+                                            precision=T.CRM_FP32_MIXED)
     cfg32.max_ncrms = NCRMS
     nstop = int(desc.dt_gl / cfg32.crm_dt)
     colsteps = NCRMS * nstop

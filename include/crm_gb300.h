@@ -139,6 +139,13 @@ typedef struct crm_call_desc {
   double dt_gl;                 /* GCM timestep [s]                      */
   int igstep;                   /* GCM step number (get_nstep())        */
   const int *gcol;              /* (ncrms) global column ids             */
+  /* Optional (ncrms) column slots, 0-based and distinct, < ld: column c of
+   * the call reads and writes slot col_map[c] of every (ld, ...) array, so a
+   * caller can integrate any subset of a resident batch; col_status and gcol
+   * stay indexed by c.  NULL: slot c.  A device pointer for crm_run_device,
+   * host for crm_run; not accepted by crm_run_device_noalloc.  No
+   * counterpart in the reference (ncrms always covers 1..ncrms). */
+  const int *col_map;
 } crm_call_desc;
 
 typedef struct crm_ctx crm_ctx;

@@ -2160,12 +2160,15 @@ static bool clamp_test(const Grid &g, const crm_state_c *st, int icrm, int ld) {
   return U(1, 1) == U(2, 1) && U(3, 2) == U(4, 2);
 }
 
-static void run_column_full(Model &M, Column &c, int icrm, crm_state_c *st, crm_rad_c *rad, crm_output_c *out) {
+// icrm: the column's slot in the (ld, ...) arrays; pos: its position in the
+// call (gcol and status index); the two differ only under a col_map.
+static void run_column_full(Model &M, Column &c, int icrm, int pos, crm_state_c *st, crm_rad_c *rad,
+                            crm_output_c *out) {
   Grid &g = M.g;
   M.alloc_column(c);
   zero_outputs(g, icrm, M.ld, out);
   M.init_column(c, icrm, st, rad, clamp_test(g, st, icrm, M.ld));
-  if (M.desc->igstep <= 1) M.setperturb(c, M.desc->gcol[icrm] * 1000);
+  if (M.desc->igstep <= 1) M.setperturb(c, M.desc->gcol[pos] * 1000);
   Model::FallScratch s;
   for (int nstep = 1; nstep <= g.nstop && c.status == CRM_OK; ++nstep) {
     M.kurant(c);
@@ -2208,14 +2211,18 @@ int oracle_crm_run(const crm_config *cfg, const crm_call_desc *desc, const crm_i
 #else
   (void)nthreads;
 #endif
+  auto slot_of = [&](int pos) { return desc->col_map ? desc->col_map[pos] : pos; };
+  for (int pos = 0; pos < ncrms; ++pos)
+    if (slot_of(pos) < 0 || slot_of(pos) >= desc->ld) return CRM_ERR_ARG;
   if (cfg->batch_mode == CRM_PER_COLUMN) {
 #pragma omp parallel for schedule(dynamic, 1)
-    for (int icrm = 0; icrm < ncrms; ++icrm) {
-      run_column_full(M, M.cols[icrm], icrm, st, rad, out);
-      M.col_status_saved[icrm] = M.cols[icrm].status;
-      M.cols[icrm] = Column();        // release memory early
+    for (int pos = 0; pos < ncrms; ++pos) {
+      run_column_full(M, M.cols[pos], slot_of(pos), pos, st, rad, out);
+      M.col_status_saved[pos] = M.cols[pos].status;
+      M.cols[pos] = Column();        // release memory early
     }
   } else {
+    if (desc->col_map) return CRM_ERR_UNSUPPORTED;
     Grid &g = M.g;
     bool clamp = clamp_test(g, st, 0, M.ld);
     std::vector<Model::FallScratch> scr(ncrms);

@@ -91,6 +91,14 @@ def test_fp64_bitexact_workload1_moist(gpu_lib):
     assert mismatches(*run_both(cfg, cin, st, rad, desc)) == []
 
 
+@pytest.mark.parametrize('nx', [16, 128])
+def test_fp64_bitexact_other_nx(gpu_lib, nx):
+    """nx = 128 (a compile-time size) and nx = 16 (the generic kernel)."""
+    cfg, cin, st, rad, desc = S.workload1(ncrms=2, nx=nx, moist=True)
+    desc.dt_gl = 300.0
+    assert mismatches(*run_both(cfg, cin, st, rad, desc)) == []
+
+
 def test_fp64_bitexact_three_gcm_steps(gpu_lib):
     """State carried across three calls (igstep 1, 2, 3), as in a GCM run."""
     cfg, cin, st, rad, desc = S.workload0(ncrms=3, moist=True)
@@ -158,3 +166,16 @@ def test_device_path_matches_host_path(gpu_lib):
     for n, _ in T.OUTPUT_FIELDS:
         assert np.array_equal(dev.out_numpy(n), getattr(out_h, n)), n
     assert int(dev.status.sum().item()) == 0
+
+
+def test_col_map_matches_oracle(gpu_lib):
+    """A call over slots (3, 0, 4) of a 5-column batch (col_map), bit for bit
+    against the oracle given the same map."""
+    import ctypes as C
+    cfg, cin, st, rad, desc = S.workload0(ncrms=5, moist=True)
+    slots = np.array([3, 0, 4], dtype=np.int32)
+    d = T.call_desc(3, 5, 400.0, desc.igstep, np.asarray(desc._keep)[slots])
+    d.col_map = slots.ctypes.data_as(C.POINTER(C.c_int))
+    a, b = run_both(cfg, cin, st, rad, d)
+    assert mismatches(a, b) == []
+    assert np.array_equal(b[0].temperature[[1, 2]], st.temperature[[1, 2]])

@@ -1,0 +1,81 @@
+"""The serving loop on the GPU: a chunk's results are the same alone and in
+a mix of concurrent chunks of other sizes (continuous batching over resident
+slots), and they equal a direct crm_run of the same columns."""
+import numpy as np
+import pytest
+
+from crm_gb300 import crm_types as T
+from crm_gb300 import synthetic as S
+
+pytestmark = pytest.mark.gpu
+
+DT_GL = 300.0
+
+
+def _configs():
+    return [T.CrmConfig(crm_nx=nx, crm_ny=1, crm_nz=nz, plev=72, crm_dx=1000.0, crm_dt=10.0,
+                        precision=T.CRM_FP32_MIXED) for nx, nz in ((32, 28), (64, 58))]
+
+
+def _chunk(cfg, ncol, gcol0, seed):
+    from crm_gb300.serve_bench import make_chunk
+    return make_chunk(cfg, ncol, gcol0, seed)
+
+
+def _drive(server, cfg, chunk, steps):
+    from crm_gb300.serving import apply_tendencies
+    cin, st, rad, gcol = chunk
+    cin = cin.copy()
+    ch = server.open_chunk(cfg, cin, st, rad, gcol)
+    res = []
+    for _ in range(steps):
+        vals, status = server.step(ch, cin, DT_GL).result(timeout=120)
+        assert not status.any()
+        res.append(vals)
+        apply_tendencies(cin, vals, DT_GL)
+    server.close_chunk(ch)
+    return res
+
+
+def test_chunk_alone_equals_chunk_in_mix(gpu_lib):
+    import threading
+    from crm_gb300.serving import CrmServer
+    cfgs = _configs()
+    a = _chunk(cfgs[1], 5, 101, seed=7)
+    server = CrmServer(cfgs, capacity=256)
+    alone = _drive(server, cfgs[1], a, 3)
+    # the same chunk again, now with four others of both sizes in flight
+    others = [(cfgs[i % 2], _chunk(cfgs[i % 2], 3 + 7 * i, 1000 * (i + 1), seed=i)) for i in range(4)]
+    out = {}
+    ts = [threading.Thread(target=lambda c=c, ch=ch, i=i: out.__setitem__(i, _drive(server, c, ch, 3)))
+          for i, (c, ch) in enumerate(others)]
+    for t in ts:
+        t.start()
+    mixed = _drive(server, cfgs[1], a, 3)
+    for t in ts:
+        t.join()
+    server.close()
+    assert len(out) == 4
+    assert server.launches >= 3
+    for s in range(3):
+        for n, v in alone[s].items():
+            assert np.array_equal(v, mixed[s][n]), (s, n)
+
+
+def test_serving_step_equals_crm_run(gpu_lib):
+    """First step of a chunk through the server == crm_run of the same columns."""
+    from crm_gb300.lib import CrmContext
+    from crm_gb300.serving import CrmServer
+    cfg = _configs()[0]
+    cin, st, rad, gcol = _chunk(cfg, 6, 11, seed=3)
+    server = CrmServer([cfg], capacity=64)
+    vals = _drive(server, cfg, (cin, st, rad, gcol), 1)[0]
+    server.close()
+    c2 = T.CrmConfig(**{**cfg.__dict__, 'max_ncrms': 6})
+    ctx = CrmContext(c2)
+    out = T.CrmOutput(6, cfg.crm_nx, 1, cfg.crm_nz, cfg.plev)
+    desc = T.call_desc(6, 6, DT_GL, 1, gcol)
+    status = ctx.run(desc, cin, st.copy(), rad.copy(), out)
+    assert not status.any()
+    for n, v in vals.items():
+        assert np.array_equal(v, getattr(out, n)), n

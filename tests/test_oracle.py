@@ -157,3 +157,24 @@ def test_cfl_violation_flags_only_that_column():
               T.call_desc(2, 2, 100.0, desc.igstep, np.asarray(desc._keep)[[0, 2]]))
     for n, v in ok[2].arrays().items():
         assert np.array_equal(v, getattr(st1, n)[[0, 2]]), n
+
+
+def test_col_map_selects_slots():
+    """A call over slots (3, 0) of a 5-column batch equals a call over a
+    2-column batch holding those columns; other slots are untouched."""
+    import ctypes as C
+    cfg, cin, st, rad, desc = S.workload0(ncrms=5, moist=True)
+    gcol = np.asarray(desc._keep)
+    slots = np.array([3, 0], dtype=np.int32)
+    d = T.call_desc(2, 5, 400.0, desc.igstep, gcol[slots])
+    d.col_map = slots.ctypes.data_as(C.POINTER(C.c_int))
+    a = _run(cfg, cin, st, rad, d)
+    assert a[0] == 0
+    b = _run(cfg, cin.take(slots), st.take(slots), rad.take(slots),
+             T.call_desc(2, 2, 400.0, desc.igstep, gcol[slots]))
+    for n, v in b[2].arrays().items():
+        assert np.array_equal(getattr(a[2], n)[slots], v), n
+        untouched = [1, 2, 4]
+        assert np.array_equal(getattr(a[2], n)[untouched], getattr(st, n)[untouched]), n
+    for n, v in b[4].arrays().items():
+        assert np.array_equal(getattr(a[4], n)[slots], v), n
