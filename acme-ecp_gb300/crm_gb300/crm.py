@@ -19,9 +19,7 @@ _contexts = {}
 
 
 def _key(cfg):
-    return (cfg.crm_nx, cfg.crm_ny, cfg.crm_nz, cfg.crm_nx_rad, cfg.crm_ny_rad, cfg.plev,
-            cfg.crm_dx, cfg.crm_dy, cfg.crm_dt, cfg.microphysics, cfg.precision,
-            cfg.batch_mode, cfg.max_ncrms)
+    return tuple(sorted(cfg.__dict__.items()))
 
 
 def get_context(cfg: T.CrmConfig):

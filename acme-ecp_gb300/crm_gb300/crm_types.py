@@ -72,7 +72,9 @@ class CCrmConfig(C.Structure):
                 ('plev', C.c_int), ('crm_dx', C.c_double),
                 ('crm_dy', C.c_double), ('crm_dt', C.c_double),
                 ('microphysics', C.c_int), ('precision', C.c_int),
-                ('batch_mode', C.c_int), ('max_ncrms', C.c_int)]
+                ('batch_mode', C.c_int), ('max_ncrms', C.c_int),
+                ('use_crm_accel', C.c_int), ('crm_accel_factor', C.c_double),
+                ('crm_accel_uv', C.c_int)]
 
 
 class CCrmInput(C.Structure):
@@ -119,6 +121,9 @@ class CrmConfig:
     precision: int = CRM_FP64
     batch_mode: int = CRM_PER_COLUMN
     max_ncrms: int = 0
+    use_crm_accel: int = 0
+    crm_accel_factor: float = 0.0
+    crm_accel_uv: int = 0
 
     def __post_init__(self):
         if not self.crm_dy:
@@ -133,7 +138,9 @@ class CrmConfig:
                           self.crm_nx_rad, self.crm_ny_rad, self.plev,
                           float(self.crm_dx), float(self.crm_dy),
                           float(self.crm_dt), self.microphysics,
-                          self.precision, self.batch_mode, self.max_ncrms)
+                          self.precision, self.batch_mode, self.max_ncrms,
+                          int(self.use_crm_accel), float(self.crm_accel_factor),
+                          int(self.crm_accel_uv))
 
 
 class _Bundle:

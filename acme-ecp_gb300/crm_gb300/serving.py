@@ -100,7 +100,8 @@ def slot_bytes(cfg):
 
 
 def config_key(cfg):
-    return (cfg.crm_nx, cfg.crm_nz, cfg.plev, cfg.crm_dx, cfg.crm_dt, cfg.precision)
+    """Everything that selects a handle except the column capacity."""
+    return tuple(sorted((k, v) for k, v in cfg.__dict__.items() if k != 'max_ncrms'))
 
 
 class DevicePool:
@@ -136,7 +137,7 @@ class DevicePool:
             self.c_out.field[i] = dp(self.out[n])
         self.ctx = [CrmContext(self.cfg) for _ in range(handles)]
         self.streams = [torch.cuda.Stream() for _ in range(handles)]
-        self._next = 0
+        self.busy = [False] * handles
         # per-launch device scratch: col_map, gcol, status (one set per handle)
         self.d_map = [torch.zeros(capacity, dtype=torch.int32, device=dev) for _ in range(handles)]
         self.d_gcol = [torch.zeros(capacity, dtype=torch.int32, device=dev) for _ in range(handles)]
@@ -182,12 +183,17 @@ class DevicePool:
                 res[n] = h
         return res
 
-    def launch(self, slots, gcol, igstep, dt_gl):
-        """One column kernel over `slots`; returns (handle index, stream)."""
+    def idle_handle(self):
+        """A handle with no launch in flight, or None."""
+        for h in range(len(self.ctx)):
+            if not self.busy[h]:
+                return h
+        return None
+
+    def launch(self, h, slots, gcol, igstep, dt_gl):
+        """One column kernel over `slots` on handle h (and its stream)."""
         from .lib import CrmError
         torch = self.torch
-        h = self._next
-        self._next = (self._next + 1) % len(self.ctx)
         stream = self.streams[h]
         n = len(slots)
         with torch.cuda.stream(stream):
@@ -202,7 +208,7 @@ class DevicePool:
                                 C.c_void_p(self.d_status[h].data_ptr()), C.c_void_p(stream.cuda_stream))
         if rc != T.CRM_OK:
             raise CrmError(rc, 'crm_run_device')
-        return h, stream
+        self.busy[h] = True
 
 
 @dataclass
@@ -227,7 +233,7 @@ class StepRequest:
 class CrmServer:
     """The service: open_chunk / step / close_chunk; see the module docstring."""
 
-    def __init__(self, configs, capacity=1024, hbm_budget=120 * 2 ** 30, handles=2):
+    def __init__(self, configs, capacity=1024, hbm_budget=120 * 2 ** 30, handles=3):
         self.configs = {config_key(c): c for c in configs}
         self.capacity = capacity
         self.budget = HbmBudget(hbm_budget)
@@ -273,6 +279,32 @@ class CrmServer:
         stream.synchronize()
         return Chunk(key, slots, list(gcol), nbytes)
 
+    def checkpoint_chunk(self, chunk, path):
+        """Write a chunk's resident CRM state (the pbuf restart fields, see
+        checkpoint.py) to `path`.  Call between steps of that chunk."""
+        from . import checkpoint as CK
+        torch = __import__('torch')
+        pool = self.pools[chunk.key]
+        stream = pool.streams[0]
+        with torch.cuda.stream(stream):
+            s = torch.tensor(chunk.slots, dtype=torch.int64).to('cuda')
+            host = {n: pool.state[n].index_select(3, s).cpu().numpy().T for n in T.STATE_FIELDS}
+            qrad = pool.rad['qrad'].index_select(3, s).cpu().numpy().T
+        stream.synchronize()
+        st = T.CrmState(**{n: np.asfortranarray(a) for n, a in host.items()})
+        cfg = T.CrmConfig(**{**pool.cfg.__dict__, 'max_ncrms': 0})
+        CK.save(path, cfg, st, np.asfortranarray(qrad), chunk.gcol)
+
+    def restore_chunk(self, path, cin):
+        """Admit a chunk from a restart file (its GCM inputs given anew)."""
+        from . import checkpoint as CK
+        cfg, st, qrad, gcol = CK.load(path)
+        rad = T.CrmRad.zeros(len(gcol), cfg.crm_nx_rad, cfg.crm_ny_rad, cfg.crm_nz)
+        rad.qrad[...] = qrad
+        ch = self.open_chunk(cfg, cin, st, rad, gcol)
+        ch.steps = 1          # a restarted chunk is past its first step
+        return ch
+
     def close_chunk(self, chunk):
         self.pools[chunk.key].slots.free(chunk.slots)
         self.budget.release(chunk.nbytes)
@@ -292,74 +324,90 @@ class CrmServer:
         self._thread.join(timeout=30)
 
     def _engine(self):
+        """Continuous batching: requests accumulate per pool while its handles
+        are busy; whenever a handle is idle, every request waiting for that
+        pool (same dt_gl and first-step flag) goes into one launch on it."""
         import torch
         torch.cuda.set_device(0)
-        inflight = []        # (requests, pool, handle, stream, event)
+        pending = {}         # pool key -> waiting requests, in arrival order
+        inflight = []        # (pool, handle, requests, outputs, status, event)
         while not self._stop.is_set():
-            # take everything waiting (block briefly when idle)
-            reqs = []
             try:
-                r = self._q.get(timeout=0.0005 if inflight else 0.05)
-                if r is not None:
-                    reqs.append(r)
+                r = self._q.get(timeout=0.0005 if (inflight or pending) else 0.05)
                 while True:
-                    r = self._q.get_nowait()
                     if r is not None:
-                        reqs.append(r)
+                        pending.setdefault(r.chunk.key, []).append(r)
+                    r = self._q.get_nowait()
             except queue.Empty:
                 pass
-            groups = {}
-            for r in reqs:
-                groups.setdefault((r.chunk.key, r.dt_gl, r.chunk.steps == 0), []).append(r)
-            for (key, dt_gl, first), rs in groups.items():
+            for key in list(pending):
                 pool = self.pools[key]
-                slots, gcol = [], []
-                for r in rs:
-                    slots += r.chunk.slots
-                    gcol += r.chunk.gcol
-                h = pool._next
-                stream = pool.streams[h]
-                for r in rs:
-                    pool.set_inputs(r.chunk.slots, r.cin, stream)
-                try:
-                    h, stream = pool.launch(slots, gcol, 1 if first else 2, dt_gl)
-                except Exception as e:    # argument errors: fail these requests
-                    for r in rs:
-                        r.future.set_exception(e)
-                    continue
-                outs = [(r, pool.gather(r.chunk.slots, STEP_OUTPUTS, stream)) for r in rs]
-                st = torch.empty(len(slots), dtype=torch.int32, pin_memory=True)
-                with torch.cuda.stream(stream):
-                    st.copy_(pool.d_status[h][:len(slots)], non_blocking=True)
-                ev = torch.cuda.Event()
-                ev.record(stream)
-                inflight.append((outs, st, ev))
-                self.launches += 1
+                while pending.get(key):
+                    h = pool.idle_handle()
+                    if h is None:
+                        break
+                    head = pending[key][0]
+                    tag = (head.dt_gl, head.chunk.steps == 0)
+                    rs = [r for r in pending[key] if (r.dt_gl, r.chunk.steps == 0) == tag]
+                    pending[key] = [r for r in pending[key] if (r.dt_gl, r.chunk.steps == 0) != tag]
+                    inflight.append(self._launch(pool, h, rs, tag))
+                if not pending.get(key):
+                    pending.pop(key, None)
             still = []
-            for outs, st, ev in inflight:
-                if ev.query():
-                    status = st.numpy()
-                    o = 0
-                    t_done = time.perf_counter()
-                    for r, res in outs:
-                        n = len(r.chunk.slots)
-                        r.chunk.steps += 1
-                        vals = {k: v.numpy().T.copy() for k, v in res.items()}
-                        with self._lock:
-                            self.latencies.append(t_done - r.t_submit)
-                        r.future.set_result((vals, status[o:o + n].copy()))
-                        o += n
-                else:
-                    still.append((outs, st, ev))
+            for item in inflight:
+                if item is not None and item[5].query():
+                    self._complete(item)
+                elif item is not None:
+                    still.append(item)
             inflight = still
 
+    def _launch(self, pool, h, rs, tag):
+        import torch
+        dt_gl, first = tag
+        slots, gcol = [], []
+        for r in rs:
+            slots += r.chunk.slots
+            gcol += r.chunk.gcol
+        stream = pool.streams[h]
+        # one host->device copy per input field for the whole group
+        cat = {n: np.concatenate([getattr(r.cin, n)[:len(r.chunk.slots)] for r in rs], axis=0)
+               for n in T.INPUT_FIELDS}
+        pool.set_inputs(slots, T.CrmInput(**cat), stream)
+        try:
+            pool.launch(h, slots, gcol, 1 if first else 2, dt_gl)
+        except Exception as e:    # argument errors: fail these requests
+            for r in rs:
+                r.future.set_exception(e)
+            return None
+        outs = pool.gather(slots, STEP_OUTPUTS, stream)
+        st = torch.empty(len(slots), dtype=torch.int32, pin_memory=True)
+        with torch.cuda.stream(stream):
+            st.copy_(pool.d_status[h][:len(slots)], non_blocking=True)
+        ev = torch.cuda.Event()
+        ev.record(stream)
+        self.launches += 1
+        return (pool, h, rs, outs, st, ev)
 
-def apply_tendencies(cin, vals, dt_gl, cpair=1.00464e3):
-    """Advance the GCM columns by the CRM tendencies, as physics_update does
-    with ptend (state += ptend * dt): T += sltend/cp dt, q += qltend dt, ..."""
-    n = vals['sltend'].shape[0]
-    cin.tl[:n] += vals['sltend'] / cpair * dt_gl
-    cin.ql[:n] = np.maximum(cin.ql[:n] + vals['qltend'] * dt_gl, 0.0)
-    cin.qccl[:n] = np.maximum(cin.qccl[:n] + vals['qcltend'] * dt_gl, 0.0)
-    cin.qiil[:n] = np.maximum(cin.qiil[:n] + vals['qiltend'] * dt_gl, 0.0)
-    return cin
+    def _complete(self, item):
+        pool, h, rs, res, st, ev = item
+        pool.busy[h] = False
+        status = st.numpy()
+        allv = {k: v.numpy().T for k, v in res.items()}    # (N, ...) per field
+        o = 0
+        t_done = time.perf_counter()
+        for r in rs:
+            n = len(r.chunk.slots)
+            r.chunk.steps += 1
+            vals = {k: v[o:o + n].copy() for k, v in allv.items()}
+            with self._lock:
+                self.latencies.append(t_done - r.t_submit)
+            r.future.set_result((vals, status[o:o + n].copy()))
+            o += n
+
+
+def apply_tendencies(cin, vals, dt_gl):
+    """Advance the GCM columns by the CRM tendencies of a step's results, as
+    physics_update does with ptend (gcm_coupling.apply_ptend)."""
+    from .gcm_coupling import apply_ptend
+    pt = {'s': vals['sltend'], 'q': vals['qltend'], 'qc': vals['qcltend'], 'qi': vals['qiltend']}
+    return apply_ptend(cin, pt, dt_gl)

@@ -74,7 +74,9 @@ static void launch_tn(int shape, const KParams &p, int grid, cudaStream_t s) {
   switch (shape) {
     case 0: launch_crm_columns<T, NX, 0>(p, grid, s); break;
     case 1: launch_crm_columns<T, NX, 1>(p, grid, s); break;
-    default: launch_crm_columns<T, NX, 2>(p, grid, s); break;
+    case 2: launch_crm_columns<T, NX, 2>(p, grid, s); break;
+    case 3: launch_crm_columns<T, NX, 3>(p, grid, s); break;
+    default: launch_crm_columns<T, NX, 4>(p, grid, s); break;
   }
 }
 
@@ -83,7 +85,9 @@ static int occupancy_tn(int shape, int nx, int nzm) {
   switch (shape) {
     case 0: return occupancy_crm_columns<T, NX, 0>(nx, nzm);
     case 1: return occupancy_crm_columns<T, NX, 1>(nx, nzm);
-    default: return occupancy_crm_columns<T, NX, 2>(nx, nzm);
+    case 2: return occupancy_crm_columns<T, NX, 2>(nx, nzm);
+    case 3: return occupancy_crm_columns<T, NX, 3>(nx, nzm);
+    default: return occupancy_crm_columns<T, NX, 4>(nx, nzm);
   }
 }
 
@@ -181,15 +185,26 @@ size_t out_elems(const crm_config &c, int f, int ld) {
 
 // Launch shape of the column kernel per precision (crm_kernel.h kShapes),
 // chosen by measurement on GB300; CRM_GB300_SHAPE=<index> overrides it.
-int default_shape(int precision) {
+int default_shape(int precision, int nx) {
   const char *e = getenv("CRM_GB300_SHAPE");
   if (e && *e) {
     int v = atoi(e);
     if (v >= 0 && v < crm::kNumShapes) return v;
   }
-  // measured, 1024 columns of 64 x 58: FP64 (256 threads, 3 CTAs/SM),
-  // FP32-mixed (256 threads, 4 CTAs/SM)
-  return precision == CRM_FP64 ? 1 : 2;
+  // measured on 1024 columns of nx x 58: FP64 best at 256 threads, 3 CTAs/SM;
+  // FP32-mixed at 256 threads, 4 CTAs/SM, with scratch planes A/B in shared
+  // memory for nx <= 32 (+5 %) but not for nx = 64 (-7 %: the planes cost
+  // more L1 than they save)
+  if (precision == CRM_FP64) return 1;
+  return nx <= 32 ? 3 : 2;
+}
+
+// crm_accel_nstop (accelerate_crm.F90:84-106): nstop / (1 + crm_accel_factor),
+// which must divide it; -1 when it does not.
+int accel_nstop(const crm_config &g, int nstop) {
+  if (!g.use_crm_accel) return nstop;
+  if (!(g.crm_accel_factor >= 0.) || nstop % (int)(1 + g.crm_accel_factor) != 0) return -1;
+  return (int)((double)nstop / (1 + g.crm_accel_factor));
 }
 
 int validate(const crm_config *c) {
@@ -217,7 +232,7 @@ int alloc_ctx(crm_ctx *c) {
   CK(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, c->device));
   const size_t esz = g.precision == CRM_FP64 ? sizeof(double) : sizeof(float);
   c->L = crm::make_layout(g.crm_nx, g.crm_nz, g.plev, g.crm_nx_rad, (int)esz);
-  c->shape = default_shape(g.precision);
+  c->shape = default_shape(g.precision, g.crm_nx);
   int per_sm = crm::occupancy_columns(g.precision, c->shape, g.crm_nx, g.crm_nz);
   if (per_sm < 1) return CRM_ERR_UNSUPPORTED;
   c->grid_max = c->nsm * per_sm;
@@ -318,6 +333,8 @@ int enqueue(crm_ctx *c, const crm_call_desc *d, const crm_input_c *in, crm_state
   if (nstop < 1) return CRM_ERR_ARG;
   double dt = d->dt_gl / nstop;
   if (60. < 2 * dt) return CRM_ERR_ARG;         // damping.F90:39-42
+  const int nstop_run = accel_nstop(g, nstop);   // crm_module.F90:718-720
+  if (nstop_run < 1) return CRM_ERR_ARG;
   crm::PrepParams pp;
   pp.ncrms = ncrms; pp.ld = ld; pp.plev = g.plev; pp.nx = g.crm_nx; pp.igstep = d->igstep;
   pp.zmid = in->zmid; pp.zint = in->zint; pp.pdel = in->pdel;
@@ -331,6 +348,9 @@ int enqueue(crm_ctx *c, const crm_call_desc *d, const crm_input_c *in, crm_state
   p.L = c->L;
   p.ncrms = ncrms; p.ld = ld; p.nstop = nstop; p.igstep = d->igstep;
   p.batch_mode = g.batch_mode; p.clamp_batch = 0;
+  p.nstop = nstop_run;
+  p.use_accel = g.use_crm_accel != 0; p.accel_uv = g.crm_accel_uv != 0;
+  p.accel_factor = g.crm_accel_factor;
   p.dx = g.crm_dx; p.dy = g.crm_dx; p.dt = dt; p.dt_gl = d->dt_gl;
   p.gams1 = c->gam[4]; p.gams2 = c->gam[5]; p.gamg1 = c->gam[7]; p.gamg2 = c->gam[8];
   p.gamr1 = c->gam[1]; p.gamr2 = c->gam[2];
@@ -669,11 +689,13 @@ extern "C" int crm_run_device_noalloc(const crm_config *cfg, const crm_call_desc
   if (nstop < 1) return CRM_ERR_ARG;
   const double dt = d->dt_gl / nstop;
   if (60. < 2 * dt) return CRM_ERR_ARG;           // damping.F90:39-42
+  const int nstop_run = accel_nstop(g, nstop);     // crm_module.F90:718-720
+  if (nstop_run < 1) return CRM_ERR_ARG;
 
   NoallocDevice dv;
   rc = noalloc_device(dv);
   if (rc != CRM_OK) return rc;
-  const int shape = default_shape(g.precision);
+  const int shape = default_shape(g.precision, nx);
   int per_sm = crm::occupancy_columns(g.precision, shape, nx, g.crm_nz);
   if (per_sm < 1) return CRM_ERR_UNSUPPORTED;
   int grid = dv.nsm * per_sm;
@@ -748,6 +770,9 @@ extern "C" int crm_run_device_noalloc(const crm_config *cfg, const crm_call_desc
   p.L = q.L;
   p.ncrms = ncrms; p.ld = d->ld; p.nstop = nstop; p.igstep = d->igstep;
   p.batch_mode = g.batch_mode; p.clamp_batch = 0;
+  p.nstop = nstop_run;
+  p.use_accel = g.use_crm_accel != 0; p.accel_uv = g.crm_accel_uv != 0;
+  p.accel_factor = g.crm_accel_factor;
   p.dx = g.crm_dx; p.dy = g.crm_dx; p.dt = dt; p.dt_gl = d->dt_gl;
   p.gams1 = gam[4]; p.gams2 = gam[5]; p.gamg1 = gam[7]; p.gamg2 = gam[8];
   p.gamr1 = gam[1]; p.gamr2 = gam[2];

@@ -84,6 +84,7 @@ struct ColShared {
   double colprec0, colprecs0;
   double cltot, clhgh, clmed, cllow;
   int jt_min, mx_max;
+  int nstop, ceaseflag, acc_flag;   // per-column step count (acceleration)
   unsigned long long t_last;
   double red_d[32];
   int red_i[64];
@@ -111,10 +112,11 @@ struct ColumnKernel : NxDim<NX> {
   int nzm, nz, plev;
   int icrm;   // slot of the column in the (ld, ...) arrays
   int cpos;   // position of the column in the call (status index)
+  T *spl;     // scratch planes A, B in shared memory, or null (slab planes)
 
-  __device__ ColumnKernel(const KParams &p_, ColShared &s_, T *b, int col)
+  __device__ ColumnKernel(const KParams &p_, ColShared &s_, T *b, int col, T *planes = nullptr)
       : NxDim<NX>(p_.L.nx), p(p_), S(s_), base(b), nzm(p_.L.nzm), nz(p_.L.nz), plev(p_.L.plev),
-        icrm(p_.col_map ? p_.col_map[col] : col), cpos(col) {}
+        icrm(p_.col_map ? p_.col_map[col] : col), cpos(col), spl(planes) {}
 
   // ---------------------------------------------------------- accessors
   // x extents of the field classes (first index, row length = nx + extra):
@@ -143,8 +145,14 @@ struct ColumnKernel : NxDim<NX> {
   __device__ __forceinline__ F2<T> DU(int l) const { return fld(p.L.du[l - 1], 1, 1); }
   __device__ __forceinline__ F2<T> DV(int l) const { return fld(p.L.dv[l - 1], 1, 0); }
   __device__ __forceinline__ F2<T> DW(int l) const { return fld(p.L.dw[l - 1], 1, 0); }
-  // scratch planes (x from -2, k from 0)
+  // scratch planes (x from -2, k from 0); A and B (contiguous: A may be
+  // used as one double-length area) live in shared memory when the launch
+  // shape provides them
   __device__ __forceinline__ F2<T> SCR(size_t off) const { return F2<T>{base + off, -2, nx + 6, 0}; }
+  __device__ __forceinline__ T *sa() const { return spl ? spl : base + p.L.s_a; }
+  __device__ __forceinline__ T *sb() const { return spl ? spl + (p.L.s_b - p.L.s_a) : base + p.L.s_b; }
+  __device__ __forceinline__ F2<T> SA() const { return F2<T>{sa(), -2, nx + 6, 0}; }
+  __device__ __forceinline__ F2<T> SB() const { return F2<T>{sb(), -2, nx + 6, 0}; }
   __device__ __forceinline__ T *PR(int id) const { return base + p.L.prof + (size_t)id * (nz + 2); }
   __device__ __forceinline__ T *OP(int id) const { return base + p.L.o_plev + (size_t)id * (plev + 2); }
   __device__ __forceinline__ T &PS(int i) const { return base[p.L.precsfc + (i - 1)]; }
@@ -353,12 +361,18 @@ struct ColumnKernel : NxDim<NX> {
     {
       size_t n = p.L.slab;
       for (size_t e = TID; e < n; e += NT) base[e] = (T)0.;
+      if (spl) {                                  // shared-memory planes A, B
+        size_t m = 2 * (p.L.s_b - p.L.s_a);
+        for (size_t e = TID; e < m; e += NT) spl[e] = (T)0.;
+      }
     }
     if (TID == 0) {
       S.na = 1; S.nb = 2; S.nc = 3;
       S.dt3[0] = S.dt3[1] = S.dt3[2] = 0.;
       S.status = CRM_OK;
       S.z0 = p.z0[icrm];
+      S.nstop = p.nstop;
+      S.ceaseflag = 0;
     }
     SYNC;
     // vertical grid (crm_module.F90:341-375)
@@ -464,7 +478,7 @@ struct ColumnKernel : NxDim<NX> {
     // initial domain means (crm_module.F90:500-546)
     const double factor_xy = 1.0 / (double)nx;
     const double idt_gl = 1.0 / p.dt_gl;
-    double *md = reinterpret_cast<double *>(base + p.L.s_a);   // FP64 copies of the means
+    double *md = reinterpret_cast<double *>(sa());   // FP64 copies of the means
     {
       const int ids[9] = {P_U0, P_V0, P_T0, P_T00, P_TABS0, P_Q0, P_QV0, P_QN0, P_QP0};
       level_sums(9, 1, nzm,
@@ -721,7 +735,7 @@ struct ColumnKernel : NxDim<NX> {
     SYNC;
     kmin = S.kmin; kmax = S.kmax;
     if (kmax == 0) return;                     // no ice cloud: nothing falls
-    F2<T> fz = SCR(p.L.s_a);
+    F2<T> fz = SA();
     T *adz = PR(P_ADZ), *rho = PR(P_RHO);
     const T dtn = (T)S.dtn, dz = (T)S.dz;
     for (int e = TID; e < nx * nz; e += NT) {
@@ -769,7 +783,7 @@ struct ColumnKernel : NxDim<NX> {
   // ---------------------------------------------------------- SGS TKE
   // shear_prod2D.F90:14-95 + tke_full.F90:108-312 (dosmagor = .true.)
   __device__ void tke_full() {
-    F2<T> u = U(), v = V(), w = W(), def2 = SCR(p.L.s_a), buoy = SCR(p.L.s_b), aprod = SCR(p.L.s_c);
+    F2<T> u = U(), v = V(), w = W(), def2 = SA(), buoy = SB(), aprod = SCR(p.L.s_c);
     T *u0 = PR(P_U0), *v0 = PR(P_V0), *adz = PR(P_ADZ), *adzw = PR(P_ADZW);
     const T dz = (T)S.dz, dx = (T)p.dx;
     const T rdx0 = (T)1. / dx;
@@ -896,7 +910,7 @@ struct ColumnKernel : NxDim<NX> {
   // advect2_mom_xy.F90:60-80 (2D) and advect2_mom_z.F90:30-122
   __device__ void advect_mom() {
     F2<T> u = U(), v = V(), w = W(), du = DU(S.na), dv = DV(S.na), dw = DW(S.na);
-    F2<T> fuz = SCR(p.L.s_a), fvz = SCR(p.L.s_b), fwz = SCR(p.L.s_c);
+    F2<T> fuz = SA(), fvz = SB(), fwz = SCR(p.L.s_c);
     T *rho = PR(P_RHO), *adz = PR(P_ADZ), *rhow = PR(P_RHOW), *adzw = PR(P_ADZW);
     const T dx25 = (T)0.25 / (T)p.dx;
     const T dz = (T)S.dz;
@@ -955,7 +969,7 @@ struct ColumnKernel : NxDim<NX> {
   // SGS_TKE/diffuse_mom2D.F90:42-160
   __device__ void diffuse_mom() {
     F2<T> u = U(), v = V(), w = W(), tk = TK(), du = DU(S.na), dv = DV(S.na), dw = DW(S.na);
-    F2<T> fu = SCR(p.L.s_a), fv = SCR(p.L.s_b), fw = SCR(p.L.s_c);
+    F2<T> fu = SA(), fv = SB(), fw = SCR(p.L.s_c);
     T *rho = PR(P_RHO), *adz = PR(P_ADZ), *rhow = PR(P_RHOW), *adzw = PR(P_ADZW);
     T *grdfx = PR(P_GRDFX), *grdfz = PR(P_GRDFZ);
     const T dx = (T)p.dx, dz = (T)S.dz;
@@ -1236,7 +1250,7 @@ struct ColumnKernel : NxDim<NX> {
     {
       const int np = nx + 1, ls = nzm + 1;
       const double *tri = TRI();
-      double *beta = reinterpret_cast<double *>(base + p.L.s_a);   // np x (nzm+1) doubles
+      double *beta = reinterpret_cast<double *>(sa());   // np x (nzm+1) doubles
       for (int i = TID + 1; i <= np; i += NT) {
         const double *al = tri + (size_t)ls + (size_t)(i - 1) * 2 * ls, *e = al + ls;
         double *be = beta + (size_t)(i - 1) * ls;
@@ -1322,7 +1336,7 @@ struct ColumnKernel : NxDim<NX> {
   // advective tendency sum and vertical flux sum.
   __device__ void advect_scalar(F2<T> f, T *fadv, T *flux) {
     F2<T> u = U(), w = W();
-    F2<T> mx = SCR(p.L.s_a), mn = SCR(p.L.s_b), uuu = SCR(p.L.s_c), www = SCR(p.L.s_d), f0 = SCR(p.L.s_e);
+    F2<T> mx = SA(), mn = SB(), uuu = SCR(p.L.s_c), www = SCR(p.L.s_d), f0 = SCR(p.L.s_e);
     F2<T> wfl1 = SCR(p.L.s_f);
     T *rho = PR(P_RHO), *adz = PR(P_ADZ), *rhow = PR(P_RHOW);
     const T eps = (T)R4(1.e-10);
@@ -1450,7 +1464,7 @@ struct ColumnKernel : NxDim<NX> {
   // part 1: terminal velocities and the column precipitation CFL number
   __device__ void precip_fall_1() {
     F2<T> tabs = TABS(), qp = QP();
-    F2<T> wp = SCR(p.L.s_a), omega = SCR(p.L.s_b);
+    F2<T> wp = SA(), omega = SB();
     T *rho = PR(P_RHO), *rhow = PR(P_RHOW), *adz = PR(P_ADZ);
     T *rhofac = PR(P_TMP4), *irhoadz = PR(P_TMP5), *iwmax = PR(P_TMP6);
     const T dtn = (T)S.dtn, dz = (T)S.dz;
@@ -1483,7 +1497,7 @@ struct ColumnKernel : NxDim<NX> {
   // part 2: nprec monotone flux-limited sedimentation sub-steps
   __device__ void precip_fall_2(int nprec) {
     F2<T> tabs = TABS(), qp = QP(), t = TT();
-    F2<T> wp = SCR(p.L.s_a), omega = SCR(p.L.s_b), tq = SCR(p.L.s_c), fz = SCR(p.L.s_d);
+    F2<T> wp = SA(), omega = SB(), tq = SCR(p.L.s_c), fz = SCR(p.L.s_d);
     F2<T> mx = SCR(p.L.s_e), mn = SCR(p.L.s_f), www = SCR(p.L.s_g);
     T *rho = PR(P_RHO), *rhow = PR(P_RHOW), *adz = PR(P_ADZ);
     T *rhofac = PR(P_TMP4), *irhoadz = PR(P_TMP5);
@@ -1573,7 +1587,7 @@ struct ColumnKernel : NxDim<NX> {
   // ---------------------------------------------------------- SGS scalar diffusion
   // SGS_TKE/diffuse_scalar.F90:33-72 + diffuse_scalar2D.F90:44-140
   __device__ void diffuse_scalar(F2<T> f, T *fdiff, T *flux) {
-    F2<T> tkh = TKH(), flx = SCR(p.L.s_a), dfdt = SCR(p.L.s_b), f0 = SCR(p.L.s_c);
+    F2<T> tkh = TKH(), flx = SA(), dfdt = SB(), f0 = SCR(p.L.s_c);
     T *rho = PR(P_RHO), *rhow = PR(P_RHOW), *adz = PR(P_ADZ), *adzw = PR(P_ADZW);
     T *grdfx = PR(P_GRDFX), *grdfz = PR(P_GRDFZ);
     const T dx = (T)p.dx, dz = (T)S.dz, dtn = (T)S.dtn;
@@ -1733,7 +1747,7 @@ struct ColumnKernel : NxDim<NX> {
   // the reference's order from the per-cell contributions
   __device__ void precip_proc() {
     F2<T> qt = QT(), qp = QP(), qn = QN(), tabs = TABS();
-    F2<T> csrc = SCR(p.L.s_a), cevp = SCR(p.L.s_b);
+    F2<T> csrc = SA(), cevp = SB();
     T *pres = PR(P_PRES);
     const T powr1 = (T)((3 + C_B_RAIN) / 4.), powr2 = (T)((5 + C_B_RAIN) / 8.);
     const T pows1 = (T)((3 + C_B_SNOW) / 4.), pows2 = (T)((5 + C_B_SNOW) / 8.);
@@ -1824,6 +1838,90 @@ struct ColumnKernel : NxDim<NX> {
   }
 
   // ---------------------------------------------------------- diagnose
+  // ---------------------------------------------------------- acceleration
+  // Mean-state acceleration, accelerate_crm.F90:109-366 (per column): the
+  // horizontal-mean change of t and qt (u, v) since the last diagnose is
+  // applied accel_factor more times; a |dT| above 5 K stops acceleration for
+  // the rest of the call and stretches nstop so the call still spans dt_gl.
+  __device__ void accelerate(int nstep) {
+    F2<T> t = TT(), qt = QT(), qv = QV(), qcl = QCL(), qci = QCI(), u = U(), v = V();
+    double *ta = reinterpret_cast<double *>(base + p.L.s_c);   // 4 x (nz + 2) FP64
+    auto TA = [&](int q, int k) -> double & { return ta[(size_t)q * (nz + 2) + k]; };
+    const double coef = 1.0 / (double)nx;
+    const int nq = p.accel_uv ? 4 : 2;
+    if (TID == 0) S.acc_flag = 0;
+    SYNC;
+    T *t0 = PR(P_T0), *q0 = PR(P_Q0), *u0 = PR(P_U0), *v0 = PR(P_V0);
+    level_sums(nq, 1, nzm,
+               [&](int q, int i, int k) -> T {
+                 switch (q) {
+                   case 0: return t(i, k) * (T)coef;
+                   case 1: return (qcl(i, k) + qci(i, k) + qv(i, k)) * (T)coef;
+                   case 2: return u(i, k) * (T)coef;
+                   default: return v(i, k) * (T)coef;
+                 }
+               },
+               [&](int, int) { return 0.; },
+               [&](int q, int k, double sv) {
+                 const T *m = q == 0 ? t0 : q == 1 ? q0 : q == 2 ? u0 : v0;
+                 double d = sv - (double)m[k];
+                 TA(q, k) = d;
+                 if (q == 0 && fabs(d) > 5.) S.acc_flag = 1;
+               });
+    SYNC;
+    if (S.acc_flag) {
+      if (TID == 0) {
+        S.ceaseflag = 1;
+        S.nstop = (int)((double)S.nstop + (double)(S.nstop - nstep + 1) * p.accel_factor);
+      }
+      SYNC;
+      return;
+    }
+    const T f = (T)p.accel_factor, tmin = (T)50.;
+    for (int e = TID; e < nx * nzm; e += NT) {
+      int i = 1 + e % nx, k = 1 + e / nx;
+      t(i, k) = mx2(tmin, t(i, k) + f * (T)TA(0, k));
+      if (p.accel_uv) {
+        u(i, k) = u(i, k) + f * (T)TA(2, k);
+        v(i, k) = v(i, k) + f * (T)TA(3, k);
+      }
+      qt(i, k) = qt(i, k) + f * (T)TA(1, k);
+    }
+    SYNC;
+    // clip negative qt per level, rescaling the positive cells (FP64 sums)
+    level_sums(2, 1, nzm,
+               [&](int q, int i, int k) -> T {
+                 T x = qt(i, k);
+                 bool neg = x < (T)0.;
+                 return q == 0 ? (neg ? x : (T)0.) : (neg ? (T)0. : x);
+               },
+               [&](int, int) { return 0.; }, [&](int q, int k, double sv) { TA(q, k) = sv; });
+    SYNC;
+    for (int e = TID; e < nx * nzm; e += NT) {
+      int i = 1 + e % nx, k = 1 + e / nx;
+      const double qneg = TA(0, k), qpoz = TA(1, k);
+      if (qpoz + qneg <= 0.) {
+        qt(i, k) = (T)0.; qv(i, k) = (T)0.; qcl(i, k) = (T)0.; qci(i, k) = (T)0.;
+      } else {
+        double factor = 1. + qneg / qpoz;
+        T q = (T)mx2(0., (double)qt(i, k) * factor);
+        qt(i, k) = q;
+        if (q <= (T)0.) {
+          qv(i, k) = (T)0.; qcl(i, k) = (T)0.; qci(i, k) = (T)0.;
+        } else {
+          T qt_res = q - qcl(i, k) - qci(i, k);
+          qv(i, k) = mx2((T)0., qt_res);
+          if (qt_res < (T)0.) {
+            T fr = (T)1. + qt_res / (qcl(i, k) + qci(i, k));
+            qcl(i, k) = qcl(i, k) * fr;
+            qci(i, k) = qci(i, k) * fr;
+          }
+        }
+      }
+    }
+    SYNC;
+  }
+
   __device__ void diagnose() {                 // diagnose.F90:21-85
     F2<T> t = TT(), tabs = TABS(), qcl = QCL(), qci = QCI(), qpl = QPL(), qpi = QPI(), qv = QV(), u = U(), v = V();
     T *gamaz = PR(P_GAMAZ);
@@ -1834,7 +1932,7 @@ struct ColumnKernel : NxDim<NX> {
     SYNC;
     const double coef = 1. / (double)nx;
     // domain means; q0 and qn0 are kept in FP64 in TMP0/TMP1 for qv0
-    double *q0d = reinterpret_cast<double *>(base + p.L.s_a);
+    double *q0d = reinterpret_cast<double *>(sa());
     level_sums_lo(7, 1, nzm,
                [&](int q, int i, int k) -> T {
                  switch (q) {
@@ -1886,7 +1984,7 @@ struct ColumnKernel : NxDim<NX> {
     }
     // interface mass fluxes (Xu et al. 2002): per-cell contributions at w
     // levels k = 1..nz, zero where a cell does not count
-    F2<T> cmu = SCR(p.L.s_a), cmd = SCR(p.L.s_b);
+    F2<T> cmu = SA(), cmd = SB();
     for (int e = TID; e < nx * nz; e += NT) {
       int i = 1 + e % nx, k = 1 + e / nx;
       T wv = w(i, k), cu = (T)0., cd = (T)0.;
@@ -1985,7 +2083,7 @@ struct ColumnKernel : NxDim<NX> {
     const int ld = p.ld;
     const double factor_xy = 1.0 / (double)nx;
     const double icrm_run_time = 1.0 / p.dt_gl;
-    const double factor_xyt = factor_xy / (double)p.nstop;
+    const double factor_xyt = factor_xy / (double)S.nstop;
     const int ptop = plev - nzm + 1;
     auto O1 = [&](int f) -> double & { return p.out[f][icrm]; };
     auto O2 = [&](int f, int l) -> double & { return p.out[f][(size_t)icrm + (size_t)ld * (l - 1)]; };
@@ -1999,7 +2097,7 @@ struct ColumnKernel : NxDim<NX> {
     // radiation means
     {
       const int nxr = p.L.nx_rad;
-      double tmp1 = ((double)nxr / (double)nx) * ((double)1 / (double)1) / (double)p.nstop;
+      double tmp1 = ((double)nxr / (double)nx) * ((double)1 / (double)1) / (double)S.nstop;
       T *rad = base + p.L.rad;
       for (int e = TID; e < nxr * nzm; e += NT) {
         int ir = 1 + e % nxr, k = 1 + e / nxr;
@@ -2010,7 +2108,7 @@ struct ColumnKernel : NxDim<NX> {
     }
     SYNC;
     // horizontal sums of the final state per CRM level (FP64 scratch)
-    double *hs = reinterpret_cast<double *>(base + p.L.s_a);    // 12 x (nz + 2)
+    double *hs = reinterpret_cast<double *>(sa());    // 12 x (nz + 2)
     auto HS = [&](int q, int k) -> double & { return hs[(size_t)q * (nz + 2) + k]; };
     {
       T *u0p = PR(P_U0), *v0p = PR(P_V0);
@@ -2091,7 +2189,7 @@ struct ColumnKernel : NxDim<NX> {
       double rhow = (double)PR(P_RHOW)[k], rho = (double)PR(P_RHO)[k];
       double tmp1 = S.dz / rhow;
       double tmp2 = tmp1 / S.dtn;
-      double ns = (double)p.nstop;
+      double ns = (double)S.nstop;
       double mkwsb0 = (double)PR(P_MKWSB0)[k] * tmp1 * rhow * factor_xy / ns;
       double mkwsb1 = (double)PR(P_MKWSB1)[k] * tmp1 * rhow * factor_xy / ns;
       double mkwle0 = (double)PR(P_MKWLE0)[k] * tmp2 * rhow * factor_xy / ns;
@@ -2149,13 +2247,13 @@ struct ColumnKernel : NxDim<NX> {
       O1(CRM_OUT_PRECTEND) = (cp - S.colprec0) / C_GGR * factor_xy * icrm_run_time;
       O1(CRM_OUT_PRECSTEND) = (cps - S.colprecs0) / C_GGR * factor_xy * icrm_run_time;
       O1(CRM_OUT_Z0M) = S.z0;
-      O1(CRM_OUT_TAUX) = 0.0 / (double)p.nstop;
-      O1(CRM_OUT_TAUY) = 0.0 / (double)p.nstop;
+      O1(CRM_OUT_TAUX) = 0.0 / (double)S.nstop;
+      O1(CRM_OUT_TAUY) = 0.0 / (double)S.nstop;
       double precc = 0, precl = 0, precsc = 0, precsl = 0;
       const double thr = (double)(10.f / 86400.f);
       for (int i = 1; i <= nx; ++i) {
-        double ps = (double)PS(i) * S.dz / p.dt / (double)p.nstop;
-        double pss = (double)PSS(i) * S.dz / p.dt / (double)p.nstop;
+        double ps = (double)PS(i) * S.dz / p.dt / (double)S.nstop;
+        double pss = (double)PSS(i) * S.dz / p.dt / (double)S.nstop;
         if (ps > thr) { precc = precc + ps; precsc = precsc + pss; }
         else { precl = precl + ps; precsl = precsl + pss; }
         p.out[CRM_OUT_PREC_CRM][(size_t)icrm + (size_t)ld * (i - 1)] = ps / 1000.;
@@ -2171,7 +2269,7 @@ struct ColumnKernel : NxDim<NX> {
       int jt = S.jt_min, mx = S.mx_max;
       O1(CRM_OUT_JT_CRM) = (jt <= plev) ? mn2((double)plev, (double)jt) : (double)plev;
       O1(CRM_OUT_MX_CRM) = mx2(1.0, (double)mx);
-      O1(CRM_OUT_TIMING_FACTOR) = (double)p.nstop / (double)p.nstop;
+      O1(CRM_OUT_TIMING_FACTOR) = (double)S.nstop / (double)S.nstop;
       p.col_status[cpos] = S.status;
     }
     SYNC;
@@ -2188,7 +2286,7 @@ struct ColumnKernel : NxDim<NX> {
     if (TID == 0) { S.jt_min = 1 << 30; S.mx_max = 0; }
     SYNC;
     PHASE_MARK(PH_INIT);
-    for (int nstep = 1; nstep <= p.nstop; ++nstep) {
+    for (int nstep = 1; nstep <= S.nstop; ++nstep) {
       kurant();
       PHASE_MARK(PH_KURANT);
       if (S.ncycle > 16) {
@@ -2254,6 +2352,7 @@ struct ColumnKernel : NxDim<NX> {
         PHASE_MARK(PH_PPROC);
         micro_diagnose();
         PHASE_MARK(PH_MDIAG);
+        if (p.use_accel && !S.ceaseflag) accelerate(nstep);
         diagnose();
         if (TID == 0) { int nn = S.na; S.na = S.nc; S.nc = S.nb; S.nb = nn; }
         SYNC;
@@ -2267,20 +2366,28 @@ struct ColumnKernel : NxDim<NX> {
   }
 };
 
+// Dynamic shared memory: FFT rows (nx+2) x nzm, one FFT work row per warp,
+// then (optionally) scratch planes A and B, each starting on 64 elements.
+__host__ __device__ inline size_t crm_round64(size_t n) { return (n + 63) / 64 * 64; }
+__host__ __device__ inline size_t crm_plane_elems(int nx, int nzm) { return crm_round64((size_t)(nx + 6) * (nzm + 2)); }
 template <typename T>
-__host__ __device__ inline size_t crm_smem_bytes(int nx, int nzm, int block) {
-  return sizeof(T) * ((size_t)(nx + 2) * nzm + (size_t)(block / 32) * (nx + 4));
+__host__ __device__ inline size_t crm_smem_bytes(int nx, int nzm, int block, int planes = 0) {
+  size_t e = (size_t)(nx + 2) * nzm + (size_t)(block / 32) * (nx + 4);
+  if (planes) e = crm_round64(e) + (size_t)planes * crm_plane_elems(nx, nzm);
+  return sizeof(T) * e;
 }
 
-template <typename T, int NX, int NTH, int MINB>
+template <typename T, int NX, int NTH, int MINB, int SMP>
 __global__ void __launch_bounds__(NTH, MINB) crm_columns_kernel(const __grid_constant__ KParams p) {
   __shared__ ColShared S;
   extern __shared__ __align__(16) unsigned char crm_dsm[];
   T *fsh = reinterpret_cast<T *>(crm_dsm);
   T *wsh = fsh + (size_t)(p.L.nx + 2) * p.L.nzm;
+  T *planes = nullptr;
+  if (SMP) planes = fsh + crm_round64((size_t)(p.L.nx + 2) * p.L.nzm + (size_t)(NTH / 32) * (p.L.nx + 4));
   T *base = reinterpret_cast<T *>(p.slabs) + (size_t)blockIdx.x * p.L.slab;
   for (int col = blockIdx.x; col < p.ncrms; col += gridDim.x) {
-    ColumnKernel<T, NX> K(p, S, base, col);
+    ColumnKernel<T, NX> K(p, S, base, col, planes);
     K.run(fsh, wsh);
     __syncthreads();
   }
@@ -2288,19 +2395,20 @@ __global__ void __launch_bounds__(NTH, MINB) crm_columns_kernel(const __grid_con
 
 template <typename T, int NX, int SHAPE>
 void launch_crm_columns(const KParams &p, int grid, cudaStream_t s) {
-  constexpr int nth = kShapes[SHAPE].threads, minb = kShapes[SHAPE].min_ctas;
-  size_t smem = crm_smem_bytes<T>(p.L.nx, p.L.nzm, nth);
-  cudaFuncSetAttribute(crm_columns_kernel<T, NX, nth, minb>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  crm_columns_kernel<T, NX, nth, minb><<<grid, nth, smem, s>>>(p);
+  constexpr int nth = kShapes[SHAPE].threads, minb = kShapes[SHAPE].min_ctas, smp = kShapes[SHAPE].smem_planes;
+  size_t smem = crm_smem_bytes<T>(p.L.nx, p.L.nzm, nth, smp);
+  cudaFuncSetAttribute(crm_columns_kernel<T, NX, nth, minb, smp>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  crm_columns_kernel<T, NX, nth, minb, smp><<<grid, nth, smem, s>>>(p);
 }
 
 template <typename T, int NX, int SHAPE>
 int occupancy_crm_columns(int nx, int nzm) {
-  constexpr int nth = kShapes[SHAPE].threads, minb = kShapes[SHAPE].min_ctas;
+  constexpr int nth = kShapes[SHAPE].threads, minb = kShapes[SHAPE].min_ctas, smp = kShapes[SHAPE].smem_planes;
   int n = 0;
-  size_t smem = crm_smem_bytes<T>(nx, nzm, nth);
-  cudaFuncSetAttribute(crm_columns_kernel<T, NX, nth, minb>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, crm_columns_kernel<T, NX, nth, minb>, nth, smem) != cudaSuccess)
+  size_t smem = crm_smem_bytes<T>(nx, nzm, nth, smp);
+  if (smem > 227 * 1024) return 0;
+  cudaFuncSetAttribute(crm_columns_kernel<T, NX, nth, minb, smp>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, crm_columns_kernel<T, NX, nth, minb, smp>, nth, smem) != cudaSuccess)
     return 0;
   return n;
 }

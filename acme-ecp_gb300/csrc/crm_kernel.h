@@ -8,6 +8,9 @@ namespace crm {
 struct KParams {
   Layout L;
   int ncrms, ld, nstop, igstep, batch_mode, clamp_batch;
+  // mean-state acceleration (nstop above is already divided by 1 + factor)
+  int use_accel, accel_uv;
+  double accel_factor;
   double dx, dy, dt, dt_gl;
   // per-call constants computed on the host (gamma functions, fall speeds)
   double gams1, gams2, gamg1, gamg2, gamr1, gamr2;
@@ -47,9 +50,10 @@ enum PhaseId {
 // measurement (crm_host.cu).
 struct KShape {
   int threads, min_ctas;
+  int smem_planes;   // scratch planes A and B in shared memory (0 or 2)
 };
-constexpr int kNumShapes = 3;
-constexpr KShape kShapes[kNumShapes] = {{256, 2}, {256, 3}, {256, 4}};
+constexpr int kNumShapes = 5;
+constexpr KShape kShapes[kNumShapes] = {{256, 2, 0}, {256, 3, 0}, {256, 4, 0}, {256, 4, 2}, {256, 3, 2}};
 
 // Horizontal sizes with a kernel specialised at compile time (the reference
 // fixes CRM_NX at build time too); any other power of two runs the generic

@@ -153,6 +153,8 @@ def main():
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--fp64-steps', type=int, default=2)
     ap.add_argument('--cpu-cols', type=int, default=512)
+    ap.add_argument('--serve-seconds', type=float, default=20.0,
+                    help='duration of the 80%%-load serving window (0: skip serving)')
     args = ap.parse_args()
     if args.impl == 'reference':
         return run_reference(args)
@@ -281,6 +283,28 @@ def main():
         den = np.linalg.norm(b)
         errs[n] = float(np.linalg.norm(a - b) / den) if den > 0 else float(np.linalg.norm(a - b))
 
+    # ---- serving: Poisson chunks of mixed (nx, nz) at 80 % of the closed-loop peak
+    serving = None
+    if rank == 0 and args.serve_seconds > 0:
+        from crm_gb300 import serve_bench as SB
+        from crm_gb300.serving import CrmServer, config_key
+        scfg = SB.chunk_configs(T.CRM_FP32_MIXED)
+        server = CrmServer(scfg, capacity=1024, hbm_budget=120 * 2 ** 30)
+        for c in scfg:
+            server.pool(config_key(c))
+        steps_per_chunk = 8
+        pk = SB.measure_peak(server, scfg, steps_per_chunk, args.serve_seconds)
+        ld = SB.run_load(server, scfg, steps_per_chunk, 0.8 * pk['column_steps_per_s'], args.serve_seconds)
+        server.close()
+        serving = {'workload': 'chunks of U{1..64} columns, crm_nx in {32,64,128}, crm_nz in {28,58}, '
+                               '72 levels, dt_gl 1200 s, %d GCM steps per chunk, Poisson arrivals, '
+                               'FP32-mixed, 120 GB HBM budget' % steps_per_chunk,
+                   'peak_column_steps_per_s': pk['column_steps_per_s'],
+                   'load': 0.8, 'offered_column_steps_per_s': ld['offered_column_steps_per_s'],
+                   'column_steps_per_s': ld['column_steps_per_s'],
+                   'p50_ms': ld['p50_ms'], 'p99_ms': ld['p99_ms'], 'chunk_steps': ld['steps'],
+                   'launches': server.launches}
+
     if rank != 0:
         if ws > 1:
             dist.destroy_process_group()
@@ -325,10 +349,11 @@ def main():
                 'h2d_bytes_per_step': int(h2d), 'd2h_bytes_per_step': int(d2h),
                 'ms_per_step': e2e_ms},
         'clocks': clk,
-        'gpu_launches': 2 * args.steps,
+        'gpu_launches': 2 * args.steps,   # crm_prep_kernel + crm_columns_kernel per timed step
         'fp64_plain': {'value': value64, 'unit': UNIT, 'ms_per_step': ms64, 'steps': args.fp64_steps},
         'fp32_over_fp64': value / value64,
         'fp32_rel_l2_vs_fp64_state': errs,
+        'serving': serving,
     }
     print(json.dumps(line))
     if ws > 1:

@@ -69,6 +69,14 @@ typedef struct crm_config {
   int precision;                /* enum crm_precision                    */
   int batch_mode;               /* enum crm_batch_mode                   */
   int max_ncrms;                /* largest ncrms a handle will be given  */
+  /* Mean-state acceleration (accelerate_crm.F90; Jones et al. 2015), the
+   * use_crm_accel / crm_accel_factor / crm_accel_uv namelist options: the
+   * horizontal-mean tendency of t and qt (and u, v) is applied
+   * crm_accel_factor extra times after each microphysics call and nstop is
+   * divided by 1 + crm_accel_factor, which must divide it. */
+  int use_crm_accel;
+  double crm_accel_factor;
+  int crm_accel_uv;
 } crm_config;
 
 /* crm_input_type (crm_input_module.F90:10-47); (ld, plev) unless noted. */

@@ -520,6 +520,9 @@ struct Model {
       return a[(size_t)icrm + (size_t)ld * ((i - 1) + (size_t)nx * ((j - 1) + (size_t)ny * (k - 1)))];
     };
     setup_grid(c, icrm);
+    c.nstop = g.nstop;
+    c.nstep = 0;
+    c.ceaseflag = false;
     c.bflx = in->bflxls[icrm];
     c.wnd = in->wndls[icrm];
     for (int k = 1; k <= nzm; ++k)
@@ -1764,7 +1767,89 @@ struct Model {
     advect_scalar2D(c, c.qp, &c.mkadv[1], &c.mkwle[1]);
     precip_fall_part1(c, s);
   }
-  void substep_b(Column &c, FallScratch &s, int nprec) {
+  // ---- mean-state acceleration (accelerate_crm.F90:109-366), split so the
+  // batch mode can take its cease decision across all columns.
+  struct AccelTend {
+    std::vector<double> t, q, u, v;
+  };
+  // horizontal means minus the previous diagnose means; true when some
+  // |ttend| exceeds 5 K (accelerate_crm.F90:181-236)
+  bool accel_tend(Column &c, AccelTend &a) {
+    const int nx = g.nx, ny = g.ny, nzm = g.nzm;
+    const double coef = 1.0 / (double)(nx * ny);
+    a.t.assign(nzm + 1, 0.); a.q.assign(nzm + 1, 0.); a.u.assign(nzm + 1, 0.); a.v.assign(nzm + 1, 0.);
+    bool cease = false;
+    for (int k = 1; k <= nzm; ++k) {
+      double tb = 0, qb = 0, ub = 0, vb = 0;
+      for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
+          tb = tb + c.t(i, j, k) * coef;
+          qb = qb + (c.qcl(i, j, k) + c.qci(i, j, k) + c.qv(i, j, k)) * coef;
+          if (g.accel_uv) {
+            ub = ub + c.u(i, j, k) * coef;
+            vb = vb + c.v(i, j, k) * coef;
+          }
+        }
+      a.t[k] = tb - c.t0(k);
+      a.q[k] = qb - c.q0(k);
+      if (g.accel_uv) { a.u[k] = ub - c.u0(k); a.v[k] = vb - c.v0(k); }
+      if (fabs(a.t[k]) > 5.) cease = true;
+    }
+    return cease;
+  }
+  // accelerate_crm.F90:238-262: no acceleration now or later; nstop grows
+  // so the integration still covers dt_gl
+  void accel_cease(Column &c) {
+    c.ceaseflag = true;
+    c.nstop = (int)((double)c.nstop + (double)(c.nstop - c.nstep + 1) * g.accel_factor);
+  }
+  // accelerate_crm.F90:264-352: apply, then clip negative qt per level and
+  // repartition qv, qcl, qci
+  void accel_apply(Column &c, const AccelTend &a) {
+    const int nx = g.nx, ny = g.ny, nzm = g.nzm;
+    const double f = g.accel_factor, tmin = 50.;
+    for (int k = 1; k <= nzm; ++k)
+      for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
+          c.t(i, j, k) = fmax2(tmin, c.t(i, j, k) + f * a.t[k]);
+          if (g.accel_uv) {
+            c.u(i, j, k) = c.u(i, j, k) + f * a.u[k];
+            c.v(i, j, k) = c.v(i, j, k) + f * a.v[k];
+          }
+          c.qt(i, j, k) = c.qt(i, j, k) + f * a.q[k];
+        }
+    for (int k = 1; k <= nzm; ++k) {
+      double qpoz = 0., qneg = 0.;
+      for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
+          if (c.qt(i, j, k) < 0.) qneg = qneg + c.qt(i, j, k);
+          else qpoz = qpoz + c.qt(i, j, k);
+        }
+      for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
+          if (qpoz + qneg <= 0.) {
+            c.qt(i, j, k) = 0.; c.qv(i, j, k) = 0.; c.qcl(i, j, k) = 0.; c.qci(i, j, k) = 0.;
+          } else {
+            double factor = 1. + qneg / qpoz;
+            c.qt(i, j, k) = fmax2(0., c.qt(i, j, k) * factor);
+            if (c.qt(i, j, k) <= 0.) {
+              c.qv(i, j, k) = 0.; c.qcl(i, j, k) = 0.; c.qci(i, j, k) = 0.;
+            } else {
+              double qt_res = c.qt(i, j, k) - c.qcl(i, j, k) - c.qci(i, j, k);
+              c.qv(i, j, k) = fmax2(0., qt_res);
+              if (qt_res < 0.) {
+                double fr = 1. + qt_res / (c.qcl(i, j, k) + c.qci(i, j, k));
+                c.qcl(i, j, k) = c.qcl(i, j, k) * fr;
+                c.qci(i, j, k) = c.qci(i, j, k) * fr;
+              }
+            }
+          }
+        }
+    }
+  }
+
+  // substep_b up to the microphysics (crm_module.F90:800-869)
+  void substep_b_micro(Column &c, FallScratch &s, int nprec) {
     precip_fall_part2(c, s, nprec);
     uvw(c);
     boundaries(c, 3);
@@ -1775,8 +1860,20 @@ struct Model {
     cloud(c);
     precip_proc(c);
     micro_diagnose(c);
+  }
+  // after the (optional) acceleration: diagnose and rotate the AB levels
+  void substep_b_end(Column &c) {
     diagnose(c);
     int nn = c.na; c.na = c.nc; c.nc = c.nb; c.nb = nn;
+  }
+  void substep_b(Column &c, FallScratch &s, int nprec) {
+    substep_b_micro(c, s, nprec);
+    if (g.use_accel && !c.ceaseflag) {   // crm_module.F90:871-876
+      AccelTend a;
+      if (accel_tend(c, a)) accel_cease(c);
+      else accel_apply(c, a);
+    }
+    substep_b_end(c);
   }
 
   // ---- per-step statistics (crm_module.F90:896-1073)
@@ -1889,6 +1986,14 @@ static int setup_grid_constants(Grid &g, const crm_config *cfg, const crm_call_d
   g.nstop = (int)(desc->dt_gl / cfg->crm_dt);   // crm_module.F90:712-713
   if (g.nstop < 1) return CRM_ERR_ARG;
   g.dt = desc->dt_gl / g.nstop;
+  // crm_accel_nstop (accelerate_crm.F90:84-106)
+  g.use_accel = cfg->use_crm_accel != 0;
+  g.accel_factor = cfg->crm_accel_factor;
+  g.accel_uv = cfg->crm_accel_uv != 0;
+  if (g.use_accel) {
+    if (!(g.accel_factor >= 0.) || g.nstop % (int)(1 + g.accel_factor) != 0) return CRM_ERR_ARG;
+    g.nstop = (int)((double)g.nstop / (1 + g.accel_factor));
+  }
   if (60. < 2 * g.dt) return CRM_ERR_ARG;       // damping.F90:39-42
   fax(g.ifaxi, g.nx);
   for (int k = 1; k <= g.ifaxi[0]; ++k)
@@ -1937,7 +2042,7 @@ static void finalize_column(Model &M, Column &c, int icrm, crm_state_c *st, crm_
   const int nx = g.nx, ny = g.ny, nzm = g.nzm, plev = g.plev, ld = M.ld, Y = g.YES3D;
   const double factor_xy = 1.0 / (double)(nx * ny);
   const double icrm_run_time = 1.0 / M.desc->dt_gl;
-  const double factor_xyt = factor_xy / (double)g.nstop;
+  const double factor_xyt = factor_xy / (double)c.nstop;
   const int ptop = plev - nzm + 1;
   auto O1 = [&](int f) -> double & { return out->field[f][icrm]; };
   auto O2 = [&](int f, int l) -> double & { return out->field[f][(size_t)icrm + (size_t)ld * (l - 1)]; };
@@ -1948,7 +2053,7 @@ static void finalize_column(Model &M, Column &c, int icrm, crm_state_c *st, crm_
   // radiation means
   {
     double fx = (double)g.nx_rad / (double)nx, fy = (double)g.ny_rad / (double)ny;
-    double tmp1 = fx * fy / (double)g.nstop;
+    double tmp1 = fx * fy / (double)c.nstop;
     for (int k = 1; k <= nzm; ++k)
       for (int j = 1; j <= g.ny_rad; ++j)
         for (int i = 1; i <= g.nx_rad; ++i) {
@@ -2016,8 +2121,8 @@ static void finalize_column(Model &M, Column &c, int icrm, crm_state_c *st, crm_
         O4(out->field[CRM_OUT_QPI], i, j, k) = c.qpi(i, j, k);
       }
   O1(CRM_OUT_Z0M) = c.z0;
-  O1(CRM_OUT_TAUX) = 0.0 / (double)g.nstop;
-  O1(CRM_OUT_TAUY) = 0.0 / (double)g.nstop;
+  O1(CRM_OUT_TAUX) = 0.0 / (double)c.nstop;
+  O1(CRM_OUT_TAUY) = 0.0 / (double)c.nstop;
   // domain means of condensate at the end of the call
   std::vector<double> qcm(plev + 1, 0.), qim(plev + 1, 0.), qrm(plev + 1, 0.), qgm(plev + 1, 0.), qsm(plev + 1, 0.);
   for (int k = 1; k <= nzm; ++k)
@@ -2052,8 +2157,8 @@ static void finalize_column(Model &M, Column &c, int icrm, crm_state_c *st, crm_
   const double thr = (double)(10.f / 86400.f);
   for (int j = 1; j <= ny; ++j)
     for (int i = 1; i <= nx; ++i) {
-      double ps = c.precsfc(i, j, 1) * c.dz / g.dt / (double)g.nstop;
-      double pss = c.precssfc(i, j, 1) * c.dz / g.dt / (double)g.nstop;
+      double ps = c.precsfc(i, j, 1) * c.dz / g.dt / (double)c.nstop;
+      double pss = c.precssfc(i, j, 1) * c.dz / g.dt / (double)c.nstop;
       if (ps > thr) { precc = precc + ps; precsc = precsc + pss; }
       else { precl = precl + ps; precsl = precsl + pss; }
       out->field[CRM_OUT_PREC_CRM][(size_t)icrm + (size_t)ld * ((i - 1) + (size_t)nx * (j - 1))] = ps / 1000.;
@@ -2102,18 +2207,18 @@ static void finalize_column(Model &M, Column &c, int icrm, crm_state_c *st, crm_
     double tmp2 = tmp1 / c.dtn;
     double mkwsb[2], mkwle[2], mkadv[2], mkdiff[2];
     for (int m = 0; m < 2; ++m) {
-      mkwsb[m] = c.mkwsb[m](k) * tmp1 * c.rhow(k) * factor_xy / (double)g.nstop;
-      mkwle[m] = c.mkwle[m](k) * tmp2 * c.rhow(k) * factor_xy / (double)g.nstop;
+      mkwsb[m] = c.mkwsb[m](k) * tmp1 * c.rhow(k) * factor_xy / (double)c.nstop;
+      mkwle[m] = c.mkwle[m](k) * tmp2 * c.rhow(k) * factor_xy / (double)c.nstop;
       mkadv[m] = c.mkadv[m](k) * factor_xy * icrm_run_time;
       mkdiff[m] = c.mkdiff[m](k) * factor_xy * icrm_run_time;
     }
     double qpsrc = c.qpsrc(k) * factor_xy * icrm_run_time;
     double qpevp = c.qpevp(k) * factor_xy * icrm_run_time;
     double qpfall = c.qpfall(k) * factor_xy * icrm_run_time;
-    double precflux = c.precflux(k) * factor_xy * c.dz / g.dt / (double)g.nstop;
+    double precflux = c.precflux(k) * factor_xy * c.dz / g.dt / (double)c.nstop;
     int l = plev - k + 1;
-    O2(CRM_OUT_FLUX_U, l) = (c.uwle(k) + c.uwsb(k)) * tmp1 * factor_xy / (double)g.nstop;
-    O2(CRM_OUT_FLUX_V, l) = (c.vwle(k) + c.vwsb(k)) * tmp1 * factor_xy / (double)g.nstop;
+    O2(CRM_OUT_FLUX_U, l) = (c.uwle(k) + c.uwsb(k)) * tmp1 * factor_xy / (double)c.nstop;
+    O2(CRM_OUT_FLUX_V, l) = (c.vwle(k) + c.vwsb(k)) * tmp1 * factor_xy / (double)c.nstop;
     O2(CRM_OUT_FLUX_QT, l) = mkwle[0] + mkwsb[0];
     O2(CRM_OUT_FLUXSGS_QT, l) = mkwsb[0];
     O2(CRM_OUT_FLUX_QP, l) = mkwle[1] + mkwsb[1];
@@ -2136,7 +2241,7 @@ static void finalize_column(Model &M, Column &c, int icrm, crm_state_c *st, crm_
     O2(CRM_OUT_QT_LS, l) = c.qtend(k);
     O2(CRM_OUT_T_LS, l) = c.ttend(k);
   }
-  O1(CRM_OUT_TIMING_FACTOR) = (double)g.nstop / (double)g.nstop;
+  O1(CRM_OUT_TIMING_FACTOR) = (double)c.nstop / (double)c.nstop;
 }
 
 }  // namespace oracle
@@ -2170,7 +2275,8 @@ static void run_column_full(Model &M, Column &c, int icrm, int pos, crm_state_c 
   M.init_column(c, icrm, st, rad, clamp_test(g, st, icrm, M.ld));
   if (M.desc->igstep <= 1) M.setperturb(c, M.desc->gcol[pos] * 1000);
   Model::FallScratch s;
-  for (int nstep = 1; nstep <= g.nstop && c.status == CRM_OK; ++nstep) {
+  for (int nstep = 1; nstep <= c.nstop && c.status == CRM_OK; ++nstep) {
+    c.nstep = nstep;
     M.kurant(c);
     c.ncycle = Model::ncycle_of(c.cfl);
     if (c.ncycle > 16) { c.status = CRM_ERR_CFL; break; }
@@ -2235,7 +2341,11 @@ int oracle_crm_run(const crm_config *cfg, const crm_call_desc *desc, const crm_i
       if (desc->igstep <= 1) M.setperturb(c, desc->gcol[icrm] * 1000);
     }
     int status = CRM_OK;
-    for (int nstep = 1; nstep <= g.nstop && status == CRM_OK; ++nstep) {
+    int nstop = g.nstop;          // batch-wide, like the reference's
+    bool cease = false;
+    std::vector<Model::AccelTend> acc(ncrms);
+    for (int nstep = 1; nstep <= nstop && status == CRM_OK; ++nstep) {
+      for (int icrm = 0; icrm < ncrms; ++icrm) M.cols[icrm].nstep = nstep;
       int ncycle = 1;
       for (int icrm = 0; icrm < ncrms; ++icrm) {
         M.kurant(M.cols[icrm]);
@@ -2251,7 +2361,21 @@ int oracle_crm_run(const crm_config *cfg, const crm_call_desc *desc, const crm_i
         int nprec = 1;
         for (int icrm = 0; icrm < ncrms; ++icrm) nprec = std::max(nprec, Model::nprec_of(M.cols[icrm].prec_cfl));
 #pragma omp parallel for schedule(dynamic, 1)
-        for (int icrm = 0; icrm < ncrms; ++icrm) M.substep_b(M.cols[icrm], scr[icrm], nprec);
+        for (int icrm = 0; icrm < ncrms; ++icrm) M.substep_b_micro(M.cols[icrm], scr[icrm], nprec);
+        if (g.use_accel && !cease) {   // one cease decision for the batch
+          bool any = false;
+          for (int icrm = 0; icrm < ncrms; ++icrm) any = M.accel_tend(M.cols[icrm], acc[icrm]) || any;
+          if (any) {
+            cease = true;
+            nstop = (int)((double)nstop + (double)(nstop - nstep + 1) * g.accel_factor);
+            for (int icrm = 0; icrm < ncrms; ++icrm) { M.cols[icrm].ceaseflag = true; M.cols[icrm].nstop = nstop; }
+          } else {
+#pragma omp parallel for schedule(dynamic, 1)
+            for (int icrm = 0; icrm < ncrms; ++icrm) M.accel_apply(M.cols[icrm], acc[icrm]);
+          }
+        }
+#pragma omp parallel for schedule(dynamic, 1)
+        for (int icrm = 0; icrm < ncrms; ++icrm) M.substep_b_end(M.cols[icrm]);
       }
 #pragma omp parallel for schedule(dynamic, 1)
       for (int icrm = 0; icrm < ncrms; ++icrm) M.step_stats(M.cols[icrm]);

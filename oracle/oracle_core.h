@@ -76,6 +76,9 @@ struct Grid {           // per-call constants shared by all columns
   double vrain, vsnow, vgrau, crain, csnow, cgrau;
   double a_bg, a_pr, a_gr;
   int batch_mode;
+  // mean-state acceleration (accelerate_crm.F90)
+  bool use_accel, accel_uv;
+  double accel_factor;
 };
 
 struct Column {
@@ -104,6 +107,9 @@ struct Column {
   double prec_cfl;
   int nprec;
   int status;
+  int nstop;               // per column: grows if acceleration ceases
+  int nstep;               // current CRM step
+  bool ceaseflag;          // acceleration stopped for the rest of the call
   // per-call accumulators
   double colprec, colprecs;
   // per-step statistics (GCM levels 1..plev, interfaces 1..plev+1)

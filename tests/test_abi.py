@@ -50,7 +50,7 @@ def test_struct_sizes_match_the_header():
     assert C.sizeof(T.CCrmOutput) == C.sizeof(C.c_void_p) * len(T.OUTPUT_FIELDS)
     assert C.sizeof(T.CCrmInput) == C.sizeof(C.c_void_p) * len(T.INPUT_FIELDS)
     assert C.sizeof(T.CCrmState) == C.sizeof(C.c_void_p) * 7
-    assert C.sizeof(T.CCrmConfig) == 6 * 4 + 3 * 8 + 4 * 4
+    assert C.sizeof(T.CCrmConfig) == 6 * 4 + 3 * 8 + 4 * 4 + 8 + 8 + 8
 
 
 @pytest.mark.skipif(has_gpu(), reason='checks the no-device path')

@@ -1,0 +1,31 @@
+"""GCM side of the CRM call: the column water identity of check_energy_chng
+holds for the oracle's output (FP64), and a few GCM steps of tendencies
+applied between calls keep it."""
+import numpy as np
+
+import oracle
+from crm_gb300 import gcm_coupling as G
+from crm_gb300 import synthetic as S
+
+
+def test_water_identity_holds():
+    for wl in (S.workload0, S.workload1):
+        cfg, cin, st, rad, desc = wl(ncrms=3, moist=True)
+        rc, stat, out = oracle.run(cfg, desc, cin, st, rad)
+        assert rc == 0
+        r = G.water_residual(cin, out, 3)
+        assert np.all(np.abs(r) <= 1e-9 * G.water_scale(cin, out, 3)), r
+
+
+def test_coupled_steps_keep_the_identity():
+    cfg, cin, st, rad, desc = S.workload0(ncrms=2, moist=True)
+    for igstep in (1, 2, 3):
+        desc.igstep = igstep
+        rc, stat, out = oracle.run(cfg, desc, cin, st, rad)
+        assert rc == 0
+        r = G.water_residual(cin, out, 2)
+        assert np.all(np.abs(r) <= 1e-9 * G.water_scale(cin, out, 2)), (igstep, r)
+        t0 = cin.tl.copy()
+        G.apply_ptend(cin, G.ptend(out, 2), desc.dt_gl)
+        assert not np.array_equal(t0, cin.tl)
+        assert np.all(cin.ql >= 0)

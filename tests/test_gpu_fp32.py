@@ -55,3 +55,48 @@ def test_fp32_mixed_workload1(gpu_lib):
     print('fp32-mixed rel-L2 vs fp64 oracle (64x58):', e)
     for n, b in BOUNDS.items():
         assert e[n] <= b, (n, e[n], b)
+
+
+def test_fp32_mixed_mean_state_acceleration(gpu_lib):
+    def wl(**kw):
+        cfg, cin, st, rad, desc = S.workload0(**kw)
+        cfg = T.CrmConfig(**{**cfg.__dict__, 'use_crm_accel': 1, 'crm_accel_factor': 2.0})
+        return cfg, cin, st, rad, desc
+    e = _errors(wl, ncrms=4, moist=True)
+    print('fp32-mixed rel-L2 vs fp64 oracle (32x28, accelerated):', e)
+    for n, b in BOUNDS.items():
+        assert e[n] <= b, (n, e[n], b)
+
+
+def test_fp32_mixed_water_budget(gpu_lib):
+    """Column water change = large-scale forcing - surface precipitation: the
+    FP64 oracle closes it to ~1e-16 relative; the FP32-mixed form (state kept
+    in FP32) to the FP32 rounding of the column water."""
+    from test_oracle import water_residual
+    cfg, cin, st, rad, desc = S.workload1(ncrms=4, moist=True)
+    cfg.precision = T.CRM_FP32_MIXED
+    cfg.max_ncrms = 4
+    ctx = CrmContext(cfg)
+    out = T.CrmOutput(4, cfg.crm_nx, 1, cfg.crm_nz, cfg.plev)
+    st1 = st.copy()
+    ctx.run(desc, cin, st1, rad.copy(), out, raise_on_error=True)
+    r = water_residual(cfg, cin, st, st1, out, desc.dt_gl)
+    print('fp32-mixed column water residual (relative):', r)
+    assert np.max(np.abs(r)) < 1e-5, r
+
+
+def test_fp32_mixed_gcm_water_identity(gpu_lib):
+    """The GCM-side identity of check_energy_chng (column water tendency +
+    surface precipitation + CRM precipitation storage = 0) for the FP32-mixed
+    form: its tendencies are FP64 sums of FP32 fields, so the identity holds
+    to the FP32 rounding of the CRM state."""
+    from crm_gb300 import gcm_coupling as G
+    cfg, cin, st, rad, desc = S.workload1(ncrms=4, moist=True)
+    cfg.precision = T.CRM_FP32_MIXED
+    cfg.max_ncrms = 4
+    ctx = CrmContext(cfg)
+    out = T.CrmOutput(4, cfg.crm_nx, 1, cfg.crm_nz, cfg.plev)
+    ctx.run(desc, cin, st.copy(), rad.copy(), out, raise_on_error=True)
+    r = G.water_residual(cin, out, 4) / G.water_scale(cin, out, 4)
+    print('fp32-mixed GCM water identity residual (relative):', r)
+    assert np.max(np.abs(r)) < 1e-4, r

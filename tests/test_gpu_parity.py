@@ -19,7 +19,7 @@ _ctx = {}
 
 
 def _context(cfg):
-    key = (cfg.crm_nx, cfg.crm_nz, cfg.plev, cfg.crm_dx, cfg.crm_dt, cfg.precision, cfg.max_ncrms)
+    key = tuple(sorted(cfg.__dict__.items()))
     if key not in _ctx:
         _ctx[key] = CrmContext(cfg)
     return _ctx[key]
@@ -179,3 +179,26 @@ def test_col_map_matches_oracle(gpu_lib):
     a, b = run_both(cfg, cin, st, rad, d)
     assert mismatches(a, b) == []
     assert np.array_equal(b[0].temperature[[1, 2]], st.temperature[[1, 2]])
+
+
+def _accel(cfg, factor=2.0, uv=0):
+    return T.CrmConfig(**{**cfg.__dict__, 'use_crm_accel': 1, 'crm_accel_factor': factor,
+                          'crm_accel_uv': uv})
+
+
+@pytest.mark.parametrize('uv', [0, 1])
+def test_fp64_bitexact_mean_state_acceleration(gpu_lib, uv):
+    """use_crm_accel with crm_accel_factor 2 (the sam1mom production default),
+    with and without crm_accel_uv."""
+    cfg, cin, st, rad, desc = S.workload0(ncrms=4, moist=True)
+    desc.dt_gl = 600.0
+    assert mismatches(*run_both(_accel(cfg, 2.0, uv), cin, st, rad, desc)) == []
+
+
+def test_fp64_bitexact_acceleration_cease(gpu_lib):
+    """A column heated ~10 K per step stops accelerating (nstop stretched);
+    its batch mate keeps accelerating."""
+    cfg, cin, st, rad, desc = S.workload1(ncrms=2, moist=True)
+    desc.dt_gl = 300.0
+    rad.qrad[1, :, :, 5:8] = 1.0
+    assert mismatches(*run_both(_accel(cfg, 2.0), cin, st, rad, desc)) == []

@@ -79,3 +79,33 @@ def test_serving_step_equals_crm_run(gpu_lib):
     assert not status.any()
     for n, v in vals.items():
         assert np.array_equal(v, getattr(out, n)), n
+
+
+def test_checkpoint_and_restore_chunk(gpu_lib, tmp_path):
+    """Two steps in one server == one step, checkpoint, a new server restored
+    from the file, second step."""
+    from crm_gb300.serving import CrmServer, apply_tendencies
+    cfg = _configs()[0]
+    cin, st, rad, gcol = _chunk(cfg, 4, 21, seed=5)
+    server = CrmServer([cfg], capacity=32)
+    ref = _drive(server, cfg, (cin, st, rad, gcol), 2)
+    server.close()
+
+    server = CrmServer([cfg], capacity=32)
+    cin1 = cin.copy()
+    ch = server.open_chunk(cfg, cin1, st, rad, gcol)
+    vals, status = server.step(ch, cin1, DT_GL).result(timeout=120)
+    assert not status.any()
+    apply_tendencies(cin1, vals, DT_GL)
+    p = str(tmp_path / 'chunk.ckpt')
+    server.checkpoint_chunk(ch, p)
+    server.close_chunk(ch)
+    server.close()
+
+    server = CrmServer([cfg], capacity=32)
+    ch = server.restore_chunk(p, cin1)
+    vals2, status = server.step(ch, cin1, DT_GL).result(timeout=120)
+    server.close()
+    assert not status.any()
+    for n, v in ref[1].items():
+        assert np.array_equal(v, vals2[n]), n

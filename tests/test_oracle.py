@@ -178,3 +178,56 @@ def test_col_map_selects_slots():
         assert np.array_equal(getattr(a[2], n)[untouched], getattr(st, n)[untouched]), n
     for n, v in b[4].arrays().items():
         assert np.array_equal(getattr(a[4], n)[slots], v), n
+
+
+def _accel(cfg, factor=2.0, uv=0):
+    return T.CrmConfig(**{**cfg.__dict__, 'use_crm_accel': 1, 'crm_accel_factor': factor,
+                          'crm_accel_uv': uv})
+
+
+def test_accel_requires_dividing_factor():
+    cfg, cin, st, rad, desc = S.workload0(ncrms=2)
+    desc.dt_gl = 200.0                       # nstop 10: 1 + 2 does not divide it
+    rc, _, _ = oracle.run(_accel(cfg, 2.0), desc, cin, st.copy(), rad.copy())
+    assert rc == T.CRM_ERR_ARG
+    rc, _, _ = oracle.run(_accel(cfg, 1.0), desc, cin, st.copy(), rad.copy())
+    assert rc == 0
+
+
+@pytest.mark.parametrize('uv', [0, 1])
+def test_accel_changes_mean_state_and_matches_batch_mode(uv):
+    cfg, cin, st, rad, desc = S.workload0(ncrms=3, moist=True)
+    desc.dt_gl = 600.0                       # 30 steps -> 10 accelerated steps
+    plain = _run(cfg, cin, st, rad, desc)
+    acc = _run(_accel(cfg, 2.0, uv), cin, st, rad, desc)
+    assert acc[0] == 0
+    for n, v in acc[2].arrays().items():
+        assert np.all(np.isfinite(v)), n
+    assert not np.array_equal(acc[2].temperature, plain[2].temperature)
+    bcfg = _accel(S.config0(batch_mode=T.CRM_REFERENCE_BATCH), 2.0, uv)
+    batch = _run(bcfg, cin, st, rad, desc)
+    assert batch[0] == 0
+    assert not _equal(acc[2:], batch[2:])
+
+
+def test_accel_ceases_on_large_mean_temperature_change():
+    """A column heated by ~10 K per step trips the 5 K limit: acceleration
+    stops and the remaining steps run unaccelerated (nstop stretched)."""
+    cfg, cin, st, rad, desc = S.workload0(ncrms=2)
+    desc.dt_gl = 600.0
+    rad_hot = rad.copy()
+    rad_hot.qrad[1, :, :, 5:8] = 0.5         # K/s in column 1 only
+    acc = _run(_accel(cfg, 2.0), cin, st, rad_hot, desc)
+    assert acc[0] == 0
+    # column 0 is unaffected by column 1's cease (per-column mode)
+    alone = _run(_accel(cfg, 2.0), cin.take([0]), st.take([0]), rad_hot.take([0]),
+                 T.call_desc(1, 1, 600.0, desc.igstep, np.asarray(desc._keep)[[0]]))
+    for n, v in alone[2].arrays().items():
+        assert np.array_equal(v[0], getattr(acc[2], n)[0]), n
+    # column 1 ceases at its first step, before any acceleration is applied,
+    # and its nstop grows from 10 to 10 + 10 * 2 = 30: exactly the plain run
+    plain = _run(cfg, cin, st, rad_hot, desc)
+    for n, v in plain[2].arrays().items():
+        assert np.array_equal(v[1], getattr(acc[2], n)[1]), n
+    for n, v in plain[4].arrays().items():
+        assert np.array_equal(v[1], getattr(acc[4], n)[1]), n
