@@ -15,6 +15,6 @@
 #endif
 
 namespace crm {
-template void launch_crm_columns<CRM_INST_T, CRM_INST_NX, CRM_INST_SHAPE>(const KParams &, int, cudaStream_t);
+template void launch_crm_columns<CRM_INST_T, CRM_INST_NX, CRM_INST_SHAPE>(const KParams &, int, cudaStream_t, bool);
 template int occupancy_crm_columns<CRM_INST_T, CRM_INST_NX, CRM_INST_SHAPE>(int, int);
 }  // namespace crm

@@ -47,6 +47,7 @@ struct crm_ctx {
   double *d_colconst = nullptr;  // z0 (ncrms), rnd (ncrms * 5 * nx)
   int *d_status = nullptr;
   unsigned long long *d_phase = nullptr;   // per-CTA phase cycle counters
+  unsigned long long *d_gsync = nullptr;   // batch-mode grid barrier + maxima
   int ld_cap = 0;
   // host-side constants
   std::vector<double> trigs, eign;
@@ -70,13 +71,12 @@ struct PrepParams {
 void launch_crm_prep(const PrepParams &p, cudaStream_t s);
 
 template <typename T, int NX>
-static void launch_tn(int shape, const KParams &p, int grid, cudaStream_t s) {
+static void launch_tn(int shape, const KParams &p, int grid, cudaStream_t s, bool coop) {
   switch (shape) {
-    case 0: launch_crm_columns<T, NX, 0>(p, grid, s); break;
-    case 1: launch_crm_columns<T, NX, 1>(p, grid, s); break;
-    case 2: launch_crm_columns<T, NX, 2>(p, grid, s); break;
-    case 3: launch_crm_columns<T, NX, 3>(p, grid, s); break;
-    default: launch_crm_columns<T, NX, 4>(p, grid, s); break;
+    case 0: launch_crm_columns<T, NX, 0>(p, grid, s, coop); break;
+    case 1: launch_crm_columns<T, NX, 1>(p, grid, s, coop); break;
+    case 2: launch_crm_columns<T, NX, 2>(p, grid, s, coop); break;
+    default: launch_crm_columns<T, NX, 3>(p, grid, s, coop); break;
   }
 }
 
@@ -86,18 +86,17 @@ static int occupancy_tn(int shape, int nx, int nzm) {
     case 0: return occupancy_crm_columns<T, NX, 0>(nx, nzm);
     case 1: return occupancy_crm_columns<T, NX, 1>(nx, nzm);
     case 2: return occupancy_crm_columns<T, NX, 2>(nx, nzm);
-    case 3: return occupancy_crm_columns<T, NX, 3>(nx, nzm);
-    default: return occupancy_crm_columns<T, NX, 4>(nx, nzm);
+    default: return occupancy_crm_columns<T, NX, 3>(nx, nzm);
   }
 }
 
 template <typename T>
-static void launch_t(int shape, const KParams &p, int grid, cudaStream_t s) {
+static void launch_t(int shape, const KParams &p, int grid, cudaStream_t s, bool coop) {
   switch (p.L.nx) {
-    case 32: launch_tn<T, 32>(shape, p, grid, s); break;
-    case 64: launch_tn<T, 64>(shape, p, grid, s); break;
-    case 128: launch_tn<T, 128>(shape, p, grid, s); break;
-    default: launch_tn<T, 0>(shape, p, grid, s); break;
+    case 32: launch_tn<T, 32>(shape, p, grid, s, coop); break;
+    case 64: launch_tn<T, 64>(shape, p, grid, s, coop); break;
+    case 128: launch_tn<T, 128>(shape, p, grid, s, coop); break;
+    default: launch_tn<T, 0>(shape, p, grid, s, coop); break;
   }
 }
 
@@ -111,9 +110,9 @@ static int occupancy_t(int shape, int nx, int nzm) {
   }
 }
 
-void launch_columns(int precision, int shape, const KParams &p, int grid, cudaStream_t s) {
-  if (precision == CRM_FP64) launch_t<double>(shape, p, grid, s);
-  else launch_t<float>(shape, p, grid, s);
+void launch_columns(int precision, int shape, const KParams &p, int grid, cudaStream_t s, bool coop) {
+  if (precision == CRM_FP64) launch_t<double>(shape, p, grid, s, coop);
+  else launch_t<float>(shape, p, grid, s, coop);
 }
 
 int occupancy_columns(int precision, int shape, int nx, int nzm) {
@@ -191,12 +190,16 @@ int default_shape(int precision, int nx) {
     int v = atoi(e);
     if (v >= 0 && v < crm::kNumShapes) return v;
   }
-  // measured on 1024 columns of nx x 58: FP64 best at 256 threads, 3 CTAs/SM;
-  // FP32-mixed at 256 threads, 4 CTAs/SM, with scratch planes A/B in shared
-  // memory for nx <= 32 (+5 %) but not for nx = 64 (-7 %: the planes cost
-  // more L1 than they save)
-  if (precision == CRM_FP64) return 1;
-  return nx <= 32 ? 3 : 2;
+  // measured on 1024 columns of nx x 58 (column-steps/s):
+  //   FP64: 256 threads at 3 CTAs/SM (69K at nx 64; 2, 4 CTAs/SM and 512
+  //     threads are 1-12 % slower);
+  //   FP32-mixed: 256 threads at 4 CTAs/SM (362K at nx 64), with scratch
+  //     planes A/B in shared memory for nx <= 32 (+5 %; -7 % at nx 64, where
+  //     the planes cost more L1 than they save), 512 threads at 2 CTAs/SM
+  //     for nx >= 128 (+7 %).
+  if (precision == CRM_FP64) return 0;
+  if (nx <= 32) return 2;
+  return nx >= 128 ? 3 : 1;
 }
 
 // crm_accel_nstop (accelerate_crm.F90:84-106): nstop / (1 + crm_accel_factor),
@@ -211,7 +214,7 @@ int validate(const crm_config *c) {
   if (!c) return CRM_ERR_ARG;
   if (c->crm_ny != 1) return CRM_ERR_UNSUPPORTED;          // 3D not built
   if (c->microphysics != CRM_MICRO_SAM1MOM) return CRM_ERR_UNSUPPORTED;
-  if (c->batch_mode != CRM_PER_COLUMN) return CRM_ERR_UNSUPPORTED;
+  if (c->batch_mode != CRM_PER_COLUMN && c->batch_mode != CRM_REFERENCE_BATCH) return CRM_ERR_ARG;
   if (c->precision != CRM_FP64 && c->precision != CRM_FP32_MIXED) return CRM_ERR_ARG;
   if (c->crm_nx < 8 || c->crm_nx % 2 || c->crm_nz < 4 || c->plev < c->crm_nz + 2) return CRM_ERR_ARG;
   if (c->crm_nx_rad < 1 || c->crm_nx % c->crm_nx_rad || c->crm_ny_rad != 1) return CRM_ERR_ARG;
@@ -271,6 +274,8 @@ int alloc_ctx(crm_ctx *c) {
   CK(cudaMemcpy(c->d_consts + c->trigs.size(), c->eign.data(), sizeof(double) * c->eign.size(), cudaMemcpyHostToDevice));
   CK(cudaMalloc(&c->d_colconst, sizeof(double) * (size_t)ld * (1 + 5 * nx)));
   CK(cudaMalloc(&c->d_status, sizeof(int) * (size_t)ld));
+  CK(cudaMalloc(&c->d_gsync, 8 * sizeof(unsigned long long)));
+  CK(cudaMemset(c->d_gsync, 0, 8 * sizeof(unsigned long long)));
 #ifdef CRM_PHASE_TIMERS
   CK(cudaMalloc(&c->d_phase, sizeof(unsigned long long) * 64 * (size_t)c->grid_max));
   CK(cudaMemset(c->d_phase, 0, sizeof(unsigned long long) * 64 * (size_t)c->grid_max));
@@ -304,6 +309,7 @@ void free_ctx(crm_ctx *c) {
   cudaFree(c->slabs); cudaFree(c->d_in); cudaFree(c->d_state); cudaFree(c->d_rad);
   cudaFree(c->d_out); cudaFree(c->d_consts); cudaFree(c->d_colconst); cudaFree(c->d_status);
   if (c->d_phase) cudaFree(c->d_phase);
+  if (c->d_gsync) cudaFree(c->d_gsync);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -374,10 +380,16 @@ int enqueue(crm_ctx *c, const crm_call_desc *d, const crm_input_c *in, crm_state
   p.col_map = d->col_map;
   p.phase_cycles = c->d_phase;
   p.col_status = d_status ? d_status : c->d_status;
+  const bool batch = g.batch_mode == CRM_REFERENCE_BATCH;
+  // reference-batch mode: one co-resident CTA per column (cooperative
+  // launch), so the batch must fit the GPU at once and slots are 0..ncrms-1
+  if (batch && (ncrms > c->grid_max || d->col_map)) return CRM_ERR_UNSUPPORTED;
+  p.gsync = c->d_gsync;
   int grid = ncrms < c->grid_max ? ncrms : c->grid_max;
   CK(cudaEventRecord(c->ev0, s));
+  if (batch) CK(cudaMemsetAsync(c->d_gsync, 0, 8 * sizeof(unsigned long long), s));
   crm::launch_crm_prep(pp, s);
-  crm::launch_columns(g.precision, c->shape, p, grid, s);
+  crm::launch_columns(g.precision, c->shape, p, grid, s, batch);
   CK(cudaGetLastError());
   CK(cudaEventRecord(c->ev1, s));
   c->last_launches = 2;
@@ -666,6 +678,7 @@ extern "C" int crm_run_device_noalloc(const crm_config *cfg, const crm_call_desc
   int rc = validate(&g);
   if (rc != CRM_OK) return rc;
   if (!d || d->ncrms < 1 || d->ld < d->ncrms || !(d->dt_gl > 0) || d->col_map) return CRM_ERR_ARG;
+  if (g.batch_mode != CRM_PER_COLUMN) return CRM_ERR_UNSUPPORTED;
   const int ncrms = d->ncrms, nx = g.crm_nx;
   NoallocPlan q;
   rc = noalloc_plan(g, ncrms, q);

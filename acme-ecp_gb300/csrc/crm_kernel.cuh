@@ -85,6 +85,7 @@ struct ColShared {
   double cltot, clhgh, clmed, cllow;
   int jt_min, mx_max;
   int nstop, ceaseflag, acc_flag;   // per-column step count (acceleration)
+  int gbar;                         // grid barriers passed (batch mode)
   unsigned long long t_last;
   double red_d[32];
   int red_i[64];
@@ -232,6 +233,55 @@ struct ColumnKernel : NxDim<NX> {
       for (int o = 16; o > 0; o >>= 1) m = mx2(m, __shfl_xor_sync(0xffffffffu, m, o));
       if (lane == 0) out(q, k, m);
     }
+  }
+
+  // ---------------------------------------------------------- batch coupling
+  // Reference-batch mode (crm_batch_mode CRM_REFERENCE_BATCH): the column
+  // kernel is a cooperative launch with one co-resident CTA per column, and
+  // the reference's batch-wide decisions (ncycle from the largest CFL,
+  // kurant.F90:54-64; nprec, microphysics.F90:602-661; the acceleration
+  // cease flag) take the maximum over all CTAs through a grid barrier.
+  // Sense-reversing barrier by thread 0; every wait is bounded (~4 s): on
+  // timeout the column records CRM_ERR_TIMEOUT and stops.
+  __device__ bool grid_barrier() {
+    unsigned int *count = reinterpret_cast<unsigned int *>(p.gsync);
+    volatile unsigned int *gen = count + 1;
+    __threadfence();
+    const unsigned int g = *gen;
+    if (atomicAdd(count, 1u) == gridDim.x - 1) {
+      atomicExch(count, 0u);
+      __threadfence();
+      atomicAdd(const_cast<unsigned int *>(gen), 1u);
+      return true;
+    }
+    for (long long it = 0; it < (1ll << 24); ++it) {
+      if (*gen != g) {
+        __threadfence();
+        return true;
+      }
+      __nanosleep(256);
+    }
+    return false;
+  }
+  // max over the columns of the call of v >= 0 (per-column mode: v itself);
+  // called by the whole CTA with the same v
+  __device__ double batch_max(double v) {
+    if (p.batch_mode != CRM_REFERENCE_BATCH) return v;
+    SYNC;
+    if (TID == 0) {
+      unsigned long long *slot = p.gsync + 2 + (S.gbar & 3);
+      atomicMax(slot, (unsigned long long)__double_as_longlong(v));
+      bool ok = grid_barrier();
+      double m = __longlong_as_double((long long)atomicAdd(slot, 0ull));
+      if (blockIdx.x == 0) atomicExch(p.gsync + 2 + ((S.gbar + 2) & 3), 0ull);
+      S.gbar = S.gbar + 1;
+      if (!ok) S.status = CRM_ERR_TIMEOUT;
+      S.red_d[0] = ok ? m : v;
+    }
+    SYNC;
+    double r = S.red_d[0];
+    SYNC;
+    return r;
   }
 
   __device__ double block_max(double v) {
@@ -437,8 +487,14 @@ struct ColumnKernel : NxDim<NX> {
     // state in (crm_module.F90:380-397) and the first-step clamp (:400-417)
     F2<T> u = U(), v = V(), w = W(), tabs = TABS(), qt = QT(), qp = QP(), qn = QN();
     bool clamp;
-    if (p.batch_mode == CRM_REFERENCE_BATCH) clamp = p.clamp_batch != 0;
-    else clamp = (p.st[0][S4(1, 1)] == p.st[0][S4(2, 1)]) && (p.st[0][S4(3, 2)] == p.st[0][S4(4, 2)]);
+    if (p.batch_mode == CRM_REFERENCE_BATCH) {
+      // the reference tests the first column of the batch only: its input
+      // state is untouched until every column has passed the first barrier
+      auto U0 = [&](int i, int k) { return p.st[0][(size_t)p.ld * ((i - 1) + (size_t)nx * (k - 1))]; };
+      clamp = (U0(1, 1) == U0(2, 1)) && (U0(3, 2) == U0(4, 2));
+    } else {
+      clamp = (p.st[0][S4(1, 1)] == p.st[0][S4(2, 1)]) && (p.st[0][S4(3, 2)] == p.st[0][S4(4, 2)]);
+    }
     const double umax = (double)(0.5f * (float)p.dx / (float)p.dt);
     for (int e = TID; e < nx * nzm; e += NT) {
       int i = 1 + e % nx, k = 1 + e / nx;
@@ -576,9 +632,10 @@ struct ColumnKernel : NxDim<NX> {
       cfl = mx2(cfl, mx2(t1, t2));
     }
     cfl = block_max(cfl);
+    const double cfl_b = batch_max(cfl);
     if (TID == 0) {
       S.cfl = cfl;
-      int n = (int)ceil(cfl / R4(0.7));
+      int n = (int)ceil(cfl_b / R4(0.7));
       S.ncycle = n > 1 ? n : 1;
     }
     SYNC;
@@ -1488,9 +1545,10 @@ struct ColumnKernel : NxDim<NX> {
       wp(i, k) = -wv * rhow[k] * dtn / dz;
     }
     double cfl = block_max((double)cflt);
+    const double cfl_b = batch_max(cfl);
     if (TID == 0) {
       S.prec_cfl = cfl;
-      S.nprec = (cfl > R4(0.9)) ? (int)ceil(cfl / R4(0.9)) : 1;
+      S.nprec = (cfl_b > R4(0.9)) ? (int)ceil(cfl_b / R4(0.9)) : 1;
     }
     SYNC;
   }
@@ -1869,7 +1927,8 @@ struct ColumnKernel : NxDim<NX> {
                  if (q == 0 && fabs(d) > 5.) S.acc_flag = 1;
                });
     SYNC;
-    if (S.acc_flag) {
+    const bool cease = batch_max(S.acc_flag ? 1.0 : 0.0) > 0.0;   // one flag per batch
+    if (cease) {
       if (TID == 0) {
         S.ceaseflag = 1;
         S.nstop = (int)((double)S.nstop + (double)(S.nstop - nstep + 1) * p.accel_factor);
@@ -2289,8 +2348,8 @@ struct ColumnKernel : NxDim<NX> {
     for (int nstep = 1; nstep <= S.nstop; ++nstep) {
       kurant();
       PHASE_MARK(PH_KURANT);
-      if (S.ncycle > 16) {
-        if (TID == 0) S.status = CRM_ERR_CFL;
+      if (S.ncycle > 16 || S.status != CRM_OK) {
+        if (TID == 0 && S.status == CRM_OK) S.status = CRM_ERR_CFL;
         SYNC;
         break;
       }
@@ -2386,6 +2445,7 @@ __global__ void __launch_bounds__(NTH, MINB) crm_columns_kernel(const __grid_con
   T *planes = nullptr;
   if (SMP) planes = fsh + crm_round64((size_t)(p.L.nx + 2) * p.L.nzm + (size_t)(NTH / 32) * (p.L.nx + 4));
   T *base = reinterpret_cast<T *>(p.slabs) + (size_t)blockIdx.x * p.L.slab;
+  if (threadIdx.x == 0) S.gbar = 0;
   for (int col = blockIdx.x; col < p.ncrms; col += gridDim.x) {
     ColumnKernel<T, NX> K(p, S, base, col, planes);
     K.run(fsh, wsh);
@@ -2394,11 +2454,20 @@ __global__ void __launch_bounds__(NTH, MINB) crm_columns_kernel(const __grid_con
 }
 
 template <typename T, int NX, int SHAPE>
-void launch_crm_columns(const KParams &p, int grid, cudaStream_t s) {
+void launch_crm_columns(const KParams &p, int grid, cudaStream_t s, bool cooperative) {
   constexpr int nth = kShapes[SHAPE].threads, minb = kShapes[SHAPE].min_ctas, smp = kShapes[SHAPE].smem_planes;
   size_t smem = crm_smem_bytes<T>(p.L.nx, p.L.nzm, nth, smp);
-  cudaFuncSetAttribute(crm_columns_kernel<T, NX, nth, minb, smp>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  crm_columns_kernel<T, NX, nth, minb, smp><<<grid, nth, smem, s>>>(p);
+  auto kern = crm_columns_kernel<T, NX, nth, minb, smp>;
+  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (cooperative) {
+    // every CTA co-resident (the batch-mode grid barrier relies on it); the
+    // launch fails rather than over-subscribe
+    KParams q = p;
+    void *args[] = {&q};
+    cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(kern), dim3(grid), dim3(nth), args, smem, s);
+  } else {
+    kern<<<grid, nth, smem, s>>>(p);
+  }
 }
 
 template <typename T, int NX, int SHAPE>

@@ -32,6 +32,10 @@ struct KParams {
   void *slabs;              // gridDim.x slabs of L.slab elements of T
   int *col_status;          // (ncrms)
   const int *col_map;       // optional (ncrms) slots: column c uses slot col_map[c]
+  // reference-batch mode: grid barrier state [count, generation] (u32 x 2,
+  // in gsync[0]) and a ring of four batch maxima gsync[2..5] (zeroed by the
+  // host before the launch); all columns are co-resident CTAs
+  unsigned long long *gsync;
   unsigned long long *phase_cycles;  // (gridDim.x, 64) when built with CRM_PHASE_TIMERS
 };
 
@@ -52,8 +56,8 @@ struct KShape {
   int threads, min_ctas;
   int smem_planes;   // scratch planes A and B in shared memory (0 or 2)
 };
-constexpr int kNumShapes = 5;
-constexpr KShape kShapes[kNumShapes] = {{256, 2, 0}, {256, 3, 0}, {256, 4, 0}, {256, 4, 2}, {256, 3, 2}};
+constexpr int kNumShapes = 4;
+constexpr KShape kShapes[kNumShapes] = {{256, 3, 0}, {256, 4, 0}, {256, 4, 2}, {512, 2, 0}};
 
 // Horizontal sizes with a kernel specialised at compile time (the reference
 // fixes CRM_NX at build time too); any other power of two runs the generic
@@ -63,12 +67,13 @@ constexpr int kNxBuilt[kNumNx] = {32, 64, 128, 0};
 
 // One instantiation per (T, NX, shape) lives in its own object (crm_columns.cu).
 template <typename T, int NX, int SHAPE>
-void launch_crm_columns(const KParams &p, int grid, cudaStream_t s);
+void launch_crm_columns(const KParams &p, int grid, cudaStream_t s, bool cooperative);
 template <typename T, int NX, int SHAPE>
 int occupancy_crm_columns(int nx, int nzm);
 
 // Dispatch on (precision, nx, shape) at run time.
-void launch_columns(int precision, int shape, const KParams &p, int grid, cudaStream_t s);
+void launch_columns(int precision, int shape, const KParams &p, int grid, cudaStream_t s,
+                    bool cooperative = false);
 int occupancy_columns(int precision, int shape, int nx, int nzm);
 
 }  // namespace crm

@@ -52,9 +52,12 @@ enum crm_microphysics { CRM_MICRO_SAM1MOM = 0, CRM_MICRO_M2005 = 1 };
 enum crm_precision { CRM_FP64 = 0, CRM_FP32_MIXED = 1 };
 /* Subcycle count ncycle (kurant.F90:54-64) and precipitation sub-steps nprec
  * (MICRO_SAM1MOM/microphysics.F90:602-661) are batch maxima in the
- * reference, and the first-step velocity clamp tests only the first column
- * (crm_module.F90:400-417).  CRM_PER_COLUMN makes each column independent of
- * its batch-mates; CRM_REFERENCE_BATCH reproduces the batch coupling. */
+ * reference, the first-step velocity clamp tests only the first column
+ * (crm_module.F90:400-417) and the acceleration cease flag is batch-wide
+ * (accelerate_crm.F90:236).  CRM_PER_COLUMN makes each column independent of
+ * its batch-mates; CRM_REFERENCE_BATCH reproduces the batch coupling: all
+ * columns of the call run at once (ncrms at most the GPU's co-resident
+ * columns, no col_map; else CRM_ERR_UNSUPPORTED). */
 enum crm_batch_mode { CRM_PER_COLUMN = 0, CRM_REFERENCE_BATCH = 1 };
 
 /* Compile-time CPP constants of the reference (bld/configure:1883-1914,

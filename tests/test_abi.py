@@ -75,8 +75,7 @@ def test_invalid_configurations_are_rejected(lib):
         h = lib.crm_create(C.byref(cfg.to_c()), C.byref(st))
         assert not h
         assert st.value in (T.CRM_ERR_ARG, T.CRM_ERR_UNSUPPORTED), kw
-    for kw in ({'crm_ny': 4}, {'microphysics': T.CRM_MICRO_M2005},
-               {'batch_mode': T.CRM_REFERENCE_BATCH}):
+    for kw in ({'crm_ny': 4}, {'microphysics': T.CRM_MICRO_M2005}):
         cfg = S.config0()
         cfg.max_ncrms = 4
         for k, v in kw.items():

@@ -202,3 +202,29 @@ def test_fp64_bitexact_acceleration_cease(gpu_lib):
     desc.dt_gl = 300.0
     rad.qrad[1, :, :, 5:8] = 1.0
     assert mismatches(*run_both(_accel(cfg, 2.0), cin, st, rad, desc)) == []
+
+
+def test_fp64_bitexact_reference_batch_mode(gpu_lib):
+    """CRM_REFERENCE_BATCH on the GPU (one cooperative launch, grid-wide
+    maxima): one column strong enough to need sub-cycling sets ncycle for the
+    whole batch, bit for bit as the oracle's batch mode does."""
+    cfg, cin, st, rad, desc = S.workload0(ncrms=4, moist=True)
+    desc.dt_gl = 400.0
+    st.w_wind[2, :, :, 10] = 40.0
+    bcfg = S.config0(batch_mode=T.CRM_REFERENCE_BATCH)
+    a, b = run_both(bcfg, cin, st, rad, desc)
+    assert mismatches(a, b) == []
+    # the coupling is real: per-column mode gives the other columns other bits
+    pc, _ = run_both(cfg, cin, st, rad, desc)
+    assert not np.array_equal(pc[0].temperature[0], a[0].temperature[0])
+    assert np.array_equal(pc[0].temperature[2], a[0].temperature[2])
+
+
+def test_fp64_bitexact_reference_batch_acceleration_cease(gpu_lib):
+    """Batch mode with mean-state acceleration: one hot column stops the
+    acceleration of every column (one cease flag per batch)."""
+    cfg, cin, st, rad, desc = S.workload0(ncrms=3)
+    desc.dt_gl = 600.0
+    rad.qrad[1, :, :, 5:8] = 0.5
+    bcfg = _accel(S.config0(batch_mode=T.CRM_REFERENCE_BATCH), 2.0)
+    assert mismatches(*run_both(bcfg, cin, st, rad, desc)) == []
