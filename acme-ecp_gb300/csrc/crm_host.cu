@@ -269,9 +269,16 @@ int alloc_ctx(crm_ctx *c) {
       c->eign[i - 1] = (2.0 * cos(factx * xnx * xi) - 2.0) * ddx2 + (2.0 * cos(facty * xny * xj) - 2.0) * ddy2;
     }
   }
-  CK(cudaMalloc(&c->d_consts, sizeof(double) * (c->trigs.size() + c->eign.size())));
-  CK(cudaMemcpy(c->d_consts, c->trigs.data(), sizeof(double) * c->trigs.size(), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(c->d_consts + c->trigs.size(), c->eign.data(), sizeof(double) * c->eign.size(), cudaMemcpyHostToDevice));
+  // trigs, eign (FP64), then trigs again as float (exact: REAL*4 values)
+  const size_t nt = c->trigs.size(), ne = c->eign.size(), ntf = (nt + 1) / 2;
+  CK(cudaMalloc(&c->d_consts, sizeof(double) * (nt + ne + ntf)));
+  CK(cudaMemcpy(c->d_consts, c->trigs.data(), sizeof(double) * nt, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(c->d_consts + nt, c->eign.data(), sizeof(double) * ne, cudaMemcpyHostToDevice));
+  {
+    std::vector<float> tf(nt);
+    for (size_t i = 0; i < nt; ++i) tf[i] = (float)c->trigs[i];
+    CK(cudaMemcpy(c->d_consts + nt + ne, tf.data(), sizeof(float) * nt, cudaMemcpyHostToDevice));
+  }
   CK(cudaMalloc(&c->d_colconst, sizeof(double) * (size_t)ld * (1 + 5 * nx)));
   CK(cudaMalloc(&c->d_status, sizeof(int) * (size_t)ld));
   CK(cudaMalloc(&c->d_gsync, 8 * sizeof(unsigned long long)));
@@ -367,6 +374,7 @@ int enqueue(crm_ctx *c, const crm_call_desc *d, const crm_input_c *in, crm_state
   for (int k = 0; k <= c->ifax[0] && k < 8; ++k) p.ifax[k] = c->ifax[k];
   p.trigs = c->d_consts;
   p.eign = c->d_consts + c->trigs.size();
+  p.trigs_f = reinterpret_cast<const float *>(c->d_consts + c->trigs.size() + c->eign.size());
   p.z0 = pp.z0;
   p.rnd = pp.rnd;
   p.zmid = in->zmid; p.zint = in->zint; p.tl = in->tl; p.ql = in->ql; p.qccl = in->qccl;
@@ -635,7 +643,7 @@ int noalloc_plan(const crm_config &g, int ncrms, NoallocPlan &q) {
   q.L = crm::make_layout(g.crm_nx, g.crm_nz, g.plev, g.crm_nx_rad, (int)q.esz);
   q.ntrigs = 3 * g.crm_nx / 2 + 2 + g.crm_nx;
   q.neign = g.crm_nx + 1;
-  q.const_bytes = round256(sizeof(double) * (size_t)(q.ntrigs + q.neign));
+  q.const_bytes = round256(sizeof(double) * (size_t)(q.ntrigs + q.neign) + sizeof(float) * (size_t)q.ntrigs);
   q.col_bytes = round256(sizeof(double) * (size_t)ncrms * (1 + 5 * (size_t)g.crm_nx));
   q.slab_bytes = round256(q.L.slab * q.esz);
   const size_t cap = CRM_NOALLOC_SCRATCH_BYTES;
@@ -715,7 +723,7 @@ extern "C" int crm_run_device_noalloc(const crm_config *cfg, const crm_call_desc
   if (grid > q.nslab) grid = q.nslab;
 
   // per-configuration constants (the same tables alloc_ctx builds), on the stack
-  double consts[kNoallocMaxTrigs + CRM_NOALLOC_MAX_NX + 1];
+  double consts[kNoallocMaxTrigs + CRM_NOALLOC_MAX_NX + 1 + (kNoallocMaxTrigs + 1) / 2];
   int ifax[20];
   fft_factors(ifax, nx);
   {
@@ -768,7 +776,12 @@ extern "C" int crm_run_device_noalloc(const crm_config *cfg, const crm_call_desc
   double *d_consts = reinterpret_cast<double *>(base);
   double *d_col = reinterpret_cast<double *>(base + q.const_bytes);
   void *d_slabs = base + q.const_bytes + q.col_bytes;
-  CK(cudaMemcpyAsync(d_consts, consts, sizeof(double) * (size_t)(q.ntrigs + q.neign), cudaMemcpyHostToDevice, s));
+  {
+    float *tf = reinterpret_cast<float *>(consts + q.ntrigs + q.neign);   // float copy of trigs
+    for (int i = 0; i < q.ntrigs; ++i) tf[i] = (float)consts[i];
+  }
+  CK(cudaMemcpyAsync(d_consts, consts, sizeof(double) * (size_t)(q.ntrigs + q.neign) + sizeof(float) * (size_t)q.ntrigs,
+                     cudaMemcpyHostToDevice, s));
 
   crm::PrepParams pp;
   pp.ncrms = ncrms; pp.ld = d->ld; pp.plev = g.plev; pp.nx = nx; pp.igstep = d->igstep;
@@ -799,6 +812,7 @@ extern "C" int crm_run_device_noalloc(const crm_config *cfg, const crm_call_desc
   p.nfax = ifax[0];
   for (int k = 0; k <= ifax[0] && k < 8; ++k) p.ifax[k] = ifax[k];
   p.trigs = d_consts;
+  p.trigs_f = reinterpret_cast<const float *>(d_consts + q.ntrigs + q.neign);
   p.eign = d_consts + q.ntrigs;
   p.z0 = pp.z0;
   p.rnd = pp.rnd;

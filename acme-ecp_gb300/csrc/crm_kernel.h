@@ -19,6 +19,7 @@ struct KParams {
   int nfax;
   int ifax[8];
   const double *trigs;      // fft trig table (3n/2 + 2 + n), REAL*4 values
+  const float *trigs_f;     // the same values as float (exact: they are REAL*4)
   const double *eign;       // (nx + 1) eigenvalues of the horizontal Laplacian
   const double *z0;         // (ncrms) roughness length
   const double *rnd;        // (ncrms, 5, nx) setperturb draws 1 - 2 r

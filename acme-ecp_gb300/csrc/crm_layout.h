@@ -50,6 +50,11 @@ enum Prof {
   P_UWLE, P_VWLE, P_UWSB, P_VWSB, P_PRECFLUX, P_QPFALL, P_TLAT, P_TLATQI, P_QIFALL,
   P_MKWLE0, P_MKWLE1, P_MKWSB0, P_MKWSB1, P_MKADV0, P_MKADV1, P_MKDIFF0, P_MKDIFF1,
   P_QPSRC, P_QPEVP,
+  // per-level reciprocals of the grid metrics, fixed for the call (the
+  // reference divides per cell or keeps such arrays per routine)
+  P_IADZ, P_IADZW, P_IRHO, P_IRHOADZ, P_IRHOWADZ, P_IRHOWADZW, P_RDZ, P_RDZW, P_MPDD,
+  P_RDXZ, P_RDXW, P_BETDZ, P_TKMAX,   // SGS closure per-level factors
+  P_BETU, P_BETD, P_RUP, P_RDN, P_RHOWDADZW,   // buoyancy, pressure RHS, diffusion
   P_TMP0, P_TMP1, P_TMP2, P_TMP3, P_TMP4, P_TMP5, P_TMP6, P_TMP7,
   P_COUNT
 };
