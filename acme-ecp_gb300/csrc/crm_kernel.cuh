@@ -220,6 +220,41 @@ struct ColumnKernel : NxDim<NX> {
     }
   }
 
+  // level_sums_lo for NQ quantities that share their loads: the FP64 form
+  // is level_sums with termq(q, i, k) (the reference's order, bit-exact);
+  // the FP32-mixed form gives one warp a whole level, termv(i, k, v) fills
+  // all NQ terms of a cell from one set of loads, and each quantity is
+  // reduced in FP32 (pairwise warp tree).
+  template <int NQ, typename TermQ, typename TermV, typename Init, typename Out>
+  __device__ void level_sums_lo_multi(int k0, int k1, TermQ termq, TermV termv, Init init, Out out) {
+    if constexpr (sizeof(T) == 8) {
+      level_sums(NQ, k0, k1, termq, init, out);
+    } else {
+      const int lane = TID & 31, warp = TID >> 5, nw = NT >> 5;
+      for (int k = k0 + warp; k <= k1; k += nw) {
+        T part[NQ];
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) part[q] = (T)0;
+        for (int i = 1 + lane; i <= nx; i += 32) {
+          T v[NQ];
+          termv(i, k, v);
+#pragma unroll
+          for (int q = 0; q < NQ; ++q) part[q] = part[q] + v[q];
+        }
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+          T x = part[q];
+          for (int o = 1; o < 32; o <<= 1) x = x + __shfl_xor_sync(0xffffffffu, x, o);
+          part[q] = x;
+        }
+        if (lane == 0) {
+#pragma unroll
+          for (int q = 0; q < NQ; ++q) out(q, k, (double)((T)init(q, k) + part[q]));
+        }
+      }
+    }
+  }
+
   // Horizontal maxima (order-independent, hence exact in both forms): one
   // warp per (q, k) with a shuffle tree.
   template <typename Term, typename Out>
@@ -484,6 +519,34 @@ struct ColumnKernel : NxDim<NX> {
       PR(P_RHOW)[nz] = (T)(2. * rhown - rhown1);
     }
     SYNC;
+    // per-level reciprocals used by the cell loops, evaluated exactly as the
+    // cell loops would (same operands and order), once per column
+    {
+      const T dzT = (T)S.dz;
+      T *adz = PR(P_ADZ), *adzw = PR(P_ADZW), *rho = PR(P_RHO), *rhow = PR(P_RHOW);
+      for (int k = TID + 1; k <= nz; k += NT) {
+        if (k <= nzm) {
+          const int kc = min(nzm, k + 1), kb = max(1, k - 1);
+          PR(P_IADZ)[k] = (T)1. / adz[k];
+          PR(P_IRHO)[k] = (T)1. / rho[k];
+          PR(P_IRHOADZ)[k] = (T)1. / (rho[k] * adz[k]);
+          PR(P_IRHOWADZ)[k] = (T)1. / (rhow[k] * adz[k]);
+          PR(P_RDZ)[k] = (T)1. / (dzT * adz[k]);
+          PR(P_MPDD)[k] = (T)(double)(2.f / (float)(kc - kb)) / adz[k];
+          if (k >= 2) {
+            PR(P_BETU)[k] = adz[k - 1] / (adz[k] + adz[k - 1]);
+            PR(P_BETD)[k] = adz[k] / (adz[k] + adz[k - 1]);
+          }
+          PR(P_RUP)[k] = rhow[k + 1] / rho[k] * PR(P_RDZ)[k];
+          PR(P_RDN)[k] = rhow[k] / rho[k] * PR(P_RDZ)[k];
+        }
+        PR(P_RHOWDADZW)[k] = rhow[k] / adzw[k];
+        PR(P_IADZW)[k] = (T)1. / adzw[k];
+        PR(P_IRHOWADZW)[k] = (T)1. / (rhow[k] * adzw[k]);
+        PR(P_RDZW)[k] = (T)1. / (dzT * adzw[k]);
+      }
+    }
+    SYNC;
     // state in (crm_module.F90:380-397) and the first-step clamp (:400-417)
     F2<T> u = U(), v = V(), w = W(), tabs = TABS(), qt = QT(), qp = QP(), qn = QN();
     bool clamp;
@@ -520,6 +583,25 @@ struct ColumnKernel : NxDim<NX> {
       PR(P_GRDFX)[k] = mn2((T)16., (T)p.dx * (T)p.dx / (adzdz * adzdz));
       PR(P_GRDFY)[k] = mn2((T)16., (T)p.dy * (T)p.dy / (adzdz * adzdz));
       PR(P_GRDFZ)[k] = (T)1.;
+    }
+    SYNC;
+    // per-level factors of the SGS closure (tke_full), evaluated exactly as
+    // its cell loops would, once per column
+    {
+      const T dzT = (T)S.dz, dxT = (T)p.dx, rdx0 = (T)1. / dxT, dtT = (T)p.dt;
+      T *adzw = PR(P_ADZW), *bet = PR(P_BET);
+      for (int k = TID + 1; k <= nz; k += NT) {
+        if (k <= nzm) PR(P_RDXZ)[k] = rdx0 * tsqrt(dxT * PR(P_RDZ)[k]);
+        PR(P_RDXW)[k] = rdx0 * tsqrt(dxT * PR(P_RDZW)[k]);
+        if (k <= nzm - 1) {
+          PR(P_BETDZ)[k] = (T)0.5 * (bet[k + 1] + bet[k]) / dzT / adzw[k + 1];
+          T cx = dxT * dxT / dtT / PR(P_GRDFX)[k];
+          T cy = (T)p.dy * (T)p.dy / dtT / PR(P_GRDFY)[k];
+          T dzm = dzT * mn2(adzw[k], adzw[k + 1]);
+          T cz = dzm * dzm / dtT / PR(P_GRDFZ)[k];
+          PR(P_TKMAX)[k] = (T)R4(0.09) / ((T)1. / cx + (T)1. / cy + (T)1. / cz);
+        }
+      }
     }
     SYNC;
     tridiag_factor();
@@ -668,8 +750,8 @@ struct ColumnKernel : NxDim<NX> {
       int i = 1 + e % nx, k = 1 + e / nx;
       if (k >= 2 && k <= nzm) {
         int kb = k - 1;
-        T betu = adz[kb] / (adz[k] + adz[kb]);
-        T betd = adz[k] / (adz[k] + adz[kb]);
+        T betu = PR(P_BETU)[k];
+        T betd = PR(P_BETD)[k];
         dw(i, k) = (T)0. +
             bet[k] * betu *
                 (tabs0[k] * (epsv * (qv(i, k) - qv0[k]) - (qcl(i, k) + qci(i, k) - qn0[k] + qpl(i, k) + qpi(i, k) - qp0[k])) +
@@ -851,12 +933,12 @@ struct ColumnKernel : NxDim<NX> {
 #define SQ(x) ((x) * (x))
       if (k >= 2 && k <= nzm - 1) {
         int kb = k - 1, kc = k + 1;
-        T rdz = (T)1. / (dz * adz[k]);
-        T rdzw_up = (T)1. / (dz * adzw[kc]);
-        T rdzw_dn = (T)1. / (dz * adzw[k]);
-        T rdx = rdx0 * tsqrt(dx * rdz);
-        T rdx_up = rdx0 * tsqrt(dx * rdzw_up);
-        T rdx_dn = rdx0 * tsqrt(dx * rdzw_dn);
+        T rdz = PR(P_RDZ)[k];
+        T rdzw_up = PR(P_RDZW)[kc];
+        T rdzw_dn = PR(P_RDZW)[k];
+        T rdx = PR(P_RDXZ)[k];
+        T rdx_up = PR(P_RDXW)[kc];
+        T rdx_dn = PR(P_RDXW)[k];
         r = (T)2. * (SQ((u(ic, k) - u(i, k)) * rdx) + SQ((w(i, kc) - w(i, k)) * rdz)) +
             (T)0.5 * (SQ((v(ic, k) - v(i, k)) * rdx) + SQ((v(i, k) - v(ib, k)) * rdx) +
                       SQ((u(ic, kc) - u0[kc] - u(ic, k) + u0[k]) * rdzw_up + (w(ic, kc) - w(i, kc)) * rdx_up) +
@@ -867,10 +949,10 @@ struct ColumnKernel : NxDim<NX> {
                       SQ((v(i, k) - v0[k] - v(i, kb) + v0[kb]) * rdzw_dn));
       } else if (k == 1) {
         int kc = k + 1;
-        T rdz = (T)1. / (dz * adz[k]);
-        T rdzw_up = (T)1. / (dz * adzw[kc]);
-        T rdx = rdx0 * tsqrt(dx * rdz);
-        T rdx_up = rdx0 * tsqrt(dx * rdzw_up);
+        T rdz = PR(P_RDZ)[k];
+        T rdzw_up = PR(P_RDZW)[kc];
+        T rdx = PR(P_RDXZ)[k];
+        T rdx_up = PR(P_RDXW)[kc];
         r = (T)2. * (SQ((u(ic, k) - u(i, k)) * rdx) + SQ((w(i, kc) - w(i, k)) * rdz)) +
             (T)0.5 * (SQ((v(ic, k) - v(i, k)) * rdx) + SQ((v(i, k) - v(ib, k)) * rdx)) +
             SQ((v(i, kc) - v0[kc] - v(i, k) + v0[k]) * rdzw_up) +
@@ -878,10 +960,10 @@ struct ColumnKernel : NxDim<NX> {
                       SQ((u(i, kc) - u0[kc] - u(i, k) + u0[k]) * rdzw_up + (w(i, kc) - w(ib, kc)) * rdx_up));
       } else {
         int kc = k + 1, kb = k - 1;
-        T rdz = (T)1. / (dz * adz[k]);
-        T rdzw_dn = (T)1. / (dz * adzw[k]);
-        T rdx = rdx0 * tsqrt(dx * rdz);
-        T rdx_dn = rdx0 * tsqrt(dx * rdzw_dn);
+        T rdz = PR(P_RDZ)[k];
+        T rdzw_dn = PR(P_RDZW)[k];
+        T rdx = PR(P_RDXZ)[k];
+        T rdx_dn = PR(P_RDXW)[k];
         r = (T)2. * (SQ((u(ic, k) - u(i, k)) * rdx) + SQ((w(i, kc) - w(i, k)) * rdz)) +
             (T)0.5 * (SQ((v(ic, k) - v(i, k)) * rdx) + SQ((v(i, k) - v(ib, k)) * rdx)) +
             SQ((v(i, k) - v0[k] - v(i, kb) + v0[kb]) * rdzw_dn) +
@@ -898,7 +980,7 @@ struct ColumnKernel : NxDim<NX> {
       int i = 1 + e % nx, k = e / nx;     // k = 0..nzm
       if (k == 0 || k == nzm) { buoy(i, k) = (T)0.; aprod(i, k) = (T)0.; continue; }
       int kc = k + 1, kb = k;
-      T betdz = (T)0.5 * (bet[kc] + bet[kb]) / dz / adzw[k + 1];
+      T betdz = PR(P_BETDZ)[k];
       T tabs_if = (T)0.5 * (tabs(i, kc) + fc * qcl(i, kc) + fs * qci(i, kc) + tabs(i, kb) + fc * qcl(i, kb) + fs * qci(i, kb));
       T qtot_if = (T)0.5 * (qv(i, kc) + qcl(i, kc) + qci(i, kc) + qv(i, kb) + qcl(i, kb) + qci(i, kb));
       T qp_if = (T)0.5 * (qpl(i, kc) + qpi(i, kc) + qpl(i, kb) + qpi(i, kb));
@@ -941,11 +1023,7 @@ struct ColumnKernel : NxDim<NX> {
       T grd = dz * adz[k];
       T Ce1 = Ce / (T)R4(0.7) * (T)R4(0.19);
       T Ce2 = Ce / (T)R4(0.7) * (T)R4(0.51);
-      T cx = dx * dx / dt / grdfx[k];
-      T cy = (T)p.dy * (T)p.dy / dt / grdfy[k];
-      T dzm = dz * mn2(adzw[k], adzw[k + 1]);
-      T cz = dzm * dzm / dt / grdfz[k];
-      T tkmax = (T)R4(0.09) / ((T)1. / cx + (T)1. / cy + (T)1. / cz);
+      T tkmax = PR(P_TKMAX)[k];
       T bs = (T)0.5 * (buoy(i, k - 1) + buoy(i, k));
       T smix;
       if (bs <= (T)0.) smix = grd;
@@ -975,7 +1053,7 @@ struct ColumnKernel : NxDim<NX> {
     for (int e = TID; e < nx * nzm; e += NT) {
       int i = 1 + e % nx, k = 1 + e / nx;
       int kc = k + 1, kcu = min(kc, nzm);
-      T irho = (T)1. / (rhow[kc] * adzw[kc]);
+      T irho = PR(P_IRHOWADZW)[kc];
       int ic = i + 1;
       T fu1 = dx25 * (u(ic - 1, k) + u(i - 1, k)) * (u(i - 1, k) + u(ic - 1, k));
       T fu2 = dx25 * (u(ic, k) + u(i, k)) * (u(i, k) + u(ic, k));
@@ -1007,7 +1085,7 @@ struct ColumnKernel : NxDim<NX> {
     for (int e = TID; e < nx * nzm; e += NT) {
       int i = 1 + e % nx, k = 1 + e / nx;
       int kc = k + 1;
-      T rhoi = (T)1. / (rho[k] * adz[k]);
+      T rhoi = PR(P_IRHOADZ)[k];
       du(i, k) = du(i, k) - (fuz(i, kc) - fuz(i, k)) * rhoi;
       dv(i, k) = dv(i, k) - (fvz(i, kc) - fvz(i, k)) * rhoi;
       fwz(i, k) = dz25 * (w(i, kc) * rhow[kc] + w(i, k) * rhow[k]) * (w(i, kc) + w(i, k));
@@ -1016,7 +1094,7 @@ struct ColumnKernel : NxDim<NX> {
     for (int e = TID; e < nx * (nzm - 1); e += NT) {
       int i = 1 + e % nx, k = 2 + e / nx;
       int kb = k - 1;
-      T rhoi = (T)1. / (rhow[k] * adzw[k]);
+      T rhoi = PR(P_IRHOWADZW)[k];
       dw(i, k) = dw(i, k) - (fwz(i, k) - fwz(i, kb)) * rhoi;
     }
     SYNC;
@@ -1063,8 +1141,8 @@ struct ColumnKernel : NxDim<NX> {
         T rdz2 = rdz * rdz * grdfz[k];
         T rdz25 = (T)0.25 * rdz2;
         T dzx = dz / dx;
-        T iadz = (T)1. / adz[k];
-        T iadzw = (T)1. / adzw[kc];
+        T iadz = PR(P_IADZ)[k];
+        T iadzw = PR(P_IADZW)[kc];
         int ib = i - 1;
         T tkz = rdz2 * tk(i, k);
         fw(i, kc) = (T)-2. * tkz * (w(i, kc) - w(i, k)) * rho[k] * iadz;
@@ -1090,11 +1168,11 @@ struct ColumnKernel : NxDim<NX> {
     for (int e = TID; e < nx * nzm; e += NT) {
       int i = 1 + e % nx, k = 1 + e / nx;
       int kc = k + 1;
-      T rhoi = (T)1. / (rho[k] * adz[k]);
+      T rhoi = PR(P_IRHOADZ)[k];
       du(i, k) = du(i, k) - (fu(i, kc) - fu(i, k)) * rhoi;
       dv(i, k) = dv(i, k) - (fv(i, kc) - fv(i, k)) * rhoi;
       if (k >= 2) {
-        T rhoiw = (T)1. / (rhow[k] * adzw[k]);
+        T rhoiw = PR(P_IRHOWADZW)[k];
         dw(i, k) = dw(i, k) - (fw(i, k + 1) - fw(i, k)) * rhoiw;
       }
     }
@@ -1109,8 +1187,13 @@ struct ColumnKernel : NxDim<NX> {
   // synchronises between passes.  Each output keeps the reference's
   // expression, so results are identical to a sequential evaluation.
   // Twiddle factors are REAL*4 values (fft.F90 has no implicit none).
+  // twiddle i of the trig table: the REAL*4 value, read as T without a
+  // widening or narrowing conversion in either form
+  __device__ __forceinline__ T tw(int i) const {
+    if constexpr (sizeof(T) == 4) return p.trigs_f[i];
+    else return p.trigs[i];
+  }
   __device__ void vpass_warp(const T *A, T *C, int nh, int ifac, int la, int lane) const {
-    const double *trigs = p.trigs;
     const int m = nh / ifac;
     for (int bf = lane; bf < m; bf += 32) {
       int g = bf / la, l = bf - g * la;
@@ -1121,7 +1204,7 @@ struct ColumnKernel : NxDim<NX> {
         C[2 * q] = a0 + a1; C[2 * q + 1] = b0 + b1;
         if (g == 0) { C[2 * (q + la)] = a0 - a1; C[2 * (q + la) + 1] = b0 - b1; }
         else {
-          T c1 = (T)trigs[kb], s1 = (T)trigs[kb + 1];
+          T c1 = tw(kb), s1 = tw(kb + 1);
           C[2 * (q + la)] = c1 * (a0 - a1) - s1 * (b0 - b1);
           C[2 * (q + la) + 1] = s1 * (a0 - a1) + c1 * (b0 - b1);
         }
@@ -1135,9 +1218,9 @@ struct ColumnKernel : NxDim<NX> {
           C1[0] = (a0 - a2) - (b1 - b3); C3[0] = (a0 - a2) + (b1 - b3);
           C1[1] = (b0 - b2) + (a1 - a3); C3[1] = (b0 - b2) - (a1 - a3);
         } else {
-          T c1 = (T)trigs[kb], s1 = (T)trigs[kb + 1];
-          T c2 = (T)trigs[2 * kb], s2 = (T)trigs[2 * kb + 1];
-          T c3 = (T)trigs[3 * kb], s3 = (T)trigs[3 * kb + 1];
+          T c1 = tw(kb), s1 = tw(kb + 1);
+          T c2 = tw(2 * kb), s2 = tw(2 * kb + 1);
+          T c3 = tw(3 * kb), s3 = tw(3 * kb + 1);
           C0[0] = (a0 + a2) + (a1 + a3); C0[1] = (b0 + b2) + (b1 + b3);
           C2[0] = c2 * ((a0 + a2) - (a1 + a3)) - s2 * ((b0 + b2) - (b1 + b3));
           C2[1] = s2 * ((a0 + a2) - (a1 + a3)) + c2 * ((b0 + b2) - (b1 + b3));
@@ -1153,7 +1236,6 @@ struct ColumnKernel : NxDim<NX> {
   // fft991_crm on a[0..n+1] (shared memory), work[0..n+1]; isign -1: grid
   // point -> spectral, +1: spectral -> grid point.  Called by a whole warp.
   __device__ void fft991_warp(T *a, T *work, int n, int isign, int lane) const {
-    const double *trigs = p.trigs;
     const int nfax = p.nfax, nh = n / 2, npair = (nh - 1) / 2;   // k = 3,5,..,nh
     bool in_work;
     if (isign == -1) {
@@ -1170,7 +1252,7 @@ struct ColumnKernel : NxDim<NX> {
       }
       for (int t = lane; t < npair; t += 32) {
         int k = 3 + 2 * t, ia = 2 + 2 * t, ib = n - 2 - 2 * t;
-        T c = (T)trigs[n + k - 1], s = (T)trigs[n + k];
+        T c = tw(n + k - 1), s = tw(n + k);
         T ap = a[ia] + a[ib], am = a[ia] - a[ib];
         T bp = a[ia + 1] + a[ib + 1], bm = a[ia + 1] - a[ib + 1];
         work[ia] = ap - (s * am + c * bp);
@@ -1207,7 +1289,7 @@ struct ColumnKernel : NxDim<NX> {
       }
       for (int t = lane; t < npair; t += 32) {
         int k = 3 + 2 * t, ia = 2 + 2 * t, ib = n - 2 - 2 * t;
-        T c = (T)trigs[n + k - 1], s = (T)trigs[n + k];
+        T c = tw(n + k - 1), s = tw(n + k);
         T wp = work[ia] + work[ib], wm = work[ia] - work[ib];
         T vp = work[ia + 1] + work[ib + 1], vm = work[ib + 1] - work[ia + 1];
         a[ia] = sc * (wp + (c * vp + s * wm));
@@ -1287,9 +1369,9 @@ struct ColumnKernel : NxDim<NX> {
     for (int e = TID; e < nx * nzm; e += NT) {
       int i = 1 + e % nx, k = 1 + e / nx;
       int kc = k + 1, ic = i + 1;
-      T rdz = (T)1. / (adz[k] * dz);
-      T rup = rhow[kc] / rho[k] * rdz;
-      T rdn = rhow[k] / rho[k] * rdz;
+      T rdz = PR(P_RDZ)[k];
+      T rup = PR(P_RUP)[k];
+      T rdn = PR(P_RDN)[k];
       T r = (rdx * (u(ic, k) - u(i, k)) + (w(i, kc) * rup - w(i, k) * rdn)) * dta +
             (rdx * (dua(ic, k) - dua(i, k)) + (dwa(i, kc) * rup - dwa(i, k) * rdn)) +
             btat * (rdx * (dub(ic, k) - dub(i, k)) + (dwb(i, kc) * rup - dwb(i, k) * rdn)) +
@@ -1341,7 +1423,7 @@ struct ColumnKernel : NxDim<NX> {
     for (int e = TID; e < nx * nzm; e += NT) {
       int i = 1 + e % nx, k = 1 + e / nx;
       int kb = max(1, k - 1);
-      T rdz = (T)1. / (dz * adzw[k]);
+      T rdz = PR(P_RDZW)[k];
       dua(i, k) = dua(i, k) - (pp(i, k) - pp(i - 1, k)) * rdx;
       dva(i, k) = dva(i, k) - (pp(i, k) - pp(i, k)) * rdy;
       dwa(i, k) = dwa(i, k) - (pp(i, k) - pp(i, kb)) * rdz;
@@ -1418,7 +1500,7 @@ struct ColumnKernel : NxDim<NX> {
                  [&](int, int) { return 0.; }, [&](int, int k, double sv) { wfl1(0, k) = (T)sv; });
     for (int e = TID; e < (nx + 4) * nzm; e += NT) {
       int i = -1 + e % (nx + 4), k = 1 + e / (nx + 4);   // -1 .. nx+2
-      T iadz = (T)1. / adz[k], irho = (T)1. / rho[k];
+      T iadz = PR(P_IADZ)[k], irho = PR(P_IRHO)[k];
       f(i, k) = f(i, k) - (uuu(i + 1, k) - uuu(i, k) + (www(i, k + 1) - www(i, k)) * iadz) * irho;
     }
     SYNC;
@@ -1426,9 +1508,9 @@ struct ColumnKernel : NxDim<NX> {
     for (int e = TID; e < (nx + 3) * nzm; e += NT) {
       int i = e % (nx + 3), k = 1 + e / (nx + 3);          // 0 .. nx+2
       int kc = min(nzm, k + 1), kb = max(1, k - 1);
-      T irho = (T)1. / rho[k];
-      T irhow = (T)1. / (rhow[k] * adz[k]);
-      T dd = (T)(double)(2.f / (float)(kc - kb)) / adz[k];
+      T irho = PR(P_IRHO)[k];
+      T irhow = PR(P_IRHOWADZ)[k];
+      T dd = PR(P_MPDD)[k];
       int ib = i - 1;
       {
         T a = u(i, k), x1 = f(ib, k), x2 = f(i, k);
@@ -1453,7 +1535,7 @@ struct ColumnKernel : NxDim<NX> {
     for (int e = TID; e < (nx + 2) * nzm; e += NT) {
       int i = e % (nx + 2), k = 1 + e / (nx + 2);          // 0 .. nx+1
       int kc = min(nzm, k + 1), kb = max(1, k - 1), ib = i - 1, ic = i + 1;
-      T iadz = (T)1. / adz[k];
+      T iadz = PR(P_IADZ)[k];
       T m1 = mx2(mx2(mx2(mx2(mx2(f(ib, k), f(ic, k)), f(i, kb)), f(i, kc)), f(i, k)), mx(i, k));
       T m2 = mn2(mn2(mn2(mn2(mn2(f(ib, k), f(ic, k)), f(i, kb)), f(i, kc)), f(i, k)), mn(i, k));
       T pu_c = -mn2((T)0., uuu(ic, k)), pu_i = mx2((T)0., uuu(i, k));
@@ -1482,7 +1564,7 @@ struct ColumnKernel : NxDim<NX> {
                  [&](int, int k, double sv) { flux[k] = (T)sv; });
     for (int e = TID; e < nx * nzm; e += NT) {
       int i = 1 + e % nx, k = 1 + e / nx;
-      T iadz = (T)1. / adz[k], irho = (T)1. / rho[k];
+      T iadz = PR(P_IADZ)[k], irho = PR(P_IRHO)[k];
       f(i, k) = mx2((T)0., f(i, k) - (uuu(i + 1, k) - uuu(i, k) + (www(i, k + 1) - www(i, k)) * iadz) * irho);
     }
     SYNC;
@@ -1669,7 +1751,7 @@ struct ColumnKernel : NxDim<NX> {
       int i = 1 + e % nx, k = 1 + e / nx;
       if (k <= nzm - 1) {
         int kc = k + 1;
-        T rhoi = rhow[kc] / adzw[kc];
+        T rhoi = PR(P_RHOWDADZW)[kc];
         T rdz2 = (T)1. / (dz * dz);
         T rdz5 = (T)0.5 * rdz2 * grdfz[k];
         T tkz = rdz5 * (tkh(i, k) + tkh(i, kc));
@@ -1688,7 +1770,7 @@ struct ColumnKernel : NxDim<NX> {
     for (int e = TID; e < nx * nzm; e += NT) {
       int i = 1 + e % nx, k = 1 + e / nx;
       int kb = k - 1;
-      T rhoi = (T)1. / (adz[k] * rho[k]);
+      T rhoi = PR(P_IRHOADZ)[k];
       T d = dtn * (dfdt(i, k) - (flx(i, k) - flx(i, kb)) * rhoi);
       f(i, k) = f(i, k) + d;
     }
@@ -1992,7 +2074,7 @@ struct ColumnKernel : NxDim<NX> {
     const double coef = 1. / (double)nx;
     // domain means; q0 and qn0 are kept in FP64 in TMP0/TMP1 for qv0
     double *q0d = reinterpret_cast<double *>(sa());
-    level_sums_lo(7, 1, nzm,
+    level_sums_lo_multi<7>(1, nzm,
                [&](int q, int i, int k) -> T {
                  switch (q) {
                    case 0: return u(i, k);
@@ -2003,6 +2085,11 @@ struct ColumnKernel : NxDim<NX> {
                    case 5: return qcl(i, k) + qci(i, k);
                    default: return qpl(i, k) + qpi(i, k);
                  }
+               },
+               [&](int i, int k, T *r) {
+                 const T c = qcl(i, k) + qci(i, k);
+                 r[0] = u(i, k); r[1] = v(i, k); r[2] = t(i, k); r[3] = tabs(i, k);
+                 r[4] = qv(i, k) + qcl(i, k) + qci(i, k); r[5] = c; r[6] = qpl(i, k) + qpi(i, k);
                },
                [&](int, int) { return 0.; },
                [&](int q, int k, double sv) {
@@ -2069,7 +2156,7 @@ struct ColumnKernel : NxDim<NX> {
                [&](int q, int k, double sv) { (q == 0 ? mui : mdi)[plev + 2 - k] = (T)sv; });
     // cloud fraction, cloud top counts, cloudy mass fluxes, water paths
     T *acc[8] = {OP(O_CLD), OP(O_CLDTOP), OP(O_MCUP), OP(O_MCDN), OP(O_MCUUP), OP(O_MCUDN), OP(O_GLIQWP), OP(O_GICEWP)};
-    level_sums_lo(8, 1, nzm,
+    level_sums_lo_multi<8>(1, nzm,
                [&](int q, int i, int k) -> T {
                  if (q == 1) return ((int)cs[4 * nx + (i - 1)] == k) ? (T)1. : (T)0.;
                  if (q == 6) return qcl(i, k);
@@ -2082,6 +2169,19 @@ struct ColumnKernel : NxDim<NX> {
                  if (q == 3) return (cloudy && ws < (T)-4.) ? rho[k] * (T)0.5 * ws * (T)1.0 : (T)0.;
                  if (q == 4) return (!cloudy && ws > (T)4.) ? rho[k] * (T)0.5 * ws : (T)0.;
                  return (!cloudy && ws < (T)-4.) ? rho[k] * (T)0.5 * ws : (T)0.;
+               },
+               [&](int i, int k, T *r) {
+                 const T ql = qcl(i, k), qi = qci(i, k);
+                 const bool cloudy = rho[k] * adz[k] * dz * (ql + qi) > thr;
+                 const T ws = w(i, k + 1) + w(i, k), m = rho[k] * (T)0.5 * ws;
+                 r[0] = cloudy ? (T)1.0 : (T)0.;
+                 r[1] = ((int)cs[4 * nx + (i - 1)] == k) ? (T)1. : (T)0.;
+                 r[2] = (cloudy && ws > (T)4.) ? m : (T)0.;
+                 r[3] = (cloudy && ws < (T)-4.) ? m : (T)0.;
+                 r[4] = (!cloudy && ws > (T)4.) ? m : (T)0.;
+                 r[5] = (!cloudy && ws < (T)-4.) ? m : (T)0.;
+                 r[6] = ql;
+                 r[7] = qi;
                },
                [&](int q, int k) { return (double)acc[q][plev - k + 1]; },
                [&](int q, int k, double sv) { acc[q][plev - k + 1] = (T)sv; });
