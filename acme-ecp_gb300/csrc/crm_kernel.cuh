@@ -1055,22 +1055,35 @@ struct ColumnKernel : NxDim<NX> {
       int kc = k + 1, kcu = min(kc, nzm);
       T irho = PR(P_IRHOWADZW)[kc];
       int ic = i + 1;
-      T fu1 = dx25 * (u(ic - 1, k) + u(i - 1, k)) * (u(i - 1, k) + u(ic - 1, k));
-      T fu2 = dx25 * (u(ic, k) + u(i, k)) * (u(i, k) + u(ic, k));
-      du(i, k) = du(i, k) - (fu2 - fu1);
-      T fv1 = dx25 * (u(ic - 1, k) + u(i - 1, k)) * (v(i - 1, k) + v(ic - 1, k));
-      T fv2 = dx25 * (u(ic, k) + u(i, k)) * (v(i, k) + v(ic, k));
-      dv(i, k) = dv(i, k) - (fv2 - fv1);
-      T fw1 = dx25 * (u(ic - 1, k) * rho[k] * adz[k] + u(ic - 1, kcu) * rho[kcu] * adz[kcu]) * (w(i - 1, kc) + w(ic - 1, kc));
-      T fw2 = dx25 * (u(ic, k) * rho[k] * adz[k] + u(ic, kcu) * rho[kcu] * adz[kcu]) * (w(i, kc) + w(ic, kc));
-      dw(i, kc) = dw(i, kc) - irho * (fw2 - fw1);
-      // vertical fluxes of u, v at w level k (k = 2..nzm); 0 at 1 and nz
+      // all loads first (the stores below may alias them for the compiler);
+      // u(ic - 1, .) is u(i, .)
+      const T um = u(i - 1, k), ui = u(i, k), uc = u(ic, k), uiu = u(i, kcu), ucu = u(ic, kcu);
+      const T vm = v(i - 1, k), vi = v(i, k), vc = v(ic, k);
+      const T wmc = w(i - 1, kc), wic = w(i, kc), wcc = w(ic, kc);
+      T fu1 = dx25 * (ui + um) * (um + ui);
+      T fu2 = dx25 * (uc + ui) * (ui + uc);
+      T fv1 = dx25 * (ui + um) * (vm + vi);
+      T fv2 = dx25 * (uc + ui) * (vi + vc);
+      T fw1 = dx25 * (ui * rho[k] * adz[k] + uiu * rho[kcu] * adz[kcu]) * (wmc + wic);
+      T fw2 = dx25 * (uc * rho[k] * adz[k] + ucu * rho[kcu] * adz[kcu]) * (wic + wcc);
+      T fzu = (T)0., fzv = (T)0.;
       if (k >= 2) {
         int kb = k - 1;
         T rhoi = dz25 * rhow[k];
         T www = rhoi * (w(i, k) + w(i - 1, k));
-        fuz(i, k) = www * (u(i, k) + u(i, kb));
-        fvz(i, k) = www * (v(i, k) + v(i, kb));
+        fzu = www * (ui + u(i, kb));
+        fzv = www * (vi + v(i, kb));
+      }
+      const T dun = du(i, k) - (fu2 - fu1);
+      const T dvn = dv(i, k) - (fv2 - fv1);
+      const T dwn = dw(i, kc) - irho * (fw2 - fw1);
+      du(i, k) = dun;
+      dv(i, k) = dvn;
+      dw(i, kc) = dwn;
+      // vertical fluxes of u, v at w level k (k = 2..nzm); 0 at 1 and nz
+      if (k >= 2) {
+        fuz(i, k) = fzu;
+        fvz(i, k) = fzv;
       } else {
         fuz(i, 1) = (T)0.; fvz(i, 1) = (T)0.;
         fuz(i, nz) = (T)0.; fvz(i, nz) = (T)0.;
@@ -1117,11 +1130,17 @@ struct ColumnKernel : NxDim<NX> {
       T rdx21 = rdx2 * grdfx[k];
       T rdx251 = rdx25 * grdfx[k];
       int ic = i + 1;
-      T tkx = rdx21 * tk(i, k);
-      fu(i, k) = (T)-2. * tkx * (u(ic, k) - u(i, k));
-      fv(i, k) = -tkx * (v(ic, k) - v(i, k));
-      tkx = rdx251 * (tk(i, k) + tk(ic, k) + tk(i, kcu) + tk(ic, kcu));
-      fw(i, k) = -tkx * (w(ic, kc) - w(i, kc) + (u(ic, kcu) - u(ic, k)) * dxz);
+      const T tki = tk(i, k), tkc = tk(ic, k), tkiu = tk(i, kcu), tkcu = tk(ic, kcu);
+      const T uc = u(ic, k), ui = u(i, k), ucu = u(ic, kcu), vc = v(ic, k), vi = v(i, k);
+      const T wcc = w(ic, kc), wic = w(i, kc);
+      T tkx = rdx21 * tki;
+      const T fuv = (T)-2. * tkx * (uc - ui);
+      const T fvv = -tkx * (vc - vi);
+      tkx = rdx251 * (tki + tkc + tkiu + tkcu);
+      const T fwv = -tkx * (wcc - wic + (ucu - uc) * dxz);
+      fu(i, k) = fuv;
+      fv(i, k) = fvv;
+      fw(i, k) = fwv;
     }
     SYNC;
     for (int e = TID; e < nx * nzm; e += NT) {
@@ -1144,11 +1163,17 @@ struct ColumnKernel : NxDim<NX> {
         T iadz = PR(P_IADZ)[k];
         T iadzw = PR(P_IADZW)[kc];
         int ib = i - 1;
-        T tkz = rdz2 * tk(i, k);
-        fw(i, kc) = (T)-2. * tkz * (w(i, kc) - w(i, k)) * rho[k] * iadz;
-        tkz = rdz25 * (tk(i, k) + tk(ib, k) + tk(i, kc) + tk(ib, kc));
-        fu(i, kc) = -tkz * ((u(i, kc) - u(i, k)) * iadzw + (w(i, kc) - w(ib, kc)) * dzx) * rhow[kc];
-        fv(i, kc) = -tkz * (v(i, kc) - v(i, k)) * iadzw * rhow[kc];
+        const T tki = tk(i, k), tkb = tk(ib, k), tkic = tk(i, kc), tkbc = tk(ib, kc);
+        const T wic = w(i, kc), wi = w(i, k), wbc = w(ib, kc);
+        const T uic = u(i, kc), ui = u(i, k), vic = v(i, kc), vi = v(i, k), rk = rho[k], rwc = rhow[kc];
+        T tkz = rdz2 * tki;
+        const T fwv = (T)-2. * tkz * (wic - wi) * rk * iadz;
+        tkz = rdz25 * (tki + tkb + tkic + tkbc);
+        const T fuv = -tkz * ((uic - ui) * iadzw + (wic - wbc) * dzx) * rwc;
+        const T fvv = -tkz * (vic - vi) * iadzw * rwc;
+        fw(i, kc) = fwv;
+        fu(i, kc) = fuv;
+        fv(i, kc) = fvv;
       } else {
         T rdz = (T)1. / dz;
         T rdz2 = rdz * rdz * grdfz[nzm - 1];
@@ -1169,11 +1194,15 @@ struct ColumnKernel : NxDim<NX> {
       int i = 1 + e % nx, k = 1 + e / nx;
       int kc = k + 1;
       T rhoi = PR(P_IRHOADZ)[k];
-      du(i, k) = du(i, k) - (fu(i, kc) - fu(i, k)) * rhoi;
-      dv(i, k) = dv(i, k) - (fv(i, kc) - fv(i, k)) * rhoi;
+      const T fuc = fu(i, kc), fuk = fu(i, k), fvc = fv(i, kc), fvk = fv(i, k);
+      const T fwc = k >= 2 ? fw(i, k + 1) : (T)0., fwk = k >= 2 ? fw(i, k) : (T)0.;
+      const T dun = du(i, k) - (fuc - fuk) * rhoi;
+      const T dvn = dv(i, k) - (fvc - fvk) * rhoi;
+      du(i, k) = dun;
+      dv(i, k) = dvn;
       if (k >= 2) {
         T rhoiw = PR(P_IRHOWADZW)[k];
-        dw(i, k) = dw(i, k) - (fw(i, k + 1) - fw(i, k)) * rhoiw;
+        dw(i, k) = dw(i, k) - (fwc - fwk) * rhoiw;
       }
     }
     SYNC;
@@ -1480,18 +1509,23 @@ struct ColumnKernel : NxDim<NX> {
     T *rho = PR(P_RHO), *adz = PR(P_ADZ), *rhow = PR(P_RHOW);
     const T eps = (T)R4(1.e-10);
     // f0, mx/mn from the initial field, upwind fluxes
+    // (every input is loaded into registers before the first store: the
+    // stores go through pointers the compiler must assume may alias f)
     for (int e = TID; e < (nx + 5) * nzm; e += NT) {
       int i = -1 + e % (nx + 5), k = 1 + e / (nx + 5);   // i = -1 .. nx+3
       int kc = min(nzm, k + 1), kb = max(1, k - 1);
-      if (i >= 0 && i <= nx + 1) {
-        int ib = i - 1, ic = i + 1;
-        mx(i, k) = mx2(mx2(mx2(mx2(f(ib, k), f(ic, k)), f(i, kb)), f(i, kc)), f(i, k));
-        mn(i, k) = mn2(mn2(mn2(mn2(f(ib, k), f(ic, k)), f(i, kb)), f(i, kc)), f(i, k));
+      const T fk = f(i, k), fb = f(i - 1, k), uk = u(i, k);
+      const bool in_w = i <= nx + 2, in_m = i >= 0 && i <= nx + 1;
+      const T fkb = in_w ? f(i, kb) : (T)0., wk = in_w ? w(i, k) : (T)0.;
+      const T fc = in_m ? f(i + 1, k) : (T)0., fkc = in_m ? f(i, kc) : (T)0.;
+      if (in_m) {
+        mx(i, k) = mx2(mx2(mx2(mx2(fb, fc), fkb), fkc), fk);
+        mn(i, k) = mn2(mn2(mn2(mn2(fb, fc), fkb), fkc), fk);
       }
-      if (fadv && i >= 1 && i <= nx) f0(i, k) = f(i, k);
-      uuu(i, k) = mx2((T)0., u(i, k)) * f(i - 1, k) + mn2((T)0., u(i, k)) * f(i, k);
-      if (i <= nx + 2) www(i, k) = mx2((T)0., w(i, k)) * f(i, kb) + mn2((T)0., w(i, k)) * f(i, k);
-      if (k == 1 && i <= nx + 2) www(i, nz) = (T)0.;
+      if (fadv && i >= 1 && i <= nx) f0(i, k) = fk;
+      uuu(i, k) = mx2((T)0., uk) * fb + mn2((T)0., uk) * fk;
+      if (in_w) www(i, k) = mx2((T)0., wk) * fkb + mn2((T)0., wk) * fk;
+      if (k == 1 && in_w) www(i, nz) = (T)0.;
     }
     SYNC;
     // first-pass (upwind) vertical flux sum, then the upwind update
@@ -1512,13 +1546,14 @@ struct ColumnKernel : NxDim<NX> {
       T irhow = PR(P_IRHOWADZ)[k];
       T dd = PR(P_MPDD)[k];
       int ib = i - 1;
+      T uval, wval = (T)0.;
       {
         T a = u(i, k), x1 = f(ib, k), x2 = f(i, k);
         T andiff = (tabs_(a) - a * a * irho) * (T)0.5 * (x2 - x1);
         T ax1 = dd * (f(ib, kc) + f(i, kc) - f(ib, kb) - f(i, kb));
         T a2 = w(ib, k) + w(ib, kc) + w(i, k) + w(i, kc);
         T across = (T)0.03125 * a * a2 * ax1;
-        uuu(i, k) = andiff - across * irho;
+        uval = andiff - across * irho;
       }
       if (i <= nx + 1) {
         int ic = i + 1;
@@ -1527,8 +1562,10 @@ struct ColumnKernel : NxDim<NX> {
         T ax1 = f(ic, kb) + f(ic, k) - f(ib, kb) - f(ib, k);
         T a2 = u(i, kb) + u(i, k) + u(ic, k) + u(ic, kb);
         T across = (T)0.03125 * a * a2 * ax1;
-        www(i, k) = (k == 1) ? (T)0. : andiff - across * irho;
+        wval = (k == 1) ? (T)0. : andiff - across * irho;
       }
+      uuu(i, k) = uval;                      // stores after every load
+      if (i <= nx + 1) www(i, k) = wval;
     }
     SYNC;
     // non-oscillatory limiter
@@ -1538,24 +1575,29 @@ struct ColumnKernel : NxDim<NX> {
       T iadz = PR(P_IADZ)[k];
       T m1 = mx2(mx2(mx2(mx2(mx2(f(ib, k), f(ic, k)), f(i, kb)), f(i, kc)), f(i, k)), mx(i, k));
       T m2 = mn2(mn2(mn2(mn2(mn2(f(ib, k), f(ic, k)), f(i, kb)), f(i, kc)), f(i, k)), mn(i, k));
-      T pu_c = -mn2((T)0., uuu(ic, k)), pu_i = mx2((T)0., uuu(i, k));
-      T pw_c = -mn2((T)0., www(i, kc)), pw_i = mx2((T)0., www(i, k));
-      mx(i, k) = rho[k] * (m1 - f(i, k)) / (pu_c + pu_i + iadz * (pw_c + pw_i) + eps);
-      T qu_c = mx2((T)0., uuu(ic, k)), qu_i = -mn2((T)0., uuu(i, k));
-      T qw_c = mx2((T)0., www(i, kc)), qw_i = -mn2((T)0., www(i, k));
-      mn(i, k) = rho[k] * (f(i, k) - m2) / (qu_c + qu_i + iadz * (qw_c + qw_i) + eps);
+      const T fk = f(i, k), uc = uuu(ic, k), ui = uuu(i, k), wc = www(i, kc), wi = www(i, k);
+      T pu_c = -mn2((T)0., uc), pu_i = mx2((T)0., ui);
+      T pw_c = -mn2((T)0., wc), pw_i = mx2((T)0., wi);
+      const T mxv = rho[k] * (m1 - fk) / (pu_c + pu_i + iadz * (pw_c + pw_i) + eps);
+      T qu_c = mx2((T)0., uc), qu_i = -mn2((T)0., ui);
+      T qw_c = mx2((T)0., wc), qw_i = -mn2((T)0., wi);
+      const T mnv = rho[k] * (fk - m2) / (qu_c + qu_i + iadz * (qw_c + qw_i) + eps);
+      mx(i, k) = mxv;
+      mn(i, k) = mnv;
     }
     SYNC;
     for (int e = TID; e < (nx + 1) * nzm; e += NT) {
       int i = 1 + e % (nx + 1), k = 1 + e / (nx + 1);      // 1 .. nx+1
       int ib = i - 1;
-      T uu = uuu(i, k);
-      uuu(i, k) = mx2((T)0., uu) * mn3((T)1., mx(i, k), mn(ib, k)) - (-mn2((T)0., uu)) * mn3((T)1., mx(ib, k), mn(i, k));
+      const T uu = uuu(i, k), mxk = mx(i, k), mnk = mn(i, k);
+      const T uval = mx2((T)0., uu) * mn3((T)1., mxk, mn(ib, k)) - (-mn2((T)0., uu)) * mn3((T)1., mx(ib, k), mnk);
       if (i <= nx) {
         int kb = max(1, k - 1);
-        T ww = www(i, k);
-        www(i, k) = mx2((T)0., ww) * mn3((T)1., mx(i, k), mn(i, kb)) - (-mn2((T)0., ww)) * mn3((T)1., mx(i, kb), mn(i, k));
+        const T ww = www(i, k);
+        const T wval = mx2((T)0., ww) * mn3((T)1., mxk, mn(i, kb)) - (-mn2((T)0., ww)) * mn3((T)1., mx(i, kb), mnk);
+        www(i, k) = wval;
       }
+      uuu(i, k) = uval;
     }
     SYNC;
     if (flux)
@@ -1677,10 +1719,13 @@ struct ColumnKernel : NxDim<NX> {
       for (int e = TID; e < nx * nzm; e += NT) {
         int i = 1 + e % nx, k = 1 + e / nx;
         int kc = min(nzm, k + 1), kb = max(1, k - 1);
-        T a = mx2(mx3(tq(i, kb), tq(i, kc), tq(i, k)), mx(i, k));
-        T b = mn2(mn3(tq(i, kb), tq(i, kc), tq(i, k)), mn(i, k));
-        mx(i, k) = rho[k] * adz[k] * (a - tq(i, k)) / (-mn2((T)0., www(i, kc)) + mx2((T)0., www(i, k)) + eps);
-        mn(i, k) = rho[k] * adz[k] * (tq(i, k) - b) / (mx2((T)0., www(i, kc)) + -mn2((T)0., www(i, k)) + eps);
+        const T tb = tq(i, kb), tc = tq(i, kc), tk0 = tq(i, k), wc = www(i, kc), wk = www(i, k);
+        T a = mx2(mx3(tb, tc, tk0), mx(i, k));
+        T b = mn2(mn3(tb, tc, tk0), mn(i, k));
+        const T mxv = rho[k] * adz[k] * (a - tk0) / (-mn2((T)0., wc) + mx2((T)0., wk) + eps);
+        const T mnv = rho[k] * adz[k] * (tk0 - b) / (mx2((T)0., wc) + -mn2((T)0., wk) + eps);
+        mx(i, k) = mxv;
+        mn(i, k) = mnv;
       }
       SYNC;
       for (int e = TID; e < nx * nzm; e += NT) {
@@ -1702,13 +1747,16 @@ struct ColumnKernel : NxDim<NX> {
         int i = 1 + e % nx, k = 1 + e / nx;
         int kc = k + 1;
         T lf_c = (kc == nz) ? (T)0. : fc + ((T)1. - omega(i, kc)) * ffus;
-        T lf_k = fc + ((T)1. - omega(i, k)) * ffus;
-        qp(i, k) = qp(i, k) - (fz(i, kc) - fz(i, k)) * irhoadz[k];
-        T lat_heat = -(lf_c * fz(i, kc) - lf_k * fz(i, k)) * irhoadz[k];
-        t(i, k) = t(i, k) - lat_heat;
+        const T omk = omega(i, k), fzc = fz(i, kc), fzk = fz(i, k), ia = irhoadz[k];
+        T lf_k = fc + ((T)1. - omk) * ffus;
+        const T qpn = qp(i, k) - (fzc - fzk) * ia;
+        T lat_heat = -(lf_c * fzc - lf_k * fzk) * ia;
+        const T tn = t(i, k) - lat_heat;
+        qp(i, k) = qpn;
+        t(i, k) = tn;
         if (k == 1) {
-          PS(i) = PS(i) - fz(i, 1) * (T)1.;
-          PSS(i) = PSS(i) - fz(i, 1) * ((T)1. - omega(i, 1)) * (T)1.;
+          PS(i) = PS(i) - fzk * (T)1.;
+          PSS(i) = PSS(i) - fzk * ((T)1. - omk) * (T)1.;
         }
       }
       SYNC;
@@ -1737,8 +1785,9 @@ struct ColumnKernel : NxDim<NX> {
       T rdx5 = (T)0.5 * rdx2 * grdfx[k];
       int ic = i + 1;
       T tkx = rdx5 * (tkh(i, k) + tkh(ic, k));
-      flx(i, k) = -tkx * (f(ic, k) - f(i, k));
-      if (fdiff && i >= 1) f0(i, k) = f(i, k);
+      const T fc = f(ic, k), fi = f(i, k);
+      flx(i, k) = -tkx * (fc - fi);
+      if (fdiff && i >= 1) f0(i, k) = fi;
     }
     SYNC;
     for (int e = TID; e < nx * nzm; e += NT) {
