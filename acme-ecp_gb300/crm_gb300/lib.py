@@ -16,7 +16,8 @@ LIB_PATH = os.path.join(HERE, 'libcrm_gb300.so')
 
 EXPORTS = ('crm_create', 'crm_destroy', 'crm_run', 'crm_run_device', 'crm_last_launch_count',
            'crm_last_kernel_ms', 'crm_set_stream', 'crm_status_string', 'crm_version',
-           'crm_debug_phase_cycles', 'crm_run_device_noalloc')
+           'crm_debug_phase_cycles', 'crm_run_device_noalloc', 'crm_num_launch_shapes',
+           'crm_launch_shape_info', 'crm_set_launch_shape', 'crm_get_launch_shape')
 
 _lib = None
 
@@ -66,6 +67,14 @@ def load(path=None, build_if_missing=False):
     lib.crm_status_string.argtypes = [C.c_int]
     lib.crm_version.restype = C.c_char_p
     lib.crm_version.argtypes = []
+    lib.crm_num_launch_shapes.restype = C.c_int
+    lib.crm_num_launch_shapes.argtypes = []
+    lib.crm_launch_shape_info.restype = C.c_int
+    lib.crm_launch_shape_info.argtypes = [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    lib.crm_set_launch_shape.restype = C.c_int
+    lib.crm_set_launch_shape.argtypes = [C.c_void_p, C.c_int]
+    lib.crm_get_launch_shape.restype = C.c_int
+    lib.crm_get_launch_shape.argtypes = [C.c_void_p]
     lib.crm_debug_phase_cycles.restype = C.c_int
     lib.crm_debug_phase_cycles.argtypes = [C.c_void_p, C.POINTER(C.c_ulonglong), C.c_int]
     _lib = lib
@@ -139,6 +148,14 @@ class CrmContext:
                                       C.c_void_p(stream))
         if rc != T.CRM_OK:
             raise CrmError(rc, 'crm_run_device')
+
+    @property
+    def launch_shape(self):
+        return self._lib.crm_get_launch_shape(self._h)
+
+    def set_launch_shape(self, shape):
+        """Select a launch shape (-1: default); returns the crm_status."""
+        return self._lib.crm_set_launch_shape(self._h, int(shape))
 
     def phase_cycles(self, n=64):
         """Per-phase cycle counters of a profiling build (None otherwise)."""

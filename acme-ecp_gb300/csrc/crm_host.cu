@@ -32,6 +32,8 @@ struct crm_ctx {
   crm_config cfg;
   crm::Layout L;
   int device = 0, nsm = 0, shape = 0, grid_max = 0;
+  int shape_grid[crm::kNumShapes] = {};   // co-resident CTAs per launch shape
+  int slab_cap = 0;                         // slabs allocated (max over shapes)
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -235,13 +237,24 @@ int alloc_ctx(crm_ctx *c) {
   CK(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, c->device));
   const size_t esz = g.precision == CRM_FP64 ? sizeof(double) : sizeof(float);
   c->L = crm::make_layout(g.crm_nx, g.crm_nz, g.plev, g.crm_nx_rad, (int)esz);
+  // co-resident CTAs of every launch shape; slabs for the largest, so the
+  // shape can change per call (crm_set_launch_shape)
+  for (int s = 0; s < crm::kNumShapes; ++s) {
+    int per = crm::occupancy_columns(g.precision, s, g.crm_nx, g.crm_nz);
+    int grid = per > 0 ? c->nsm * per : 0;
+    if (grid > g.max_ncrms) grid = g.max_ncrms;
+    c->shape_grid[s] = grid;
+    if (grid > c->slab_cap) c->slab_cap = grid;
+  }
   c->shape = default_shape(g.precision, g.crm_nx);
-  int per_sm = crm::occupancy_columns(g.precision, c->shape, g.crm_nx, g.crm_nz);
-  if (per_sm < 1) return CRM_ERR_UNSUPPORTED;
-  c->grid_max = c->nsm * per_sm;
-  if (c->grid_max > g.max_ncrms) c->grid_max = g.max_ncrms;
+  if (c->shape_grid[c->shape] < 1) {
+    for (int s = 0; s < crm::kNumShapes; ++s)
+      if (c->shape_grid[s] > 0) { c->shape = s; break; }
+  }
+  if (c->shape_grid[c->shape] < 1) return CRM_ERR_UNSUPPORTED;
+  c->grid_max = c->shape_grid[c->shape];
   c->slab_bytes = c->L.slab * esz;
-  CK(cudaMalloc(&c->slabs, c->slab_bytes * (size_t)c->grid_max));
+  CK(cudaMalloc(&c->slabs, c->slab_bytes * (size_t)c->slab_cap));
   c->ld_cap = g.max_ncrms;
   const int ld = c->ld_cap, plev = g.plev, nx = g.crm_nx, nz = g.crm_nz;
   c->in_elems = (size_t)ld * (plev + 1);
@@ -284,8 +297,8 @@ int alloc_ctx(crm_ctx *c) {
   CK(cudaMalloc(&c->d_gsync, 8 * sizeof(unsigned long long)));
   CK(cudaMemset(c->d_gsync, 0, 8 * sizeof(unsigned long long)));
 #ifdef CRM_PHASE_TIMERS
-  CK(cudaMalloc(&c->d_phase, sizeof(unsigned long long) * 64 * (size_t)c->grid_max));
-  CK(cudaMemset(c->d_phase, 0, sizeof(unsigned long long) * 64 * (size_t)c->grid_max));
+  CK(cudaMalloc(&c->d_phase, sizeof(unsigned long long) * 64 * (size_t)c->slab_cap));
+  CK(cudaMemset(c->d_phase, 0, sizeof(unsigned long long) * 64 * (size_t)c->slab_cap));
 #endif
   // gamma functions and fall speeds (precip_init.F90:25-49, microphysics.F90:500-507)
   const double b_rain = R4H(0.8), b_snow = 0.25, b_grau = 0.5;
@@ -479,18 +492,39 @@ const char *crm_status_string(int s) {
 // -DCRM_PHASE_TIMERS); returns the number of phases written or -1.
 int crm_debug_phase_cycles(crm_ctx *ctx, unsigned long long *out, int n) {
   if (!ctx || !ctx->d_phase || !out) return -1;
-  std::vector<unsigned long long> h((size_t)64 * ctx->grid_max);
+  std::vector<unsigned long long> h((size_t)64 * ctx->slab_cap);
   if (cudaMemcpy(h.data(), ctx->d_phase, sizeof(unsigned long long) * h.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
     return -1;
   int m = n < crm::PH_COUNT ? n : crm::PH_COUNT;
   for (int i = 0; i < m; ++i) {
     unsigned long long s = 0;
-    for (int b = 0; b < ctx->grid_max; ++b) s += h[(size_t)b * 64 + i];
+    for (int b = 0; b < ctx->slab_cap; ++b) s += h[(size_t)b * 64 + i];
     out[i] = s;
   }
   cudaMemset(ctx->d_phase, 0, sizeof(unsigned long long) * h.size());
   return m;
 }
+
+int crm_num_launch_shapes(void) { return crm::kNumShapes; }
+
+int crm_launch_shape_info(int shape, int *threads, int *ctas_per_sm, int *smem_planes) {
+  if (shape < 0 || shape >= crm::kNumShapes) return CRM_ERR_ARG;
+  if (threads) *threads = crm::kShapes[shape].threads;
+  if (ctas_per_sm) *ctas_per_sm = crm::kShapes[shape].min_ctas;
+  if (smem_planes) *smem_planes = crm::kShapes[shape].smem_planes;
+  return CRM_OK;
+}
+
+int crm_set_launch_shape(crm_ctx *ctx, int shape) {
+  if (!ctx) return CRM_ERR_ARG;
+  if (shape == -1) shape = default_shape(ctx->cfg.precision, ctx->cfg.crm_nx);
+  if (shape < 0 || shape >= crm::kNumShapes || ctx->shape_grid[shape] < 1) return CRM_ERR_ARG;
+  ctx->shape = shape;
+  ctx->grid_max = ctx->shape_grid[shape];
+  return CRM_OK;
+}
+
+int crm_get_launch_shape(const crm_ctx *ctx) { return ctx ? ctx->shape : -1; }
 
 const char *crm_version(void) { return "crm-gb300 0.1 (sm_103a; 2D sam1mom; fp64 plain + fp32 mixed)"; }
 

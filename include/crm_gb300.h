@@ -239,6 +239,17 @@ const char *crm_status_string(int status);
  * normal build.  No counterpart in the reference (its GPTL timers
  * t_startf/t_stopf time the whole CRM call, crm_module.F90:377,1598). */
 int crm_debug_phase_cycles(crm_ctx *ctx, unsigned long long *out, int n);
+/* Launch shapes of the column kernel (threads per CTA, CTAs per SM the
+ * register budget is sized for, scratch planes in shared memory): the search
+ * space of an autotuner (crm_gb300/autotune.py).  Results do not depend on
+ * the shape.  No counterpart in the reference (its OpenACC schedule is the
+ * compiler's).  crm_set_launch_shape selects one for later calls on the
+ * handle (-1: the measured default); CRM_ERR_ARG when out of range or not
+ * launchable for this configuration. */
+int crm_num_launch_shapes(void);
+int crm_launch_shape_info(int shape, int *threads, int *ctas_per_sm, int *smem_planes);
+int crm_set_launch_shape(crm_ctx *ctx, int shape);
+int crm_get_launch_shape(const crm_ctx *ctx);
 /* Library version string. */
 const char *crm_version(void);
 
