@@ -153,6 +153,7 @@ def main():
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--fp64-steps', type=int, default=2)
     ap.add_argument('--cpu-cols', type=int, default=512)
+    ap.add_argument('--autotune', type=int, default=1, help='choose the launch shape by timing (1) or use the default table (0)')
     ap.add_argument('--serve-seconds', type=float, default=20.0,
                     help='duration of the 80%%-load serving window (0: skip serving)')
     args = ap.parse_args()
@@ -166,6 +167,7 @@ def main():
     from crm_gb300.device import DeviceCrmArrays
     from crm_gb300.lib import CrmContext
     from crm_gb300.shard import column_shard
+    from crm_gb300.autotune import autotune
 
     ws, rank, local = dist_info()
     if ws > 1:
@@ -196,10 +198,17 @@ def main():
     colsteps = NCRMS * nstop
     cells = cfg32.crm_nx * cfg32.crm_ny * cfg32.crm_nz
 
+    tuned = {}
+
     def device_rate(cfg, steps, warmup):
         ctx = CrmContext(cfg)
         dev = DeviceCrmArrays(cfg, cin, st, rad, desc, desc._keep)
         stream = torch.cuda.current_stream().cuda_stream
+        # launch shape chosen by the autotuner on this batch (untimed)
+        if args.autotune:
+            best, times = autotune(ctx, dev, st, reps=1, stream=stream)
+            tuned['fp64' if cfg.precision == T.CRM_FP64 else 'fp32'] = {
+                'shape': best, 'ms_per_shape': {str(k): round(v, 2) for k, v in times.items()}}
         for _ in range(warmup):
             dev.reset_state(st)
             ctx.run_device(dev, stream)
@@ -354,6 +363,7 @@ def main():
         'fp32_over_fp64': value / value64,
         'fp32_rel_l2_vs_fp64_state': errs,
         'serving': serving,
+        'launch_shapes': tuned,
     }
     print(json.dumps(line))
     if ws > 1:

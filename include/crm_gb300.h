@@ -241,8 +241,8 @@ const char *crm_status_string(int status);
 int crm_debug_phase_cycles(crm_ctx *ctx, unsigned long long *out, int n);
 /* Launch shapes of the column kernel (threads per CTA, CTAs per SM the
  * register budget is sized for, scratch planes in shared memory): the search
- * space of an autotuner (crm_gb300/autotune.py).  Results do not depend on
- * the shape.  No counterpart in the reference (its OpenACC schedule is the
+ * space of an autotuner (crm_gb300/autotune.py).  FP64 results do not
+ * depend on the shape; FP32-mixed results agree to FP32 rounding.  No counterpart in the reference (its OpenACC schedule is the
  * compiler's).  crm_set_launch_shape selects one for later calls on the
  * handle (-1: the measured default); CRM_ERR_ARG when out of range or not
  * launchable for this configuration. */
