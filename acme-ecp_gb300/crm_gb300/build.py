@@ -31,7 +31,11 @@ for _n in NX_BUILT:
     for _s in range(NUM_SHAPES):
         _d = ['-DCRM_INST_NX=%d' % _n, '-DCRM_INST_SHAPE=%d' % _s]
         UNITS['crm_fp64_nx%d_s%d' % (_n, _s)] = ('crm_columns', ['-fmad=false', '-DCRM_INST_T=double'] + _d)
-        UNITS['crm_fp32_nx%d_s%d' % (_n, _s)] = ('crm_columns', ['-DCRM_INST_T=float'] + _d)
+        # FP32-mixed form: FP32 division and square root to the hardware's
+        # approximate instructions (<= 2 ulp), denormals flushed; the FP64
+        # parts of the form are unaffected by these flags
+        UNITS['crm_fp32_nx%d_s%d' % (_n, _s)] = ('crm_columns', ['-DCRM_INST_T=float', '-prec-div=false',
+                                                                 '-prec-sqrt=false', '-ftz=true'] + _d)
 
 
 def _nvcc():

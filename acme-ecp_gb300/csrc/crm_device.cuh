@@ -30,6 +30,10 @@ __device__ __forceinline__ float tlog(float x) { return __logf(x); }
 // CPU restatement: returns b only if it compares greater (smaller).
 template <typename T> __device__ __forceinline__ T mx2(T a, T b) { return (b > a) ? b : a; }
 template <typename T> __device__ __forceinline__ T mn2(T a, T b) { return (b < a) ? b : a; }
+// FP32-mixed form: the hardware min/max, one instruction; it differs from
+// the rule above only for NaN operands and the sign of a zero result.
+template <> __device__ __forceinline__ float mx2<float>(float a, float b) { return fmaxf(a, b); }
+template <> __device__ __forceinline__ float mn2<float>(float a, float b) { return fminf(a, b); }
 template <typename T> __device__ __forceinline__ T mx3(T a, T b, T c) { return mx2(mx2(a, b), c); }
 template <typename T> __device__ __forceinline__ T mn3(T a, T b, T c) { return mn2(mn2(a, b), c); }
 

@@ -193,15 +193,14 @@ int default_shape(int precision, int nx) {
     if (v >= 0 && v < crm::kNumShapes) return v;
   }
   // measured on 1024 columns of nx x 58 (column-steps/s):
-  //   FP64: 256 threads at 3 CTAs/SM (69K at nx 64; 2, 4 CTAs/SM and 512
-  //     threads are 1-12 % slower);
-  //   FP32-mixed: 256 threads at 4 CTAs/SM (362K at nx 64), with scratch
-  //     planes A/B in shared memory for nx <= 32 (+5 %; -7 % at nx 64, where
-  //     the planes cost more L1 than they save), 512 threads at 2 CTAs/SM
-  //     for nx >= 128 (+7 %).
+  //   FP64: 256 threads at 3 CTAs/SM (90K at nx 64; 4 CTAs/SM and 512
+  //     threads are 1-14 % slower);
+  //   FP32-mixed: 256 threads at 4 CTAs/SM with scratch planes A/B in
+  //     shared memory for nx <= 64 (920K at nx 32, 499K at nx 64: +2 % over
+  //     the planes in global memory), 512 threads at 2 CTAs/SM for
+  //     nx >= 128 (239K; the planes do not fit 4 CTAs/SM there).
   if (precision == CRM_FP64) return 0;
-  if (nx <= 32) return 2;
-  return nx >= 128 ? 3 : 1;
+  return nx >= 128 ? 3 : 2;
 }
 
 // crm_accel_nstop (accelerate_crm.F90:84-106): nstop / (1 + crm_accel_factor),
