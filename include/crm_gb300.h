@@ -243,9 +243,11 @@ int crm_debug_phase_cycles(crm_ctx *ctx, unsigned long long *out, int n);
  * register budget is sized for, scratch planes in shared memory): the search
  * space of an autotuner (crm_gb300/autotune.py).  FP64 results do not
  * depend on the shape; FP32-mixed results agree to FP32 rounding.  No counterpart in the reference (its OpenACC schedule is the
- * compiler's).  crm_set_launch_shape selects one for later calls on the
- * handle (-1: the measured default); CRM_ERR_ARG when out of range or not
- * launchable for this configuration. */
+ * compiler's).  By default a handle chooses per call: the shape with the
+ * most threads per column among those that hold the whole call at once
+ * (latency), else the measured throughput default.  crm_set_launch_shape
+ * fixes one for later calls (-1: back to the per-call choice); CRM_ERR_ARG
+ * when out of range or not launchable for this configuration. */
 int crm_num_launch_shapes(void);
 int crm_launch_shape_info(int shape, int *threads, int *ctas_per_sm, int *smem_planes);
 int crm_set_launch_shape(crm_ctx *ctx, int shape);
