@@ -255,6 +255,42 @@ struct ColumnKernel : NxDim<NX> {
     }
   }
 
+  // level_sums for NQ quantities that share their loads, FP64-accumulated:
+  // the FP64 form is level_sums with termq (bit-exact); the FP32-mixed form
+  // gives one warp a level, termv fills all NQ terms of a cell, and each
+  // quantity is reduced like level_sums (FP32 within groups of four lanes,
+  // FP64 across the groups).
+  template <int NQ, typename TermQ, typename TermV, typename Init, typename Out>
+  __device__ void level_sums_multi(int k0, int k1, TermQ termq, TermV termv, Init init, Out out) {
+    if constexpr (sizeof(T) == 8) {
+      level_sums(NQ, k0, k1, termq, init, out);
+    } else {
+      const int lane = TID & 31, warp = TID >> 5, nw = NT >> 5;
+      for (int k = k0 + warp; k <= k1; k += nw) {
+        T part[NQ];
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) part[q] = (T)0;
+        for (int i = 1 + lane; i <= nx; i += 32) {
+          T v[NQ];
+          termv(i, k, v);
+#pragma unroll
+          for (int q = 0; q < NQ; ++q) part[q] = part[q] + v[q];
+        }
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+          T x = part[q];
+          x = x + __shfl_xor_sync(0xffffffffu, x, 1);
+          x = x + __shfl_xor_sync(0xffffffffu, x, 2);
+          double sd = (double)x;
+          sd = sd + __shfl_xor_sync(0xffffffffu, sd, 4);
+          sd = sd + __shfl_xor_sync(0xffffffffu, sd, 8);
+          sd = sd + __shfl_xor_sync(0xffffffffu, sd, 16);
+          if (lane == 0) out(q, k, init(q, k) + sd);
+        }
+      }
+    }
+  }
+
   // Horizontal maxima (order-independent, hence exact in both forms): one
   // warp per (q, k) with a shuffle tree.
   template <typename Term, typename Out>
@@ -460,6 +496,16 @@ struct ColumnKernel : NxDim<NX> {
       S.ceaseflag = 0;
     }
     SYNC;
+    {
+      // crm_rad%qrad of this column, cached in the slab's sixth radiation
+      // plane (the GCM array is strided by ld; the heating is read every step)
+      const int nxr = p.L.nx_rad;
+      T *qr = base + p.L.rad + (size_t)5 * nxr * nzm;
+      for (int e = TID; e < nxr * nzm; e += NT) {
+        int ir = e % nxr, k = e / nxr;
+        qr[e] = (T)p.qrad[(size_t)icrm + (size_t)p.ld * (ir + (size_t)nxr * k)];
+      }
+    }
     // vertical grid (crm_module.F90:341-375)
     for (int k = TID + 1; k <= nzm; k += NT) {
       double z = IN(p.zmid, plev_ - k + 1) - IN(p.zint, plev_ + 1);
@@ -782,7 +828,7 @@ struct ColumnKernel : NxDim<NX> {
     // negative-vapour fixer: per-level sums (a cell outside a sum adds an
     // exact zero, which leaves a sum that starts at +0 unchanged)
     T *qneg = PR(P_TMP0), *qpoz = PR(P_TMP1), *nneg = PR(P_TMP2);
-    level_sums(3, 1, nzm,
+    level_sums_multi<3>(1, nzm,
                [&](int q, int i, int k) -> T {
                  T v = qt(i, k);
                  bool neg = v < (T)0.;
@@ -790,11 +836,18 @@ struct ColumnKernel : NxDim<NX> {
                  if (q == 1) return neg ? (T)0. : v;
                  return neg ? (T)1. : (T)0.;
                },
+               [&](int i, int k, T *r) {
+                 const T v = qt(i, k);
+                 const bool neg = v < (T)0.;
+                 r[0] = neg ? v : (T)0.;
+                 r[1] = neg ? (T)0. : v;
+                 r[2] = neg ? (T)1. : (T)0.;
+               },
                [&](int, int) { return 0.; },
                [&](int q, int k, double sv) { (q == 0 ? qneg : q == 1 ? qpoz : nneg)[k] = (T)sv; });
     SYNC;
-    const int gx = nx / p.L.nx_rad;
-    const double *qrad = p.qrad;
+    const int gx = nx / p.L.nx_rad, nxr = p.L.nx_rad;
+    const T *qrad = base + p.L.rad + (size_t)5 * nxr * nzm;    // (nx_rad, nzm), cached at init
     for (int e = TID; e < nx * nzm; e += NT) {
       int i = 1 + e % nx, k = 1 + e / nx;
       if (nneg[k] > (T)0. && qpoz[k] + qneg[k] > (T)0.) {
@@ -802,7 +855,7 @@ struct ColumnKernel : NxDim<NX> {
         qt(i, k) = mx2((T)0., qt(i, k) * factor);
       }
       int i_rad = (i - 1) / gx + 1;
-      T qr = (T)qrad[(size_t)icrm + (size_t)p.ld * ((i_rad - 1) + (size_t)p.L.nx_rad * (k - 1))];
+      T qr = qrad[(size_t)(k - 1) * nxr + (i_rad - 1)];
       t(i, k) = t(i, k) + qr * dtn;
     }
     SYNC;
