@@ -291,6 +291,28 @@ struct ColumnKernel : NxDim<NX> {
     }
   }
 
+  // FP32-mixed form: t and qt each carry a per-cell residue plane, the part
+  // of past increments that the FP32 value could not hold (t ~ 300 K lies on
+  // a 2^-15 K grid, and steady increments of a few grid steps would be
+  // rounded the same way every step; carrying the same residues for u, v, w
+  // was measured to change no output).  add_carry returns x + d with the
+  // residue r folded into the increment and leaves in r the rounding error
+  // of the result (TwoSum: exact at any magnitudes; it has no product, so no
+  // contraction applies).  The FP64 form has no residues (rct/rcq null).
+  __device__ __forceinline__ static T add_carry(T x, T d, T &r) {
+    const T y = d + r, s = x + y, yb = s - x;
+    r = (x - (s - yb)) + (y - yb);
+    return s;
+  }
+  __device__ __forceinline__ T *rct() const {
+    if constexpr (sizeof(T) == 4) return base + p.L.fcomp;
+    return nullptr;
+  }
+  __device__ __forceinline__ T *rcq() const {
+    if constexpr (sizeof(T) == 4) return base + p.L.fcomp + (size_t)nx * nzm;
+    return nullptr;
+  }
+
   // Horizontal maxima (order-independent, hence exact in both forms): one
   // warp per (q, k) with a shuffle tree.
   template <typename Term, typename Out>
@@ -817,10 +839,19 @@ struct ColumnKernel : NxDim<NX> {
     F2<T> t = TT(), qt = QT(), du = DU(S.na), dv = DV(S.na);
     const T dtn = (T)S.dtn;
     T *ttend = PR(P_TTEND), *qtend = PR(P_QTEND), *utend = PR(P_UTEND), *vtend = PR(P_VTEND);
+    // The FP32-mixed form adds the steady forcing through the carried
+    // residues (add_carry): rounded the same way every step, -1.5 K/day at
+    // dt 10 s would be biased by up to ~5 %.  Its t forcing is added after
+    // the fixer below, which does not read t.
+    T *rc_t = rct(), *rc_q = rcq();
     for (int e = TID; e < nx * nzm; e += NT) {
       int i = 1 + e % nx, k = 1 + e / nx;
-      t(i, k) = t(i, k) + ttend[k] * dtn;
-      qt(i, k) = qt(i, k) + qtend[k] * dtn;
+      if constexpr (sizeof(T) == 8) {
+        t(i, k) = t(i, k) + ttend[k] * dtn;
+        qt(i, k) = qt(i, k) + qtend[k] * dtn;
+      } else {
+        qt(i, k) = add_carry(qt(i, k), qtend[k] * dtn, rc_q[e]);
+      }
       du(i, k) = du(i, k) + utend[k];
       dv(i, k) = dv(i, k) + vtend[k];
     }
@@ -856,7 +887,11 @@ struct ColumnKernel : NxDim<NX> {
       }
       int i_rad = (i - 1) / gx + 1;
       T qr = qrad[(size_t)(k - 1) * nxr + (i_rad - 1)];
-      t(i, k) = t(i, k) + qr * dtn;
+      if constexpr (sizeof(T) == 8) {
+        t(i, k) = t(i, k) + qr * dtn;
+      } else {
+        t(i, k) = add_carry(t(i, k), ttend[k] * dtn + qr * dtn, rc_t[e]);
+      }
     }
     SYNC;
   }
@@ -895,8 +930,14 @@ struct ColumnKernel : NxDim<NX> {
         du(i, k) = du(i, k) - (u(i, k) - u0l[k]) * tau[k];
         dv(i, k) = dv(i, k) - (v(i, k) - v0l[k]) * tau[k];
         dw(i, k) = dw(i, k) - w(i, k) * tau[k];
-        t(i, k) = t(i, k) - dtn * (t(i, k) - t0l[k]) * tau[k];
-        qt(i, k) = qt(i, k) - dtn * (qv(i, k) - qv0[k]) * tau[k];
+        if constexpr (sizeof(T) == 8) {
+          t(i, k) = t(i, k) - dtn * (t(i, k) - t0l[k]) * tau[k];
+          qt(i, k) = qt(i, k) - dtn * (qv(i, k) - qv0[k]) * tau[k];
+        } else {
+          const size_t o = (size_t)(i - 1) + (size_t)nx * (k - 1);
+          t(i, k) = add_carry(t(i, k), -(dtn * (t(i, k) - t0l[k]) * tau[k]), rct()[o]);
+          qt(i, k) = add_carry(qt(i, k), -(dtn * (qv(i, k) - qv0[k]) * tau[k]), rcq()[o]);
+        }
       }
     }
     SYNC;
@@ -1555,7 +1596,7 @@ struct ColumnKernel : NxDim<NX> {
   // ADV_MPDATA/advect_scalar.F90:39-72 + advect_scalar2D.F90:60-240.
   // f is advected in place; fadv/flux (may be null) receive the per-level
   // advective tendency sum and vertical flux sum.
-  __device__ void advect_scalar(F2<T> f, T *fadv, T *flux) {
+  __device__ void advect_scalar(F2<T> f, T *fadv, T *flux, T *rc = nullptr) {
     F2<T> u = U(), w = W();
     F2<T> mx = SA(), mn = SB(), uuu = SCR(p.L.s_c), www = SCR(p.L.s_d), f0 = SCR(p.L.s_e);
     F2<T> wfl1 = SCR(p.L.s_f);
@@ -1588,7 +1629,15 @@ struct ColumnKernel : NxDim<NX> {
     for (int e = TID; e < (nx + 4) * nzm; e += NT) {
       int i = -1 + e % (nx + 4), k = 1 + e / (nx + 4);   // -1 .. nx+2
       T iadz = PR(P_IADZ)[k], irho = PR(P_IRHO)[k];
-      f(i, k) = f(i, k) - (uuu(i + 1, k) - uuu(i, k) + (www(i, k + 1) - www(i, k)) * iadz) * irho;
+      const T c1 = (uuu(i + 1, k) - uuu(i, k) + (www(i, k + 1) - www(i, k)) * iadz) * irho;
+      if (sizeof(T) == 4 && rc && i >= 1 && i <= nx) {
+        // the residue keeps this rounding error (the next update folds it in)
+        T err = (T)0.;
+        f(i, k) = add_carry(f(i, k), -c1, err);
+        rc[(i - 1) + nx * (k - 1)] += err;
+      } else {
+        f(i, k) = f(i, k) - c1;
+      }
     }
     SYNC;
     // antidiffusive velocities (andiff, across)
@@ -1660,7 +1709,16 @@ struct ColumnKernel : NxDim<NX> {
     for (int e = TID; e < nx * nzm; e += NT) {
       int i = 1 + e % nx, k = 1 + e / nx;
       T iadz = PR(P_IADZ)[k], irho = PR(P_IRHO)[k];
-      f(i, k) = mx2((T)0., f(i, k) - (uuu(i + 1, k) - uuu(i, k) + (www(i, k + 1) - www(i, k)) * iadz) * irho);
+      const T c2 = (uuu(i + 1, k) - uuu(i, k) + (www(i, k + 1) - www(i, k)) * iadz) * irho;
+      if (sizeof(T) == 4 && rc) {
+        T r = rc[e];
+        T s = add_carry(f(i, k), -c2, r);
+        if (!(s > (T)0.)) { s = (T)0.; r = (T)0.; }   // the positive-definite clip
+        rc[e] = r;
+        f(i, k) = s;
+      } else {
+        f(i, k) = mx2((T)0., f(i, k) - c2);
+      }
     }
     SYNC;
     if (fadv) {
@@ -1827,7 +1885,7 @@ struct ColumnKernel : NxDim<NX> {
 
   // ---------------------------------------------------------- SGS scalar diffusion
   // SGS_TKE/diffuse_scalar.F90:33-72 + diffuse_scalar2D.F90:44-140
-  __device__ void diffuse_scalar(F2<T> f, T *fdiff, T *flux) {
+  __device__ void diffuse_scalar(F2<T> f, T *fdiff, T *flux, T *rc = nullptr) {
     F2<T> tkh = TKH(), flx = SA(), dfdt = SB(), f0 = SCR(p.L.s_c);
     T *rho = PR(P_RHO), *rhow = PR(P_RHOW), *adz = PR(P_ADZ), *adzw = PR(P_ADZW);
     T *grdfx = PR(P_GRDFX), *grdfz = PR(P_GRDFZ);
@@ -1874,7 +1932,8 @@ struct ColumnKernel : NxDim<NX> {
       int kb = k - 1;
       T rhoi = PR(P_IRHOADZ)[k];
       T d = dtn * (dfdt(i, k) - (flx(i, k) - flx(i, kb)) * rhoi);
-      f(i, k) = f(i, k) + d;
+      if (sizeof(T) == 4 && rc) f(i, k) = add_carry(f(i, k), d, rc[e]);
+      else f(i, k) = f(i, k) + d;
     }
     SYNC;
     if (fdiff) {
@@ -2589,9 +2648,9 @@ struct ColumnKernel : NxDim<NX> {
         adams();
         boundaries(2);
         PHASE_MARK(PH_ADAMS);
-        advect_scalar(TT(), nullptr, nullptr);
+        advect_scalar(TT(), nullptr, nullptr, rct());
         PHASE_MARK(PH_ADV_T);
-        advect_scalar(QT(), PR(P_MKADV0), PR(P_MKWLE0));
+        advect_scalar(QT(), PR(P_MKADV0), PR(P_MKWLE0), rcq());
         PHASE_MARK(PH_ADV_QT);
         advect_scalar(QP(), PR(P_MKADV1), PR(P_MKWLE1));
         PHASE_MARK(PH_ADV_QP);
@@ -2602,9 +2661,9 @@ struct ColumnKernel : NxDim<NX> {
         uvw();
         boundaries(3);
         PHASE_MARK(PH_UVW);
-        diffuse_scalar(TT(), nullptr, nullptr);
+        diffuse_scalar(TT(), nullptr, nullptr, rct());
         PHASE_MARK(PH_DIFF_T);
-        diffuse_scalar(QT(), PR(P_MKDIFF0), PR(P_MKWSB0));
+        diffuse_scalar(QT(), PR(P_MKDIFF0), PR(P_MKWSB0), rcq());
         diffuse_scalar(QP(), PR(P_MKDIFF1), PR(P_MKWSB1));
         PHASE_MARK(PH_DIFF_Q);
         if (S.icycle == 1) precip_init();

@@ -35,6 +35,7 @@ struct Layout {
   size_t rad;            // rad accumulators 5 x (nx_rad x nzm) + qrad
   size_t rnd;            // setperturb random numbers 5 x nx
   size_t colstat;        // per-column scratch for step statistics, 8 x nx
+  size_t fcomp;          // FP32-mixed form only: carried residues of t, qt (2 x nx x nzm)
   size_t tri;            // FP64 tridiagonal factors (see tridiag_factor)
   size_t slab;           // total elements per column
 };
@@ -116,6 +117,7 @@ inline Layout make_layout(int nx, int nzm, int plev, int nx_rad, int esz) {
   L.rad = take((size_t)6 * nx_rad * nzm);
   L.rnd = take((size_t)5 * nx);
   L.colstat = take((size_t)8 * nx);
+  L.fcomp = esz == 4 ? take((size_t)2 * nx * nzm) : 0;
   {
     size_t nd = (size_t)(nzm + 1) + (size_t)(nx + 1) * 2 * (nzm + 1) + (size_t)(nx + 1);
     L.tri = take(nd * 8 / esz + 2);

@@ -285,12 +285,17 @@ def main():
     value64 = ws * colsteps / (ms64 / 1000.0)
 
     # ---- accuracy of the FP32-mixed form against the FP64 form (same inputs)
-    errs = {}
-    for n in ('temperature', 'qt', 'u_wind', 'w_wind', 'qp'):
-        a = dev32.state_numpy(n)[:NCRMS].astype(np.float64)
-        b = dev64.state_numpy(n)[:NCRMS]
+    # (the FP64 form equals the oracle bit for bit, so this is the error
+    # against the oracle): every state field and every crm() output
+    def rel(a, b):
         den = np.linalg.norm(b)
-        errs[n] = float(np.linalg.norm(a - b) / den) if den > 0 else float(np.linalg.norm(a - b))
+        return float(np.linalg.norm(a - b) / den) if den > 0 else float(np.linalg.norm(a - b))
+
+    errs, errs_out = {}, {}
+    for n in st.arrays():
+        errs[n] = rel(dev32.state_numpy(n)[:NCRMS].astype(np.float64), dev64.state_numpy(n)[:NCRMS])
+    for n in T.CrmOutput(1, 64, 1, 58, 72).arrays():
+        errs_out[n] = rel(dev32.out_numpy(n)[:NCRMS].astype(np.float64), dev64.out_numpy(n)[:NCRMS])
 
     # ---- serving: Poisson chunks of mixed (nx, nz) at 80 % of the closed-loop peak
     serving = None
@@ -362,6 +367,7 @@ def main():
         'fp64_plain': {'value': value64, 'unit': UNIT, 'ms_per_step': ms64, 'steps': args.fp64_steps},
         'fp32_over_fp64': value / value64,
         'fp32_rel_l2_vs_fp64_state': errs,
+        'fp32_rel_l2_vs_fp64_outputs': errs_out,
         'serving': serving,
         'launch_shapes': tuned,
     }

@@ -1,10 +1,11 @@
 """FP32-mixed form against the FP64 oracle.
 
 The mixed form keeps FP64 only for the pressure tridiagonal solve, the domain
-sums and the saturation-adjustment Newton iteration.  After one GCM step
-(60-120 CRM steps of a convecting boundary layer) rounding differences grow
-chaotically, so the comparison is statistical: relative L2 error per field,
-with the bounds stated below, plus exact agreement of the status codes.
+sums and the saturation-adjustment Newton iteration; t and qt carry per-cell
+FP32 residues of their updates.  After one GCM step (60-120 CRM steps of a
+convecting boundary layer) rounding differences have been amplified by the
+flow, so the comparison is statistical: relative L2 error per field, with the
+bounds stated below, plus exact agreement of the status codes.
 """
 import numpy as np
 import pytest
@@ -18,9 +19,15 @@ from conftest import rel_l2
 
 pytestmark = pytest.mark.gpu
 
-# relative L2 bounds after one GCM step (state fields and GCM tendencies)
-BOUNDS = {'temperature': 1e-4, 'qt': 1e-2, 'u_wind': 1e-1, 'w_wind': 1.0, 'qp': 1.0,
-          'sltend': 5e-1, 'qltend': 1.0}
+# relative L2 bounds after one GCM step: state fields and GCM tendencies
+# (measured 1e-7..9e-4; every other crm() output is held to OUTPUT_BOUND,
+# measured <= 6e-3)
+BOUNDS = {'temperature': 2e-6, 'qt': 3e-5, 'u_wind': 1e-4, 'w_wind': 5e-3, 'qp': 5e-4,
+          'sltend': 2e-3, 'qltend': 1e-3, 'qcltend': 1e-3, 'qiltend': 1e-3}
+OUTPUT_BOUND = 3e-2
+# the tendency target (1e-4 relative L2), met where the GCM step's
+# temperature change is large against FP32 resolution of the static energy
+TENDENCY_TARGET = 1e-4
 
 
 def _errors(wl, **kw):
@@ -35,26 +42,34 @@ def _errors(wl, **kw):
     st_g, rad_g = st.copy(), rad.copy()
     ctx.run(desc, cin, st_g, rad_g, out_g, raise_on_error=True)
     e = {n: rel_l2(getattr(st_g, n), getattr(st_o, n)) for n in ('temperature', 'qt', 'u_wind', 'w_wind', 'qp')}
-    e['sltend'] = rel_l2(out_g.sltend, out_o.sltend)
-    e['qltend'] = rel_l2(out_g.qltend, out_o.qltend)
     for n, a in out_g.arrays().items():
         assert np.isfinite(a).all(), n
+        e[n] = rel_l2(a, getattr(out_o, n))
     return e
+
+
+def _check(e):
+    for n, b in BOUNDS.items():
+        assert e[n] <= b, (n, e[n], b)
+    for n, v in e.items():
+        assert v <= OUTPUT_BOUND, (n, v, OUTPUT_BOUND)
 
 
 @pytest.mark.parametrize('moist', [False, True])
 def test_fp32_mixed_workload0(gpu_lib, moist):
     e = _errors(S.workload0, ncrms=4, moist=moist)
     print('fp32-mixed rel-L2 vs fp64 oracle (32x28, moist=%s):' % moist, e)
-    for n, b in BOUNDS.items():
-        assert e[n] <= b, (n, e[n], b)
+    _check(e)
+    if moist:
+        for n in ('sltend', 'qltend', 'qcltend', 'qiltend'):
+            assert e[n] <= TENDENCY_TARGET, (n, e[n])
 
 
 def test_fp32_mixed_workload1(gpu_lib):
     e = _errors(S.workload1, ncrms=4)
     print('fp32-mixed rel-L2 vs fp64 oracle (64x58):', e)
-    for n, b in BOUNDS.items():
-        assert e[n] <= b, (n, e[n], b)
+    _check(e)
+    assert e['qltend'] <= TENDENCY_TARGET, e['qltend']
 
 
 def test_fp32_mixed_mean_state_acceleration(gpu_lib):
@@ -64,8 +79,7 @@ def test_fp32_mixed_mean_state_acceleration(gpu_lib):
         return cfg, cin, st, rad, desc
     e = _errors(wl, ncrms=4, moist=True)
     print('fp32-mixed rel-L2 vs fp64 oracle (32x28, accelerated):', e)
-    for n, b in BOUNDS.items():
-        assert e[n] <= b, (n, e[n], b)
+    _check(e)
 
 
 def test_fp32_mixed_water_budget(gpu_lib):
