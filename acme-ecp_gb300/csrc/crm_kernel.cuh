@@ -1444,7 +1444,10 @@ struct ColumnKernel : NxDim<NX> {
   __device__ double *TRI() const { return reinterpret_cast<double *>(base + p.L.tri); }
   __device__ void tridiag_factor() {
     const int np = nx + 1, ls = nzm + 1;
-    double *tri = TRI();        // [a(k)] + np x ([alfa(k)] [e(k)]) + np last pivots
+    // [a(k)], then alfa(k, i) and e(k, i) with the Fourier index i fastest
+    // (the solve runs one coefficient per thread, so its loads coalesce), then
+    // the np last pivots
+    double *tri = TRI();
     double *ak = tri;
     T *rho = PR(P_RHO), *rhow = PR(P_RHOW), *adz = PR(P_ADZ), *adzw = PR(P_ADZW);
     const double dz = S.dz;
@@ -1452,7 +1455,9 @@ struct ColumnKernel : NxDim<NX> {
       ak[k] = (double)rhow[k] / ((double)adz[k] * (double)adzw[k] * dz * dz);
     SYNC;
     for (int i = TID + 1; i <= np; i += NT) {
-      double *al = tri + (size_t)ls + (size_t)(i - 1) * 2 * ls, *e = al + ls;
+      double *alb = tri + (size_t)ls + (i - 1), *eb = alb + (size_t)ls * np;
+      auto al = [&](int k) -> double & { return alb[(size_t)k * np]; };
+      auto e = [&](int k) -> double & { return eb[(size_t)k * np]; };
       int id = (int)(((float)i - 0.1f) / 2.0f);
       double eign = p.eign[i - 1];
       double a1 = ak[1];
@@ -1460,17 +1465,19 @@ struct ColumnKernel : NxDim<NX> {
       double b;
       if (id == 0) b = 1. / (eign * (double)rho[1] - a1 - c1);
       else b = 1. / (eign * (double)rho[1] - c1);
-      al[1] = -c1 * b;
-      e[1] = b;
+      al(1) = -c1 * b;
+      e(1) = b;
+      double alprev = -c1 * b;
       for (int k = 2; k <= nzm - 1; ++k) {
         double a = ak[k];
         double c = (double)rhow[k + 1] / ((double)adz[k] * (double)adzw[k + 1] * dz * dz);
-        double ee = 1. / (eign * (double)rho[k] - a - c + a * al[k - 1]);
-        al[k] = -c * ee;
-        e[k] = ee;
+        double ee = 1. / (eign * (double)rho[k] - a - c + a * alprev);
+        alprev = -c * ee;
+        al(k) = alprev;
+        e(k) = ee;
       }
       double an = ak[nzm];
-      tri[(size_t)ls + (size_t)np * 2 * ls + (i - 1)] = eign * (double)rho[nzm] - an + an * al[nzm - 1];
+      tri[(size_t)ls + (size_t)np * 2 * ls + (i - 1)] = eign * (double)rho[nzm] - an + an * alprev;
     }
     SYNC;
   }
@@ -1512,22 +1519,52 @@ struct ColumnKernel : NxDim<NX> {
     {
       const int np = nx + 1, ls = nzm + 1;
       const double *tri = TRI();
-      double *beta = reinterpret_cast<double *>(sa());   // np x (nzm+1) doubles
+      double *beta = reinterpret_cast<double *>(sa());   // (nzm+1) x np doubles, i fastest
       for (int i = TID + 1; i <= np; i += NT) {
-        const double *al = tri + (size_t)ls + (size_t)(i - 1) * 2 * ls, *e = al + ls;
-        double *be = beta + (size_t)(i - 1) * ls;
+        const double *al = tri + (size_t)ls + (i - 1), *e = al + (size_t)ls * np;
+        double *be = beta + (i - 1);
         T *ff = fsh + (i - 1);
-        double bprev = (double)ff[0] * e[1];
-        be[1] = bprev;
-        for (int k = 2; k <= nzm - 1; ++k) {
-          bprev = ((double)ff[(size_t)nx2 * (k - 1)] - tri[k] * bprev) * e[k];
-          be[k] = bprev;
+        double bprev = (double)ff[0] * e[np];
+        be[np] = bprev;
+        // the recurrences are serial in k: the loads of each group of
+        // levels are issued together, ahead of its arithmetic (the stores
+        // to be/ff could alias them, so the compiler would not hoist them)
+        constexpr int G = 4;
+        for (int k0 = 2; k0 <= nzm - 1; k0 += G) {
+          double ev[G], tv[G];
+          T fv[G];
+#pragma unroll
+          for (int j = 0; j < G; ++j) {
+            const int k = min(k0 + j, nzm - 1);
+            ev[j] = e[(size_t)k * np];
+            tv[j] = tri[k];
+            fv[j] = ff[(size_t)nx2 * (k - 1)];
+          }
+#pragma unroll
+          for (int j = 0; j < G; ++j) {
+            if (k0 + j <= nzm - 1) {
+              bprev = ((double)fv[j] - tv[j] * bprev) * ev[j];
+              be[(size_t)(k0 + j) * np] = bprev;
+            }
+          }
         }
         double fk = ((double)ff[(size_t)nx2 * (nzm - 1)] - tri[nzm] * bprev) / tri[(size_t)ls + (size_t)np * 2 * ls + (i - 1)];
         ff[(size_t)nx2 * (nzm - 1)] = (T)fk;
-        for (int k = nzm - 1; k >= 1; --k) {
-          fk = al[k] * fk + be[k];
-          ff[(size_t)nx2 * (k - 1)] = (T)fk;
+        for (int k0 = nzm - 1; k0 >= 1; k0 -= G) {
+          double av[G], bv[G];
+#pragma unroll
+          for (int j = 0; j < G; ++j) {
+            const int k = max(k0 - j, 1);
+            av[j] = al[(size_t)k * np];
+            bv[j] = be[(size_t)k * np];
+          }
+#pragma unroll
+          for (int j = 0; j < G; ++j) {
+            if (k0 - j >= 1) {
+              fk = av[j] * fk + bv[j];
+              ff[(size_t)nx2 * (k0 - j - 1)] = (T)fk;
+            }
+          }
         }
       }
     }
