@@ -79,7 +79,7 @@ namespace crm {
 
 // per-CTA scalars of the column being integrated
 struct ColShared {
-  int na, nb, nc, ncycle, icycle, nprec, status, kmin, kmax, n_damp, col;
+  int na, nb, nc, ncycle, icycle, nprec, prec_any, status, kmin, kmax, n_damp, col;
   double dt3[3], at, bt, ct, dtn, dtfactor, dz, cfl, prec_cfl, z0;
   double colprec0, colprecs0;
   double cltot, clhgh, clmed, cllow;
@@ -1808,6 +1808,7 @@ struct ColumnKernel : NxDim<NX> {
     // the maximum is taken in T and widened once (widening is exact and
     // monotone, so the result equals a maximum of widened values)
     T cflt = (T)0.;
+    int moving = 0;
     for (int e = TID; e < nx * nzm; e += NT) {
       int i = 1 + e % nx, k = 1 + e / nx;
       omega(i, k) = mx2((T)0., mn2((T)1., (tabs(i, k) - (T)C_TPRMIN) * (T)p.a_pr));
@@ -1815,11 +1816,19 @@ struct ColumnKernel : NxDim<NX> {
       T wv = rhofac[k] * tmp;
       cflt = mx2(cflt, wv * iwmax[k]);
       wp(i, k) = -wv * rhow[k] * dtn / dz;
+      moving |= (wv != (T)0.);
     }
+    // With every fall speed zero (wp = -0 everywhere) the sedimentation
+    // sub-steps change no bit of qp, t, the surface precipitation or the
+    // qpfall/precflux sums (every flux works out to +0 and every update adds
+    // or subtracts a zero to a value it leaves unchanged, signs of zero
+    // included), so precip_fall_2 is skipped for such a column.
+    moving = __syncthreads_or(moving);
     double cfl = block_max((double)cflt);
     const double cfl_b = batch_max(cfl);
     if (TID == 0) {
       S.prec_cfl = cfl;
+      S.prec_any = moving;
       S.nprec = (cfl_b > R4(0.9)) ? (int)ceil(cfl_b / R4(0.9)) : 1;
     }
     SYNC;
@@ -2693,7 +2702,7 @@ struct ColumnKernel : NxDim<NX> {
         PHASE_MARK(PH_ADV_QP);
         precip_fall_1();
         PHASE_MARK(PH_FALL1);
-        precip_fall_2(S.nprec);
+        if (S.prec_any) precip_fall_2(S.nprec);
         PHASE_MARK(PH_FALL2);
         uvw();
         boundaries(3);
