@@ -1633,6 +1633,30 @@ struct ColumnKernel : NxDim<NX> {
   // ADV_MPDATA/advect_scalar.F90:39-72 + advect_scalar2D.F90:60-240.
   // f is advected in place; fadv/flux (may be null) receive the per-level
   // advective tendency sum and vertical flux sum.
+  // True when every stored value of a scalar field (x halos included) is +0
+  // bit for bit.  Advection (MPDATA) and SGS diffusion of such a field leave
+  // every bit of it unchanged and give +0 for their statistics (every flux is
+  // a signed zero, every update adds or subtracts a zero to +0), so a column
+  // without precipitating water skips both for qp.
+  __device__ bool all_pos_zero(F2<T> f) {
+    int nonzero = 0;
+    for (int e = TID; e < (nx + 6) * nzm; e += NT) {
+      const int i = -2 + e % (nx + 6), k = 1 + e / (nx + 6);
+      const T v = f(i, k);
+      if constexpr (sizeof(T) == 8) nonzero |= (__double_as_longlong(v) != 0);
+      else nonzero |= (__float_as_uint(v) != 0u);
+    }
+    return !__syncthreads_or(nonzero);
+  }
+  // the statistics a skipped advection or diffusion of a zero field gives
+  __device__ void zero_stats(T *a, T *b) {
+    for (int k = TID + 1; k <= nzm; k += NT) {
+      if (a) a[k] = (T)0.;
+      if (b) b[k] = (T)0.;
+    }
+    SYNC;
+  }
+
   __device__ void advect_scalar(F2<T> f, T *fadv, T *flux, T *rc = nullptr) {
     F2<T> u = U(), w = W();
     F2<T> mx = SA(), mn = SB(), uuu = SCR(p.L.s_c), www = SCR(p.L.s_d), f0 = SCR(p.L.s_e);
@@ -2698,7 +2722,8 @@ struct ColumnKernel : NxDim<NX> {
         PHASE_MARK(PH_ADV_T);
         advect_scalar(QT(), PR(P_MKADV0), PR(P_MKWLE0), rcq());
         PHASE_MARK(PH_ADV_QT);
-        advect_scalar(QP(), PR(P_MKADV1), PR(P_MKWLE1));
+        if (all_pos_zero(QP())) zero_stats(PR(P_MKADV1), PR(P_MKWLE1));
+        else advect_scalar(QP(), PR(P_MKADV1), PR(P_MKWLE1));
         PHASE_MARK(PH_ADV_QP);
         precip_fall_1();
         PHASE_MARK(PH_FALL1);
@@ -2710,7 +2735,8 @@ struct ColumnKernel : NxDim<NX> {
         diffuse_scalar(TT(), nullptr, nullptr, rct());
         PHASE_MARK(PH_DIFF_T);
         diffuse_scalar(QT(), PR(P_MKDIFF0), PR(P_MKWSB0), rcq());
-        diffuse_scalar(QP(), PR(P_MKDIFF1), PR(P_MKWSB1));
+        if (all_pos_zero(QP())) zero_stats(PR(P_MKDIFF1), PR(P_MKWSB1));
+        else diffuse_scalar(QP(), PR(P_MKDIFF1), PR(P_MKWSB1));
         PHASE_MARK(PH_DIFF_Q);
         if (S.icycle == 1) precip_init();
         PHASE_MARK(PH_PINIT);
