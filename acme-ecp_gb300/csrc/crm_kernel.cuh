@@ -1633,6 +1633,22 @@ struct ColumnKernel : NxDim<NX> {
   // ADV_MPDATA/advect_scalar.F90:39-72 + advect_scalar2D.F90:60-240.
   // f is advected in place; fadv/flux (may be null) receive the per-level
   // advective tendency sum and vertical flux sum.
+  // Runs a pass over cells e = TID, TID + NT, ... < n two cells per thread at
+  // a time: calc(e) only loads and computes, put(e, r) only stores, so both
+  // cells' loads are in flight together (stores through the field pointers
+  // would otherwise keep the compiler from hoisting the second cell's loads).
+  template <typename Calc, typename Put>
+  __device__ __forceinline__ void for_cells2(int n, Calc calc, Put put) {
+    int e = TID;
+    for (; e + NT < n; e += 2 * NT) {
+      const auto r0 = calc(e);
+      const auto r1 = calc(e + NT);
+      put(e, r0);
+      put(e + NT, r1);
+    }
+    if (e < n) put(e, calc(e));
+  }
+
   // True when every stored value of a scalar field (x halos included) is +0
   // bit for bit.  Advection (MPDATA) and SGS diffusion of such a field leave
   // every bit of it unchanged and give +0 for their statistics (every flux is
@@ -1663,124 +1679,167 @@ struct ColumnKernel : NxDim<NX> {
     F2<T> wfl1 = SCR(p.L.s_f);
     T *rho = PR(P_RHO), *adz = PR(P_ADZ), *rhow = PR(P_RHOW);
     const T eps = (T)R4(1.e-10);
+    // Every pass gathers from other cells and writes only its own cell, so
+    // each runs two cells per thread at a time (for_cells2: both cells'
+    // loads are issued before either's stores).
     // f0, mx/mn from the initial field, upwind fluxes
-    // (every input is loaded into registers before the first store: the
-    // stores go through pointers the compiler must assume may alias f)
-    for (int e = TID; e < (nx + 5) * nzm; e += NT) {
-      int i = -1 + e % (nx + 5), k = 1 + e / (nx + 5);   // i = -1 .. nx+3
-      int kc = min(nzm, k + 1), kb = max(1, k - 1);
-      const T fk = f(i, k), fb = f(i - 1, k), uk = u(i, k);
-      const bool in_w = i <= nx + 2, in_m = i >= 0 && i <= nx + 1;
-      const T fkb = in_w ? f(i, kb) : (T)0., wk = in_w ? w(i, k) : (T)0.;
-      const T fc = in_m ? f(i + 1, k) : (T)0., fkc = in_m ? f(i, kc) : (T)0.;
-      if (in_m) {
-        mx(i, k) = mx2(mx2(mx2(mx2(fb, fc), fkb), fkc), fk);
-        mn(i, k) = mn2(mn2(mn2(mn2(fb, fc), fkb), fkc), fk);
-      }
-      if (fadv && i >= 1 && i <= nx) f0(i, k) = fk;
-      uuu(i, k) = mx2((T)0., uk) * fb + mn2((T)0., uk) * fk;
-      if (in_w) www(i, k) = mx2((T)0., wk) * fkb + mn2((T)0., wk) * fk;
-      if (k == 1 && in_w) www(i, nz) = (T)0.;
-    }
+    struct R1 { int i, k; T mx, mn, fk, uuu, www; };
+    for_cells2((nx + 5) * nzm,
+      [&](int e) -> R1 {
+        R1 r;
+        r.i = -1 + e % (nx + 5); r.k = 1 + e / (nx + 5);    // i = -1 .. nx+3
+        const int i = r.i, k = r.k, kc = min(nzm, k + 1), kb = max(1, k - 1);
+        const T fk = f(i, k), fb = f(i - 1, k), uk = u(i, k);
+        const bool in_w = i <= nx + 2, in_m = i >= 0 && i <= nx + 1;
+        const T fkb = in_w ? f(i, kb) : (T)0., wk = in_w ? w(i, k) : (T)0.;
+        const T fc = in_m ? f(i + 1, k) : (T)0., fkc = in_m ? f(i, kc) : (T)0.;
+        r.mx = mx2(mx2(mx2(mx2(fb, fc), fkb), fkc), fk);
+        r.mn = mn2(mn2(mn2(mn2(fb, fc), fkb), fkc), fk);
+        r.fk = fk;
+        r.uuu = mx2((T)0., uk) * fb + mn2((T)0., uk) * fk;
+        r.www = mx2((T)0., wk) * fkb + mn2((T)0., wk) * fk;
+        return r;
+      },
+      [&](int, const R1 &r) {
+        const int i = r.i, k = r.k;
+        const bool in_w = i <= nx + 2, in_m = i >= 0 && i <= nx + 1;
+        if (in_m) { mx(i, k) = r.mx; mn(i, k) = r.mn; }
+        if (fadv && i >= 1 && i <= nx) f0(i, k) = r.fk;
+        uuu(i, k) = r.uuu;
+        if (in_w) {
+          www(i, k) = r.www;
+          if (k == 1) www(i, nz) = (T)0.;
+        }
+      });
     SYNC;
-    // first-pass (upwind) vertical flux sum, then the upwind update
+    // first-pass (upwind) vertical flux sum, then the upwind update; the
+    // residue keeps the update's rounding error (the next update folds it in)
     if (flux)
       level_sums_lo(1, 1, nzm, [&](int, int i, int k) -> T { return www(i, k); },
                  [&](int, int) { return 0.; }, [&](int, int k, double sv) { wfl1(0, k) = (T)sv; });
-    for (int e = TID; e < (nx + 4) * nzm; e += NT) {
-      int i = -1 + e % (nx + 4), k = 1 + e / (nx + 4);   // -1 .. nx+2
-      T iadz = PR(P_IADZ)[k], irho = PR(P_IRHO)[k];
-      const T c1 = (uuu(i + 1, k) - uuu(i, k) + (www(i, k + 1) - www(i, k)) * iadz) * irho;
-      if (sizeof(T) == 4 && rc && i >= 1 && i <= nx) {
-        // the residue keeps this rounding error (the next update folds it in)
-        T err = (T)0.;
-        f(i, k) = add_carry(f(i, k), -c1, err);
-        rc[(i - 1) + nx * (k - 1)] += err;
-      } else {
-        f(i, k) = f(i, k) - c1;
-      }
-    }
+    struct R2 { int i, k; T fn, err; };
+    for_cells2((nx + 4) * nzm,
+      [&](int e) -> R2 {
+        R2 r;
+        r.i = -1 + e % (nx + 4); r.k = 1 + e / (nx + 4);    // -1 .. nx+2
+        const int i = r.i, k = r.k;
+        const T iadz = PR(P_IADZ)[k], irho = PR(P_IRHO)[k];
+        const T c1 = (uuu(i + 1, k) - uuu(i, k) + (www(i, k + 1) - www(i, k)) * iadz) * irho;
+        r.err = (T)0.;
+        if (sizeof(T) == 4 && rc && i >= 1 && i <= nx) r.fn = add_carry(f(i, k), -c1, r.err);
+        else r.fn = f(i, k) - c1;
+        return r;
+      },
+      [&](int, const R2 &r) {
+        f(r.i, r.k) = r.fn;
+        if (sizeof(T) == 4 && rc && r.i >= 1 && r.i <= nx) rc[(r.i - 1) + nx * (r.k - 1)] += r.err;
+      });
     SYNC;
     // antidiffusive velocities (andiff, across)
-    for (int e = TID; e < (nx + 3) * nzm; e += NT) {
-      int i = e % (nx + 3), k = 1 + e / (nx + 3);          // 0 .. nx+2
-      int kc = min(nzm, k + 1), kb = max(1, k - 1);
-      T irho = PR(P_IRHO)[k];
-      T irhow = PR(P_IRHOWADZ)[k];
-      T dd = PR(P_MPDD)[k];
-      int ib = i - 1;
-      T uval, wval = (T)0.;
-      {
-        T a = u(i, k), x1 = f(ib, k), x2 = f(i, k);
-        T andiff = (tabs_(a) - a * a * irho) * (T)0.5 * (x2 - x1);
-        T ax1 = dd * (f(ib, kc) + f(i, kc) - f(ib, kb) - f(i, kb));
-        T a2 = w(ib, k) + w(ib, kc) + w(i, k) + w(i, kc);
-        T across = (T)0.03125 * a * a2 * ax1;
-        uval = andiff - across * irho;
-      }
-      if (i <= nx + 1) {
-        int ic = i + 1;
-        T a = w(i, k), x1 = f(i, kb), x2 = f(i, k);
-        T andiff = (tabs_(a) - a * a * irhow) * (T)0.5 * (x2 - x1);
-        T ax1 = f(ic, kb) + f(ic, k) - f(ib, kb) - f(ib, k);
-        T a2 = u(i, kb) + u(i, k) + u(ic, k) + u(ic, kb);
-        T across = (T)0.03125 * a * a2 * ax1;
-        wval = (k == 1) ? (T)0. : andiff - across * irho;
-      }
-      uuu(i, k) = uval;                      // stores after every load
-      if (i <= nx + 1) www(i, k) = wval;
-    }
+    struct R3 { int i, k; T uval, wval; };
+    for_cells2((nx + 3) * nzm,
+      [&](int e) -> R3 {
+        R3 r;
+        r.i = e % (nx + 3); r.k = 1 + e / (nx + 3);          // 0 .. nx+2
+        const int i = r.i, k = r.k, kc = min(nzm, k + 1), kb = max(1, k - 1), ib = i - 1;
+        const T irho = PR(P_IRHO)[k], irhow = PR(P_IRHOWADZ)[k], dd = PR(P_MPDD)[k];
+        {
+          T a = u(i, k), x1 = f(ib, k), x2 = f(i, k);
+          T andiff = (tabs_(a) - a * a * irho) * (T)0.5 * (x2 - x1);
+          T ax1 = dd * (f(ib, kc) + f(i, kc) - f(ib, kb) - f(i, kb));
+          T a2 = w(ib, k) + w(ib, kc) + w(i, k) + w(i, kc);
+          T across = (T)0.03125 * a * a2 * ax1;
+          r.uval = andiff - across * irho;
+        }
+        r.wval = (T)0.;
+        if (i <= nx + 1) {
+          int ic = i + 1;
+          T a = w(i, k), x1 = f(i, kb), x2 = f(i, k);
+          T andiff = (tabs_(a) - a * a * irhow) * (T)0.5 * (x2 - x1);
+          T ax1 = f(ic, kb) + f(ic, k) - f(ib, kb) - f(ib, k);
+          T a2 = u(i, kb) + u(i, k) + u(ic, k) + u(ic, kb);
+          T across = (T)0.03125 * a * a2 * ax1;
+          r.wval = (k == 1) ? (T)0. : andiff - across * irho;
+        }
+        return r;
+      },
+      [&](int, const R3 &r) {
+        uuu(r.i, r.k) = r.uval;
+        if (r.i <= nx + 1) www(r.i, r.k) = r.wval;
+      });
     SYNC;
     // non-oscillatory limiter
-    for (int e = TID; e < (nx + 2) * nzm; e += NT) {
-      int i = e % (nx + 2), k = 1 + e / (nx + 2);          // 0 .. nx+1
-      int kc = min(nzm, k + 1), kb = max(1, k - 1), ib = i - 1, ic = i + 1;
-      T iadz = PR(P_IADZ)[k];
-      T m1 = mx2(mx2(mx2(mx2(mx2(f(ib, k), f(ic, k)), f(i, kb)), f(i, kc)), f(i, k)), mx(i, k));
-      T m2 = mn2(mn2(mn2(mn2(mn2(f(ib, k), f(ic, k)), f(i, kb)), f(i, kc)), f(i, k)), mn(i, k));
-      const T fk = f(i, k), uc = uuu(ic, k), ui = uuu(i, k), wc = www(i, kc), wi = www(i, k);
-      T pu_c = -mn2((T)0., uc), pu_i = mx2((T)0., ui);
-      T pw_c = -mn2((T)0., wc), pw_i = mx2((T)0., wi);
-      const T mxv = rho[k] * (m1 - fk) / (pu_c + pu_i + iadz * (pw_c + pw_i) + eps);
-      T qu_c = mx2((T)0., uc), qu_i = -mn2((T)0., ui);
-      T qw_c = mx2((T)0., wc), qw_i = -mn2((T)0., wi);
-      const T mnv = rho[k] * (fk - m2) / (qu_c + qu_i + iadz * (qw_c + qw_i) + eps);
-      mx(i, k) = mxv;
-      mn(i, k) = mnv;
-    }
+    struct R4 { int i, k; T mxv, mnv; };
+    for_cells2((nx + 2) * nzm,
+      [&](int e) -> R4 {
+        R4 r;
+        r.i = e % (nx + 2); r.k = 1 + e / (nx + 2);          // 0 .. nx+1
+        const int i = r.i, k = r.k, kc = min(nzm, k + 1), kb = max(1, k - 1), ib = i - 1, ic = i + 1;
+        const T iadz = PR(P_IADZ)[k];
+        T m1 = mx2(mx2(mx2(mx2(mx2(f(ib, k), f(ic, k)), f(i, kb)), f(i, kc)), f(i, k)), mx(i, k));
+        T m2 = mn2(mn2(mn2(mn2(mn2(f(ib, k), f(ic, k)), f(i, kb)), f(i, kc)), f(i, k)), mn(i, k));
+        const T fk = f(i, k), uc = uuu(ic, k), ui = uuu(i, k), wc = www(i, kc), wi = www(i, k);
+        T pu_c = -mn2((T)0., uc), pu_i = mx2((T)0., ui);
+        T pw_c = -mn2((T)0., wc), pw_i = mx2((T)0., wi);
+        r.mxv = rho[k] * (m1 - fk) / (pu_c + pu_i + iadz * (pw_c + pw_i) + eps);
+        T qu_c = mx2((T)0., uc), qu_i = -mn2((T)0., ui);
+        T qw_c = mx2((T)0., wc), qw_i = -mn2((T)0., wi);
+        r.mnv = rho[k] * (fk - m2) / (qu_c + qu_i + iadz * (qw_c + qw_i) + eps);
+        return r;
+      },
+      [&](int, const R4 &r) {
+        mx(r.i, r.k) = r.mxv;
+        mn(r.i, r.k) = r.mnv;
+      });
     SYNC;
-    for (int e = TID; e < (nx + 1) * nzm; e += NT) {
-      int i = 1 + e % (nx + 1), k = 1 + e / (nx + 1);      // 1 .. nx+1
-      int ib = i - 1;
-      const T uu = uuu(i, k), mxk = mx(i, k), mnk = mn(i, k);
-      const T uval = mx2((T)0., uu) * mn3((T)1., mxk, mn(ib, k)) - (-mn2((T)0., uu)) * mn3((T)1., mx(ib, k), mnk);
-      if (i <= nx) {
-        int kb = max(1, k - 1);
-        const T ww = www(i, k);
-        const T wval = mx2((T)0., ww) * mn3((T)1., mxk, mn(i, kb)) - (-mn2((T)0., ww)) * mn3((T)1., mx(i, kb), mnk);
-        www(i, k) = wval;
-      }
-      uuu(i, k) = uval;
-    }
+    struct R5 { int i, k; T uval, wval; };
+    for_cells2((nx + 1) * nzm,
+      [&](int e) -> R5 {
+        R5 r;
+        r.i = 1 + e % (nx + 1); r.k = 1 + e / (nx + 1);      // 1 .. nx+1
+        const int i = r.i, k = r.k, ib = i - 1;
+        const T uu = uuu(i, k), mxk = mx(i, k), mnk = mn(i, k);
+        r.uval = mx2((T)0., uu) * mn3((T)1., mxk, mn(ib, k)) - (-mn2((T)0., uu)) * mn3((T)1., mx(ib, k), mnk);
+        r.wval = (T)0.;
+        if (i <= nx) {
+          int kb = max(1, k - 1);
+          const T ww = www(i, k);
+          r.wval = mx2((T)0., ww) * mn3((T)1., mxk, mn(i, kb)) - (-mn2((T)0., ww)) * mn3((T)1., mx(i, kb), mnk);
+        }
+        return r;
+      },
+      [&](int, const R5 &r) {
+        if (r.i <= nx) www(r.i, r.k) = r.wval;
+        uuu(r.i, r.k) = r.uval;
+      });
     SYNC;
     if (flux)
       level_sums_lo(1, 1, nzm, [&](int, int i, int k) -> T { return www(i, k); },
                  [&](int, int k) { return (double)wfl1(0, k); },
                  [&](int, int k, double sv) { flux[k] = (T)sv; });
-    for (int e = TID; e < nx * nzm; e += NT) {
-      int i = 1 + e % nx, k = 1 + e / nx;
-      T iadz = PR(P_IADZ)[k], irho = PR(P_IRHO)[k];
-      const T c2 = (uuu(i + 1, k) - uuu(i, k) + (www(i, k + 1) - www(i, k)) * iadz) * irho;
-      if (sizeof(T) == 4 && rc) {
-        T r = rc[e];
-        T s = add_carry(f(i, k), -c2, r);
-        if (!(s > (T)0.)) { s = (T)0.; r = (T)0.; }   // the positive-definite clip
-        rc[e] = r;
-        f(i, k) = s;
-      } else {
-        f(i, k) = mx2((T)0., f(i, k) - c2);
-      }
-    }
+    // final update with the positive-definite clip
+    struct R6 { int i, k; T fn, r; };
+    for_cells2(nx * nzm,
+      [&](int e) -> R6 {
+        R6 r;
+        r.i = 1 + e % nx; r.k = 1 + e / nx;
+        const int i = r.i, k = r.k;
+        const T iadz = PR(P_IADZ)[k], irho = PR(P_IRHO)[k];
+        const T c2 = (uuu(i + 1, k) - uuu(i, k) + (www(i, k + 1) - www(i, k)) * iadz) * irho;
+        if (sizeof(T) == 4 && rc) {
+          r.r = rc[e];
+          r.fn = add_carry(f(i, k), -c2, r.r);
+          if (!(r.fn > (T)0.)) { r.fn = (T)0.; r.r = (T)0.; }
+        } else {
+          r.r = (T)0.;
+          r.fn = mx2((T)0., f(i, k) - c2);
+        }
+        return r;
+      },
+      [&](int e, const R6 &r) {
+        f(r.i, r.k) = r.fn;
+        if (sizeof(T) == 4 && rc) rc[e] = r.r;
+      });
     SYNC;
     if (fadv) {
       level_sums_lo(1, 1, nzm, [&](int, int i, int k) -> T { return f(i, k) - f0(i, k); },
