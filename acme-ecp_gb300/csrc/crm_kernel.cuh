@@ -2418,14 +2418,12 @@ struct ColumnKernel : NxDim<NX> {
       cs[(i - 1)] = cwp; cs[nx + (i - 1)] = cwph; cs[2 * nx + (i - 1)] = cwpm; cs[3 * nx + (i - 1)] = cwpl;
       cs[4 * nx + (i - 1)] = (T)top;
     }
-    // interface mass fluxes (Xu et al. 2002): per-cell contributions at w
-    // levels k = 1..nz, zero where a cell does not count
-    F2<T> cmu = SA(), cmd = SB();
-    for (int e = TID; e < nx * nz; e += NT) {
-      int i = 1 + e % nx, k = 1 + e / nx;
-      T wv = w(i, k), cu = (T)0., cd = (T)0.;
-      // qsat > 0, so a cell without condensate never passes the threshold:
-      // qsatw is evaluated only where condensate exists (same result)
+    // cloudy mass flux of a cell at w level k (Xu et al. 2002): qsat > 0, so
+    // a cell without condensate never passes the threshold and qsatw is
+    // evaluated only where condensate exists (same result)
+    auto mass_flux = [&](int i, int k, T &cu, T &cd) {
+      const T wv = w(i, k);
+      cu = (T)0.; cd = (T)0.;
       if (wv > (T)0.) {
         int kx = max(1, k - 1);
         T cond = qcl(i, kx) + qci(i, kx);
@@ -2436,64 +2434,115 @@ struct ColumnKernel : NxDim<NX> {
         if (cond > (T)0. && cond > mn2((T)R4(1.e-5), (T)R4(0.01) * qsatw(tabs(i, kx), pres[kx]))) cd = rhow[k] * wv;
         else if (qpl(i, kx) + qpi(i, kx) > (T)R4(1.0e-4)) cd = rhow[k] * wv;
       }
-      cmu(i, k) = cu;
-      cmd(i, k) = cd;
-    }
-    SYNC;
+    };
     T *mui = OP(O_MUI), *mdi = OP(O_MDI);
-    level_sums_lo(2, 1, nz, [&](int q, int i, int k) -> T { return q == 0 ? cmu(i, k) : cmd(i, k); },
-               [&](int q, int k) { return (double)(q == 0 ? mui : mdi)[plev + 2 - k]; },
-               [&](int q, int k, double sv) { (q == 0 ? mui : mdi)[plev + 2 - k] = (T)sv; });
-    // cloud fraction, cloud top counts, cloudy mass fluxes, water paths
     T *acc[8] = {OP(O_CLD), OP(O_CLDTOP), OP(O_MCUP), OP(O_MCDN), OP(O_MCUUP), OP(O_MCUDN), OP(O_GLIQWP), OP(O_GICEWP)};
-    level_sums_lo_multi<8>(1, nzm,
-               [&](int q, int i, int k) -> T {
-                 if (q == 1) return ((int)cs[4 * nx + (i - 1)] == k) ? (T)1. : (T)0.;
-                 if (q == 6) return qcl(i, k);
-                 if (q == 7) return qci(i, k);
-                 T tmp1 = rho[k] * adz[k] * dz;
-                 bool cloudy = tmp1 * (qcl(i, k) + qci(i, k)) > thr;
-                 if (q == 0) return cloudy ? (T)1.0 : (T)0.;
-                 T ws = w(i, k + 1) + w(i, k);
-                 if (q == 2) return (cloudy && ws > (T)4.) ? rho[k] * (T)0.5 * ws * (T)1.0 : (T)0.;
-                 if (q == 3) return (cloudy && ws < (T)-4.) ? rho[k] * (T)0.5 * ws * (T)1.0 : (T)0.;
-                 if (q == 4) return (!cloudy && ws > (T)4.) ? rho[k] * (T)0.5 * ws : (T)0.;
-                 return (!cloudy && ws < (T)-4.) ? rho[k] * (T)0.5 * ws : (T)0.;
-               },
-               [&](int i, int k, T *r) {
-                 const T ql = qcl(i, k), qi = qci(i, k);
-                 const bool cloudy = rho[k] * adz[k] * dz * (ql + qi) > thr;
-                 const T ws = w(i, k + 1) + w(i, k), m = rho[k] * (T)0.5 * ws;
-                 r[0] = cloudy ? (T)1.0 : (T)0.;
-                 r[1] = ((int)cs[4 * nx + (i - 1)] == k) ? (T)1. : (T)0.;
-                 r[2] = (cloudy && ws > (T)4.) ? m : (T)0.;
-                 r[3] = (cloudy && ws < (T)-4.) ? m : (T)0.;
-                 r[4] = (!cloudy && ws > (T)4.) ? m : (T)0.;
-                 r[5] = (!cloudy && ws < (T)-4.) ? m : (T)0.;
-                 r[6] = ql;
-                 r[7] = qi;
-               },
-               [&](int q, int k) { return (double)acc[q][plev - k + 1]; },
-               [&](int q, int k, double sv) { acc[q][plev - k + 1] = (T)sv; });
-    // radiation-group sums (crm_module.F90:1000-1028)
-    const int nxr = p.L.nx_rad, gx = nx / nxr;
+    const int nxr = p.L.nx_rad;
     T *rad = base + p.L.rad;
-    for (int e = TID; e < nxr * nzm; e += NT) {
-      int ir = 1 + e % nxr, k = 1 + e / nxr;
-      size_t o = (size_t)(k - 1) * nxr + (ir - 1);
-      T st = rad[o], sq = rad[(size_t)nxr * nzm + o], sc = rad[(size_t)2 * nxr * nzm + o];
-      T si = rad[(size_t)3 * nxr * nzm + o], sl = rad[(size_t)4 * nxr * nzm + o];
-      for (int i = (ir - 1) * gx + 1; i <= ir * gx; ++i) {
-        st = st + tabs(i, k);
-        sq = sq + mx2((T)0., qv(i, k));
-        sc = sc + qcl(i, k);
-        si = si + qci(i, k);
-        if (qcl(i, k) + qci(i, k) > (T)0) sl = sl + (T)1.0;
+    if (sizeof(T) == 4 && nxr == nx) {
+      // FP32-mixed form, one radiation column per CRM column: the level
+      // statistics, the mass fluxes at w levels 1..nzm and the radiation
+      // sums in one pass (a warp per level, each cell visited once); the same
+      // terms and FP32 warp reductions as the separate passes below
+      SYNC;                                     // cloud tops (cs) complete
+      const size_t pl = (size_t)nx * nzm;
+      level_sums_lo_multi<10>(1, nzm,
+                 [&](int, int, int) -> T { return (T)0.; },   // (FP64 form: not used)
+                 [&](int i, int k, T *r) {
+                   const T ql = qcl(i, k), qi = qci(i, k);
+                   const bool cloudy = rho[k] * adz[k] * dz * (ql + qi) > thr;
+                   const T ws = w(i, k + 1) + w(i, k), m = rho[k] * (T)0.5 * ws;
+                   r[0] = cloudy ? (T)1.0 : (T)0.;
+                   r[1] = ((int)cs[4 * nx + (i - 1)] == k) ? (T)1. : (T)0.;
+                   r[2] = (cloudy && ws > (T)4.) ? m : (T)0.;
+                   r[3] = (cloudy && ws < (T)-4.) ? m : (T)0.;
+                   r[4] = (!cloudy && ws > (T)4.) ? m : (T)0.;
+                   r[5] = (!cloudy && ws < (T)-4.) ? m : (T)0.;
+                   r[6] = ql;
+                   r[7] = qi;
+                   mass_flux(i, k, r[8], r[9]);
+                   const size_t o = (size_t)(k - 1) * nx + (i - 1);
+                   const T st = rad[o] + tabs(i, k), sq = rad[pl + o] + mx2((T)0., qv(i, k));
+                   const T sc = rad[2 * pl + o] + ql, si = rad[3 * pl + o] + qi;
+                   const T sl = (ql + qi > (T)0) ? rad[4 * pl + o] + (T)1.0 : rad[4 * pl + o];
+                   rad[o] = st; rad[pl + o] = sq; rad[2 * pl + o] = sc; rad[3 * pl + o] = si; rad[4 * pl + o] = sl;
+                 },
+                 [&](int q, int k) {
+                   return (double)(q < 8 ? acc[q][plev - k + 1] : (q == 8 ? mui : mdi)[plev + 2 - k]);
+                 },
+                 [&](int q, int k, double sv) {
+                   (q < 8 ? acc[q][plev - k + 1] : (q == 8 ? mui : mdi)[plev + 2 - k]) = (T)sv;
+                 });
+      // w level nz (the rigid lid) for the mass fluxes
+      level_sums_lo(2, nz, nz,
+                 [&](int q, int i, int k) -> T { T cu, cd; mass_flux(i, k, cu, cd); return q == 0 ? cu : cd; },
+                 [&](int q, int k) { return (double)(q == 0 ? mui : mdi)[plev + 2 - k]; },
+                 [&](int q, int k, double sv) { (q == 0 ? mui : mdi)[plev + 2 - k] = (T)sv; });
+      SYNC;
+    } else {
+      // interface mass fluxes (Xu et al. 2002): per-cell contributions at w
+      // levels k = 1..nz, zero where a cell does not count
+      F2<T> cmu = SA(), cmd = SB();
+      for (int e = TID; e < nx * nz; e += NT) {
+        int i = 1 + e % nx, k = 1 + e / nx;
+        T cu, cd;
+        mass_flux(i, k, cu, cd);
+        cmu(i, k) = cu;
+        cmd(i, k) = cd;
       }
-      rad[o] = (T)st; rad[(size_t)nxr * nzm + o] = (T)sq; rad[(size_t)2 * nxr * nzm + o] = (T)sc;
-      rad[(size_t)3 * nxr * nzm + o] = (T)si; rad[(size_t)4 * nxr * nzm + o] = (T)sl;
+      SYNC;
+      level_sums_lo(2, 1, nz, [&](int q, int i, int k) -> T { return q == 0 ? cmu(i, k) : cmd(i, k); },
+                 [&](int q, int k) { return (double)(q == 0 ? mui : mdi)[plev + 2 - k]; },
+                 [&](int q, int k, double sv) { (q == 0 ? mui : mdi)[plev + 2 - k] = (T)sv; });
+      // cloud fraction, cloud top counts, cloudy mass fluxes, water paths
+      level_sums_lo_multi<8>(1, nzm,
+                 [&](int q, int i, int k) -> T {
+                   if (q == 1) return ((int)cs[4 * nx + (i - 1)] == k) ? (T)1. : (T)0.;
+                   if (q == 6) return qcl(i, k);
+                   if (q == 7) return qci(i, k);
+                   T tmp1 = rho[k] * adz[k] * dz;
+                   bool cloudy = tmp1 * (qcl(i, k) + qci(i, k)) > thr;
+                   if (q == 0) return cloudy ? (T)1.0 : (T)0.;
+                   T ws = w(i, k + 1) + w(i, k);
+                   if (q == 2) return (cloudy && ws > (T)4.) ? rho[k] * (T)0.5 * ws * (T)1.0 : (T)0.;
+                   if (q == 3) return (cloudy && ws < (T)-4.) ? rho[k] * (T)0.5 * ws * (T)1.0 : (T)0.;
+                   if (q == 4) return (!cloudy && ws > (T)4.) ? rho[k] * (T)0.5 * ws : (T)0.;
+                   return (!cloudy && ws < (T)-4.) ? rho[k] * (T)0.5 * ws : (T)0.;
+                 },
+                 [&](int i, int k, T *r) {
+                   const T ql = qcl(i, k), qi = qci(i, k);
+                   const bool cloudy = rho[k] * adz[k] * dz * (ql + qi) > thr;
+                   const T ws = w(i, k + 1) + w(i, k), m = rho[k] * (T)0.5 * ws;
+                   r[0] = cloudy ? (T)1.0 : (T)0.;
+                   r[1] = ((int)cs[4 * nx + (i - 1)] == k) ? (T)1. : (T)0.;
+                   r[2] = (cloudy && ws > (T)4.) ? m : (T)0.;
+                   r[3] = (cloudy && ws < (T)-4.) ? m : (T)0.;
+                   r[4] = (!cloudy && ws > (T)4.) ? m : (T)0.;
+                   r[5] = (!cloudy && ws < (T)-4.) ? m : (T)0.;
+                   r[6] = ql;
+                   r[7] = qi;
+                 },
+                 [&](int q, int k) { return (double)acc[q][plev - k + 1]; },
+                 [&](int q, int k, double sv) { acc[q][plev - k + 1] = (T)sv; });
+      // radiation-group sums (crm_module.F90:1000-1028)
+      const int gx = nx / nxr;
+      for (int e = TID; e < nxr * nzm; e += NT) {
+        int ir = 1 + e % nxr, k = 1 + e / nxr;
+        size_t o = (size_t)(k - 1) * nxr + (ir - 1);
+        T st = rad[o], sq = rad[(size_t)nxr * nzm + o], sc = rad[(size_t)2 * nxr * nzm + o];
+        T si = rad[(size_t)3 * nxr * nzm + o], sl = rad[(size_t)4 * nxr * nzm + o];
+        for (int i = (ir - 1) * gx + 1; i <= ir * gx; ++i) {
+          st = st + tabs(i, k);
+          sq = sq + mx2((T)0., qv(i, k));
+          sc = sc + qcl(i, k);
+          si = si + qci(i, k);
+          if (qcl(i, k) + qci(i, k) > (T)0) sl = sl + (T)1.0;
+        }
+        rad[o] = (T)st; rad[(size_t)nxr * nzm + o] = (T)sq; rad[(size_t)2 * nxr * nzm + o] = (T)sc;
+        rad[(size_t)3 * nxr * nzm + o] = (T)si; rad[(size_t)4 * nxr * nzm + o] = (T)sl;
+      }
+      SYNC;
     }
-    SYNC;
     if (TID < 32) {
       // shaded cloud fractions (counts, exact in any order): cf3d = 1, so a
       // column counts wherever its layer class exists (crm_module.F90:1053-1072)
