@@ -72,6 +72,7 @@ struct PrepParams {
   double *rnd;
 };
 void launch_crm_prep(const PrepParams &p, cudaStream_t s);
+int launch_crm_consts(void *dst, const void *src, size_t bytes, cudaStream_t s);
 
 template <typename T, int NX>
 static void launch_tn(int shape, const KParams &p, int grid, cudaStream_t s, bool coop) {
@@ -670,8 +671,10 @@ int crm_run(crm_ctx *c, const crm_call_desc *d, const crm_input_c *in, crm_state
 // crm_run_device_noalloc: the same two kernels with their scratch in one
 // fixed static device array instead of handle buffers.  Nothing here calls
 // cudaMalloc/cudaFree or allocates host memory: the per-configuration
-// constants are built in fixed-size host arrays on the stack and copied into
-// the static array on the caller's stream.
+// constants are built in fixed-size host arrays on the stack and written into
+// the static array by small kernels that carry them as parameters, so every
+// device operation of a call is a kernel launch on the caller's stream and
+// the call can be captured into a CUDA graph.
 
 namespace {
 
@@ -840,8 +843,10 @@ extern "C" int crm_run_device_noalloc(const crm_config *cfg, const crm_call_desc
     float *tf = reinterpret_cast<float *>(consts + q.ntrigs + q.neign);   // float copy of trigs
     for (int i = 0; i < q.ntrigs; ++i) tf[i] = (float)consts[i];
   }
-  CK(cudaMemcpyAsync(d_consts, consts, sizeof(double) * (size_t)(q.ntrigs + q.neign) + sizeof(float) * (size_t)q.ntrigs,
-                     cudaMemcpyHostToDevice, s));
+  // uploaded as kernel parameters, so that the call can be captured into a
+  // CUDA graph (the stack buffer is gone by the time a graph replays)
+  crm::launch_crm_consts(d_consts, consts,
+                         sizeof(double) * (size_t)(q.ntrigs + q.neign) + sizeof(float) * (size_t)q.ntrigs, s);
 
   crm::PrepParams pp;
   pp.ncrms = ncrms; pp.ld = d->ld; pp.plev = g.plev; pp.nx = nx; pp.igstep = d->igstep;

@@ -4,6 +4,7 @@
 // Mersenne-Twister variant of cam/RNG_MT.F90:52-142, seed gcol*1000).
 // One thread per column.  Compiled with -fmad=false: z0 uses the
 // deterministic exp/log/atan, so it matches a CPU evaluation bit for bit.
+#include <cstring>
 #include <cstdint>
 #include <cuda_runtime.h>
 #include "../../include/crm_detmath.h"
@@ -95,6 +96,34 @@ __global__ void crm_prep_kernel(const __grid_constant__ PrepParams p) {
 void launch_crm_prep(const PrepParams &p, cudaStream_t s) {
   int block = 128, grid = (p.ncrms + block - 1) / block;
   crm_prep_kernel<<<grid, block, 0, s>>>(p);
+}
+
+// Host bytes carried to the device as kernel parameters: a launch recorded
+// into a CUDA graph keeps its parameters by value, where a copy from host
+// memory would keep only the host address.
+struct ConstChunk {
+  unsigned long long w[480];
+  int nwords;
+};
+
+__global__ void crm_consts_kernel(unsigned long long *dst, const __grid_constant__ ConstChunk c) {
+  for (int i = threadIdx.x; i < c.nwords; i += blockDim.x) dst[i] = c.w[i];
+}
+
+int launch_crm_consts(void *dst, const void *src, size_t bytes, cudaStream_t s) {
+  ConstChunk c;
+  int launches = 0;
+  const unsigned char *from = static_cast<const unsigned char *>(src);
+  unsigned char *to = static_cast<unsigned char *>(dst);
+  for (size_t off = 0; off < bytes; off += sizeof c.w) {
+    const size_t n = bytes - off < sizeof c.w ? bytes - off : sizeof c.w;
+    memset(c.w, 0, sizeof c.w);
+    memcpy(c.w, from + off, n);
+    c.nwords = (int)((n + 7) / 8);
+    crm_consts_kernel<<<1, 128, 0, s>>>(reinterpret_cast<unsigned long long *>(to + off), c);
+    ++launches;
+  }
+  return launches;
 }
 
 }  // namespace crm

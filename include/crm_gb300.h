@@ -180,7 +180,10 @@ int crm_run(crm_ctx *ctx, const crm_call_desc *desc, const crm_input_c *in,
  * col_status (ncrms ints) is a device pointer or NULL.  The work is enqueued
  * on `stream` (a cudaStream_t, NULL for the handle's stream) and the call
  * returns without synchronising; argument errors are returned at once.  This
- * is the path a GCM that keeps its physics state on the GPU would call. */
+ * is the path a GCM that keeps its physics state on the GPU would call.  The
+ * enqueued work is kernel launches and event records only (plus a memset in
+ * reference-batch mode), so a call can be captured into a CUDA graph and the
+ * graph replayed; crm_last_kernel_ms is not defined for a captured call. */
 int crm_run_device(crm_ctx *ctx, const crm_call_desc *desc, const crm_input_c *in,
                    crm_state_c *state, crm_rad_c *rad, crm_output_c *out,
                    int *col_status, void *stream);
@@ -215,7 +218,9 @@ int crm_run_device(crm_ctx *ctx, const crm_call_desc *desc, const crm_input_c *i
  *
  * The array's device address is looked up once per device, by the first call
  * made with that device current; make that first call before any stream
- * capture begins.  Every call on a device shares the one array and leaves its
+ * capture begins.  Every device operation of a call is a kernel launch on
+ * `stream` (the per-configuration constants travel as kernel parameters), so
+ * later calls can be captured into a CUDA graph and replayed.  Every call on a device shares the one array and leaves its
  * last contents behind; nothing in it needs to start at zero (the kernel
  * clears a column's slab when it starts the column, and the set-up values and
  * constants are rewritten by every call).  Calls that overlap in time on the
