@@ -24,7 +24,7 @@ OBJ = os.path.join(PKG, '_build')
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 COMMON = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC,-ffp-contract=off',
           '-I' + os.path.join(REPO, 'include')]
-NUM_SHAPES = 5             # crm_kernel.h kShapes
+NUM_SHAPES = 6             # crm_kernel.h kShapes
 NX_BUILT = (32, 64, 128, 0)  # crm_kernel.h kNxBuilt (0: generic nx)
 UNITS = {'crm_prep': ('crm_prep', ['-fmad=false']), 'crm_host': ('crm_host', [])}
 for _n in NX_BUILT:

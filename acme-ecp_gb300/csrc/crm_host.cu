@@ -81,7 +81,8 @@ static void launch_tn(int shape, const KParams &p, int grid, cudaStream_t s, boo
     case 1: launch_crm_columns<T, NX, 1>(p, grid, s, coop); break;
     case 2: launch_crm_columns<T, NX, 2>(p, grid, s, coop); break;
     case 3: launch_crm_columns<T, NX, 3>(p, grid, s, coop); break;
-    default: launch_crm_columns<T, NX, 4>(p, grid, s, coop); break;
+    case 4: launch_crm_columns<T, NX, 4>(p, grid, s, coop); break;
+    default: launch_crm_columns<T, NX, 5>(p, grid, s, coop); break;
   }
 }
 
@@ -92,7 +93,8 @@ static int occupancy_tn(int shape, int nx, int nzm) {
     case 1: return occupancy_crm_columns<T, NX, 1>(nx, nzm);
     case 2: return occupancy_crm_columns<T, NX, 2>(nx, nzm);
     case 3: return occupancy_crm_columns<T, NX, 3>(nx, nzm);
-    default: return occupancy_crm_columns<T, NX, 4>(nx, nzm);
+    case 4: return occupancy_crm_columns<T, NX, 4>(nx, nzm);
+    default: return occupancy_crm_columns<T, NX, 5>(nx, nzm);
   }
 }
 
@@ -196,15 +198,16 @@ int default_shape(int precision, int nx) {
     int v = atoi(e);
     if (v >= 0 && v < crm::kNumShapes) return v;
   }
-  // measured on 1024 columns of nx x 58 (column-steps/s):
-  //   FP64: 256 threads at 3 CTAs/SM (90K at nx 64; 4 CTAs/SM and 512
-  //     threads are 1-14 % slower);
+  // measured on 1024 columns of nx x 58, 30 steps (column-steps/s):
+  //   FP64: 256 threads at 3 CTAs/SM (105K at nx 64; the other shapes are
+  //     4-15 % slower);
   //   FP32-mixed: 256 threads at 4 CTAs/SM with scratch planes A/B in
-  //     shared memory for nx <= 64 (920K at nx 32, 499K at nx 64: +2 % over
-  //     the planes in global memory), 512 threads at 2 CTAs/SM for
-  //     nx >= 128 (239K; the planes do not fit 4 CTAs/SM there).
+  //     shared memory for nx <= 64 (1.06M at nx 32, 586K at nx 64; 4-17 %
+  //     over the other shapes), 512 threads at 2 CTAs/SM with the planes in
+  //     shared memory for nx >= 128 (291K against 282K without them and
+  //     192K at 256 threads).
   if (precision == CRM_FP64) return 0;
-  return nx >= 128 ? 3 : 2;
+  return nx >= 128 ? 5 : 2;
 }
 
 // crm_accel_nstop (accelerate_crm.F90:84-106): nstop / (1 + crm_accel_factor),

@@ -57,8 +57,9 @@ struct KShape {
   int threads, min_ctas;
   int smem_planes;   // scratch planes A and B in shared memory (0 or 2)
 };
-constexpr int kNumShapes = 5;
-constexpr KShape kShapes[kNumShapes] = {{256, 3, 0}, {256, 4, 0}, {256, 4, 2}, {512, 2, 0}, {1024, 1, 0}};
+constexpr int kNumShapes = 6;
+constexpr KShape kShapes[kNumShapes] = {{256, 3, 0}, {256, 4, 0}, {256, 4, 2}, {512, 2, 0}, {1024, 1, 0},
+                                        {512, 2, 2}};
 
 // Horizontal sizes with a kernel specialised at compile time (the reference
 // fixes CRM_NX at build time too); any other power of two runs the generic
