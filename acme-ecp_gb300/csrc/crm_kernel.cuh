@@ -920,6 +920,21 @@ struct ColumnKernel : NxDim<NX> {
                [&](int q, int i, int k) -> T { return (q == 0 ? u(i, k) : q == 1 ? v(i, k) : t(i, k)) / nxy; },
                [&](int, int) { return 0.; },
                [&](int q, int k, double sv) { (q == 0 ? u0l : q == 1 ? v0l : t0l)[k] = (T)sv; });
+    // FP32-mixed form: the sponge relaxes t towards its level mean strongly
+    // (up to dtn/60 s per step), so an FP32 mean, off by up to half a unit
+    // in the last place, would pull the whole sponge layer by that much; the
+    // mean of t plus its residue is taken in FP64 instead
+    double *t0d = reinterpret_cast<double *>(sa());
+    if constexpr (sizeof(T) == 4) {
+      const int lane = TID & 31, warp = TID >> 5, nw = NT >> 5;
+      for (int k = nzm - n_damp + warp; k <= nzm; k += nw) {
+        if (k < 1) continue;
+        double s = 0.;
+        for (int i = 1 + lane; i <= nx; i += 32) s = s + ((double)t(i, k) + (double)rct()[(size_t)(i - 1) + (size_t)nx * (k - 1)]);
+        for (int o = 16; o > 0; o >>= 1) s = s + __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) t0d[k] = s / (double)nx;
+      }
+    }
     SYNC;
     F2<T> w = W(), qt = QT(), qv = QV(), du = DU(S.na), dv = DV(S.na), dw = DW(S.na);
     const T dtn = (T)S.dtn;
@@ -935,7 +950,8 @@ struct ColumnKernel : NxDim<NX> {
           qt(i, k) = qt(i, k) - dtn * (qv(i, k) - qv0[k]) * tau[k];
         } else {
           const size_t o = (size_t)(i - 1) + (size_t)nx * (k - 1);
-          t(i, k) = add_carry(t(i, k), -(dtn * (t(i, k) - t0l[k]) * tau[k]), rct()[o]);
+          const T anom = (T)(((double)t(i, k) + (double)rct()[o]) - t0d[k]);
+          t(i, k) = add_carry(t(i, k), -(dtn * anom * tau[k]), rct()[o]);
           qt(i, k) = add_carry(qt(i, k), -(dtn * (qv(i, k) - qv0[k]) * tau[k]), rcq()[o]);
         }
       }
@@ -2636,6 +2652,35 @@ struct ColumnKernel : NxDim<NX> {
                  [&](int, int) { return 0.; }, [&](int q, int k, double sv) { HS(q, k) = sv; });
     }
     SYNC;
+    // FP32-mixed form: the means of tabs and qv behind sltend and qltend (and
+    // the state's temperature and qt) from t and qt with their carried
+    // residues, diagnosed in FP64.  FP32 tabs and qv are rounded to within
+    // half a unit in the last place, which in a layer where nothing happens is
+    // the same bias in every cell and does not average out.
+    auto tabs_d = [&](int i, int k) -> double {
+      const size_t e = (size_t)(i - 1) + (size_t)nx * (k - 1);
+      return ((double)TT()(i, k) + (double)rct()[e]) - (double)PR(P_GAMAZ)[k] +
+             C_FAC_COND * ((double)qcl(i, k) + (double)qpl(i, k)) + C_FAC_SUB * ((double)qci(i, k) + (double)qpi(i, k));
+    };
+    auto qt_d = [&](int i, int k) -> double {
+      return (double)qt(i, k) + (double)rcq()[(size_t)(i - 1) + (size_t)nx * (k - 1)];
+    };
+    if constexpr (sizeof(T) == 4) {
+      const int lane = TID & 31, warp = TID >> 5, nw = NT >> 5;
+      for (int k = 1 + warp; k <= nzm; k += nw) {
+        double st = 0., sq = 0.;
+        for (int i = 1 + lane; i <= nx; i += 32) {
+          st = st + tabs_d(i, k);
+          sq = sq + (qt_d(i, k) - (double)qn(i, k));
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+          st = st + __shfl_xor_sync(0xffffffffu, st, o);
+          sq = sq + __shfl_xor_sync(0xffffffffu, sq, o);
+        }
+        if (lane == 0) { HS(0, k) = st; HS(1, k) = sq; }
+      }
+      SYNC;
+    }
     // GCM-level tendencies and statistics
     for (int l = TID + 1; l <= plev; l += NT) {
       double tln, qln, qccln, qiiln;
@@ -2721,8 +2766,13 @@ struct ColumnKernel : NxDim<NX> {
       p.st[0][o] = (double)u(i, k);
       p.st[1][o] = (double)v(i, k);
       p.st[2][o] = (double)w(i, k);
-      p.st[3][o] = (double)tabs(i, k);
-      p.st[4][o] = (double)qt(i, k);
+      if constexpr (sizeof(T) == 4) {
+        p.st[3][o] = tabs_d(i, k);
+        p.st[4][o] = qt_d(i, k);
+      } else {
+        p.st[3][o] = (double)tabs(i, k);
+        p.st[4][o] = (double)qt(i, k);
+      }
       p.st[5][o] = (double)qp(i, k);
       p.st[6][o] = (double)qn(i, k);
       p.out[CRM_OUT_TK][o] = (double)tk(i, k);
