@@ -228,3 +228,26 @@ def test_fp64_bitexact_reference_batch_acceleration_cease(gpu_lib):
     rad.qrad[1, :, :, 5:8] = 0.5
     bcfg = _accel(S.config0(batch_mode=T.CRM_REFERENCE_BATCH), 2.0)
     assert mismatches(*run_both(bcfg, cin, st, rad, desc)) == []
+
+
+def test_fp64_bitexact_mixed_precipitating_columns(gpu_lib):
+    """Columns with and without precipitating water in one batch: the kernel
+    skips sedimentation and qp transport for a column whose fall speeds are
+    all zero or whose qp is +0 everywhere, which must change no bit — signs
+    of zero included — of any column's state or outputs."""
+    cfg, cin, st, rad, desc = S.workload0(ncrms=6, moist=True)
+    _, cin_d, st_d, _, _ = S.workload0(ncrms=6, moist=False)
+    for c in (1, 3, 5):                       # dry columns between moist ones
+        for n in ('qt', 'qp', 'qn', 'temperature'):
+            getattr(st, n)[c] = getattr(st_d, n)[c]
+        cin.qccl[c] = cin_d.qccl[c]
+        cin.qiil[c] = cin_d.qiil[c]
+    a, b = run_both(cfg, cin, st, rad, desc)
+    assert mismatches(a, b) == []
+    (st_o, _, out_o), (st_g, _, out_g) = a, b
+    assert np.any(st_o.qp[0] > 0) and not np.any(st_o.qp[1] > 0)
+    for n, x in list(st_o.arrays().items()) + list(out_o.arrays().items()):
+        y = getattr(st_g, n) if n in st_o.arrays() else getattr(out_g, n)
+        xb = np.ascontiguousarray(x).view(np.uint64)
+        yb = np.ascontiguousarray(y).view(np.uint64)
+        assert np.array_equal(xb, yb), n
