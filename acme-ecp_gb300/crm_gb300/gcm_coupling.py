@@ -13,14 +13,34 @@ the CRM the water identity is exact:
 
 i.e. the GCM column loses what fell out at the surface plus what is still
 stored in the CRM as precipitating water (prectend is the change of the
-CRM's column qp over the call, crm_module.F90:1086-1100).  This module states
-the tendency, the update and that residual.
+CRM's column qp over the call, crm_module.F90:1086-1100).
+
+The energy side of check_energy_chng closes the same way.  Inside the CRM
+the liquid-ice static energy t (crm_module.F90:508-509) changes only by the
+large-scale forcing (which returns the column to the GCM state), the
+radiative heating qrad (crm_module.F90:766-777) and the latent heat carried
+out by precipitation at the surface (precip_fall, ice_fall); damping keeps
+the level means, advection and SGS diffusion conserve it, and condensation
+and precipitation processes leave it unchanged.  Writing tabs from t at the
+end of the call gives, per column [W/m2],
+
+    sum_k pdel_k / g (sltend - Lc qcltend - Ls qiltend)
+        = cp sum_k pdel_k / g <qrad>_k
+          + rho_water (Lc (precc + precl) + Lf (precsc + precsl))
+          + Lc prectend + Lf precstend
+
+with the CRM's own latent heats (crm/params.F90:49-55) and the levels
+whose tendencies crm() zeroes (the top two) left out of the qrad sum.
+This module states the tendency, the update and both residuals.
 """
 import numpy as np
 
 GRAVIT = 9.80616       # shr_const_g
 CPAIR = 1.00464e3      # shr_const_cpdair
 RHO_WATER = 1000.0     # precipitation rates are m/s of liquid water
+LCOND = 2.501e6        # CRM latent heats (crm/params.F90, CRM branch)
+LFUS = 3.337e5
+LSUB = LCOND + LFUS
 
 
 def ptend(out, ncol):
@@ -56,3 +76,34 @@ def water_scale(cin, out, ncol):
     pd = np.asarray(cin.pdel[:ncol]) / GRAVIT
     dw = np.sum(pd * np.abs(out.qltend[:ncol] + out.qcltend[:ncol] + out.qiltend[:ncol]), axis=1)
     return dw + np.abs((out.precc[:ncol] + out.precl[:ncol]) * RHO_WATER) + np.abs(out.prectend[:ncol])
+
+
+def _energy_terms(cin, rad, out, ncol, nzm):
+    pd = np.asarray(cin.pdel[:ncol]) / GRAVIT
+    plev = pd.shape[1]
+    lhs = np.sum(pd * (out.sltend[:ncol] - LCOND * out.qcltend[:ncol] - LSUB * out.qiltend[:ncol]), axis=1)
+    qr = np.asarray(rad.qrad[:ncol, :, 0, :]).mean(axis=1)       # (ncol, crm_nz), K/s
+    rad_heat = np.zeros(ncol)
+    for k in range(1, nzm - 1):              # CRM level k is GCM level plev - k + 1
+        rad_heat += pd[:, plev - k] * CPAIR * qr[:, k - 1]
+    prec = RHO_WATER * (LCOND * (out.precc[:ncol] + out.precl[:ncol]) +
+                        LFUS * (out.precsc[:ncol] + out.precsl[:ncol]))
+    store = LCOND * out.prectend[:ncol] + LFUS * out.precstend[:ncol]
+    return lhs, rad_heat, prec, store
+
+
+def energy_residual(cin, rad, out, ncol, nzm):
+    """Per column [W/m2]: column energy tendency - radiative heating - latent
+    heat of the surface precipitation - latent heat of the CRM's precipitation
+    storage change (zero up to rounding).  rad holds the qrad the call was
+    given; nzm = crm_nz."""
+    lhs, rad_heat, prec, store = _energy_terms(cin, rad, out, ncol, nzm)
+    return lhs - rad_heat - prec - store
+
+
+def energy_scale(cin, rad, out, ncol, nzm):
+    """Magnitude of the terms of energy_residual, to make it relative."""
+    pd = np.asarray(cin.pdel[:ncol]) / GRAVIT
+    _, rad_heat, prec, store = _energy_terms(cin, rad, out, ncol, nzm)
+    dw = np.sum(pd * np.abs(out.sltend[:ncol]), axis=1)
+    return dw + np.abs(rad_heat) + np.abs(prec) + np.abs(store)

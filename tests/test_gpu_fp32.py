@@ -114,3 +114,22 @@ def test_fp32_mixed_gcm_water_identity(gpu_lib):
     r = G.water_residual(cin, out, 4) / G.water_scale(cin, out, 4)
     print('fp32-mixed GCM water identity residual (relative):', r)
     assert np.max(np.abs(r)) < 1e-4, r
+
+
+@pytest.mark.parametrize('moist', [False, True])
+def test_fp32_mixed_gcm_energy_identity(gpu_lib, moist):
+    """The column energy identity (energy tendency = radiative heating +
+    latent heat of the surface precipitation and of the CRM's precipitation
+    storage change) for the FP32-mixed form; the FP64 oracle closes it to
+    ~1e-8 of its terms."""
+    from crm_gb300 import gcm_coupling as G
+    cfg, cin, st, rad, desc = S.workload1(ncrms=4, moist=moist)
+    cfg.precision = T.CRM_FP32_MIXED
+    cfg.max_ncrms = 4
+    ctx = CrmContext(cfg)
+    out = T.CrmOutput(4, cfg.crm_nx, 1, cfg.crm_nz, cfg.plev)
+    rad_in = rad.copy()
+    ctx.run(desc, cin, st.copy(), rad.copy(), out, raise_on_error=True)
+    r = G.energy_residual(cin, rad_in, out, 4, cfg.crm_nz) / G.energy_scale(cin, rad_in, out, 4, cfg.crm_nz)
+    print('fp32-mixed GCM energy identity residual (relative, moist=%s):' % moist, r)
+    assert np.max(np.abs(r)) < 1e-3, r
