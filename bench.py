@@ -334,6 +334,21 @@ def main():
         traffic = tr.get('bytes_per_launch_scaled')
     except Exception:
         pass
+    # the FP64 form is bound by the FP64 pipe (2 lanes per SM per clock on
+    # GB300): its FP64 warp-instructions per column-step (ncu) against the
+    # pipe's peak at the sampled SM clock
+    fp64_pipe = None
+    try:
+        with open(os.path.join(REPO, 'profiles', 'crm_columns_fp64_pipe.json')) as f:
+            fp = json.load(f)
+        nsm = torch.cuda.get_device_properties(local).multi_processor_count
+        mhz = (clk or {}).get('sm_mhz') or 2070.0
+        peak_inst = nsm * fp['peak_fp64_warp_inst_per_sm_cycle'] * mhz * 1e6
+        fp64_pipe = {'frac': value64 / ws * fp['fp64_warp_inst_per_column_step'] / peak_inst,
+                     'fp64_warp_inst_per_column_step': fp['fp64_warp_inst_per_column_step'],
+                     'peak_warp_inst_per_s': peak_inst, 'sm_mhz': mhz}
+    except Exception:
+        pass
     cb = None
     if ws == 1:
         try:
@@ -364,7 +379,8 @@ def main():
                 'ms_per_step': e2e_ms},
         'clocks': clk,
         'gpu_launches': 2 * args.steps,   # crm_prep_kernel + crm_columns_kernel per timed step
-        'fp64_plain': {'value': value64, 'unit': UNIT, 'ms_per_step': ms64, 'steps': args.fp64_steps},
+        'fp64_plain': {'value': value64, 'unit': UNIT, 'ms_per_step': ms64, 'steps': args.fp64_steps,
+                       'fp64_pipe': fp64_pipe},
         'fp32_over_fp64': value / value64,
         'fp32_rel_l2_vs_fp64_state': errs,
         'fp32_rel_l2_vs_fp64_outputs': errs_out,
