@@ -345,9 +345,10 @@ void free_ctx(crm_ctx *c) {
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
 }
 
-// Enqueue the set-up and column kernels for device-resident arguments.
-int enqueue(crm_ctx *c, const crm_call_desc *d, const crm_input_c *in, crm_state_c *st, crm_rad_c *rad,
-            crm_output_c *out, int *d_status, cudaStream_t s) {
+// Checks one call on device-resident arguments and fills the parameters of
+// its set-up and column kernels.
+int build_params(crm_ctx *c, const crm_call_desc *d, const crm_input_c *in, crm_state_c *st, crm_rad_c *rad,
+                 crm_output_c *out, int *d_status, crm::KParams &p, crm::PrepParams &pp) {
   const crm_config &g = c->cfg;
   const int ncrms = d->ncrms, ld = d->ld;
   if (ncrms < 1 || ld < ncrms || ncrms > g.max_ncrms || !(d->dt_gl > 0)) return CRM_ERR_ARG;
@@ -371,7 +372,6 @@ int enqueue(crm_ctx *c, const crm_call_desc *d, const crm_input_c *in, crm_state
   if (60. < 2 * dt) return CRM_ERR_ARG;         // damping.F90:39-42
   const int nstop_run = accel_nstop(g, nstop);   // crm_module.F90:718-720
   if (nstop_run < 1) return CRM_ERR_ARG;
-  crm::PrepParams pp;
   pp.ncrms = ncrms; pp.ld = ld; pp.plev = g.plev; pp.nx = g.crm_nx; pp.igstep = d->igstep;
   pp.zmid = in->zmid; pp.zint = in->zint; pp.pdel = in->pdel;
   pp.tau00 = in->tau00; pp.bflxls = in->bflxls; pp.wndls = in->wndls;
@@ -379,7 +379,6 @@ int enqueue(crm_ctx *c, const crm_call_desc *d, const crm_input_c *in, crm_state
   pp.col_map = d->col_map;
   pp.z0 = c->d_colconst;
   pp.rnd = c->d_colconst + g.max_ncrms;
-  crm::KParams p;
   memset(&p, 0, sizeof p);
   p.L = c->L;
   p.ncrms = ncrms; p.ld = ld; p.nstop = nstop; p.igstep = d->igstep;
@@ -411,6 +410,18 @@ int enqueue(crm_ctx *c, const crm_call_desc *d, const crm_input_c *in, crm_state
   p.col_map = d->col_map;
   p.phase_cycles = c->d_phase;
   p.col_status = d_status ? d_status : c->d_status;
+  return CRM_OK;
+}
+
+// Enqueue the set-up and column kernels for device-resident arguments.
+int enqueue(crm_ctx *c, const crm_call_desc *d, const crm_input_c *in, crm_state_c *st, crm_rad_c *rad,
+            crm_output_c *out, int *d_status, cudaStream_t s) {
+  crm::KParams p;
+  crm::PrepParams pp;
+  int rc = build_params(c, d, in, st, rad, out, d_status, p, pp);
+  if (rc != CRM_OK) return rc;
+  const crm_config &g = c->cfg;
+  const int ncrms = d->ncrms;
   if (c->shape_auto) {
     // A call that fits the GPU in one round runs fastest with the most
     // threads per column (1024 threads: 10.2 ms for 16 columns of 64 x 58
