@@ -758,12 +758,15 @@ struct ColumnKernel : NxDim<NX> {
   // ---------------------------------------------------------- kurant
   // kurant.F90:31-64 and kurant_sgs (SGS_TKE/sgs.F90:342-367); per column
   __device__ void kurant() {
-    F2<T> u = U(), v = V(), w = W(), tkh = TKH();
+    F2<T> u = U(), w = W(), tkh = TKH();
     T *wm = PR(P_TMP0), *uhm = PR(P_TMP1), *tkhm = PR(P_TMP2);
+    // the horizontal speed of the 2D reference is sqrt(u*u + 0*(v*v)); for
+    // a finite v the second term is +0 and the sum is u*u exactly, so v is
+    // not read
     level_max(3, 1, nzm,
               [&](int q, int i, int k) -> T {
                 if (q == 0) return tabs_(w(i, k));
-                if (q == 1) { T uu = u(i, k), vv = v(i, k); return tsqrt(uu * uu + (T)0. * (vv * vv)); }
+                if (q == 1) { T uu = u(i, k); return tsqrt(uu * uu); }
                 return tkh(i, k);
               },
               [&](int q, int k, T m) { (q == 0 ? wm : q == 1 ? uhm : tkhm)[k] = m; });
