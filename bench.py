@@ -119,6 +119,14 @@ def cpu_baseline(ncols, nthreads=0):
                       % (ncols, NCRMS), 'seconds': dt, 'rc': rc}
 
 
+def workload_config(nstop=120):
+    """The bench workload, as both arms report it in `config`."""
+    return {'workload': '2D CRM batch: %d columns x (64 x 1 x 58), dx 1 km, dt 10 s, '
+                        'dt_gl 1200 s (%d CRM steps), sam1mom, SGS TKE, MPDATA' % (NCRMS, nstop),
+            'ncrms': NCRMS, 'crm_nx': 64, 'crm_nz': 58, 'plev': 72, 'nstop': nstop,
+            'batch_mode': 'per-column'}
+
+
 def run_reference(args):
     ws, rank, _ = dist_info()
     if rank != 0:
@@ -138,8 +146,8 @@ def run_reference(args):
             'warmup': args.warmup, 'ms_per_step': 1000 * total / args.steps,
             'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
             'dtype': 'f64', 'data': 'synthetic', 'impl': 'reference',
-            'config': {'workload': '2D CRM nx64 nz58 dx1km dt10s, 1 GCM step of 1200 s, sam1mom; '
-                                   '%d-column sample per step on the host cores' % ncols},
+            'config': dict(workload_config(), form='fp64, CPU restatement of crm() on the host cores',
+                           sample='%d of the %d columns per step' % (ncols, NCRMS)),
             'cpu_baseline': {k: cb[k] for k in ('value', 'unit', 'cores', 'kind', 'sample')},
             'e2e': {'value': v, 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
     print(json.dumps(line))
@@ -363,12 +371,9 @@ def main():
         'scaling': 'weak', 'vs_baseline': None,
         'dtype': 'f32 (f64 tridiagonal solve, domain sums, saturation Newton)',
         'data': 'synthetic (idealised soundings, seeded)',
-        'config': {'workload': '2D CRM batch: %d columns x (64 x 1 x 58), dx 1 km, dt 10 s, '
-                               'dt_gl 1200 s (%d CRM steps), sam1mom, SGS TKE, MPDATA' % (NCRMS, nstop),
-                   'ncrms': NCRMS, 'crm_nx': 64, 'crm_nz': 58, 'plev': 72, 'nstop': nstop,
-                   'form': 'fp32-mixed', 'batch_mode': 'per-column',
-                   'l2': 'inputs larger than L2: every step re-reads the %d MB state' %
-                         (dev32.nbytes_state() // 2 ** 20)},
+        'config': dict(workload_config(nstop), form='fp32-mixed',
+                       l2='inputs larger than L2: every step re-reads the %d MB state' %
+                          (dev32.nbytes_state() // 2 ** 20)),
         'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
                      'frac': achieved / peak, 'traffic': traffic,
                      'peak_kind': peak_kind, 'kernel_ms': kernel_ms,
