@@ -2296,6 +2296,21 @@ using namespace oracle;
 
 extern "C" {
 
+// Test hook: fft991 on one vector a[0..n+1] with the pressure solver's trig
+// table and factors (isign -1: grid point -> spectral, +1: back).  Returns
+// CRM_ERR_ARG for a length the transform does not factor (radix 2..5).
+int oracle_fft991(double *a, int n, int isign) {
+  if (!a || n < 4 || n % 2) return CRM_ERR_ARG;
+  int ifax[20] = {0};
+  fax(ifax, n);
+  for (int k = 1; k <= ifax[0]; ++k)
+    if (ifax[k] > 5) return CRM_ERR_ARG;
+  std::vector<double> trigs, work((size_t)n + 2);
+  fftrig(trigs, n);
+  fft991(a, work.data(), trigs.data(), ifax, n, isign);
+  return CRM_OK;
+}
+
 // Run the restatement of crm() on the host.  Same arguments and array
 // conventions as crm_run() in include/crm_gb300.h; nthreads <= 0 uses the
 // OpenMP default.  Returns a crm_status.

@@ -50,6 +50,8 @@ def load(check=False):
                                        C.POINTER(T.CCrmInput), C.POINTER(T.CCrmState),
                                        C.POINTER(T.CCrmRad), C.POINTER(T.CCrmOutput),
                                        C.POINTER(C.c_int), C.c_int]
+        lib.oracle_fft991.restype = C.c_int
+        lib.oracle_fft991.argtypes = [C.POINTER(C.c_double), C.c_int, C.c_int]
         if check:
             return lib
         _lib = lib
@@ -69,3 +71,14 @@ def run(cfg, desc, cin, state, rad, out=None, nthreads=0, check=False):
                             C.byref(c_rad), C.byref(c_out),
                             status.ctypes.data_as(C.POINTER(C.c_int)), int(nthreads))
     return rc, status, out
+
+
+def fft991(x, isign):
+    """The oracle's fft991 on one vector (len n + 2, float64, modified in
+    place copy): isign -1 grid point -> spectral, +1 back."""
+    import numpy as np
+    a = np.ascontiguousarray(np.array(x, dtype=np.float64))
+    rc = load().oracle_fft991(a.ctypes.data_as(C.POINTER(C.c_double)), a.size - 2, int(isign))
+    if rc != 0:
+        raise ValueError('fft991: unsupported length %d' % (a.size - 2))
+    return a
