@@ -8,7 +8,12 @@
 // loops are spread over the CTA's threads with a barrier between phases;
 // every sum over the horizontal runs sequentially in the reference's loop
 // order (one thread per level), so the FP64 form reproduces the CPU
-// restatement bit for bit.
+// restatement bit for bit.  The FP32-mixed form adds what only it needs:
+// warp-parallel sums, per-cell residues carried by the t and qt updates
+// (add_carry), FP64 means where a mean feeds a relaxation or a returned
+// tendency.  Both forms skip work that provably changes no bit (the
+// sedimentation of a column with no falling precipitation, qp transport of a
+// column whose qp is +0 everywhere).
 #pragma once
 #include "crm_device.cuh"
 #include "crm_kernel.h"
