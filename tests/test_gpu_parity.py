@@ -251,3 +251,31 @@ def test_fp64_bitexact_mixed_precipitating_columns(gpu_lib):
         xb = np.ascontiguousarray(x).view(np.uint64)
         yb = np.ascontiguousarray(y).view(np.uint64)
         assert np.array_equal(xb, yb), n
+
+
+def test_col_map_slot_out_of_range_is_reported_per_column(gpu_lib):
+    """A col_map entry outside 0..ld-1 is refused by the set-up and column
+    kernels before they touch that slot: its position reports
+    CRM_ERR_ARG, the other positions integrate as in a call without it."""
+    import ctypes as C
+    cfg, cin, st, rad, desc = S.workload0(ncrms=5, moist=True)
+    desc.dt_gl = 200.0
+    keep = np.asarray(desc._keep)
+    good = np.array([3, 0], dtype=np.int32)
+    bad = np.array([3, 5, 0, -1], dtype=np.int32)       # 5 = ld, -1: out of range
+    d_good = T.call_desc(2, 5, desc.dt_gl, desc.igstep, keep[good])
+    d_good.col_map = good.ctypes.data_as(C.POINTER(C.c_int))
+    gcol_bad = np.array([keep[3], keep[0], keep[0], keep[0]], dtype=np.int32)
+    d_bad = T.call_desc(4, 5, desc.dt_gl, desc.igstep, gcol_bad)
+    d_bad.col_map = bad.ctypes.data_as(C.POINTER(C.c_int))
+    st_a, rad_a = st.copy(), rad.copy()
+    rc_a, stat_a, out_a = run_gpu(cfg, cin, st_a, rad_a, d_good)
+    assert rc_a == 0, stat_a
+    st_b, rad_b = st.copy(), rad.copy()
+    rc_b, stat_b, out_b = run_gpu(cfg, cin, st_b, rad_b, d_bad)
+    assert list(stat_b) == [T.CRM_OK, T.CRM_ERR_ARG, T.CRM_OK, T.CRM_ERR_ARG], stat_b
+    assert rc_b == T.CRM_ERR_ARG
+    for n, x in st_a.arrays().items():
+        assert np.array_equal(x, getattr(st_b, n)), n
+    for n, x in out_a.arrays().items():
+        assert np.array_equal(x[[3, 0]], getattr(out_b, n)[[3, 0]]), n
