@@ -133,3 +133,19 @@ def test_fp32_mixed_gcm_energy_identity(gpu_lib, moist):
     r = G.energy_residual(cin, rad_in, out, 4, cfg.crm_nz) / G.energy_scale(cin, rad_in, out, 4, cfg.crm_nz)
     print('fp32-mixed GCM energy identity residual (relative, moist=%s):' % moist, r)
     assert np.max(np.abs(r)) < 1e-3, r
+
+
+def test_fp32_mixed_reference_batch_mode(gpu_lib):
+    """CRM_REFERENCE_BATCH in the FP32-mixed form: the grid-wide maxima
+    couple the columns the same way (ncycle from the batch), within the
+    FP32 bounds of the oracle's batch mode."""
+    def wl(**kw):
+        cfg, cin, st, rad, desc = S.workload0(**kw)
+        cfg = T.CrmConfig(**{**cfg.__dict__, 'batch_mode': T.CRM_REFERENCE_BATCH})
+        desc.dt_gl = 400.0
+        st.w_wind[2, :, :, 10] = 40.0
+        return cfg, cin, st, rad, desc
+    e = _errors(wl, ncrms=4, moist=True)
+    print('fp32-mixed rel-L2 vs fp64 oracle (32x28, reference batch mode):', e)
+    for n in ('temperature', 'qt', 'u_wind', 'sltend', 'qltend'):
+        assert e[n] <= 10 * BOUNDS[n], (n, e[n])
