@@ -3,7 +3,8 @@
     python acme-ecp_gb300/crm_gb300/profile_case.py --ncrms 152 --dt-gl 100 \
         --precision fp32 --reps 2
 
-runs the 64 x 58 workload (--workload 1; --workload 0: the 32 x 28 one) on
+runs the 64 x 58 workload (--workload 64x58, the default; 32x28: 16-column
+sized one at dx 4 km, dt 20 s) on
 device-resident arrays (crm_run_device) `reps` times and prints the kernel
 time of each call.  Sized so that a profiler capture of one launch ends in
 seconds.
@@ -23,7 +24,7 @@ def main():
     ap.add_argument('--precision', default='fp32', choices=['fp32', 'fp64'])
     ap.add_argument('--reps', type=int, default=2)
     ap.add_argument('--nx', type=int, default=64)
-    ap.add_argument('--workload', type=int, default=1, choices=[0, 1])
+    ap.add_argument('--workload', default='64x58', choices=['32x28', '64x58'])
     ap.add_argument('--shape', type=int, default=None,
                     help='column-kernel launch shape index (crm_kernel.h kShapes)')
     ap.add_argument('--phase-timers', action='store_true',
@@ -40,10 +41,10 @@ def main():
     from crm_gb300.lib import CrmContext
     L.load(path=B.build(phase_timers=args.phase_timers))
     prec = T.CRM_FP32_MIXED if args.precision == 'fp32' else T.CRM_FP64
-    if args.workload == 0:
-        cfg, cin, st, rad, desc = S.workload0(ncrms=args.ncrms, precision=prec)
+    if args.workload == '32x28':
+        cfg, cin, st, rad, desc = S.workload_32x28(ncrms=args.ncrms, precision=prec)
     else:
-        cfg, cin, st, rad, desc = S.workload1(ncrms=args.ncrms, nx=args.nx, precision=prec)
+        cfg, cin, st, rad, desc = S.workload_64x58(ncrms=args.ncrms, nx=args.nx, precision=prec)
     desc.dt_gl = args.dt_gl
     cfg.max_ncrms = args.ncrms
     ctx = CrmContext(cfg)

@@ -152,27 +152,27 @@ def make_inputs(cfg: CrmConfig, ncrms, t_sfc, shf, lhf, dt_gl=1200.0, seed=0,
     return cin, st, rad, desc
 
 
-def config0(precision=0, batch_mode=0):
+def config_32x28(precision=0, batch_mode=0):
     """Plain 2D CRM, FAST-compset shape: nx 32, nz 28 of 30 levels, dx 4 km, dt 20 s."""
     return CrmConfig(crm_nx=32, crm_ny=1, crm_nz=28, plev=30, crm_dx=4000.0,
                      crm_dt=20.0, precision=precision, batch_mode=batch_mode)
 
 
-def config1(precision=0, batch_mode=0, nx=64):
+def config_64x58(precision=0, batch_mode=0, nx=64):
     """2D CRM, V1-compset shape: nx 64, nz 58 of 72 levels, dx 1 km, dt 10 s."""
     return CrmConfig(crm_nx=nx, crm_ny=1, crm_nz=58, plev=72, crm_dx=1000.0,
                      crm_dt=10.0, precision=precision, batch_mode=batch_mode)
 
 
-def workload0(ncrms=16, seed=0, moist=False, **kw):
+def workload_32x28(ncrms=16, seed=0, moist=False, **kw):
     """16 columns, T_sfc 300 K, SHF 10 W/m2, LHF 100 W/m2."""
-    cfg = config0(**kw)
+    cfg = config_32x28(**kw)
     return (cfg,) + make_inputs(cfg, ncrms, 300.0, 10.0, 100.0, seed=seed, moist=moist)
 
 
-def workload1(ncrms=1024, seed=0, nx=64, moist=False, gcol0=1, **kw):
+def workload_64x58(ncrms=1024, seed=0, nx=64, moist=False, gcol0=1, **kw):
     """lat ~ U[-60, 60] deg (seeded), T_sfc = 271 + 29 cos(lat), fluxes * cos(lat)."""
-    cfg = config1(nx=nx, **kw)
+    cfg = config_64x58(nx=nx, **kw)
     rng = np.random.Generator(np.random.PCG64(10_000 + seed))
     lat = rng.uniform(-60.0, 60.0, size=ncrms)
     cl = np.cos(np.deg2rad(lat))

@@ -109,7 +109,7 @@ def cpu_baseline(ncols, nthreads=0):
     import oracle
     from crm_gb300 import synthetic as S
     oracle.build()
-    cfg, cin, st, rad, desc = S.workload1(ncrms=ncols)
+    cfg, cin, st, rad, desc = S.workload_64x58(ncrms=ncols)
     cores = nthreads or os.cpu_count()
     t0 = time.perf_counter()
     rc, _, _ = oracle.run(cfg, desc, cin, st, rad, nthreads=cores)
@@ -199,7 +199,7 @@ def main():
     # weak scaling: NCRMS columns per rank, rank r owning global columns
     # [r * NCRMS, (r + 1) * NCRMS) (contiguous blocks, no data exchange)
     first, count = column_shard(ws * NCRMS, rank, ws)
-    cfg32, cin, st, rad, desc = S.workload1(ncrms=count, seed=first, gcol0=first + 1,
+    cfg32, cin, st, rad, desc = S.workload_64x58(ncrms=count, seed=first, gcol0=first + 1,
                                             precision=T.CRM_FP32_MIXED)
     cfg32.max_ncrms = NCRMS
     nstop = int(desc.dt_gl / cfg32.crm_dt)
@@ -287,7 +287,7 @@ def main():
            sum(a.nbytes for a in out_p.arrays().values()) + 4 * NCRMS)
 
     # ---- FP64 plain form
-    cfg64 = S.config1(precision=T.CRM_FP64)
+    cfg64 = S.config_64x58(precision=T.CRM_FP64)
     cfg64.max_ncrms = NCRMS
     ctx64, dev64, ms64, _ = device_rate(cfg64, args.fp64_steps, 1)
     value64 = ws * colsteps / (ms64 / 1000.0)

@@ -27,8 +27,8 @@ OUT_FIELDS = ('precc', 'precl', 'cltot', 'sltend', 'qltend', 'qcltend', 'qiltend
 
 CASES = {
     # name: (workload, kwargs, dt_gl)
-    'workload0_moist_2col': ('workload0', {'ncrms': 2, 'moist': True}, 400.0),
-    'workload1_moist_1col': ('workload1', {'ncrms': 1, 'moist': True}, 100.0),
+    'w32x28_moist_2col': ('workload_32x28', {'ncrms': 2, 'moist': True}, 400.0),
+    'w64x58_moist_1col': ('workload_64x58', {'ncrms': 1, 'moist': True}, 100.0),
 }
 
 

@@ -55,7 +55,7 @@ def test_struct_sizes_match_the_header():
 
 @pytest.mark.skipif(has_gpu(), reason='checks the no-device path')
 def test_create_without_device_fails_loudly(lib):
-    cfg = S.config0()
+    cfg = S.config_32x28()
     cfg.max_ncrms = 4
     st = C.c_int(-1)
     h = lib.crm_create(C.byref(cfg.to_c()), C.byref(st))
@@ -67,7 +67,7 @@ def test_create_without_device_fails_loudly(lib):
 
 def test_invalid_configurations_are_rejected(lib):
     for kw in ({'crm_nx': 30}, {'crm_nx': 7}, {'plev': 20}, {'crm_dt': 40.0}):
-        cfg = S.config0()
+        cfg = S.config_32x28()
         cfg.max_ncrms = 4
         for k, v in kw.items():
             setattr(cfg, k, v)
@@ -76,7 +76,7 @@ def test_invalid_configurations_are_rejected(lib):
         assert not h
         assert st.value in (T.CRM_ERR_ARG, T.CRM_ERR_UNSUPPORTED), kw
     for kw in ({'crm_ny': 4}, {'microphysics': T.CRM_MICRO_M2005}):
-        cfg = S.config0()
+        cfg = S.config_32x28()
         cfg.max_ncrms = 4
         for k, v in kw.items():
             setattr(cfg, k, v)
@@ -88,14 +88,14 @@ def test_invalid_configurations_are_rejected(lib):
 def test_noalloc_rejects_oversize_before_touching_the_device(lib):
     # set-up values of 100000 columns (257 MB) or crm_nx 2048 exceed the fixed
     # 32 MiB scratch of crm_run_device_noalloc; the check needs no GPU
-    cfg = S.config1()
+    cfg = S.config_64x58()
     d = T.CCrmCallDesc(0, 100000, 100000, 100.0, 2, None)
     rc = lib.crm_run_device_noalloc(C.byref(cfg.to_c()), C.byref(d), C.byref(T.CCrmInput()),
                                     C.byref(T.CCrmState()), C.byref(T.CCrmRad()),
                                     C.byref(T.CCrmOutput()), None, None)
     assert rc == T.CRM_ERR_TOO_LARGE
     d = T.CCrmCallDesc(0, 1, 1, 100.0, 2, None)
-    rc = lib.crm_run_device_noalloc(C.byref(S.config1(nx=2048).to_c()), C.byref(d),
+    rc = lib.crm_run_device_noalloc(C.byref(S.config_64x58(nx=2048).to_c()), C.byref(d),
                                     C.byref(T.CCrmInput()), C.byref(T.CCrmState()),
                                     C.byref(T.CCrmRad()), C.byref(T.CCrmOutput()), None, None)
     assert rc == T.CRM_ERR_TOO_LARGE

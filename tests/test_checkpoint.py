@@ -10,7 +10,7 @@ from crm_gb300 import synthetic as S
 
 
 def test_round_trip(tmp_path):
-    cfg, cin, st, rad, desc = S.workload1(ncrms=3, moist=True)
+    cfg, cin, st, rad, desc = S.workload_64x58(ncrms=3, moist=True)
     p = str(tmp_path / 'crm.ckpt')
     CK.save(p, cfg, st, rad.qrad, list(desc._keep))
     cfg2, st2, qrad2, gcol2 = CK.load(p)
@@ -29,7 +29,7 @@ def test_rejects_foreign_and_truncated(tmp_path):
     p.write_bytes(b'not a checkpoint')
     with pytest.raises(ValueError):
         CK.load(str(p))
-    cfg, cin, st, rad, desc = S.workload0(ncrms=2)
+    cfg, cin, st, rad, desc = S.workload_32x28(ncrms=2)
     q = str(tmp_path / 'ok')
     CK.save(q, cfg, st, rad.qrad, list(desc._keep))
     data = open(q, 'rb').read()
@@ -40,7 +40,7 @@ def test_rejects_foreign_and_truncated(tmp_path):
 
 def test_resume_equals_uninterrupted(tmp_path):
     """Two GCM steps in a row == one step, checkpoint, restart, second step."""
-    cfg, cin, st, rad, desc = S.workload0(ncrms=3, moist=True)
+    cfg, cin, st, rad, desc = S.workload_32x28(ncrms=3, moist=True)
     desc.dt_gl = 400.0
     a_st, a_rad = st.copy(), rad.copy()
     for igstep in (1, 2):

@@ -9,7 +9,7 @@ from crm_gb300 import synthetic as S
 
 
 def test_water_identity_holds():
-    for wl in (S.workload0, S.workload1):
+    for wl in (S.workload_32x28, S.workload_64x58):
         cfg, cin, st, rad, desc = wl(ncrms=3, moist=True)
         rc, stat, out = oracle.run(cfg, desc, cin, st, rad)
         assert rc == 0
@@ -18,7 +18,7 @@ def test_water_identity_holds():
 
 
 def test_coupled_steps_keep_the_identity():
-    cfg, cin, st, rad, desc = S.workload0(ncrms=2, moist=True)
+    cfg, cin, st, rad, desc = S.workload_32x28(ncrms=2, moist=True)
     for igstep in (1, 2, 3):
         desc.igstep = igstep
         rc, stat, out = oracle.run(cfg, desc, cin, st, rad)
@@ -32,7 +32,7 @@ def test_coupled_steps_keep_the_identity():
 
 
 def test_energy_identity_holds():
-    for wl, moist in ((S.workload0, False), (S.workload0, True), (S.workload1, True)):
+    for wl, moist in ((S.workload_32x28, False), (S.workload_32x28, True), (S.workload_64x58, True)):
         cfg, cin, st, rad, desc = wl(ncrms=3, moist=moist)
         rad_in = rad.copy()
         rc, stat, out = oracle.run(cfg, desc, cin, st, rad)
@@ -45,7 +45,7 @@ def test_energy_identity_holds():
 def test_energy_identity_detects_a_missing_term():
     """The identity is not vacuous: dropping the surface precipitation term
     of a precipitating column leaves a residual of its size."""
-    cfg, cin, st, rad, desc = S.workload0(ncrms=2, moist=True)
+    cfg, cin, st, rad, desc = S.workload_32x28(ncrms=2, moist=True)
     rad_in = rad.copy()
     rc, stat, out = oracle.run(cfg, desc, cin, st, rad)
     assert rc == 0

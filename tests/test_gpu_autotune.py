@@ -18,7 +18,7 @@ def test_shapes_agree_and_autotune(gpu_lib, precision):
     from crm_gb300.autotune import autotune, shapes
     from crm_gb300.device import DeviceCrmArrays
     from crm_gb300.lib import CrmContext
-    cfg, cin, st, rad, desc = S.workload1(ncrms=24, moist=True, precision=precision)
+    cfg, cin, st, rad, desc = S.workload_64x58(ncrms=24, moist=True, precision=precision)
     desc.dt_gl = 100.0
     cfg.max_ncrms = 24
     ctx = CrmContext(cfg)

@@ -56,8 +56,8 @@ def _check(e):
 
 
 @pytest.mark.parametrize('moist', [False, True])
-def test_fp32_mixed_workload0(gpu_lib, moist):
-    e = _errors(S.workload0, ncrms=4, moist=moist)
+def test_fp32_mixed_32x28(gpu_lib, moist):
+    e = _errors(S.workload_32x28, ncrms=4, moist=moist)
     print('fp32-mixed rel-L2 vs fp64 oracle (32x28, moist=%s):' % moist, e)
     _check(e)
     if moist:
@@ -65,8 +65,8 @@ def test_fp32_mixed_workload0(gpu_lib, moist):
             assert e[n] <= TENDENCY_TARGET, (n, e[n])
 
 
-def test_fp32_mixed_workload1(gpu_lib):
-    e = _errors(S.workload1, ncrms=4)
+def test_fp32_mixed_64x58(gpu_lib):
+    e = _errors(S.workload_64x58, ncrms=4)
     print('fp32-mixed rel-L2 vs fp64 oracle (64x58):', e)
     _check(e)
     assert e['qltend'] <= TENDENCY_TARGET, e['qltend']
@@ -74,7 +74,7 @@ def test_fp32_mixed_workload1(gpu_lib):
 
 def test_fp32_mixed_mean_state_acceleration(gpu_lib):
     def wl(**kw):
-        cfg, cin, st, rad, desc = S.workload0(**kw)
+        cfg, cin, st, rad, desc = S.workload_32x28(**kw)
         cfg = T.CrmConfig(**{**cfg.__dict__, 'use_crm_accel': 1, 'crm_accel_factor': 2.0})
         return cfg, cin, st, rad, desc
     e = _errors(wl, ncrms=4, moist=True)
@@ -87,7 +87,7 @@ def test_fp32_mixed_water_budget(gpu_lib):
     FP64 oracle closes it to ~1e-16 relative; the FP32-mixed form (state kept
     in FP32) to the FP32 rounding of the column water."""
     from test_oracle import water_residual
-    cfg, cin, st, rad, desc = S.workload1(ncrms=4, moist=True)
+    cfg, cin, st, rad, desc = S.workload_64x58(ncrms=4, moist=True)
     cfg.precision = T.CRM_FP32_MIXED
     cfg.max_ncrms = 4
     ctx = CrmContext(cfg)
@@ -105,7 +105,7 @@ def test_fp32_mixed_gcm_water_identity(gpu_lib):
     form: its tendencies are FP64 sums of FP32 fields, so the identity holds
     to the FP32 rounding of the CRM state."""
     from crm_gb300 import gcm_coupling as G
-    cfg, cin, st, rad, desc = S.workload1(ncrms=4, moist=True)
+    cfg, cin, st, rad, desc = S.workload_64x58(ncrms=4, moist=True)
     cfg.precision = T.CRM_FP32_MIXED
     cfg.max_ncrms = 4
     ctx = CrmContext(cfg)
@@ -123,7 +123,7 @@ def test_fp32_mixed_gcm_energy_identity(gpu_lib, moist):
     storage change) for the FP32-mixed form; the FP64 oracle closes it to
     ~1e-8 of its terms."""
     from crm_gb300 import gcm_coupling as G
-    cfg, cin, st, rad, desc = S.workload1(ncrms=4, moist=moist)
+    cfg, cin, st, rad, desc = S.workload_64x58(ncrms=4, moist=moist)
     cfg.precision = T.CRM_FP32_MIXED
     cfg.max_ncrms = 4
     ctx = CrmContext(cfg)
@@ -140,7 +140,7 @@ def test_fp32_mixed_reference_batch_mode(gpu_lib):
     couple the columns the same way (ncycle from the batch), within the
     FP32 bounds of the oracle's batch mode."""
     def wl(**kw):
-        cfg, cin, st, rad, desc = S.workload0(**kw)
+        cfg, cin, st, rad, desc = S.workload_32x28(**kw)
         cfg = T.CrmConfig(**{**cfg.__dict__, 'batch_mode': T.CRM_REFERENCE_BATCH})
         desc.dt_gl = 400.0
         st.w_wind[2, :, :, 10] = 40.0

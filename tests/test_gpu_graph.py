@@ -28,7 +28,7 @@ def _run_graph(gpu_lib, prec, noalloc):
     import torch
     from crm_gb300.device import DeviceCrmArrays
     from crm_gb300.lib import CrmContext, run_device_noalloc
-    cfg, cin, st, rad, desc = S.workload0(ncrms=8, moist=True)
+    cfg, cin, st, rad, desc = S.workload_32x28(ncrms=8, moist=True)
     desc.dt_gl = 200.0
     cfg.precision = prec
     cfg.max_ncrms = desc.ld

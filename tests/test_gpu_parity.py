@@ -61,47 +61,47 @@ def mismatches(a, b):
     return bad
 
 
-def test_fp64_bitexact_workload0_short(gpu_lib):
-    cfg, cin, st, rad, desc = S.workload0(ncrms=4)
+def test_fp64_bitexact_32x28_short(gpu_lib):
+    cfg, cin, st, rad, desc = S.workload_32x28(ncrms=4)
     desc.dt_gl = 200.0          # 10 CRM steps
     assert mismatches(*run_both(cfg, cin, st, rad, desc)) == []
 
 
-def test_fp64_bitexact_workload0_full(gpu_lib):
-    cfg, cin, st, rad, desc = S.workload0(ncrms=16)
+def test_fp64_bitexact_32x28_full(gpu_lib):
+    cfg, cin, st, rad, desc = S.workload_32x28(ncrms=16)
     assert mismatches(*run_both(cfg, cin, st, rad, desc)) == []
 
 
-def test_fp64_bitexact_workload0_moist(gpu_lib):
+def test_fp64_bitexact_32x28_moist(gpu_lib):
     """Supersaturated layers, falling rain and ice: every microphysics branch."""
-    cfg, cin, st, rad, desc = S.workload0(ncrms=4, moist=True)
+    cfg, cin, st, rad, desc = S.workload_32x28(ncrms=4, moist=True)
     a, b = run_both(cfg, cin, st, rad, desc)
     assert a[2].cltot.max() > 0 and a[2].precc.max() > 0
     assert mismatches(a, b) == []
 
 
-def test_fp64_bitexact_workload1(gpu_lib):
+def test_fp64_bitexact_64x58(gpu_lib):
     """64 x 58 columns, dx 1 km, 120 CRM steps."""
-    cfg, cin, st, rad, desc = S.workload1(ncrms=4)
+    cfg, cin, st, rad, desc = S.workload_64x58(ncrms=4)
     assert mismatches(*run_both(cfg, cin, st, rad, desc)) == []
 
 
-def test_fp64_bitexact_workload1_moist(gpu_lib):
-    cfg, cin, st, rad, desc = S.workload1(ncrms=2, moist=True)
+def test_fp64_bitexact_64x58_moist(gpu_lib):
+    cfg, cin, st, rad, desc = S.workload_64x58(ncrms=2, moist=True)
     assert mismatches(*run_both(cfg, cin, st, rad, desc)) == []
 
 
 @pytest.mark.parametrize('nx', [16, 128])
 def test_fp64_bitexact_other_nx(gpu_lib, nx):
     """nx = 128 (a compile-time size) and nx = 16 (the generic kernel)."""
-    cfg, cin, st, rad, desc = S.workload1(ncrms=2, nx=nx, moist=True)
+    cfg, cin, st, rad, desc = S.workload_64x58(ncrms=2, nx=nx, moist=True)
     desc.dt_gl = 300.0
     assert mismatches(*run_both(cfg, cin, st, rad, desc)) == []
 
 
 def test_fp64_bitexact_three_gcm_steps(gpu_lib):
     """State carried across three calls (igstep 1, 2, 3), as in a GCM run."""
-    cfg, cin, st, rad, desc = S.workload0(ncrms=3, moist=True)
+    cfg, cin, st, rad, desc = S.workload_32x28(ncrms=3, moist=True)
     st_o, rad_o, st_g, rad_g = st.copy(), rad.copy(), st.copy(), rad.copy()
     for step in (1, 2, 3):
         desc.igstep = step
@@ -115,7 +115,7 @@ def test_fp64_bitexact_three_gcm_steps(gpu_lib):
 def test_columns_independent_and_ld_padding(gpu_lib):
     """Per-column mode: a column's result is the same alone and in a batch,
     and columns beyond ncrms of a padded (ld > ncrms) array are untouched."""
-    cfg, cin, st, rad, desc = S.workload0(ncrms=5, moist=True)
+    cfg, cin, st, rad, desc = S.workload_32x28(ncrms=5, moist=True)
     st_all = st.copy()
     rad_all = rad.copy()
     rc, _, out_all = run_gpu(cfg, cin, st_all, rad_all, desc)
@@ -139,7 +139,7 @@ def test_columns_independent_and_ld_padding(gpu_lib):
 def test_cfl_violation_is_reported_per_column(gpu_lib):
     """kurant() needs > 16 subcycles: the reference aborts the model
     (kurant.F90:66-75); here only that column reports CRM_ERR_CFL."""
-    cfg, cin, st, rad, desc = S.workload0(ncrms=3)
+    cfg, cin, st, rad, desc = S.workload_32x28(ncrms=3)
     st.w_wind[1, 5, 0, 3] = 400.0
     st_o = st.copy()
     rc_o, stat_o, _ = oracle.run(cfg, desc, cin, st_o, rad.copy())
@@ -153,7 +153,7 @@ def test_device_path_matches_host_path(gpu_lib):
     """crm_run_device on device-resident arrays == crm_run on host arrays."""
     import torch
     from crm_gb300.device import DeviceCrmArrays
-    cfg, cin, st, rad, desc = S.workload0(ncrms=4, moist=True)
+    cfg, cin, st, rad, desc = S.workload_32x28(ncrms=4, moist=True)
     st_h, rad_h = st.copy(), rad.copy()
     rc, _, out_h = run_gpu(cfg, cin, st_h, rad_h, desc)
     assert rc == 0
@@ -172,7 +172,7 @@ def test_col_map_matches_oracle(gpu_lib):
     """A call over slots (3, 0, 4) of a 5-column batch (col_map), bit for bit
     against the oracle given the same map."""
     import ctypes as C
-    cfg, cin, st, rad, desc = S.workload0(ncrms=5, moist=True)
+    cfg, cin, st, rad, desc = S.workload_32x28(ncrms=5, moist=True)
     slots = np.array([3, 0, 4], dtype=np.int32)
     d = T.call_desc(3, 5, 400.0, desc.igstep, np.asarray(desc._keep)[slots])
     d.col_map = slots.ctypes.data_as(C.POINTER(C.c_int))
@@ -190,7 +190,7 @@ def _accel(cfg, factor=2.0, uv=0):
 def test_fp64_bitexact_mean_state_acceleration(gpu_lib, uv):
     """use_crm_accel with crm_accel_factor 2 (the sam1mom production default),
     with and without crm_accel_uv."""
-    cfg, cin, st, rad, desc = S.workload0(ncrms=4, moist=True)
+    cfg, cin, st, rad, desc = S.workload_32x28(ncrms=4, moist=True)
     desc.dt_gl = 600.0
     assert mismatches(*run_both(_accel(cfg, 2.0, uv), cin, st, rad, desc)) == []
 
@@ -198,7 +198,7 @@ def test_fp64_bitexact_mean_state_acceleration(gpu_lib, uv):
 def test_fp64_bitexact_acceleration_cease(gpu_lib):
     """A column heated ~10 K per step stops accelerating (nstop stretched);
     its batch mate keeps accelerating."""
-    cfg, cin, st, rad, desc = S.workload1(ncrms=2, moist=True)
+    cfg, cin, st, rad, desc = S.workload_64x58(ncrms=2, moist=True)
     desc.dt_gl = 300.0
     rad.qrad[1, :, :, 5:8] = 1.0
     assert mismatches(*run_both(_accel(cfg, 2.0), cin, st, rad, desc)) == []
@@ -208,10 +208,10 @@ def test_fp64_bitexact_reference_batch_mode(gpu_lib):
     """CRM_REFERENCE_BATCH on the GPU (one cooperative launch, grid-wide
     maxima): one column strong enough to need sub-cycling sets ncycle for the
     whole batch, bit for bit as the oracle's batch mode does."""
-    cfg, cin, st, rad, desc = S.workload0(ncrms=4, moist=True)
+    cfg, cin, st, rad, desc = S.workload_32x28(ncrms=4, moist=True)
     desc.dt_gl = 400.0
     st.w_wind[2, :, :, 10] = 40.0
-    bcfg = S.config0(batch_mode=T.CRM_REFERENCE_BATCH)
+    bcfg = S.config_32x28(batch_mode=T.CRM_REFERENCE_BATCH)
     a, b = run_both(bcfg, cin, st, rad, desc)
     assert mismatches(a, b) == []
     # the coupling is real: per-column mode gives the other columns other bits
@@ -223,10 +223,10 @@ def test_fp64_bitexact_reference_batch_mode(gpu_lib):
 def test_fp64_bitexact_reference_batch_acceleration_cease(gpu_lib):
     """Batch mode with mean-state acceleration: one hot column stops the
     acceleration of every column (one cease flag per batch)."""
-    cfg, cin, st, rad, desc = S.workload0(ncrms=3)
+    cfg, cin, st, rad, desc = S.workload_32x28(ncrms=3)
     desc.dt_gl = 600.0
     rad.qrad[1, :, :, 5:8] = 0.5
-    bcfg = _accel(S.config0(batch_mode=T.CRM_REFERENCE_BATCH), 2.0)
+    bcfg = _accel(S.config_32x28(batch_mode=T.CRM_REFERENCE_BATCH), 2.0)
     assert mismatches(*run_both(bcfg, cin, st, rad, desc)) == []
 
 
@@ -235,8 +235,8 @@ def test_fp64_bitexact_mixed_precipitating_columns(gpu_lib):
     skips sedimentation and qp transport for a column whose fall speeds are
     all zero or whose qp is +0 everywhere, which must change no bit — signs
     of zero included — of any column's state or outputs."""
-    cfg, cin, st, rad, desc = S.workload0(ncrms=6, moist=True)
-    _, cin_d, st_d, _, _ = S.workload0(ncrms=6, moist=False)
+    cfg, cin, st, rad, desc = S.workload_32x28(ncrms=6, moist=True)
+    _, cin_d, st_d, _, _ = S.workload_32x28(ncrms=6, moist=False)
     for c in (1, 3, 5):                       # dry columns between moist ones
         for n in ('qt', 'qp', 'qn', 'temperature'):
             getattr(st, n)[c] = getattr(st_d, n)[c]
@@ -258,7 +258,7 @@ def test_col_map_slot_out_of_range_is_reported_per_column(gpu_lib):
     kernels before they touch that slot: its position reports
     CRM_ERR_ARG, the other positions integrate as in a call without it."""
     import ctypes as C
-    cfg, cin, st, rad, desc = S.workload0(ncrms=5, moist=True)
+    cfg, cin, st, rad, desc = S.workload_32x28(ncrms=5, moist=True)
     desc.dt_gl = 200.0
     keep = np.asarray(desc._keep)
     good = np.array([3, 0], dtype=np.int32)

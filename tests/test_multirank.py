@@ -48,7 +48,7 @@ def _worker(rank, world, port, outdir):
     os.environ['MASTER_ADDR'] = '127.0.0.1'
     os.environ['MASTER_PORT'] = str(port)
     dist.init_process_group('gloo', rank=rank, world_size=world)
-    cfg, cin, st, rad, desc = S.workload0(ncrms=NCOLS, moist=True)
+    cfg, cin, st, rad, desc = S.workload_32x28(ncrms=NCOLS, moist=True)
     first, count = column_shard(NCOLS, rank, world)
     cols = list(range(first, first + count))
     d = T.call_desc(count, count, 200.0, desc.igstep, np.asarray(desc._keep)[cols])
@@ -74,7 +74,7 @@ def test_two_gloo_ranks_match_one_process(tmp_path):
     port = _free_port()
     mp.spawn(_worker, args=(2, port, str(tmp_path)), nprocs=2, join=True)
     got = np.load(os.path.join(tmp_path, 'gathered.npz'))
-    cfg, cin, st, rad, desc = S.workload0(ncrms=NCOLS, moist=True)
+    cfg, cin, st, rad, desc = S.workload_32x28(ncrms=NCOLS, moist=True)
     desc.dt_gl = 200.0
     rc, stat, out = oracle.run(cfg, desc, cin, st, rad)
     assert rc == 0

@@ -57,7 +57,7 @@ def water_residual(cfg, cin, st0, st1, out, dt_gl):
 
 @pytest.mark.parametrize('moist', [False, True])
 def test_water_budget_closes_32x28(moist):
-    cfg, cin, st, rad, desc = S.workload0(ncrms=4, moist=moist)
+    cfg, cin, st, rad, desc = S.workload_32x28(ncrms=4, moist=moist)
     rc, stat, st1, _, out = _run(cfg, cin, st, rad, desc)
     assert rc == 0 and not stat.any()
     r = water_residual(cfg, cin, st, st1, out, desc.dt_gl)
@@ -67,7 +67,7 @@ def test_water_budget_closes_32x28(moist):
 
 
 def test_water_budget_closes_64x58():
-    cfg, cin, st, rad, desc = S.workload1(ncrms=2, moist=True)
+    cfg, cin, st, rad, desc = S.workload_64x58(ncrms=2, moist=True)
     desc.dt_gl = 300.0
     rc, stat, st1, _, out = _run(cfg, cin, st, rad, desc)
     assert rc == 0 and not stat.any()
@@ -76,7 +76,7 @@ def test_water_budget_closes_64x58():
 
 
 def test_thread_count_does_not_change_results():
-    cfg, cin, st, rad, desc = S.workload0(ncrms=6, moist=True)
+    cfg, cin, st, rad, desc = S.workload_32x28(ncrms=6, moist=True)
     desc.dt_gl = 400.0
     a = _run(cfg, cin, st, rad, desc, nthreads=1)
     b = _run(cfg, cin, st, rad, desc, nthreads=3)
@@ -84,7 +84,7 @@ def test_thread_count_does_not_change_results():
 
 
 def test_columns_independent_of_batch_mates():
-    cfg, cin, st, rad, desc = S.workload0(ncrms=6, moist=True)
+    cfg, cin, st, rad, desc = S.workload_32x28(ncrms=6, moist=True)
     desc.dt_gl = 400.0
     full = _run(cfg, cin, st, rad, desc)
     gcol = np.asarray(desc._keep)
@@ -99,10 +99,10 @@ def test_columns_independent_of_batch_mates():
 
 
 def test_reference_batch_mode_equals_per_column_without_subcycling():
-    cfg, cin, st, rad, desc = S.workload0(ncrms=4, moist=True)
+    cfg, cin, st, rad, desc = S.workload_32x28(ncrms=4, moist=True)
     desc.dt_gl = 400.0
     a = _run(cfg, cin, st, rad, desc)
-    cfg_b = S.config0(batch_mode=T.CRM_REFERENCE_BATCH)
+    cfg_b = S.config_32x28(batch_mode=T.CRM_REFERENCE_BATCH)
     b = _run(cfg_b, cin, st, rad, desc)
     assert a[0] == 0 and b[0] == 0
     assert not _equal(a[2:], b[2:])
@@ -114,7 +114,7 @@ def test_translation_invariance():
     # shift-equivariant, only to ~1e-7 relative: a shifted run differs at that
     # level in the pressure correction.  An indexing or halo error would show
     # as an O(1) difference of the perturbation fields.
-    cfg, cin, st, rad, desc = S.workload0(ncrms=2)
+    cfg, cin, st, rad, desc = S.workload_32x28(ncrms=2)
     d = T.call_desc(2, 2, 100.0, 2, desc._keep)     # igstep 2: no setperturb
     a = _run(cfg, cin, st, rad, d)
     sh = 5
@@ -136,7 +136,7 @@ def test_translation_invariance():
 
 
 def test_uniform_state_stays_uniform():
-    cfg, cin, st, rad, desc = S.workload0(ncrms=2)
+    cfg, cin, st, rad, desc = S.workload_32x28(ncrms=2)
     st.temperature[...] = st.temperature[:, :1]     # drop the seeded perturbation
     d = T.call_desc(2, 2, 400.0, 2, desc._keep)     # and setperturb
     _, stat, st1, _, _ = _run(cfg, cin, st, rad, d)
@@ -147,7 +147,7 @@ def test_uniform_state_stays_uniform():
 
 
 def test_cfl_violation_flags_only_that_column():
-    cfg, cin, st, rad, desc = S.workload0(ncrms=3)
+    cfg, cin, st, rad, desc = S.workload_32x28(ncrms=3)
     desc.dt_gl = 100.0
     st.w_wind[1, :, :, 10] = 2000.0
     rc, stat, st1, _, out = _run(cfg, cin, st, rad, desc)
@@ -163,7 +163,7 @@ def test_col_map_selects_slots():
     """A call over slots (3, 0) of a 5-column batch equals a call over a
     2-column batch holding those columns; other slots are untouched."""
     import ctypes as C
-    cfg, cin, st, rad, desc = S.workload0(ncrms=5, moist=True)
+    cfg, cin, st, rad, desc = S.workload_32x28(ncrms=5, moist=True)
     gcol = np.asarray(desc._keep)
     slots = np.array([3, 0], dtype=np.int32)
     d = T.call_desc(2, 5, 400.0, desc.igstep, gcol[slots])
@@ -186,7 +186,7 @@ def _accel(cfg, factor=2.0, uv=0):
 
 
 def test_accel_requires_dividing_factor():
-    cfg, cin, st, rad, desc = S.workload0(ncrms=2)
+    cfg, cin, st, rad, desc = S.workload_32x28(ncrms=2)
     desc.dt_gl = 200.0                       # nstop 10: 1 + 2 does not divide it
     rc, _, _ = oracle.run(_accel(cfg, 2.0), desc, cin, st.copy(), rad.copy())
     assert rc == T.CRM_ERR_ARG
@@ -196,7 +196,7 @@ def test_accel_requires_dividing_factor():
 
 @pytest.mark.parametrize('uv', [0, 1])
 def test_accel_changes_mean_state_and_matches_batch_mode(uv):
-    cfg, cin, st, rad, desc = S.workload0(ncrms=3, moist=True)
+    cfg, cin, st, rad, desc = S.workload_32x28(ncrms=3, moist=True)
     desc.dt_gl = 600.0                       # 30 steps -> 10 accelerated steps
     plain = _run(cfg, cin, st, rad, desc)
     acc = _run(_accel(cfg, 2.0, uv), cin, st, rad, desc)
@@ -204,7 +204,7 @@ def test_accel_changes_mean_state_and_matches_batch_mode(uv):
     for n, v in acc[2].arrays().items():
         assert np.all(np.isfinite(v)), n
     assert not np.array_equal(acc[2].temperature, plain[2].temperature)
-    bcfg = _accel(S.config0(batch_mode=T.CRM_REFERENCE_BATCH), 2.0, uv)
+    bcfg = _accel(S.config_32x28(batch_mode=T.CRM_REFERENCE_BATCH), 2.0, uv)
     batch = _run(bcfg, cin, st, rad, desc)
     assert batch[0] == 0
     assert not _equal(acc[2:], batch[2:])
@@ -213,7 +213,7 @@ def test_accel_changes_mean_state_and_matches_batch_mode(uv):
 def test_accel_ceases_on_large_mean_temperature_change():
     """A column heated by ~10 K per step trips the 5 K limit: acceleration
     stops and the remaining steps run unaccelerated (nstop stretched)."""
-    cfg, cin, st, rad, desc = S.workload0(ncrms=2)
+    cfg, cin, st, rad, desc = S.workload_32x28(ncrms=2)
     desc.dt_gl = 600.0
     rad_hot = rad.copy()
     rad_hot.qrad[1, :, :, 5:8] = 0.5         # K/s in column 1 only

@@ -59,15 +59,15 @@ def test_hbm_budget():
 
 
 def test_slot_bytes_scale():
-    small = slot_bytes(S.config1(nx=32))
-    big = slot_bytes(S.config1(nx=128))
+    small = slot_bytes(S.config_64x58(nx=32))
+    big = slot_bytes(S.config_64x58(nx=128))
     assert 3.5 < big / small < 4.1
     # 120 GB holds ~10^5 columns of 128 x 58
     assert 120 * 2 ** 30 // big > 50_000
 
 
 def test_apply_tendencies():
-    cfg, cin, st, rad, desc = S.workload0(ncrms=3)
+    cfg, cin, st, rad, desc = S.workload_32x28(ncrms=3)
     t0, q0 = cin.tl.copy(), cin.ql.copy()
     vals = {'sltend': np.full((3, cfg.plev), 1004.64), 'qltend': np.full((3, cfg.plev), -1e-9),
             'qcltend': np.zeros((3, cfg.plev)), 'qiltend': np.zeros((3, cfg.plev))}

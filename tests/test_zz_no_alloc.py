@@ -51,29 +51,29 @@ def _pair(gpu_lib, cfg, cin, st, rad, desc, calls=2):
     ctx.close()
 
 
-def test_noalloc_matches_fp64_workload0(gpu_lib):
-    cfg, cin, st, rad, desc = S.workload0(ncrms=16, moist=True)
+def test_noalloc_matches_fp64_32x28(gpu_lib):
+    cfg, cin, st, rad, desc = S.workload_32x28(ncrms=16, moist=True)
     desc.dt_gl = 200.0
     _pair(gpu_lib, cfg, cin, st, rad, desc)
 
 
-def test_noalloc_matches_fp64_workload1_looped(gpu_lib):
+def test_noalloc_matches_fp64_64x58_looped(gpu_lib):
     # 48 columns of 64 x 58 in FP64 need about 68 MB of slabs: the 32 MiB
     # scratch holds 21, so each CTA runs two or three columns in turn.
-    cfg, cin, st, rad, desc = S.workload1(ncrms=48, moist=True)
+    cfg, cin, st, rad, desc = S.workload_64x58(ncrms=48, moist=True)
     desc.dt_gl = 100.0
     _pair(gpu_lib, cfg, cin, st, rad, desc)
 
 
-def test_noalloc_matches_fp32_workload1(gpu_lib):
-    cfg, cin, st, rad, desc = S.workload1(ncrms=64, precision=T.CRM_FP32_MIXED)
+def test_noalloc_matches_fp32_64x58(gpu_lib):
+    cfg, cin, st, rad, desc = S.workload_64x58(ncrms=64, precision=T.CRM_FP32_MIXED)
     desc.dt_gl = 100.0
     _pair(gpu_lib, cfg, cin, st, rad, desc)
 
 
 def test_noalloc_rejects_oversize(gpu_lib):
     import ctypes as C
-    cfg, cin, st, rad, desc = S.workload1(ncrms=4)
+    cfg, cin, st, rad, desc = S.workload_64x58(ncrms=4)
     # 100000 columns of set-up values alone (257 MB) exceed the scratch; the
     # size check runs before any device work and before the array pointers
     # are looked at, so empty argument structs are enough here.
@@ -82,7 +82,7 @@ def test_noalloc_rejects_oversize(gpu_lib):
                                         C.byref(T.CCrmState()), C.byref(T.CCrmRad()),
                                         C.byref(T.CCrmOutput()), None, None)
     assert rc == T.CRM_ERR_TOO_LARGE
-    big = S.config1(nx=2048)
+    big = S.config_64x58(nx=2048)
     d = T.CCrmCallDesc(0, 1, 1, 100.0, 2, None)
     rc = gpu_lib.crm_run_device_noalloc(C.byref(big.to_c()), C.byref(d), C.byref(T.CCrmInput()),
                                         C.byref(T.CCrmState()), C.byref(T.CCrmRad()),
