@@ -279,3 +279,12 @@ def test_col_map_slot_out_of_range_is_reported_per_column(gpu_lib):
         assert np.array_equal(x, getattr(st_b, n)), n
     for n, x in out_a.arrays().items():
         assert np.array_equal(x[[3, 0]], getattr(out_b, n)[[3, 0]]), n
+
+
+@pytest.mark.parametrize('seed', range(4))
+def test_fp64_bitexact_random_columns(gpu_lib, seed):
+    """Random soundings, surface fluxes, winds, moisture and call lengths
+    (the cases of test_oracle_properties.py): bit for bit."""
+    from test_oracle_properties import _case
+    cfg, cin, st, rad, desc, ncol = _case(seed)
+    assert mismatches(*run_both(cfg, cin, st, rad, desc)) == []
