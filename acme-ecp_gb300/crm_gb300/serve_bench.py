@@ -126,7 +126,9 @@ def measure_peak(server, configs, steps, duration, concurrency=64, seed=1):
 
 
 def run_load(server, configs, steps, rate_colsteps, duration, seed=2):
-    """Open loop: Poisson chunk arrivals offering `rate_colsteps`."""
+    """Open loop: Poisson chunk arrivals offering `rate_colsteps` (> 0)."""
+    if not rate_colsteps > 0:
+        raise ValueError('run_load needs a positive offered rate, got %r' % (rate_colsteps,))
     mean_work = 32.5 * (DT_GL / 10.0) * steps        # E[ncol] * nstop * steps per chunk
     lam = rate_colsteps / mean_work                  # chunks per second
     d = Driver(server, configs, steps, seed)

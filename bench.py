@@ -207,6 +207,7 @@ def main():
     cells = cfg32.crm_nx * cfg32.crm_ny * cfg32.crm_nz
 
     tuned = {}
+    medians = {}        # median per-step time of each form on this rank [ms]
 
     def device_rate(cfg, steps, warmup):
         ctx = CrmContext(cfg)
@@ -227,14 +228,18 @@ def main():
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         tot = 0.0
+        step_ms = []
         for _ in range(steps):
             dev.reset_state(st)
             e0.record()
             ctx.run_device(dev, stream)
             e1.record()
             e1.synchronize()
-            tot += e0.elapsed_time(e1)
+            dt = e0.elapsed_time(e1)
+            tot += dt
+            step_ms.append(dt)
             kms.append(ctx.last_kernel_ms)
+        medians['fp64' if cfg.precision == T.CRM_FP64 else 'fp32'] = float(np.median(step_ms))
         barrier()
         t = torch.tensor([tot], device='cuda')
         if ws > 1:
@@ -316,16 +321,21 @@ def main():
             server.pool(config_key(c))
         steps_per_chunk = 8
         pk = SB.measure_peak(server, scfg, steps_per_chunk, args.serve_seconds)
-        ld = SB.run_load(server, scfg, steps_per_chunk, 0.8 * pk['column_steps_per_s'], args.serve_seconds)
+        if pk['column_steps_per_s'] > 0:
+            ld = SB.run_load(server, scfg, steps_per_chunk, 0.8 * pk['column_steps_per_s'],
+                             args.serve_seconds)
+            serving = {'workload': 'chunks of U{1..64} columns, crm_nx in {32,64,128}, crm_nz in {28,58}, '
+                                   '72 levels, dt_gl 1200 s, %d GCM steps per chunk, Poisson arrivals, '
+                                   'FP32-mixed, 120 GB HBM budget' % steps_per_chunk,
+                       'peak_column_steps_per_s': pk['column_steps_per_s'],
+                       'load': 0.8, 'offered_column_steps_per_s': ld['offered_column_steps_per_s'],
+                       'column_steps_per_s': ld['column_steps_per_s'],
+                       'p50_ms': ld['p50_ms'], 'p99_ms': ld['p99_ms'], 'chunk_steps': ld['steps'],
+                       'launches': server.launches}
+        else:
+            # a window too short for any chunk-step to finish
+            serving = {'skipped': 'no chunk-step completed in the %.1f s peak window' % args.serve_seconds}
         server.close()
-        serving = {'workload': 'chunks of U{1..64} columns, crm_nx in {32,64,128}, crm_nz in {28,58}, '
-                               '72 levels, dt_gl 1200 s, %d GCM steps per chunk, Poisson arrivals, '
-                               'FP32-mixed, 120 GB HBM budget' % steps_per_chunk,
-                   'peak_column_steps_per_s': pk['column_steps_per_s'],
-                   'load': 0.8, 'offered_column_steps_per_s': ld['offered_column_steps_per_s'],
-                   'column_steps_per_s': ld['column_steps_per_s'],
-                   'p50_ms': ld['p50_ms'], 'p99_ms': ld['p99_ms'], 'chunk_steps': ld['steps'],
-                   'launches': server.launches}
 
     if rank != 0:
         if ws > 1:
@@ -367,7 +377,8 @@ def main():
                   'sample': 'failed: %s' % e}
     line = {
         'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': ws, 'steps': args.steps,
-        'warmup': args.warmup, 'ms_per_step': ms32, 'higher_is_better': True,
+        'warmup': args.warmup, 'ms_per_step': ms32, 'ms_per_step_median': medians.get('fp32'),
+        'higher_is_better': True,
         'scaling': 'weak', 'vs_baseline': None,
         'dtype': 'f32 (f64 tridiagonal solve, domain sums, saturation Newton)',
         'data': 'synthetic (idealised soundings, seeded)',
@@ -384,7 +395,8 @@ def main():
                 'ms_per_step': e2e_ms},
         'clocks': clk,
         'gpu_launches': 2 * args.steps,   # crm_prep_kernel + crm_columns_kernel per timed step
-        'fp64_plain': {'value': value64, 'unit': UNIT, 'ms_per_step': ms64, 'steps': args.fp64_steps,
+        'fp64_plain': {'value': value64, 'unit': UNIT, 'ms_per_step': ms64,
+                       'ms_per_step_median': medians.get('fp64'), 'steps': args.fp64_steps,
                        'fp64_pipe': fp64_pipe},
         'fp32_over_fp64': value / value64,
         'fp32_rel_l2_vs_fp64_state': errs,
