@@ -99,3 +99,40 @@ def test_noalloc_rejects_oversize_before_touching_the_device(lib):
                                     C.byref(T.CCrmInput()), C.byref(T.CCrmState()),
                                     C.byref(T.CCrmRad()), C.byref(T.CCrmOutput()), None, None)
     assert rc == T.CRM_ERR_TOO_LARGE
+
+
+def _c_struct_fields(name):
+    src = open(os.path.join(REPO, 'include', 'crm_gb300.h')).read()
+    src = re.sub(r'/\*.*?\*/', '', src, flags=re.S)
+    body = re.search(r'typedef struct %s \{(.*?)\} %s;' % (name, name), src, flags=re.S).group(1)
+    fields = []
+    for decl in body.split(';'):
+        decl = decl.strip()
+        if not decl:
+            continue
+        decl = re.sub(r'^(const\s+)?(int|double|unsigned)\s*', '', decl)
+        fields += [f.strip().lstrip('*').strip() for f in decl.split(',')]
+    return fields
+
+
+def _fortran_type_fields(doc, name):
+    body = re.search(r'type, bind\(C\) :: %s\n(.*?)\n\s*end type' % name, doc, flags=re.S).group(1)
+    body = body.replace('&\n', ' ')
+    fields = []
+    for line in body.splitlines():
+        line = line.split('!')[0]
+        if '::' in line:
+            fields += [f.strip() for f in line.split('::')[1].split(',') if f.strip()]
+    return fields
+
+
+def test_integration_fortran_binding_mirrors_the_header():
+    """The bind(C) types a maintainer copies from INTEGRATION.md declare the
+    same components, in the same order, as include/crm_gb300.h."""
+    doc = open(os.path.join(REPO, 'INTEGRATION.md')).read()
+    for c_name, f_name in (('crm_config', 'crm_config_c'), ('crm_call_desc', 'crm_call_desc_c'),
+                           ('crm_input_c', 'crm_input_c'), ('crm_state_c', 'crm_state_c'),
+                           ('crm_rad_c', 'crm_rad_c')):
+        assert _fortran_type_fields(doc, f_name) == _c_struct_fields(c_name), c_name
+    n = int(re.search(r'field\((\d+)\)', doc).group(1))
+    assert n == len(T.OUTPUT_FIELDS)
