@@ -74,3 +74,16 @@ def test_apply_tendencies():
     apply_tendencies(cin, vals, 10.0)
     assert np.allclose(cin.tl - t0, 10.0)
     assert np.all(cin.ql >= 0) and np.allclose(cin.ql, np.maximum(q0 - 1e-8, 0))
+
+
+def test_config_key_groups_by_physics_not_capacity():
+    from crm_gb300 import crm_types as T
+    from crm_gb300.serving import config_key
+    a = S.config_64x58()
+    b = S.config_64x58()
+    b.max_ncrms = 4096                                   # capacity only
+    assert config_key(a) == config_key(b)
+    for change in ({'crm_nx': 32}, {'crm_nz': 28}, {'precision': T.CRM_FP32_MIXED},
+                   {'use_crm_accel': 1}, {'crm_dt': 20.0}, {'batch_mode': T.CRM_REFERENCE_BATCH}):
+        c = T.CrmConfig(**{**a.__dict__, **change})
+        assert config_key(c) != config_key(a), change
