@@ -136,3 +136,19 @@ def test_integration_fortran_binding_mirrors_the_header():
         assert _fortran_type_fields(doc, f_name) == _c_struct_fields(c_name), c_name
     n = int(re.search(r'field\((\d+)\)', doc).group(1))
     assert n == len(T.OUTPUT_FIELDS)
+
+
+def test_launch_shape_table(lib):
+    """The shape table the autotuner walks is readable without a device:
+    whole warps, at most 1024 threads, register budgets that fit an SM
+    (at most 2048 threads per SM), and an
+    out-of-range index refused."""
+    from crm_gb300.autotune import shapes
+    table = shapes()
+    assert len(table) == lib.crm_num_launch_shapes() >= 5
+    for s, threads, ctas, planes in table:
+        assert threads % 32 == 0 and 32 <= threads <= 1024, s
+        assert 1 <= ctas and threads * ctas <= 2048, s
+        assert planes in (0, 2), s
+    t, c, m = C.c_int(), C.c_int(), C.c_int()
+    assert lib.crm_launch_shape_info(len(table), C.byref(t), C.byref(c), C.byref(m)) != 0
