@@ -4,6 +4,12 @@
 // TEST INFRASTRUCTURE ONLY: loaded by tests/, __graft_entry__.smoke() and the
 // CPU-baseline leg of bench.py.  The product never links or calls this file.
 //
+// PARITY UNPINNED: the reference ships no golden vectors or fixtures for
+// crm(), and its Fortran cannot be compiled here, so this restatement is not
+// checked against outputs of the reference itself; it is held to the
+// reference's conservation identities and to mathematical properties
+// (tests/test_oracle*.py, tests/test_gcm_coupling.py).
+//
 // Every routine follows the reference source named in its comment line by
 // line, including the Fortran numerics contract of the reference build:
 //  * unsuffixed real literals are default REAL (FP32) and are rounded to float

@@ -3,6 +3,10 @@
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
 CPU-baseline leg of bench.py, never by the library itself.
 
+PARITY UNPINNED: no reference outputs exist to check the restatement against
+(no golden vectors in the reference, no Fortran compiler to run it); it is
+held to conservation identities and mathematical properties instead.
+
 The restatement is compiled with -ffp-contract=off so that every floating
 point operation is a separately rounded IEEE operation, the same contract the
 FP64 device form is compiled with (nvcc -fmad=false).
