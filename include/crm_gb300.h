@@ -230,6 +230,10 @@ int crm_run_device_noalloc(const crm_config *cfg, const crm_call_desc *desc,
                            const crm_input_c *in, crm_state_c *state, crm_rad_c *rad,
                            crm_output_c *out, int *col_status, void *stream);
 
+/* Handle services with no counterpart in the reference (its crm() runs on
+ * the calling thread with no stream, timer or status API; errors go to
+ * endrun, e.g. kurant.F90:66-75). */
+
 /* Number of kernel launches issued by the last crm_run on this handle. */
 int crm_last_launch_count(const crm_ctx *ctx);
 /* Duration of the compute kernels of the last crm_run [ms] (CUDA events on
@@ -237,6 +241,7 @@ int crm_last_launch_count(const crm_ctx *ctx);
 double crm_last_kernel_ms(const crm_ctx *ctx);
 /* Bind the handle to a CUDA stream (cudaStream_t passed as void*). */
 int crm_set_stream(crm_ctx *ctx, void *stream);
+/* Text of a crm_status (what the reference would have passed to endrun). */
 const char *crm_status_string(int status);
 /* Per-phase cycle counters of the column kernel, summed over its CTAs since
  * the last read, in a profiling build of the library (compiled with
@@ -247,8 +252,8 @@ int crm_debug_phase_cycles(crm_ctx *ctx, unsigned long long *out, int n);
 /* Launch shapes of the column kernel (threads per CTA, CTAs per SM the
  * register budget is sized for, scratch planes in shared memory): the search
  * space of an autotuner (crm_gb300/autotune.py).  FP64 results do not
- * depend on the shape; FP32-mixed results agree to FP32 rounding.  No counterpart in the reference (its OpenACC schedule is the
- * compiler's).  By default a handle chooses per call: the shape with the
+ * depend on the shape; FP32-mixed results agree to FP32 rounding.  No
+ * counterpart in the reference (its OpenACC schedule is the compiler's).  By default a handle chooses per call: the shape with the
  * most threads per column among those that hold the whole call at once
  * (latency), else the measured throughput default.  crm_set_launch_shape
  * fixes one for later calls (-1: back to the per-call choice); CRM_ERR_ARG
