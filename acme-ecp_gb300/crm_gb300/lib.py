@@ -17,7 +17,8 @@ LIB_PATH = os.path.join(HERE, 'libcrm_gb300.so')
 EXPORTS = ('crm_create', 'crm_destroy', 'crm_run', 'crm_run_device', 'crm_last_launch_count',
            'crm_last_kernel_ms', 'crm_set_stream', 'crm_status_string', 'crm_version',
            'crm_debug_phase_cycles', 'crm_run_device_noalloc', 'crm_num_launch_shapes',
-           'crm_launch_shape_info', 'crm_set_launch_shape', 'crm_get_launch_shape')
+           'crm_launch_shape_info', 'crm_set_launch_shape', 'crm_get_launch_shape',
+           'crm_device_bytes', 'crm_plan_device_bytes', 'crm_debug_barrier_test')
 
 _lib = None
 
@@ -75,6 +76,12 @@ def load(path=None, build_if_missing=False):
     lib.crm_set_launch_shape.argtypes = [C.c_void_p, C.c_int]
     lib.crm_get_launch_shape.restype = C.c_int
     lib.crm_get_launch_shape.argtypes = [C.c_void_p]
+    lib.crm_debug_barrier_test.restype = C.c_int
+    lib.crm_debug_barrier_test.argtypes = [C.c_void_p, C.c_longlong, C.c_int]
+    lib.crm_device_bytes.restype = C.c_ulonglong
+    lib.crm_device_bytes.argtypes = [C.c_void_p]
+    lib.crm_plan_device_bytes.restype = C.c_int
+    lib.crm_plan_device_bytes.argtypes = [C.POINTER(T.CCrmConfig), C.POINTER(C.c_ulonglong)]
     lib.crm_debug_phase_cycles.restype = C.c_int
     lib.crm_debug_phase_cycles.argtypes = [C.c_void_p, C.POINTER(C.c_ulonglong), C.c_int]
     _lib = lib
@@ -86,6 +93,17 @@ def status_string(s):
         return load().crm_status_string(int(s)).decode()
     except OSError:
         return 'status %d' % s
+
+
+def plan_device_bytes(cfg):
+    """Device bytes crm_create would allocate for cfg (nothing allocated)."""
+    lib = load()
+    n = C.c_ulonglong(0)
+    c_cfg = cfg.to_c()
+    rc = lib.crm_plan_device_bytes(C.byref(c_cfg), C.byref(n))
+    if rc != T.CRM_OK:
+        raise CrmError(rc, 'crm_plan_device_bytes')
+    return int(n.value)
 
 
 def run_device_noalloc(cfg, dev, stream=0):
@@ -162,6 +180,11 @@ class CrmContext:
         buf = (C.c_ulonglong * n)()
         m = self._lib.crm_debug_phase_cycles(self._h, buf, n)
         return None if m < 0 else [int(buf[i]) for i in range(m)]
+
+    @property
+    def device_bytes(self):
+        """Device memory this handle holds [bytes]."""
+        return int(self._lib.crm_device_bytes(self._h))
 
     @property
     def last_kernel_ms(self):

@@ -7,15 +7,24 @@ state in the physics buffer between GCM steps (pbuf 'global' fields,
 crm_physics.F90:126-191).  Here the same two facts are organised for a GPU
 that serves many chunks at once:
 
+  * each configuration gets a device-resident pool of column slots; the
+    pool's device memory (its slot arrays and the handles' column slabs) is
+    charged to the HBM budget when the pool is created, before anything is
+    allocated, and a pool is made smaller, or idle pools of other
+    configurations are released, when the budget cannot hold a full one;
+    a new configuration that does not fit at all is refused (BudgetError,
+    CRM_ERR_BUDGET);
   * each chunk (1..64 GCM columns of one CRM configuration) is *admitted*:
-    it receives slots in a device-resident pool of its configuration, if the
-    pool has room and the HBM budget allows; otherwise it waits;
+    it receives slots in its configuration's pool if the pool has room;
+    otherwise it waits;
   * its CRM state stays in those slots across GCM steps; a step request
     carries only the new GCM input profiles;
   * the engine thread gathers every step request that is waiting, groups
     them by configuration and launches ONE column kernel per group over the
     union of their slots (crm_run_device with a col_map), so requests that
-    arrive while others are on the GPU join the next launch; groups of
+    arrive while others are on the GPU join the next launch; a chunk has at
+    most one step in flight (its next request waits until the current one
+    completes, since both would integrate the same slots); groups of
     different configurations and successive launches of one configuration
     run on their own streams and overlap on the device;
   * results (the crm_output fields a GCM step consumes) are copied back per
@@ -67,8 +76,13 @@ class SlotPool:
         return len(self._free)
 
 
+class BudgetError(RuntimeError):
+    """A configuration's pool does not fit the HBM budget (CRM_ERR_BUDGET)."""
+    status = T.CRM_ERR_BUDGET
+
+
 class HbmBudget:
-    """Bytes of device memory the service may hold for resident columns."""
+    """Bytes of device memory the service may hold (pools and handles)."""
 
     def __init__(self, total_bytes):
         self.total = int(total_bytes)
@@ -97,6 +111,13 @@ def slot_bytes(cfg):
     inp = 11 * (plev + 1) + 10
     out = 6 * nx * nz + nx + 16 + 39 * plev
     return 8 * (state + rad + inp + out) + 8
+
+
+def pool_bytes(cfg, capacity, handles, handle_bytes):
+    """Device bytes a DevicePool of `capacity` slots holds: the resident
+    arrays of every slot, the per-launch slot maps of each handle, and the
+    handles themselves (handle_bytes(cfg with max_ncrms = capacity))."""
+    return capacity * slot_bytes(cfg) + handles * 12 * capacity + handles * handle_bytes(capacity)
 
 
 def config_key(cfg):
@@ -142,6 +163,12 @@ class DevicePool:
         self.d_map = [torch.zeros(capacity, dtype=torch.int32, device=dev) for _ in range(handles)]
         self.d_gcol = [torch.zeros(capacity, dtype=torch.int32, device=dev) for _ in range(handles)]
         self.d_status = [torch.zeros(capacity, dtype=torch.int32, device=dev) for _ in range(handles)]
+
+    def close(self):
+        """Free the handles (the torch arrays go with the pool object)."""
+        for c in self.ctx:
+            c.close()
+        self.ctx = []
 
     # -- host <-> slots (on a given stream)
     def _scatter(self, dst, slots_t, host):
@@ -235,6 +262,7 @@ class CrmServer:
 
     def __init__(self, configs, capacity=1024, hbm_budget=120 * 2 ** 30, handles=3):
         self.configs = {config_key(c): c for c in configs}
+        self.pool_charge = {}
         self.capacity = capacity
         self.budget = HbmBudget(hbm_budget)
         self.handles = handles
@@ -248,29 +276,62 @@ class CrmServer:
         self._thread = threading.Thread(target=self._engine, daemon=True)
         self._thread.start()
 
-    def pool(self, key):
+    def _handle_bytes(self, cfg):
+        from .lib import plan_device_bytes
+        return lambda cap: plan_device_bytes(T.CrmConfig(**{**cfg.__dict__, 'max_ncrms': cap}))
+
+    def _release_idle_pools(self, keep):
+        """Free the pools (other than `keep`) that hold no chunk."""
+        for k in list(self.pools):
+            p = self.pools[k]
+            if k != keep and p.slots.available == p.capacity and not any(p.busy):
+                del self.pools[k]
+                self.budget.release(self.pool_charge.pop(k))
+                p.close()
+
+    def pool(self, key, need=1):
+        """The pool of a configuration, created on first use: charged to the
+        budget before it allocates; capacity halves while it does not fit
+        (down to `need` slots), else BudgetError."""
         with self._lock:
             p = self.pools.get(key)
-            if p is None:
-                p = DevicePool(self.configs[key], self.capacity, self.handles)
-                self.pools[key] = p
-            return p
+            if p is not None:
+                return p
+            cfg = self.configs[key]
+            hb = self._handle_bytes(cfg)
+            cap = self.capacity
+            for attempt in range(2):
+                while cap >= need:
+                    nbytes = pool_bytes(cfg, cap, self.handles, hb)
+                    if self.budget.reserve(nbytes):
+                        p = DevicePool(cfg, cap, self.handles)
+                        self.pools[key] = p
+                        self.pool_charge[key] = nbytes
+                        return p
+                    if cap == need:
+                        break
+                    cap = max(need, cap // 2)
+                if attempt == 0:
+                    self._release_idle_pools(key)
+                    cap = self.capacity
+            raise BudgetError('HBM budget: %d of %d bytes in use; a pool of %d slots of this '
+                              'configuration does not fit' % (self.budget.used, self.budget.total, need))
 
     # -- admission
     def open_chunk(self, cfg, cin, st, rad, gcol, timeout=60.0):
         """Admit a chunk: slots + budget, then its state is copied in.
         Waits (up to timeout s) while the pool or the budget is full."""
         key = config_key(cfg)
-        pool = self.pool(key)
         n = len(gcol)
+        pool = self.pool(key, need=n)
+        if n > pool.capacity:
+            raise BudgetError('chunk of %d columns exceeds its pool (%d slots)' % (n, pool.capacity))
         nbytes = n * slot_bytes(cfg)
         t0 = time.perf_counter()
         while True:
-            if self.budget.reserve(nbytes):
-                slots = pool.slots.alloc(n)
-                if slots is not None:
-                    break
-                self.budget.release(nbytes)
+            slots = pool.slots.alloc(n)
+            if slots is not None:
+                break
             if time.perf_counter() - t0 > timeout:
                 raise TimeoutError('admission timed out')
             time.sleep(0.001)
@@ -307,7 +368,6 @@ class CrmServer:
 
     def close_chunk(self, chunk):
         self.pools[chunk.key].slots.free(chunk.slots)
-        self.budget.release(chunk.nbytes)
 
     # -- steps
     def step(self, chunk, cin, dt_gl):
@@ -331,6 +391,7 @@ class CrmServer:
         torch.cuda.set_device(0)
         pending = {}         # pool key -> waiting requests, in arrival order
         inflight = []        # (pool, handle, requests, outputs, status, event)
+        busy = set()         # chunks with a step in flight
         while not self._stop.is_set():
             try:
                 r = self._q.get(timeout=0.0005 if (inflight or pending) else 0.05)
@@ -346,18 +407,22 @@ class CrmServer:
                     h = pool.idle_handle()
                     if h is None:
                         break
-                    head = pending[key][0]
-                    tag = (head.dt_gl, head.chunk.steps == 0)
-                    rs = [r for r in pending[key] if (r.dt_gl, r.chunk.steps == 0) == tag]
-                    pending[key] = [r for r in pending[key] if (r.dt_gl, r.chunk.steps == 0) != tag]
-                    inflight.append(self._launch(pool, h, rs, tag))
+                    rs, rest = select_launch(pending[key], busy)
+                    if not rs:
+                        break
+                    pending[key] = rest
+                    item = self._launch(pool, h, rs, (rs[0].dt_gl, rs[0].chunk.steps == 0))
+                    if item is not None:
+                        busy.update(id(r.chunk) for r in rs)
+                        inflight.append(item)
                 if not pending.get(key):
                     pending.pop(key, None)
             still = []
             for item in inflight:
-                if item is not None and item[5].query():
+                if item[5].query():
                     self._complete(item)
-                elif item is not None:
+                    busy.difference_update(id(r.chunk) for r in item[2])
+                else:
                     still.append(item)
             inflight = still
 
@@ -403,6 +468,29 @@ class CrmServer:
                 self.latencies.append(t_done - r.t_submit)
             r.future.set_result((vals, status[o:o + n].copy()))
             o += n
+
+
+def select_launch(waiting, busy):
+    """Split the waiting requests of one pool into (this launch, the rest).
+
+    The launch takes the oldest request whose chunk has no step in flight
+    and every later one with the same (dt_gl, first-step) tag, at most one
+    request per chunk: a chunk's later steps wait for its earlier ones,
+    whose results they depend on, and two requests of one chunk in one
+    launch would integrate the same slots twice."""
+    head = next((r for r in waiting if id(r.chunk) not in busy), None)
+    if head is None:
+        return [], list(waiting)
+    tag = (head.dt_gl, head.chunk.steps == 0)
+    take, rest, seen = [], [], set()
+    for r in waiting:
+        c = id(r.chunk)
+        if c not in busy and c not in seen and (r.dt_gl, r.chunk.steps == 0) == tag:
+            take.append(r)
+            seen.add(c)
+        else:
+            rest.append(r)
+    return take, rest
 
 
 def apply_tendencies(cin, vals, dt_gl):

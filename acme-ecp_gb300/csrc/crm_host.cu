@@ -55,8 +55,10 @@ struct crm_ctx {
   // host-side constants
   std::vector<double> trigs, eign;
   int ifax[20];
-  double gam[10];
-  double vrain, vsnow, vgrau, crain, csnow, cgrau, a_bg, a_pr, a_gr;
+  crm::KParams mc;                // gamma functions and fall speeds (micro_consts)
+  size_t device_bytes = 0;        // device memory the handle holds
+  long long barrier_spins = 1ll << 24;      // grid-barrier wait limit (spins)
+  int barrier_withhold = -1;                 // test hook, see crm_debug_barrier_test
   int last_launches = 0;
   double last_kernel_ms = 0.;
   bool pending_timing = false;
@@ -154,8 +156,8 @@ done:
 }
 
 // fftrig_crm (fft.F90:247-300), mode 3: REAL*4 pi, del, angle, cos, sin
-void fft_trigs(std::vector<double> &trigs, int n) {
-  trigs.assign(3 * n / 2 + 2 + n, 0.0);
+void fft_trigs_into(double *trigs, int n) {
+  for (int i = 0; i < 3 * n / 2 + 2 + n; ++i) trigs[i] = 0.0;
   float pi_f = (float)(2.0f * asinf(1.0f));
   int nn = n / 2;
   float del = (float)((double)(pi_f + pi_f) / (double)nn);
@@ -171,6 +173,10 @@ void fft_trigs(std::vector<double> &trigs, int n) {
     trigs[la + i - 1] = (double)cosf(angle);
     trigs[la + i] = (double)sinf(angle);
   }
+}
+void fft_trigs(std::vector<double> &trigs, int n) {
+  trigs.assign(3 * n / 2 + 2 + n, 0.0);
+  fft_trigs_into(trigs.data(), n);
 }
 
 float gammafff(float x) { return (float)exp(lgamma((double)x)); }
@@ -237,14 +243,62 @@ int validate(const crm_config *c) {
   return CRM_OK;
 }
 
-int alloc_ctx(crm_ctx *c) {
+// Per-configuration constants, written into caller-provided storage so that
+// the handle (alloc_ctx) and the no-allocation entry build the same values:
+//   trigs: 3 nx / 2 + 2 + nx REAL*4 trig values (fft.F90:247-300)
+//   eign:  nx + 1 Laplacian eigenvalues (pressure.F90:172-198, 2D: jd = 0)
+void laplace_eigen(double *eign, const crm_config &g) {
+  const int nx = g.crm_nx;
+  double dx = g.crm_dx, dy = g.crm_dx;
+  double ddx2 = 1.0 / (dx * dx), ddy2 = 1.0 / (dy * dy);
+  double pii = 3.14159265358979323846;
+  double xnx = pii / nx, xny = pii / 1;
+  int jd = (int)(((float)1 - 0.1f) / 2.f);
+  double xj = jd, facty = 2.0;
+  for (int i = 1; i <= nx + 1; ++i) {
+    int id = (int)(((float)i - 0.1f) / 2.f);
+    double xi = id, factx = 2.0;
+    eign[i - 1] = (2.0 * cos(factx * xnx * xi) - 2.0) * ddx2 + (2.0 * cos(facty * xny * xj) - 2.0) * ddy2;
+  }
+}
+
+// Gamma functions and fall-speed coefficients of sam1mom
+// (precip_init.F90:25-49, microphysics.F90:500-507) into the kernel
+// parameters.
+void micro_consts(crm::KParams &p) {
+  const double b_rain = R4H(0.8), b_snow = 0.25, b_grau = 0.5;
+  double gam[10];
+  gam[0] = gammafff(3.f);
+  gam[1] = gammafff((float)(3. + b_rain));
+  gam[2] = gammafff((float)((5. + b_rain) / 2.));
+  gam[3] = gammafff((float)(4. + b_rain));
+  gam[4] = gammafff((float)(3. + b_snow));
+  gam[5] = gammafff((float)((5. + b_snow) / 2.));
+  gam[6] = gammafff((float)(4. + b_snow));
+  gam[7] = gammafff((float)(3. + b_grau));
+  gam[8] = gammafff((float)((5. + b_grau) / 2.));
+  gam[9] = gammafff((float)(4. + b_grau));
+  p.gams1 = gam[4]; p.gams2 = gam[5]; p.gamg1 = gam[7]; p.gamg2 = gam[8];
+  p.gamr1 = gam[1]; p.gamr2 = gam[2];
+  p.crain = b_rain / 4.; p.csnow = b_snow / 4.; p.cgrau = b_grau / 4.;
+  p.vrain = 842. * gam[3] / 6. / det_pow(kPi4 * 1000. * 8.e6, p.crain);
+  p.vsnow = R4H(4.84) * gam[6] / 6. / det_pow(kPi4 * 100. * 3.e6, p.csnow);
+  p.vgrau = 94.5 * gam[9] / 6. / det_pow(kPi4 * 400. * 4.e6, p.cgrau);
+  p.a_bg = 1. / (R4H(273.16) - R4H(253.16));
+  p.a_pr = 1. / (R4H(283.16) - R4H(268.16));
+  p.a_gr = 1. / (R4H(283.16) - R4H(223.16));
+}
+
+// Sizes of a handle's device buffers, decided without allocating: the slab
+// count is the largest co-resident CTA count over the launch shapes (so the
+// shape can change per call), capped at max_ncrms.
+int plan_ctx(crm_ctx *c) {
   const crm_config &g = c->cfg;
   CK(cudaGetDevice(&c->device));
   CK(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, c->device));
   const size_t esz = g.precision == CRM_FP64 ? sizeof(double) : sizeof(float);
   c->L = crm::make_layout(g.crm_nx, g.crm_nz, g.plev, g.crm_nx_rad, (int)esz);
-  // co-resident CTAs of every launch shape; slabs for the largest, so the
-  // shape can change per call (crm_set_launch_shape)
+  c->slab_cap = 0;
   for (int s = 0; s < crm::kNumShapes; ++s) {
     int per = crm::occupancy_columns(g.precision, s, g.crm_nx, g.crm_nz);
     int grid = per > 0 ? c->nsm * per : 0;
@@ -252,6 +306,27 @@ int alloc_ctx(crm_ctx *c) {
     c->shape_grid[s] = grid;
     if (grid > c->slab_cap) c->slab_cap = grid;
   }
+  c->slab_bytes = c->L.slab * esz;
+  c->ld_cap = g.max_ncrms;
+  return CRM_OK;
+}
+
+// Device bytes alloc_ctx allocates for a planned handle (the staging
+// buffers of crm_run come later, on its first call).
+size_t handle_bytes(const crm_ctx *c) {
+  const crm_config &g = c->cfg;
+  const size_t ld = (size_t)c->ld_cap, nt = 3 * (size_t)g.crm_nx / 2 + 2 + g.crm_nx;
+  size_t b = c->slab_bytes * (size_t)c->slab_cap;
+  b += sizeof(double) * (nt + g.crm_nx + 1 + (nt + 1) / 2);
+  b += sizeof(double) * ld * (1 + 5 * (size_t)g.crm_nx);
+  b += sizeof(int) * ld + 8 * sizeof(unsigned long long);
+  return b;
+}
+
+int alloc_ctx(crm_ctx *c) {
+  const crm_config &g = c->cfg;
+  int rc = plan_ctx(c);
+  if (rc != CRM_OK) return rc;
   c->shape = default_shape(g.precision, g.crm_nx);
   {
     const char *e = getenv("CRM_GB300_SHAPE");
@@ -263,35 +338,12 @@ int alloc_ctx(crm_ctx *c) {
   }
   if (c->shape_grid[c->shape] < 1) return CRM_ERR_UNSUPPORTED;
   c->grid_max = c->shape_grid[c->shape];
-  c->slab_bytes = c->L.slab * esz;
   CK(cudaMalloc(&c->slabs, c->slab_bytes * (size_t)c->slab_cap));
-  c->ld_cap = g.max_ncrms;
-  const int ld = c->ld_cap, plev = g.plev, nx = g.crm_nx, nz = g.crm_nz;
-  c->in_elems = (size_t)ld * (plev + 1);
-  // GCM profiles, then tau00, bflxls, wndls (ld each), gcol and col_map (ld ints each)
-  CK(cudaMalloc(&c->d_in, sizeof(double) * c->in_elems * I_NIN + sizeof(double) * 4 * ld));
-  CK(cudaMalloc(&c->d_state, sizeof(double) * (size_t)ld * nx * nz * 7));
-  CK(cudaMalloc(&c->d_rad, sizeof(double) * (size_t)ld * g.crm_nx_rad * nz * 6));
-  size_t no = 0;
-  for (int f = 0; f < CRM_NOUT; ++f) no += out_elems(g, f, ld);
-  CK(cudaMalloc(&c->d_out, sizeof(double) * no));
+  const int ld = c->ld_cap, nx = g.crm_nx;
   fft_factors(c->ifax, nx);
   fft_trigs(c->trigs, nx);
-  // eigenvalues (pressure.F90:172-198), 2D: jd = 0
   c->eign.assign(nx + 1, 0.0);
-  {
-    double dx = g.crm_dx, dy = g.crm_dx;
-    double ddx2 = 1.0 / (dx * dx), ddy2 = 1.0 / (dy * dy);
-    double pii = 3.14159265358979323846;
-    double xnx = pii / nx, xny = pii / 1;
-    int jd = (int)(((float)1 - 0.1f) / 2.f);
-    double xj = jd, facty = 2.0;
-    for (int i = 1; i <= nx + 1; ++i) {
-      int id = (int)(((float)i - 0.1f) / 2.f);
-      double xi = id, factx = 2.0;
-      c->eign[i - 1] = (2.0 * cos(factx * xnx * xi) - 2.0) * ddx2 + (2.0 * cos(facty * xny * xj) - 2.0) * ddy2;
-    }
-  }
+  laplace_eigen(c->eign.data(), g);
   // trigs, eign (FP64), then trigs again as float (exact: REAL*4 values)
   const size_t nt = c->trigs.size(), ne = c->eign.size(), ntf = (nt + 1) / 2;
   CK(cudaMalloc(&c->d_consts, sizeof(double) * (nt + ne + ntf)));
@@ -306,31 +358,35 @@ int alloc_ctx(crm_ctx *c) {
   CK(cudaMalloc(&c->d_status, sizeof(int) * (size_t)ld));
   CK(cudaMalloc(&c->d_gsync, 8 * sizeof(unsigned long long)));
   CK(cudaMemset(c->d_gsync, 0, 8 * sizeof(unsigned long long)));
+  c->device_bytes = handle_bytes(c);
 #ifdef CRM_PHASE_TIMERS
   CK(cudaMalloc(&c->d_phase, sizeof(unsigned long long) * 64 * (size_t)c->slab_cap));
   CK(cudaMemset(c->d_phase, 0, sizeof(unsigned long long) * 64 * (size_t)c->slab_cap));
 #endif
-  // gamma functions and fall speeds (precip_init.F90:25-49, microphysics.F90:500-507)
-  const double b_rain = R4H(0.8), b_snow = 0.25, b_grau = 0.5;
-  c->gam[0] = gammafff(3.f);
-  c->gam[1] = gammafff((float)(3. + b_rain));
-  c->gam[2] = gammafff((float)((5. + b_rain) / 2.));
-  c->gam[3] = gammafff((float)(4. + b_rain));
-  c->gam[4] = gammafff((float)(3. + b_snow));
-  c->gam[5] = gammafff((float)((5. + b_snow) / 2.));
-  c->gam[6] = gammafff((float)(4. + b_snow));
-  c->gam[7] = gammafff((float)(3. + b_grau));
-  c->gam[8] = gammafff((float)((5. + b_grau) / 2.));
-  c->gam[9] = gammafff((float)(4. + b_grau));
-  c->crain = b_rain / 4.; c->csnow = b_snow / 4.; c->cgrau = b_grau / 4.;
-  c->vrain = 842. * c->gam[3] / 6. / det_pow(kPi4 * 1000. * 8.e6, c->crain);
-  c->vsnow = R4H(4.84) * c->gam[6] / 6. / det_pow(kPi4 * 100. * 3.e6, c->csnow);
-  c->vgrau = 94.5 * c->gam[9] / 6. / det_pow(kPi4 * 400. * 4.e6, c->cgrau);
-  c->a_bg = 1. / (R4H(273.16) - R4H(253.16));
-  c->a_pr = 1. / (R4H(283.16) - R4H(268.16));
-  c->a_gr = 1. / (R4H(283.16) - R4H(223.16));
+  micro_consts(c->mc);
   CK(cudaEventCreate(&c->ev0));
   CK(cudaEventCreate(&c->ev1));
+  return CRM_OK;
+}
+
+// crm_run's staging buffers for host arguments, allocated by its first call
+// (a handle used only through crm_run_device never holds them).
+int ensure_staging(crm_ctx *c) {
+  if (c->d_in) return CRM_OK;
+  const crm_config &g = c->cfg;
+  const int ld = c->ld_cap, plev = g.plev, nx = g.crm_nx, nz = g.crm_nz;
+  c->in_elems = (size_t)ld * (plev + 1);
+  // GCM profiles, then tau00, bflxls, wndls (ld each), gcol and col_map (ld ints each)
+  const size_t b_in = sizeof(double) * c->in_elems * I_NIN + sizeof(double) * 4 * ld;
+  const size_t b_st = sizeof(double) * (size_t)ld * nx * nz * 7;
+  const size_t b_rad = sizeof(double) * (size_t)ld * g.crm_nx_rad * nz * 6;
+  size_t no = 0;
+  for (int f = 0; f < CRM_NOUT; ++f) no += out_elems(g, f, ld);
+  CK(cudaMalloc(&c->d_in, b_in));
+  CK(cudaMalloc(&c->d_state, b_st));
+  CK(cudaMalloc(&c->d_rad, b_rad));
+  CK(cudaMalloc(&c->d_out, sizeof(double) * no));
+  c->device_bytes += b_in + b_st + b_rad + sizeof(double) * no;
   return CRM_OK;
 }
 
@@ -387,11 +443,11 @@ int build_params(crm_ctx *c, const crm_call_desc *d, const crm_input_c *in, crm_
   p.use_accel = g.use_crm_accel != 0; p.accel_uv = g.crm_accel_uv != 0;
   p.accel_factor = g.crm_accel_factor;
   p.dx = g.crm_dx; p.dy = g.crm_dx; p.dt = dt; p.dt_gl = d->dt_gl;
-  p.gams1 = c->gam[4]; p.gams2 = c->gam[5]; p.gamg1 = c->gam[7]; p.gamg2 = c->gam[8];
-  p.gamr1 = c->gam[1]; p.gamr2 = c->gam[2];
-  p.vrain = c->vrain; p.vsnow = c->vsnow; p.vgrau = c->vgrau;
-  p.crain = c->crain; p.csnow = c->csnow; p.cgrau = c->cgrau;
-  p.a_bg = c->a_bg; p.a_pr = c->a_pr; p.a_gr = c->a_gr;
+  p.gams1 = c->mc.gams1; p.gams2 = c->mc.gams2; p.gamg1 = c->mc.gamg1; p.gamg2 = c->mc.gamg2;
+  p.gamr1 = c->mc.gamr1; p.gamr2 = c->mc.gamr2;
+  p.vrain = c->mc.vrain; p.vsnow = c->mc.vsnow; p.vgrau = c->mc.vgrau;
+  p.crain = c->mc.crain; p.csnow = c->mc.csnow; p.cgrau = c->mc.cgrau;
+  p.a_bg = c->mc.a_bg; p.a_pr = c->mc.a_pr; p.a_gr = c->mc.a_gr;
   p.nfax = c->ifax[0];
   for (int k = 0; k <= c->ifax[0] && k < 8; ++k) p.ifax[k] = c->ifax[k];
   p.trigs = c->d_consts;
@@ -441,6 +497,8 @@ int enqueue(crm_ctx *c, const crm_call_desc *d, const crm_input_c *in, crm_state
   // launch), so the batch must fit the GPU at once and slots are 0..ncrms-1
   if (batch && (ncrms > c->grid_max || d->col_map)) return CRM_ERR_UNSUPPORTED;
   p.gsync = c->d_gsync;
+  p.barrier_spins = c->barrier_spins;
+  p.barrier_withhold = c->barrier_withhold;
   int grid = ncrms < c->grid_max ? ncrms : c->grid_max;
   CK(cudaEventRecord(c->ev0, s));
   if (batch) CK(cudaMemsetAsync(c->d_gsync, 0, 8 * sizeof(unsigned long long), s));
@@ -567,6 +625,30 @@ int crm_set_launch_shape(crm_ctx *ctx, int shape) {
 
 int crm_get_launch_shape(const crm_ctx *ctx) { return ctx ? ctx->shape : -1; }
 
+int crm_debug_barrier_test(crm_ctx *ctx, long long spin_limit, int withhold_column) {
+  if (!ctx || spin_limit < 1 || withhold_column < -1) return CRM_ERR_ARG;
+  ctx->barrier_spins = spin_limit;
+  ctx->barrier_withhold = withhold_column;
+  return CRM_OK;
+}
+
+unsigned long long crm_device_bytes(const crm_ctx *ctx) { return ctx ? (unsigned long long)ctx->device_bytes : 0ull; }
+
+int crm_plan_device_bytes(const crm_config *cfg, unsigned long long *bytes) {
+  if (!bytes) return CRM_ERR_ARG;
+  *bytes = 0;
+  int rc = validate(cfg);
+  int ndev = 0;
+  if (rc == CRM_OK && (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1)) rc = CRM_ERR_NO_DEVICE;
+  if (rc != CRM_OK) return rc;
+  crm_ctx c;
+  c.cfg = *cfg;
+  rc = plan_ctx(&c);
+  if (rc != CRM_OK) return rc;
+  *bytes = handle_bytes(&c);
+  return CRM_OK;
+}
+
 const char *crm_version(void) { return "crm-gb300 0.1 (sm_103a; 2D sam1mom; fp64 plain + fp32 mixed)"; }
 
 int crm_run_device(crm_ctx *c, const crm_call_desc *d, const crm_input_c *in, crm_state_c *st, crm_rad_c *rad,
@@ -583,6 +665,10 @@ int crm_run(crm_ctx *c, const crm_call_desc *d, const crm_input_c *in, crm_state
   const int ncrms = d->ncrms, ld = d->ld, plev = g.plev, nx = g.crm_nx, nz = g.crm_nz;
   if (ncrms < 1 || ld < ncrms || ld > c->ld_cap) return CRM_ERR_ARG;
   if (!d->gcol && d->igstep <= 1) return CRM_ERR_ARG;
+  {
+    int rs = ensure_staging(c);
+    if (rs != CRM_OK) return rs;
+  }
   cudaStream_t s = c->stream;
   // stage the host arguments through the handle's device buffers
   crm_input_c din;
@@ -804,49 +890,9 @@ extern "C" int crm_run_device_noalloc(const crm_config *cfg, const crm_call_desc
   int ifax[20];
   fft_factors(ifax, nx);
   {
-    double *trigs = consts;
-    for (int i = 0; i < q.ntrigs; ++i) trigs[i] = 0.0;
-    float pi_f = (float)(2.0f * asinf(1.0f));
-    int nn = nx / 2;
-    float del = (float)((double)(pi_f + pi_f) / (double)nn);
-    for (int i = 1; i <= nn + nn; i += 2) {
-      float angle = (float)(0.5 * (double)(i - 1) * (double)del);
-      trigs[i - 1] = (double)cosf(angle);
-      trigs[i] = (double)sinf(angle);
-    }
-    del = 0.5f * del;
-    int nh = (nn + 1) / 2, l = nh + nh, la = nn + nn;
-    for (int i = 1; i <= l; i += 2) {
-      float angle = (float)(0.5 * (double)(i - 1) * (double)del);
-      trigs[la + i - 1] = (double)cosf(angle);
-      trigs[la + i] = (double)sinf(angle);
-    }
-    double *eign = consts + q.ntrigs;
-    double dx = g.crm_dx, dy = g.crm_dx;
-    double ddx2 = 1.0 / (dx * dx), ddy2 = 1.0 / (dy * dy);
-    double pii = 3.14159265358979323846;
-    double xnx = pii / nx, xny = pii / 1;
-    int jd = (int)(((float)1 - 0.1f) / 2.f);
-    double xj = jd, facty = 2.0;
-    for (int i = 1; i <= nx + 1; ++i) {
-      int id = (int)(((float)i - 0.1f) / 2.f);
-      double xi = id, factx = 2.0;
-      eign[i - 1] = (2.0 * cos(factx * xnx * xi) - 2.0) * ddx2 + (2.0 * cos(facty * xny * xj) - 2.0) * ddy2;
-    }
+    fft_trigs_into(consts, nx);
+    laplace_eigen(consts + q.ntrigs, g);
   }
-  double gam[10];
-  const double b_rain = R4H(0.8), b_snow = 0.25, b_grau = 0.5;
-  gam[0] = gammafff(3.f);
-  gam[1] = gammafff((float)(3. + b_rain));
-  gam[2] = gammafff((float)((5. + b_rain) / 2.));
-  gam[3] = gammafff((float)(4. + b_rain));
-  gam[4] = gammafff((float)(3. + b_snow));
-  gam[5] = gammafff((float)((5. + b_snow) / 2.));
-  gam[6] = gammafff((float)(4. + b_snow));
-  gam[7] = gammafff((float)(3. + b_grau));
-  gam[8] = gammafff((float)((5. + b_grau) / 2.));
-  gam[9] = gammafff((float)(4. + b_grau));
-  const double crain = b_rain / 4., csnow = b_snow / 4., cgrau = b_grau / 4.;
 
   cudaStream_t s = (cudaStream_t)stream;
   unsigned char *base = dv.scratch;
@@ -879,15 +925,9 @@ extern "C" int crm_run_device_noalloc(const crm_config *cfg, const crm_call_desc
   p.use_accel = g.use_crm_accel != 0; p.accel_uv = g.crm_accel_uv != 0;
   p.accel_factor = g.crm_accel_factor;
   p.dx = g.crm_dx; p.dy = g.crm_dx; p.dt = dt; p.dt_gl = d->dt_gl;
-  p.gams1 = gam[4]; p.gams2 = gam[5]; p.gamg1 = gam[7]; p.gamg2 = gam[8];
-  p.gamr1 = gam[1]; p.gamr2 = gam[2];
-  p.vrain = 842. * gam[3] / 6. / det_pow(kPi4 * 1000. * 8.e6, crain);
-  p.vsnow = R4H(4.84) * gam[6] / 6. / det_pow(kPi4 * 100. * 3.e6, csnow);
-  p.vgrau = 94.5 * gam[9] / 6. / det_pow(kPi4 * 400. * 4.e6, cgrau);
-  p.crain = crain; p.csnow = csnow; p.cgrau = cgrau;
-  p.a_bg = 1. / (R4H(273.16) - R4H(253.16));
-  p.a_pr = 1. / (R4H(283.16) - R4H(268.16));
-  p.a_gr = 1. / (R4H(283.16) - R4H(223.16));
+  p.barrier_spins = 1ll << 24;
+  p.barrier_withhold = -1;
+  micro_consts(p);
   p.nfax = ifax[0];
   for (int k = 0; k <= ifax[0] && k < 8; ++k) p.ifax[k] = ifax[k];
   p.trigs = d_consts;

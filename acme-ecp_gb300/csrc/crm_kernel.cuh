@@ -82,6 +82,18 @@ namespace crm {
 #define NT ((int)blockDim.x)
 #define SYNC __syncthreads()
 
+// CFL of a column whose state is not finite (enters the batch maximum)
+constexpr double kCflNonfinite = 1.0e300;
+
+// ncycle = max(1, ceil(cfl / 0.7)) (kurant.F90:54-64), saturated at 10^6 so
+// that an unbounded CFL converts to an int safely; anything above 16 stops
+// the column
+__device__ __forceinline__ int ncycle_of(double cfl) {
+  double n = ceil(cfl / R4(0.7));
+  if (!(n < 1.0e6)) return 1000000;
+  return n > 1. ? (int)n : 1;
+}
+
 // per-CTA scalars of the column being integrated
 struct ColShared {
   int na, nb, nc, ncycle, icycle, nprec, prec_any, status, kmin, kmax, n_damp, col;
@@ -344,6 +356,7 @@ struct ColumnKernel : NxDim<NX> {
   __device__ bool grid_barrier() {
     unsigned int *count = reinterpret_cast<unsigned int *>(p.gsync);
     volatile unsigned int *gen = count + 1;
+    if (cpos == p.barrier_withhold && S.gbar == 0) return false;   // test hook: never arrives
     __threadfence();
     const unsigned int g = *gen;
     if (atomicAdd(count, 1u) == gridDim.x - 1) {
@@ -352,7 +365,7 @@ struct ColumnKernel : NxDim<NX> {
       atomicAdd(const_cast<unsigned int *>(gen), 1u);
       return true;
     }
-    for (long long it = 0; it < (1ll << 24); ++it) {
+    for (long long it = 0; it < p.barrier_spins; ++it) {
       if (*gen != g) {
         __threadfence();
         return true;
@@ -366,7 +379,11 @@ struct ColumnKernel : NxDim<NX> {
   __device__ double batch_max(double v) {
     if (p.batch_mode != CRM_REFERENCE_BATCH) return v;
     SYNC;
-    if (TID == 0) {
+    if (TID == 0 && S.status == CRM_ERR_TIMEOUT) {
+      // a column whose earlier wait ran out does not arrive again: the
+      // others' waits run out too, and the call ends with CRM_ERR_TIMEOUT
+      S.red_d[0] = v;
+    } else if (TID == 0) {
       unsigned long long *slot = p.gsync + 2 + (S.gbar & 3);
       atomicMax(slot, (unsigned long long)__double_as_longlong(v));
       bool ok = grid_barrier();
@@ -767,16 +784,21 @@ struct ColumnKernel : NxDim<NX> {
     T *wm = PR(P_TMP0), *uhm = PR(P_TMP1), *tkhm = PR(P_TMP2);
     // the horizontal speed of the 2D reference is sqrt(u*u + 0*(v*v)); for
     // a finite v the second term is +0 and the sum is u*u exactly, so v is
-    // not read
+    // not read.  The same pass screens u, w and tkh for NaN/Inf: every
+    // prognostic field feeds w (buoyancy) or u and tkh within a step, so a
+    // column whose state stops being finite is caught at the next step.
+    bool bad = false;
     level_max(3, 1, nzm,
               [&](int q, int i, int k) -> T {
-                if (q == 0) return tabs_(w(i, k));
-                if (q == 1) { T uu = u(i, k); return tsqrt(uu * uu); }
-                return tkh(i, k);
+                if (q == 0) { T ww = w(i, k); bad |= !isfinite(ww); return tabs_(ww); }
+                if (q == 1) { T uu = u(i, k); bad |= !isfinite(uu); return tsqrt(uu * uu); }
+                T th = tkh(i, k);
+                bad |= !isfinite(th);
+                return th;
               },
               [&](int q, int k, T m) { (q == 0 ? wm : q == 1 ? uhm : tkhm)[k] = m; });
     if (TID == 0) wm[nz] = (T)0.;
-    SYNC;
+    const int nonfinite = __syncthreads_or(bad);
     double cfl = 0.;
     const double rdx = 1. / p.dx;
     for (int k = TID + 1; k <= nzm; k += NT) {
@@ -790,11 +812,16 @@ struct ColumnKernel : NxDim<NX> {
       cfl = mx2(cfl, mx2(t1, t2));
     }
     cfl = block_max(cfl);
+    // a non-finite column enters the batch maximum as an unbounded CFL, so
+    // in reference-batch mode every column of the call stops at this step
+    // (the reference would have aborted the model) instead of waiting at a
+    // grid barrier the stopped column never reaches
+    if (nonfinite) cfl = kCflNonfinite;
     const double cfl_b = batch_max(cfl);
     if (TID == 0) {
       S.cfl = cfl;
-      int n = (int)ceil(cfl_b / R4(0.7));
-      S.ncycle = n > 1 ? n : 1;
+      if (nonfinite && S.status == CRM_OK) S.status = CRM_ERR_NONFINITE;
+      S.ncycle = ncycle_of(cfl_b);
     }
     SYNC;
   }
@@ -1936,7 +1963,10 @@ struct ColumnKernel : NxDim<NX> {
     if (TID == 0) {
       S.prec_cfl = cfl;
       S.prec_any = moving;
-      S.nprec = (cfl_b > R4(0.9)) ? (int)ceil(cfl_b / R4(0.9)) : 1;
+      // ceil(cfl / 0.9) sub-steps (microphysics.F90:602-661), saturated at
+      // 10^4 so that garbage fall speeds cannot make the loop unbounded
+      const double nf = ceil(cfl_b / R4(0.9));
+      S.nprec = (cfl_b > R4(0.9)) ? (nf < 1.0e4 ? (int)nf : 10000) : 1;
     }
     SYNC;
   }

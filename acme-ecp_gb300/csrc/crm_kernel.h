@@ -37,6 +37,12 @@ struct KParams {
   // in gsync[0]) and a ring of four batch maxima gsync[2..5] (zeroed by the
   // host before the launch); all columns are co-resident CTAs
   unsigned long long *gsync;
+  // spin iterations of one grid-barrier wait before it gives up (~4 s at the
+  // default 2^24), and a test hook: the CTA integrating call position
+  // barrier_withhold never arrives at the first barrier (-1: none), so the
+  // others' waits run out and report CRM_ERR_TIMEOUT
+  long long barrier_spins;
+  int barrier_withhold;
   unsigned long long *phase_cycles;  // (gridDim.x, 64) when built with CRM_PHASE_TIMERS
 };
 

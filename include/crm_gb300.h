@@ -216,9 +216,15 @@ int crm_run_device(crm_ctx *ctx, const crm_call_desc *desc, const crm_input_c *i
  * not fit, or with crm_nx > CRM_NOALLOC_MAX_NX, returns CRM_ERR_TOO_LARGE
  * before touching the device.
  *
+ * The array is part of the library's device code, so every device on which
+ * the library's kernels are loaded holds these 32 MiB until the process exits,
+ * whether or not this entry point is ever called.
+ *
  * The array's device address is looked up once per device, by the first call
  * made with that device current; make that first call before any stream
- * capture begins.  Every device operation of a call is a kernel launch on
+ * capture begins.  The address is kept for the life of the process: it
+ * assumes the device's primary context is never reset (cudaDeviceReset) and
+ * that calls come from that primary context.  Every device operation of a call is a kernel launch on
  * `stream` (the per-configuration constants travel as kernel parameters), so
  * later calls can be captured into a CUDA graph and replayed.  Every call on a device shares the one array and leaves its
  * last contents behind; nothing in it needs to start at zero (the kernel
@@ -262,6 +268,25 @@ int crm_num_launch_shapes(void);
 int crm_launch_shape_info(int shape, int *threads, int *ctas_per_sm, int *smem_planes);
 int crm_set_launch_shape(crm_ctx *ctx, int shape);
 int crm_get_launch_shape(const crm_ctx *ctx);
+/* Test hook of the reference-batch grid barrier (no counterpart in the
+ * reference): every wait at the barrier gives up after spin_limit polls
+ * (default 2^24, about 4 s) and the column then reports CRM_ERR_TIMEOUT;
+ * withhold_column >= 0 makes the column at that call position skip its
+ * arrival at the first barrier, so the other columns' waits run out.  Lets a
+ * test drive the timeout path without a GPU fault; -1 restores normal
+ * arrivals.  Applies to later calls on the handle. */
+int crm_debug_barrier_test(crm_ctx *ctx, long long spin_limit, int withhold_column);
+/* Device memory a handle holds [bytes]: its column slabs, per-column set-up
+ * values and constants from crm_create on, plus the staging buffers of host
+ * arguments from its first crm_run on (a handle driven only through
+ * crm_run_device never allocates those).  crm_plan_device_bytes gives what
+ * crm_create would allocate for cfg without allocating anything, so a
+ * serving loop can admit a new configuration against an HBM budget before
+ * it creates the handle.  No counterpart in the reference (its crm()
+ * allocates and frees the module arrays on every call,
+ * crm_module.F90:199-266,1666-1716). */
+unsigned long long crm_device_bytes(const crm_ctx *ctx);
+int crm_plan_device_bytes(const crm_config *cfg, unsigned long long *bytes);
 /* Library version string. */
 const char *crm_version(void);
 

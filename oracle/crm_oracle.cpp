@@ -687,9 +687,12 @@ struct Model {
   void kurant(Column &c) {
     const int nx = g.nx, ny = g.ny, nzm = g.nzm, Y = g.YES3D;
     std::vector<double> wm(nzm + 2, 0.0), uhm(nzm + 2, 0.0);
+    bool bad = false;     // no counterpart in the reference (it has no finiteness check)
     for (int k = 1; k <= nzm; ++k)
       for (int j = 1; j <= ny; ++j)
         for (int i = 1; i <= nx; ++i) {
+          bad = bad || !std::isfinite(c.w(i, j, k)) || !std::isfinite(c.u(i, j, k)) ||
+                !std::isfinite(c.tkh(i, j, k)) || (Y && !std::isfinite(c.v(i, j, k)));
           wm[k] = fmax2(wm[k], fabs(c.w(i, j, k)));
           double uu = c.u(i, j, k), vv = c.v(i, j, k);
           uhm[k] = fmax2(uhm[k], sqrt(uu * uu + (double)Y * (vv * vv)));
@@ -711,11 +714,15 @@ struct Model {
                          (double)((float)Y * 0.5f) * tkhmax * c.grdf_y(k) * g.dt / (g.dy * g.dy));
       cfl = fmax2(cfl, tmp);
     }
-    c.cfl = cfl;
+    // a column whose state is not finite stops here with CRM_ERR_NONFINITE;
+    // its CFL is unbounded, so a reference batch stops with it
+    c.nonfinite = bad;
+    c.cfl = bad ? 1.0e300 : cfl;
   }
   static int ncycle_of(double cfl) {
-    int n = (int)std::ceil(cfl / R4(0.7));
-    return std::max(1, std::max(1, n));
+    double n = std::ceil(cfl / R4(0.7));
+    if (!(n < 1.0e6)) return 1000000;
+    return std::max(1, (int)n);
   }
 
   // ---- abcoefs.F90:7-31
@@ -1425,9 +1432,12 @@ struct Model {
         }
     c.prec_cfl = prec_cfl;
   }
+  // nprec = ceil(cfl / 0.9) (microphysics.F90:602-661), saturated at 10^4
+  // sub-steps so that garbage fall speeds cannot make the loop unbounded
   static int nprec_of(double prec_cfl) {
-    if (prec_cfl > R4(0.9)) return (int)std::ceil(prec_cfl / R4(0.9));
-    return 1;
+    if (!(prec_cfl > R4(0.9))) return 1;
+    double n = std::ceil(prec_cfl / R4(0.9));
+    return n < 1.0e4 ? (int)n : 10000;
   }
   void precip_fall_part2(Column &c, FallScratch &s, int nprec) {
     const int nx = g.nx, ny = g.ny, nzm = g.nzm, nz = g.nz;
@@ -2284,6 +2294,7 @@ static void run_column_full(Model &M, Column &c, int icrm, int pos, crm_state_c 
   for (int nstep = 1; nstep <= c.nstop && c.status == CRM_OK; ++nstep) {
     c.nstep = nstep;
     M.kurant(c);
+    if (c.nonfinite) { c.status = CRM_ERR_NONFINITE; break; }
     c.ncycle = Model::ncycle_of(c.cfl);
     if (c.ncycle > 16) { c.status = CRM_ERR_CFL; break; }
     for (int icyc = 1; icyc <= c.ncycle; ++icyc) {
@@ -2401,7 +2412,8 @@ int oracle_crm_run(const crm_config *cfg, const crm_call_desc *desc, const crm_i
 #pragma omp parallel for schedule(dynamic, 1)
       for (int icrm = 0; icrm < ncrms; ++icrm) M.step_stats(M.cols[icrm]);
     }
-    for (int icrm = 0; icrm < ncrms; ++icrm) M.col_status_saved[icrm] = status;
+    for (int icrm = 0; icrm < ncrms; ++icrm)
+      M.col_status_saved[icrm] = M.cols[icrm].nonfinite ? CRM_ERR_NONFINITE : status;
 #pragma omp parallel for schedule(dynamic, 1)
     for (int icrm = 0; icrm < ncrms; ++icrm) finalize_column(M, M.cols[icrm], icrm, st, rad, out);
   }

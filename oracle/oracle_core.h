@@ -104,6 +104,7 @@ struct Column {
   int na, nb, nc, ncycle, icycle;
   double dt3[3], at, bt, ct, dtn, dtfactor;
   double cfl;              // last kurant cfl
+  bool nonfinite = false;  // last kurant found a NaN/Inf in u, v, w or tkh
   double prec_cfl;
   int nprec;
   int status;

@@ -1,6 +1,6 @@
 """A small, self-contained crm() run for profilers (ncu) and quick timing.
 
-    python acme-ecp_gb300/crm_gb300/profile_case.py --ncrms 152 --dt-gl 100 \
+    python profile_case.py --ncrms 152 --dt-gl 100 \
         --precision fp32 --reps 2
 
 runs the 64 x 58 workload (--workload 64x58, the default; 32x28: 16-column
@@ -14,7 +14,7 @@ import os
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-sys.path.insert(0, os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(HERE, 'acme-ecp_gb300'))
 
 
 def main():

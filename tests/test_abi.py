@@ -127,9 +127,9 @@ def _fortran_type_fields(doc, name):
 
 
 def test_integration_fortran_binding_mirrors_the_header():
-    """The bind(C) types a maintainer copies from the integration notes
-    declare the same components, in the same order, as the C header."""
-    doc = open(os.path.join(REPO, 'INTEGRATION.md')).read()
+    """The bind(C) types of the Fortran binding module declare the same
+    components, in the same order, as the C header."""
+    doc = open(os.path.join(REPO, 'include', 'crm_gb300_bind.F90')).read()
     for c_name, f_name in (('crm_config', 'crm_config_c'), ('crm_call_desc', 'crm_call_desc_c'),
                            ('crm_input_c', 'crm_input_c'), ('crm_state_c', 'crm_state_c'),
                            ('crm_rad_c', 'crm_rad_c')):

@@ -109,3 +109,72 @@ def test_checkpoint_and_restore_chunk(gpu_lib, tmp_path):
     assert not status.any()
     for n, v in ref[1].items():
         assert np.array_equal(v, vals2[n]), n
+
+
+def test_two_steps_of_one_chunk_submitted_back_to_back(gpu_lib):
+    """A chunk's second request, submitted before its first completes, waits
+    for it: the results equal the two steps run one after the other."""
+    from crm_gb300.serving import CrmServer
+    cfg = _configs()[0]
+    cin, st, rad, gcol = _chunk(cfg, 5, 31, seed=9)
+    server = CrmServer([cfg], capacity=32)
+    ch = server.open_chunk(cfg, cin, st, rad, gcol)
+    seq = []
+    for _ in range(2):
+        vals, status = server.step(ch, cin, DT_GL).result(timeout=120)
+        assert not status.any()
+        seq.append(vals)
+    server.close_chunk(ch)
+    ch = server.open_chunk(cfg, cin, st, rad, gcol)
+    f1 = server.step(ch, cin, DT_GL)
+    f2 = server.step(ch, cin, DT_GL)
+    both = [f1.result(timeout=120), f2.result(timeout=120)]
+    server.close()
+    assert ch.steps == 2
+    for s in range(2):
+        assert not both[s][1].any()
+        for n, v in seq[s].items():
+            assert np.array_equal(v, both[s][0][n]), (s, n)
+    # the second step differs from the first (it continued the state)
+    assert not np.array_equal(seq[0]['sltend'], seq[1]['sltend'])
+
+
+def test_pool_is_charged_to_the_budget(gpu_lib):
+    """A pool's device memory is charged when it is created: a budget that
+    cannot hold any pool of the configuration refuses the chunk with
+    CRM_ERR_BUDGET, one that holds part of a full pool gets a smaller pool,
+    and closing the server's chunks lets another configuration take the
+    memory of an idle pool."""
+    from crm_gb300.lib import plan_device_bytes
+    from crm_gb300.serving import BudgetError, CrmServer, pool_bytes
+    cfgs = _configs()
+    cfg = cfgs[0]
+    cin, st, rad, gcol = _chunk(cfg, 4, 41, seed=2)
+    hb = lambda cap: plan_device_bytes(T.CrmConfig(**{**cfg.__dict__, 'max_ncrms': cap}))
+    full = pool_bytes(cfg, 256, 3, hb)
+    small = pool_bytes(cfg, 4, 3, hb)
+    server = CrmServer(cfgs, capacity=256, hbm_budget=small - 1)
+    with pytest.raises(BudgetError) as e:
+        server.open_chunk(cfg, cin, st, rad, gcol)
+    assert e.value.status == T.CRM_ERR_BUDGET
+    server.close()
+    # room for a small pool of each configuration, not for both at once
+    c1 = cfgs[1]
+    hb1 = lambda cap: plan_device_bytes(T.CrmConfig(**{**c1.__dict__, 'max_ncrms': cap}))
+    small1 = pool_bytes(c1, 4, 3, hb1)
+    assert small + small1 - 1 < full
+    server = CrmServer(cfgs, capacity=256, hbm_budget=small + small1 - 1)
+    ch = server.open_chunk(cfg, cin, st, rad, gcol)
+    pool = server.pools[ch.key]
+    assert 4 <= pool.capacity < 256
+    assert server.budget.used == server.pool_charge[ch.key] <= server.budget.total
+    held = sum(c.device_bytes for c in pool.ctx)
+    assert held <= server.pool_charge[ch.key]
+    server.close_chunk(ch)
+    # the other configuration needs the memory: the idle pool is released
+    cin1, st1, rad1, gcol1 = _chunk(c1, 4, 51, seed=3)
+    ch1 = server.open_chunk(c1, cin1, st1, rad1, gcol1)
+    assert ch.key not in server.pools and ch1.key in server.pools
+    assert server.budget.used == server.pool_charge[ch1.key]
+    server.close_chunk(ch1)
+    server.close()

@@ -231,3 +231,31 @@ def test_accel_ceases_on_large_mean_temperature_change():
         assert np.array_equal(v[1], getattr(acc[2], n)[1]), n
     for n, v in plain[4].arrays().items():
         assert np.array_equal(v[1], getattr(acc[4], n)[1]), n
+
+
+def test_nonfinite_column_is_reported_and_isolated():
+    """A NaN in one column's state stops that column with CRM_ERR_NONFINITE
+    (the reference has no such check and carries the NaN on); the other
+    columns give the same bits as a batch without it."""
+    cfg, cin, st, rad, desc = S.workload_32x28(ncrms=3)
+    desc.dt_gl = 200.0
+    bad = st.copy()
+    bad.temperature[1, 7, 0, 2] = np.nan
+    rc, stat, st_b, rad_b, out_b = _run(cfg, cin, bad, rad, desc)
+    assert rc == T.CRM_ERR_NONFINITE and list(stat) == [0, T.CRM_ERR_NONFINITE, 0]
+    rc, stat, st_g, rad_g, out_g = _run(cfg, cin, st, rad, desc)
+    assert rc == 0
+    for x, y in ((st_b, st_g), (rad_b, rad_g), (out_b, out_g)):
+        for n, v in x.arrays().items():
+            w = getattr(y, n)
+            assert np.array_equal(v[[0, 2]], w[[0, 2]]), n
+
+
+def test_nonfinite_column_stops_a_reference_batch():
+    """Batch mode: the non-finite column's unbounded CFL stops the batch;
+    it reports CRM_ERR_NONFINITE and the others CRM_ERR_CFL."""
+    cfg, cin, st, rad, desc = S.workload_32x28(ncrms=3, batch_mode=T.CRM_REFERENCE_BATCH)
+    desc.dt_gl = 200.0
+    st.w_wind[2, 3, 0, 5] = np.inf
+    rc, stat, *_ = _run(cfg, cin, st, rad, desc)
+    assert list(stat) == [T.CRM_ERR_CFL, T.CRM_ERR_CFL, T.CRM_ERR_NONFINITE]

@@ -87,3 +87,30 @@ def test_config_key_groups_by_physics_not_capacity():
                    {'use_crm_accel': 1}, {'crm_dt': 20.0}, {'batch_mode': T.CRM_REFERENCE_BATCH}):
         c = T.CrmConfig(**{**a.__dict__, **change})
         assert config_key(c) != config_key(a), change
+
+
+def test_select_launch_one_request_per_chunk():
+    """A launch takes at most one request per chunk and none of a chunk with
+    a step in flight; requests with another (dt_gl, first-step) tag wait."""
+    from crm_gb300.serving import Chunk, StepRequest, select_launch
+    a, b, c = (Chunk(('k',), [i], [i], 8) for i in range(3))
+    b.steps = 1
+    rs = [StepRequest(a, None, 300.0), StepRequest(a, None, 300.0), StepRequest(c, None, 300.0),
+          StepRequest(b, None, 300.0), StepRequest(c, None, 600.0)]
+    take, rest = select_launch(rs, busy=set())
+    assert [r.chunk for r in take] == [a, c]
+    assert rest == [rs[1], rs[3], rs[4]]
+    take, rest = select_launch(rs, busy={id(a)})
+    assert [r.chunk for r in take] == [c]
+    take, rest = select_launch([rs[1], rs[3]], busy={id(a)})
+    assert [r.chunk for r in take] == [b] and rest == [rs[1]]
+    take, rest = select_launch([rs[1]], busy={id(a)})
+    assert take == [] and rest == [rs[1]]
+
+
+def test_pool_bytes_counts_slots_maps_and_handles():
+    from crm_gb300.serving import pool_bytes
+    cfg = S.config_64x58(nx=64)
+    hb = lambda cap: 1000 * min(cap, 608)
+    assert pool_bytes(cfg, 10, 3, hb) == 10 * slot_bytes(cfg) + 3 * 12 * 10 + 3 * 10000
+    assert pool_bytes(cfg, 2048, 3, hb) - pool_bytes(cfg, 1024, 3, hb) == 1024 * (slot_bytes(cfg) + 36)
