@@ -329,6 +329,47 @@ static void fft991(double *a, double *work, const double *trigs, const int *ifax
 }
 
 // ---------------------------------------------------------------- model
+// ---------------------------------------------------------------- RNG_MT.F90
+// cam/RNG_MT.F90:52-142: a Mersenne-Twister variant.  The seeding is the old
+// 69069 linear congruential fill (RNG_MT_set_seed :52-63), the upper mask is
+// -1147483648 (0xBB9ACA00, not 0x80000000; :13), and the draw maps a
+// negative (signed) tempered word y to (y + 2^32) / 2^32 and a non-negative
+// one to (y + 0.5) / 2^32 (:133-137).
+struct RngMT {
+  int32_t mt[624];
+  int mti;
+  explicit RngMT(int seed) {
+    mt[0] = (int32_t)seed;
+    for (mti = 1; mti < 624; ++mti) mt[mti] = (int32_t)((uint32_t)69069 * (uint32_t)mt[mti - 1]);
+  }
+  double gen() {
+    const int32_t UMASK = -1147483648, LMASK = 2147483647;
+    const int32_t MATA = -1727483681, TMASKB = -1658038656, TMASKC = -272236544;
+    int32_t y;
+    if (mti >= 624) {
+      int kk;
+      for (kk = 0; kk < 624 - 397; ++kk) {
+        y = (mt[kk] & UMASK) | (mt[kk + 1] & LMASK);
+        mt[kk] = mt[kk + 397] ^ (int32_t)((uint32_t)y >> 1) ^ ((y & 1) ? MATA : 0);
+      }
+      for (; kk < 623; ++kk) {
+        y = (mt[kk] & UMASK) | (mt[kk + 1] & LMASK);
+        mt[kk] = mt[kk + (397 - 624)] ^ (int32_t)((uint32_t)y >> 1) ^ ((y & 1) ? MATA : 0);
+      }
+      y = (mt[623] & UMASK) | (mt[0] & LMASK);
+      mt[623] = mt[396] ^ (int32_t)((uint32_t)y >> 1) ^ ((y & 1) ? MATA : 0);
+      mti = 0;
+    }
+    y = mt[mti++];
+    y ^= (int32_t)((uint32_t)y >> 11);
+    y ^= (int32_t)(((uint32_t)y << 7) & (uint32_t)TMASKB);
+    y ^= (int32_t)(((uint32_t)y << 15) & (uint32_t)TMASKC);
+    y ^= (int32_t)((uint32_t)y >> 18);
+    if (y < 0) return ((double)y + 4294967296.0) / 4294967296.0;
+    return ((double)y + 0.5) / 4294967296.0;
+  }
+};
+
 struct Model {
   Grid g;
   std::vector<Column> cols;
@@ -637,36 +678,8 @@ struct Model {
   // setperturb (crm/setperturb.F90:7-84) with RNG_MT (cam/RNG_MT.F90:52-142)
   void setperturb(Column &c, int iseed) {
     const int nx = g.nx, ny = g.ny;
-    int32_t mt[624];
-    int mti;
-    const int32_t UMASK = -1147483648, LMASK = 2147483647;
-    const int32_t MATA = -1727483681, TMASKB = -1658038656, TMASKC = -272236544;
-    mt[0] = (int32_t)iseed;
-    for (mti = 1; mti < 624; ++mti) mt[mti] = (int32_t)((uint32_t)69069 * (uint32_t)mt[mti - 1]);
-    auto gen = [&]() -> double {
-      int32_t y;
-      if (mti >= 624) {
-        int kk;
-        for (kk = 0; kk < 624 - 397; ++kk) {
-          y = (mt[kk] & UMASK) | (mt[kk + 1] & LMASK);
-          mt[kk] = mt[kk + 397] ^ (int32_t)((uint32_t)y >> 1) ^ ((y & 1) ? MATA : 0);
-        }
-        for (; kk < 623; ++kk) {
-          y = (mt[kk] & UMASK) | (mt[kk + 1] & LMASK);
-          mt[kk] = mt[kk + (397 - 624)] ^ (int32_t)((uint32_t)y >> 1) ^ ((y & 1) ? MATA : 0);
-        }
-        y = (mt[623] & UMASK) | (mt[0] & LMASK);
-        mt[623] = mt[396] ^ (int32_t)((uint32_t)y >> 1) ^ ((y & 1) ? MATA : 0);
-        mti = 0;
-      }
-      y = mt[mti++];
-      y ^= (int32_t)((uint32_t)y >> 11);
-      y ^= (int32_t)(((uint32_t)y << 7) & (uint32_t)TMASKB);
-      y ^= (int32_t)(((uint32_t)y << 15) & (uint32_t)TMASKC);
-      y ^= (int32_t)((uint32_t)y >> 18);
-      if (y < 0) return ((double)y + 4294967296.0) / 4294967296.0;
-      return ((double)y + 0.5) / 4294967296.0;
-    };
+    RngMT rng(iseed);
+    auto gen = [&]() -> double { return rng.gen(); };
     const double factor_xy = 1. / (double)(nx * ny);
     for (int k = 1; k <= 5; ++k) {
       double perturb_k_scaling = (double)(5 + 1 - k) / (double)5;
@@ -2424,6 +2437,33 @@ int oracle_crm_run(const crm_config *cfg, const crm_call_desc *desc, const crm_i
     if (s != CRM_OK) worst = s;
   }
   return worst;
+}
+
+// Test hooks for known-answer checks of single routines.
+// RNG_MT: n draws after RNG_MT_set_seed(seed).
+int oracle_rng_mt(int seed, int n, double *out) {
+  if (!out || n < 0) return CRM_ERR_ARG;
+  RngMT r(seed);
+  for (int i = 0; i < n; ++i) out[i] = r.gen();
+  return CRM_OK;
+}
+// sat.F90: which = 0 esatw, 1 esati, 2 dtesatw, 3 dtesati, 4 qsatw, 5 qsati,
+// 6 dtqsatw, 7 dtqsati at temperatures t [K] (and pressures p [mb] for 4-7).
+int oracle_sat(int which, const double *t, const double *p, int n, double *out) {
+  if (!t || !out || n < 0 || which < 0 || which > 7 || (which >= 4 && !p)) return CRM_ERR_ARG;
+  for (int i = 0; i < n; ++i) {
+    switch (which) {
+      case 0: out[i] = esatw(t[i]); break;
+      case 1: out[i] = esati(t[i]); break;
+      case 2: out[i] = dtesatw(t[i]); break;
+      case 3: out[i] = dtesati(t[i]); break;
+      case 4: out[i] = qsatw(t[i], p[i]); break;
+      case 5: out[i] = qsati(t[i], p[i]); break;
+      case 6: out[i] = dtqsatw(t[i], p[i]); break;
+      default: out[i] = dtqsati(t[i], p[i]); break;
+    }
+  }
+  return CRM_OK;
 }
 
 int oracle_version(void) { return 1; }

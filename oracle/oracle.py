@@ -54,6 +54,11 @@ def load(check=False):
                                        C.POINTER(T.CCrmInput), C.POINTER(T.CCrmState),
                                        C.POINTER(T.CCrmRad), C.POINTER(T.CCrmOutput),
                                        C.POINTER(C.c_int), C.c_int]
+        lib.oracle_rng_mt.restype = C.c_int
+        lib.oracle_rng_mt.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double)]
+        lib.oracle_sat.restype = C.c_int
+        lib.oracle_sat.argtypes = [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int,
+                                   C.POINTER(C.c_double)]
         lib.oracle_fft991.restype = C.c_int
         lib.oracle_fft991.argtypes = [C.POINTER(C.c_double), C.c_int, C.c_int]
         if check:
@@ -86,3 +91,26 @@ def fft991(x, isign):
     if rc != 0:
         raise ValueError('fft991: unsupported length %d' % (a.size - 2))
     return a
+
+
+def rng_mt(seed, n):
+    """n draws of the oracle's RNG_MT after set_seed(seed)."""
+    out = np.zeros(n)
+    rc = load().oracle_rng_mt(int(seed), int(n), out.ctypes.data_as(C.POINTER(C.c_double)))
+    assert rc == 0
+    return out
+
+
+SAT_FUNCS = ('esatw', 'esati', 'dtesatw', 'dtesati', 'qsatw', 'qsati', 'dtqsatw', 'dtqsati')
+
+
+def sat(name, t, p=None):
+    """The oracle's sat.F90 function `name` at temperatures t (pressures p)."""
+    t = np.ascontiguousarray(t, dtype=np.float64)
+    pp = None if p is None else np.ascontiguousarray(p, dtype=np.float64)
+    out = np.zeros_like(t)
+    rc = load().oracle_sat(SAT_FUNCS.index(name), t.ctypes.data_as(C.POINTER(C.c_double)),
+                           None if pp is None else pp.ctypes.data_as(C.POINTER(C.c_double)),
+                           t.size, out.ctypes.data_as(C.POINTER(C.c_double)))
+    assert rc == 0
+    return out
