@@ -7,6 +7,8 @@ Objects, compiled in parallel:
   crm_prep.cu     per-column set-up kernel (z0, setperturb draws), -fmad=false
   crm_host.cu     the C ABI (include/crm_gb300.h), host code built with
                   -ffp-contract=off for the same reason
+  crm_serve.cu    the continuous-batching service of the C ABI (crm_submit,
+                  crm_poll) over resident column slots
 """
 import os
 import subprocess
@@ -26,7 +28,8 @@ COMMON = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC,-ffp-contract=o
           '-I' + os.path.join(REPO, 'include')]
 NUM_SHAPES = 6             # crm_kernel.h kShapes
 NX_BUILT = (32, 64, 128, 0)  # crm_kernel.h kNxBuilt (0: generic nx)
-UNITS = {'crm_prep': ('crm_prep', ['-fmad=false']), 'crm_host': ('crm_host', [])}
+UNITS = {'crm_prep': ('crm_prep', ['-fmad=false']), 'crm_host': ('crm_host', []),
+         'crm_serve': ('crm_serve', [])}
 for _n in NX_BUILT:
     for _s in range(NUM_SHAPES):
         _d = ['-DCRM_INST_NX=%d' % _n, '-DCRM_INST_SHAPE=%d' % _s]

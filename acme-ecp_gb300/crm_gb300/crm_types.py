@@ -25,6 +25,7 @@ CRM_ERR_TIMEOUT = 6
 CRM_ERR_BUDGET = 7
 CRM_ERR_NO_DEVICE = 8
 CRM_ERR_TOO_LARGE = 9
+CRM_PENDING = 10
 
 CRM_MICRO_SAM1MOM = 0
 CRM_MICRO_M2005 = 1

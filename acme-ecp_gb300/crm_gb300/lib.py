@@ -18,7 +18,9 @@ EXPORTS = ('crm_create', 'crm_destroy', 'crm_run', 'crm_run_device', 'crm_last_l
            'crm_last_kernel_ms', 'crm_set_stream', 'crm_status_string', 'crm_version',
            'crm_debug_phase_cycles', 'crm_run_device_noalloc', 'crm_num_launch_shapes',
            'crm_launch_shape_info', 'crm_set_launch_shape', 'crm_get_launch_shape',
-           'crm_device_bytes', 'crm_plan_device_bytes', 'crm_debug_barrier_test')
+           'crm_device_bytes', 'crm_plan_device_bytes', 'crm_debug_barrier_test',
+           'crm_server_create', 'crm_server_destroy', 'crm_server_device_bytes', 'crm_server_launches',
+           'crm_chunk_open', 'crm_chunk_read_state', 'crm_chunk_close', 'crm_submit', 'crm_poll')
 
 _lib = None
 
@@ -76,6 +78,29 @@ def load(path=None, build_if_missing=False):
     lib.crm_set_launch_shape.argtypes = [C.c_void_p, C.c_int]
     lib.crm_get_launch_shape.restype = C.c_int
     lib.crm_get_launch_shape.argtypes = [C.c_void_p]
+    lib.crm_server_create.restype = C.c_void_p
+    lib.crm_server_create.argtypes = [C.POINTER(T.CCrmConfig), C.c_int, C.c_int, C.c_ulonglong,
+                                      C.POINTER(C.c_int)]
+    lib.crm_server_destroy.restype = None
+    lib.crm_server_destroy.argtypes = [C.c_void_p]
+    lib.crm_server_device_bytes.restype = C.c_ulonglong
+    lib.crm_server_device_bytes.argtypes = [C.c_void_p]
+    lib.crm_server_launches.restype = C.c_longlong
+    lib.crm_server_launches.argtypes = [C.c_void_p]
+    lib.crm_chunk_open.restype = C.c_int
+    lib.crm_chunk_open.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.c_int,
+                                   C.POINTER(T.CCrmState), C.POINTER(T.CCrmRad), C.POINTER(C.c_int)]
+    lib.crm_chunk_read_state.restype = C.c_int
+    lib.crm_chunk_read_state.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(T.CCrmState),
+                                         C.POINTER(C.c_double)]
+    lib.crm_chunk_close.restype = C.c_int
+    lib.crm_chunk_close.argtypes = [C.c_void_p, C.c_int]
+    lib.crm_submit.restype = C.c_int
+    lib.crm_submit.argtypes = [C.c_void_p, C.c_int, C.POINTER(T.CCrmInput), C.POINTER(C.c_double),
+                               C.c_int, C.c_double, C.POINTER(T.CCrmOutput), C.POINTER(T.CCrmRad),
+                               C.POINTER(C.c_int), C.POINTER(C.c_longlong)]
+    lib.crm_poll.restype = C.c_int
+    lib.crm_poll.argtypes = [C.c_void_p, C.c_longlong, C.c_int]
     lib.crm_debug_barrier_test.restype = C.c_int
     lib.crm_debug_barrier_test.argtypes = [C.c_void_p, C.c_longlong, C.c_int]
     lib.crm_device_bytes.restype = C.c_ulonglong

@@ -45,7 +45,8 @@ enum crm_status {
   CRM_ERR_TIMEOUT = 6,      /* a bounded device wait gave up                 */
   CRM_ERR_BUDGET = 7,       /* serving admission: HBM budget exhausted       */
   CRM_ERR_NO_DEVICE = 8,    /* no CUDA device                                */
-  CRM_ERR_TOO_LARGE = 9     /* exceeds crm_run_device_noalloc's fixed scratch */
+  CRM_ERR_TOO_LARGE = 9,    /* exceeds crm_run_device_noalloc's fixed scratch */
+  CRM_PENDING = 10          /* crm_poll: the step has not completed yet      */
 };
 
 enum crm_microphysics { CRM_MICRO_SAM1MOM = 0, CRM_MICRO_M2005 = 1 };
@@ -287,6 +288,70 @@ int crm_debug_barrier_test(crm_ctx *ctx, long long spin_limit, int withhold_colu
  * crm_module.F90:199-266,1666-1716). */
 unsigned long long crm_device_bytes(const crm_ctx *ctx);
 int crm_plan_device_bytes(const crm_config *cfg, unsigned long long *bytes);
+/* ------------------------------------------------------------ serving
+ * Continuous batching for C and Fortran hosts.  No counterpart in the
+ * reference, which integrates each chunk synchronously inside
+ * crm_physics_tend (cam/crm_physics.F90:1145-1156) and keeps each column's
+ * CRM state in the physics buffer between GCM steps (crm_physics.F90:126-191,
+ * pbuf 'global' fields).  A server keeps that state on the device: a pool of
+ * `capacity` column slots of one configuration and `nhandles` column-kernel
+ * handles with their own streams.  A chunk of GCM columns is admitted into
+ * free slots (crm_chunk_open copies its CRM state in); each GCM step of a
+ * chunk is a request (crm_submit) carrying only the chunk's new input
+ * profiles.  An engine thread gathers the waiting requests, at most one per
+ * chunk (a chunk's next step waits for its current one) and all of one
+ * (dt_gl, first-step) kind, and runs ONE column-kernel launch over the union
+ * of their slots on an idle handle; requests that arrive meanwhile join the
+ * next launch, and launches on different handles overlap on the device.
+ * Per-column mode (the only mode served) makes a chunk's results the same
+ * alone and in any mix.  All calls are thread-safe. */
+typedef struct crm_server crm_server;
+
+/* hbm_budget_bytes bounds the device memory the server holds (slot arrays,
+ * handles, staging): a configuration that does not fit gets NULL and
+ * *status = CRM_ERR_BUDGET before anything is allocated.  cfg->max_ncrms
+ * is ignored (capacity takes its place); batch_mode must be
+ * CRM_PER_COLUMN. */
+crm_server *crm_server_create(const crm_config *cfg, int capacity, int nhandles,
+                              unsigned long long hbm_budget_bytes, int *status);
+/* Stops the engine after the launches in flight; requests not yet
+ * launched are dropped. */
+void crm_server_destroy(crm_server *srv);
+/* Device bytes the server holds; launches it has issued. */
+unsigned long long crm_server_device_bytes(const crm_server *srv);
+long long crm_server_launches(const crm_server *srv);
+
+/* Admit ncols GCM columns whose CRM state is columns 0..ncols-1 of host
+ * arrays of leading dimension ld (crm_state_c, and rad->qrad; the other rad
+ * pointers are not read); gcol: their global column ids (the setperturb seed
+ * of their first step).  *chunk receives the chunk id.  CRM_ERR_BUDGET when
+ * fewer than ncols slots are free (retry after closing chunks). */
+int crm_chunk_open(crm_server *srv, int ncols, const int *gcol, int ld, const crm_state_c *st,
+                   const crm_rad_c *rad, int *chunk);
+/* Copy a chunk's resident CRM state (and, if qrad is not NULL, its
+ * radiative heating) to host arrays of leading dimension ld, e.g. for a
+ * restart file; CRM_ERR_ARG while a step of the chunk is queued. */
+int crm_chunk_read_state(crm_server *srv, int chunk, int ld, crm_state_c *st, double *qrad);
+/* Release a chunk's slots; CRM_ERR_ARG while a step of it is queued. */
+int crm_chunk_close(crm_server *srv, int chunk);
+
+/* Submit one GCM step of a chunk: `in` holds its new GCM input profiles as
+ * host arrays of leading dimension ld (columns 0..ncols-1; the fields
+ * crm_run reads), qrad (may be NULL: keep the resident heating) its new
+ * radiative heating (ld, nx_rad, ny_rad, nz).  The results are written, when
+ * the step completes, into the caller's host arrays: every non-NULL field of
+ * `out` (ld, ...), the non-NULL rad means of `rad_means` (its qrad is not
+ * used) and col_status (ncols; may be NULL).  Those arrays must stay valid
+ * until crm_poll reports completion.  Returns at once with a ticket.  The
+ * first step of a chunk runs setperturb (igstep 1). */
+int crm_submit(crm_server *srv, int chunk, const crm_input_c *in, const double *qrad, int ld,
+               double dt_gl, crm_output_c *out, crm_rad_c *rad_means, int *col_status,
+               long long *ticket);
+/* CRM_PENDING while the step runs (wait = 0), else the step's worst column
+ * status once its results are in the caller's arrays (wait != 0 blocks until
+ * then).  A completed ticket is released by the call that reports it. */
+int crm_poll(crm_server *srv, long long ticket, int wait);
+
 /* Library version string. */
 const char *crm_version(void);
 
