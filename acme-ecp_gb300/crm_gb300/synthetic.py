@@ -178,3 +178,20 @@ def workload_64x58(ncrms=1024, seed=0, nx=64, moist=False, gcol0=1, **kw):
     cl = np.cos(np.deg2rad(lat))
     return (cfg,) + make_inputs(cfg, ncrms, 271.0 + 29.0 * cl, 10.0 * cl,
                                 100.0 * cl, seed=seed, moist=moist, gcol0=gcol0)
+
+
+def config_3d(precision=0, batch_mode=0, nx=32, ny=32, nz=58, dx=2000.0):
+    """3D CRM: nx x ny x nz of 72 levels, dx = dy = 2 km, dt 10 s."""
+    return CrmConfig(crm_nx=nx, crm_ny=ny, crm_nz=nz, plev=72, crm_dx=dx, crm_dy=dx,
+                     crm_dt=10.0, precision=precision, batch_mode=batch_mode)
+
+
+def workload_3d(ncrms=256, seed=0, nx=32, ny=32, nz=58, moist=False, gcol0=1, **kw):
+    """The 64 x 58 workload's soundings (lat ~ U[-60, 60] deg, T_sfc = 271 +
+    29 cos(lat), fluxes * cos(lat)) with v rising 0 -> 5 m/s over 0-12 km."""
+    cfg = config_3d(nx=nx, ny=ny, nz=nz, **kw)
+    rng = np.random.Generator(np.random.PCG64(10_000 + seed))
+    lat = rng.uniform(-60.0, 60.0, size=ncrms)
+    cl = np.cos(np.deg2rad(lat))
+    return (cfg,) + make_inputs(cfg, ncrms, 271.0 + 29.0 * cl, 10.0 * cl,
+                                100.0 * cl, seed=seed, moist=moist, gcol0=gcol0, v_top=5.0)

@@ -436,43 +436,54 @@ struct Model {
   A3 &DV(Column &c, int l) { return c.dvdt[l - 1]; }
   A3 &DW(Column &c, int l) { return c.dwdt[l - 1]; }
 
-  // ---- bound_exchange.F90:14-239 / periodic.F90 (2D: x direction only)
-  void exch(A3 &f, int dimz, int i_1, int i_2) {
-    const int nx = g.nx;
+  // ---- bound_exchange.F90:14-239 / periodic.F90: periodic halos.  Every
+  // halo value is copied from the interior (x first, then y with the x
+  // halos and corners in 3D), so the result is the periodic wrap of the
+  // interior onto i in [1-i_1, nx+i_2], j in [1-j_1, ny+j_2] (3D only).
+  void exch(A3 &f, int dimz, int i_1, int i_2, int j_1 = 1, int j_2 = 1) {
+    const int nx = g.nx, ny = g.ny;
     int i1 = i_1 - 1, i2 = i_2 - 1;
-    for (int k = 1; k <= dimz; ++k)
-      for (int j = f.y1 + (g.YES3D ? 0 : 0); j <= f.y2; ++j) {
-        if (!g.YES3D && j != 1) continue;
-        if (g.YES3D && (j < 1 || j > g.ny)) continue;
-        for (int i = -i1; i <= 0; ++i) f(i, j, k) = f(i + nx, j, k);
-        for (int i = nx + 1; i <= nx + 1 + i2; ++i) f(i, j, k) = f(i - nx, j, k);
+    if (!g.YES3D) {
+      for (int k = 1; k <= dimz; ++k) {
+        for (int i = -i1; i <= 0; ++i) f(i, 1, k) = f(i + nx, 1, k);
+        for (int i = nx + 1; i <= nx + 1 + i2; ++i) f(i, 1, k) = f(i - nx, 1, k);
       }
+      return;
+    }
+    int j1 = j_1 - 1, j2 = j_2 - 1;
+    auto wrap = [](int a, int n) { return a < 1 ? a + n : (a > n ? a - n : a); };
+    for (int k = 1; k <= dimz; ++k)
+      for (int j = -j1; j <= ny + 1 + j2; ++j)
+        for (int i = -i1; i <= nx + 1 + i2; ++i) {
+          if (i >= 1 && i <= nx && j >= 1 && j <= ny) continue;
+          f(i, j, k) = f(wrap(i, nx), wrap(j, ny), k);
+        }
   }
   void boundaries(Column &c, int flag) {   // periodic.F90:8-136
     const int nzm = g.nzm, nz = g.nz;
     if (flag == 0) {
-      exch(c.u, nzm, 1, 1);
-      exch(c.v, nzm, 1, 1);
+      exch(c.u, nzm, 1, 1, 1, 1);
+      exch(c.v, nzm, 1, 1, 1, 1);
       // w(:,:,nz) carries the (zero) sstxy through the exchange, then is zeroed
       for (int j = 1; j <= g.ny; ++j)
         for (int i = 1; i <= g.nx; ++i) c.w(i, j, nz) = 0.0;
-      exch(c.w, nz, 1, 1);
+      exch(c.w, nz, 1, 1, 1, 1);
       for (int j = 1 - g.YES3D; j <= g.ny + g.YES3D; ++j)
         for (int i = 0; i <= g.nx + 1; ++i) c.w(i, j, nz) = 0.0;
     } else if (flag == 2) {
-      exch(c.u, nzm, 2, 3);
-      exch(c.v, nzm, 2, 2);
-      exch(c.w, nz, 2, 2);
-      exch(c.t, nzm, 3, 3);
-      exch(c.qt, nzm, 3, 3);
-      exch(c.qp, nzm, 3, 3);
+      exch(c.u, nzm, 2, 3, 2, 2);
+      exch(c.v, nzm, 2, 2, 2, 3);
+      exch(c.w, nz, 2, 2, 2, 2);
+      exch(c.t, nzm, 3, 3, 3, 3);
+      exch(c.qt, nzm, 3, 3, 3, 3);
+      exch(c.qp, nzm, 3, 3, 3, 3);
     } else if (flag == 3) {
-      exch(c.t, nzm, 1, 1);
-      exch(c.qt, nzm, 1, 1);
-      exch(c.qp, nzm, 1, 1);
+      exch(c.t, nzm, 1, 1, 1, 1);
+      exch(c.qt, nzm, 1, 1, 1, 1);
+      exch(c.qp, nzm, 1, 1, 1, 1);
     } else if (flag == 4) {
-      exch(c.tk, nzm, 1, 1);
-      exch(c.tkh, nzm, 1, 1);
+      exch(c.tk, nzm, 1, 1, 1, 1);
+      exch(c.tkh, nzm, 1, 1, 1, 1);
     }
   }
 
@@ -905,6 +916,77 @@ struct Model {
   }
 
   // ---- shear_prod2D.F90:7-96
+  // SGS_TKE/shear_prod3D.F90:7-140
+  void shear_prod3D(Column &c, A3 &def2) {
+    const double rdx0 = 1. / g.dx, rdy0 = 1. / g.dy, dx = g.dx, dy = g.dy;
+    const int nzm = g.nzm;
+    A3 &u = c.u, &v = c.v, &w = c.w;
+    A1 &u0 = c.u0, &v0 = c.v0;
+    auto sq = [](double x) { return x * x; };
+    for (int k = 1; k <= nzm; ++k)
+      for (int j = 1; j <= g.ny; ++j)
+        for (int i = 1; i <= g.nx; ++i) {
+          int jb = j - 1, jc = j + 1, ib = i - 1, ic = i + 1;
+          if (k >= 2 && k <= nzm - 1) {
+            int kb = k - 1, kc = k + 1;
+            double rdz = 1. / (c.dz * c.adz(k));
+            double rdzw_up = 1. / (c.dz * c.adzw(kc));
+            double rdzw_dn = 1. / (c.dz * c.adzw(k));
+            double rdx = rdx0 * sqrt(dx * rdz), rdy = rdy0 * sqrt(dy * rdz);
+            double rdx_up = rdx0 * sqrt(dx * rdzw_up), rdy_up = rdy0 * sqrt(dy * rdzw_up);
+            double rdx_dn = rdx0 * sqrt(dx * rdzw_dn), rdy_dn = rdy0 * sqrt(dy * rdzw_dn);
+            double d = 2. * (sq((u(ic, j, k) - u(i, j, k)) * rdx) + sq((v(i, jc, k) - v(i, j, k)) * rdy) +
+                             sq((w(i, j, kc) - w(i, j, k)) * rdz)) +
+                       0.25 * (sq((u(ic, jc, k) - u(ic, j, k)) * rdy + (v(ic, jc, k) - v(i, jc, k)) * rdx) +
+                               sq((u(i, jc, k) - u(i, j, k)) * rdy + (v(i, jc, k) - v(ib, jc, k)) * rdx) +
+                               sq((u(ic, j, k) - u(ic, jb, k)) * rdy + (v(ic, j, k) - v(i, j, k)) * rdx) +
+                               sq((u(i, j, k) - u(i, jb, k)) * rdy + (v(i, j, k) - v(ib, j, k)) * rdx));
+            d = d + 0.25 * (sq((u(ic, j, kc) - u0(kc) - u(ic, j, k) + u0(k)) * rdzw_up + (w(ic, j, kc) - w(i, j, kc)) * rdx_up) +
+                            sq((u(i, j, kc) - u0(kc) - u(i, j, k) + u0(k)) * rdzw_up + (w(i, j, kc) - w(ib, j, kc)) * rdx_up) +
+                            sq((u(ic, j, k) - u0(k) - u(ic, j, kb) + u0(kb)) * rdzw_dn + (w(ic, j, k) - w(i, j, k)) * rdx_dn) +
+                            sq((u(i, j, k) - u0(k) - u(i, j, kb) + u0(kb)) * rdzw_dn + (w(i, j, k) - w(ib, j, k)) * rdx_dn));
+            d = d + 0.25 * (sq((v(i, jc, kc) - v0(kc) - v(i, jc, k) + v0(k)) * rdzw_up + (w(i, jc, kc) - w(i, j, kc)) * rdy_up) +
+                            sq((v(i, j, kc) - v0(kc) - v(i, j, k) + v0(k)) * rdzw_up + (w(i, j, kc) - w(i, jb, kc)) * rdy_up) +
+                            sq((v(i, jc, k) - v0(k) - v(i, jc, kb) + v0(kb)) * rdzw_dn + (w(i, jc, k) - w(i, j, k)) * rdy_dn) +
+                            sq((v(i, j, k) - v0(k) - v(i, j, kb) + v0(kb)) * rdzw_dn + (w(i, j, k) - w(i, jb, k)) * rdy_dn));
+            def2(i, j, k) = d;
+          } else if (k == 1) {
+            int kc = k + 1;
+            double rdz = 1. / (c.dz * c.adz(k));
+            double rdzw_up = 1. / (c.dz * c.adzw(kc));
+            double rdx = rdx0 * sqrt(dx * rdz), rdy = rdy0 * sqrt(dy * rdz);
+            double rdx_up = rdx0 * sqrt(dx * rdzw_up), rdy_up = rdy0 * sqrt(dy * rdzw_up);
+            def2(i, j, k) =
+                2. * (sq((u(ic, j, k) - u(i, j, k)) * rdx) + sq((v(i, jc, k) - v(i, j, k)) * rdy) +
+                      sq((w(i, j, kc) - w(i, j, k)) * rdz)) +
+                0.25 * (sq((u(ic, jc, k) - u(ic, j, k)) * rdy + (v(ic, jc, k) - v(i, jc, k)) * rdx) +
+                        sq((u(i, jc, k) - u(i, j, k)) * rdy + (v(i, jc, k) - v(ib, jc, k)) * rdx) +
+                        sq((u(ic, j, k) - u(ic, jb, k)) * rdy + (v(ic, j, k) - v(i, j, k)) * rdx) +
+                        sq((u(i, j, k) - u(i, jb, k)) * rdy + (v(i, j, k) - v(ib, j, k)) * rdx)) +
+                0.5 * (sq((v(i, jc, kc) - v0(kc) - v(i, jc, k) + v0(k)) * rdzw_up + (w(i, jc, kc) - w(i, j, kc)) * rdy_up) +
+                       sq((v(i, j, kc) - v0(kc) - v(i, j, k) + v0(k)) * rdzw_up + (w(i, j, kc) - w(i, jb, kc)) * rdy_up)) +
+                0.5 * (sq((u(ic, j, kc) - u0(kc) - u(ic, j, k) + u0(k)) * rdzw_up + (w(ic, j, kc) - w(i, j, kc)) * rdx_up) +
+                       sq((u(i, j, kc) - u0(kc) - u(i, j, k) + u0(k)) * rdzw_up + (w(i, j, kc) - w(ib, j, kc)) * rdx_up));
+          } else {  // k == nzm
+            int kc = k + 1, kb = k - 1;
+            double rdz = 1. / (c.dz * c.adz(k));
+            double rdzw_dn = 1. / (c.dz * c.adzw(k));
+            double rdx = rdx0 * sqrt(dx * rdz), rdy = rdy0 * sqrt(dy * rdz);
+            double rdx_dn = rdx0 * sqrt(dx * rdzw_dn), rdy_dn = rdy0 * sqrt(dy * rdzw_dn);
+            def2(i, j, k) =
+                2. * (sq((u(ic, j, k) - u(i, j, k)) * rdx) + sq((v(i, jc, k) - v(i, j, k)) * rdy) +
+                      sq((w(i, j, kc) - w(i, j, k)) * rdz)) +
+                0.25 * (sq((u(ic, jc, k) - u(ic, j, k)) * rdy + (v(ic, jc, k) - v(i, jc, k)) * rdx) +
+                        sq((u(i, jc, k) - u(i, j, k)) * rdy + (v(i, jc, k) - v(ib, jc, k)) * rdx) +
+                        sq((u(ic, j, k) - u(ic, jb, k)) * rdy + (v(ic, j, k) - v(i, j, k)) * rdx) +
+                        sq((u(i, j, k) - u(i, jb, k)) * rdy + (v(i, j, k) - v(ib, j, k)) * rdx)) +
+                0.5 * (sq((v(i, jc, k) - v0(k) - v(i, jc, kb) + v0(kb)) * rdzw_dn + (w(i, jc, k) - w(i, j, k)) * rdy_dn) +
+                       sq((v(i, j, k) - v0(k) - v(i, j, kb) + v0(kb)) * rdzw_dn + (w(i, j, k) - w(i, jb, k)) * rdy_dn)) +
+                0.5 * (sq((u(ic, j, k) - u0(k) - u(ic, j, kb) + u0(kb)) * rdzw_dn + (w(ic, j, k) - w(i, j, k)) * rdx_dn) +
+                       sq((u(i, j, k) - u0(k) - u(i, j, kb) + u0(kb)) * rdzw_dn + (w(i, j, k) - w(ib, j, k)) * rdx_dn));
+          }
+        }
+  }
   void shear_prod2D(Column &c, A3 &def2) {
     const double rdx0 = 1. / g.dx, dx = g.dx;
     const int j = 1, nzm = g.nzm;
@@ -961,7 +1043,8 @@ struct Model {
     const int nx = g.nx, ny = g.ny, nzm = g.nzm;
     A3 def2;
     def2.init(1, nx, 1, ny, 1, nzm);
-    shear_prod2D(c, def2);
+    if (g.YES3D) shear_prod3D(c, def2);    // tke_full.F90:109-113
+    else shear_prod2D(c, def2);
     A3 buoy_v, aprod_v;
     buoy_v.init(1, nx, 1, ny, 0, nzm);
     aprod_v.init(1, nx, 1, ny, 0, nzm);
@@ -1036,61 +1119,189 @@ struct Model {
   }
 
   // ---- advect2_mom_xy.F90:7-86 (2D) and advect2_mom_z.F90:7-128
+  // advect2_mom_xy.F90:7-86 and advect2_mom_z.F90:7-128 (2D and 3D)
   void advect_mom(Column &c) {
-    const int nx = g.nx, nzm = g.nzm, nz = g.nz, j = 1;
+    const int nx = g.nx, ny = g.ny, nzm = g.nzm, nz = g.nz;
     A3 &dudt = DU(c, c.na), &dvdt = DV(c, c.na), &dwdt = DW(c, c.na);
     A3 &u = c.u, &v = c.v, &w = c.w;
     const double dx25 = 0.25 / g.dx;
+    const double dy25 = 0.25 / g.dy;
     for (int k = 1; k <= nzm; ++k)
-      for (int i = 1; i <= nx; ++i) {
-        int kc = k + 1, kcu = std::min(kc, nzm);
-        double irho = 1. / (c.rhow(kc) * c.adzw(kc));
-        int ic = i + 1;
-        double fu1 = dx25 * (u(ic - 1, j, k) + u(i - 1, j, k)) * (u(i - 1, j, k) + u(ic - 1, j, k));
-        double fu2 = dx25 * (u(ic, j, k) + u(i, j, k)) * (u(i, j, k) + u(ic, j, k));
-        dudt(i, j, k) = dudt(i, j, k) - (fu2 - fu1);
-        double fv1 = dx25 * (u(ic - 1, j, k) + u(i - 1, j, k)) * (v(i - 1, j, k) + v(ic - 1, j, k));
-        double fv2 = dx25 * (u(ic, j, k) + u(i, j, k)) * (v(i, j, k) + v(ic, j, k));
-        dvdt(i, j, k) = dvdt(i, j, k) - (fv2 - fv1);
-        double fw1 = dx25 * (u(ic - 1, j, k) * c.rho(k) * c.adz(k) + u(ic - 1, j, kcu) * c.rho(kcu) * c.adz(kcu)) *
-                     (w(i - 1, j, kc) + w(ic - 1, j, kc));
-        double fw2 = dx25 * (u(ic, j, k) * c.rho(k) * c.adz(k) + u(ic, j, kcu) * c.rho(kcu) * c.adz(kcu)) *
-                     (w(i, j, kc) + w(ic, j, kc));
-        dwdt(i, j, kc) = dwdt(i, j, kc) - irho * (fw2 - fw1);
-      }
+      for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
+          int kc = k + 1, kcu = std::min(kc, nzm);
+          double irho = 1. / (c.rhow(kc) * c.adzw(kc));
+          int ic = i + 1;
+          double fu1 = dx25 * (u(ic - 1, j, k) + u(i - 1, j, k)) * (u(i - 1, j, k) + u(ic - 1, j, k));
+          double fu2 = dx25 * (u(ic, j, k) + u(i, j, k)) * (u(i, j, k) + u(ic, j, k));
+          dudt(i, j, k) = dudt(i, j, k) - (fu2 - fu1);
+          double fv1, fv2;
+          if (g.YES3D) {
+            int jb = j - 1;
+            fv1 = dx25 * (u(ic - 1, j, k) + u(ic - 1, jb, k)) * (v(i - 1, j, k) + v(ic - 1, j, k));
+            fv2 = dx25 * (u(ic, j, k) + u(ic, jb, k)) * (v(i, j, k) + v(ic, j, k));
+          } else {
+            fv1 = dx25 * (u(ic - 1, j, k) + u(i - 1, j, k)) * (v(i - 1, j, k) + v(ic - 1, j, k));
+            fv2 = dx25 * (u(ic, j, k) + u(i, j, k)) * (v(i, j, k) + v(ic, j, k));
+          }
+          dvdt(i, j, k) = dvdt(i, j, k) - (fv2 - fv1);
+          double fw1 = dx25 * (u(ic - 1, j, k) * c.rho(k) * c.adz(k) + u(ic - 1, j, kcu) * c.rho(kcu) * c.adz(kcu)) *
+                       (w(i - 1, j, kc) + w(ic - 1, j, kc));
+          double fw2 = dx25 * (u(ic, j, k) * c.rho(k) * c.adz(k) + u(ic, j, kcu) * c.rho(kcu) * c.adz(kcu)) *
+                       (w(i, j, kc) + w(ic, j, kc));
+          dwdt(i, j, kc) = dwdt(i, j, kc) - irho * (fw2 - fw1);
+          if (g.YES3D) {                       // the y terms (advect2_mom_xy.F90:46-60)
+            int jc = j + 1, ib = i - 1;
+            fu1 = dy25 * (v(i, jc - 1, k) + v(ib, jc - 1, k)) * (u(i, j - 1, k) + u(i, jc - 1, k));
+            fu2 = dy25 * (v(i, jc, k) + v(ib, jc, k)) * (u(i, j, k) + u(i, jc, k));
+            dudt(i, j, k) = dudt(i, j, k) - (fu2 - fu1);
+            fv1 = dy25 * (v(i, jc - 1, k) + v(i, j - 1, k)) * (v(i, j - 1, k) + v(i, jc - 1, k));
+            fv2 = dy25 * (v(i, jc, k) + v(i, j, k)) * (v(i, j, k) + v(i, jc, k));
+            dvdt(i, j, k) = dvdt(i, j, k) - (fv2 - fv1);
+            fw1 = dy25 * (v(i, jc - 1, k) * c.rho(k) * c.adz(k) + v(i, jc - 1, kcu) * c.rho(kcu) * c.adz(kcu)) *
+                  (w(i, j - 1, kc) + w(i, jc - 1, kc));
+            fw2 = dy25 * (v(i, jc, k) * c.rho(k) * c.adz(k) + v(i, jc, kcu) * c.rho(kcu) * c.adz(kcu)) *
+                  (w(i, j, kc) + w(i, jc, kc));
+            dwdt(i, j, kc) = dwdt(i, j, kc) - irho * (fw2 - fw1);
+          }
+        }
     // vertical
     A3 fuz, fvz, fwz;
-    fuz.init(1, nx, 1, 1, 1, nz); fvz.init(1, nx, 1, 1, 1, nz); fwz.init(1, nx, 1, 1, 1, nzm);
+    fuz.init(1, nx, 1, ny, 1, nz); fvz.init(1, nx, 1, ny, 1, nz); fwz.init(1, nx, 1, ny, 1, nzm);
     for (int k = 1; k <= nz; ++k) { c.uwle(k) = 0.; c.vwle(k) = 0.; }
     for (int k = 2; k <= nzm; ++k)
+      for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
+          double dz25 = 1. / (4. * c.dz);
+          int kb = k - 1;
+          double rhoi = dz25 * c.rhow(k);
+          double www = rhoi * (w(i, j, k) + w(i - 1, j, k));
+          fuz(i, j, k) = www * (u(i, j, k) + u(i, j, kb));
+          if (g.YES3D) fvz(i, j, k) = rhoi * (w(i, j, k) + w(i, j - 1, k)) * (v(i, j, k) + v(i, j, kb));
+          else fvz(i, j, k) = www * (v(i, j, k) + v(i, j, kb));
+          c.uwle(k) = c.uwle(k) + fuz(i, j, k);
+          c.vwle(k) = c.vwle(k) + fvz(i, j, k);
+        }
+    for (int k = 1; k <= nzm; ++k)
+      for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
+          double dz25 = 1. / (4. * c.dz);
+          int kc = k + 1;
+          double rhoi = 1. / (c.rho(k) * c.adz(k));
+          dudt(i, j, k) = dudt(i, j, k) - (fuz(i, j, kc) - fuz(i, j, k)) * rhoi;
+          dvdt(i, j, k) = dvdt(i, j, k) - (fvz(i, j, kc) - fvz(i, j, k)) * rhoi;
+          fwz(i, j, k) = dz25 * (w(i, j, kc) * c.rhow(kc) + w(i, j, k) * c.rhow(k)) * (w(i, j, kc) + w(i, j, k));
+        }
+    for (int k = 2; k <= nzm; ++k)
+      for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
+          int kb = k - 1;
+          double rhoi = 1. / (c.rhow(k) * c.adzw(k));
+          dwdt(i, j, k) = dwdt(i, j, k) - (fwz(i, j, k) - fwz(i, j, kb)) * rhoi;
+        }
+  }
+  // SGS_TKE/diffuse_mom3D.F90:7-207 (fluxbu, fluxbv, fluxtu, fluxtv are 0)
+  void diffuse_mom3D(Column &c) {
+    const int nx = g.nx, ny = g.ny, nzm = g.nzm, nz = g.nz;
+    A3 &dudt = DU(c, c.na), &dvdt = DV(c, c.na), &dwdt = DW(c, c.na);
+    A3 &u = c.u, &v = c.v, &w = c.w, &tk = c.tk;
+    A3 fu, fv, fw;
+    fu.init(0, nx, 0, ny, 1, nz); fv.init(0, nx, 0, ny, 1, nz); fw.init(0, nx, 0, ny, 1, nz);
+    const double rdx2 = 1. / (g.dx * g.dx), rdy2 = 1. / (g.dy * g.dy);
+    const double rdx25 = 0.25 * rdx2, rdy25 = 0.25 * rdy2;
+    const double dxy = g.dx / g.dy, dyx = g.dy / g.dx;
+    for (int k = 1; k <= nzm; ++k)
+      for (int j = 1; j <= ny; ++j)
+        for (int i = 0; i <= nx; ++i) {
+          int jb = j - 1, kc = k + 1, kcu = std::min(kc, nzm), ic = i + 1;
+          double dxz = g.dx / (c.dz * c.adzw(kc));
+          double rdx21 = rdx2 * c.grdf_x(k);
+          double rdx251 = rdx25 * c.grdf_x(k);
+          double tkx = rdx21 * tk(i, j, k);
+          fu(i, j, k) = -2. * tkx * (u(ic, j, k) - u(i, j, k));
+          tkx = rdx251 * (tk(i, j, k) + tk(i, jb, k) + tk(ic, j, k) + tk(ic, jb, k));
+          fv(i, j, k) = -tkx * (v(ic, j, k) - v(i, j, k) + (u(ic, j, k) - u(ic, jb, k)) * dxy);
+          tkx = rdx251 * (tk(i, j, k) + tk(ic, j, k) + tk(i, j, kcu) + tk(ic, j, kcu));
+          fw(i, j, k) = -tkx * (w(ic, j, kc) - w(i, j, kc) + (u(ic, j, kcu) - u(ic, j, k)) * dxz);
+        }
+    for (int k = 1; k <= nzm; ++k)
+      for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
+          int kc = k + 1, ib = i - 1;
+          dudt(i, j, k) = dudt(i, j, k) - (fu(i, j, k) - fu(ib, j, k));
+          dvdt(i, j, k) = dvdt(i, j, k) - (fv(i, j, k) - fv(ib, j, k));
+          dwdt(i, j, kc) = dwdt(i, j, kc) - (fw(i, j, k) - fw(ib, j, k));
+        }
+    for (int k = 1; k <= nzm; ++k)
+      for (int j = 0; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
+          int jc = j + 1, kc = k + 1, kcu = std::min(kc, nzm), ib = i - 1;
+          double dyz = g.dy / (c.dz * c.adzw(kc));
+          double rdy21 = rdy2 * c.grdf_y(k);
+          double rdy251 = rdy25 * c.grdf_y(k);
+          double tky = rdy21 * tk(i, j, k);
+          fv(i, j, k) = -2. * tky * (v(i, jc, k) - v(i, j, k));
+          tky = rdy251 * (tk(i, j, k) + tk(ib, j, k) + tk(i, jc, k) + tk(ib, jc, k));
+          fu(i, j, k) = -tky * (u(i, jc, k) - u(i, j, k) + (v(i, jc, k) - v(ib, jc, k)) * dyx);
+          tky = rdy251 * (tk(i, j, k) + tk(i, jc, k) + tk(i, j, kcu) + tk(i, jc, kcu));
+          fw(i, j, k) = -tky * (w(i, jc, kc) - w(i, j, kc) + (v(i, jc, kcu) - v(i, jc, k)) * dyz);
+        }
+    for (int k = 1; k <= nzm; ++k)
+      for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
+          int jb = j - 1, kc = k + 1;
+          dudt(i, j, k) = dudt(i, j, k) - (fu(i, j, k) - fu(i, jb, k));
+          dvdt(i, j, k) = dvdt(i, j, k) - (fv(i, j, k) - fv(i, jb, k));
+          dwdt(i, j, kc) = dwdt(i, j, kc) - (fw(i, j, k) - fw(i, jb, k));
+        }
+    for (int k = 1; k <= nzm; ++k) { c.uwsb(k) = 0.; c.vwsb(k) = 0.; }
+    for (int k = 1; k <= nzm - 1; ++k)
+      for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
+          int jb = j - 1, kc = k + 1, ib = i - 1;
+          double rdz = 1. / c.dz;
+          double rdz2 = rdz * rdz * c.grdf_z(k);
+          double rdz25 = 0.25 * rdz2;
+          double iadz = 1. / c.adz(k);
+          double iadzw = 1. / c.adzw(kc);
+          double dzx = c.dz / g.dx, dzy = c.dz / g.dy;
+          double tkz = rdz2 * tk(i, j, k);
+          fw(i, j, kc) = -2. * tkz * (w(i, j, kc) - w(i, j, k)) * c.rho(k) * iadz;
+          tkz = rdz25 * (tk(i, j, k) + tk(ib, j, k) + tk(i, j, kc) + tk(ib, j, kc));
+          fu(i, j, kc) = -tkz * ((u(i, j, kc) - u(i, j, k)) * iadzw + (w(i, j, kc) - w(ib, j, kc)) * dzx) * c.rhow(kc);
+          tkz = rdz25 * (tk(i, j, k) + tk(i, jb, k) + tk(i, j, kc) + tk(i, jb, kc));
+          fv(i, j, kc) = -tkz * ((v(i, j, kc) - v(i, j, k)) * iadzw + (w(i, j, kc) - w(i, jb, kc)) * dzy) * c.rhow(kc);
+          c.uwsb(kc) = c.uwsb(kc) + fu(i, j, kc);
+          c.vwsb(kc) = c.vwsb(kc) + fv(i, j, kc);
+        }
+    for (int j = 1; j <= ny; ++j)
       for (int i = 1; i <= nx; ++i) {
-        double dz25 = 1. / (4. * c.dz);
-        int kb = k - 1;
-        double rhoi = dz25 * c.rhow(k);
-        double www = rhoi * (w(i, j, k) + w(i - 1, j, k));
-        fuz(i, j, k) = www * (u(i, j, k) + u(i, j, kb));
-        fvz(i, j, k) = www * (v(i, j, k) + v(i, j, kb));
-        c.uwle(k) = c.uwle(k) + fuz(i, j, k);
-        c.vwle(k) = c.vwle(k) + fvz(i, j, k);
+        double rdz = 1. / c.dz;
+        double rdz2 = rdz * rdz * c.grdf_z(nzm - 1);
+        double tkz = rdz2 * c.grdf_z(nzm) * tk(i, j, nzm);
+        fw(i, j, nz) = -2. * tkz * (w(i, j, nz) - w(i, j, nzm)) / c.adz(nzm) * c.rho(nzm);
+        fu(i, j, 1) = 0.0 * rdz * c.rhow(1);
+        fv(i, j, 1) = 0.0 * rdz * c.rhow(1);
+        fu(i, j, nz) = 0.0 * rdz * c.rhow(nz);
+        fv(i, j, nz) = 0.0 * rdz * c.rhow(nz);
+        c.uwsb(1) = c.uwsb(1) + fu(i, j, 1);
+        c.vwsb(1) = c.vwsb(1) + fv(i, j, 1);
       }
     for (int k = 1; k <= nzm; ++k)
-      for (int i = 1; i <= nx; ++i) {
-        double dz25 = 1. / (4. * c.dz);
-        int kc = k + 1;
-        double rhoi = 1. / (c.rho(k) * c.adz(k));
-        dudt(i, j, k) = dudt(i, j, k) - (fuz(i, j, kc) - fuz(i, j, k)) * rhoi;
-        dvdt(i, j, k) = dvdt(i, j, k) - (fvz(i, j, kc) - fvz(i, j, k)) * rhoi;
-        fwz(i, j, k) = dz25 * (w(i, j, kc) * c.rhow(kc) + w(i, j, k) * c.rhow(k)) * (w(i, j, kc) + w(i, j, k));
-      }
+      for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
+          int kc = k + 1;
+          double rhoi = 1. / (c.rho(k) * c.adz(k));
+          dudt(i, j, k) = dudt(i, j, k) - (fu(i, j, kc) - fu(i, j, k)) * rhoi;
+          dvdt(i, j, k) = dvdt(i, j, k) - (fv(i, j, kc) - fv(i, j, k)) * rhoi;
+        }
     for (int k = 2; k <= nzm; ++k)
-      for (int i = 1; i <= nx; ++i) {
-        int kb = k - 1;
-        double rhoi = 1. / (c.rhow(k) * c.adzw(k));
-        dwdt(i, j, k) = dwdt(i, j, k) - (fwz(i, j, k) - fwz(i, j, kb)) * rhoi;
-      }
+      for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
+          double rhoi = 1. / (c.rhow(k) * c.adzw(k));
+          dwdt(i, j, k) = dwdt(i, j, k) - (fw(i, j, k + 1) - fw(i, j, k)) * rhoi;
+        }
   }
-
-  // ---- diffuse_mom2D.F90:7-162
   void diffuse_mom2D(Column &c) {
     const int nx = g.nx, nzm = g.nzm, nz = g.nz, j = 1;
     A3 &dudt = DU(c, c.na), &dvdt = DV(c, c.na), &dwdt = DW(c, c.na);
@@ -1165,7 +1376,108 @@ struct Model {
   }
 
   // ---- pressure.F90:8-323 + press_rhs.F90 + press_grad.F90 (2D)
+  // pressure.F90:8-323 with press_rhs.F90:8-106 and press_grad.F90:8-76, 3D:
+  // real transform in x of every row, then in y of every x coefficient
+  // (i = 1..nx+1), a tridiagonal solve per (i, j) coefficient with the
+  // eigenvalue eign(i, j), and the inverse transforms in the reverse order.
+  void pressure3D(Column &c) {
+    const int nx = g.nx, ny = g.ny, nzm = g.nzm;
+    A3 &u = c.u, &v = c.v, &w = c.w;
+    A3 &dua = DU(c, c.na), &dub = DU(c, c.nb), &duc = DU(c, c.nc);
+    A3 &dva = DV(c, c.na), &dvb = DV(c, c.nb), &dvc = DV(c, c.nc);
+    A3 &dwa = DW(c, c.na), &dwb = DW(c, c.nb), &dwc = DW(c, c.nc);
+    auto bound_duvdt = [&]() {        // bound_duvdt.F90:14-31
+      for (int k = 1; k <= nzm; ++k)
+        for (int j = 1; j <= ny; ++j) dua(nx + 1, j, k) = dua(1, j, k);
+      for (int k = 1; k <= nzm; ++k)
+        for (int i = 1; i <= nx; ++i) dva(i, ny + 1, k) = dva(i, 1, k);
+    };
+    bound_duvdt();
+    const double rdx = 1. / g.dx, rdy = 1. / g.dy;
+    const double btat = c.bt / c.at, ctat = c.ct / c.at;
+    for (int k = 1; k <= nzm; ++k)
+      for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
+          int kc = k + 1, jc = j + 1, ic = i + 1;
+          double rdz = 1. / (c.adz(k) * c.dz);
+          double rup = c.rhow(kc) / c.rho(k) * rdz;
+          double rdn = c.rhow(k) / c.rho(k) * rdz;
+          double dta = 1. / c.dt3[c.na - 1] / c.at;
+          c.p(i, j, k) = (rdx * (u(ic, j, k) - u(i, j, k)) + rdy * (v(i, jc, k) - v(i, j, k)) +
+                          (w(i, j, kc) * rup - w(i, j, k) * rdn)) * dta +
+                         (rdx * (dua(ic, j, k) - dua(i, j, k)) + rdy * (dva(i, jc, k) - dva(i, j, k)) +
+                          (dwa(i, j, kc) * rup - dwa(i, j, k) * rdn)) +
+                         btat * (rdx * (dub(ic, j, k) - dub(i, j, k)) + rdy * (dvb(i, jc, k) - dvb(i, j, k)) +
+                                 (dwb(i, j, kc) * rup - dwb(i, j, k) * rdn)) +
+                         ctat * (rdx * (duc(ic, j, k) - duc(i, j, k)) + rdy * (dvc(i, jc, k) - dvc(i, j, k)) +
+                                 (dwc(i, j, kc) * rup - dwc(i, j, k) * rdn));
+          c.p(i, j, k) = c.p(i, j, k) * c.rho(k);
+        }
+    const int nx2 = nx + 2, ny2 = ny + 2;
+    // f(i, j, k), i = 1..nx2, j = 1..ny2 (1-based), level k = 1..nzm
+    std::vector<double> f((size_t)nx2 * ny2 * (nzm + 1), 0.0), work((size_t)std::max(nx2, ny2) + 2, 0.0);
+    std::vector<double> col((size_t)ny2, 0.0);
+    auto F = [&](int i, int j, int k) -> double & { return f[((size_t)k * ny2 + (j - 1)) * nx2 + (i - 1)]; };
+    for (int k = 1; k <= nzm; ++k) {
+      for (int j = 1; j <= ny; ++j) {
+        for (int i = 1; i <= nx; ++i) F(i, j, k) = c.p(i, j, k);
+        fft991(&F(1, j, k), work.data(), g.trigxi.data(), g.ifaxi, nx, -1);
+      }
+      for (int i = 1; i <= nx + 1; ++i) {
+        for (int j = 1; j <= ny2; ++j) col[j - 1] = F(i, j, k);
+        fft991(col.data(), work.data(), g.trigxj.data(), g.ifaxj, ny, -1);
+        for (int j = 1; j <= ny2; ++j) F(i, j, k) = col[j - 1];
+      }
+    }
+    std::vector<double> a(nzm + 1), cc(nzm + 1), alfa(nzm + 1), beta(nzm + 1);
+    for (int k = 1; k <= nzm; ++k) {
+      a[k] = c.rhow(k) / (c.adz(k) * c.adzw(k) * c.dz * c.dz);
+      cc[k] = c.rhow(k + 1) / (c.adz(k) * c.adzw(k + 1) * c.dz * c.dz);
+    }
+    for (int j = 1; j <= ny2; ++j)
+      for (int i = 1; i <= nx + 1; ++i) {
+        int jd = (int)(((float)j - 0.1f) / 2.0f);
+        int id = (int)(((float)i - 0.1f) / 2.0f);
+        double eign = g.eign[(size_t)(j - 1) * g.eign_ni + (i - 1)];
+        double b;
+        if (id + jd == 0) b = 1. / (eign * c.rho(1) - a[1] - cc[1]);
+        else b = 1. / (eign * c.rho(1) - cc[1]);
+        alfa[1] = -cc[1] * b;
+        beta[1] = F(i, j, 1) * b;
+        for (int k = 2; k <= nzm - 1; ++k) {
+          double e = 1. / (eign * c.rho(k) - a[k] - cc[k] + a[k] * alfa[k - 1]);
+          alfa[k] = -cc[k] * e;
+          beta[k] = (F(i, j, k) - a[k] * beta[k - 1]) * e;
+        }
+        F(i, j, nzm) = (F(i, j, nzm) - a[nzm] * beta[nzm - 1]) / (eign * c.rho(nzm) - a[nzm] + a[nzm] * alfa[nzm - 1]);
+        for (int k = nzm - 1; k >= 1; --k) F(i, j, k) = alfa[k] * F(i, j, k + 1) + beta[k];
+      }
+    for (int k = 1; k <= nzm; ++k) {
+      for (int i = 1; i <= nx + 1; ++i) {
+        for (int j = 1; j <= ny2; ++j) col[j - 1] = F(i, j, k);
+        fft991(col.data(), work.data(), g.trigxj.data(), g.ifaxj, ny, +1);
+        for (int j = 1; j <= ny2; ++j) F(i, j, k) = col[j - 1];
+      }
+      for (int j = 1; j <= ny; ++j) fft991(&F(1, j, k), work.data(), g.trigxi.data(), g.ifaxi, nx, +1);
+      for (int j = 0; j <= ny; ++j)
+        for (int i = 0; i <= nx; ++i) c.p(i, j, k) = F(i == 0 ? nx : i, j == 0 ? ny : j, k);
+    }
+    for (int k = 1; k <= nzm; ++k)
+      for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
+          int kb = std::max(1, k - 1), jb = j - 1, ib = i - 1;
+          double rdz = 1. / (c.dz * c.adzw(k));
+          dua(i, j, k) = dua(i, j, k) - (c.p(i, j, k) - c.p(ib, j, k)) * rdx;
+          dva(i, j, k) = dva(i, j, k) - (c.p(i, j, k) - c.p(i, jb, k)) * rdy;
+          dwa(i, j, k) = dwa(i, j, k) - (c.p(i, j, k) - c.p(i, j, kb)) * rdz;
+        }
+    for (int k = 1; k <= nzm; ++k)
+      for (int j = 0; j <= ny; ++j)
+        for (int i = 0; i <= nx; ++i) c.p(i, j, k) = c.p(i, j, k) * c.rho(k);
+    bound_duvdt();
+  }
   void pressure(Column &c) {
+    if (g.YES3D) { pressure3D(c); return; }
     const int nx = g.nx, nzm = g.nzm, j = 1;
     A3 &u = c.u, &w = c.w;
     // bound_duvdt (bound_duvdt.F90): periodic copy of dudt(nxp1, na)
@@ -1279,6 +1591,147 @@ struct Model {
   }
 
   // ---- advect_scalar.F90:9-76 + ADV_MPDATA/advect_scalar2D.F90:8-244
+  // ADV_MPDATA/advect_scalar3D.F90:8-349 (nonos, no walls), with the
+  // advect_scalar.F90 wrapper's fadv (horizontal sum of the change)
+  void advect_scalar3D(Column &c, A3 &f, A1 *fadv, A1 *flux) {
+    const int nx = g.nx, ny = g.ny, nzm = g.nzm, nz = g.nz;
+    A3 &u = c.u, &v = c.v, &w = c.w;
+    std::vector<double> f0;
+    if (fadv) {
+      f0.resize((size_t)(nx + 1) * (ny + 1) * (nzm + 1));
+      for (int k = 1; k <= nzm; ++k)
+        for (int j = 1; j <= ny; ++j)
+          for (int i = 1; i <= nx; ++i) f0[((size_t)k * (ny + 1) + j) * (nx + 1) + i] = f(i, j, k);
+    }
+    A3 mx, mn, uuu, vvv, www;
+    mx.init(0, nx + 1, 0, ny + 1, 1, nzm);
+    mn.init(0, nx + 1, 0, ny + 1, 1, nzm);
+    uuu.init(-1, nx + 3, -1, ny + 2, 1, nzm);
+    vvv.init(-1, nx + 2, -1, ny + 3, 1, nzm);
+    www.init(-1, nx + 2, -1, ny + 2, 1, nz);
+    std::vector<double> iadz(nzm + 1), irho(nzm + 1), irhow(nzm + 1), fl(nz + 1, 0.0);
+    const double eps = R4(1.e-10);
+    auto andiff = [](double x1, double x2, double a, double b) { return (fabs(a) - a * a * b) * 0.5 * (x2 - x1); };
+    auto across = [](double x1, double a1, double a2) { return 0.03125 * a1 * a2 * x1; };
+    auto pp = [](double y) { return fmax2(0., y); };
+    auto pn = [](double y) { return -fmin2(0., y); };
+    auto max7 = [](double a, double b, double c_, double d, double e, double f_, double g_) {
+      return fmax2(fmax2(fmax2(fmax2(fmax2(fmax2(a, b), c_), d), e), f_), g_);
+    };
+    auto min7 = [](double a, double b, double c_, double d, double e, double f_, double g_) {
+      return fmin2(fmin2(fmin2(fmin2(fmin2(fmin2(a, b), c_), d), e), f_), g_);
+    };
+    for (int j = -1; j <= ny + 2; ++j)
+      for (int i = -1; i <= nx + 2; ++i) www(i, j, nz) = 0.;
+    for (int k = 1; k <= nzm; ++k)
+      for (int j = 0; j <= ny + 1; ++j)
+        for (int i = 0; i <= nx + 1; ++i) {
+          int kc = std::min(nzm, k + 1), kb = std::max(1, k - 1);
+          mx(i, j, k) = max7(f(i - 1, j, k), f(i + 1, j, k), f(i, j - 1, k), f(i, j + 1, k), f(i, j, kb), f(i, j, kc), f(i, j, k));
+          mn(i, j, k) = min7(f(i - 1, j, k), f(i + 1, j, k), f(i, j - 1, k), f(i, j + 1, k), f(i, j, kb), f(i, j, kc), f(i, j, k));
+        }
+    for (int k = 1; k <= nzm; ++k)
+      for (int j = -1; j <= ny + 3; ++j)
+        for (int i = -1; i <= nx + 3; ++i) {
+          int kb = std::max(1, k - 1);
+          if (j <= ny + 2) uuu(i, j, k) = fmax2(0., u(i, j, k)) * f(i - 1, j, k) + fmin2(0., u(i, j, k)) * f(i, j, k);
+          if (i <= nx + 2) vvv(i, j, k) = fmax2(0., v(i, j, k)) * f(i, j - 1, k) + fmin2(0., v(i, j, k)) * f(i, j, k);
+          if (i <= nx + 2 && j <= ny + 2)
+            www(i, j, k) = fmax2(0., w(i, j, k)) * f(i, j, kb) + fmin2(0., w(i, j, k)) * f(i, j, k);
+          if (i == -1 && j == -1) fl[k] = 0.;
+        }
+    for (int k = 1; k <= nzm; ++k) {
+      irho[k] = 1. / c.rho(k);
+      iadz[k] = 1. / c.adz(k);
+      irhow[k] = 1. / (c.rhow(k) * c.adz(k));
+    }
+    for (int k = 1; k <= nzm; ++k)
+      for (int j = -1; j <= ny + 2; ++j)
+        for (int i = -1; i <= nx + 2; ++i) {
+          if (i >= 1 && i <= nx && j >= 1 && j <= ny) fl[k] = fl[k] + www(i, j, k);
+          f(i, j, k) = f(i, j, k) - (uuu(i + 1, j, k) - uuu(i, j, k) + vvv(i, j + 1, k) - vvv(i, j, k) +
+                                     (www(i, j, k + 1) - www(i, j, k)) * iadz[k]) * irho[k];
+        }
+    for (int k = 1; k <= nzm; ++k)
+      for (int j = 0; j <= ny + 2; ++j)
+        for (int i = 0; i <= nx + 2; ++i) {
+          int kc = std::min(nzm, k + 1), kb = std::max(1, k - 1);
+          double dd = (double)(2.f / (float)(kc - kb)) / c.adz(k);
+          int jb = j - 1, jc = j + 1, ib = i - 1, ic = i + 1;
+          if (j <= ny + 1)
+            uuu(i, j, k) = andiff(f(ib, j, k), f(i, j, k), u(i, j, k), irho[k]) -
+                           (across(f(ib, jc, k) + f(i, jc, k) - f(ib, jb, k) - f(i, jb, k), u(i, j, k),
+                                   v(ib, j, k) + v(ib, jc, k) + v(i, jc, k) + v(i, j, k)) +
+                            across(dd * (f(ib, j, kc) + f(i, j, kc) - f(ib, j, kb) - f(i, j, kb)), u(i, j, k),
+                                   w(ib, j, k) + w(ib, j, kc) + w(i, j, k) + w(i, j, kc))) * irho[k];
+          if (i <= nx + 1)
+            vvv(i, j, k) = andiff(f(i, jb, k), f(i, j, k), v(i, j, k), irho[k]) -
+                           (across(f(ic, jb, k) + f(ic, j, k) - f(ib, jb, k) - f(ib, j, k), v(i, j, k),
+                                   u(i, jb, k) + u(i, j, k) + u(ic, j, k) + u(ic, jb, k)) +
+                            across(dd * (f(i, jb, kc) + f(i, j, kc) - f(i, jb, kb) - f(i, j, kb)), v(i, j, k),
+                                   w(i, jb, k) + w(i, j, k) + w(i, j, kc) + w(i, jb, kc))) * irho[k];
+          if (i <= nx + 1 && j <= ny + 1)
+            www(i, j, k) = andiff(f(i, j, kb), f(i, j, k), w(i, j, k), irhow[k]) -
+                           (across(f(ic, j, kb) + f(ic, j, k) - f(ib, j, kb) - f(ib, j, k), w(i, j, k),
+                                   u(i, j, kb) + u(i, j, k) + u(ic, j, k) + u(ic, j, kb)) +
+                            across(f(i, jc, k) + f(i, jc, kb) - f(i, jb, k) - f(i, jb, kb), w(i, j, k),
+                                   v(i, j, kb) + v(i, jc, kb) + v(i, jc, k) + v(i, j, k))) * irho[k];
+        }
+    for (int j = -1; j <= ny + 2; ++j)
+      for (int i = -1; i <= nx + 2; ++i) www(i, j, 1) = 0.;
+    for (int k = 1; k <= nzm; ++k)
+      for (int j = 0; j <= ny + 1; ++j)
+        for (int i = 0; i <= nx + 1; ++i) {
+          int kc = std::min(nzm, k + 1), kb = std::max(1, k - 1);
+          mx(i, j, k) = fmax2(max7(f(i - 1, j, k), f(i + 1, j, k), f(i, j - 1, k), f(i, j + 1, k), f(i, j, kb), f(i, j, kc), f(i, j, k)), mx(i, j, k));
+          mn(i, j, k) = fmin2(min7(f(i - 1, j, k), f(i + 1, j, k), f(i, j - 1, k), f(i, j + 1, k), f(i, j, kb), f(i, j, kc), f(i, j, k)), mn(i, j, k));
+        }
+    for (int k = 1; k <= nzm; ++k)
+      for (int j = 0; j <= ny + 1; ++j)
+        for (int i = 0; i <= nx + 1; ++i) {
+          int kc = std::min(nzm, k + 1), jc = j + 1, ic = i + 1;
+          mx(i, j, k) = c.rho(k) * (mx(i, j, k) - f(i, j, k)) /
+                        (pn(uuu(ic, j, k)) + pp(uuu(i, j, k)) + pn(vvv(i, jc, k)) + pp(vvv(i, j, k)) +
+                         (pn(www(i, j, kc)) + pp(www(i, j, k))) * iadz[k] + eps);
+          mn(i, j, k) = c.rho(k) * (f(i, j, k) - mn(i, j, k)) /
+                        (pp(uuu(ic, j, k)) + pn(uuu(i, j, k)) + pp(vvv(i, jc, k)) + pn(vvv(i, j, k)) +
+                         (pp(www(i, j, kc)) + pn(www(i, j, k))) * iadz[k] + eps);
+        }
+    for (int k = 1; k <= nzm; ++k)
+      for (int j = 1; j <= ny + 1; ++j)
+        for (int i = 1; i <= nx + 1; ++i) {
+          if (j <= ny) {
+            int ib = i - 1;
+            uuu(i, j, k) = pp(uuu(i, j, k)) * fmin3(1., mx(i, j, k), mn(ib, j, k)) -
+                           pn(uuu(i, j, k)) * fmin3(1., mx(ib, j, k), mn(i, j, k));
+          }
+          if (i <= nx) {
+            int jb = j - 1;
+            vvv(i, j, k) = pp(vvv(i, j, k)) * fmin3(1., mx(i, j, k), mn(i, jb, k)) -
+                           pn(vvv(i, j, k)) * fmin3(1., mx(i, jb, k), mn(i, j, k));
+          }
+          if (i <= nx && j <= ny) {
+            int kb = std::max(1, k - 1);
+            www(i, j, k) = pp(www(i, j, k)) * fmin3(1., mx(i, j, k), mn(i, j, kb)) -
+                           pn(www(i, j, k)) * fmin3(1., mx(i, j, kb), mn(i, j, k));
+            fl[k] = fl[k] + www(i, j, k);
+          }
+        }
+    for (int k = 1; k <= nzm; ++k)
+      for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i)
+          f(i, j, k) = fmax2(0., f(i, j, k) - (uuu(i + 1, j, k) - uuu(i, j, k) + vvv(i, j + 1, k) - vvv(i, j, k) +
+                                               (www(i, j, k + 1) - www(i, j, k)) * iadz[k]) * irho[k]);
+    if (flux)
+      for (int k = 1; k <= nzm; ++k) (*flux)(k) = fl[k];
+    if (fadv)
+      for (int k = 1; k <= nzm; ++k) {
+        double s_ = 0.;
+        for (int j = 1; j <= ny; ++j)
+          for (int i = 1; i <= nx; ++i) s_ = s_ + (f(i, j, k) - f0[((size_t)k * (ny + 1) + j) * (nx + 1) + i]);
+        (*fadv)(k) = s_;
+      }
+  }
   void advect_scalar2D(Column &c, A3 &f, A1 *fadv, A1 *flux) {
     const int nx = g.nx, nzm = g.nzm, nz = g.nz, j = 1;
     A3 &u = c.u, &w = c.w;
@@ -1533,6 +1986,84 @@ struct Model {
   }
 
   // ---- diffuse_scalar.F90:6-72 + diffuse_scalar2D.F90:6-140
+  // SGS_TKE/diffuse_scalar3D.F90:6-218 (fluxb = fluxt = 0, no walls), with
+  // the sgs_scalars wrapper's fdiff (horizontal sum of the change)
+  void diffuse_scalar3D(Column &c, A3 &f, A1 *fdiff, A1 *flux) {
+    const int nx = g.nx, ny = g.ny, nzm = g.nzm, nz = g.nz;
+    std::vector<double> df;
+    if (fdiff) {
+      df.resize((size_t)(nx + 1) * (ny + 1) * (nzm + 1));
+      for (int k = 1; k <= nzm; ++k)
+        for (int j = 1; j <= ny; ++j)
+          for (int i = 1; i <= nx; ++i) df[((size_t)k * (ny + 1) + j) * (nx + 1) + i] = f(i, j, k);
+    }
+    const double rdx2 = 1. / (g.dx * g.dx), rdy2 = 1. / (g.dy * g.dy);
+    A3 flx_x, flx_y, flx_z, dfdt;
+    flx_x.init(0, nx, 0, ny, 1, nzm);
+    flx_y.init(0, nx, 0, ny, 1, nzm);
+    flx_z.init(1, nx, 1, ny, 0, nzm);
+    dfdt.init(1, nx, 1, ny, 1, nzm);
+    A3 &tkh = c.tkh;
+    for (int k = 1; k <= nzm; ++k)
+      for (int j = 0; j <= ny; ++j)
+        for (int i = 0; i <= nx; ++i) {
+          if (j >= 1) {
+            int ic = i + 1;
+            double rdx5 = 0.5 * rdx2 * c.grdf_x(k);
+            double tkx = rdx5 * (tkh(i, j, k) + tkh(ic, j, k));
+            flx_x(i, j, k) = -tkx * (f(ic, j, k) - f(i, j, k));
+          }
+          if (i >= 1) {
+            int jc = j + 1;
+            double rdy5 = 0.5 * rdy2 * c.grdf_y(k);
+            double tky = rdy5 * (tkh(i, j, k) + tkh(i, jc, k));
+            flx_y(i, j, k) = -tky * (f(i, jc, k) - f(i, j, k));
+          }
+        }
+    for (int k = 1; k <= nzm; ++k)
+      for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
+          dfdt(i, j, k) = dfdt(i, j, k) - (flx_x(i, j, k) - flx_x(i - 1, j, k));
+          dfdt(i, j, k) = dfdt(i, j, k) - (flx_y(i, j, k) - flx_y(i, j - 1, k));
+        }
+    std::vector<double> fl(nz + 1, 0.0);
+    for (int k = 1; k <= nzm; ++k)
+      for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
+          if (k <= nzm - 1) {
+            int kc = k + 1;
+            double rhoi = c.rhow(kc) / c.adzw(kc);
+            double rdz2 = 1. / (c.dz * c.dz);
+            double rdz5 = 0.5 * rdz2 * c.grdf_z(k);
+            double tkz = rdz5 * (tkh(i, j, k) + tkh(i, j, kc));
+            flx_z(i, j, k) = -tkz * (f(i, j, kc) - f(i, j, k)) * rhoi;
+            fl[kc] = fl[kc] + flx_z(i, j, k);
+          } else {
+            double tmp = 1. / c.adzw(nz);
+            double rdz = 1. / c.dz;
+            flx_z(i, j, 0) = 0.0 * rdz * c.rhow(1);
+            flx_z(i, j, nzm) = 0.0 * rdz * tmp * c.rhow(nz);
+            fl[1] = fl[1] + flx_z(i, j, 0);
+          }
+        }
+    for (int k = 1; k <= nzm; ++k)
+      for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
+          int kb = k - 1;
+          double rhoi = 1. / (c.adz(k) * c.rho(k));
+          dfdt(i, j, k) = c.dtn * (dfdt(i, j, k) - (flx_z(i, j, k) - flx_z(i, j, kb)) * rhoi);
+          f(i, j, k) = f(i, j, k) + dfdt(i, j, k);
+        }
+    if (flux)
+      for (int k = 1; k <= nzm; ++k) (*flux)(k) = fl[k];
+    if (fdiff)
+      for (int k = 1; k <= nzm; ++k) {
+        double s_ = 0.;
+        for (int j = 1; j <= ny; ++j)
+          for (int i = 1; i <= nx; ++i) s_ = s_ + (f(i, j, k) - df[((size_t)k * (ny + 1) + j) * (nx + 1) + i]);
+        (*fdiff)(k) = s_;
+      }
+  }
   void diffuse_scalar2D(Column &c, A3 &f, A1 *fdiff, A1 *flux) {
     const int nx = g.nx, nzm = g.nzm, nz = g.nz, j = 1;
     std::vector<double> df;
@@ -1787,13 +2318,20 @@ struct Model {
     tke_full(c);
     boundaries(c, 4);
     advect_mom(c);
-    diffuse_mom2D(c);
+    if (g.YES3D) diffuse_mom3D(c);       // diffuse_mom.F90:15-31
+    else diffuse_mom2D(c);
     pressure(c);
     adams(c);
     boundaries(c, 2);
-    advect_scalar2D(c, c.t, nullptr, nullptr);
-    advect_scalar2D(c, c.qt, &c.mkadv[0], &c.mkwle[0]);
-    advect_scalar2D(c, c.qp, &c.mkadv[1], &c.mkwle[1]);
+    if (g.YES3D) {                       // advect_scalar.F90:52-56
+      advect_scalar3D(c, c.t, nullptr, nullptr);
+      advect_scalar3D(c, c.qt, &c.mkadv[0], &c.mkwle[0]);
+      advect_scalar3D(c, c.qp, &c.mkadv[1], &c.mkwle[1]);
+    } else {
+      advect_scalar2D(c, c.t, nullptr, nullptr);
+      advect_scalar2D(c, c.qt, &c.mkadv[0], &c.mkwle[0]);
+      advect_scalar2D(c, c.qp, &c.mkadv[1], &c.mkwle[1]);
+    }
     precip_fall_part1(c, s);
   }
   // ---- mean-state acceleration (accelerate_crm.F90:109-366), split so the
@@ -1882,9 +2420,15 @@ struct Model {
     precip_fall_part2(c, s, nprec);
     uvw(c);
     boundaries(c, 3);
-    diffuse_scalar2D(c, c.t, nullptr, nullptr);
-    diffuse_scalar2D(c, c.qt, &c.mkdiff[0], &c.mkwsb[0]);
-    diffuse_scalar2D(c, c.qp, &c.mkdiff[1], &c.mkwsb[1]);
+    if (g.YES3D) {                       // diffuse_scalar.F90:30-36
+      diffuse_scalar3D(c, c.t, nullptr, nullptr);
+      diffuse_scalar3D(c, c.qt, &c.mkdiff[0], &c.mkwsb[0]);
+      diffuse_scalar3D(c, c.qp, &c.mkdiff[1], &c.mkwsb[1]);
+    } else {
+      diffuse_scalar2D(c, c.t, nullptr, nullptr);
+      diffuse_scalar2D(c, c.qt, &c.mkdiff[0], &c.mkwsb[0]);
+      diffuse_scalar2D(c, c.qp, &c.mkdiff[1], &c.mkwsb[1]);
+    }
     if (c.icycle == 1) precip_init(c);
     cloud(c);
     precip_proc(c);
@@ -2008,8 +2552,8 @@ static int setup_grid_constants(Grid &g, const crm_config *cfg, const crm_call_d
   g.dx = cfg->crm_dx;
   g.dy = (g.ny == 1) ? g.dx : cfg->crm_dy;    // setparm.F90:56,70
   g.batch_mode = cfg->batch_mode;
-  if (g.YES3D) return CRM_ERR_UNSUPPORTED;
   if (g.nx < 4 || g.nx % 2 || g.nzm < 4 || g.plev < g.nzm + 1) return CRM_ERR_ARG;
+  if (g.YES3D && (g.ny < 4 || g.ny % 2 || !(g.dy > 0))) return CRM_ERR_ARG;
   if (g.nx % g.nx_rad || g.ny % g.ny_rad) return CRM_ERR_ARG;
   if (cfg->microphysics != CRM_MICRO_SAM1MOM) return CRM_ERR_UNSUPPORTED;
   g.nstop = (int)(desc->dt_gl / cfg->crm_dt);   // crm_module.F90:712-713
@@ -2028,19 +2572,29 @@ static int setup_grid_constants(Grid &g, const crm_config *cfg, const crm_call_d
   for (int k = 1; k <= g.ifaxi[0]; ++k)
     if (g.ifaxi[k] > 5) return CRM_ERR_ARG;
   fftrig(g.trigxi, g.nx);
-  // eigenvalues (pressure.F90:172-198), 2D: j = 1 only
-  g.eign_ni = g.nx + 1; g.eign_nj = 1;
-  g.eign.assign(g.eign_ni, 0.0);
+  if (g.YES3D) {
+    fax(g.ifaxj, g.ny);
+    for (int k = 1; k <= g.ifaxj[0]; ++k)
+      if (g.ifaxj[k] > 5) return CRM_ERR_ARG;
+    fftrig(g.trigxj, g.ny);
+  }
+  // eigenvalues (pressure.F90:172-198) for i = 1..nx+1 and j = 1..ny+2
+  // (2D: j = 1 only), periodic in both directions (no walls)
+  g.eign_ni = g.nx + 1; g.eign_nj = g.YES3D ? g.ny + 2 : 1;
+  g.eign.assign((size_t)g.eign_ni * g.eign_nj, 0.0);
   {
     double ddx2 = 1.0 / (g.dx * g.dx), ddy2 = 1.0 / (g.dy * g.dy);
     double pii = 3.14159265358979323846;
     double xnx = pii / g.nx, xny = pii / g.ny;
-    int jd = (int)(((float)1 - 0.1f) / 2.f);
-    double xj = jd, facty = 2.0;
-    for (int i = 1; i <= g.nx + 1; ++i) {
-      int id = (int)(((float)i - 0.1f) / 2.f);
-      double xi = id, factx = 2.0;
-      g.eign[i - 1] = (2.0 * cos(factx * xnx * xi) - 2.0) * ddx2 + (2.0 * cos(facty * xny * xj) - 2.0) * ddy2;
+    for (int j = 1; j <= g.eign_nj; ++j) {
+      int jd = (int)(((float)j - 0.1f) / 2.f);
+      double xj = jd, facty = 2.0;
+      for (int i = 1; i <= g.nx + 1; ++i) {
+        int id = (int)(((float)i - 0.1f) / 2.f);
+        double xi = id, factx = 2.0;
+        g.eign[(size_t)(j - 1) * g.eign_ni + (i - 1)] =
+            (2.0 * cos(factx * xnx * xi) - 2.0) * ddx2 + (2.0 * cos(facty * xny * xj) - 2.0) * ddy2;
+      }
     }
   }
   // gamma functions: gammafff.c returns (float)exp(lgamma(x)) for float x
