@@ -518,6 +518,21 @@ struct ColumnKernel : NxDim<NX> {
     SYNC;
   }
 
+  // profile id of the q-th initial mean (the order of init_column's sums)
+  __device__ __forceinline__ static int ids9(int q) {
+    switch (q) {
+      case 0: return P_U0;
+      case 1: return P_V0;
+      case 2: return P_T0;
+      case 3: return P_T00;
+      case 4: return P_TABS0;
+      case 5: return P_Q0;
+      case 6: return P_QV0;
+      case 7: return P_QN0;
+      default: return P_QP0;
+    }
+  }
+
   // ---------------------------------------------------------- init
   // crm_module.F90:320-681
   __device__ void init_column() {
@@ -699,8 +714,22 @@ struct ColumnKernel : NxDim<NX> {
     F2<T> t = TT(), qcl = QCL(), qci = QCI(), qpl = QPL(), qpi = QPI(), qv = QV();
     for (int e = TID; e < nx * nzm; e += NT) {
       int i = 1 + e % nx, k = 1 + e / nx;
-      t(i, k) = tabs(i, k) + PR(P_GAMAZ)[k] - (T)C_FAC_COND * qcl(i, k) - (T)C_FAC_SUB * qci(i, k) -
-                (T)C_FAC_COND * qpl(i, k) - (T)C_FAC_SUB * qpi(i, k);
+      if constexpr (sizeof(T) == 8) {
+        t(i, k) = tabs(i, k) + PR(P_GAMAZ)[k] - (T)C_FAC_COND * qcl(i, k) - (T)C_FAC_SUB * qci(i, k) -
+                  (T)C_FAC_COND * qpl(i, k) - (T)C_FAC_SUB * qpi(i, k);
+      } else {
+        // FP32-mixed form: t and qt start from the FP64 state with the
+        // rounding of their FP32 values in the residue planes, so the
+        // carried (value + residue) pairs hold the input state to ~1e-12
+        const size_t o = S4(i, k);
+        const double td = p.st[3][o] + (double)PR(P_GAMAZ)[k] - C_FAC_COND * (double)qcl(i, k) -
+                          C_FAC_SUB * (double)qci(i, k) - C_FAC_COND * (double)qpl(i, k) -
+                          C_FAC_SUB * (double)qpi(i, k);
+        const T tf = (T)td;
+        t(i, k) = tf;
+        rct()[e] = (T)(td - (double)tf);
+        rcq()[e] = (T)(p.st[4][o] - (double)qt(i, k));
+      }
     }
     SYNC;
     // initial domain means (crm_module.F90:500-546)
@@ -730,6 +759,40 @@ struct ColumnKernel : NxDim<NX> {
                  });
     }
     SYNC;
+    if constexpr (sizeof(T) == 4) {
+      // FP32-mixed form: the means of t (t0, t00) and of the total water (q0,
+      // qv0) from the values plus their residues, in FP64: the nudging
+      // tendencies below and setperturb's rescaling aim at these means, and
+      // an FP32 mean would shift every cell of a level by its rounding
+      const int lane = TID & 31, warp = TID >> 5, nw = NT >> 5;
+      for (int k = 1 + warp; k <= nzm; k += nw) {
+        double st = 0., st0 = 0., sq = 0., sv = 0.;
+        for (int i = 1 + lane; i <= nx; i += 32) {
+          const size_t e = (size_t)(i - 1) + (size_t)nx * (k - 1);
+          const double tt = (double)t(i, k) + (double)rct()[e];
+          const double rq = (double)rcq()[e];
+          st = st + tt;
+          st0 = st0 + (tt + (C_FAC_COND * (double)qpl(i, k) + C_FAC_SUB * (double)qpi(i, k)));
+          sq = sq + (((double)qv(i, k) + rq) + ((double)qcl(i, k) + (double)qci(i, k)));
+          sv = sv + ((double)qv(i, k) + rq);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+          st = st + __shfl_xor_sync(0xffffffffu, st, o);
+          st0 = st0 + __shfl_xor_sync(0xffffffffu, st0, o);
+          sq = sq + __shfl_xor_sync(0xffffffffu, sq, o);
+          sv = sv + __shfl_xor_sync(0xffffffffu, sv, o);
+        }
+        if (lane == 0) {
+          const double m[4] = {st * factor_xy, st0 * factor_xy, sq * factor_xy, sv * factor_xy};
+          const int q[4] = {2, 3, 5, 6};
+          for (int a = 0; a < 4; ++a) {
+            md[(size_t)q[a] * (nz + 2) + k] = m[a];
+            PR(ids9(q[a]))[k] = (T)m[a];
+          }
+        }
+      }
+      SYNC;
+    }
     for (int k = TID + 1; k <= nzm; k += NT) {
       double u0 = md[k], v0 = md[(nz + 2) + k], t00 = md[3 * (nz + 2) + k];
       double q0 = md[5 * (nz + 2) + k];
@@ -766,12 +829,29 @@ struct ColumnKernel : NxDim<NX> {
         double scaling = (double)(5 + 1 - k) / (double)5;
         double t02 = 0.0;
         const double *r = p.rnd + ((size_t)icrm * 5 + (k - 1)) * nx;
-        for (int i = 1; i <= nx; ++i) {
-          t(i, k) = t(i, k) + (T)(1.0 * r[i - 1] * scaling);
-          t02 = t02 + (double)t(i, k) * fxy;
+        if constexpr (sizeof(T) == 8) {
+          for (int i = 1; i <= nx; ++i) {
+            t(i, k) = t(i, k) + (T)(1.0 * r[i - 1] * scaling);
+            t02 = t02 + (double)t(i, k) * fxy;
+          }
+          T t0k = PR(P_T0)[k];
+          for (int i = 1; i <= nx; ++i) t(i, k) = (T)((double)(t(i, k) * t0k) / t02);
+        } else {
+          // FP32-mixed form: the perturbed t and its rescaling to the level
+          // mean t0 in FP64 on the (value + residue) pairs
+          T *rt = rct() + (size_t)nx * (k - 1);
+          for (int i = 1; i <= nx; ++i) {
+            const double tt = ((double)t(i, k) + (double)rt[i - 1]) + 1.0 * r[i - 1] * scaling;
+            t02 = t02 + tt * fxy;
+          }
+          const double t0k = md[2 * (nz + 2) + k];
+          for (int i = 1; i <= nx; ++i) {
+            const double tt = (((double)t(i, k) + (double)rt[i - 1]) + 1.0 * r[i - 1] * scaling) * t0k / t02;
+            const T tf = (T)tt;
+            t(i, k) = tf;
+            rt[i - 1] = (T)(tt - (double)tf);
+          }
         }
-        T t0k = PR(P_T0)[k];
-        for (int i = 1; i <= nx; ++i) t(i, k) = (T)((double)(t(i, k) * t0k) / t02);
       }
       SYNC;
     }
