@@ -1,7 +1,8 @@
 """Build libcrm_gb300.so (sm_103a) in-tree with nvcc.
 
 Objects, compiled in parallel:
-  crm_columns.cu  the column kernel, once per (precision, launch shape):
+  crm_columns.cu  the column kernel, once per (precision, nx, launch shape)
+                  and for the 3D CRM once per (precision, launch shape):
                   FP64 with -fmad=false (bit-identical to a CPU run of the
                   same algorithm), and the FP32-mixed form
   crm_prep.cu     per-column set-up kernel (z0, setperturb draws), -fmad=false
@@ -39,6 +40,14 @@ for _n in NX_BUILT:
         # parts of the form are unaffected by these flags
         UNITS['crm_fp32_nx%d_s%d' % (_n, _s)] = ('crm_columns', ['-DCRM_INST_T=float', '-prec-div=false',
                                                                  '-prec-sqrt=false', '-ftz=true'] + _d)
+# 3D CRM: the generic kernel (nx, ny from the layout), launch shapes without
+# shared-memory scratch planes only
+SHAPES_3D = (0, 1, 3, 4)
+for _s in SHAPES_3D:
+    _d = ['-DCRM_INST_NX=0', '-DCRM_INST_NY=0', '-DCRM_INST_SHAPE=%d' % _s]
+    UNITS['crm_fp64_3d_s%d' % _s] = ('crm_columns', ['-fmad=false', '-DCRM_INST_T=double'] + _d)
+    UNITS['crm_fp32_3d_s%d' % _s] = ('crm_columns', ['-DCRM_INST_T=float', '-prec-div=false',
+                                                     '-prec-sqrt=false', '-ftz=true'] + _d)
 
 
 def _nvcc():

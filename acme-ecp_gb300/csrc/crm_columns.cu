@@ -5,7 +5,8 @@
 //   -DCRM_INST_T=float  -DCRM_INST_SHAPE=s   FP32-mixed form: fields and bulk
 //       arithmetic in FP32; the pressure tridiagonal solve, the conservation
 //       sums and the saturation-adjustment Newton iteration in FP64;
-// -DCRM_INST_NX=n: the compile-time horizontal size (0: generic).
+// -DCRM_INST_NX=n: the compile-time horizontal size (0: generic);
+// -DCRM_INST_NY=m: 1 (default) the 2D CRM, 0 the generic 3D CRM.
 // The build compiles this file once per (precision, nx, launch shape), in
 // parallel.
 #include "crm_kernel.cuh"
@@ -14,7 +15,12 @@
 #error "define CRM_INST_T, CRM_INST_NX and CRM_INST_SHAPE"
 #endif
 
+#ifndef CRM_INST_NY
+#define CRM_INST_NY 1
+#endif
+
 namespace crm {
-template void launch_crm_columns<CRM_INST_T, CRM_INST_NX, CRM_INST_SHAPE>(const KParams &, int, cudaStream_t, bool);
-template int occupancy_crm_columns<CRM_INST_T, CRM_INST_NX, CRM_INST_SHAPE>(int, int);
+template void launch_crm_columns<CRM_INST_T, CRM_INST_NX, CRM_INST_NY, CRM_INST_SHAPE>(const KParams &, int, cudaStream_t,
+                                                                                       bool);
+template int occupancy_crm_columns<CRM_INST_T, CRM_INST_NX, CRM_INST_NY, CRM_INST_SHAPE>(int, int, int);
 }  // namespace crm

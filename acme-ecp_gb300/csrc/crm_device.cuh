@@ -91,10 +91,26 @@ template <typename T> __device__ __forceinline__ T dtqsatw(T t, T p) { return ((
 template <typename T> __device__ __forceinline__ T dtqsati(T t, T p) { return ((T)R4(0.622) * dtesati(t)) / p; }
 
 // ------------------------------------------------------------ accessors
-template <typename T> struct F2 {     // (i, k) view of a slab field
+// (i, k) view of a slab field of the 2D CRM (Y3 = false); a 3D CRM field
+// (Y3 = true) is stored level by level, each level nya rows of nxa, and is
+// addressed either as (i, j, k) or, by the phases that never look at a
+// horizontal neighbour, as (h, k) with h = i + nx (j - 1) the interior cell
+// index 1..nx*ny (nx a power of two: lnx = log2 nx).
+template <typename T, bool Y3 = false> struct F2 {
   T *p;
   int x1, nxa, z1;
-  __device__ __forceinline__ T &operator()(int i, int k) const { return p[(k - z1) * nxa + (i - x1)]; }
+  int y1, plane, lnx;                 // 3D only
+  __device__ __forceinline__ T &operator()(int h, int k) const {
+    if constexpr (!Y3) {
+      return p[(k - z1) * nxa + (h - x1)];
+    } else {
+      const int hh = h - 1, i = (hh & ((1 << lnx) - 1)) + 1, j = (hh >> lnx) + 1;
+      return p[(size_t)(k - z1) * plane + (j - y1) * nxa + (i - x1)];
+    }
+  }
+  __device__ __forceinline__ T &operator()(int i, int j, int k) const {
+    return p[(size_t)(k - z1) * plane + (j - y1) * nxa + (i - x1)];
+  }
 };
 
 }  // namespace crm

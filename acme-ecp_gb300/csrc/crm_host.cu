@@ -46,15 +46,15 @@ struct crm_ctx {
   double *d_state = nullptr;     // 7 state fields
   double *d_rad = nullptr;       // qrad + 5 outputs
   double *d_out = nullptr;       // all outputs
-  double *d_consts = nullptr;    // trigs, eign
-  double *d_colconst = nullptr;  // z0 (ncrms), rnd (ncrms * 5 * nx)
+  double *d_consts = nullptr;    // trigs, eign, trigs (float), 3D: trigs_y, trigs_y (float)
+  double *d_colconst = nullptr;  // z0 (ncrms), rnd (ncrms * 5 * nx * ny)
   int *d_status = nullptr;
   unsigned long long *d_phase = nullptr;   // per-CTA phase cycle counters
   unsigned long long *d_gsync = nullptr;   // batch-mode grid barrier + maxima
   int ld_cap = 0;
   // host-side constants
-  std::vector<double> trigs, eign;
-  int ifax[20];
+  std::vector<double> trigs, eign, trigs_y;
+  int ifax[20], ifax_y[20];
   crm::KParams mc;                // gamma functions and fall speeds (micro_consts)
   size_t device_bytes = 0;        // device memory the handle holds
   long long barrier_spins = 1ll << 24;      // grid-barrier wait limit (spins)
@@ -76,47 +76,73 @@ struct PrepParams {
 void launch_crm_prep(const PrepParams &p, cudaStream_t s);
 int launch_crm_consts(void *dst, const void *src, size_t bytes, cudaStream_t s);
 
-template <typename T, int NX>
+// 3D builds no shapes with shared-memory scratch planes (its planes do not
+// fit): shapes 2 and 5 are never chosen there (occupancy 0)
+template <typename T, int NX, int NY>
 static void launch_tn(int shape, const KParams &p, int grid, cudaStream_t s, bool coop) {
+  if constexpr (NY != 1) {
+    switch (shape) {
+      case 0: launch_crm_columns<T, NX, NY, 0>(p, grid, s, coop); break;
+      case 1: launch_crm_columns<T, NX, NY, 1>(p, grid, s, coop); break;
+      case 4: launch_crm_columns<T, NX, NY, 4>(p, grid, s, coop); break;
+      default: launch_crm_columns<T, NX, NY, 3>(p, grid, s, coop); break;
+    }
+    return;
+  }
   switch (shape) {
-    case 0: launch_crm_columns<T, NX, 0>(p, grid, s, coop); break;
-    case 1: launch_crm_columns<T, NX, 1>(p, grid, s, coop); break;
-    case 2: launch_crm_columns<T, NX, 2>(p, grid, s, coop); break;
-    case 3: launch_crm_columns<T, NX, 3>(p, grid, s, coop); break;
-    case 4: launch_crm_columns<T, NX, 4>(p, grid, s, coop); break;
-    default: launch_crm_columns<T, NX, 5>(p, grid, s, coop); break;
+    case 0: launch_crm_columns<T, NX, NY, 0>(p, grid, s, coop); break;
+    case 1: launch_crm_columns<T, NX, NY, 1>(p, grid, s, coop); break;
+    case 2: launch_crm_columns<T, NX, NY, 2>(p, grid, s, coop); break;
+    case 3: launch_crm_columns<T, NX, NY, 3>(p, grid, s, coop); break;
+    case 4: launch_crm_columns<T, NX, NY, 4>(p, grid, s, coop); break;
+    default: launch_crm_columns<T, NX, NY, 5>(p, grid, s, coop); break;
   }
 }
 
-template <typename T, int NX>
-static int occupancy_tn(int shape, int nx, int nzm) {
+template <typename T, int NX, int NY>
+static int occupancy_tn(int shape, int nx, int ny, int nzm) {
+  if constexpr (NY != 1) {
+    switch (shape) {
+      case 0: return occupancy_crm_columns<T, NX, NY, 0>(nx, ny, nzm);
+      case 1: return occupancy_crm_columns<T, NX, NY, 1>(nx, ny, nzm);
+      case 3: return occupancy_crm_columns<T, NX, NY, 3>(nx, ny, nzm);
+      case 4: return occupancy_crm_columns<T, NX, NY, 4>(nx, ny, nzm);
+      default: return 0;
+    }
+  }
   switch (shape) {
-    case 0: return occupancy_crm_columns<T, NX, 0>(nx, nzm);
-    case 1: return occupancy_crm_columns<T, NX, 1>(nx, nzm);
-    case 2: return occupancy_crm_columns<T, NX, 2>(nx, nzm);
-    case 3: return occupancy_crm_columns<T, NX, 3>(nx, nzm);
-    case 4: return occupancy_crm_columns<T, NX, 4>(nx, nzm);
-    default: return occupancy_crm_columns<T, NX, 5>(nx, nzm);
+    case 0: return occupancy_crm_columns<T, NX, NY, 0>(nx, ny, nzm);
+    case 1: return occupancy_crm_columns<T, NX, NY, 1>(nx, ny, nzm);
+    case 2: return occupancy_crm_columns<T, NX, NY, 2>(nx, ny, nzm);
+    case 3: return occupancy_crm_columns<T, NX, NY, 3>(nx, ny, nzm);
+    case 4: return occupancy_crm_columns<T, NX, NY, 4>(nx, ny, nzm);
+    default: return occupancy_crm_columns<T, NX, NY, 5>(nx, ny, nzm);
   }
 }
 
+// 2D: a kernel specialised on nx where one is built; 3D: the generic kernel
 template <typename T>
 static void launch_t(int shape, const KParams &p, int grid, cudaStream_t s, bool coop) {
+  if (p.L.ny > 1) {
+    launch_tn<T, 0, 0>(shape, p, grid, s, coop);
+    return;
+  }
   switch (p.L.nx) {
-    case 32: launch_tn<T, 32>(shape, p, grid, s, coop); break;
-    case 64: launch_tn<T, 64>(shape, p, grid, s, coop); break;
-    case 128: launch_tn<T, 128>(shape, p, grid, s, coop); break;
-    default: launch_tn<T, 0>(shape, p, grid, s, coop); break;
+    case 32: launch_tn<T, 32, 1>(shape, p, grid, s, coop); break;
+    case 64: launch_tn<T, 64, 1>(shape, p, grid, s, coop); break;
+    case 128: launch_tn<T, 128, 1>(shape, p, grid, s, coop); break;
+    default: launch_tn<T, 0, 1>(shape, p, grid, s, coop); break;
   }
 }
 
 template <typename T>
-static int occupancy_t(int shape, int nx, int nzm) {
+static int occupancy_t(int shape, int nx, int nzm, int ny) {
+  if (ny > 1) return occupancy_tn<T, 0, 0>(shape, nx, ny, nzm);
   switch (nx) {
-    case 32: return occupancy_tn<T, 32>(shape, nx, nzm);
-    case 64: return occupancy_tn<T, 64>(shape, nx, nzm);
-    case 128: return occupancy_tn<T, 128>(shape, nx, nzm);
-    default: return occupancy_tn<T, 0>(shape, nx, nzm);
+    case 32: return occupancy_tn<T, 32, 1>(shape, nx, 1, nzm);
+    case 64: return occupancy_tn<T, 64, 1>(shape, nx, 1, nzm);
+    case 128: return occupancy_tn<T, 128, 1>(shape, nx, 1, nzm);
+    default: return occupancy_tn<T, 0, 1>(shape, nx, 1, nzm);
   }
 }
 
@@ -125,8 +151,8 @@ void launch_columns(int precision, int shape, const KParams &p, int grid, cudaSt
   else launch_t<float>(shape, p, grid, s, coop);
 }
 
-int occupancy_columns(int precision, int shape, int nx, int nzm) {
-  return precision == CRM_FP64 ? occupancy_t<double>(shape, nx, nzm) : occupancy_t<float>(shape, nx, nzm);
+int occupancy_columns(int precision, int shape, int nx, int nzm, int ny) {
+  return precision == CRM_FP64 ? occupancy_t<double>(shape, nx, nzm, ny) : occupancy_t<float>(shape, nx, nzm, ny);
 }
 }  // namespace crm
 
@@ -198,12 +224,14 @@ size_t out_elems(const crm_config &c, int f, int ld) {
 
 // Launch shape of the column kernel per precision (crm_kernel.h kShapes),
 // chosen by measurement on GB300; CRM_GB300_SHAPE=<index> overrides it.
-int default_shape(int precision, int nx) {
+int default_shape(int precision, int nx, int ny = 1) {
   const char *e = getenv("CRM_GB300_SHAPE");
   if (e && *e) {
     int v = atoi(e);
     if (v >= 0 && v < crm::kNumShapes) return v;
   }
+  // 3D (nx x ny cells per level): 512 threads at 2 CTAs/SM
+  if (ny > 1) return 3;
   // measured on 1024 columns of nx x 58, 30 steps (column-steps/s):
   //   FP64: 256 threads at 3 CTAs/SM (105K at nx 64; the other shapes are
   //     4-15 % slower);
@@ -224,41 +252,72 @@ int accel_nstop(const crm_config &g, int nstop) {
   return (int)((double)nstop / (1 + g.crm_accel_factor));
 }
 
+// A transform length the device FFT takes: fax_crm factors 2 and 4 only
+// (vpass_warp), at most 7 of them.
+int check_fft_size(int n) {
+  int f[20];
+  fft_factors(f, n);
+  if (f[0] < 1) return CRM_ERR_ARG;
+  for (int k = 1; k <= f[0]; ++k)
+    if (f[k] != 2 && f[k] != 4) return CRM_ERR_UNSUPPORTED;
+  if (f[0] > 7) return CRM_ERR_ARG;
+  return CRM_OK;
+}
+
+// The y spacing: crm_dy where a 3D configuration gives one, else crm_dx (the
+// reference's grid takes dy = dx)
+double crm_dy_of(const crm_config &g) { return g.crm_ny > 1 && g.crm_dy > 0 ? g.crm_dy : g.crm_dx; }
+
 int validate(const crm_config *c) {
   if (!c) return CRM_ERR_ARG;
-  if (c->crm_ny != 1) return CRM_ERR_UNSUPPORTED;          // 3D not built
+  if (c->crm_ny < 1) return CRM_ERR_ARG;
   if (c->microphysics != CRM_MICRO_SAM1MOM) return CRM_ERR_UNSUPPORTED;
   if (c->batch_mode != CRM_PER_COLUMN && c->batch_mode != CRM_REFERENCE_BATCH) return CRM_ERR_ARG;
   if (c->precision != CRM_FP64 && c->precision != CRM_FP32_MIXED) return CRM_ERR_ARG;
   if (c->crm_nx < 8 || c->crm_nx % 2 || c->crm_nz < 4 || c->plev < c->crm_nz + 2) return CRM_ERR_ARG;
-  if (c->crm_nx_rad < 1 || c->crm_nx % c->crm_nx_rad || c->crm_ny_rad != 1) return CRM_ERR_ARG;
+  if (c->crm_nx_rad < 1 || c->crm_nx % c->crm_nx_rad) return CRM_ERR_ARG;
   if (!(c->crm_dx > 0) || !(c->crm_dt > 0) || 60. < 2 * c->crm_dt) return CRM_ERR_ARG;
   if (c->max_ncrms < 1) return CRM_ERR_ARG;
-  int f[20];
-  fft_factors(f, c->crm_nx);
-  if (f[0] < 1) return CRM_ERR_ARG;
-  for (int k = 1; k <= f[0]; ++k)
-    if (f[k] != 2 && f[k] != 4) return CRM_ERR_UNSUPPORTED;  // device FFT: radix 2, 4
-  if (f[0] > 7) return CRM_ERR_ARG;
+  int rc = check_fft_size(c->crm_nx);
+  if (rc != CRM_OK) return rc;
+  if (c->crm_ny == 1) {
+    if (c->crm_ny_rad != 1) return CRM_ERR_ARG;
+  } else {
+    // 3D: ny a transform length of its own; radiation on every CRM column
+    if (c->crm_ny < 8) return CRM_ERR_ARG;
+    rc = check_fft_size(c->crm_ny);
+    if (rc != CRM_OK) return rc;
+    if (c->crm_dy < 0) return CRM_ERR_ARG;
+    if (c->crm_ny_rad < 1 || c->crm_ny % c->crm_ny_rad) return CRM_ERR_ARG;
+    if (c->crm_nx_rad != c->crm_nx || c->crm_ny_rad != c->crm_ny) return CRM_ERR_UNSUPPORTED;
+  }
   return CRM_OK;
 }
 
 // Per-configuration constants, written into caller-provided storage so that
 // the handle (alloc_ctx) and the no-allocation entry build the same values:
-//   trigs: 3 nx / 2 + 2 + nx REAL*4 trig values (fft.F90:247-300)
-//   eign:  nx + 1 Laplacian eigenvalues (pressure.F90:172-198, 2D: jd = 0)
+//   trigs: 3 n / 2 + 2 + n REAL*4 trig values of a transform of length n
+//          (fft.F90:247-300)
+//   eign:  Laplacian eigenvalues (pressure.F90:172-198), (nx + 1) x (ny + 2)
+//          with i fastest in 3D, nx + 1 in 2D (jd = 0)
+size_t n_trigs(int n) { return 3 * (size_t)n / 2 + 2 + n; }
+size_t n_eigen(const crm_config &g) { return (size_t)(g.crm_nx + 1) * (g.crm_ny > 1 ? g.crm_ny + 2 : 1); }
 void laplace_eigen(double *eign, const crm_config &g) {
-  const int nx = g.crm_nx;
-  double dx = g.crm_dx, dy = g.crm_dx;
+  const int nx = g.crm_nx, ny = g.crm_ny;
+  double dx = g.crm_dx, dy = crm_dy_of(g);
   double ddx2 = 1.0 / (dx * dx), ddy2 = 1.0 / (dy * dy);
   double pii = 3.14159265358979323846;
-  double xnx = pii / nx, xny = pii / 1;
-  int jd = (int)(((float)1 - 0.1f) / 2.f);
-  double xj = jd, facty = 2.0;
-  for (int i = 1; i <= nx + 1; ++i) {
-    int id = (int)(((float)i - 0.1f) / 2.f);
-    double xi = id, factx = 2.0;
-    eign[i - 1] = (2.0 * cos(factx * xnx * xi) - 2.0) * ddx2 + (2.0 * cos(facty * xny * xj) - 2.0) * ddy2;
+  double xnx = pii / nx, xny = pii / ny;
+  const int nj = ny > 1 ? ny + 2 : 1;
+  for (int j = 1; j <= nj; ++j) {
+    int jd = (int)(((float)j - 0.1f) / 2.f);
+    double xj = jd, facty = 2.0;
+    for (int i = 1; i <= nx + 1; ++i) {
+      int id = (int)(((float)i - 0.1f) / 2.f);
+      double xi = id, factx = 2.0;
+      eign[(size_t)(j - 1) * (nx + 1) + (i - 1)] =
+          (2.0 * cos(factx * xnx * xi) - 2.0) * ddx2 + (2.0 * cos(facty * xny * xj) - 2.0) * ddy2;
+    }
   }
 }
 
@@ -297,10 +356,10 @@ int plan_ctx(crm_ctx *c) {
   CK(cudaGetDevice(&c->device));
   CK(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, c->device));
   const size_t esz = g.precision == CRM_FP64 ? sizeof(double) : sizeof(float);
-  c->L = crm::make_layout(g.crm_nx, g.crm_nz, g.plev, g.crm_nx_rad, (int)esz);
+  c->L = crm::make_layout(g.crm_nx, g.crm_nz, g.plev, g.crm_nx_rad, (int)esz, g.crm_ny, g.crm_ny_rad);
   c->slab_cap = 0;
   for (int s = 0; s < crm::kNumShapes; ++s) {
-    int per = crm::occupancy_columns(g.precision, s, g.crm_nx, g.crm_nz);
+    int per = crm::occupancy_columns(g.precision, s, g.crm_nx, g.crm_nz, g.crm_ny);
     int grid = per > 0 ? c->nsm * per : 0;
     if (grid > g.max_ncrms) grid = g.max_ncrms;
     c->shape_grid[s] = grid;
@@ -315,10 +374,10 @@ int plan_ctx(crm_ctx *c) {
 // buffers of crm_run come later, on its first call).
 size_t handle_bytes(const crm_ctx *c) {
   const crm_config &g = c->cfg;
-  const size_t ld = (size_t)c->ld_cap, nt = 3 * (size_t)g.crm_nx / 2 + 2 + g.crm_nx;
+  const size_t ld = (size_t)c->ld_cap, nt = n_trigs(g.crm_nx), nty = g.crm_ny > 1 ? n_trigs(g.crm_ny) : 0;
   size_t b = c->slab_bytes * (size_t)c->slab_cap;
-  b += sizeof(double) * (nt + g.crm_nx + 1 + (nt + 1) / 2);
-  b += sizeof(double) * ld * (1 + 5 * (size_t)g.crm_nx);
+  b += sizeof(double) * (nt + n_eigen(g) + (nt + 1) / 2 + nty + (nty + 1) / 2);
+  b += sizeof(double) * ld * (1 + 5 * (size_t)g.crm_nx * g.crm_ny);
   b += sizeof(int) * ld + 8 * sizeof(unsigned long long);
   return b;
 }
@@ -327,7 +386,7 @@ int alloc_ctx(crm_ctx *c) {
   const crm_config &g = c->cfg;
   int rc = plan_ctx(c);
   if (rc != CRM_OK) return rc;
-  c->shape = default_shape(g.precision, g.crm_nx);
+  c->shape = default_shape(g.precision, g.crm_nx, g.crm_ny);
   {
     const char *e = getenv("CRM_GB300_SHAPE");
     if (e && *e) c->shape_auto = false;
@@ -339,14 +398,22 @@ int alloc_ctx(crm_ctx *c) {
   if (c->shape_grid[c->shape] < 1) return CRM_ERR_UNSUPPORTED;
   c->grid_max = c->shape_grid[c->shape];
   CK(cudaMalloc(&c->slabs, c->slab_bytes * (size_t)c->slab_cap));
-  const int ld = c->ld_cap, nx = g.crm_nx;
+  const int ld = c->ld_cap, nx = g.crm_nx, ny = g.crm_ny;
   fft_factors(c->ifax, nx);
   fft_trigs(c->trigs, nx);
-  c->eign.assign(nx + 1, 0.0);
+  c->eign.assign(n_eigen(g), 0.0);
   laplace_eigen(c->eign.data(), g);
-  // trigs, eign (FP64), then trigs again as float (exact: REAL*4 values)
+  c->ifax_y[0] = 0;
+  c->trigs_y.clear();
+  if (ny > 1) {
+    fft_factors(c->ifax_y, ny);
+    fft_trigs(c->trigs_y, ny);
+  }
+  // trigs, eign (FP64), trigs again as float (exact: REAL*4 values), then
+  // in 3D the y table as FP64 and as float
   const size_t nt = c->trigs.size(), ne = c->eign.size(), ntf = (nt + 1) / 2;
-  CK(cudaMalloc(&c->d_consts, sizeof(double) * (nt + ne + ntf)));
+  const size_t nty = c->trigs_y.size(), ntyf = (nty + 1) / 2;
+  CK(cudaMalloc(&c->d_consts, sizeof(double) * (nt + ne + ntf + nty + ntyf)));
   CK(cudaMemcpy(c->d_consts, c->trigs.data(), sizeof(double) * nt, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(c->d_consts + nt, c->eign.data(), sizeof(double) * ne, cudaMemcpyHostToDevice));
   {
@@ -354,7 +421,14 @@ int alloc_ctx(crm_ctx *c) {
     for (size_t i = 0; i < nt; ++i) tf[i] = (float)c->trigs[i];
     CK(cudaMemcpy(c->d_consts + nt + ne, tf.data(), sizeof(float) * nt, cudaMemcpyHostToDevice));
   }
-  CK(cudaMalloc(&c->d_colconst, sizeof(double) * (size_t)ld * (1 + 5 * nx)));
+  if (nty) {
+    double *dy = c->d_consts + nt + ne + ntf;
+    CK(cudaMemcpy(dy, c->trigs_y.data(), sizeof(double) * nty, cudaMemcpyHostToDevice));
+    std::vector<float> tf(nty);
+    for (size_t i = 0; i < nty; ++i) tf[i] = (float)c->trigs_y[i];
+    CK(cudaMemcpy(dy + nty, tf.data(), sizeof(float) * nty, cudaMemcpyHostToDevice));
+  }
+  CK(cudaMalloc(&c->d_colconst, sizeof(double) * (size_t)ld * (1 + 5 * (size_t)nx * ny)));
   CK(cudaMalloc(&c->d_status, sizeof(int) * (size_t)ld));
   CK(cudaMalloc(&c->d_gsync, 8 * sizeof(unsigned long long)));
   CK(cudaMemset(c->d_gsync, 0, 8 * sizeof(unsigned long long)));
@@ -374,12 +448,12 @@ int alloc_ctx(crm_ctx *c) {
 int ensure_staging(crm_ctx *c) {
   if (c->d_in) return CRM_OK;
   const crm_config &g = c->cfg;
-  const int ld = c->ld_cap, plev = g.plev, nx = g.crm_nx, nz = g.crm_nz;
+  const int ld = c->ld_cap, plev = g.plev, nx = g.crm_nx, ny = g.crm_ny, nz = g.crm_nz;
   c->in_elems = (size_t)ld * (plev + 1);
   // GCM profiles, then tau00, bflxls, wndls (ld each), gcol and col_map (ld ints each)
   const size_t b_in = sizeof(double) * c->in_elems * I_NIN + sizeof(double) * 4 * ld;
-  const size_t b_st = sizeof(double) * (size_t)ld * nx * nz * 7;
-  const size_t b_rad = sizeof(double) * (size_t)ld * g.crm_nx_rad * nz * 6;
+  const size_t b_st = sizeof(double) * (size_t)ld * nx * ny * nz * 7;
+  const size_t b_rad = sizeof(double) * (size_t)ld * g.crm_nx_rad * g.crm_ny_rad * nz * 6;
   size_t no = 0;
   for (int f = 0; f < CRM_NOUT; ++f) no += out_elems(g, f, ld);
   CK(cudaMalloc(&c->d_in, b_in));
@@ -428,7 +502,7 @@ int build_params(crm_ctx *c, const crm_call_desc *d, const crm_input_c *in, crm_
   if (60. < 2 * dt) return CRM_ERR_ARG;         // damping.F90:39-42
   const int nstop_run = accel_nstop(g, nstop);   // crm_module.F90:718-720
   if (nstop_run < 1) return CRM_ERR_ARG;
-  pp.ncrms = ncrms; pp.ld = ld; pp.plev = g.plev; pp.nx = g.crm_nx; pp.igstep = d->igstep;
+  pp.ncrms = ncrms; pp.ld = ld; pp.plev = g.plev; pp.nx = g.crm_nx * g.crm_ny; pp.igstep = d->igstep;
   pp.zmid = in->zmid; pp.zint = in->zint; pp.pdel = in->pdel;
   pp.tau00 = in->tau00; pp.bflxls = in->bflxls; pp.wndls = in->wndls;
   pp.gcol = d->gcol;
@@ -442,7 +516,7 @@ int build_params(crm_ctx *c, const crm_call_desc *d, const crm_input_c *in, crm_
   p.nstop = nstop_run;
   p.use_accel = g.use_crm_accel != 0; p.accel_uv = g.crm_accel_uv != 0;
   p.accel_factor = g.crm_accel_factor;
-  p.dx = g.crm_dx; p.dy = g.crm_dx; p.dt = dt; p.dt_gl = d->dt_gl;
+  p.dx = g.crm_dx; p.dy = crm_dy_of(g); p.dt = dt; p.dt_gl = d->dt_gl;
   p.gams1 = c->mc.gams1; p.gams2 = c->mc.gams2; p.gamg1 = c->mc.gamg1; p.gamg2 = c->mc.gamg2;
   p.gamr1 = c->mc.gamr1; p.gamr2 = c->mc.gamr2;
   p.vrain = c->mc.vrain; p.vsnow = c->mc.vsnow; p.vgrau = c->mc.vgrau;
@@ -453,6 +527,12 @@ int build_params(crm_ctx *c, const crm_call_desc *d, const crm_input_c *in, crm_
   p.trigs = c->d_consts;
   p.eign = c->d_consts + c->trigs.size();
   p.trigs_f = reinterpret_cast<const float *>(c->d_consts + c->trigs.size() + c->eign.size());
+  if (!c->trigs_y.empty()) {
+    p.nfax_y = c->ifax_y[0];
+    for (int k = 0; k <= c->ifax_y[0] && k < 8; ++k) p.ifax_y[k] = c->ifax_y[k];
+    p.trigs_y = c->d_consts + c->trigs.size() + c->eign.size() + (c->trigs.size() + 1) / 2;
+    p.trigs_y_f = reinterpret_cast<const float *>(p.trigs_y + c->trigs_y.size());
+  }
   p.z0 = pp.z0;
   p.rnd = pp.rnd;
   p.zmid = in->zmid; p.zint = in->zint; p.tl = in->tl; p.ql = in->ql; p.qccl = in->qccl;
@@ -486,7 +566,7 @@ int enqueue(crm_ctx *c, const crm_call_desc *d, const crm_input_c *in, crm_state
     for (int s2 = 0; s2 < crm::kNumShapes; ++s2)
       if (c->shape_grid[s2] >= ncrms && (best < 0 || crm::kShapes[s2].threads > crm::kShapes[best].threads))
         best = s2;
-    const int dflt = default_shape(g.precision, g.crm_nx);
+    const int dflt = default_shape(g.precision, g.crm_nx, g.crm_ny);
     if (best < 0 || c->shape_grid[dflt] >= ncrms && crm::kShapes[dflt].threads >= crm::kShapes[best].threads)
       best = dflt;
     c->shape = best;
@@ -612,7 +692,7 @@ int crm_set_launch_shape(crm_ctx *ctx, int shape) {
   if (!ctx) return CRM_ERR_ARG;
   if (shape == -1) {                       // back to the per-call choice
     ctx->shape_auto = true;
-    ctx->shape = default_shape(ctx->cfg.precision, ctx->cfg.crm_nx);
+    ctx->shape = default_shape(ctx->cfg.precision, ctx->cfg.crm_nx, ctx->cfg.crm_ny);
     ctx->grid_max = ctx->shape_grid[ctx->shape];
     return CRM_OK;
   }
@@ -649,7 +729,7 @@ int crm_plan_device_bytes(const crm_config *cfg, unsigned long long *bytes) {
   return CRM_OK;
 }
 
-const char *crm_version(void) { return "crm-gb300 0.1 (sm_103a; 2D sam1mom; fp64 plain + fp32 mixed)"; }
+const char *crm_version(void) { return "crm-gb300 0.2 (sm_103a; 2D and 3D sam1mom; fp64 plain + fp32 mixed)"; }
 
 int crm_run_device(crm_ctx *c, const crm_call_desc *d, const crm_input_c *in, crm_state_c *st, crm_rad_c *rad,
                    crm_output_c *out, int *col_status, void *stream) {
@@ -662,7 +742,7 @@ int crm_run(crm_ctx *c, const crm_call_desc *d, const crm_input_c *in, crm_state
             crm_output_c *out, int *col_status) {
   if (!c || !d || !in || !st || !rad || !out) return CRM_ERR_ARG;
   const crm_config &g = c->cfg;
-  const int ncrms = d->ncrms, ld = d->ld, plev = g.plev, nx = g.crm_nx, nz = g.crm_nz;
+  const int ncrms = d->ncrms, ld = d->ld, plev = g.plev, nx = g.crm_nx, ny = g.crm_ny, nz = g.crm_nz;
   if (ncrms < 1 || ld < ncrms || ld > c->ld_cap) return CRM_ERR_ARG;
   if (!d->gcol && d->igstep <= 1) return CRM_ERR_ARG;
   {
@@ -700,7 +780,7 @@ int crm_run(crm_ctx *c, const crm_call_desc *d, const crm_input_c *in, crm_state
   dd.gcol = d->gcol ? dgcol : nullptr;
   dd.col_map = d->col_map ? dmap : nullptr;
   double *sp[7] = {st->u_wind, st->v_wind, st->w_wind, st->temperature, st->qt, st->qp, st->qn};
-  const size_t n4 = (size_t)ld * nx * nz;
+  const size_t n4 = (size_t)ld * nx * ny * nz;
   crm_state_c dst_state;
   double **ds[7] = {&dst_state.u_wind, &dst_state.v_wind, &dst_state.w_wind, &dst_state.temperature,
                     &dst_state.qt, &dst_state.qp, &dst_state.qn};
@@ -709,7 +789,7 @@ int crm_run(crm_ctx *c, const crm_call_desc *d, const crm_input_c *in, crm_state
     CK(cudaMemcpyAsync(c->d_state + f * n4, sp[f], sizeof(double) * n4, cudaMemcpyHostToDevice, s));
     *ds[f] = c->d_state + f * n4;
   }
-  const size_t nr = (size_t)ld * g.crm_nx_rad * nz;
+  const size_t nr = (size_t)ld * g.crm_nx_rad * g.crm_ny_rad * nz;
   if (!rad->qrad) return CRM_ERR_ARG;
   CK(cudaMemcpyAsync(c->d_rad, rad->qrad, sizeof(double) * nr, cudaMemcpyHostToDevice, s));
   crm_rad_c drad;
@@ -848,6 +928,7 @@ extern "C" int crm_run_device_noalloc(const crm_config *cfg, const crm_call_desc
   g.max_ncrms = 1;   // no handle: the column count is bounded by the scratch only
   int rc = validate(&g);
   if (rc != CRM_OK) return rc;
+  if (g.crm_ny > 1) return CRM_ERR_UNSUPPORTED;   // 2D only: the fixed tables hold one transform
   if (!d || d->ncrms < 1 || d->ld < d->ncrms || !(d->dt_gl > 0) || d->col_map) return CRM_ERR_ARG;
   if (g.batch_mode != CRM_PER_COLUMN) return CRM_ERR_UNSUPPORTED;
   const int ncrms = d->ncrms, nx = g.crm_nx;

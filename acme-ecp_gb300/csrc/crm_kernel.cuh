@@ -121,9 +121,36 @@ template <> struct NxDim<0> {
   __device__ explicit NxDim(int n) : nx(n) {}
 };
 
-template <typename T, int NX>
-struct ColumnKernel : NxDim<NX> {
+// The CRM's y size: 1 for the 2D CRM (compile-time, so the 2D kernel is the
+// same code as without a y dimension), a compile-time size or 0 (run time)
+// for the 3D CRM.
+template <int NY> struct NyDim {
+  static constexpr int ny = NY;
+  __device__ explicit NyDim(int) {}
+};
+template <> struct NyDim<0> {
+  const int ny;
+  __device__ explicit NyDim(int n) : ny(n) {}
+};
+
+template <typename T, int NX, int NY = 1>
+struct ColumnKernel : NxDim<NX>, NyDim<NY> {
   using NxDim<NX>::nx;
+  using NyDim<NY>::ny;
+  static constexpr bool Y3 = NY != 1;
+  using FT = F2<T, Y3>;
+  // horizontal cells of the column: phases that never look at a horizontal
+  // neighbour run over h = 1..NH() (the (h, k) accessor decodes h in 3D)
+  __device__ __forceinline__ int NH() const {
+    if constexpr (Y3) return nx * ny;
+    else return nx;
+  }
+  // radiation columns (crm_nx_rad x crm_ny_rad; the 3D form has one per CRM
+  // column, so the group of cell h is h there)
+  __device__ __forceinline__ int NR() const {
+    if constexpr (Y3) return p.L.nx_rad * p.L.ny_rad;
+    else return p.L.nx_rad;
+  }
   const KParams &p;
   ColShared &S;
   T *base;
@@ -131,46 +158,55 @@ struct ColumnKernel : NxDim<NX> {
   int icrm;   // slot of the column in the (ld, ...) arrays
   int cpos;   // position of the column in the call (status index)
   T *spl;     // scratch planes A, B in shared memory, or null (slab planes)
+  int fdir = 0;  // direction of the transform in progress (3D: 1 is y)
 
   __device__ ColumnKernel(const KParams &p_, ColShared &s_, T *b, int col, T *planes = nullptr)
-      : NxDim<NX>(p_.L.nx), p(p_), S(s_), base(b), nzm(p_.L.nzm), nz(p_.L.nz), plev(p_.L.plev),
+      : NxDim<NX>(p_.L.nx), NyDim<NY>(p_.L.ny), p(p_), S(s_), base(b), nzm(p_.L.nzm), nz(p_.L.nz), plev(p_.L.plev),
         icrm(p_.col_map ? p_.col_map[col] : col), cpos(col), spl(planes) {}
 
   // ---------------------------------------------------------- accessors
   // x extents of the field classes (first index, row length = nx + extra):
   // the halo widths of crm/grid.F90:31-46 with NADV = NADVS = 0, as laid
   // out by make_layout (crm_layout.h)
-  __device__ __forceinline__ F2<T> fld(size_t off, int x1, int extra, int z1 = 1) const {
-    return F2<T>{base + off, x1, nx + extra, z1};
+  // y extents come from the layout (3D) and are {1, 1} in 2D
+  __device__ __forceinline__ FT fld(size_t off, int x1, int extra, XRange y, int z1 = 1) const {
+    if constexpr (Y3) return FT{base + off, x1, nx + extra, z1, y.x1, (nx + extra) * y.nxa, p.L.lnx};
+    else return FT{base + off, x1, nx + extra, z1, 1, nx + extra, 0};
   }
-  __device__ __forceinline__ F2<T> U() const { return fld(p.L.u, -1, 5); }
-  __device__ __forceinline__ F2<T> V() const { return fld(p.L.v, -1, 4); }
-  __device__ __forceinline__ F2<T> W() const { return fld(p.L.w, -1, 4); }
-  __device__ __forceinline__ F2<T> TT() const { return fld(p.L.t, -2, 6); }
-  __device__ __forceinline__ F2<T> QT() const { return fld(p.L.qt, -2, 6); }
-  __device__ __forceinline__ F2<T> QP() const { return fld(p.L.qp, -2, 6); }
-  __device__ __forceinline__ F2<T> TKE() const { return fld(p.L.tke, 1, 0); }
-  __device__ __forceinline__ F2<T> TK() const { return fld(p.L.tk, 0, 2); }
-  __device__ __forceinline__ F2<T> TKH() const { return fld(p.L.tkh, 0, 2); }
-  __device__ __forceinline__ F2<T> PP() const { return fld(p.L.p, 0, 1); }
-  __device__ __forceinline__ F2<T> TABS() const { return fld(p.L.tabs, 1, 0); }
-  __device__ __forceinline__ F2<T> QV() const { return fld(p.L.qv, 1, 0); }
-  __device__ __forceinline__ F2<T> QCL() const { return fld(p.L.qcl, 1, 0); }
-  __device__ __forceinline__ F2<T> QCI() const { return fld(p.L.qci, 1, 0); }
-  __device__ __forceinline__ F2<T> QPL() const { return fld(p.L.qpl, 1, 0); }
-  __device__ __forceinline__ F2<T> QPI() const { return fld(p.L.qpi, 1, 0); }
-  __device__ __forceinline__ F2<T> QN() const { return fld(p.L.qn, 1, 0); }
-  __device__ __forceinline__ F2<T> DU(int l) const { return fld(p.L.du[l - 1], 1, 1); }
-  __device__ __forceinline__ F2<T> DV(int l) const { return fld(p.L.dv[l - 1], 1, 0); }
-  __device__ __forceinline__ F2<T> DW(int l) const { return fld(p.L.dw[l - 1], 1, 0); }
-  // scratch planes (x from -2, k from 0); A and B (contiguous: A may be
-  // used as one double-length area) live in shared memory when the launch
-  // shape provides them
-  __device__ __forceinline__ F2<T> SCR(size_t off) const { return F2<T>{base + off, -2, nx + 6, 0}; }
+  __device__ __forceinline__ FT U() const { return fld(p.L.u, -1, 5, p.L.yu); }
+  __device__ __forceinline__ FT V() const { return fld(p.L.v, -1, 4, p.L.yv); }
+  __device__ __forceinline__ FT W() const { return fld(p.L.w, -1, 4, p.L.yw); }
+  __device__ __forceinline__ FT TT() const { return fld(p.L.t, -2, 6, p.L.ys); }
+  __device__ __forceinline__ FT QT() const { return fld(p.L.qt, -2, 6, p.L.ys); }
+  __device__ __forceinline__ FT QP() const { return fld(p.L.qp, -2, 6, p.L.ys); }
+  __device__ __forceinline__ FT TKE() const { return fld(p.L.tke, 1, 0, p.L.yi); }
+  __device__ __forceinline__ FT TK() const { return fld(p.L.tk, 0, 2, p.L.yd); }
+  __device__ __forceinline__ FT TKH() const { return fld(p.L.tkh, 0, 2, p.L.yd); }
+  __device__ __forceinline__ FT PP() const { return fld(p.L.p, 0, 1, p.L.yp); }
+  __device__ __forceinline__ FT TABS() const { return fld(p.L.tabs, 1, 0, p.L.yi); }
+  __device__ __forceinline__ FT QV() const { return fld(p.L.qv, 1, 0, p.L.yi); }
+  __device__ __forceinline__ FT QCL() const { return fld(p.L.qcl, 1, 0, p.L.yi); }
+  __device__ __forceinline__ FT QCI() const { return fld(p.L.qci, 1, 0, p.L.yi); }
+  __device__ __forceinline__ FT QPL() const { return fld(p.L.qpl, 1, 0, p.L.yi); }
+  __device__ __forceinline__ FT QPI() const { return fld(p.L.qpi, 1, 0, p.L.yi); }
+  __device__ __forceinline__ FT QN() const { return fld(p.L.qn, 1, 0, p.L.yi); }
+  __device__ __forceinline__ FT DU(int l) const { return fld(p.L.du[l - 1], 1, 1, p.L.yi); }
+  __device__ __forceinline__ FT DV(int l) const { return fld(p.L.dv[l - 1], 1, 0, p.L.ydv); }
+  __device__ __forceinline__ FT DW(int l) const { return fld(p.L.dw[l - 1], 1, 0, p.L.yi); }
+  // scratch planes (x from -2, k from 0; 3D: y from -2); A and B
+  // (contiguous: A may be used as one double-length area) live in shared
+  // memory when the launch shape provides them (2D only)
+  __device__ __forceinline__ FT SCR(size_t off) const { return fld(off, -2, 6, p.L.ysc, 0); }
   __device__ __forceinline__ T *sa() const { return spl ? spl : base + p.L.s_a; }
   __device__ __forceinline__ T *sb() const { return spl ? spl + (p.L.s_b - p.L.s_a) : base + p.L.s_b; }
-  __device__ __forceinline__ F2<T> SA() const { return F2<T>{sa(), -2, nx + 6, 0}; }
-  __device__ __forceinline__ F2<T> SB() const { return F2<T>{sb(), -2, nx + 6, 0}; }
+  __device__ __forceinline__ FT SA() const {
+    if constexpr (Y3) return SCR(p.L.s_a);
+    else return FT{sa(), -2, nx + 6, 0, 1, nx + 6, 0};
+  }
+  __device__ __forceinline__ FT SB() const {
+    if constexpr (Y3) return SCR(p.L.s_b);
+    else return FT{sb(), -2, nx + 6, 0, 1, nx + 6, 0};
+  }
   __device__ __forceinline__ T *PR(int id) const { return base + p.L.prof + (size_t)id * (nz + 2); }
   __device__ __forceinline__ T *OP(int id) const { return base + p.L.o_plev + (size_t)id * (plev + 2); }
   __device__ __forceinline__ T &PS(int i) const { return base[p.L.precsfc + (i - 1)]; }
@@ -178,12 +214,13 @@ struct ColumnKernel : NxDim<NX> {
 
   __device__ __forceinline__ double IN(const double *a, int l) const { return a[(size_t)icrm + (size_t)p.ld * (l - 1)]; }
   __device__ __forceinline__ size_t S4(int i, int k) const {
-    return (size_t)icrm + (size_t)p.ld * ((i - 1) + (size_t)nx * (k - 1));
+    return (size_t)icrm + (size_t)p.ld * ((i - 1) + (size_t)NH() * (k - 1));
   }
 
   // ---------------------------------------------------------- reductions
   // Horizontal sums for every level k in [k0, k1] and quantity q < nq:
-  // out(q, k, s) receives s = init(q, k) + sum over i = 1..nx of term(q, i, k).
+  // out(q, k, s) receives s = init(q, k) + sum over the horizontal cells
+  // i = 1..NH() (3D: h in the reference's (j, i) loop order) of term(q, i, k).
   // FP64 form: one thread per (q, k) adding in the reference's loop order,
   // so the result is bit-identical to a sequential CPU evaluation.
   // FP32-mixed form: one warp per (q, k); each lane adds its (at most four)
@@ -197,7 +234,7 @@ struct ColumnKernel : NxDim<NX> {
       for (int e = TID; e < npairs; e += NT) {
         int q = e / nk, k = k0 + e % nk;
         double s = init(q, k);
-        for (int i = 1; i <= nx; ++i) s = s + (double)term(q, i, k);
+        for (int i = 1; i <= NH(); ++i) s = s + (double)term(q, i, k);
         out(q, k, s);
       }
     } else {
@@ -205,7 +242,7 @@ struct ColumnKernel : NxDim<NX> {
       for (int e = warp; e < npairs; e += nw) {
         int q = e / nk, k = k0 + e % nk;
         T part = (T)0;
-        for (int i = 1 + lane; i <= nx; i += 32) part = part + term(q, i, k);
+        for (int i = 1 + lane; i <= NH(); i += 32) part = part + term(q, i, k);
         part = part + __shfl_xor_sync(0xffffffffu, part, 1);
         part = part + __shfl_xor_sync(0xffffffffu, part, 2);
         double sd = (double)part;
@@ -218,7 +255,7 @@ struct ColumnKernel : NxDim<NX> {
   }
   // Horizontal sums that only feed statistics and diagnostics (no
   // conservation fixer): the FP64 form is level_sums itself; the FP32-mixed
-  // form reduces the warp entirely in FP32 (pairwise, error ~log2(nx) ulp),
+  // form reduces the warp entirely in FP32 (pairwise, error ~log2(NH()) ulp),
   // sparing the slow FP64 pipe.
   template <typename Term, typename Init, typename Out>
   __device__ void level_sums_lo(int nq, int k0, int k1, Term term, Init init, Out out) {
@@ -230,7 +267,7 @@ struct ColumnKernel : NxDim<NX> {
       for (int e = warp; e < npairs; e += nw) {
         int q = e / nk, k = k0 + e % nk;
         T part = (T)0;
-        for (int i = 1 + lane; i <= nx; i += 32) part = part + term(q, i, k);
+        for (int i = 1 + lane; i <= NH(); i += 32) part = part + term(q, i, k);
         for (int o = 1; o < 32; o <<= 1) part = part + __shfl_xor_sync(0xffffffffu, part, o);
         if (lane == 0) out(q, k, (double)((T)init(q, k) + part));
       }
@@ -252,7 +289,7 @@ struct ColumnKernel : NxDim<NX> {
         T part[NQ];
 #pragma unroll
         for (int q = 0; q < NQ; ++q) part[q] = (T)0;
-        for (int i = 1 + lane; i <= nx; i += 32) {
+        for (int i = 1 + lane; i <= NH(); i += 32) {
           T v[NQ];
           termv(i, k, v);
 #pragma unroll
@@ -287,7 +324,7 @@ struct ColumnKernel : NxDim<NX> {
         T part[NQ];
 #pragma unroll
         for (int q = 0; q < NQ; ++q) part[q] = (T)0;
-        for (int i = 1 + lane; i <= nx; i += 32) {
+        for (int i = 1 + lane; i <= NH(); i += 32) {
           T v[NQ];
           termv(i, k, v);
 #pragma unroll
@@ -326,7 +363,7 @@ struct ColumnKernel : NxDim<NX> {
     return nullptr;
   }
   __device__ __forceinline__ T *rcq() const {
-    if constexpr (sizeof(T) == 4) return base + p.L.fcomp + (size_t)nx * nzm;
+    if constexpr (sizeof(T) == 4) return base + p.L.fcomp + (size_t)NH() * nzm;
     return nullptr;
   }
 
@@ -339,7 +376,7 @@ struct ColumnKernel : NxDim<NX> {
     for (int e = warp; e < npairs; e += nw) {
       int q = e / nk, k = k0 + e % nk;
       T m = (T)0;
-      for (int i = 1 + lane; i <= nx; i += 32) m = mx2(m, term(q, i, k));
+      for (int i = 1 + lane; i <= NH(); i += 32) m = mx2(m, term(q, i, k));
       for (int o = 16; o > 0; o >>= 1) m = mx2(m, __shfl_xor_sync(0xffffffffu, m, o));
       if (lane == 0) out(q, k, m);
     }
@@ -417,7 +454,7 @@ struct ColumnKernel : NxDim<NX> {
 
   // ---------------------------------------------------------- halos
   // bound_exchange.F90:188-236 (2D): periodic copies in x only
-  __device__ void exch(F2<T> f, int k1, int k2, int i_1, int i_2) {
+  __device__ void exch(FT f, int k1, int k2, int i_1, int i_2) {
     int i1 = i_1 - 1, i2 = i_2 - 1;
     int nl = i1 + 1, nr = i2 + 1, per = nl + nr;
     int n = (k2 - k1 + 1) * per;
@@ -427,11 +464,67 @@ struct ColumnKernel : NxDim<NX> {
       else { int i = nx + 1 + (r - nl); f(i, k) = f(i - nx, k); }
     }
   }
+  // bound_exchange.F90:14-239 in 3D: every halo cell of the rectangle
+  // [1 - i_1, nx + i_2] x [1 - j_1, ny + j_2] takes the interior value it
+  // wraps to (the reference copies x halos, y halos and corners from the
+  // interior only, so the order of the copies does not matter)
+  __device__ void exch3(FT f, int k1, int k2, int i_1, int i_2, int j_1, int j_2) {
+    const int x0 = 1 - i_1, xw = nx + i_1 + i_2, y0 = 1 - j_1, ni = i_1 + i_2;
+    const int nrow = (j_1 + j_2) * xw, per = nrow + ny * ni;
+    const int n = (k2 - k1 + 1) * per;
+    for (int e = TID; e < n; e += NT) {
+      const int k = k1 + e / per, r = e % per;
+      int i, j;
+      if (r < nrow) {
+        const int jj = r / xw;
+        i = x0 + r % xw;
+        j = jj < j_1 ? y0 + jj : ny + 1 + (jj - j_1);
+      } else {
+        const int r2 = r - nrow, ii = r2 % ni;
+        j = 1 + r2 / ni;
+        i = ii < i_1 ? x0 + ii : nx + 1 + (ii - i_1);
+      }
+      const int si = i < 1 ? i + nx : (i > nx ? i - nx : i);
+      const int sj = j < 1 ? j + ny : (j > ny ? j - ny : j);
+      f(i, j, k) = f(si, sj, k);
+    }
+  }
+  __device__ void boundaries3(int flag) {     // periodic.F90:8-136, 3D
+    if (flag == 0) {
+      exch3(U(), 1, nzm, 1, 1, 1, 1);
+      exch3(V(), 1, nzm, 1, 1, 1, 1);
+      FT w = W();
+      for (int h = TID + 1; h <= NH(); h += NT) w(h, nz) = (T)0.;
+      SYNC;
+      exch3(w, 1, nz, 1, 1, 1, 1);
+      SYNC;
+      for (int e = TID; e < (nx + 2) * (ny + 2); e += NT) w(e % (nx + 2), e / (nx + 2), nz) = (T)0.;
+    } else if (flag == 2) {
+      exch3(U(), 1, nzm, 2, 3, 2, 2);
+      exch3(V(), 1, nzm, 2, 2, 2, 3);
+      exch3(W(), 1, nz, 2, 2, 2, 2);
+      exch3(TT(), 1, nzm, 3, 3, 3, 3);
+      exch3(QT(), 1, nzm, 3, 3, 3, 3);
+      exch3(QP(), 1, nzm, 3, 3, 3, 3);
+    } else if (flag == 3) {
+      exch3(TT(), 1, nzm, 1, 1, 1, 1);
+      exch3(QT(), 1, nzm, 1, 1, 1, 1);
+      exch3(QP(), 1, nzm, 1, 1, 1, 1);
+    } else if (flag == 4) {
+      exch3(TK(), 1, nzm, 1, 1, 1, 1);
+      exch3(TKH(), 1, nzm, 1, 1, 1, 1);
+    }
+    SYNC;
+  }
   __device__ void boundaries(int flag) {      // periodic.F90:8-136
+    if constexpr (Y3) {
+      boundaries3(flag);
+      return;
+    }
     if (flag == 0) {
       exch(U(), 1, nzm, 1, 1);
       exch(V(), 1, nzm, 1, 1);
-      F2<T> w = W();
+      FT w = W();
       for (int i = TID + 1; i <= nx; i += NT) w(i, nz) = (T)0.;
       SYNC;
       exch(w, 1, nz, 1, 1);
@@ -457,10 +550,10 @@ struct ColumnKernel : NxDim<NX> {
 
   // ---------------------------------------------------------- micro_diagnose
   __device__ void micro_diagnose() {          // MICRO_SAM1MOM/microphysics.F90:334-357
-    F2<T> qv = QV(), qt = QT(), qn = QN(), tabs = TABS(), qcl = QCL(), qci = QCI(), qpl = QPL(), qpi = QPI(), qp = QP();
+    FT qv = QV(), qt = QT(), qn = QN(), tabs = TABS(), qcl = QCL(), qci = QCI(), qpl = QPL(), qpi = QPI(), qp = QP();
     const T a_bg = (T)p.a_bg, a_pr = (T)p.a_pr;
-    for (int e = TID; e < nx * nzm; e += NT) {
-      int i = 1 + e % nx, k = 1 + e / nx;
+    for (int e = TID; e < NH() * nzm; e += NT) {
+      int i = 1 + e % NH(), k = 1 + e / NH();
       qv(i, k) = qt(i, k) - qn(i, k);
       T omn = mx2((T)0., mn2((T)1., (tabs(i, k) - (T)C_TBGMIN) * a_bg));
       qcl(i, k) = qn(i, k) * omn;
@@ -558,7 +651,7 @@ struct ColumnKernel : NxDim<NX> {
     {
       // crm_rad%qrad of this column, cached in the slab's sixth radiation
       // plane (the GCM array is strided by ld; the heating is read every step)
-      const int nxr = p.L.nx_rad;
+      const int nxr = NR();
       T *qr = base + p.L.rad + (size_t)5 * nxr * nzm;
       for (int e = TID; e < nxr * nzm; e += NT) {
         int ir = e % nxr, k = e / nxr;
@@ -653,24 +746,25 @@ struct ColumnKernel : NxDim<NX> {
     }
     SYNC;
     // state in (crm_module.F90:380-397) and the first-step clamp (:400-417)
-    F2<T> u = U(), v = V(), w = W(), tabs = TABS(), qt = QT(), qp = QP(), qn = QN();
+    FT u = U(), v = V(), w = W(), tabs = TABS(), qt = QT(), qp = QP(), qn = QN();
     bool clamp;
     if (p.batch_mode == CRM_REFERENCE_BATCH) {
       // the reference tests the first column of the batch only: its input
       // state is untouched until every column has passed the first barrier
-      auto U0 = [&](int i, int k) { return p.st[0][(size_t)p.ld * ((i - 1) + (size_t)nx * (k - 1))]; };
+      auto U0 = [&](int i, int k) { return p.st[0][(size_t)p.ld * ((i - 1) + (size_t)NH() * (k - 1))]; };
       clamp = (U0(1, 1) == U0(2, 1)) && (U0(3, 2) == U0(4, 2));
     } else {
       clamp = (p.st[0][S4(1, 1)] == p.st[0][S4(2, 1)]) && (p.st[0][S4(3, 2)] == p.st[0][S4(4, 2)]);
     }
     const double umax = (double)(0.5f * (float)p.dx / (float)p.dt);
-    for (int e = TID; e < nx * nzm; e += NT) {
-      int i = 1 + e % nx, k = 1 + e / nx;
+    for (int e = TID; e < NH() * nzm; e += NT) {
+      int i = 1 + e % NH(), k = 1 + e / NH();
       size_t o = S4(i, k);
-      double uu = p.st[0][o], vv = p.st[1][o] * 0.0;
+      constexpr double YD = Y3 ? 1. : 0.;      // v is zero in the 2D CRM
+      double uu = p.st[0][o], vv = p.st[1][o] * YD;
       if (clamp) {
         uu = mn2(umax, mx2(-umax, uu));
-        vv = mn2(umax, mx2(-umax, vv)) * 0.0;
+        vv = mn2(umax, mx2(-umax, vv)) * YD;
       }
       u(i, k) = (T)uu;
       v(i, k) = (T)vv;
@@ -698,6 +792,11 @@ struct ColumnKernel : NxDim<NX> {
       for (int k = TID + 1; k <= nz; k += NT) {
         if (k <= nzm) PR(P_RDXZ)[k] = rdx0 * tsqrt(dxT * PR(P_RDZ)[k]);
         PR(P_RDXW)[k] = rdx0 * tsqrt(dxT * PR(P_RDZW)[k]);
+        if constexpr (Y3) {
+          const T dyT = (T)p.dy, rdy0 = (T)1. / dyT;
+          if (k <= nzm) PR(P_RDYZ)[k] = rdy0 * tsqrt(dyT * PR(P_RDZ)[k]);
+          PR(P_RDYW)[k] = rdy0 * tsqrt(dyT * PR(P_RDZW)[k]);
+        }
         if (k <= nzm - 1) {
           PR(P_BETDZ)[k] = (T)0.5 * (bet[k + 1] + bet[k]) / dzT / adzw[k + 1];
           T cx = dxT * dxT / dtT / PR(P_GRDFX)[k];
@@ -711,9 +810,9 @@ struct ColumnKernel : NxDim<NX> {
     SYNC;
     tridiag_factor();
     // t from tabs (crm_module.F90:508-509)
-    F2<T> t = TT(), qcl = QCL(), qci = QCI(), qpl = QPL(), qpi = QPI(), qv = QV();
-    for (int e = TID; e < nx * nzm; e += NT) {
-      int i = 1 + e % nx, k = 1 + e / nx;
+    FT t = TT(), qcl = QCL(), qci = QCI(), qpl = QPL(), qpi = QPI(), qv = QV();
+    for (int e = TID; e < NH() * nzm; e += NT) {
+      int i = 1 + e % NH(), k = 1 + e / NH();
       if constexpr (sizeof(T) == 8) {
         t(i, k) = tabs(i, k) + PR(P_GAMAZ)[k] - (T)C_FAC_COND * qcl(i, k) - (T)C_FAC_SUB * qci(i, k) -
                   (T)C_FAC_COND * qpl(i, k) - (T)C_FAC_SUB * qpi(i, k);
@@ -733,7 +832,7 @@ struct ColumnKernel : NxDim<NX> {
     }
     SYNC;
     // initial domain means (crm_module.F90:500-546)
-    const double factor_xy = 1.0 / (double)nx;
+    const double factor_xy = 1.0 / (double)NH();
     const double idt_gl = 1.0 / p.dt_gl;
     double *md = reinterpret_cast<double *>(sa());   // FP64 copies of the means
     {
@@ -767,8 +866,8 @@ struct ColumnKernel : NxDim<NX> {
       const int lane = TID & 31, warp = TID >> 5, nw = NT >> 5;
       for (int k = 1 + warp; k <= nzm; k += nw) {
         double st = 0., st0 = 0., sq = 0., sv = 0.;
-        for (int i = 1 + lane; i <= nx; i += 32) {
-          const size_t e = (size_t)(i - 1) + (size_t)nx * (k - 1);
+        for (int i = 1 + lane; i <= NH(); i += 32) {
+          const size_t e = (size_t)(i - 1) + (size_t)NH() * (k - 1);
           const double tt = (double)t(i, k) + (double)rct()[e];
           const double rq = (double)rcq()[e];
           st = st + tt;
@@ -798,7 +897,7 @@ struct ColumnKernel : NxDim<NX> {
       double q0 = md[5 * (nz + 2) + k];
       int l = plev_ - k + 1;
       double uln = mn2(umax, mx2(-umax, IN(p.ul, l)));
-      double vln = mn2(umax, mx2(-umax, IN(p.vl, l))) * 0.0;
+      double vln = mn2(umax, mx2(-umax, IN(p.vl, l))) * (Y3 ? 1. : 0.);
       double tl = IN(p.tl, l), qccl = IN(p.qccl, l), qiil = IN(p.qiil, l), ql = IN(p.ql, l);
       double gamaz = (double)PR(P_GAMAZ)[k];
       PR(P_TTEND)[k] = (T)((tl + gamaz - C_FAC_COND * (qccl + qiil) - C_FAC_FUS * qiil - t00) * idt_gl);
@@ -811,7 +910,7 @@ struct ColumnKernel : NxDim<NX> {
       double cp = 0, cps = 0;
       for (int k = 1; k <= nzm; ++k) {
         double pdel = IN(p.pdel, plev_ - k + 1);
-        for (int i = 1; i <= nx; ++i) {
+        for (int i = 1; i <= NH(); ++i) {
           cp = cp + (double)(qpl(i, k) + qpi(i, k)) * pdel;
           cps = cps + (double)qpi(i, k) * pdel;
         }
@@ -824,28 +923,28 @@ struct ColumnKernel : NxDim<NX> {
     precip_init();
     // setperturb (setperturb.F90:33-80) with draws precomputed on the host
     if (p.igstep <= 1) {
-      const double fxy = 1. / (double)nx;
+      const double fxy = 1. / (double)NH();
       for (int k = TID + 1; k <= 5; k += NT) {
         double scaling = (double)(5 + 1 - k) / (double)5;
         double t02 = 0.0;
-        const double *r = p.rnd + ((size_t)icrm * 5 + (k - 1)) * nx;
+        const double *r = p.rnd + ((size_t)icrm * 5 + (k - 1)) * NH();
         if constexpr (sizeof(T) == 8) {
-          for (int i = 1; i <= nx; ++i) {
+          for (int i = 1; i <= NH(); ++i) {
             t(i, k) = t(i, k) + (T)(1.0 * r[i - 1] * scaling);
             t02 = t02 + (double)t(i, k) * fxy;
           }
           T t0k = PR(P_T0)[k];
-          for (int i = 1; i <= nx; ++i) t(i, k) = (T)((double)(t(i, k) * t0k) / t02);
+          for (int i = 1; i <= NH(); ++i) t(i, k) = (T)((double)(t(i, k) * t0k) / t02);
         } else {
           // FP32-mixed form: the perturbed t and its rescaling to the level
           // mean t0 in FP64 on the (value + residue) pairs
-          T *rt = rct() + (size_t)nx * (k - 1);
-          for (int i = 1; i <= nx; ++i) {
+          T *rt = rct() + (size_t)NH() * (k - 1);
+          for (int i = 1; i <= NH(); ++i) {
             const double tt = ((double)t(i, k) + (double)rt[i - 1]) + 1.0 * r[i - 1] * scaling;
             t02 = t02 + tt * fxy;
           }
           const double t0k = md[2 * (nz + 2) + k];
-          for (int i = 1; i <= nx; ++i) {
+          for (int i = 1; i <= NH(); ++i) {
             const double tt = (((double)t(i, k) + (double)rt[i - 1]) + 1.0 * r[i - 1] * scaling) * t0k / t02;
             const T tf = (T)tt;
             t(i, k) = tf;
@@ -860,7 +959,7 @@ struct ColumnKernel : NxDim<NX> {
   // ---------------------------------------------------------- kurant
   // kurant.F90:31-64 and kurant_sgs (SGS_TKE/sgs.F90:342-367); per column
   __device__ void kurant() {
-    F2<T> u = U(), w = W(), tkh = TKH();
+    FT u = U(), w = W(), tkh = TKH();
     T *wm = PR(P_TMP0), *uhm = PR(P_TMP1), *tkhm = PR(P_TMP2);
     // the horizontal speed of the 2D reference is sqrt(u*u + 0*(v*v)); for
     // a finite v the second term is +0 and the sum is u*u exactly, so v is
@@ -868,10 +967,20 @@ struct ColumnKernel : NxDim<NX> {
     // prognostic field feeds w (buoyancy) or u and tkh within a step, so a
     // column whose state stops being finite is caught at the next step.
     bool bad = false;
+    FT v = V();
     level_max(3, 1, nzm,
               [&](int q, int i, int k) -> T {
                 if (q == 0) { T ww = w(i, k); bad |= !isfinite(ww); return tabs_(ww); }
-                if (q == 1) { T uu = u(i, k); bad |= !isfinite(uu); return tsqrt(uu * uu); }
+                if (q == 1) {
+                  T uu = u(i, k);
+                  bad |= !isfinite(uu);
+                  if constexpr (Y3) {
+                    T vv = v(i, k);
+                    bad |= !isfinite(vv);
+                    return tsqrt(uu * uu + (T)1. * (vv * vv));
+                  }
+                  return tsqrt(uu * uu);
+                }
                 T th = tkh(i, k);
                 bad |= !isfinite(th);
                 return th;
@@ -883,12 +992,14 @@ struct ColumnKernel : NxDim<NX> {
     const double rdx = 1. / p.dx;
     for (int k = TID + 1; k <= nzm; k += NT) {
       double dza = S.dz * (double)PR(P_ADZW)[k];
-      double t1 = mx2((double)uhm[k] * p.dt * sqrt(rdx * rdx + 0. * ((1. / p.dy) * (1. / p.dy))),
+      constexpr double YD = Y3 ? 1. : 0.;
+      constexpr float YF = Y3 ? 1.f : 0.f;
+      double t1 = mx2((double)uhm[k] * p.dt * sqrt(rdx * rdx + YD * ((1. / p.dy) * (1. / p.dy))),
                       mx2((double)wm[k], (double)wm[k + 1]) * p.dt / dza);
       double tk = (double)tkhm[k];
       double t2 = mx3(0.5 * tk * (double)PR(P_GRDFZ)[k] * p.dt / (dza * dza),
                       0.5 * tk * (double)PR(P_GRDFX)[k] * p.dt / (p.dx * p.dx),
-                      (double)(0.f * 0.5f) * tk * (double)PR(P_GRDFY)[k] * p.dt / (p.dy * p.dy));
+                      (double)(YF * 0.5f) * tk * (double)PR(P_GRDFY)[k] * p.dt / (p.dy * p.dy));
       cfl = mx2(cfl, mx2(t1, t2));
     }
     cfl = block_max(cfl);
@@ -923,14 +1034,20 @@ struct ColumnKernel : NxDim<NX> {
 
   // ---------------------------------------------------------- zero, buoyancy
   __device__ void zero_and_buoyancy() {       // zero.F90:17-29, buoyancy.F90:15-37
-    F2<T> du = DU(S.na), dv = DV(S.na), dw = DW(S.na);
-    for (int e = TID; e < (nx + 1) * nzm; e += NT) { int i = 1 + e % (nx + 1), k = 1 + e / (nx + 1); du(i, k) = (T)0.; }
-    for (int e = TID; e < nx * nzm; e += NT) { int i = 1 + e % nx, k = 1 + e / nx; dv(i, k) = (T)0.; }
-    F2<T> tabs = TABS(), qv = QV(), qcl = QCL(), qci = QCI(), qpl = QPL(), qpi = QPI();
+    FT du = DU(S.na), dv = DV(S.na), dw = DW(S.na);
+    if constexpr (Y3) {                  // the whole arrays, x and y halos included
+      const size_t nu = (size_t)(nx + 1) * p.L.yi.nxa * nzm, nv = (size_t)nx * p.L.ydv.nxa * nzm;
+      for (size_t e = TID; e < nu; e += NT) du.p[e] = (T)0.;
+      for (size_t e = TID; e < nv; e += NT) dv.p[e] = (T)0.;
+    } else {
+      for (int e = TID; e < (nx + 1) * nzm; e += NT) { int i = 1 + e % (nx + 1), k = 1 + e / (nx + 1); du(i, k) = (T)0.; }
+      for (int e = TID; e < nx * nzm; e += NT) { int i = 1 + e % nx, k = 1 + e / nx; dv(i, k) = (T)0.; }
+    }
+    FT tabs = TABS(), qv = QV(), qcl = QCL(), qci = QCI(), qpl = QPL(), qpi = QPI();
     const T epsv = (T)C_EPSV;
     T *adz = PR(P_ADZ), *bet = PR(P_BET), *tabs0 = PR(P_TABS0), *qv0 = PR(P_QV0), *qn0 = PR(P_QN0), *qp0 = PR(P_QP0);
-    for (int e = TID; e < nx * nz; e += NT) {
-      int i = 1 + e % nx, k = 1 + e / nx;
+    for (int e = TID; e < NH() * nz; e += NT) {
+      int i = 1 + e % NH(), k = 1 + e / NH();
       if (k >= 2 && k <= nzm) {
         int kb = k - 1;
         T betu = PR(P_BETU)[k];
@@ -951,7 +1068,7 @@ struct ColumnKernel : NxDim<NX> {
 
   // ---------------------------------------------------------- forcing + radiation
   __device__ void forcing_radiation() {       // forcing.F90:31-74, crm_module.F90:766-777
-    F2<T> t = TT(), qt = QT(), du = DU(S.na), dv = DV(S.na);
+    FT t = TT(), qt = QT(), du = DU(S.na), dv = DV(S.na);
     const T dtn = (T)S.dtn;
     T *ttend = PR(P_TTEND), *qtend = PR(P_QTEND), *utend = PR(P_UTEND), *vtend = PR(P_VTEND);
     // The FP32-mixed form adds the steady forcing through the carried
@@ -959,8 +1076,8 @@ struct ColumnKernel : NxDim<NX> {
     // dt 10 s would be biased by up to ~5 %.  Its t forcing is added after
     // the fixer below, which does not read t.
     T *rc_t = rct(), *rc_q = rcq();
-    for (int e = TID; e < nx * nzm; e += NT) {
-      int i = 1 + e % nx, k = 1 + e / nx;
+    for (int e = TID; e < NH() * nzm; e += NT) {
+      int i = 1 + e % NH(), k = 1 + e / NH();
       if constexpr (sizeof(T) == 8) {
         t(i, k) = t(i, k) + ttend[k] * dtn;
         qt(i, k) = qt(i, k) + qtend[k] * dtn;
@@ -992,10 +1109,10 @@ struct ColumnKernel : NxDim<NX> {
                [&](int, int) { return 0.; },
                [&](int q, int k, double sv) { (q == 0 ? qneg : q == 1 ? qpoz : nneg)[k] = (T)sv; });
     SYNC;
-    const int gx = nx / p.L.nx_rad, nxr = p.L.nx_rad;
+    const int gx = NH() / NR(), nxr = NR();
     const T *qrad = base + p.L.rad + (size_t)5 * nxr * nzm;    // (nx_rad, nzm), cached at init
-    for (int e = TID; e < nx * nzm; e += NT) {
-      int i = 1 + e % nx, k = 1 + e / nx;
+    for (int e = TID; e < NH() * nzm; e += NT) {
+      int i = 1 + e % NH(), k = 1 + e / NH();
       if (nneg[k] > (T)0. && qpoz[k] + qneg[k] > (T)0.) {
         T factor = (T)1. + qneg[k] / qpoz[k];
         qt(i, k) = mx2((T)0., qt(i, k) * factor);
@@ -1022,9 +1139,9 @@ struct ColumnKernel : NxDim<NX> {
     }
     SYNC;
     const int n_damp = S.n_damp;
-    F2<T> u = U(), v = V(), t = TT();
+    FT u = U(), v = V(), t = TT();
     T *tau = PR(P_TMP0), *u0l = PR(P_TMP1), *v0l = PR(P_TMP2), *t0l = PR(P_TMP3);
-    const T nxy = (T)(double)nx;
+    const T nxy = (T)(double)NH();
     for (int k = TID + 1; k <= nzm; k += NT) {
       if (k >= nzm - n_damp) {
         T tk = (T)60. * tpow((T)450. / (T)60., (z[nzm] - z[k]) / (z[nzm] - z[nzm - n_damp]));
@@ -1045,17 +1162,17 @@ struct ColumnKernel : NxDim<NX> {
       for (int k = nzm - n_damp + warp; k <= nzm; k += nw) {
         if (k < 1) continue;
         double s = 0.;
-        for (int i = 1 + lane; i <= nx; i += 32) s = s + ((double)t(i, k) + (double)rct()[(size_t)(i - 1) + (size_t)nx * (k - 1)]);
+        for (int i = 1 + lane; i <= NH(); i += 32) s = s + ((double)t(i, k) + (double)rct()[(size_t)(i - 1) + (size_t)NH() * (k - 1)]);
         for (int o = 16; o > 0; o >>= 1) s = s + __shfl_xor_sync(0xffffffffu, s, o);
-        if (lane == 0) t0d[k] = s / (double)nx;
+        if (lane == 0) t0d[k] = s / (double)NH();
       }
     }
     SYNC;
-    F2<T> w = W(), qt = QT(), qv = QV(), du = DU(S.na), dv = DV(S.na), dw = DW(S.na);
+    FT w = W(), qt = QT(), qv = QV(), du = DU(S.na), dv = DV(S.na), dw = DW(S.na);
     const T dtn = (T)S.dtn;
     T *qv0 = PR(P_QV0);
-    for (int e = TID; e < nx * nzm; e += NT) {
-      int i = 1 + e % nx, k = 1 + e / nx;
+    for (int e = TID; e < NH() * nzm; e += NT) {
+      int i = 1 + e % NH(), k = 1 + e / NH();
       if (k >= nzm - n_damp) {
         du(i, k) = du(i, k) - (u(i, k) - u0l[k]) * tau[k];
         dv(i, k) = dv(i, k) - (v(i, k) - v0l[k]) * tau[k];
@@ -1064,7 +1181,7 @@ struct ColumnKernel : NxDim<NX> {
           t(i, k) = t(i, k) - dtn * (t(i, k) - t0l[k]) * tau[k];
           qt(i, k) = qt(i, k) - dtn * (qv(i, k) - qv0[k]) * tau[k];
         } else {
-          const size_t o = (size_t)(i - 1) + (size_t)nx * (k - 1);
+          const size_t o = (size_t)(i - 1) + (size_t)NH() * (k - 1);
           const T anom = (T)(((double)t(i, k) + (double)rct()[o]) - t0d[k]);
           t(i, k) = add_carry(t(i, k), -(dtn * anom * tau[k]), rct()[o]);
           qt(i, k) = add_carry(qt(i, k), -(dtn * (qv(i, k) - qv0[k]) * tau[k]), rcq()[o]);
@@ -1076,10 +1193,10 @@ struct ColumnKernel : NxDim<NX> {
 
   // ---------------------------------------------------------- ice_fall
   __device__ void ice_fall() {                 // ice_fall.F90:26-167
-    F2<T> qcl = QCL(), qci = QCI(), tabs = TABS();
+    FT qcl = QCL(), qci = QCI(), tabs = TABS();
     int kmin = nzm + 1, kmax = 0;
-    for (int e = TID; e < nx * nzm; e += NT) {
-      int i = 1 + e % nx, k = 1 + e / nx;
+    for (int e = TID; e < NH() * nzm; e += NT) {
+      int i = 1 + e % NH(), k = 1 + e / NH();
       if (qcl(i, k) + qci(i, k) > (T)0. && tabs(i, k) < (T)R4(273.15)) {
         kmin = min(kmin, k);
         kmax = max(kmax, k);
@@ -1099,11 +1216,11 @@ struct ColumnKernel : NxDim<NX> {
     SYNC;
     kmin = S.kmin; kmax = S.kmax;
     if (kmax == 0) return;                     // no ice cloud: nothing falls
-    F2<T> fz = SA();
+    FT fz = SA();
     T *adz = PR(P_ADZ), *rho = PR(P_RHO);
     const T dtn = (T)S.dtn, dz = (T)S.dz;
-    for (int e = TID; e < nx * nz; e += NT) {
-      int i = 1 + e % nx, k = 1 + e / nx;
+    for (int e = TID; e < NH() * nz; e += NT) {
+      int i = 1 + e % NH(), k = 1 + e / NH();
       T f = (T)0.;
       if (k >= max(1, kmin - 1) && k <= kmax) {
         int kc = min(nzm, k + 1), kb = max(1, k - 1);
@@ -1124,9 +1241,9 @@ struct ColumnKernel : NxDim<NX> {
       fz(i, k) = f;
     }
     SYNC;
-    F2<T> qt = QT(), t = TT();
-    for (int e = TID; e < nx * nzm; e += NT) {
-      int i = 1 + e % nx, k = 1 + e / nx;
+    FT qt = QT(), t = TT();
+    for (int e = TID; e < NH() * nzm; e += NT) {
+      int i = 1 + e % NH(), k = 1 + e / NH();
       if (k >= max(1, kmin - 2) && k <= kmax) {
         T coef = dtn / (dz * adz[k] * rho[k]);
         T dqi = coef * (fz(i, k) - fz(i, k + 1));
@@ -1135,7 +1252,7 @@ struct ColumnKernel : NxDim<NX> {
         t(i, k) = t(i, k) - lat_heat;
       }
     }
-    for (int i = TID + 1; i <= nx; i += NT) {
+    for (int i = TID + 1; i <= NH(); i += NT) {
       T coef = dtn / dz;
       T dqi = -coef * fz(i, 1);
       PS(i) = PS(i) + dqi;
@@ -1144,18 +1261,69 @@ struct ColumnKernel : NxDim<NX> {
     SYNC;
   }
 
+  // ---------------------------------------------------------- SGS TKE, 3D
+#define SQ(x) ((x) * (x))
+  // SGS_TKE/shear_prod3D.F90:14-138 into def2(i, j, k); the per-level
+  // factors rdx, rdy (grid anisotropy) come from the column's tables
+  __device__ void shear_prod3(FT def2) {
+    FT u = U(), v = V(), w = W();
+    T *u0 = PR(P_U0), *v0 = PR(P_V0);
+    const int nxy = nx * ny;
+    for (int e = TID; e < nxy * nzm; e += NT) {
+      const int i = 1 + e % nx, j = 1 + (e / nx) % ny, k = 1 + e / nxy;
+      const int ib = i - 1, ic = i + 1, jb = j - 1, jc = j + 1;
+      const T rdz = PR(P_RDZ)[k], rdx = PR(P_RDXZ)[k], rdy = PR(P_RDYZ)[k];
+      // horizontal shear, shared by every level branch
+      T r = (T)2. * (SQ((u(ic, j, k) - u(i, j, k)) * rdx) + SQ((v(i, jc, k) - v(i, j, k)) * rdy) +
+                     SQ((w(i, j, k + 1) - w(i, j, k)) * rdz)) +
+            (T)0.25 * (SQ((u(ic, jc, k) - u(ic, j, k)) * rdy + (v(ic, jc, k) - v(i, jc, k)) * rdx) +
+                       SQ((u(i, jc, k) - u(i, j, k)) * rdy + (v(i, jc, k) - v(ib, jc, k)) * rdx) +
+                       SQ((u(ic, j, k) - u(ic, jb, k)) * rdy + (v(ic, j, k) - v(i, j, k)) * rdx) +
+                       SQ((u(i, j, k) - u(i, jb, k)) * rdy + (v(i, j, k) - v(ib, j, k)) * rdx));
+      if (k >= 2 && k <= nzm - 1) {
+        const int kb = k - 1, kc = k + 1;
+        const T rzu = PR(P_RDZW)[kc], rzd = PR(P_RDZW)[k];
+        const T rxu = PR(P_RDXW)[kc], rxd = PR(P_RDXW)[k], ryu = PR(P_RDYW)[kc], ryd = PR(P_RDYW)[k];
+        r = r + (T)0.25 * (SQ((u(ic, j, kc) - u0[kc] - u(ic, j, k) + u0[k]) * rzu + (w(ic, j, kc) - w(i, j, kc)) * rxu) +
+                           SQ((u(i, j, kc) - u0[kc] - u(i, j, k) + u0[k]) * rzu + (w(i, j, kc) - w(ib, j, kc)) * rxu) +
+                           SQ((u(ic, j, k) - u0[k] - u(ic, j, kb) + u0[kb]) * rzd + (w(ic, j, k) - w(i, j, k)) * rxd) +
+                           SQ((u(i, j, k) - u0[k] - u(i, j, kb) + u0[kb]) * rzd + (w(i, j, k) - w(ib, j, k)) * rxd));
+        r = r + (T)0.25 * (SQ((v(i, jc, kc) - v0[kc] - v(i, jc, k) + v0[k]) * rzu + (w(i, jc, kc) - w(i, j, kc)) * ryu) +
+                           SQ((v(i, j, kc) - v0[kc] - v(i, j, k) + v0[k]) * rzu + (w(i, j, kc) - w(i, jb, kc)) * ryu) +
+                           SQ((v(i, jc, k) - v0[k] - v(i, jc, kb) + v0[kb]) * rzd + (w(i, jc, k) - w(i, j, k)) * ryd) +
+                           SQ((v(i, j, k) - v0[k] - v(i, j, kb) + v0[kb]) * rzd + (w(i, j, k) - w(i, jb, k)) * ryd));
+      } else if (k == 1) {
+        const int kc = k + 1;
+        const T rzu = PR(P_RDZW)[kc], rxu = PR(P_RDXW)[kc], ryu = PR(P_RDYW)[kc];
+        r = r + (T)0.5 * (SQ((v(i, jc, kc) - v0[kc] - v(i, jc, k) + v0[k]) * rzu + (w(i, jc, kc) - w(i, j, kc)) * ryu) +
+                          SQ((v(i, j, kc) - v0[kc] - v(i, j, k) + v0[k]) * rzu + (w(i, j, kc) - w(i, jb, kc)) * ryu));
+        r = r + (T)0.5 * (SQ((u(ic, j, kc) - u0[kc] - u(ic, j, k) + u0[k]) * rzu + (w(ic, j, kc) - w(i, j, kc)) * rxu) +
+                          SQ((u(i, j, kc) - u0[kc] - u(i, j, k) + u0[k]) * rzu + (w(i, j, kc) - w(ib, j, kc)) * rxu));
+      } else {
+        const int kb = k - 1;
+        const T rzd = PR(P_RDZW)[k], rxd = PR(P_RDXW)[k], ryd = PR(P_RDYW)[k];
+        r = r + (T)0.5 * (SQ((v(i, jc, k) - v0[k] - v(i, jc, kb) + v0[kb]) * rzd + (w(i, jc, k) - w(i, j, k)) * ryd) +
+                          SQ((v(i, j, k) - v0[k] - v(i, j, kb) + v0[kb]) * rzd + (w(i, j, k) - w(i, jb, k)) * ryd));
+        r = r + (T)0.5 * (SQ((u(ic, j, k) - u0[k] - u(ic, j, kb) + u0[kb]) * rzd + (w(ic, j, k) - w(i, j, k)) * rxd) +
+                          SQ((u(i, j, k) - u0[k] - u(i, j, kb) + u0[kb]) * rzd + (w(i, j, k) - w(ib, j, k)) * rxd));
+      }
+      def2(i, j, k) = r;
+    }
+  }
+
   // ---------------------------------------------------------- SGS TKE
   // shear_prod2D.F90:14-95 + tke_full.F90:108-312 (dosmagor = .true.)
   __device__ void tke_full() {
-    F2<T> u = U(), v = V(), w = W(), def2 = SA(), buoy = SB(), aprod = SCR(p.L.s_c);
+    FT u = U(), v = V(), w = W(), def2 = SA(), buoy = SB(), aprod = SCR(p.L.s_c);
     T *u0 = PR(P_U0), *v0 = PR(P_V0), *adz = PR(P_ADZ), *adzw = PR(P_ADZW);
     const T dz = (T)S.dz, dx = (T)p.dx;
     const T rdx0 = (T)1. / dx;
+    if constexpr (Y3) shear_prod3(def2);
+    else
     for (int e = TID; e < nx * nzm; e += NT) {
       int i = 1 + e % nx, k = 1 + e / nx;
       int ib = i - 1, ic = i + 1;
       T r;
-#define SQ(x) ((x) * (x))
       if (k >= 2 && k <= nzm - 1) {
         int kb = k - 1, kc = k + 1;
         T rdz = PR(P_RDZ)[k];
@@ -1198,7 +1366,7 @@ struct ColumnKernel : NxDim<NX> {
       def2(i, k) = r;
     }
     // SGS buoyancy flux at the interfaces k+1/2, k = 1..nzm-1
-    F2<T> tabs = TABS(), qv = QV(), qcl = QCL(), qci = QCI(), qpl = QPL(), qpi = QPI(), t = TT(), tkh = TKH();
+    FT tabs = TABS(), qv = QV(), qcl = QCL(), qci = QCI(), qpl = QPL(), qpi = QPI(), t = TT(), tkh = TKH();
     T *bet = PR(P_BET), *presi = PR(P_PRESI);
     const T epsv = (T)C_EPSV, fc = (T)C_FAC_COND, fs = (T)C_FAC_SUB, ff = (T)C_FAC_FUS;
     for (int e = TID; e < nx * (nzm + 1); e += NT) {
@@ -1237,7 +1405,7 @@ struct ColumnKernel : NxDim<NX> {
     }
     SYNC;
     // eddy viscosity / conductivity (Smagorinsky), levels 1..nzm-1
-    F2<T> tk = TK(), tke = TKE();
+    FT tk = TK(), tke = TKE();
     const T Cs = (T)R4(0.15), Ck = (T)R4(0.1);
     const T Ce = Ck * Ck * Ck / ((Cs * Cs) * (Cs * Cs));
     const T Pr = (T)1.;
@@ -1266,11 +1434,199 @@ struct ColumnKernel : NxDim<NX> {
 #undef SQ
   }
 
+  // ---------------------------------------------------------- advect_mom, 3D
+  // advect2_mom_xy.F90:23-57 (RUN3D) and advect2_mom_z.F90:30-122
+  __device__ void advect_mom3() {
+    FT u = U(), v = V(), w = W(), du = DU(S.na), dv = DV(S.na), dw = DW(S.na);
+    FT fuz = SA(), fvz = SB(), fwz = SCR(p.L.s_c);
+    T *rho = PR(P_RHO), *adz = PR(P_ADZ), *rhow = PR(P_RHOW);
+    const T dx25 = (T)0.25 / (T)p.dx, dy25 = (T)0.25 / (T)p.dy;
+    const T dz = (T)S.dz;
+    const T dz25 = (T)1. / ((T)4. * dz);
+    const int nxy = nx * ny;
+    for (int e = TID; e < nxy * nzm; e += NT) {
+      const int i = 1 + e % nx, j = 1 + (e / nx) % ny, k = 1 + e / nxy;
+      const int kc = k + 1, kcu = min(kc, nzm), ic = i + 1, ib = i - 1, jb = j - 1, jc = j + 1;
+      const T irho = PR(P_IRHOWADZW)[kc];
+      T fu1 = dx25 * (u(ic - 1, j, k) + u(i - 1, j, k)) * (u(i - 1, j, k) + u(ic - 1, j, k));
+      T fu2 = dx25 * (u(ic, j, k) + u(i, j, k)) * (u(i, j, k) + u(ic, j, k));
+      T dun = du(i, j, k) - (fu2 - fu1);
+      T fv1 = dx25 * (u(ic - 1, j, k) + u(ic - 1, jb, k)) * (v(i - 1, j, k) + v(ic - 1, j, k));
+      T fv2 = dx25 * (u(ic, j, k) + u(ic, jb, k)) * (v(i, j, k) + v(ic, j, k));
+      T dvn = dv(i, j, k) - (fv2 - fv1);
+      T fw1 = dx25 * (u(ic - 1, j, k) * rho[k] * adz[k] + u(ic - 1, j, kcu) * rho[kcu] * adz[kcu]) *
+              (w(i - 1, j, kc) + w(ic - 1, j, kc));
+      T fw2 = dx25 * (u(ic, j, k) * rho[k] * adz[k] + u(ic, j, kcu) * rho[kcu] * adz[kcu]) * (w(i, j, kc) + w(ic, j, kc));
+      T dwn = dw(i, j, kc) - irho * (fw2 - fw1);
+      fu1 = dy25 * (v(i, jc - 1, k) + v(ib, jc - 1, k)) * (u(i, j - 1, k) + u(i, jc - 1, k));
+      fu2 = dy25 * (v(i, jc, k) + v(ib, jc, k)) * (u(i, j, k) + u(i, jc, k));
+      dun = dun - (fu2 - fu1);
+      fv1 = dy25 * (v(i, jc - 1, k) + v(i, j - 1, k)) * (v(i, j - 1, k) + v(i, jc - 1, k));
+      fv2 = dy25 * (v(i, jc, k) + v(i, j, k)) * (v(i, j, k) + v(i, jc, k));
+      dvn = dvn - (fv2 - fv1);
+      fw1 = dy25 * (v(i, jc - 1, k) * rho[k] * adz[k] + v(i, jc - 1, kcu) * rho[kcu] * adz[kcu]) *
+            (w(i, j - 1, kc) + w(i, jc - 1, kc));
+      fw2 = dy25 * (v(i, jc, k) * rho[k] * adz[k] + v(i, jc, kcu) * rho[kcu] * adz[kcu]) * (w(i, j, kc) + w(i, jc, kc));
+      dwn = dwn - irho * (fw2 - fw1);
+      T fzu = (T)0., fzv = (T)0.;
+      if (k >= 2) {
+        const int kb = k - 1;
+        const T rhoi = dz25 * rhow[k];
+        fzu = rhoi * (w(i, j, k) + w(i - 1, j, k)) * (u(i, j, k) + u(i, j, kb));
+        fzv = rhoi * (w(i, j, k) + w(i, j - 1, k)) * (v(i, j, k) + v(i, j, kb));
+      }
+      du(i, j, k) = dun;
+      dv(i, j, k) = dvn;
+      dw(i, j, kc) = dwn;
+      if (k >= 2) {
+        fuz(i, j, k) = fzu;
+        fvz(i, j, k) = fzv;
+      } else {
+        fuz(i, j, 1) = (T)0.; fvz(i, j, 1) = (T)0.;
+        fuz(i, j, nz) = (T)0.; fvz(i, j, nz) = (T)0.;
+      }
+    }
+    SYNC;
+    T *uwle = PR(P_UWLE), *vwle = PR(P_VWLE);
+    if (TID == 0) { uwle[1] = (T)0.; vwle[1] = (T)0.; uwle[nz] = (T)0.; vwle[nz] = (T)0.; }
+    level_sums_lo(2, 2, nzm, [&](int q, int h, int k) -> T { return q == 0 ? fuz(h, k) : fvz(h, k); },
+               [&](int, int) { return 0.; },
+               [&](int q, int k, double sv) { (q == 0 ? uwle : vwle)[k] = (T)sv; });
+    for (int e = TID; e < nxy * nzm; e += NT) {
+      const int i = 1 + e % nx, j = 1 + (e / nx) % ny, k = 1 + e / nxy;
+      const int kc = k + 1;
+      const T rhoi = PR(P_IRHOADZ)[k];
+      du(i, j, k) = du(i, j, k) - (fuz(i, j, kc) - fuz(i, j, k)) * rhoi;
+      dv(i, j, k) = dv(i, j, k) - (fvz(i, j, kc) - fvz(i, j, k)) * rhoi;
+      fwz(i, j, k) = dz25 * (w(i, j, kc) * rhow[kc] + w(i, j, k) * rhow[k]) * (w(i, j, kc) + w(i, j, k));
+    }
+    SYNC;
+    for (int e = TID; e < nxy * (nzm - 1); e += NT) {
+      const int i = 1 + e % nx, j = 1 + (e / nx) % ny, k = 2 + e / nxy;
+      const T rhoi = PR(P_IRHOWADZW)[k];
+      dw(i, j, k) = dw(i, j, k) - (fwz(i, j, k) - fwz(i, j, k - 1)) * rhoi;
+    }
+    SYNC;
+  }
+
+  // ---------------------------------------------------------- diffuse_mom3D
+  // SGS_TKE/diffuse_mom3D.F90:40-204 (fluxbu, fluxbv, fluxtu, fluxtv are 0)
+  __device__ void diffuse_mom3() {
+    FT u = U(), v = V(), w = W(), tk = TK(), du = DU(S.na), dv = DV(S.na), dw = DW(S.na);
+    FT fu = SA(), fv = SB(), fw = SCR(p.L.s_c);
+    T *rho = PR(P_RHO), *adz = PR(P_ADZ), *rhow = PR(P_RHOW), *adzw = PR(P_ADZW);
+    T *grdfx = PR(P_GRDFX), *grdfy = PR(P_GRDFY), *grdfz = PR(P_GRDFZ);
+    const T dx = (T)p.dx, dy = (T)p.dy, dz = (T)S.dz;
+    const T rdx2 = (T)1. / (dx * dx), rdy2 = (T)1. / (dy * dy);
+    const T rdx25 = (T)0.25 * rdx2, rdy25 = (T)0.25 * rdy2;
+    const T dxy = dx / dy, dyx = dy / dx;
+    const int nxy = nx * ny;
+    // x faces i = 0..nx
+    for (int e = TID; e < (nx + 1) * ny * nzm; e += NT) {
+      const int i = e % (nx + 1), j = 1 + (e / (nx + 1)) % ny, k = 1 + e / ((nx + 1) * ny);
+      const int jb = j - 1, kc = k + 1, kcu = min(kc, nzm), ic = i + 1;
+      const T dxz = dx / (dz * adzw[kc]);
+      const T rdx21 = rdx2 * grdfx[k];
+      const T rdx251 = rdx25 * grdfx[k];
+      T tkx = rdx21 * tk(i, j, k);
+      const T fuv = (T)-2. * tkx * (u(ic, j, k) - u(i, j, k));
+      tkx = rdx251 * (tk(i, j, k) + tk(i, jb, k) + tk(ic, j, k) + tk(ic, jb, k));
+      const T fvv = -tkx * (v(ic, j, k) - v(i, j, k) + (u(ic, j, k) - u(ic, jb, k)) * dxy);
+      tkx = rdx251 * (tk(i, j, k) + tk(ic, j, k) + tk(i, j, kcu) + tk(ic, j, kcu));
+      const T fwv = -tkx * (w(ic, j, kc) - w(i, j, kc) + (u(ic, j, kcu) - u(ic, j, k)) * dxz);
+      fu(i, j, k) = fuv;
+      fv(i, j, k) = fvv;
+      fw(i, j, k) = fwv;
+    }
+    SYNC;
+    for (int e = TID; e < nxy * nzm; e += NT) {
+      const int i = 1 + e % nx, j = 1 + (e / nx) % ny, k = 1 + e / nxy;
+      const int kc = k + 1, ib = i - 1;
+      du(i, j, k) = du(i, j, k) - (fu(i, j, k) - fu(ib, j, k));
+      dv(i, j, k) = dv(i, j, k) - (fv(i, j, k) - fv(ib, j, k));
+      dw(i, j, kc) = dw(i, j, kc) - (fw(i, j, k) - fw(ib, j, k));
+    }
+    SYNC;
+    // y faces j = 0..ny
+    for (int e = TID; e < nx * (ny + 1) * nzm; e += NT) {
+      const int i = 1 + e % nx, j = (e / nx) % (ny + 1), k = 1 + e / (nx * (ny + 1));
+      const int jc = j + 1, kc = k + 1, kcu = min(kc, nzm), ib = i - 1;
+      const T dyz = dy / (dz * adzw[kc]);
+      const T rdy21 = rdy2 * grdfy[k];
+      const T rdy251 = rdy25 * grdfy[k];
+      T tky = rdy21 * tk(i, j, k);
+      const T fvv = (T)-2. * tky * (v(i, jc, k) - v(i, j, k));
+      tky = rdy251 * (tk(i, j, k) + tk(ib, j, k) + tk(i, jc, k) + tk(ib, jc, k));
+      const T fuv = -tky * (u(i, jc, k) - u(i, j, k) + (v(i, jc, k) - v(ib, jc, k)) * dyx);
+      tky = rdy251 * (tk(i, j, k) + tk(i, jc, k) + tk(i, j, kcu) + tk(i, jc, kcu));
+      const T fwv = -tky * (w(i, jc, kc) - w(i, j, kc) + (v(i, jc, kcu) - v(i, jc, k)) * dyz);
+      fv(i, j, k) = fvv;
+      fu(i, j, k) = fuv;
+      fw(i, j, k) = fwv;
+    }
+    SYNC;
+    for (int e = TID; e < nxy * nzm; e += NT) {
+      const int i = 1 + e % nx, j = 1 + (e / nx) % ny, k = 1 + e / nxy;
+      const int kc = k + 1, jb = j - 1;
+      du(i, j, k) = du(i, j, k) - (fu(i, j, k) - fu(i, jb, k));
+      dv(i, j, k) = dv(i, j, k) - (fv(i, j, k) - fv(i, jb, k));
+      dw(i, j, kc) = dw(i, j, kc) - (fw(i, j, k) - fw(i, jb, k));
+    }
+    SYNC;
+    // vertical fluxes at w levels (reuse fu, fv, fw)
+    for (int e = TID; e < nxy * nzm; e += NT) {
+      const int i = 1 + e % nx, j = 1 + (e / nx) % ny, k = 1 + e / nxy;
+      const T rdz = (T)1. / dz;
+      if (k <= nzm - 1) {
+        const int jb = j - 1, kc = k + 1, ib = i - 1;
+        const T rdz2 = rdz * rdz * grdfz[k];
+        const T rdz25 = (T)0.25 * rdz2;
+        const T iadz = (T)1. / adz[k];
+        const T iadzw = (T)1. / adzw[kc];
+        const T dzx = dz / dx, dzy = dz / dy;
+        T tkz = rdz2 * tk(i, j, k);
+        const T fwv = (T)-2. * tkz * (w(i, j, kc) - w(i, j, k)) * rho[k] * iadz;
+        tkz = rdz25 * (tk(i, j, k) + tk(ib, j, k) + tk(i, j, kc) + tk(ib, j, kc));
+        const T fuv = -tkz * ((u(i, j, kc) - u(i, j, k)) * iadzw + (w(i, j, kc) - w(ib, j, kc)) * dzx) * rhow[kc];
+        tkz = rdz25 * (tk(i, j, k) + tk(i, jb, k) + tk(i, j, kc) + tk(i, jb, kc));
+        const T fvv = -tkz * ((v(i, j, kc) - v(i, j, k)) * iadzw + (w(i, j, kc) - w(i, jb, kc)) * dzy) * rhow[kc];
+        fw(i, j, kc) = fwv;
+        fu(i, j, kc) = fuv;
+        fv(i, j, kc) = fvv;
+      } else {
+        const T rdz2 = rdz * rdz * grdfz[nzm - 1];
+        const T tkz = rdz2 * grdfz[nzm] * tk(i, j, nzm);
+        fw(i, j, nz) = (T)-2. * tkz * (w(i, j, nz) - w(i, j, nzm)) / adz[nzm] * rho[nzm];
+        fu(i, j, 1) = (T)0.0 * rdz * rhow[1];
+        fv(i, j, 1) = (T)0.0 * rdz * rhow[1];
+        fu(i, j, nz) = (T)0.0 * rdz * rhow[nz];
+        fv(i, j, nz) = (T)0.0 * rdz * rhow[nz];
+      }
+    }
+    SYNC;
+    T *uwsb = PR(P_UWSB), *vwsb = PR(P_VWSB);
+    level_sums_lo(2, 1, nzm, [&](int q, int h, int k) -> T { return q == 0 ? fu(h, k) : fv(h, k); },
+               [&](int, int) { return 0.; },
+               [&](int q, int k, double sv) { (q == 0 ? uwsb : vwsb)[k] = (T)sv; });
+    for (int e = TID; e < nxy * nzm; e += NT) {
+      const int i = 1 + e % nx, j = 1 + (e / nx) % ny, k = 1 + e / nxy;
+      const int kc = k + 1;
+      const T rhoi = (T)1. / (rho[k] * adz[k]);
+      du(i, j, k) = du(i, j, k) - (fu(i, j, kc) - fu(i, j, k)) * rhoi;
+      dv(i, j, k) = dv(i, j, k) - (fv(i, j, kc) - fv(i, j, k)) * rhoi;
+      if (k >= 2) {
+        const T rhoiw = (T)1. / (rhow[k] * adzw[k]);
+        dw(i, j, k) = dw(i, j, k) - (fw(i, j, k + 1) - fw(i, j, k)) * rhoiw;
+      }
+    }
+    SYNC;
+  }
+
   // ---------------------------------------------------------- advect_mom
   // advect2_mom_xy.F90:60-80 (2D) and advect2_mom_z.F90:30-122
   __device__ void advect_mom() {
-    F2<T> u = U(), v = V(), w = W(), du = DU(S.na), dv = DV(S.na), dw = DW(S.na);
-    F2<T> fuz = SA(), fvz = SB(), fwz = SCR(p.L.s_c);
+    FT u = U(), v = V(), w = W(), du = DU(S.na), dv = DV(S.na), dw = DW(S.na);
+    FT fuz = SA(), fvz = SB(), fwz = SCR(p.L.s_c);
     T *rho = PR(P_RHO), *adz = PR(P_ADZ), *rhow = PR(P_RHOW), *adzw = PR(P_ADZW);
     const T dx25 = (T)0.25 / (T)p.dx;
     const T dz = (T)S.dz;
@@ -1341,8 +1697,8 @@ struct ColumnKernel : NxDim<NX> {
   // ---------------------------------------------------------- diffuse_mom2D
   // SGS_TKE/diffuse_mom2D.F90:42-160
   __device__ void diffuse_mom() {
-    F2<T> u = U(), v = V(), w = W(), tk = TK(), du = DU(S.na), dv = DV(S.na), dw = DW(S.na);
-    F2<T> fu = SA(), fv = SB(), fw = SCR(p.L.s_c);
+    FT u = U(), v = V(), w = W(), tk = TK(), du = DU(S.na), dv = DV(S.na), dw = DW(S.na);
+    FT fu = SA(), fv = SB(), fw = SCR(p.L.s_c);
     T *rho = PR(P_RHO), *adz = PR(P_ADZ), *rhow = PR(P_RHOW), *adzw = PR(P_ADZW);
     T *grdfx = PR(P_GRDFX), *grdfz = PR(P_GRDFZ);
     const T dx = (T)p.dx, dz = (T)S.dz;
@@ -1444,8 +1800,23 @@ struct ColumnKernel : NxDim<NX> {
   // twiddle i of the trig table: the REAL*4 value, read as T without a
   // widening or narrowing conversion in either form
   __device__ __forceinline__ T tw(int i) const {
+    if constexpr (Y3) {
+      if (fdir) {
+        if constexpr (sizeof(T) == 4) return p.trigs_y_f[i];
+        else return p.trigs_y[i];
+      }
+    }
     if constexpr (sizeof(T) == 4) return p.trigs_f[i];
     else return p.trigs[i];
+  }
+  // transform factors of the current direction (3D: fdir 1 is y)
+  __device__ __forceinline__ int nfax_() const {
+    if constexpr (Y3) return fdir ? p.nfax_y : p.nfax;
+    else return p.nfax;
+  }
+  __device__ __forceinline__ int ifax_(int k) const {
+    if constexpr (Y3) return fdir ? p.ifax_y[k] : p.ifax[k];
+    else return p.ifax[k];
   }
   __device__ void vpass_warp(const T *A, T *C, int nh, int ifac, int la, int lane) const {
     const int m = nh / ifac;
@@ -1490,7 +1861,7 @@ struct ColumnKernel : NxDim<NX> {
   // fft991_crm on a[0..n+1] (shared memory), work[0..n+1]; isign -1: grid
   // point -> spectral, +1: spectral -> grid point.  Called by a whole warp.
   __device__ void fft991_warp(T *a, T *work, int n, int isign, int lane) const {
-    const int nfax = p.nfax, nh = n / 2, npair = (nh - 1) / 2;   // k = 3,5,..,nh
+    const int nfax = nfax_(), nh = n / 2, npair = (nh - 1) / 2;   // k = 3,5,..,nh
     bool in_work;
     if (isign == -1) {
       if (nfax % 2 == 1) in_work = false;
@@ -1523,10 +1894,10 @@ struct ColumnKernel : NxDim<NX> {
     __syncwarp();
     int la = 1;
     for (int k = 1; k <= nfax; ++k) {
-      if (in_work) vpass_warp(work, a, nh, p.ifax[k], la, lane);
-      else vpass_warp(a, work, nh, p.ifax[k], la, lane);
+      if (in_work) vpass_warp(work, a, nh, ifax_(k), la, lane);
+      else vpass_warp(a, work, nh, ifax_(k), la, lane);
       in_work = !in_work;
-      la *= p.ifax[k];
+      la *= ifax_(k);
     }
     if (isign == -1) {
       // fft99b_crm: work -> a
@@ -1574,7 +1945,9 @@ struct ColumnKernel : NxDim<NX> {
   // substep, the last pivot kept as a divisor.
   __device__ double *TRI() const { return reinterpret_cast<double *>(base + p.L.tri); }
   __device__ void tridiag_factor() {
-    const int np = nx + 1, ls = nzm + 1;
+    // coefficients c = (i - 1) + (nx + 1) (j - 1): i = 1..nx+1, j = 1..ny+2 in
+    // 3D, j = 1 in 2D
+    const int np = (nx + 1) * (Y3 ? ny + 2 : 1), ls = nzm + 1;
     // [a(k)], then alfa(k, i) and e(k, i) with the Fourier index i fastest
     // (the solve runs one coefficient per thread, so its loads coalesce), then
     // the np last pivots
@@ -1589,12 +1962,14 @@ struct ColumnKernel : NxDim<NX> {
       double *alb = tri + (size_t)ls + (i - 1), *eb = alb + (size_t)ls * np;
       auto al = [&](int k) -> double & { return alb[(size_t)k * np]; };
       auto e = [&](int k) -> double & { return eb[(size_t)k * np]; };
-      int id = (int)(((float)i - 0.1f) / 2.0f);
+      const int ic = (i - 1) % (nx + 1) + 1, jc = (i - 1) / (nx + 1) + 1;
+      int id = (int)(((float)ic - 0.1f) / 2.0f);
+      int jd = (int)(((float)jc - 0.1f) / 2.0f);
       double eign = p.eign[i - 1];
       double a1 = ak[1];
       double c1 = (double)rhow[2] / ((double)adz[1] * (double)adzw[2] * dz * dz);
       double b;
-      if (id == 0) b = 1. / (eign * (double)rho[1] - a1 - c1);
+      if (id + jd == 0) b = 1. / (eign * (double)rho[1] - a1 - c1);
       else b = 1. / (eign * (double)rho[1] - c1);
       al(1) = -c1 * b;
       e(1) = b;
@@ -1613,12 +1988,145 @@ struct ColumnKernel : NxDim<NX> {
     SYNC;
   }
 
+  // pressure.F90:97-310, press_rhs.F90:48-101, press_grad.F90:18-72 and
+  // bound_duvdt.F90 in 3D: the coefficients live in the slab (fft_f,
+  // (nx+2) x (ny+2) x nzm); each warp transforms rows in x (every j) and
+  // then columns in y (every x coefficient i = 1..nx+1) through its own
+  // shared-memory row and work buffers; one FP64 tridiagonal solve per
+  // (i, j) coefficient; the inverse transforms in the reverse order
+  __device__ void pressure3(T *wsh) {
+    FT u = U(), v = V(), w = W(), pp = PP();
+    FT dua = DU(S.na), dub = DU(S.nb), duc = DU(S.nc);
+    FT dva = DV(S.na), dvb = DV(S.nb), dvc = DV(S.nc);
+    FT dwa = DW(S.na), dwb = DW(S.nb), dwc = DW(S.nc);
+    T *rho = PR(P_RHO);
+    const int nxy = nx * ny, nx2 = nx + 2, ny2 = ny + 2, np = (nx + 1) * ny2;
+    T *F = base + p.L.fft_f;
+    auto FF = [&](int i, int j, int k) -> T & { return F[((size_t)(k - 1) * ny2 + (j - 1)) * nx2 + (i - 1)]; };
+    auto bound_duvdt = [&]() {
+      for (int e = TID; e < ny * nzm; e += NT) {
+        const int j = 1 + e % ny, k = 1 + e / ny;
+        dua(nx + 1, j, k) = dua(1, j, k);
+      }
+      for (int e = TID; e < nx * nzm; e += NT) {
+        const int i = 1 + e % nx, k = 1 + e / nx;
+        dva(i, ny + 1, k) = dva(i, 1, k);
+      }
+    };
+    bound_duvdt();
+    SYNC;
+    const T rdx = (T)1. / (T)p.dx, rdy = (T)1. / (T)p.dy;
+    const T btat = (T)(S.bt / S.at), ctat = (T)(S.ct / S.at);
+    const T dta = (T)(1. / S.dt3[S.na - 1] / S.at);
+    for (int e = TID; e < nxy * nzm; e += NT) {
+      const int i = 1 + e % nx, j = 1 + (e / nx) % ny, k = 1 + e / nxy;
+      const int kc = k + 1, jc = j + 1, ic = i + 1;
+      const T rup = PR(P_RUP)[k], rdn = PR(P_RDN)[k];
+      const T r = (rdx * (u(ic, j, k) - u(i, j, k)) + rdy * (v(i, jc, k) - v(i, j, k)) +
+                   (w(i, j, kc) * rup - w(i, j, k) * rdn)) * dta +
+                  (rdx * (dua(ic, j, k) - dua(i, j, k)) + rdy * (dva(i, jc, k) - dva(i, j, k)) +
+                   (dwa(i, j, kc) * rup - dwa(i, j, k) * rdn)) +
+                  btat * (rdx * (dub(ic, j, k) - dub(i, j, k)) + rdy * (dvb(i, jc, k) - dvb(i, j, k)) +
+                          (dwb(i, j, kc) * rup - dwb(i, j, k) * rdn)) +
+                  ctat * (rdx * (duc(ic, j, k) - duc(i, j, k)) + rdy * (dvc(i, jc, k) - dvc(i, j, k)) +
+                          (dwc(i, j, kc) * rup - dwc(i, j, k) * rdn));
+      FF(i, j, k) = r * rho[k];
+    }
+    SYNC;
+    PHASE_MARK(PH_PRESS_RHS);
+    const int warp = TID >> 5, lane = TID & 31, nwarps = NT >> 5;
+    const int nmax = nx > ny ? nx : ny;
+    T *ra = wsh + (size_t)warp * (2 * nmax + 8), *wk = ra + nmax + 2;
+    auto xrows = [&](int isign) {
+      fdir = 0;
+      for (int r = warp; r < ny * nzm; r += nwarps) {
+        const int j = 1 + r % ny, k = 1 + r / ny;
+        T *row = &FF(1, j, k);
+        for (int m = lane; m < nx2; m += 32) ra[m] = row[m];
+        __syncwarp();
+        fft991_warp(ra, wk, nx, isign, lane);
+        for (int m = lane; m < nx2; m += 32) row[m] = ra[m];
+        __syncwarp();
+      }
+    };
+    auto ycols = [&](int isign) {
+      fdir = 1;
+      for (int r = warp; r < (nx + 1) * nzm; r += nwarps) {
+        const int i = 1 + r % (nx + 1), k = 1 + r / (nx + 1);
+        for (int m = lane; m < ny2; m += 32) ra[m] = FF(i, 1 + m, k);
+        __syncwarp();
+        fft991_warp(ra, wk, ny, isign, lane);
+        for (int m = lane; m < ny2; m += 32) FF(i, 1 + m, k) = ra[m];
+        __syncwarp();
+      }
+      fdir = 0;
+    };
+    xrows(-1);
+    SYNC;
+    ycols(-1);
+    SYNC;
+    PHASE_MARK(PH_FFT_FWD);
+    // vertical tridiagonal solve per coefficient c = (i-1) + (nx+1)(j-1), in FP64
+    {
+      const int ls = nzm + 1;
+      const size_t lstride = (size_t)nx2 * ny2;
+      const double *tri = TRI();
+      double *beta = reinterpret_cast<double *>(sa());   // (nzm+1) x np doubles, c fastest (planes A and B)
+      for (int c = TID; c < np; c += NT) {
+        const int i = 1 + c % (nx + 1), j = 1 + c / (nx + 1);
+        const double *al = tri + (size_t)ls + c, *e = al + (size_t)ls * np;
+        double *be = beta + c;
+        T *ff = F + (size_t)(j - 1) * nx2 + (i - 1);
+        double bprev = (double)ff[0] * e[np];
+        be[np] = bprev;
+        for (int k = 2; k <= nzm - 1; ++k) {
+          bprev = ((double)ff[lstride * (k - 1)] - tri[k] * bprev) * e[(size_t)k * np];
+          be[(size_t)k * np] = bprev;
+        }
+        double fk = ((double)ff[lstride * (nzm - 1)] - tri[nzm] * bprev) / tri[(size_t)ls + (size_t)np * 2 * ls + c];
+        ff[lstride * (nzm - 1)] = (T)fk;
+        for (int k = nzm - 1; k >= 1; --k) {
+          fk = al[(size_t)k * np] * fk + be[(size_t)k * np];
+          ff[lstride * (k - 1)] = (T)fk;
+        }
+      }
+    }
+    SYNC;
+    PHASE_MARK(PH_TRIDIAG);
+    ycols(+1);
+    SYNC;
+    xrows(+1);
+    SYNC;
+    PHASE_MARK(PH_FFT_INV);
+    for (int e = TID; e < (nx + 1) * (ny + 1) * nzm; e += NT) {
+      const int i = e % (nx + 1), j = (e / (nx + 1)) % (ny + 1), k = 1 + e / ((nx + 1) * (ny + 1));
+      pp(i, j, k) = FF(i == 0 ? nx : i, j == 0 ? ny : j, k);
+    }
+    SYNC;
+    for (int e = TID; e < nxy * nzm; e += NT) {
+      const int i = 1 + e % nx, j = 1 + (e / nx) % ny, k = 1 + e / nxy;
+      const int kb = max(1, k - 1);
+      const T rdz = PR(P_RDZW)[k];
+      dua(i, j, k) = dua(i, j, k) - (pp(i, j, k) - pp(i - 1, j, k)) * rdx;
+      dva(i, j, k) = dva(i, j, k) - (pp(i, j, k) - pp(i, j - 1, k)) * rdy;
+      dwa(i, j, k) = dwa(i, j, k) - (pp(i, j, k) - pp(i, j, kb)) * rdz;
+    }
+    SYNC;
+    for (int e = TID; e < (nx + 1) * (ny + 1) * nzm; e += NT) {
+      const int i = e % (nx + 1), j = (e / (nx + 1)) % (ny + 1), k = 1 + e / ((nx + 1) * (ny + 1));
+      pp(i, j, k) = pp(i, j, k) * rho[k];
+    }
+    bound_duvdt();
+    SYNC;
+    PHASE_MARK(PH_PRESS_GRAD);
+  }
+
   // pressure.F90:97-310, press_rhs.F90:48-101, press_grad.F90:18-72,
   // bound_duvdt.F90 (2D); the Fourier coefficients live in shared memory
   __device__ void pressure(T *fsh, T *wsh) {
-    F2<T> u = U(), w = W(), pp = PP();
-    F2<T> dua = DU(S.na), dub = DU(S.nb), duc = DU(S.nc);
-    F2<T> dwa = DW(S.na), dwb = DW(S.nb), dwc = DW(S.nc);
+    FT u = U(), w = W(), pp = PP();
+    FT dua = DU(S.na), dub = DU(S.nb), duc = DU(S.nc);
+    FT dwa = DW(S.na), dwb = DW(S.nb), dwc = DW(S.nc);
     T *rho = PR(P_RHO), *rhow = PR(P_RHOW), *adz = PR(P_ADZ), *adzw = PR(P_ADZW);
     const T dz = (T)S.dz;
     for (int k = TID + 1; k <= nzm; k += NT) dua(nx + 1, k) = dua(1, k);
@@ -1709,7 +2217,7 @@ struct ColumnKernel : NxDim<NX> {
       pp(i, k) = fsh[(size_t)nx2 * (k - 1) + ((i == 0 ? nx : i) - 1)];
     }
     SYNC;
-    F2<T> dva = DV(S.na);
+    FT dva = DV(S.na);
     const T rdy = (T)1. / (T)p.dy;
     for (int e = TID; e < nx * nzm; e += NT) {
       int i = 1 + e % nx, k = 1 + e / nx;
@@ -1731,15 +2239,15 @@ struct ColumnKernel : NxDim<NX> {
 
   // ---------------------------------------------------------- adams / uvw
   __device__ void adams() {                    // adams.F90:17-38
-    F2<T> u = U(), v = V(), w = W();
-    F2<T> dua = DU(S.na), dub = DU(S.nb), duc = DU(S.nc);
-    F2<T> dva = DV(S.na), dvb = DV(S.nb), dvc = DV(S.nc);
-    F2<T> dwa = DW(S.na), dwb = DW(S.nb), dwc = DW(S.nc);
+    FT u = U(), v = V(), w = W();
+    FT dua = DU(S.na), dub = DU(S.nb), duc = DU(S.nc);
+    FT dva = DV(S.na), dvb = DV(S.nb), dvc = DV(S.nc);
+    FT dwa = DW(S.na), dwb = DW(S.nb), dwc = DW(S.nc);
     const T dtdx = (T)(S.dtn / p.dx), dtdz = (T)(S.dtn / S.dz), dtdy = (T)(S.dtn / p.dy);
     const T d3 = (T)S.dt3[S.na - 1], at = (T)S.at, bt = (T)S.bt, ct = (T)S.ct;
     T *rho = PR(P_RHO), *rhow = PR(P_RHOW);
-    for (int e = TID; e < nx * nzm; e += NT) {
-      int i = 1 + e % nx, k = 1 + e / nx;
+    for (int e = TID; e < NH() * nzm; e += NT) {
+      int i = 1 + e % NH(), k = 1 + e / NH();
       T rhox = rho[k] * dtdx, rhoy = rho[k] * dtdy, rhoz = rhow[k] * dtdz;
       T un = u(i, k) + d3 * (at * dua(i, k) + bt * dub(i, k) + ct * duc(i, k));
       T vn = v(i, k) + d3 * (at * dva(i, k) + bt * dvb(i, k) + ct * dvc(i, k));
@@ -1752,9 +2260,9 @@ struct ColumnKernel : NxDim<NX> {
     SYNC;
   }
   __device__ void uvw() {                      // uvw.F90
-    F2<T> u = U(), v = V(), w = W(), duc = DU(S.nc), dvc = DV(S.nc), dwc = DW(S.nc);
-    for (int e = TID; e < nx * nzm; e += NT) {
-      int i = 1 + e % nx, k = 1 + e / nx;
+    FT u = U(), v = V(), w = W(), duc = DU(S.nc), dvc = DV(S.nc), dwc = DW(S.nc);
+    for (int e = TID; e < NH() * nzm; e += NT) {
+      int i = 1 + e % NH(), k = 1 + e / NH();
       u(i, k) = duc(i, k); v(i, k) = dvc(i, k); w(i, k) = dwc(i, k);
     }
     SYNC;
@@ -1785,11 +2293,15 @@ struct ColumnKernel : NxDim<NX> {
   // every bit of it unchanged and give +0 for their statistics (every flux is
   // a signed zero, every update adds or subtracts a zero to +0), so a column
   // without precipitating water skips both for qp.
-  __device__ bool all_pos_zero(F2<T> f) {
+  __device__ bool all_pos_zero(FT f) {
     int nonzero = 0;
-    for (int e = TID; e < (nx + 6) * nzm; e += NT) {
-      const int i = -2 + e % (nx + 6), k = 1 + e / (nx + 6);
-      const T v = f(i, k);
+    // 2D: the x row of every level 1..nzm; 3D: every stored cell of those
+    // levels (x and y halos included), which lie contiguous
+    const int n = Y3 ? f.plane * nzm : (nx + 6) * nzm;
+    for (int e = TID; e < n; e += NT) {
+      T v;
+      if constexpr (Y3) v = f.p[e];
+      else v = f(-2 + e % (nx + 6), 1 + e / (nx + 6));
       if constexpr (sizeof(T) == 8) nonzero |= (__double_as_longlong(v) != 0);
       else nonzero |= (__float_as_uint(v) != 0u);
     }
@@ -1804,10 +2316,10 @@ struct ColumnKernel : NxDim<NX> {
     SYNC;
   }
 
-  __device__ void advect_scalar(F2<T> f, T *fadv, T *flux, T *rc = nullptr) {
-    F2<T> u = U(), w = W();
-    F2<T> mx = SA(), mn = SB(), uuu = SCR(p.L.s_c), www = SCR(p.L.s_d), f0 = SCR(p.L.s_e);
-    F2<T> wfl1 = SCR(p.L.s_f);
+  __device__ void advect_scalar(FT f, T *fadv, T *flux, T *rc = nullptr) {
+    FT u = U(), w = W();
+    FT mx = SA(), mn = SB(), uuu = SCR(p.L.s_c), www = SCR(p.L.s_d), f0 = SCR(p.L.s_e);
+    FT wfl1 = SCR(p.L.s_f);
     T *rho = PR(P_RHO), *adz = PR(P_ADZ), *rhow = PR(P_RHOW);
     const T eps = (T)R4(1.e-10);
     // Every pass gathers from other cells and writes only its own cell, so
@@ -1979,6 +2491,187 @@ struct ColumnKernel : NxDim<NX> {
     }
   }
 
+  // ---------------------------------------------------------- MPDATA, 3D
+  // ADV_MPDATA/advect_scalar3D.F90:8-349 (nonos, no walls) with the
+  // advect_scalar.F90 wrapper's fadv; scratch planes: mx, mn in A, B, the
+  // fluxes uuu, vvv, www in C, D, E, the initial field in F, the first-pass
+  // vertical flux sum in G
+  __device__ void advect_scalar3(FT f, T *fadv, T *flux, T *rc = nullptr) {
+    FT u = U(), v = V(), w = W();
+    FT mx = SA(), mn = SB(), uuu = SCR(p.L.s_c), vvv = SCR(p.L.s_d), www = SCR(p.L.s_e), f0 = SCR(p.L.s_f);
+    FT wfl1 = SCR(p.L.s_g);
+    T *rho = PR(P_RHO);
+    const T eps = (T)R4(1.e-10);
+    const int nxy = nx * ny;
+    auto mx7 = [](T a, T b, T c, T d, T e, T f_, T g) { return mx2(mx2(mx2(mx2(mx2(mx2(a, b), c), d), e), f_), g); };
+    auto mn7 = [](T a, T b, T c, T d, T e, T f_, T g) { return mn2(mn2(mn2(mn2(mn2(mn2(a, b), c), d), e), f_), g); };
+    // bounds of the initial field, upwind fluxes (i = -1..nx+3, j = -1..ny+3)
+    {
+      const int wx = nx + 5, wy = ny + 5;
+      for (int e = TID; e < wx * wy * nzm; e += NT) {
+        const int i = -1 + e % wx, j = -1 + (e / wx) % wy, k = 1 + e / (wx * wy);
+        const int kc = min(nzm, k + 1), kb = max(1, k - 1);
+        if (i >= 0 && i <= nx + 1 && j >= 0 && j <= ny + 1) {
+          const T a = f(i - 1, j, k), b = f(i + 1, j, k), c = f(i, j - 1, k), d = f(i, j + 1, k);
+          const T fb = f(i, j, kb), fc = f(i, j, kc), fk = f(i, j, k);
+          mx(i, j, k) = mx7(a, b, c, d, fb, fc, fk);
+          mn(i, j, k) = mn7(a, b, c, d, fb, fc, fk);
+        }
+        if (j <= ny + 2) {
+          const T uk = u(i, j, k);
+          uuu(i, j, k) = mx2((T)0., uk) * f(i - 1, j, k) + mn2((T)0., uk) * f(i, j, k);
+        }
+        if (i <= nx + 2) {
+          const T vk = v(i, j, k);
+          vvv(i, j, k) = mx2((T)0., vk) * f(i, j - 1, k) + mn2((T)0., vk) * f(i, j, k);
+        }
+        if (i <= nx + 2 && j <= ny + 2) {
+          const T wk = w(i, j, k);
+          www(i, j, k) = mx2((T)0., wk) * f(i, j, kb) + mn2((T)0., wk) * f(i, j, k);
+          if (k == 1) www(i, j, nz) = (T)0.;
+        }
+        if (fadv && i >= 1 && i <= nx && j >= 1 && j <= ny) f0(i, j, k) = f(i, j, k);
+      }
+    }
+    SYNC;
+    if (flux)
+      level_sums_lo(1, 1, nzm, [&](int, int h, int k) -> T { return www(h, k); },
+                    [&](int, int) { return 0.; }, [&](int, int k, double sv) { wfl1(0, 0, k) = (T)sv; });
+    // upwind update (i = -1..nx+2, j = -1..ny+2); the residue keeps the
+    // interior update's rounding error
+    {
+      const int wx = nx + 4, wy = ny + 4;
+      for (int e = TID; e < wx * wy * nzm; e += NT) {
+        const int i = -1 + e % wx, j = -1 + (e / wx) % wy, k = 1 + e / (wx * wy);
+        const T iadz = PR(P_IADZ)[k], irho = PR(P_IRHO)[k];
+        const T c1 = (uuu(i + 1, j, k) - uuu(i, j, k) + vvv(i, j + 1, k) - vvv(i, j, k) +
+                      (www(i, j, k + 1) - www(i, j, k)) * iadz) * irho;
+        if (sizeof(T) == 4 && rc && i >= 1 && i <= nx && j >= 1 && j <= ny) {
+          T err = (T)0.;
+          f(i, j, k) = add_carry(f(i, j, k), -c1, err);
+          rc[(size_t)(i - 1) + (size_t)nx * (j - 1) + (size_t)nxy * (k - 1)] += err;
+        } else {
+          f(i, j, k) = f(i, j, k) - c1;
+        }
+      }
+    }
+    SYNC;
+    // antidiffusive velocities (i = 0..nx+2, j = 0..ny+2)
+    {
+      const int wx = nx + 3, wy = ny + 3;
+      for (int e = TID; e < wx * wy * nzm; e += NT) {
+        const int i = e % wx, j = (e / wx) % wy, k = 1 + e / (wx * wy);
+        const int kc = min(nzm, k + 1), kb = max(1, k - 1), ib = i - 1, ic = i + 1, jb = j - 1, jc = j + 1;
+        const T irho = PR(P_IRHO)[k], irhow = PR(P_IRHOWADZ)[k], dd = PR(P_MPDD)[k];
+        T uval = (T)0., vval = (T)0., wval = (T)0.;
+        if (j <= ny + 1) {
+          const T a = u(i, j, k);
+          const T andiff = (tabs_(a) - a * a * irho) * (T)0.5 * (f(i, j, k) - f(ib, j, k));
+          const T ac1 = (T)0.03125 * a * (v(ib, j, k) + v(ib, jc, k) + v(i, jc, k) + v(i, j, k)) *
+                        (f(ib, jc, k) + f(i, jc, k) - f(ib, jb, k) - f(i, jb, k));
+          const T ac2 = (T)0.03125 * a * (w(ib, j, k) + w(ib, j, kc) + w(i, j, k) + w(i, j, kc)) *
+                        (dd * (f(ib, j, kc) + f(i, j, kc) - f(ib, j, kb) - f(i, j, kb)));
+          uval = andiff - (ac1 + ac2) * irho;
+        }
+        if (i <= nx + 1) {
+          const T a = v(i, j, k);
+          const T andiff = (tabs_(a) - a * a * irho) * (T)0.5 * (f(i, j, k) - f(i, jb, k));
+          const T ac1 = (T)0.03125 * a * (u(i, jb, k) + u(i, j, k) + u(ic, j, k) + u(ic, jb, k)) *
+                        (f(ic, jb, k) + f(ic, j, k) - f(ib, jb, k) - f(ib, j, k));
+          const T ac2 = (T)0.03125 * a * (w(i, jb, k) + w(i, j, k) + w(i, j, kc) + w(i, jb, kc)) *
+                        (dd * (f(i, jb, kc) + f(i, j, kc) - f(i, jb, kb) - f(i, j, kb)));
+          vval = andiff - (ac1 + ac2) * irho;
+        }
+        if (i <= nx + 1 && j <= ny + 1 && k > 1) {
+          const T a = w(i, j, k);
+          const T andiff = (tabs_(a) - a * a * irhow) * (T)0.5 * (f(i, j, k) - f(i, j, kb));
+          const T ac1 = (T)0.03125 * a * (u(i, j, kb) + u(i, j, k) + u(ic, j, k) + u(ic, j, kb)) *
+                        (f(ic, j, kb) + f(ic, j, k) - f(ib, j, kb) - f(ib, j, k));
+          const T ac2 = (T)0.03125 * a * (v(i, j, kb) + v(i, jc, kb) + v(i, jc, k) + v(i, j, k)) *
+                        (f(i, jc, k) + f(i, jc, kb) - f(i, jb, k) - f(i, jb, kb));
+          wval = andiff - (ac1 + ac2) * irho;
+        }
+        if (j <= ny + 1) uuu(i, j, k) = uval;
+        if (i <= nx + 1) vvv(i, j, k) = vval;
+        if (i <= nx + 1 && j <= ny + 1) www(i, j, k) = wval;
+      }
+    }
+    SYNC;
+    // non-oscillatory limiter (i = 0..nx+1, j = 0..ny+1)
+    {
+      const int wx = nx + 2, wy = ny + 2;
+      for (int e = TID; e < wx * wy * nzm; e += NT) {
+        const int i = e % wx, j = (e / wx) % wy, k = 1 + e / (wx * wy);
+        const int kc = min(nzm, k + 1), kb = max(1, k - 1);
+        const T iadz = PR(P_IADZ)[k];
+        const T a = f(i - 1, j, k), b = f(i + 1, j, k), c = f(i, j - 1, k), d = f(i, j + 1, k);
+        const T fb = f(i, j, kb), fc = f(i, j, kc), fk = f(i, j, k);
+        const T m1 = mx2(mx7(a, b, c, d, fb, fc, fk), mx(i, j, k));
+        const T m2 = mn2(mn7(a, b, c, d, fb, fc, fk), mn(i, j, k));
+        const T uc = uuu(i + 1, j, k), ui = uuu(i, j, k), vc = vvv(i, j + 1, k), vi = vvv(i, j, k);
+        const T wc = www(i, j, kc), wi = www(i, j, k);
+        const T dmx = -mn2((T)0., uc) + mx2((T)0., ui) + -mn2((T)0., vc) + mx2((T)0., vi) +
+                      (-mn2((T)0., wc) + mx2((T)0., wi)) * iadz + eps;
+        const T dmn = mx2((T)0., uc) + -mn2((T)0., ui) + mx2((T)0., vc) + -mn2((T)0., vi) +
+                      (mx2((T)0., wc) + -mn2((T)0., wi)) * iadz + eps;
+        mx(i, j, k) = rho[k] * (m1 - fk) / dmx;
+        mn(i, j, k) = rho[k] * (fk - m2) / dmn;
+      }
+    }
+    SYNC;
+    // limited antidiffusive fluxes (i = 1..nx+1, j = 1..ny+1)
+    {
+      const int wx = nx + 1, wy = ny + 1;
+      for (int e = TID; e < wx * wy * nzm; e += NT) {
+        const int i = 1 + e % wx, j = 1 + (e / wx) % wy, k = 1 + e / (wx * wy);
+        const T mxk = mx(i, j, k), mnk = mn(i, j, k);
+        if (j <= ny) {
+          const T uu = uuu(i, j, k);
+          uuu(i, j, k) = mx2((T)0., uu) * mn3((T)1., mxk, mn(i - 1, j, k)) -
+                         (-mn2((T)0., uu)) * mn3((T)1., mx(i - 1, j, k), mnk);
+        }
+        if (i <= nx) {
+          const T vv = vvv(i, j, k);
+          vvv(i, j, k) = mx2((T)0., vv) * mn3((T)1., mxk, mn(i, j - 1, k)) -
+                         (-mn2((T)0., vv)) * mn3((T)1., mx(i, j - 1, k), mnk);
+        }
+        if (i <= nx && j <= ny) {
+          const int kb = max(1, k - 1);
+          const T ww = www(i, j, k);
+          www(i, j, k) = mx2((T)0., ww) * mn3((T)1., mxk, mn(i, j, kb)) -
+                         (-mn2((T)0., ww)) * mn3((T)1., mx(i, j, kb), mnk);
+        }
+      }
+    }
+    SYNC;
+    if (flux)
+      level_sums_lo(1, 1, nzm, [&](int, int h, int k) -> T { return www(h, k); },
+                    [&](int, int k) { return (double)wfl1(0, 0, k); },
+                    [&](int, int k, double sv) { flux[k] = (T)sv; });
+    // final update with the positive-definite clip
+    for (int e = TID; e < nxy * nzm; e += NT) {
+      const int i = 1 + e % nx, j = 1 + (e / nx) % ny, k = 1 + e / nxy;
+      const T iadz = PR(P_IADZ)[k], irho = PR(P_IRHO)[k];
+      const T c2 = (uuu(i + 1, j, k) - uuu(i, j, k) + vvv(i, j + 1, k) - vvv(i, j, k) +
+                    (www(i, j, k + 1) - www(i, j, k)) * iadz) * irho;
+      if (sizeof(T) == 4 && rc) {
+        T r = rc[e];
+        T fn = add_carry(f(i, j, k), -c2, r);
+        if (!(fn > (T)0.)) { fn = (T)0.; r = (T)0.; }
+        f(i, j, k) = fn;
+        rc[e] = r;
+      } else {
+        f(i, j, k) = mx2((T)0., f(i, j, k) - c2);
+      }
+    }
+    SYNC;
+    if (fadv) {
+      level_sums_lo(1, 1, nzm, [&](int, int h, int k) -> T { return f(h, k) - f0(h, k); },
+                    [&](int, int) { return 0.; }, [&](int, int k, double sv) { fadv[k] = (T)sv; });
+      SYNC;
+    }
+  }
+
   // ---------------------------------------------------------- precip_fall
   // MICRO_SAM1MOM/microphysics.F90:453-486 (term_vel_qp) and :491-833
   __device__ T term_vel(T tabs, T rho, T qploc) const {
@@ -2006,8 +2699,8 @@ struct ColumnKernel : NxDim<NX> {
   }
   // part 1: terminal velocities and the column precipitation CFL number
   __device__ void precip_fall_1() {
-    F2<T> tabs = TABS(), qp = QP();
-    F2<T> wp = SA(), omega = SB();
+    FT tabs = TABS(), qp = QP();
+    FT wp = SA(), omega = SB();
     T *rho = PR(P_RHO), *rhow = PR(P_RHOW), *adz = PR(P_ADZ);
     T *rhofac = PR(P_TMP4), *irhoadz = PR(P_TMP5), *iwmax = PR(P_TMP6);
     const T dtn = (T)S.dtn, dz = (T)S.dz;
@@ -2023,8 +2716,8 @@ struct ColumnKernel : NxDim<NX> {
     // monotone, so the result equals a maximum of widened values)
     T cflt = (T)0.;
     int moving = 0;
-    for (int e = TID; e < nx * nzm; e += NT) {
-      int i = 1 + e % nx, k = 1 + e / nx;
+    for (int e = TID; e < NH() * nzm; e += NT) {
+      int i = 1 + e % NH(), k = 1 + e / NH();
       omega(i, k) = mx2((T)0., mn2((T)1., (tabs(i, k) - (T)C_TPRMIN) * (T)p.a_pr));
       T tmp = term_vel(tabs(i, k), rho[k], qp(i, k));
       T wv = rhofac[k] * tmp;
@@ -2052,9 +2745,9 @@ struct ColumnKernel : NxDim<NX> {
   }
   // part 2: nprec monotone flux-limited sedimentation sub-steps
   __device__ void precip_fall_2(int nprec) {
-    F2<T> tabs = TABS(), qp = QP(), t = TT();
-    F2<T> wp = SA(), omega = SB(), tq = SCR(p.L.s_c), fz = SCR(p.L.s_d);
-    F2<T> mx = SCR(p.L.s_e), mn = SCR(p.L.s_f), www = SCR(p.L.s_g);
+    FT tabs = TABS(), qp = QP(), t = TT();
+    FT wp = SA(), omega = SB(), tq = SCR(p.L.s_c), fz = SCR(p.L.s_d);
+    FT mx = SCR(p.L.s_e), mn = SCR(p.L.s_f), www = SCR(p.L.s_g);
     T *rho = PR(P_RHO), *rhow = PR(P_RHOW), *adz = PR(P_ADZ);
     T *rhofac = PR(P_TMP4), *irhoadz = PR(P_TMP5);
     T *qpfall = PR(P_QPFALL), *precflux = PR(P_PRECFLUX);
@@ -2062,15 +2755,15 @@ struct ColumnKernel : NxDim<NX> {
     const T dtn = (T)S.dtn, dz = (T)S.dz;
     const T fc = (T)C_FAC_COND, ffus = (T)C_FAC_FUS;
     if (nprec > 1) {
-      for (int e = TID; e < nx * nzm; e += NT) {
-        int i = 1 + e % nx, k = 1 + e / nx;
+      for (int e = TID; e < NH() * nzm; e += NT) {
+        int i = 1 + e % NH(), k = 1 + e / NH();
         wp(i, k) = wp(i, k) / (T)(double)nprec;
       }
       SYNC;
     }
     for (int iprec = 1; iprec <= nprec; ++iprec) {
-      for (int e = TID; e < nx * nzm; e += NT) {
-        int i = 1 + e % nx, k = 1 + e / nx;
+      for (int e = TID; e < NH() * nzm; e += NT) {
+        int i = 1 + e % NH(), k = 1 + e / NH();
         int kc = min(nzm, k + 1), kb = max(1, k - 1);
         T q0 = qp(i, k), qb = qp(i, kb), qc = qp(i, kc);
         mx(i, k) = mx3(qb, qc, q0);
@@ -2079,19 +2772,19 @@ struct ColumnKernel : NxDim<NX> {
         if (k == 1) { fz(i, nz) = (T)0.; www(i, nz) = (T)0.; }
       }
       SYNC;
-      for (int e = TID; e < nx * nzm; e += NT) {
-        int i = 1 + e % nx, k = 1 + e / nx;
+      for (int e = TID; e < NH() * nzm; e += NT) {
+        int i = 1 + e % NH(), k = 1 + e / NH();
         tq(i, k) = qp(i, k) - (fz(i, k + 1) - fz(i, k)) * irhoadz[k];
       }
       SYNC;
-      for (int e = TID; e < nx * nzm; e += NT) {
-        int i = 1 + e % nx, k = 1 + e / nx;
+      for (int e = TID; e < NH() * nzm; e += NT) {
+        int i = 1 + e % NH(), k = 1 + e / NH();
         int kb = max(1, k - 1);
         www(i, k) = (T)0.5 * ((T)1. + wp(i, k) * irhoadz[k]) * (tq(i, kb) * wp(i, kb) - tq(i, k) * wp(i, k));
       }
       SYNC;
-      for (int e = TID; e < nx * nzm; e += NT) {
-        int i = 1 + e % nx, k = 1 + e / nx;
+      for (int e = TID; e < NH() * nzm; e += NT) {
+        int i = 1 + e % NH(), k = 1 + e / NH();
         int kc = min(nzm, k + 1), kb = max(1, k - 1);
         const T tb = tq(i, kb), tc = tq(i, kc), tk0 = tq(i, k), wc = www(i, kc), wk = www(i, k);
         T a = mx2(mx3(tb, tc, tk0), mx(i, k));
@@ -2102,8 +2795,8 @@ struct ColumnKernel : NxDim<NX> {
         mn(i, k) = mnv;
       }
       SYNC;
-      for (int e = TID; e < nx * nzm; e += NT) {
-        int i = 1 + e % nx, k = 1 + e / nx;
+      for (int e = TID; e < NH() * nzm; e += NT) {
+        int i = 1 + e % NH(), k = 1 + e / NH();
         int kb = max(1, k - 1);
         T ww = www(i, k);
         fz(i, k) = fz(i, k) + mx2((T)0., ww) * mn3((T)1., mx(i, k), mn(i, kb)) - (-mn2((T)0., ww)) * mn3((T)1., mx(i, kb), mn(i, k));
@@ -2117,8 +2810,8 @@ struct ColumnKernel : NxDim<NX> {
                  },
                  [&](int q, int k) { return (double)(q == 0 ? qpfall[k] : precflux[k]); },
                  [&](int q, int k, double sv) { (q == 0 ? qpfall : precflux)[k] = (T)sv; });
-      for (int e = TID; e < nx * nzm; e += NT) {
-        int i = 1 + e % nx, k = 1 + e / nx;
+      for (int e = TID; e < NH() * nzm; e += NT) {
+        int i = 1 + e % NH(), k = 1 + e / NH();
         int kc = k + 1;
         T lf_c = (kc == nz) ? (T)0. : fc + ((T)1. - omega(i, kc)) * ffus;
         const T omk = omega(i, k), fzc = fz(i, kc), fzk = fz(i, k), ia = irhoadz[k];
@@ -2135,8 +2828,8 @@ struct ColumnKernel : NxDim<NX> {
       }
       SYNC;
       if (iprec < nprec) {
-        for (int e = TID; e < nx * nzm; e += NT) {
-          int i = 1 + e % nx, k = 1 + e / nx;
+        for (int e = TID; e < NH() * nzm; e += NT) {
+          int i = 1 + e % NH(), k = 1 + e / NH();
           T tmp = term_vel(tabs(i, k), rho[k], qp(i, k));
           T wv = rhofac[k] * tmp;
           wp(i, k) = -wv * rhow[k] * dtn / dz / (T)(double)nprec;
@@ -2148,8 +2841,8 @@ struct ColumnKernel : NxDim<NX> {
 
   // ---------------------------------------------------------- SGS scalar diffusion
   // SGS_TKE/diffuse_scalar.F90:33-72 + diffuse_scalar2D.F90:44-140
-  __device__ void diffuse_scalar(F2<T> f, T *fdiff, T *flux, T *rc = nullptr) {
-    F2<T> tkh = TKH(), flx = SA(), dfdt = SB(), f0 = SCR(p.L.s_c);
+  __device__ void diffuse_scalar(FT f, T *fdiff, T *flux, T *rc = nullptr) {
+    FT tkh = TKH(), flx = SA(), dfdt = SB(), f0 = SCR(p.L.s_c);
     T *rho = PR(P_RHO), *rhow = PR(P_RHOW), *adz = PR(P_ADZ), *adzw = PR(P_ADZW);
     T *grdfx = PR(P_GRDFX), *grdfz = PR(P_GRDFZ);
     const T dx = (T)p.dx, dz = (T)S.dz, dtn = (T)S.dtn;
@@ -2206,17 +2899,81 @@ struct ColumnKernel : NxDim<NX> {
     }
   }
 
+  // ---------------------------------------------------------- SGS scalar diffusion, 3D
+  // SGS_TKE/diffuse_scalar3D.F90:6-218 (fluxb = fluxt = 0, no walls) with
+  // the sgs_scalars wrapper's fdiff; scratch planes: x and y fluxes in A, B,
+  // the tendency in C, vertical fluxes in D (levels 0..nzm), the initial
+  // field in E
+  __device__ void diffuse_scalar3(FT f, T *fdiff, T *flux, T *rc = nullptr) {
+    FT tkh = TKH(), flx = SA(), fly = SB(), dfdt = SCR(p.L.s_c), flz = SCR(p.L.s_d), f0 = SCR(p.L.s_e);
+    T *rhow = PR(P_RHOW), *adzw = PR(P_ADZW);
+    T *grdfx = PR(P_GRDFX), *grdfy = PR(P_GRDFY), *grdfz = PR(P_GRDFZ);
+    const T dx = (T)p.dx, dy = (T)p.dy, dz = (T)S.dz, dtn = (T)S.dtn;
+    const T rdx2 = (T)1. / (dx * dx), rdy2 = (T)1. / (dy * dy);
+    const int nxy = nx * ny;
+    for (int e = TID; e < (nx + 1) * (ny + 1) * nzm; e += NT) {
+      const int i = e % (nx + 1), j = (e / (nx + 1)) % (ny + 1), k = 1 + e / ((nx + 1) * (ny + 1));
+      const T fk = f(i, j, k);
+      if (j >= 1) {
+        const T rdx5 = (T)0.5 * rdx2 * grdfx[k];
+        const T tkx = rdx5 * (tkh(i, j, k) + tkh(i + 1, j, k));
+        flx(i, j, k) = -tkx * (f(i + 1, j, k) - fk);
+      }
+      if (i >= 1) {
+        const T rdy5 = (T)0.5 * rdy2 * grdfy[k];
+        const T tky = rdy5 * (tkh(i, j, k) + tkh(i, j + 1, k));
+        fly(i, j, k) = -tky * (f(i, j + 1, k) - fk);
+      }
+      if (fdiff && i >= 1 && j >= 1) f0(i, j, k) = fk;
+    }
+    SYNC;
+    for (int e = TID; e < nxy * nzm; e += NT) {
+      const int i = 1 + e % nx, j = 1 + (e / nx) % ny, k = 1 + e / nxy;
+      dfdt(i, j, k) = ((T)0. - (flx(i, j, k) - flx(i - 1, j, k))) - (fly(i, j, k) - fly(i, j - 1, k));
+      if (k <= nzm - 1) {
+        const int kc = k + 1;
+        const T rhoi = PR(P_RHOWDADZW)[kc];
+        const T rdz2 = (T)1. / (dz * dz);
+        const T rdz5 = (T)0.5 * rdz2 * grdfz[k];
+        const T tkz = rdz5 * (tkh(i, j, k) + tkh(i, j, kc));
+        flz(i, j, k) = -tkz * (f(i, j, kc) - f(i, j, k)) * rhoi;
+      } else {
+        const T tmp = (T)1. / adzw[nz];
+        const T rdz = (T)1. / dz;
+        flz(i, j, 0) = (T)0.0 * rdz * rhow[1];
+        flz(i, j, nzm) = (T)0.0 * rdz * tmp * rhow[nz];
+      }
+    }
+    SYNC;
+    if (flux)
+      level_sums_lo(1, 1, nzm, [&](int, int h, int k) -> T { return flz(h, k == 1 ? 0 : k - 1); },
+                    [&](int, int) { return 0.; }, [&](int, int k, double sv) { flux[k] = (T)sv; });
+    for (int e = TID; e < nxy * nzm; e += NT) {
+      const int i = 1 + e % nx, j = 1 + (e / nx) % ny, k = 1 + e / nxy;
+      const T rhoi = PR(P_IRHOADZ)[k];
+      const T d = dtn * (dfdt(i, j, k) - (flz(i, j, k) - flz(i, j, k - 1)) * rhoi);
+      if (sizeof(T) == 4 && rc) f(i, j, k) = add_carry(f(i, j, k), d, rc[e]);
+      else f(i, j, k) = f(i, j, k) + d;
+    }
+    SYNC;
+    if (fdiff) {
+      level_sums_lo(1, 1, nzm, [&](int, int h, int k) -> T { return f(h, k) - f0(h, k); },
+                    [&](int, int) { return 0.; }, [&](int, int k, double sv) { fdiff[k] = (T)sv; });
+      SYNC;
+    }
+  }
+
   // ---------------------------------------------------------- cloud
   // MICRO_SAM1MOM/cloud.F90:26-111: saturation adjustment, Newton in FP64
   __device__ void cloud() {
-    F2<T> qt = QT(), qp = QP(), qn = QN(), tabs = TABS(), t = TT();
+    FT qt = QT(), qp = QP(), qn = QN(), tabs = TABS(), t = TT();
     T *gamaz = PR(P_GAMAZ), *pres = PR(P_PRES);
     const double an = 1. / (C_TBGMAX - C_TBGMIN), bn = C_TBGMIN * an;
     const double ap = 1. / (C_TPRMAX - C_TPRMIN), bp = C_TPRMIN * ap;
     const double fac1 = C_FAC_COND + (1 + bp) * C_FAC_FUS;
     const double fac2 = C_FAC_FUS * ap;
-    for (int e = TID; e < nx * nzm; e += NT) {
-      int i = 1 + e % nx, k = 1 + e / nx;
+    for (int e = TID; e < NH() * nzm; e += NT) {
+      int i = 1 + e % NH(), k = 1 + e / NH();
       if constexpr (sizeof(T) == 4) {
         // FP32-mixed form: a cell that is clearly unsaturated (total water
         // 0.1 % or more below saturation, far beyond FP32 rounding of qsat)
@@ -2310,16 +3067,16 @@ struct ColumnKernel : NxDim<NX> {
   // MICRO_SAM1MOM/precip_proc.F90:40-148; qpsrc/qpevp summed per level in
   // the reference's order from the per-cell contributions
   __device__ void precip_proc() {
-    F2<T> qt = QT(), qp = QP(), qn = QN(), tabs = TABS();
-    F2<T> csrc = SA(), cevp = SB();
+    FT qt = QT(), qp = QP(), qn = QN(), tabs = TABS();
+    FT csrc = SA(), cevp = SB();
     T *pres = PR(P_PRES);
     const T powr1 = (T)((3 + C_B_RAIN) / 4.), powr2 = (T)((5 + C_B_RAIN) / 8.);
     const T pows1 = (T)((3 + C_B_SNOW) / 4.), pows2 = (T)((5 + C_B_SNOW) / 8.);
     const T powg1 = (T)((3 + C_B_GRAU) / 4.), powg2 = (T)((5 + C_B_GRAU) / 8.);
     const T dtn = (T)S.dtn;
     const T a_bg = (T)p.a_bg, a_pr = (T)p.a_pr, a_gr = (T)p.a_gr;
-    for (int e = TID; e < nx * nzm; e += NT) {
-      int i = 1 + e % nx, k = 1 + e / nx;
+    for (int e = TID; e < NH() * nzm; e += NT) {
+      int i = 1 + e % NH(), k = 1 + e / NH();
       T q = qt(i, k), qpv = qp(i, k), qnv = qn(i, k), tb = tabs(i, k);
       T src = (T)0., evp = (T)0.;
       if (qnv + qpv > (T)0.) {
@@ -2408,10 +3165,10 @@ struct ColumnKernel : NxDim<NX> {
   // applied accel_factor more times; a |dT| above 5 K stops acceleration for
   // the rest of the call and stretches nstop so the call still spans dt_gl.
   __device__ void accelerate(int nstep) {
-    F2<T> t = TT(), qt = QT(), qv = QV(), qcl = QCL(), qci = QCI(), u = U(), v = V();
+    FT t = TT(), qt = QT(), qv = QV(), qcl = QCL(), qci = QCI(), u = U(), v = V();
     double *ta = reinterpret_cast<double *>(base + p.L.s_c);   // 4 x (nz + 2) FP64
     auto TA = [&](int q, int k) -> double & { return ta[(size_t)q * (nz + 2) + k]; };
-    const double coef = 1.0 / (double)nx;
+    const double coef = 1.0 / (double)NH();
     const int nq = p.accel_uv ? 4 : 2;
     if (TID == 0) S.acc_flag = 0;
     SYNC;
@@ -2443,8 +3200,8 @@ struct ColumnKernel : NxDim<NX> {
       return;
     }
     const T f = (T)p.accel_factor, tmin = (T)50.;
-    for (int e = TID; e < nx * nzm; e += NT) {
-      int i = 1 + e % nx, k = 1 + e / nx;
+    for (int e = TID; e < NH() * nzm; e += NT) {
+      int i = 1 + e % NH(), k = 1 + e / NH();
       t(i, k) = mx2(tmin, t(i, k) + f * (T)TA(0, k));
       if (p.accel_uv) {
         u(i, k) = u(i, k) + f * (T)TA(2, k);
@@ -2462,8 +3219,8 @@ struct ColumnKernel : NxDim<NX> {
                },
                [&](int, int) { return 0.; }, [&](int q, int k, double sv) { TA(q, k) = sv; });
     SYNC;
-    for (int e = TID; e < nx * nzm; e += NT) {
-      int i = 1 + e % nx, k = 1 + e / nx;
+    for (int e = TID; e < NH() * nzm; e += NT) {
+      int i = 1 + e % NH(), k = 1 + e / NH();
       const double qneg = TA(0, k), qpoz = TA(1, k);
       if (qpoz + qneg <= 0.) {
         qt(i, k) = (T)0.; qv(i, k) = (T)0.; qcl(i, k) = (T)0.; qci(i, k) = (T)0.;
@@ -2488,14 +3245,14 @@ struct ColumnKernel : NxDim<NX> {
   }
 
   __device__ void diagnose() {                 // diagnose.F90:21-85
-    F2<T> t = TT(), tabs = TABS(), qcl = QCL(), qci = QCI(), qpl = QPL(), qpi = QPI(), qv = QV(), u = U(), v = V();
+    FT t = TT(), tabs = TABS(), qcl = QCL(), qci = QCI(), qpl = QPL(), qpi = QPI(), qv = QV(), u = U(), v = V();
     T *gamaz = PR(P_GAMAZ);
-    for (int e = TID; e < nx * nzm; e += NT) {
-      int i = 1 + e % nx, k = 1 + e / nx;
+    for (int e = TID; e < NH() * nzm; e += NT) {
+      int i = 1 + e % NH(), k = 1 + e / NH();
       tabs(i, k) = t(i, k) - gamaz[k] + (T)C_FAC_COND * (qcl(i, k) + qpl(i, k)) + (T)C_FAC_SUB * (qci(i, k) + qpi(i, k));
     }
     SYNC;
-    const double coef = 1. / (double)nx;
+    const double coef = 1. / (double)NH();
     // domain means; q0 and qn0 are kept in FP64 in TMP0/TMP1 for qv0
     double *q0d = reinterpret_cast<double *>(sa());
     level_sums_lo_multi<7>(1, nzm,
@@ -2531,13 +3288,13 @@ struct ColumnKernel : NxDim<NX> {
   // ---------------------------------------------------------- step statistics
   // crm_module.F90:896-1073, accumulated every CRM step
   __device__ void step_stats() {
-    F2<T> qcl = QCL(), qci = QCI(), qpl = QPL(), qpi = QPI(), w = W(), tabs = TABS(), qv = QV();
+    FT qcl = QCL(), qci = QCI(), qpl = QPL(), qpi = QPI(), w = W(), tabs = TABS(), qv = QV();
     T *rho = PR(P_RHO), *adz = PR(P_ADZ), *pres = PR(P_PRES), *rhow = PR(P_RHOW);
-    T *cs = base + p.L.colstat;     // 5 x nx: cwp, cwph, cwpm, cwpl, top level
+    T *cs = base + p.L.colstat;     // 5 x NH(): cwp, cwph, cwpm, cwpl, top level
     const T dz = (T)S.dz;
     const T thr = (T)R4(0.001);
     // condensate paths from the top down, per CRM column (i)
-    for (int i = TID + 1; i <= nx; i += NT) {
+    for (int i = TID + 1; i <= NH(); i += NT) {
       T cwp = (T)0., cwph = (T)0., cwpm = (T)0., cwpl = (T)0.;
       int top = 0;
       for (int k = 1; k <= nzm; ++k) {
@@ -2549,8 +3306,8 @@ struct ColumnKernel : NxDim<NX> {
         else if (pres[kk] < (T)400.) cwph = cwph + tmp1;
         else cwpm = cwpm + tmp1;
       }
-      cs[(i - 1)] = cwp; cs[nx + (i - 1)] = cwph; cs[2 * nx + (i - 1)] = cwpm; cs[3 * nx + (i - 1)] = cwpl;
-      cs[4 * nx + (i - 1)] = (T)top;
+      cs[(i - 1)] = cwp; cs[NH() + (i - 1)] = cwph; cs[2 * NH() + (i - 1)] = cwpm; cs[3 * NH() + (i - 1)] = cwpl;
+      cs[4 * NH() + (i - 1)] = (T)top;
     }
     // cloudy mass flux of a cell at w level k (Xu et al. 2002): qsat > 0, so
     // a cell without condensate never passes the threshold and qsatw is
@@ -2571,15 +3328,15 @@ struct ColumnKernel : NxDim<NX> {
     };
     T *mui = OP(O_MUI), *mdi = OP(O_MDI);
     T *acc[8] = {OP(O_CLD), OP(O_CLDTOP), OP(O_MCUP), OP(O_MCDN), OP(O_MCUUP), OP(O_MCUDN), OP(O_GLIQWP), OP(O_GICEWP)};
-    const int nxr = p.L.nx_rad;
+    const int nxr = NR();
     T *rad = base + p.L.rad;
-    if (sizeof(T) == 4 && nxr == nx) {
+    if (sizeof(T) == 4 && nxr == NH()) {
       // FP32-mixed form, one radiation column per CRM column: the level
       // statistics, the mass fluxes at w levels 1..nzm and the radiation
       // sums in one pass (a warp per level, each cell visited once); the same
       // terms and FP32 warp reductions as the separate passes below
       SYNC;                                     // cloud tops (cs) complete
-      const size_t pl = (size_t)nx * nzm;
+      const size_t pl = (size_t)NH() * nzm;
       level_sums_lo_multi<10>(1, nzm,
                  [&](int, int, int) -> T { return (T)0.; },   // (FP64 form: not used)
                  [&](int i, int k, T *r) {
@@ -2587,7 +3344,7 @@ struct ColumnKernel : NxDim<NX> {
                    const bool cloudy = rho[k] * adz[k] * dz * (ql + qi) > thr;
                    const T ws = w(i, k + 1) + w(i, k), m = rho[k] * (T)0.5 * ws;
                    r[0] = cloudy ? (T)1.0 : (T)0.;
-                   r[1] = ((int)cs[4 * nx + (i - 1)] == k) ? (T)1. : (T)0.;
+                   r[1] = ((int)cs[4 * NH() + (i - 1)] == k) ? (T)1. : (T)0.;
                    r[2] = (cloudy && ws > (T)4.) ? m : (T)0.;
                    r[3] = (cloudy && ws < (T)-4.) ? m : (T)0.;
                    r[4] = (!cloudy && ws > (T)4.) ? m : (T)0.;
@@ -2595,7 +3352,7 @@ struct ColumnKernel : NxDim<NX> {
                    r[6] = ql;
                    r[7] = qi;
                    mass_flux(i, k, r[8], r[9]);
-                   const size_t o = (size_t)(k - 1) * nx + (i - 1);
+                   const size_t o = (size_t)(k - 1) * NH() + (i - 1);
                    const T st = rad[o] + tabs(i, k), sq = rad[pl + o] + mx2((T)0., qv(i, k));
                    const T sc = rad[2 * pl + o] + ql, si = rad[3 * pl + o] + qi;
                    const T sl = (ql + qi > (T)0) ? rad[4 * pl + o] + (T)1.0 : rad[4 * pl + o];
@@ -2616,9 +3373,9 @@ struct ColumnKernel : NxDim<NX> {
     } else {
       // interface mass fluxes (Xu et al. 2002): per-cell contributions at w
       // levels k = 1..nz, zero where a cell does not count
-      F2<T> cmu = SA(), cmd = SB();
-      for (int e = TID; e < nx * nz; e += NT) {
-        int i = 1 + e % nx, k = 1 + e / nx;
+      FT cmu = SA(), cmd = SB();
+      for (int e = TID; e < NH() * nz; e += NT) {
+        int i = 1 + e % NH(), k = 1 + e / NH();
         T cu, cd;
         mass_flux(i, k, cu, cd);
         cmu(i, k) = cu;
@@ -2631,7 +3388,7 @@ struct ColumnKernel : NxDim<NX> {
       // cloud fraction, cloud top counts, cloudy mass fluxes, water paths
       level_sums_lo_multi<8>(1, nzm,
                  [&](int q, int i, int k) -> T {
-                   if (q == 1) return ((int)cs[4 * nx + (i - 1)] == k) ? (T)1. : (T)0.;
+                   if (q == 1) return ((int)cs[4 * NH() + (i - 1)] == k) ? (T)1. : (T)0.;
                    if (q == 6) return qcl(i, k);
                    if (q == 7) return qci(i, k);
                    T tmp1 = rho[k] * adz[k] * dz;
@@ -2648,7 +3405,7 @@ struct ColumnKernel : NxDim<NX> {
                    const bool cloudy = rho[k] * adz[k] * dz * (ql + qi) > thr;
                    const T ws = w(i, k + 1) + w(i, k), m = rho[k] * (T)0.5 * ws;
                    r[0] = cloudy ? (T)1.0 : (T)0.;
-                   r[1] = ((int)cs[4 * nx + (i - 1)] == k) ? (T)1. : (T)0.;
+                   r[1] = ((int)cs[4 * NH() + (i - 1)] == k) ? (T)1. : (T)0.;
                    r[2] = (cloudy && ws > (T)4.) ? m : (T)0.;
                    r[3] = (cloudy && ws < (T)-4.) ? m : (T)0.;
                    r[4] = (!cloudy && ws > (T)4.) ? m : (T)0.;
@@ -2659,7 +3416,7 @@ struct ColumnKernel : NxDim<NX> {
                  [&](int q, int k) { return (double)acc[q][plev - k + 1]; },
                  [&](int q, int k, double sv) { acc[q][plev - k + 1] = (T)sv; });
       // radiation-group sums (crm_module.F90:1000-1028)
-      const int gx = nx / nxr;
+      const int gx = NH() / nxr;
       for (int e = TID; e < nxr * nzm; e += NT) {
         int ir = 1 + e % nxr, k = 1 + e / nxr;
         size_t o = (size_t)(k - 1) * nxr + (ir - 1);
@@ -2687,11 +3444,11 @@ struct ColumnKernel : NxDim<NX> {
         else anym = true;
       }
       int ct = 0, ch = 0, cm = 0, cl = 0;
-      for (int i = 1 + TID; i <= nx; i += 32) {
+      for (int i = 1 + TID; i <= NH(); i += 32) {
         ct += cs[(i - 1)] > thr;
-        ch += cs[nx + (i - 1)] > thr;
-        cm += cs[2 * nx + (i - 1)] > thr;
-        cl += cs[3 * nx + (i - 1)] > thr;
+        ch += cs[NH() + (i - 1)] > thr;
+        cm += cs[2 * NH() + (i - 1)] > thr;
+        cl += cs[3 * NH() + (i - 1)] > thr;
       }
       for (int o = 16; o > 0; o >>= 1) {
         ct += __shfl_xor_sync(0xffffffffu, ct, o);
@@ -2713,7 +3470,7 @@ struct ColumnKernel : NxDim<NX> {
   // crm_module.F90:1086-1594
   __device__ void finalize() {
     const int ld = p.ld;
-    const double factor_xy = 1.0 / (double)nx;
+    const double factor_xy = 1.0 / (double)NH();
     const double icrm_run_time = 1.0 / p.dt_gl;
     const double factor_xyt = factor_xy / (double)S.nstop;
     const int ptop = plev - nzm + 1;
@@ -2724,12 +3481,13 @@ struct ColumnKernel : NxDim<NX> {
       int f = CRM_OUT_FIRST_2D + e / plev, l = 1 + e % plev;
       O2(f, l) = 0.;
     }
-    F2<T> tabs = TABS(), qv = QV(), qcl = QCL(), qci = QCI(), qpl = QPL(), qpi = QPI(), u = U(), v = V(), w = W();
-    F2<T> qt = QT(), qp = QP(), qn = QN(), tk = TK(), tkh = TKH(), tke = TKE();
+    FT tabs = TABS(), qv = QV(), qcl = QCL(), qci = QCI(), qpl = QPL(), qpi = QPI(), u = U(), v = V(), w = W();
+    FT qt = QT(), qp = QP(), qn = QN(), tk = TK(), tkh = TKH(), tke = TKE();
     // radiation means
     {
-      const int nxr = p.L.nx_rad;
-      double tmp1 = ((double)nxr / (double)nx) * ((double)1 / (double)1) / (double)S.nstop;
+      const int nxr = NR();
+      // crm_nx_rad_fac * crm_ny_rad_fac / nstop (crm_module.F90:1080-1083)
+      double tmp1 = ((double)p.L.nx_rad / (double)nx) * ((double)p.L.ny_rad / (double)ny) / (double)S.nstop;
       T *rad = base + p.L.rad;
       for (int e = TID; e < nxr * nzm; e += NT) {
         int ir = 1 + e % nxr, k = 1 + e / nxr;
@@ -2776,18 +3534,18 @@ struct ColumnKernel : NxDim<NX> {
     // half a unit in the last place, which in a layer where nothing happens is
     // the same bias in every cell and does not average out.
     auto tabs_d = [&](int i, int k) -> double {
-      const size_t e = (size_t)(i - 1) + (size_t)nx * (k - 1);
+      const size_t e = (size_t)(i - 1) + (size_t)NH() * (k - 1);
       return ((double)TT()(i, k) + (double)rct()[e]) - (double)PR(P_GAMAZ)[k] +
              C_FAC_COND * ((double)qcl(i, k) + (double)qpl(i, k)) + C_FAC_SUB * ((double)qci(i, k) + (double)qpi(i, k));
     };
     auto qt_d = [&](int i, int k) -> double {
-      return (double)qt(i, k) + (double)rcq()[(size_t)(i - 1) + (size_t)nx * (k - 1)];
+      return (double)qt(i, k) + (double)rcq()[(size_t)(i - 1) + (size_t)NH() * (k - 1)];
     };
     if constexpr (sizeof(T) == 4) {
       const int lane = TID & 31, warp = TID >> 5, nw = NT >> 5;
       for (int k = 1 + warp; k <= nzm; k += nw) {
         double st = 0., sq = 0.;
-        for (int i = 1 + lane; i <= nx; i += 32) {
+        for (int i = 1 + lane; i <= NH(); i += 32) {
           st = st + tabs_d(i, k);
           sq = sq + (qt_d(i, k) - (double)qn(i, k));
         }
@@ -2878,8 +3636,8 @@ struct ColumnKernel : NxDim<NX> {
       O2(CRM_OUT_T_LS, l) = (double)PR(P_TTEND)[k];
     }
     // state and 4D outputs
-    for (int e = TID; e < nx * nzm; e += NT) {
-      int i = 1 + e % nx, k = 1 + e / nx;
+    for (int e = TID; e < NH() * nzm; e += NT) {
+      int i = 1 + e % NH(), k = 1 + e / NH();
       size_t o = S4(i, k);
       p.st[0][o] = (double)u(i, k);
       p.st[1][o] = (double)v(i, k);
@@ -2905,7 +3663,7 @@ struct ColumnKernel : NxDim<NX> {
       double cp = 0, cps = 0;
       for (int k = 1; k <= nzm; ++k) {
         double pdel = IN(p.pdel, plev - k + 1);
-        for (int i = 1; i <= nx; ++i) {
+        for (int i = 1; i <= NH(); ++i) {
           cp = cp + (double)(qpl(i, k) + qpi(i, k)) * pdel;
           cps = cps + (double)qpi(i, k) * pdel;
         }
@@ -2917,7 +3675,7 @@ struct ColumnKernel : NxDim<NX> {
       O1(CRM_OUT_TAUY) = 0.0 / (double)S.nstop;
       double precc = 0, precl = 0, precsc = 0, precsl = 0;
       const double thr = (double)(10.f / 86400.f);
-      for (int i = 1; i <= nx; ++i) {
+      for (int i = 1; i <= NH(); ++i) {
         double ps = (double)PS(i) * S.dz / p.dt / (double)S.nstop;
         double pss = (double)PSS(i) * S.dz / p.dt / (double)S.nstop;
         if (ps > thr) { precc = precc + ps; precsc = precsc + pss; }
@@ -2986,20 +3744,32 @@ struct ColumnKernel : NxDim<NX> {
         tke_full();
         PHASE_MARK(PH_TKE);
         boundaries(4);
-        advect_mom();
+        if constexpr (Y3) advect_mom3();
+        else advect_mom();
         PHASE_MARK(PH_ADVMOM);
-        diffuse_mom();
+        if constexpr (Y3) diffuse_mom3();
+        else diffuse_mom();
         PHASE_MARK(PH_DIFFMOM);
-        pressure(fsh, wsh);
+        if constexpr (Y3) pressure3(fsh);
+        else pressure(fsh, wsh);
         adams();
         boundaries(2);
         PHASE_MARK(PH_ADAMS);
-        advect_scalar(TT(), nullptr, nullptr, rct());
-        PHASE_MARK(PH_ADV_T);
-        advect_scalar(QT(), PR(P_MKADV0), PR(P_MKWLE0), rcq());
-        PHASE_MARK(PH_ADV_QT);
-        if (all_pos_zero(QP())) zero_stats(PR(P_MKADV1), PR(P_MKWLE1));
-        else advect_scalar(QP(), PR(P_MKADV1), PR(P_MKWLE1));
+        if constexpr (Y3) {
+          advect_scalar3(TT(), nullptr, nullptr, rct());
+          PHASE_MARK(PH_ADV_T);
+          advect_scalar3(QT(), PR(P_MKADV0), PR(P_MKWLE0), rcq());
+          PHASE_MARK(PH_ADV_QT);
+          if (all_pos_zero(QP())) zero_stats(PR(P_MKADV1), PR(P_MKWLE1));
+          else advect_scalar3(QP(), PR(P_MKADV1), PR(P_MKWLE1));
+        } else {
+          advect_scalar(TT(), nullptr, nullptr, rct());
+          PHASE_MARK(PH_ADV_T);
+          advect_scalar(QT(), PR(P_MKADV0), PR(P_MKWLE0), rcq());
+          PHASE_MARK(PH_ADV_QT);
+          if (all_pos_zero(QP())) zero_stats(PR(P_MKADV1), PR(P_MKWLE1));
+          else advect_scalar(QP(), PR(P_MKADV1), PR(P_MKWLE1));
+        }
         PHASE_MARK(PH_ADV_QP);
         precip_fall_1();
         PHASE_MARK(PH_FALL1);
@@ -3008,11 +3778,19 @@ struct ColumnKernel : NxDim<NX> {
         uvw();
         boundaries(3);
         PHASE_MARK(PH_UVW);
-        diffuse_scalar(TT(), nullptr, nullptr, rct());
-        PHASE_MARK(PH_DIFF_T);
-        diffuse_scalar(QT(), PR(P_MKDIFF0), PR(P_MKWSB0), rcq());
-        if (all_pos_zero(QP())) zero_stats(PR(P_MKDIFF1), PR(P_MKWSB1));
-        else diffuse_scalar(QP(), PR(P_MKDIFF1), PR(P_MKWSB1));
+        if constexpr (Y3) {
+          diffuse_scalar3(TT(), nullptr, nullptr, rct());
+          PHASE_MARK(PH_DIFF_T);
+          diffuse_scalar3(QT(), PR(P_MKDIFF0), PR(P_MKWSB0), rcq());
+          if (all_pos_zero(QP())) zero_stats(PR(P_MKDIFF1), PR(P_MKWSB1));
+          else diffuse_scalar3(QP(), PR(P_MKDIFF1), PR(P_MKWSB1));
+        } else {
+          diffuse_scalar(TT(), nullptr, nullptr, rct());
+          PHASE_MARK(PH_DIFF_T);
+          diffuse_scalar(QT(), PR(P_MKDIFF0), PR(P_MKWSB0), rcq());
+          if (all_pos_zero(QP())) zero_stats(PR(P_MKDIFF1), PR(P_MKWSB1));
+          else diffuse_scalar(QP(), PR(P_MKDIFF1), PR(P_MKWSB1));
+        }
         PHASE_MARK(PH_DIFF_Q);
         if (S.icycle == 1) precip_init();
         PHASE_MARK(PH_PINIT);
@@ -3047,28 +3825,44 @@ __host__ __device__ inline size_t crm_smem_bytes(int nx, int nzm, int block, int
   return sizeof(T) * e;
 }
 
-template <typename T, int NX, int NTH, int MINB, int SMP>
+// 3D: the Fourier coefficients live in the slab; shared memory holds one
+// transform row and one work row (2 max(nx, ny) + 8) per warp
+template <typename T>
+__host__ __device__ inline size_t crm_smem_bytes3(int nx, int ny, int block) {
+  const int nmax = nx > ny ? nx : ny;
+  return sizeof(T) * (size_t)(block / 32) * (size_t)(2 * nmax + 8);
+}
+
+template <typename T, int NX, int NY, int NTH, int MINB, int SMP>
 __global__ void __launch_bounds__(NTH, MINB) crm_columns_kernel(const __grid_constant__ KParams p) {
   __shared__ ColShared S;
   extern __shared__ __align__(16) unsigned char crm_dsm[];
   T *fsh = reinterpret_cast<T *>(crm_dsm);
   T *wsh = fsh + (size_t)(p.L.nx + 2) * p.L.nzm;
   T *planes = nullptr;
-  if (SMP) planes = fsh + crm_round64((size_t)(p.L.nx + 2) * p.L.nzm + (size_t)(NTH / 32) * (p.L.nx + 4));
+  if constexpr (SMP && NY == 1)
+    planes = fsh + crm_round64((size_t)(p.L.nx + 2) * p.L.nzm + (size_t)(NTH / 32) * (p.L.nx + 4));
   T *base = reinterpret_cast<T *>(p.slabs) + (size_t)blockIdx.x * p.L.slab;
   if (threadIdx.x == 0) S.gbar = 0;
   for (int col = blockIdx.x; col < p.ncrms; col += gridDim.x) {
-    ColumnKernel<T, NX> K(p, S, base, col, planes);
+    ColumnKernel<T, NX, NY> K(p, S, base, col, planes);
     K.run(fsh, wsh);
     __syncthreads();
   }
 }
 
-template <typename T, int NX, int SHAPE>
+template <typename T, int NX, int NY, int SHAPE>
+size_t crm_launch_smem(int nx, int ny, int nzm) {
+  constexpr int nth = kShapes[SHAPE].threads, smp = kShapes[SHAPE].smem_planes;
+  if constexpr (NY != 1) return crm_smem_bytes3<T>(nx, ny, nth);
+  else return crm_smem_bytes<T>(nx, nzm, nth, smp);
+}
+
+template <typename T, int NX, int NY, int SHAPE>
 void launch_crm_columns(const KParams &p, int grid, cudaStream_t s, bool cooperative) {
   constexpr int nth = kShapes[SHAPE].threads, minb = kShapes[SHAPE].min_ctas, smp = kShapes[SHAPE].smem_planes;
-  size_t smem = crm_smem_bytes<T>(p.L.nx, p.L.nzm, nth, smp);
-  auto kern = crm_columns_kernel<T, NX, nth, minb, smp>;
+  size_t smem = crm_launch_smem<T, NX, NY, SHAPE>(p.L.nx, p.L.ny, p.L.nzm);
+  auto kern = crm_columns_kernel<T, NX, NY, nth, minb, smp>;
   cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (cooperative) {
     // every CTA co-resident (the batch-mode grid barrier relies on it); the
@@ -3081,15 +3875,18 @@ void launch_crm_columns(const KParams &p, int grid, cudaStream_t s, bool coopera
   }
 }
 
-template <typename T, int NX, int SHAPE>
-int occupancy_crm_columns(int nx, int nzm) {
+// CTAs of the shape resident per SM (0: the shape does not fit); 3D runs
+// without shared-memory scratch planes, so those shapes report 0 there
+template <typename T, int NX, int NY, int SHAPE>
+int occupancy_crm_columns(int nx, int ny, int nzm) {
   constexpr int nth = kShapes[SHAPE].threads, minb = kShapes[SHAPE].min_ctas, smp = kShapes[SHAPE].smem_planes;
+  if (NY != 1 && smp) return 0;
   int n = 0;
-  size_t smem = crm_smem_bytes<T>(nx, nzm, nth, smp);
+  size_t smem = crm_launch_smem<T, NX, NY, SHAPE>(nx, ny, nzm);
   if (smem > 227 * 1024) return 0;
-  cudaFuncSetAttribute(crm_columns_kernel<T, NX, nth, minb, smp>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, crm_columns_kernel<T, NX, nth, minb, smp>, nth, smem) != cudaSuccess)
-    return 0;
+  auto kern = crm_columns_kernel<T, NX, NY, nth, minb, smp>;
+  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, nth, smem) != cudaSuccess) return 0;
   return n;
 }
 

@@ -20,7 +20,12 @@ struct KParams {
   int ifax[8];
   const double *trigs;      // fft trig table (3n/2 + 2 + n), REAL*4 values
   const float *trigs_f;     // the same values as float (exact: they are REAL*4)
-  const double *eign;       // (nx + 1) eigenvalues of the horizontal Laplacian
+  const double *eign;       // (nx + 1) x (ny + 2) eigenvalues of the horizontal Laplacian (2D: ny + 2 -> 1)
+  // the y transform of the 3D CRM (fft.F90 factors and REAL*4 trig table of ny)
+  int nfax_y;
+  int ifax_y[8];
+  const double *trigs_y;
+  const float *trigs_y_f;
   const double *z0;         // (ncrms) roughness length
   const double *rnd;        // (ncrms, 5, nx) setperturb draws 1 - 2 r
   // crm_input (device, Fortran (ld, *) order)
@@ -73,15 +78,16 @@ constexpr KShape kShapes[kNumShapes] = {{256, 3, 0}, {256, 4, 0}, {256, 4, 2}, {
 constexpr int kNumNx = 4;
 constexpr int kNxBuilt[kNumNx] = {32, 64, 128, 0};
 
-// One instantiation per (T, NX, shape) lives in its own object (crm_columns.cu).
-template <typename T, int NX, int SHAPE>
+// One instantiation per (T, NX, NY, shape) lives in its own object
+// (crm_columns.cu); NY = 1 is the 2D CRM, NY = 0 the generic 3D CRM.
+template <typename T, int NX, int NY, int SHAPE>
 void launch_crm_columns(const KParams &p, int grid, cudaStream_t s, bool cooperative);
-template <typename T, int NX, int SHAPE>
-int occupancy_crm_columns(int nx, int nzm);
+template <typename T, int NX, int NY, int SHAPE>
+int occupancy_crm_columns(int nx, int ny, int nzm);
 
-// Dispatch on (precision, nx, shape) at run time.
+// Dispatch on (precision, nx, ny, shape) at run time.
 void launch_columns(int precision, int shape, const KParams &p, int grid, cudaStream_t s,
                     bool cooperative = false);
-int occupancy_columns(int precision, int shape, int nx, int nzm);
+int occupancy_columns(int precision, int shape, int nx, int nzm, int ny = 1);
 
 }  // namespace crm

@@ -5,7 +5,9 @@
 // memory that stays resident in L1/L2 across the whole GCM step.  Index
 // ranges (halos included) are those of the reference's module arrays
 // (crm/grid.F90:31-46 with NADV = NADVS = 0, crm/vars.F90:200-238,
-// SGS_TKE/sgs.F90:50-60).  2D (ny = 1) only.
+// SGS_TKE/sgs.F90:50-60).  A 3D column (ny > 1) stores every field level
+// by level, each level nya rows of nxa (the y halos of the same module
+// arrays); ny = 1 gives the 2D layout, with no y halo.
 #pragma once
 #include <cstddef>
 
@@ -18,8 +20,11 @@ struct XRange {
 
 struct Layout {
   int nx, nzm, nz, plev, nx_rad;
+  int ny, ny_rad, yes3d, lnx;      // ny = 1 and yes3d = 0: 2D; lnx = log2 nx (3D)
   // x ranges
   XRange xu, xv, xw, xs, xd, xp, xi, xdu;
+  // y ranges (2D: {1, 1} each)
+  XRange yu, yv, yw, ys, yd, yp, yi, ydv, ysc;
   // offsets (in elements) of every array inside one column slab
   size_t u, v, w, t, qt, qp, tke, tk, tkh, p, tabs, qv, qcl, qci, qpl, qpi, qn;
   size_t du[3], dv[3], dw[3];
@@ -55,6 +60,7 @@ enum Prof {
   // reference divides per cell or keeps such arrays per routine)
   P_IADZ, P_IADZW, P_IRHO, P_IRHOADZ, P_IRHOWADZ, P_IRHOWADZW, P_RDZ, P_RDZW, P_MPDD,
   P_RDXZ, P_RDXW, P_BETDZ, P_TKMAX,   // SGS closure per-level factors
+  P_RDYZ, P_RDYW,                      // the same in y (3D)
   P_BETU, P_BETD, P_RUP, P_RDN, P_RHOWDADZW,   // buoyancy, pressure RHS, diffusion
   P_TMP0, P_TMP1, P_TMP2, P_TMP3, P_TMP4, P_TMP5, P_TMP6, P_TMP7,
   P_COUNT
@@ -67,9 +73,14 @@ enum OPlev {
 };
 
 // esz: bytes per element of the bulk type (8: FP64 form, 4: FP32-mixed)
-inline Layout make_layout(int nx, int nzm, int plev, int nx_rad, int esz) {
+inline Layout make_layout(int nx, int nzm, int plev, int nx_rad, int esz, int ny = 1, int ny_rad = 1) {
   Layout L{};
   L.nx = nx; L.nzm = nzm; L.nz = nzm + 1; L.plev = plev; L.nx_rad = nx_rad;
+  L.ny = ny; L.ny_rad = ny_rad;
+  const int Y = ny > 1 ? 1 : 0;
+  L.yes3d = Y;
+  L.lnx = 0;
+  while ((1 << L.lnx) < nx) ++L.lnx;
   L.xu = {-1, nx + 5};
   L.xv = {-1, nx + 4};
   L.xw = {-1, nx + 4};
@@ -78,48 +89,62 @@ inline Layout make_layout(int nx, int nzm, int plev, int nx_rad, int esz) {
   L.xp = {0, nx + 1};
   L.xi = {1, nx};
   L.xdu = {1, nx + 1};
+  // y extents of the same arrays (crm/grid.F90:31-46 with YES3D)
+  L.yu = {1 - 2 * Y, ny + 4 * Y};
+  L.yv = {1 - 2 * Y, ny + 5 * Y};
+  L.yw = {1 - 2 * Y, ny + 4 * Y};
+  L.ys = {1 - 3 * Y, ny + 6 * Y};
+  L.yd = {1 - Y, ny + 2 * Y};
+  L.yp = {1 - Y, ny + Y};
+  L.yi = {1, ny};
+  L.ydv = {1, ny + Y};
+  L.ysc = {1 - 3 * Y, ny + 6 * Y};
   size_t o = 0;
   auto take = [&](size_t n) { size_t r = o; o += (n + 63) / 64 * 64; return r; };
   const int nz = L.nz;
-  L.u = take((size_t)L.xu.nxa * nzm);
-  L.v = take((size_t)L.xv.nxa * nzm);
-  L.w = take((size_t)L.xw.nxa * nz);
-  L.t = take((size_t)L.xs.nxa * nzm);
-  L.qt = take((size_t)L.xs.nxa * nzm);
-  L.qp = take((size_t)L.xs.nxa * nzm);
-  L.tke = take((size_t)L.xi.nxa * nzm);
-  L.tk = take((size_t)L.xd.nxa * nzm);
-  L.tkh = take((size_t)L.xd.nxa * nzm);
-  L.p = take((size_t)L.xp.nxa * nzm);
-  L.tabs = take((size_t)nx * nzm);
-  L.qv = take((size_t)nx * nzm);
-  L.qcl = take((size_t)nx * nzm);
-  L.qci = take((size_t)nx * nzm);
-  L.qpl = take((size_t)nx * nzm);
-  L.qpi = take((size_t)nx * nzm);
-  L.qn = take((size_t)nx * nzm);
+  auto plane = [&](XRange x, XRange y) { return (size_t)x.nxa * y.nxa; };
+  L.u = take(plane(L.xu, L.yu) * nzm);
+  L.v = take(plane(L.xv, L.yv) * nzm);
+  L.w = take(plane(L.xw, L.yw) * nz);
+  L.t = take(plane(L.xs, L.ys) * nzm);
+  L.qt = take(plane(L.xs, L.ys) * nzm);
+  L.qp = take(plane(L.xs, L.ys) * nzm);
+  L.tke = take(plane(L.xi, L.yi) * nzm);
+  L.tk = take(plane(L.xd, L.yd) * nzm);
+  L.tkh = take(plane(L.xd, L.yd) * nzm);
+  L.p = take(plane(L.xp, L.yp) * nzm);
+  const size_t nh = (size_t)nx * ny;
+  L.tabs = take(nh * nzm);
+  L.qv = take(nh * nzm);
+  L.qcl = take(nh * nzm);
+  L.qci = take(nh * nzm);
+  L.qpl = take(nh * nzm);
+  L.qpi = take(nh * nzm);
+  L.qn = take(nh * nzm);
   for (int l = 0; l < 3; ++l) {
-    L.du[l] = take((size_t)L.xdu.nxa * nzm);
-    L.dv[l] = take((size_t)nx * nzm);
-    L.dw[l] = take((size_t)nx * nz);
+    L.du[l] = take(plane(L.xdu, L.yi) * nzm);
+    L.dv[l] = take(plane(L.xi, L.ydv) * nzm);
+    L.dw[l] = take(nh * nz);
   }
-  L.precsfc = take(nx);
-  L.precssfc = take(nx);
-  const size_t sc = (size_t)(nx + 6) * (nz + 1);
+  L.precsfc = take(nh);
+  L.precssfc = take(nh);
+  const size_t sc = (size_t)(nx + 6) * L.ysc.nxa * (nz + 1);
   L.s_a = take(sc); L.s_b = take(sc); L.s_c = take(sc); L.s_d = take(sc);
   L.s_e = take(sc); L.s_f = take(sc); L.s_g = take(sc); L.s_h = take(sc);
-  L.fft_f = take((size_t)(nx + 2) * (nzm + 1));
+  const size_t ny2 = Y ? (size_t)ny + 2 : 1;
+  L.fft_f = take((size_t)(nx + 2) * ny2 * (nzm + 1));
   L.fft_w = take((size_t)(nx + 4) * (nzm + 1));
   L.nprof = P_COUNT;
   L.prof = take((size_t)(nz + 2) * P_COUNT);
   L.n_oplev = O_COUNT;
   L.o_plev = take((size_t)(plev + 2) * O_COUNT);
-  L.rad = take((size_t)6 * nx_rad * nzm);
-  L.rnd = take((size_t)5 * nx);
-  L.colstat = take((size_t)8 * nx);
-  L.fcomp = esz == 4 ? take((size_t)2 * nx * nzm) : 0;
+  L.rad = take((size_t)6 * nx_rad * ny_rad * nzm);
+  L.rnd = take((size_t)5 * nh);
+  L.colstat = take((size_t)8 * nh);
+  L.fcomp = esz == 4 ? take((size_t)2 * nh * nzm) : 0;
   {
-    size_t nd = (size_t)(nzm + 1) + (size_t)(nx + 1) * 2 * (nzm + 1) + (size_t)(nx + 1);
+    const size_t np = (size_t)(nx + 1) * ny2;    // Fourier coefficients per level
+    size_t nd = (size_t)(nzm + 1) + np * 2 * (nzm + 1) + np;
     L.tri = take(nd * 8 / esz + 2);
   }
   L.slab = o;

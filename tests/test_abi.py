@@ -66,7 +66,7 @@ def test_create_without_device_fails_loudly(lib):
 
 
 def test_invalid_configurations_are_rejected(lib):
-    for kw in ({'crm_nx': 30}, {'crm_nx': 7}, {'plev': 20}, {'crm_dt': 40.0}):
+    for kw in ({'crm_nx': 30}, {'crm_nx': 7}, {'plev': 20}, {'crm_dt': 40.0}, {'crm_ny': 4}):
         cfg = S.config_32x28()
         cfg.max_ncrms = 4
         for k, v in kw.items():
@@ -75,7 +75,10 @@ def test_invalid_configurations_are_rejected(lib):
         h = lib.crm_create(C.byref(cfg.to_c()), C.byref(st))
         assert not h
         assert st.value in (T.CRM_ERR_ARG, T.CRM_ERR_UNSUPPORTED), kw
-    for kw in ({'crm_ny': 4}, {'microphysics': T.CRM_MICRO_M2005}):
+    # not built: 3D transform lengths with a factor 3 or 5, 3D radiation
+    # groups coarser than the CRM grid, the two-moment microphysics
+    for kw in ({'crm_ny': 12, 'crm_ny_rad': 12}, {'crm_ny': 16, 'crm_ny_rad': 8},
+               {'microphysics': T.CRM_MICRO_M2005}):
         cfg = S.config_32x28()
         cfg.max_ncrms = 4
         for k, v in kw.items():
