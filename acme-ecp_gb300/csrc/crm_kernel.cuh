@@ -151,6 +151,12 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
     if constexpr (Y3) return p.L.nx_rad * p.L.ny_rad;
     else return p.L.nx_rad;
   }
+  // the end-of-call sums of crm_module.F90:1034-1060 run i outer, j inner:
+  // the n-th cell (n = 1..NH()) of that order as a cell h = i + nx (j - 1)
+  __device__ __forceinline__ int h_ij(int n) const {
+    if constexpr (Y3) return (n - 1) / ny + 1 + nx * ((n - 1) % ny);
+    else return n;
+  }
   const KParams &p;
   ColShared &S;
   T *base;
@@ -1369,8 +1375,8 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
     FT tabs = TABS(), qv = QV(), qcl = QCL(), qci = QCI(), qpl = QPL(), qpi = QPI(), t = TT(), tkh = TKH();
     T *bet = PR(P_BET), *presi = PR(P_PRESI);
     const T epsv = (T)C_EPSV, fc = (T)C_FAC_COND, fs = (T)C_FAC_SUB, ff = (T)C_FAC_FUS;
-    for (int e = TID; e < nx * (nzm + 1); e += NT) {
-      int i = 1 + e % nx, k = e / nx;     // k = 0..nzm
+    for (int e = TID; e < NH() * (nzm + 1); e += NT) {
+      int i = 1 + e % NH(), k = e / NH();     // k = 0..nzm
       if (k == 0 || k == nzm) { buoy(i, k) = (T)0.; aprod(i, k) = (T)0.; continue; }
       int kc = k + 1, kb = k;
       T betdz = PR(P_BETDZ)[k];
@@ -1411,8 +1417,8 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
     const T Pr = (T)1.;
     const T dt = (T)p.dt;
     T *grdfx = PR(P_GRDFX), *grdfy = PR(P_GRDFY), *grdfz = PR(P_GRDFZ);
-    for (int e = TID; e < nx * (nzm - 1); e += NT) {
-      int i = 1 + e % nx, k = 1 + e / nx;
+    for (int e = TID; e < NH() * (nzm - 1); e += NT) {
+      int i = 1 + e % NH(), k = 1 + e / NH();
       T grd = dz * adz[k];
       T Ce1 = Ce / (T)R4(0.7) * (T)R4(0.19);
       T Ce2 = Ce / (T)R4(0.7) * (T)R4(0.51);
@@ -3498,12 +3504,15 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
     }
     SYNC;
     // horizontal sums of the final state per CRM level (FP64 scratch)
-    double *hs = reinterpret_cast<double *>(sa());    // 12 x (nz + 2)
+    double *hs = reinterpret_cast<double *>(sa());    // 14 x (nz + 2)
     auto HS = [&](int q, int k) -> double & { return hs[(size_t)q * (nz + 2) + k]; };
     {
       T *u0p = PR(P_U0), *v0p = PR(P_V0);
-      level_sums(12, 1, nzm,
+      // 3D: tln, qln, qccln, qiiln sum i outer, j inner; the condensate
+      // means (12, 13: qcl, qci) j outer like every other sum
+      level_sums(Y3 ? 14 : 12, 1, nzm,
                  [&](int q, int i, int k) -> T {
+                   if (q < 4) i = h_ij(i);
                    switch (q) {
                      case 0: return tabs(i, k);
                      case 1: return qv(i, k);
@@ -3522,7 +3531,9 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
                      case 8: { T d = v(i, k) - v0p[k]; return d * d; }
                      case 9: { T w1 = w(i, k + 1), w0 = w(i, k); return (T)0.5 * (w1 * w1 + w0 * w0); }
                      case 10: return tke(i, k);
-                     default: return tk(i, k);
+                     case 11: return tk(i, k);
+                     case 12: return qcl(i, k);
+                     default: return qci(i, k);
                    }
                  },
                  [&](int, int) { return 0.; }, [&](int q, int k, double sv) { HS(q, k) = sv; });
@@ -3598,7 +3609,7 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
     // flux and condensate profiles at CRM levels
     for (int k = TID + 1; k <= nzm; k += NT) {
       int l = plev - k + 1;
-      double qcm = HS(2, k), qim = HS(3, k), qrm = HS(4, k), qgm = HS(5, k), qsm = HS(6, k);
+      double qcm = HS(Y3 ? 12 : 2, k), qim = HS(Y3 ? 13 : 3, k), qrm = HS(4, k), qgm = HS(5, k), qsm = HS(6, k);
       double u2z = HS(7, k), v2z = HS(8, k), w2z = HS(9, k), stke = HS(10, k), stk = HS(11, k);
       O2(CRM_OUT_QC_MEAN, l) = qcm * factor_xy;
       O2(CRM_OUT_QI_MEAN, l) = qim * factor_xy;
@@ -3626,7 +3637,7 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
       O2(CRM_OUT_QP_TRANS, l) = mkadv1 + mkdiff1;
       double tkesgsz = rho * stke * factor_xy;
       O2(CRM_OUT_TKESGSZ, l) = tkesgsz;
-      O2(CRM_OUT_TKEZ, l) = rho * 0.5 * (u2z + v2z * 0.0 + w2z) * factor_xy + tkesgsz;
+      O2(CRM_OUT_TKEZ, l) = rho * 0.5 * (u2z + v2z * (Y3 ? 1.0 : 0.0) + w2z) * factor_xy + tkesgsz;
       O2(CRM_OUT_TKZ, l) = stk * factor_xy;
       O2(CRM_OUT_PRECFLUX, l) = ((double)PR(P_PRECFLUX)[k] * factor_xy * S.dz / p.dt / ns) / 1000.;
       O2(CRM_OUT_QP_FALL, l) = (double)PR(P_QPFALL)[k] * factor_xy * icrm_run_time;
@@ -3663,7 +3674,8 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
       double cp = 0, cps = 0;
       for (int k = 1; k <= nzm; ++k) {
         double pdel = IN(p.pdel, plev - k + 1);
-        for (int i = 1; i <= NH(); ++i) {
+        for (int n = 1; n <= NH(); ++n) {
+          const int i = h_ij(n);
           cp = cp + (double)(qpl(i, k) + qpi(i, k)) * pdel;
           cps = cps + (double)qpi(i, k) * pdel;
         }

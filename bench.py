@@ -168,6 +168,8 @@ def main():
                     help='duration of each serving window: the closed-loop peak and the 25/50/80/100%% '
                          'loads (0: skip serving)')
     ap.add_argument('--serve-steps', type=int, default=48, help='GCM steps per served chunk')
+    ap.add_argument('--steps-3d', type=int, default=2,
+                    help='timed steps of the 3D batch (256 columns of 32 x 32 x 58; 0: skip it)')
     ap.add_argument('--moist-steps', type=int, default=3,
                     help='timed steps of the moist 1024-column batch (0: skip it)')
     args = ap.parse_args()
@@ -215,14 +217,14 @@ def main():
     tuned = {}
     medians = {}        # median per-step time of each form on this rank [ms]
 
-    def device_rate(cfg, steps, warmup, work=None, tag=None):
+    def device_rate(cfg, steps, warmup, work=None, tag=None, tune=True):
         w_cin, w_st, w_rad, w_desc = work or (cin, st, rad, desc)
         tag = tag or ('fp64' if cfg.precision == T.CRM_FP64 else 'fp32')
         ctx = CrmContext(cfg)
         dev = DeviceCrmArrays(cfg, w_cin, w_st, w_rad, w_desc, w_desc._keep)
         stream = torch.cuda.current_stream().cuda_stream
         # launch shape chosen by the autotuner on this batch (untimed)
-        if args.autotune:
+        if args.autotune and tune:
             best, times = autotune(ctx, dev, w_st, reps=1, stream=stream)
             tuned[tag] = {'shape': best, 'ms_per_shape': {str(k): round(v, 2) for k, v in times.items()}}
         for _ in range(warmup):
@@ -311,12 +313,9 @@ def main():
         den = np.linalg.norm(b)
         return float(np.linalg.norm(a - b) / den) if den > 0 else float(np.linalg.norm(a - b))
 
-    def form_errors(d32, d64):
-        es, eo = {}, {}
-        for n in st.arrays():
-            es[n] = rel(d32.state_numpy(n)[:NCRMS].astype(np.float64), d64.state_numpy(n)[:NCRMS])
-        for n in T.CrmOutput(1, 64, 1, 58, 72).arrays():
-            eo[n] = rel(d32.out_numpy(n)[:NCRMS].astype(np.float64), d64.out_numpy(n)[:NCRMS])
+    def form_errors(d32, d64, n=NCRMS):
+        es = {k: rel(d32.state_numpy(k)[:n], d64.state_numpy(k)[:n]) for k in d32.state}
+        eo = {k: rel(d32.out_numpy(k)[:n], d64.out_numpy(k)[:n]) for k in d32.out}
         return es, eo
 
     errs, errs_out = form_errors(dev32, dev64)
@@ -343,6 +342,32 @@ def main():
                  'fp32_rel_l2_vs_fp64_tendencies': {n: meo[n] for n in ('sltend', 'qltend', 'qcltend', 'qiltend')},
                  'fp32_rel_l2_vs_fp64_state': mes, 'fp32_rel_l2_vs_fp64_outputs': meo}
         del mctx32, mdev32, mctx64, mdev64
+
+    # ---- the 3D CRM: 256 columns of 32 x 32 x 58 (dx = dy = 2 km), dt_gl
+    # 1200 s, the headline's soundings with a sheared v
+    three_d = None
+    if args.steps_3d > 0:
+        n3 = 256
+        f3, c3 = column_shard(ws * n3, rank, ws)
+        w3 = S.workload_3d(ncrms=c3, seed=f3, gcol0=f3 + 1, precision=T.CRM_FP32_MIXED)
+        cfg3, work3 = w3[0], w3[1:]
+        cfg3.max_ncrms = n3
+        cs3 = n3 * int(work3[3].dt_gl / cfg3.crm_dt)
+        ctx3, dev3, ms3, kms3 = device_rate(cfg3, args.steps_3d, 1, work3, 'fp32_3d')
+        cfg3d = S.config_3d(precision=T.CRM_FP64)
+        cfg3d.max_ncrms = n3
+        ctx3d, dev3d, ms3d, _ = device_rate(cfg3d, 1, 1, work3, 'fp64_3d', tune=False)
+        es3, eo3 = form_errors(dev3, dev3d, n3)
+        cells3 = cfg3.crm_nx * cfg3.crm_ny * cfg3.crm_nz
+        three_d = {'workload': '%d columns of %d x %d x %d, dx = dy = %.0f m, dt %.0f s, dt_gl %.0f s' %
+                               (n3, cfg3.crm_nx, cfg3.crm_ny, cfg3.crm_nz, cfg3.crm_dx, cfg3.crm_dt, work3[3].dt_gl),
+                   'value': ws * cs3 / (ms3 / 1000.0), 'unit': UNIT, 'ms_per_step': ms3,
+                   'kernel_ms': float(np.median(kms3)), 'steps': args.steps_3d,
+                   'cell_steps_per_s': ws * cs3 * cells3 / (ms3 / 1000.0),
+                   'fp64_value': ws * cs3 / (ms3d / 1000.0), 'fp64_ms_per_step': ms3d, 'fp64_steps': 1,
+                   'fp32_rel_l2_vs_fp64_state': es3,
+                   'fp32_rel_l2_vs_fp64_tendencies': {n: eo3[n] for n in ('sltend', 'qltend', 'qcltend', 'qiltend')}}
+        del ctx3, dev3, ctx3d, dev3d
 
     # ---- serving: Poisson chunks of mixed (nx, nz) at 80 % of the closed-loop peak
     serving = None
@@ -446,6 +471,7 @@ def main():
         'fp32_rel_l2_vs_fp64_outputs': errs_out,
         'serving': serving,
         'moist': moist,
+        'crm_3d': three_d,
         'launch_shapes': tuned,
     }
     print(json.dumps(line))

@@ -1,8 +1,8 @@
 /*
  * crm_gb300.h -- C ABI of the GB300-native superparameterized CRM step.
  *
- * One call advances ncrms embedded 2D cloud-resolving models (one per GCM
- * column) over one GCM timestep dt_gl, exactly like the Fortran entry
+ * One call advances ncrms embedded 2D or 3D cloud-resolving models (one per
+ * GCM column) over one GCM timestep dt_gl, exactly like the Fortran entry
  *
  *   subroutine crm(lchnk, icol, ncrms, dt_gl, plev, crm_input, crm_state,
  *                  crm_rad, crm_ecpp_output, crm_output)
@@ -62,7 +62,14 @@ enum crm_precision { CRM_FP64 = 0, CRM_FP32_MIXED = 1 };
 enum crm_batch_mode { CRM_PER_COLUMN = 0, CRM_REFERENCE_BATCH = 1 };
 
 /* Compile-time CPP constants of the reference (bld/configure:1883-1914,
- * crmdims.F90, domain.F90), passed at run time. */
+ * crmdims.F90, domain.F90), passed at run time.
+ *
+ * Built: crm_nx a power of two >= 8 (the device transform takes factors 2
+ * and 4); crm_ny = 1 (2D; crm_ny_rad = 1, crm_dy unused: dy = dx) or crm_ny
+ * a power of two >= 8 (3D; crm_dy > 0, or 0 for dy = dx), the 3D CRM with
+ * radiation on every CRM column (crm_nx_rad = crm_nx, crm_ny_rad = crm_ny).
+ * Other transform lengths and coarser 3D radiation groups give
+ * CRM_ERR_UNSUPPORTED. */
 typedef struct crm_config {
   int crm_nx, crm_ny, crm_nz;   /* CRM_NX, CRM_NY, CRM_NZ (ny == 1: 2D)  */
   int crm_nx_rad, crm_ny_rad;   /* radiation column groups               */
@@ -215,7 +222,8 @@ int crm_run_device(crm_ctx *ctx, const crm_call_desc *desc, const crm_input_c *i
  * kernel then runs with that many CTAs (fewer than crm_run_device uses, so
  * it is slower).  A call whose constants, per-column values and one slab do
  * not fit, or with crm_nx > CRM_NOALLOC_MAX_NX, returns CRM_ERR_TOO_LARGE
- * before touching the device.
+ * before touching the device.  The 3D CRM (crm_ny > 1) is taken by the
+ * handle entry points only: here it returns CRM_ERR_UNSUPPORTED.
  *
  * The array is part of the library's device code, so every device on which
  * the library's kernels are loaded holds these 32 MiB until the process exits,

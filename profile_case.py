@@ -4,7 +4,8 @@
         --precision fp32 --reps 2
 
 runs the 64 x 58 workload (--workload 64x58, the default; 32x28: 16-column
-sized one at dx 4 km, dt 20 s) on
+sized one at dx 4 km, dt 20 s; 3d: the 3D CRM, --nx x --ny x 58 at dx = dy
+= 2 km, dt 10 s) on
 device-resident arrays (crm_run_device) `reps` times and prints the kernel
 time of each call.  Sized so that a profiler capture of one launch ends in
 seconds.
@@ -24,7 +25,8 @@ def main():
     ap.add_argument('--precision', default='fp32', choices=['fp32', 'fp64'])
     ap.add_argument('--reps', type=int, default=2)
     ap.add_argument('--nx', type=int, default=64)
-    ap.add_argument('--workload', default='64x58', choices=['32x28', '64x58'])
+    ap.add_argument('--ny', type=int, default=32, help='3D workload: crm_ny')
+    ap.add_argument('--workload', default='64x58', choices=['32x28', '64x58', '3d'])
     ap.add_argument('--shape', type=int, default=None,
                     help='column-kernel launch shape index (crm_kernel.h kShapes)')
     ap.add_argument('--phase-timers', action='store_true',
@@ -43,6 +45,8 @@ def main():
     prec = T.CRM_FP32_MIXED if args.precision == 'fp32' else T.CRM_FP64
     if args.workload == '32x28':
         cfg, cin, st, rad, desc = S.workload_32x28(ncrms=args.ncrms, precision=prec)
+    elif args.workload == '3d':
+        cfg, cin, st, rad, desc = S.workload_3d(ncrms=args.ncrms, nx=args.nx, ny=args.ny, precision=prec)
     else:
         cfg, cin, st, rad, desc = S.workload_64x58(ncrms=args.ncrms, nx=args.nx, precision=prec)
     desc.dt_gl = args.dt_gl
