@@ -64,5 +64,62 @@ module crm_gb300_bind
       import :: c_ptr
       type(c_ptr), value :: h
     end subroutine
+
+    ! continuous batching (crm_server_create ... crm_poll in crm_gb300.h):
+    ! the chunk's CRM state stays on the device between GCM steps in place
+    ! of the physics-buffer round trip of crm_physics.F90:126-191
+    function crm_server_create(cfg, capacity, nhandles, hbm_budget_bytes, status) &
+        bind(C, name='crm_server_create') result(srv)
+      import :: c_ptr, c_int, c_long_long, crm_config_c
+      type(crm_config_c), intent(in)   :: cfg
+      integer(c_int), value            :: capacity, nhandles
+      integer(c_long_long), value      :: hbm_budget_bytes
+      integer(c_int), intent(out)      :: status
+      type(c_ptr) :: srv
+    end function
+    subroutine crm_server_destroy(srv) bind(C, name='crm_server_destroy')
+      import :: c_ptr
+      type(c_ptr), value :: srv
+    end subroutine
+    integer(c_int) function crm_chunk_open(srv, ncols, gcol, ld, st, rad, chunk) bind(C, name='crm_chunk_open')
+      import :: c_ptr, c_int, crm_state_c, crm_rad_c
+      type(c_ptr), value              :: srv
+      integer(c_int), value           :: ncols, ld
+      integer(c_int), intent(in)      :: gcol(*)
+      type(crm_state_c), intent(in)   :: st
+      type(crm_rad_c), intent(in)     :: rad
+      integer(c_int), intent(out)     :: chunk
+    end function
+    integer(c_int) function crm_chunk_read_state(srv, chunk, ld, st, qrad) bind(C, name='crm_chunk_read_state')
+      import :: c_ptr, c_int, crm_state_c
+      type(c_ptr), value              :: srv
+      integer(c_int), value           :: chunk, ld
+      type(crm_state_c), intent(in)   :: st
+      type(c_ptr), value              :: qrad
+    end function
+    integer(c_int) function crm_chunk_close(srv, chunk) bind(C, name='crm_chunk_close')
+      import :: c_ptr, c_int
+      type(c_ptr), value    :: srv
+      integer(c_int), value :: chunk
+    end function
+    integer(c_int) function crm_submit(srv, chunk, inp, qrad, ld, dt_gl, out, rad_means, col_status, ticket) &
+        bind(C, name='crm_submit')
+      import :: c_ptr, c_int, c_double, c_long_long, crm_input_c, crm_output_c
+      type(c_ptr), value               :: srv
+      integer(c_int), value            :: chunk, ld
+      type(crm_input_c), intent(in)    :: inp
+      type(c_ptr), value               :: qrad         ! c_null_ptr: keep the resident heating
+      real(c_double), value            :: dt_gl
+      type(crm_output_c), intent(in)   :: out
+      type(c_ptr), value               :: rad_means    ! c_loc(crm_rad_c) or c_null_ptr
+      type(c_ptr), value               :: col_status   ! c_loc(status(1)) or c_null_ptr
+      integer(c_long_long), intent(out) :: ticket
+    end function
+    integer(c_int) function crm_poll(srv, ticket, wait) bind(C, name='crm_poll')
+      import :: c_ptr, c_int, c_long_long
+      type(c_ptr), value          :: srv
+      integer(c_long_long), value :: ticket
+      integer(c_int), value       :: wait
+    end function
   end interface
 end module

@@ -141,6 +141,26 @@ def test_integration_fortran_binding_mirrors_the_header():
     assert n == len(T.OUTPUT_FIELDS)
 
 
+def test_fortran_binding_interfaces_are_exported(lib):
+    """Every bind(C, name=...) interface of the Fortran module names a
+    function the header declares and the library exports, with as many
+    arguments as the C prototype."""
+    doc = open(os.path.join(REPO, 'include', 'crm_gb300_bind.F90')).read()
+    hdr = re.sub(r'/\*.*?\*/', '', open(os.path.join(REPO, 'include', 'crm_gb300.h')).read(), flags=re.S)
+    names = re.findall(r"(?:function|subroutine)[ \t]+(\w+)[ \t]*\(([^)]*)\)[^\n]*(?:&\s*\n[^\n]*)?bind\(C, name='(\w+)'\)",
+                       doc)
+    assert {n for _, _, n in names} >= {'crm_create', 'crm_run', 'crm_destroy', 'crm_server_create',
+                                       'crm_submit', 'crm_poll', 'crm_chunk_open', 'crm_chunk_close'}
+    for fname, args, cname in names:
+        assert fname == cname
+        assert hasattr(lib, cname), cname
+        proto = re.search(r'\b%s\s*\(([^)]*)\)\s*;' % cname, hdr)
+        assert proto, cname
+        n_c = len([a for a in proto.group(1).split(',') if a.strip() and a.strip() != 'void'])
+        n_f = len([a for a in args.split(',') if a.strip()])
+        assert n_c == n_f, (cname, n_c, n_f)
+
+
 def test_launch_shape_table(lib):
     """The shape table the autotuner walks is readable without a device:
     whole warps, at most 1024 threads, register budgets that fit an SM
