@@ -1,14 +1,17 @@
-// crm_oracle.cpp -- CPU FP64 restatement of the reference crm() (2D,
+// crm_oracle.cpp -- CPU FP64 restatement of the reference crm() (2D and 3D,
 // sam1mom, SGS_TKE, MPDATA), used as the parity oracle of the GB300 library.
 //
 // TEST INFRASTRUCTURE ONLY: loaded by tests/, __graft_entry__.smoke() and the
 // CPU-baseline leg of bench.py.  The product never links or calls this file.
 //
-// PARITY UNPINNED: the reference ships no golden vectors or fixtures for
-// crm(), and its Fortran cannot be compiled here, so this restatement is not
-// checked against outputs of the reference itself; it is held to the
-// reference's conservation identities and to mathematical properties
-// (tests/test_oracle*.py, tests/test_gcm_coupling.py).
+// PARITY UNPINNED for the whole call: the reference ships no golden vectors
+// or fixtures for crm(), and its Fortran cannot be compiled here, so the
+// call's outputs are not checked against outputs of the reference itself;
+// they are held to the reference's conservation identities and to
+// mathematical properties (tests/test_oracle*.py, tests/test_gcm_coupling.py).
+// Two routines are pinned against values computed from the reference's own
+// source text: the sat.F90 saturation functions and the RNG_MT.F90 draws
+// (tests/golden/kat.json, tests/test_oracle_kat.py).
 //
 // Every routine follows the reference source named in its comment line by
 // line, including the Fortran numerics contract of the reference build:
