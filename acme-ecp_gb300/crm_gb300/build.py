@@ -10,6 +10,8 @@ Objects, compiled in parallel:
                   -ffp-contract=off for the same reason
   crm_serve.cu    the continuous-batching service of the C ABI (crm_submit,
                   crm_poll) over resident column slots
+  crm_tc_probe.cu crm_debug_tc_transform: the tensor-core transforms of the
+                  3D pressure solve on their own
 """
 import os
 import subprocess
@@ -30,7 +32,7 @@ COMMON = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC,-ffp-contract=o
 NUM_SHAPES = 6             # crm_kernel.h kShapes
 NX_BUILT = (32, 64, 128, 0)  # crm_kernel.h kNxBuilt (0: generic nx)
 UNITS = {'crm_prep': ('crm_prep', ['-fmad=false']), 'crm_host': ('crm_host', []),
-         'crm_serve': ('crm_serve', [])}
+         'crm_serve': ('crm_serve', []), 'crm_tc_probe': ('crm_tc_probe', [])}
 for _n in NX_BUILT:
     for _s in range(NUM_SHAPES):
         _d = ['-DCRM_INST_NX=%d' % _n, '-DCRM_INST_SHAPE=%d' % _s]

@@ -20,7 +20,8 @@ EXPORTS = ('crm_create', 'crm_destroy', 'crm_run', 'crm_run_device', 'crm_last_l
            'crm_launch_shape_info', 'crm_set_launch_shape', 'crm_get_launch_shape',
            'crm_device_bytes', 'crm_plan_device_bytes', 'crm_debug_barrier_test',
            'crm_server_create', 'crm_server_destroy', 'crm_server_device_bytes', 'crm_server_launches',
-           'crm_chunk_open', 'crm_chunk_read_state', 'crm_chunk_close', 'crm_submit', 'crm_poll')
+           'crm_chunk_open', 'crm_chunk_read_state', 'crm_chunk_close', 'crm_submit', 'crm_poll',
+           'crm_debug_tc_transform')
 
 _lib = None
 
@@ -107,6 +108,8 @@ def load(path=None, build_if_missing=False):
     lib.crm_device_bytes.argtypes = [C.c_void_p]
     lib.crm_plan_device_bytes.restype = C.c_int
     lib.crm_plan_device_bytes.argtypes = [C.POINTER(T.CCrmConfig), C.POINTER(C.c_ulonglong)]
+    lib.crm_debug_tc_transform.restype = C.c_int
+    lib.crm_debug_tc_transform.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)]
     lib.crm_debug_phase_cycles.restype = C.c_int
     lib.crm_debug_phase_cycles.argtypes = [C.c_void_p, C.POINTER(C.c_ulonglong), C.c_int]
     _lib = lib

@@ -22,5 +22,5 @@
 namespace crm {
 template void launch_crm_columns<CRM_INST_T, CRM_INST_NX, CRM_INST_NY, CRM_INST_SHAPE>(const KParams &, int, cudaStream_t,
                                                                                        bool);
-template int occupancy_crm_columns<CRM_INST_T, CRM_INST_NX, CRM_INST_NY, CRM_INST_SHAPE>(int, int, int);
+template int occupancy_crm_columns<CRM_INST_T, CRM_INST_NX, CRM_INST_NY, CRM_INST_SHAPE>(int, int, int, int);
 }  // namespace crm

@@ -23,6 +23,7 @@
 #include "../../include/crm_gb300.h"
 #include "../../include/crm_detmath.h"
 #include "crm_kernel.h"
+#include "crm_tc.cuh"
 
 using namespace crm_detmath;
 
@@ -34,6 +35,8 @@ struct crm_ctx {
   int device = 0, nsm = 0, shape = 0, grid_max = 0;
   int shape_grid[crm::kNumShapes] = {};   // co-resident CTAs per launch shape
   int slab_cap = 0;                         // slabs allocated (max over shapes)
+  int tc_n = 0;                             // 3D transforms on the tensor cores (n) or 0
+  float *d_dft = nullptr;                   // their matrices (inside d_consts)
   bool shape_auto = true;                   // choose the shape per call
   cudaStream_t stream = nullptr;
   bool own_stream = false;
@@ -100,23 +103,23 @@ static void launch_tn(int shape, const KParams &p, int grid, cudaStream_t s, boo
 }
 
 template <typename T, int NX, int NY>
-static int occupancy_tn(int shape, int nx, int ny, int nzm) {
+static int occupancy_tn(int shape, int nx, int ny, int nzm, int tc_n) {
   if constexpr (NY != 1) {
     switch (shape) {
-      case 0: return occupancy_crm_columns<T, NX, NY, 0>(nx, ny, nzm);
-      case 1: return occupancy_crm_columns<T, NX, NY, 1>(nx, ny, nzm);
-      case 3: return occupancy_crm_columns<T, NX, NY, 3>(nx, ny, nzm);
-      case 4: return occupancy_crm_columns<T, NX, NY, 4>(nx, ny, nzm);
+      case 0: return occupancy_crm_columns<T, NX, NY, 0>(nx, ny, nzm, tc_n);
+      case 1: return occupancy_crm_columns<T, NX, NY, 1>(nx, ny, nzm, tc_n);
+      case 3: return occupancy_crm_columns<T, NX, NY, 3>(nx, ny, nzm, tc_n);
+      case 4: return occupancy_crm_columns<T, NX, NY, 4>(nx, ny, nzm, tc_n);
       default: return 0;
     }
   }
   switch (shape) {
-    case 0: return occupancy_crm_columns<T, NX, NY, 0>(nx, ny, nzm);
-    case 1: return occupancy_crm_columns<T, NX, NY, 1>(nx, ny, nzm);
-    case 2: return occupancy_crm_columns<T, NX, NY, 2>(nx, ny, nzm);
-    case 3: return occupancy_crm_columns<T, NX, NY, 3>(nx, ny, nzm);
-    case 4: return occupancy_crm_columns<T, NX, NY, 4>(nx, ny, nzm);
-    default: return occupancy_crm_columns<T, NX, NY, 5>(nx, ny, nzm);
+    case 0: return occupancy_crm_columns<T, NX, NY, 0>(nx, ny, nzm, tc_n);
+    case 1: return occupancy_crm_columns<T, NX, NY, 1>(nx, ny, nzm, tc_n);
+    case 2: return occupancy_crm_columns<T, NX, NY, 2>(nx, ny, nzm, tc_n);
+    case 3: return occupancy_crm_columns<T, NX, NY, 3>(nx, ny, nzm, tc_n);
+    case 4: return occupancy_crm_columns<T, NX, NY, 4>(nx, ny, nzm, tc_n);
+    default: return occupancy_crm_columns<T, NX, NY, 5>(nx, ny, nzm, tc_n);
   }
 }
 
@@ -136,13 +139,13 @@ static void launch_t(int shape, const KParams &p, int grid, cudaStream_t s, bool
 }
 
 template <typename T>
-static int occupancy_t(int shape, int nx, int nzm, int ny) {
-  if (ny > 1) return occupancy_tn<T, 0, 0>(shape, nx, ny, nzm);
+static int occupancy_t(int shape, int nx, int nzm, int ny, int tc_n) {
+  if (ny > 1) return occupancy_tn<T, 0, 0>(shape, nx, ny, nzm, tc_n);
   switch (nx) {
-    case 32: return occupancy_tn<T, 32, 1>(shape, nx, 1, nzm);
-    case 64: return occupancy_tn<T, 64, 1>(shape, nx, 1, nzm);
-    case 128: return occupancy_tn<T, 128, 1>(shape, nx, 1, nzm);
-    default: return occupancy_tn<T, 0, 1>(shape, nx, 1, nzm);
+    case 32: return occupancy_tn<T, 32, 1>(shape, nx, 1, nzm, 0);
+    case 64: return occupancy_tn<T, 64, 1>(shape, nx, 1, nzm, 0);
+    case 128: return occupancy_tn<T, 128, 1>(shape, nx, 1, nzm, 0);
+    default: return occupancy_tn<T, 0, 1>(shape, nx, 1, nzm, 0);
   }
 }
 
@@ -151,10 +154,65 @@ void launch_columns(int precision, int shape, const KParams &p, int grid, cudaSt
   else launch_t<float>(shape, p, grid, s, coop);
 }
 
-int occupancy_columns(int precision, int shape, int nx, int nzm, int ny) {
-  return precision == CRM_FP64 ? occupancy_t<double>(shape, nx, nzm, ny) : occupancy_t<float>(shape, nx, nzm, ny);
+int occupancy_columns(int precision, int shape, int nx, int nzm, int ny, int tc_n) {
+  return precision == CRM_FP64 ? occupancy_t<double>(shape, nx, nzm, ny, tc_n)
+                               : occupancy_t<float>(shape, nx, nzm, ny, tc_n);
 }
 }  // namespace crm
+
+namespace crm_tc_host {
+// floats of the transform matrices of length n: forward (n+2 rounded up to
+// 16 rows, n columns), inverse (n rows, n+2 rounded up to 8 columns)
+size_t dft_elems(int n) {
+  if (!n) return 0;
+  const crm::tc::Dims d(n);
+  return (size_t)d.nf * n + (size_t)n * d.ki;
+}
+// The real transform of length n as matrices (fft991's output order and
+// scaling, crm/fft.F90): forward Bf[2k][i] = cos(2 pi i k / n) / n,
+// Bf[2k+1][i] = -sin(2 pi i k / n) / n; inverse Bi[i][2k] = w_k cos,
+// Bi[i][2k+1] = -w_k sin, w_0 = w_n/2 = 1, else 2; Im X_0 and Im X_n/2 rows
+// and columns exactly zero; the padding zero.  Angles reduced exactly
+// (i k mod n) before the trigonometry, in FP64.
+void dft_matrices(float *out, int n) {
+  const crm::tc::Dims d(n);
+  const double pi = 3.14159265358979323846;
+  auto cs = [&](int m, double &c, double &sn) {
+    m %= n;
+    if (m == 0) { c = 1.; sn = 0.; return; }
+    if (2 * m == n) { c = -1.; sn = 0.; return; }
+    if (4 * m == n) { c = 0.; sn = 1.; return; }
+    if (4 * m == 3 * n) { c = 0.; sn = -1.; return; }
+    c = cos(2. * pi * m / n);
+    sn = sin(2. * pi * m / n);
+  };
+  float *bf = out, *bi = out + (size_t)d.nf * n;
+  for (int r = 0; r < d.nf; ++r)
+    for (int i = 0; i < n; ++i) {
+      double v = 0.;
+      if (r < n + 2) {
+        const int k = r / 2;
+        double c, sn;
+        cs(i * k, c, sn);
+        v = (r % 2 == 0) ? c / n : -sn / n;
+      }
+      bf[(size_t)r * n + i] = (float)v;
+    }
+  for (int i = 0; i < n; ++i)
+    for (int col = 0; col < d.ki; ++col) {
+      double v = 0.;
+      if (col < n + 2) {
+        const int k = col / 2;
+        const double w = (k == 0 || 2 * k == n) ? 1. : 2.;
+        double c, sn;
+        cs(i * k, c, sn);
+        v = (col % 2 == 0) ? w * c : -w * sn;
+      }
+      bi[(size_t)i * d.ki + col] = (float)v;
+    }
+}
+
+}  // namespace crm_tc_host
 
 namespace {
 
@@ -348,6 +406,19 @@ void micro_consts(crm::KParams &p) {
   p.a_gr = 1. / (R4H(283.16) - R4H(223.16));
 }
 
+// The 3D FP32-mixed form with nx = ny in {16, 32} runs the transforms of the
+// pressure solve on the tensor cores; CRM_GB300_TRANSFORM=fft keeps the warp
+// FFT there.
+int tc_n_of(const crm_config &g) {
+  if (g.precision != CRM_FP32_MIXED || g.crm_ny <= 1 || g.crm_nx != g.crm_ny) return 0;
+  if (g.crm_nx != 16 && g.crm_nx != 32) return 0;
+  const char *e = getenv("CRM_GB300_TRANSFORM");
+  if (e && strcmp(e, "fft") == 0) return 0;
+  return g.crm_nx;
+}
+using crm_tc_host::dft_elems;
+using crm_tc_host::dft_matrices;
+
 // Sizes of a handle's device buffers, decided without allocating: the slab
 // count is the largest co-resident CTA count over the launch shapes (so the
 // shape can change per call), capped at max_ncrms.
@@ -357,9 +428,10 @@ int plan_ctx(crm_ctx *c) {
   CK(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, c->device));
   const size_t esz = g.precision == CRM_FP64 ? sizeof(double) : sizeof(float);
   c->L = crm::make_layout(g.crm_nx, g.crm_nz, g.plev, g.crm_nx_rad, (int)esz, g.crm_ny, g.crm_ny_rad);
+  c->tc_n = tc_n_of(g);
   c->slab_cap = 0;
   for (int s = 0; s < crm::kNumShapes; ++s) {
-    int per = crm::occupancy_columns(g.precision, s, g.crm_nx, g.crm_nz, g.crm_ny);
+    int per = crm::occupancy_columns(g.precision, s, g.crm_nx, g.crm_nz, g.crm_ny, c->tc_n);
     int grid = per > 0 ? c->nsm * per : 0;
     if (grid > g.max_ncrms) grid = g.max_ncrms;
     c->shape_grid[s] = grid;
@@ -376,7 +448,7 @@ size_t handle_bytes(const crm_ctx *c) {
   const crm_config &g = c->cfg;
   const size_t ld = (size_t)c->ld_cap, nt = n_trigs(g.crm_nx), nty = g.crm_ny > 1 ? n_trigs(g.crm_ny) : 0;
   size_t b = c->slab_bytes * (size_t)c->slab_cap;
-  b += sizeof(double) * (nt + n_eigen(g) + (nt + 1) / 2 + nty + (nty + 1) / 2);
+  b += sizeof(double) * (nt + n_eigen(g) + (nt + 1) / 2 + nty + (nty + 1) / 2 + (dft_elems(c->tc_n) + 1) / 2);
   b += sizeof(double) * ld * (1 + 5 * (size_t)g.crm_nx * g.crm_ny);
   b += sizeof(int) * ld + 8 * sizeof(unsigned long long);
   return b;
@@ -413,7 +485,8 @@ int alloc_ctx(crm_ctx *c) {
   // in 3D the y table as FP64 and as float
   const size_t nt = c->trigs.size(), ne = c->eign.size(), ntf = (nt + 1) / 2;
   const size_t nty = c->trigs_y.size(), ntyf = (nty + 1) / 2;
-  CK(cudaMalloc(&c->d_consts, sizeof(double) * (nt + ne + ntf + nty + ntyf)));
+  const size_t ndft = dft_elems(c->tc_n), ndftd = (ndft + 1) / 2;
+  CK(cudaMalloc(&c->d_consts, sizeof(double) * (nt + ne + ntf + nty + ntyf + ndftd)));
   CK(cudaMemcpy(c->d_consts, c->trigs.data(), sizeof(double) * nt, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(c->d_consts + nt, c->eign.data(), sizeof(double) * ne, cudaMemcpyHostToDevice));
   {
@@ -427,6 +500,12 @@ int alloc_ctx(crm_ctx *c) {
     std::vector<float> tf(nty);
     for (size_t i = 0; i < nty; ++i) tf[i] = (float)c->trigs_y[i];
     CK(cudaMemcpy(dy + nty, tf.data(), sizeof(float) * nty, cudaMemcpyHostToDevice));
+  }
+  if (ndft) {
+    std::vector<float> m(ndft);
+    dft_matrices(m.data(), c->tc_n);
+    c->d_dft = reinterpret_cast<float *>(c->d_consts + nt + ne + ntf + nty + ntyf);
+    CK(cudaMemcpy(c->d_dft, m.data(), sizeof(float) * ndft, cudaMemcpyHostToDevice));
   }
   CK(cudaMalloc(&c->d_colconst, sizeof(double) * (size_t)ld * (1 + 5 * (size_t)nx * ny)));
   CK(cudaMalloc(&c->d_status, sizeof(int) * (size_t)ld));
@@ -533,6 +612,8 @@ int build_params(crm_ctx *c, const crm_call_desc *d, const crm_input_c *in, crm_
     p.trigs_y = c->d_consts + c->trigs.size() + c->eign.size() + (c->trigs.size() + 1) / 2;
     p.trigs_y_f = reinterpret_cast<const float *>(p.trigs_y + c->trigs_y.size());
   }
+  p.tc_n = c->tc_n;
+  p.dft_tc = c->d_dft;
   p.z0 = pp.z0;
   p.rnd = pp.rnd;
   p.zmid = in->zmid; p.zint = in->zint; p.tl = in->tl; p.ql = in->ql; p.qccl = in->qccl;

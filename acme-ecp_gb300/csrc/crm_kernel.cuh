@@ -17,6 +17,7 @@
 #pragma once
 #include "crm_device.cuh"
 #include "crm_kernel.h"
+#include "crm_tc.cuh"
 
 namespace crm {
 
@@ -106,6 +107,10 @@ struct ColShared {
   unsigned long long t_last;
   double red_d[32];
   int red_i[64];
+  // tensor-core transforms of the 3D pressure solve (crm_tc.cuh)
+  unsigned long long tc_mbar;
+  unsigned tc_tmem, tc_phase;
+  int tc_fail;
 };
 
 // The CRM's horizontal size: a compile-time constant for the sizes built
@@ -2000,7 +2005,7 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
   // then columns in y (every x coefficient i = 1..nx+1) through its own
   // shared-memory row and work buffers; one FP64 tridiagonal solve per
   // (i, j) coefficient; the inverse transforms in the reverse order
-  __device__ void pressure3(T *wsh) {
+  __device__ void pressure3(T *wsh, float *tcsm) {
     FT u = U(), v = V(), w = W(), pp = PP();
     FT dua = DU(S.na), dub = DU(S.nb), duc = DU(S.nc);
     FT dva = DV(S.na), dvb = DV(S.nb), dvc = DV(S.nc);
@@ -2067,10 +2072,19 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
       }
       fdir = 0;
     };
-    xrows(-1);
-    SYNC;
-    ycols(-1);
-    SYNC;
+    bool tcp = false;   // FP32-mixed, nx = ny in {16, 32}: the tensor-core transforms
+    if constexpr (sizeof(T) == 4) tcp = p.tc_n != 0;
+    if (tcp) {
+      if constexpr (sizeof(T) == 4) {
+        tc::Engine E(p.tc_n, tcsm, S.tc_tmem, tc::smem_u32(&S.tc_mbar), &S.tc_phase, &S.tc_fail, TID, NT);
+        for (int k0 = 1; k0 <= nzm; k0 += E.d.L) E.forward_tile(FF, k0, nzm);
+      }
+    } else {
+      xrows(-1);
+      SYNC;
+      ycols(-1);
+      SYNC;
+    }
     PHASE_MARK(PH_FFT_FWD);
     // vertical tridiagonal solve per coefficient c = (i-1) + (nx+1)(j-1), in FP64
     {
@@ -2099,10 +2113,18 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
     }
     SYNC;
     PHASE_MARK(PH_TRIDIAG);
-    ycols(+1);
-    SYNC;
-    xrows(+1);
-    SYNC;
+    if (tcp) {
+      if constexpr (sizeof(T) == 4) {
+        tc::Engine E(p.tc_n, tcsm, S.tc_tmem, tc::smem_u32(&S.tc_mbar), &S.tc_phase, &S.tc_fail, TID, NT);
+        for (int k0 = 1; k0 <= nzm; k0 += E.d.L) E.inverse_tile(FF, k0, nzm);
+        if (TID == 0 && S.tc_fail && S.status == CRM_OK) S.status = CRM_ERR_TIMEOUT;
+      }
+    } else {
+      ycols(+1);
+      SYNC;
+      xrows(+1);
+      SYNC;
+    }
     PHASE_MARK(PH_FFT_INV);
     for (int e = TID; e < (nx + 1) * (ny + 1) * nzm; e += NT) {
       const int i = e % (nx + 1), j = (e / (nx + 1)) % (ny + 1), k = 1 + e / ((nx + 1) * (ny + 1));
@@ -3714,7 +3736,7 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
   // ---------------------------------------------------------- one column
   // Inlined into the kernel: as a separate function its register allocation
   // spilled around the call (12 % slower in the FP32-mixed form).
-  __device__ __forceinline__ void run(T *fsh, T *wsh) {
+  __device__ __forceinline__ void run(T *fsh, T *wsh, float *tcsm = nullptr) {
     if (icrm < 0 || icrm >= p.ld) {            // bad slot in col_map: no access
       if (TID == 0) p.col_status[cpos] = CRM_ERR_ARG;
       return;
@@ -3762,7 +3784,7 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
         if constexpr (Y3) diffuse_mom3();
         else diffuse_mom();
         PHASE_MARK(PH_DIFFMOM);
-        if constexpr (Y3) pressure3(fsh);
+        if constexpr (Y3) pressure3(fsh, tcsm);
         else pressure(fsh, wsh);
         adams();
         boundaries(2);
@@ -3839,10 +3861,13 @@ __host__ __device__ inline size_t crm_smem_bytes(int nx, int nzm, int block, int
 
 // 3D: the Fourier coefficients live in the slab; shared memory holds one
 // transform row and one work row (2 max(nx, ny) + 8) per warp
+// (with the tensor-core transforms, tc_n != 0, their operands instead)
 template <typename T>
-__host__ __device__ inline size_t crm_smem_bytes3(int nx, int ny, int block) {
+__host__ __device__ inline size_t crm_smem_bytes3(int nx, int ny, int block, int tc_n = 0) {
   const int nmax = nx > ny ? nx : ny;
-  return sizeof(T) * (size_t)(block / 32) * (size_t)(2 * nmax + 8);
+  const size_t fft = sizeof(T) * (size_t)(block / 32) * (size_t)(2 * nmax + 8);
+  const size_t tcb = tc::smem_bytes(tc_n);
+  return fft > tcb ? fft : tcb;
 }
 
 template <typename T, int NX, int NY, int NTH, int MINB, int SMP>
@@ -3856,24 +3881,57 @@ __global__ void __launch_bounds__(NTH, MINB) crm_columns_kernel(const __grid_con
     planes = fsh + crm_round64((size_t)(p.L.nx + 2) * p.L.nzm + (size_t)(NTH / 32) * (p.L.nx + 4));
   T *base = reinterpret_cast<T *>(p.slabs) + (size_t)blockIdx.x * p.L.slab;
   if (threadIdx.x == 0) S.gbar = 0;
+  float *tcsm = nullptr;
+  if constexpr (NY != 1 && sizeof(T) == 4) {
+    if (p.tc_n) {
+      // tensor memory for the transforms' accumulator (warp 0), the
+      // mbarrier their commits arrive on, the constant matrices split into
+      // TF32 head and tail
+      tcsm = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(crm_dsm) + 127) & ~(uintptr_t)127);
+      if (threadIdx.x < 32) {
+        tc::tmem_alloc(tc::smem_u32(&S.tc_tmem), tc::kTmemCols);
+        tc::fence_before();
+      }
+      if (threadIdx.x == 0) {
+        tc::mbar_init(tc::smem_u32(&S.tc_mbar));
+        S.tc_phase = 0;
+        S.tc_fail = 0;
+      }
+      tc::Engine(p.tc_n, tcsm, 0u, 0u, nullptr, nullptr, threadIdx.x, NTH).load_mats(p.dft_tc);
+      __syncthreads();
+      tc::fence_after();
+    }
+  }
   for (int col = blockIdx.x; col < p.ncrms; col += gridDim.x) {
     ColumnKernel<T, NX, NY> K(p, S, base, col, planes);
-    K.run(fsh, wsh);
+    K.run(fsh, wsh, tcsm);
     __syncthreads();
+  }
+  if constexpr (NY != 1 && sizeof(T) == 4) {
+    if (p.tc_n) {
+      // a commit that outlived its wait is awaited (bounded) before the
+      // accumulator is released
+      if (threadIdx.x == 0 && S.tc_fail) tc::mbar_wait(tc::smem_u32(&S.tc_mbar), S.tc_phase ^ 1u, tc::kWaitLimit);
+      __syncthreads();
+      if (threadIdx.x < 32) {
+        tc::fence_after();
+        tc::tmem_free(S.tc_tmem, tc::kTmemCols);
+      }
+    }
   }
 }
 
 template <typename T, int NX, int NY, int SHAPE>
-size_t crm_launch_smem(int nx, int ny, int nzm) {
+size_t crm_launch_smem(int nx, int ny, int nzm, int tc_n) {
   constexpr int nth = kShapes[SHAPE].threads, smp = kShapes[SHAPE].smem_planes;
-  if constexpr (NY != 1) return crm_smem_bytes3<T>(nx, ny, nth);
+  if constexpr (NY != 1) return crm_smem_bytes3<T>(nx, ny, nth, sizeof(T) == 4 ? tc_n : 0);
   else return crm_smem_bytes<T>(nx, nzm, nth, smp);
 }
 
 template <typename T, int NX, int NY, int SHAPE>
 void launch_crm_columns(const KParams &p, int grid, cudaStream_t s, bool cooperative) {
   constexpr int nth = kShapes[SHAPE].threads, minb = kShapes[SHAPE].min_ctas, smp = kShapes[SHAPE].smem_planes;
-  size_t smem = crm_launch_smem<T, NX, NY, SHAPE>(p.L.nx, p.L.ny, p.L.nzm);
+  size_t smem = crm_launch_smem<T, NX, NY, SHAPE>(p.L.nx, p.L.ny, p.L.nzm, p.tc_n);
   auto kern = crm_columns_kernel<T, NX, NY, nth, minb, smp>;
   cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (cooperative) {
@@ -3890,11 +3948,11 @@ void launch_crm_columns(const KParams &p, int grid, cudaStream_t s, bool coopera
 // CTAs of the shape resident per SM (0: the shape does not fit); 3D runs
 // without shared-memory scratch planes, so those shapes report 0 there
 template <typename T, int NX, int NY, int SHAPE>
-int occupancy_crm_columns(int nx, int ny, int nzm) {
+int occupancy_crm_columns(int nx, int ny, int nzm, int tc_n) {
   constexpr int nth = kShapes[SHAPE].threads, minb = kShapes[SHAPE].min_ctas, smp = kShapes[SHAPE].smem_planes;
   if (NY != 1 && smp) return 0;
   int n = 0;
-  size_t smem = crm_launch_smem<T, NX, NY, SHAPE>(nx, ny, nzm);
+  size_t smem = crm_launch_smem<T, NX, NY, SHAPE>(nx, ny, nzm, tc_n);
   if (smem > 227 * 1024) return 0;
   auto kern = crm_columns_kernel<T, NX, NY, nth, minb, smp>;
   cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

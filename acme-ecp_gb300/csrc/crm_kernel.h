@@ -26,6 +26,12 @@ struct KParams {
   int ifax_y[8];
   const double *trigs_y;
   const float *trigs_y_f;
+  // 3D FP32-mixed form with nx = ny in {16, 32}: the transforms of the
+  // pressure solve on the tensor cores (crm_tc.cuh); tc_n = nx, dft_tc the
+  // forward ((n+2 rounded up to 16) x n) and inverse (n x (n+2 rounded up to
+  // 8)) transform matrices, row-major; tc_n = 0: the warp FFT
+  int tc_n;
+  const float *dft_tc;
   const double *z0;         // (ncrms) roughness length
   const double *rnd;        // (ncrms, 5, nx) setperturb draws 1 - 2 r
   // crm_input (device, Fortran (ld, *) order)
@@ -83,11 +89,11 @@ constexpr int kNxBuilt[kNumNx] = {32, 64, 128, 0};
 template <typename T, int NX, int NY, int SHAPE>
 void launch_crm_columns(const KParams &p, int grid, cudaStream_t s, bool cooperative);
 template <typename T, int NX, int NY, int SHAPE>
-int occupancy_crm_columns(int nx, int ny, int nzm);
+int occupancy_crm_columns(int nx, int ny, int nzm, int tc_n);
 
 // Dispatch on (precision, nx, ny, shape) at run time.
 void launch_columns(int precision, int shape, const KParams &p, int grid, cudaStream_t s,
                     bool cooperative = false);
-int occupancy_columns(int precision, int shape, int nx, int nzm, int ny = 1);
+int occupancy_columns(int precision, int shape, int nx, int nzm, int ny = 1, int tc_n = 0);
 
 }  // namespace crm

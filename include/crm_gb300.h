@@ -360,6 +360,15 @@ int crm_submit(crm_server *srv, int chunk, const crm_input_c *in, const double *
  * then).  A completed ticket is released by the call that reports it. */
 int crm_poll(crm_server *srv, long long ticket, int wait);
 
+/* The 3D pressure solve's x/y transforms on the tensor cores (the FP32-mixed
+ * form's path for crm_nx = crm_ny in {16, 32}), on their own: one CTA
+ * transforms nlev levels of ff, each (n + 2) x (n + 2) floats, x fastest, in
+ * the layout of the solve: dir = -1 forward (rows j = 1..n, columns i = 1..n
+ * of each level in; the fft991 coefficients of the 2D real transform out in
+ * columns 1..n+1, rows 1..n+2), dir = +1 inverse (back to rows and columns
+ * 1..n).  Host arrays; for tests. */
+int crm_debug_tc_transform(int n, int nlev, int dir, const float *in, float *out);
+
 /* Library version string. */
 const char *crm_version(void);
 
