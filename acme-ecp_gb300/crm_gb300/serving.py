@@ -340,10 +340,9 @@ class CrmServer:
         stream.synchronize()
         return Chunk(key, slots, list(gcol), nbytes)
 
-    def checkpoint_chunk(self, chunk, path):
-        """Write a chunk's resident CRM state (the pbuf restart fields, see
-        checkpoint.py) to `path`.  Call between steps of that chunk."""
-        from . import checkpoint as CK
+    def chunk_state(self, chunk):
+        """A chunk's resident CRM state: (config, CrmState, qrad).  Call
+        between steps of that chunk."""
         torch = __import__('torch')
         pool = self.pools[chunk.key]
         stream = pool.streams[0]
@@ -354,7 +353,22 @@ class CrmServer:
         stream.synchronize()
         st = T.CrmState(**{n: np.asfortranarray(a) for n, a in host.items()})
         cfg = T.CrmConfig(**{**pool.cfg.__dict__, 'max_ncrms': 0})
-        CK.save(path, cfg, st, np.asfortranarray(qrad), chunk.gcol)
+        return cfg, st, np.asfortranarray(qrad)
+
+    def checkpoint_chunk(self, chunk, path):
+        """Write a chunk's resident CRM state (the pbuf restart fields, see
+        checkpoint.py) to `path`.  Call between steps of that chunk."""
+        from . import checkpoint as CK
+        cfg, st, qrad = self.chunk_state(chunk)
+        CK.save(path, cfg, st, qrad, chunk.gcol)
+
+    def write_gcm_restart(self, chunk, path, ncol):
+        """Write a chunk's resident CRM state as the GCM's restart file holds
+        it (CRM_* variables of dimensions (pbuf_NNNNN, ncol), netCDF classic,
+        pbuf_restart.write_crm_state); ncol: the physics grid's columns."""
+        from . import pbuf_restart as PR
+        cfg, st, qrad = self.chunk_state(chunk)
+        PR.write_crm_state(path, cfg, ncol, chunk.gcol, st, qrad)
 
     def restore_chunk(self, path, cin):
         """Admit a chunk from a restart file (its GCM inputs given anew)."""
@@ -364,6 +378,19 @@ class CrmServer:
         rad.qrad[...] = qrad
         ch = self.open_chunk(cfg, cin, st, rad, gcol)
         ch.steps = 1          # a restarted chunk is past its first step
+        return ch
+
+    def restore_chunk_from_gcm_restart(self, path, cfg, gcol, cin):
+        """Admit a chunk of GCM columns gcol (global ids, 1-based) with the
+        CRM state the GCM's own restart file holds for them (the CRM_*
+        physics-buffer fields, pbuf_restart.read_crm_state); its GCM inputs
+        given anew."""
+        from . import pbuf_restart as PR
+        st, qrad = PR.read_crm_state(path, cfg, gcol)
+        rad = T.CrmRad.zeros(len(gcol), cfg.crm_nx_rad or cfg.crm_nx, cfg.crm_ny_rad or cfg.crm_ny, cfg.crm_nz)
+        rad.qrad[...] = qrad
+        ch = self.open_chunk(cfg, cin, st, rad, gcol)
+        ch.steps = 1          # past its first step: no setperturb
         return ch
 
     def close_chunk(self, chunk):

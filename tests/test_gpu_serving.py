@@ -111,6 +111,37 @@ def test_checkpoint_and_restore_chunk(gpu_lib, tmp_path):
         assert np.array_equal(v, vals2[n]), n
 
 
+def test_resume_chunk_from_a_gcm_restart_file(gpu_lib, tmp_path):
+    """Two steps in one server == one step, the chunk's state written in the
+    GCM restart file's layout (CRM_* on a 64-column grid), a new server
+    resuming the chunk from that file, second step."""
+    from crm_gb300.serving import CrmServer, apply_tendencies
+    cfg = _configs()[1]
+    cin, st, rad, gcol = _chunk(cfg, 4, 30, seed=6)
+    server = CrmServer([cfg], capacity=32)
+    ref = _drive(server, cfg, (cin, st, rad, gcol), 2)
+    server.close()
+
+    server = CrmServer([cfg], capacity=32)
+    cin1 = cin.copy()
+    ch = server.open_chunk(cfg, cin1, st, rad, gcol)
+    vals, status = server.step(ch, cin1, DT_GL).result(timeout=120)
+    assert not status.any()
+    apply_tendencies(cin1, vals, DT_GL)
+    p = str(tmp_path / 'gcm_restart.nc')
+    server.write_gcm_restart(ch, p, ncol=64)
+    server.close_chunk(ch)
+    server.close()
+
+    server = CrmServer([cfg], capacity=32)
+    ch = server.restore_chunk_from_gcm_restart(p, cfg, gcol, cin1)
+    vals2, status = server.step(ch, cin1, DT_GL).result(timeout=120)
+    server.close()
+    assert not status.any()
+    for n, v in ref[1].items():
+        assert np.array_equal(v, vals2[n]), n
+
+
 def test_two_steps_of_one_chunk_submitted_back_to_back(gpu_lib):
     """A chunk's second request, submitted before its first completes, waits
     for it: the results equal the two steps run one after the other."""
