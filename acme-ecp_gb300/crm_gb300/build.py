@@ -50,6 +50,10 @@ for _s in SHAPES_3D:
     UNITS['crm_fp64_3d_s%d' % _s] = ('crm_columns', ['-fmad=false', '-DCRM_INST_T=double'] + _d)
     UNITS['crm_fp32_3d_s%d' % _s] = ('crm_columns', ['-DCRM_INST_T=float', '-prec-div=false',
                                                      '-prec-sqrt=false', '-ftz=true'] + _d)
+# the 3D FP32-mixed form with the tensor-core transforms (one launch shape,
+# crm_kernel.h kTcShape)
+UNITS['crm_fp32_3d_tc'] = ('crm_columns', ['-DCRM_INST_T=float', '-prec-div=false', '-prec-sqrt=false', '-ftz=true',
+                                           '-DCRM_INST_NX=0', '-DCRM_INST_NY=0', '-DCRM_INST_SHAPE=4', '-DCRM_INST_TC=1'])
 
 
 def _nvcc():

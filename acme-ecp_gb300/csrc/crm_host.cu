@@ -84,6 +84,12 @@ int launch_crm_consts(void *dst, const void *src, size_t bytes, cudaStream_t s);
 template <typename T, int NX, int NY>
 static void launch_tn(int shape, const KParams &p, int grid, cudaStream_t s, bool coop) {
   if constexpr (NY != 1) {
+    if constexpr (sizeof(T) == 4) {
+      if (p.tc_n) {            // the tensor-core instance has one shape
+        launch_crm_columns<T, NX, NY, kTcShape, 1>(p, grid, s, coop);
+        return;
+      }
+    }
     switch (shape) {
       case 0: launch_crm_columns<T, NX, NY, 0>(p, grid, s, coop); break;
       case 1: launch_crm_columns<T, NX, NY, 1>(p, grid, s, coop); break;
@@ -105,6 +111,12 @@ static void launch_tn(int shape, const KParams &p, int grid, cudaStream_t s, boo
 template <typename T, int NX, int NY>
 static int occupancy_tn(int shape, int nx, int ny, int nzm, int tc_n) {
   if constexpr (NY != 1) {
+    if (tc_n) {
+      if constexpr (sizeof(T) == 4) {
+        if (shape == kTcShape) return occupancy_crm_columns<T, NX, NY, kTcShape, 1>(nx, ny, nzm, tc_n);
+      }
+      return 0;
+    }
     switch (shape) {
       case 0: return occupancy_crm_columns<T, NX, NY, 0>(nx, ny, nzm, tc_n);
       case 1: return occupancy_crm_columns<T, NX, NY, 1>(nx, ny, nzm, tc_n);
@@ -406,14 +418,16 @@ void micro_consts(crm::KParams &p) {
   p.a_gr = 1. / (R4H(283.16) - R4H(223.16));
 }
 
-// The 3D FP32-mixed form with nx = ny in {16, 32} runs the transforms of the
-// pressure solve on the tensor cores; CRM_GB300_TRANSFORM=fft keeps the warp
-// FFT there.
+// The 3D FP32-mixed form with nx = ny in {16, 32} can run the transforms of
+// the pressure solve on the tensor cores (CRM_GB300_TRANSFORM=tc).  Not the
+// default: they are 2.5x faster than the warp FFT, but a kernel with tcgen05
+// code runs one CTA per SM, and the warp-FFT kernel at two CTAs per SM is
+// 9 % faster overall on 256 columns of 32 x 32 x 58.
 int tc_n_of(const crm_config &g) {
   if (g.precision != CRM_FP32_MIXED || g.crm_ny <= 1 || g.crm_nx != g.crm_ny) return 0;
   if (g.crm_nx != 16 && g.crm_nx != 32) return 0;
   const char *e = getenv("CRM_GB300_TRANSFORM");
-  if (e && strcmp(e, "fft") == 0) return 0;
+  if (!e || strcmp(e, "tc") != 0) return 0;
   return g.crm_nx;
 }
 using crm_tc_host::dft_elems;

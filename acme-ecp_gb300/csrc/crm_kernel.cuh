@@ -138,7 +138,10 @@ template <> struct NyDim<0> {
   __device__ explicit NyDim(int n) : ny(n) {}
 };
 
-template <typename T, int NX, int NY = 1>
+// TC = 1: the 3D FP32-mixed form with the pressure solve's transforms on
+// the tensor cores (crm_tc.cuh); a kernel that contains tcgen05 code runs
+// one CTA per SM on GB300, so it is a separate instance
+template <typename T, int NX, int NY = 1, int TC = 0>
 struct ColumnKernel : NxDim<NX>, NyDim<NY> {
   using NxDim<NX>::nx;
   using NyDim<NY>::ny;
@@ -2072,9 +2075,7 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
       }
       fdir = 0;
     };
-    bool tcp = false;   // FP32-mixed, nx = ny in {16, 32}: the tensor-core transforms
-    if constexpr (sizeof(T) == 4) tcp = p.tc_n != 0;
-    if (tcp) {
+    if constexpr (TC != 0) {
       if constexpr (sizeof(T) == 4) {
         tc::Engine E(p.tc_n, tcsm, S.tc_tmem, tc::smem_u32(&S.tc_mbar), &S.tc_phase, &S.tc_fail, TID, NT);
         for (int k0 = 1; k0 <= nzm; k0 += E.d.L) E.forward_tile(FF, k0, nzm);
@@ -2113,7 +2114,7 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
     }
     SYNC;
     PHASE_MARK(PH_TRIDIAG);
-    if (tcp) {
+    if constexpr (TC != 0) {
       if constexpr (sizeof(T) == 4) {
         tc::Engine E(p.tc_n, tcsm, S.tc_tmem, tc::smem_u32(&S.tc_mbar), &S.tc_phase, &S.tc_fail, TID, NT);
         for (int k0 = 1; k0 <= nzm; k0 += E.d.L) E.inverse_tile(FF, k0, nzm);
@@ -3870,7 +3871,7 @@ __host__ __device__ inline size_t crm_smem_bytes3(int nx, int ny, int block, int
   return fft > tcb ? fft : tcb;
 }
 
-template <typename T, int NX, int NY, int NTH, int MINB, int SMP>
+template <typename T, int NX, int NY, int NTH, int MINB, int SMP, int TC>
 __global__ void __launch_bounds__(NTH, MINB) crm_columns_kernel(const __grid_constant__ KParams p) {
   __shared__ ColShared S;
   extern __shared__ __align__(16) unsigned char crm_dsm[];
@@ -3882,7 +3883,7 @@ __global__ void __launch_bounds__(NTH, MINB) crm_columns_kernel(const __grid_con
   T *base = reinterpret_cast<T *>(p.slabs) + (size_t)blockIdx.x * p.L.slab;
   if (threadIdx.x == 0) S.gbar = 0;
   float *tcsm = nullptr;
-  if constexpr (NY != 1 && sizeof(T) == 4) {
+  if constexpr (TC != 0 && NY != 1 && sizeof(T) == 4) {
     if (p.tc_n) {
       // tensor memory for the transforms' accumulator (warp 0), the
       // mbarrier their commits arrive on, the constant matrices split into
@@ -3903,11 +3904,11 @@ __global__ void __launch_bounds__(NTH, MINB) crm_columns_kernel(const __grid_con
     }
   }
   for (int col = blockIdx.x; col < p.ncrms; col += gridDim.x) {
-    ColumnKernel<T, NX, NY> K(p, S, base, col, planes);
+    ColumnKernel<T, NX, NY, TC> K(p, S, base, col, planes);
     K.run(fsh, wsh, tcsm);
     __syncthreads();
   }
-  if constexpr (NY != 1 && sizeof(T) == 4) {
+  if constexpr (TC != 0 && NY != 1 && sizeof(T) == 4) {
     if (p.tc_n) {
       // a commit that outlived its wait is awaited (bounded) before the
       // accumulator is released
@@ -3921,18 +3922,18 @@ __global__ void __launch_bounds__(NTH, MINB) crm_columns_kernel(const __grid_con
   }
 }
 
-template <typename T, int NX, int NY, int SHAPE>
+template <typename T, int NX, int NY, int SHAPE, int TC>
 size_t crm_launch_smem(int nx, int ny, int nzm, int tc_n) {
   constexpr int nth = kShapes[SHAPE].threads, smp = kShapes[SHAPE].smem_planes;
-  if constexpr (NY != 1) return crm_smem_bytes3<T>(nx, ny, nth, sizeof(T) == 4 ? tc_n : 0);
+  if constexpr (NY != 1) return crm_smem_bytes3<T>(nx, ny, nth, (TC != 0 && sizeof(T) == 4) ? tc_n : 0);
   else return crm_smem_bytes<T>(nx, nzm, nth, smp);
 }
 
-template <typename T, int NX, int NY, int SHAPE>
+template <typename T, int NX, int NY, int SHAPE, int TC>
 void launch_crm_columns(const KParams &p, int grid, cudaStream_t s, bool cooperative) {
   constexpr int nth = kShapes[SHAPE].threads, minb = kShapes[SHAPE].min_ctas, smp = kShapes[SHAPE].smem_planes;
-  size_t smem = crm_launch_smem<T, NX, NY, SHAPE>(p.L.nx, p.L.ny, p.L.nzm, p.tc_n);
-  auto kern = crm_columns_kernel<T, NX, NY, nth, minb, smp>;
+  size_t smem = crm_launch_smem<T, NX, NY, SHAPE, TC>(p.L.nx, p.L.ny, p.L.nzm, p.tc_n);
+  auto kern = crm_columns_kernel<T, NX, NY, nth, minb, smp, TC>;
   cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (cooperative) {
     // every CTA co-resident (the batch-mode grid barrier relies on it); the
@@ -3947,14 +3948,14 @@ void launch_crm_columns(const KParams &p, int grid, cudaStream_t s, bool coopera
 
 // CTAs of the shape resident per SM (0: the shape does not fit); 3D runs
 // without shared-memory scratch planes, so those shapes report 0 there
-template <typename T, int NX, int NY, int SHAPE>
+template <typename T, int NX, int NY, int SHAPE, int TC>
 int occupancy_crm_columns(int nx, int ny, int nzm, int tc_n) {
   constexpr int nth = kShapes[SHAPE].threads, minb = kShapes[SHAPE].min_ctas, smp = kShapes[SHAPE].smem_planes;
   if (NY != 1 && smp) return 0;
   int n = 0;
-  size_t smem = crm_launch_smem<T, NX, NY, SHAPE>(nx, ny, nzm, tc_n);
+  size_t smem = crm_launch_smem<T, NX, NY, SHAPE, TC>(nx, ny, nzm, tc_n);
   if (smem > 227 * 1024) return 0;
-  auto kern = crm_columns_kernel<T, NX, NY, nth, minb, smp>;
+  auto kern = crm_columns_kernel<T, NX, NY, nth, minb, smp, TC>;
   cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, nth, smem) != cudaSuccess) return 0;
   return n;

@@ -84,12 +84,16 @@ constexpr KShape kShapes[kNumShapes] = {{256, 3, 0}, {256, 4, 0}, {256, 4, 2}, {
 constexpr int kNumNx = 4;
 constexpr int kNxBuilt[kNumNx] = {32, 64, 128, 0};
 
-// One instantiation per (T, NX, NY, shape) lives in its own object
-// (crm_columns.cu); NY = 1 is the 2D CRM, NY = 0 the generic 3D CRM.
-template <typename T, int NX, int NY, int SHAPE>
+// One instantiation per (T, NX, NY, shape, TC) lives in its own object
+// (crm_columns.cu); NY = 1 is the 2D CRM, NY = 0 the generic 3D CRM; TC = 1
+// the 3D FP32-mixed form with the tensor-core transforms.
+template <typename T, int NX, int NY, int SHAPE, int TC = 0>
 void launch_crm_columns(const KParams &p, int grid, cudaStream_t s, bool cooperative);
-template <typename T, int NX, int NY, int SHAPE>
+template <typename T, int NX, int NY, int SHAPE, int TC = 0>
 int occupancy_crm_columns(int nx, int ny, int nzm, int tc_n);
+// the launch shape of the TC = 1 instance (1024 threads, one CTA per SM: a
+// kernel with tcgen05 code is not co-resident with another CTA on GB300)
+constexpr int kTcShape = 4;
 
 // Dispatch on (precision, nx, ny, shape) at run time.
 void launch_columns(int precision, int shape, const KParams &p, int grid, cudaStream_t s,

@@ -27,9 +27,20 @@
 // layout (8 rows x 16 bytes per core matrix, K-adjacent core matrices 128
 // bytes apart, 8-row groups (K/4) x 128 bytes apart); the accumulator is a
 // 128-lane x N-column fp32 tile in tensor memory, read back with tcgen05.ld.
-// 3xTF32: every operand is split into a TF32 head (round to nearest) and a
-// TF32 tail (the remainder), and D = A_lo B_hi + A_hi B_lo + A_hi B_hi, which
-// carries the products to about FP32 accuracy.
+// Split TF32: every operand is split into three TF32 parts (head, middle,
+// tail: each the remainder rounded to nearest), x = x0 + x1 + x2 to 2^-33,
+// and D = sum of the six products A_p B_q with p + q <= 2 (smallest first),
+// which carries the products to FP32 accuracy (a two-part split, the usual
+// 3xTF32, leaves 2^-22 per product: measured 1.5e-4 against 9e-5 relative L2
+// on a GCM tendency where the FP32 FFT stays within 1e-4).
+// Means: an FFT's first butterflies subtract pairs of inputs, so a row's
+// mean never enters its other coefficients; a product with the DFT matrix
+// would spread eps |mean| into every one of them (and the pressure field's
+// horizontal mean is large against its perturbations).  Every pass therefore
+// takes the mean out of the operand rows and adds it back exactly: forward,
+// each row's mean (computed on the CUDA cores) is subtracted and becomes the
+// X_0 coefficient; inverse, the X_0 input is left out of the product and
+// added to every output.
 //
 // One thread issues the MMAs and commits them to an mbarrier; every wait on
 // it is bounded (a timeout marks the column CRM_ERR_TIMEOUT and skips the
@@ -42,6 +53,8 @@
 namespace crm {
 namespace tc {
 
+constexpr int kSplit = 3;      // TF32 parts per operand element
+
 // dimensions of the transform of length n (n = 16 or 32)
 struct Dims {
   int n, L, nf, ki;     // L = 128 / n levels per tile; nf = N of the forward
@@ -53,13 +66,14 @@ struct Dims {
   __host__ __device__ int bf_elems() const { return nf * n; }
   __host__ __device__ int bi_elems() const { return n * ki; }
   __host__ __device__ int gny_elems() const { return (L * n + 31) / 32 * 32; }
-  __host__ __device__ int off_alo() const { return a_elems(); }
-  __host__ __device__ int off_bfhi() const { return 2 * a_elems(); }
-  __host__ __device__ int off_bflo() const { return off_bfhi() + bf_elems(); }
-  __host__ __device__ int off_bihi() const { return off_bflo() + bf_elems(); }
-  __host__ __device__ int off_bilo() const { return off_bihi() + bi_elems(); }
-  __host__ __device__ int off_gny() const { return off_bilo() + bi_elems(); }
-  __host__ __device__ int total_elems() const { return off_gny() + gny_elems(); }
+  __host__ __device__ int aux_elems() const { return 2 * 128; }       // row means / X_0 terms
+  // part p of the staged operand A, of Bf, of Bi
+  __host__ __device__ int off_a(int p) const { return p * a_elems(); }
+  __host__ __device__ int off_bf(int p) const { return kSplit * a_elems() + p * bf_elems(); }
+  __host__ __device__ int off_bi(int p) const { return kSplit * (a_elems() + bf_elems()) + p * bi_elems(); }
+  __host__ __device__ int off_gny() const { return kSplit * (a_elems() + bf_elems() + bi_elems()); }
+  __host__ __device__ int off_aux() const { return off_gny() + gny_elems(); }
+  __host__ __device__ int total_elems() const { return off_aux() + aux_elems(); }
 };
 
 // shared-memory bytes of the tensor-core transform (0: not used)
@@ -83,10 +97,12 @@ __device__ __forceinline__ float tf32_head(float x) {
   asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
   return __uint_as_float(r);
 }
-// x = head + tail, both TF32
-__device__ __forceinline__ void split3(float x, float &hi, float &lo) {
-  hi = tf32_head(x);
-  lo = tf32_head(x - hi);
+// x = v[0] + v[1] + v[2], each TF32 (every remainder exact in FP32)
+__device__ __forceinline__ void splitk(float x, float *v) {
+  v[0] = tf32_head(x);
+  const float r1 = x - v[0];
+  v[1] = tf32_head(r1);
+  v[2] = tf32_head(r1 - v[1]);
 }
 
 // shared-memory matrix descriptor: no swizzle, K-major
@@ -175,9 +191,40 @@ struct Engine {
   __device__ Engine(int n, float *sm_, uint32_t tmem_, uint32_t mbar_, uint32_t *phase_, int *fail_, int tid_, int nt_)
       : d(n), sm(sm_), tmem(tmem_), mbar(mbar_), phase(phase_), fail(fail_), tid(tid_), nt(nt_) {}
 
-  __device__ float *ahi() const { return sm; }
-  __device__ float *alo() const { return sm + d.off_alo(); }
   __device__ float *gny() const { return sm + d.off_gny(); }
+  __device__ float *aux0() const { return sm + d.off_aux(); }
+  __device__ float *aux1() const { return sm + d.off_aux() + 128; }
+
+  // element e of operand A (or of a matrix at part offsets off(p)): split
+  // store, and the value back
+  __device__ void put_a(int e, float x) const {
+    float v[kSplit];
+    splitk(x, v);
+#pragma unroll
+    for (int p = 0; p < kSplit; ++p) sm[d.off_a(p) + e] = v[p];
+  }
+  __device__ float get_a(int e) const {
+    float x = 0.f;
+#pragma unroll
+    for (int p = kSplit - 1; p >= 0; --p) x += sm[d.off_a(p) + e];
+    return x;
+  }
+
+  // the mean of each of the 128 rows of the staged operand (n valid
+  // columns, layout K = kl) into m[], then those rows minus their mean;
+  // one thread per row
+  __device__ void center_rows(int kl, float *m) const {
+    for (int r = tid; r < 128; r += nt) {
+      float sum = 0.f;
+      for (int q = 0; q < d.n; ++q) sum += get_a(cm_index(r, q, kl));
+      const float mean = sum / (float)d.n;
+      m[r] = mean;
+      for (int q = 0; q < d.n; ++q) {
+        const int e = cm_index(r, q, kl);
+        put_a(e, get_a(e) - mean);
+      }
+    }
+  }
 
   // the constant matrices into shared memory, split (once per CTA)
   __device__ void load_mats(const float *mats) const {
@@ -185,46 +232,57 @@ struct Engine {
     for (int e = tid; e < d.bf_elems(); e += nt) {
       int r, q;
       cm_coords(e, d.n, r, q);
-      float hi, lo;
-      split3(bf[r * d.n + q], hi, lo);
-      sm[d.off_bfhi() + e] = hi;
-      sm[d.off_bflo() + e] = lo;
+      float v[kSplit];
+      splitk(bf[r * d.n + q], v);
+#pragma unroll
+      for (int p = 0; p < kSplit; ++p) sm[d.off_bf(p) + e] = v[p];
     }
     for (int e = tid; e < d.bi_elems(); e += nt) {
       int r, q;
       cm_coords(e, d.ki, r, q);
-      float hi, lo;
-      split3(bi[r * d.ki + q], hi, lo);
-      sm[d.off_bihi() + e] = hi;
-      sm[d.off_bilo() + e] = lo;
+      float v[kSplit];
+      splitk(bi[r * d.ki + q], v);
+#pragma unroll
+      for (int p = 0; p < kSplit; ++p) sm[d.off_bi(p) + e] = v[p];
     }
   }
-  __device__ float bf(int r, int q) const {       // Bf[r][q], head + tail
+  __device__ float bf(int r, int q) const {       // Bf[r][q]
     const int e = cm_index(r, q, d.n);
-    return sm[d.off_bfhi() + e] + sm[d.off_bflo() + e];
+    float x = 0.f;
+#pragma unroll
+    for (int p = kSplit - 1; p >= 0; --p) x += sm[d.off_bf(p) + e];
+    return x;
   }
   __device__ float bi(int r, int q) const {       // Bi[r][q]
     const int e = cm_index(r, q, d.ki);
-    return sm[d.off_bihi() + e] + sm[d.off_bilo() + e];
+    float x = 0.f;
+#pragma unroll
+    for (int p = kSplit - 1; p >= 0; --p) x += sm[d.off_bi(p) + e];
+    return x;
   }
 
-  // D (128 x N) = A (128 x K, staged in ahi/alo) . B^T (B: N x K at boff),
-  // 3xTF32; every thread returns once D is in tensor memory
-  __device__ void gemm(int K, int N, int bhi_off, int blo_off) {
+  // D (128 x N) = A (128 x K, staged) . B^T (B: N x K, parts at boff(p)):
+  // the products A_p B_q with p + q < kSplit, smallest first; every thread
+  // returns once D is in tensor memory
+  template <typename BOff>
+  __device__ void gemm(int K, int N, BOff boff) {
     fence_async_smem();          // the operands written by this thread, to the tensor cores
     __syncthreads();
     if (tid == 0 && !*fail) {
       fence_after();
       const uint32_t id = idesc_tf32(N);
       const uint32_t sbo = (uint32_t)(K / 4) * 128u;
-      const uint32_t a_hi = smem_u32(ahi()), a_lo = smem_u32(alo());
-      const uint32_t b_hi = smem_u32(sm + bhi_off), b_lo = smem_u32(sm + blo_off);
-      for (int s = 0; s < K / 8; ++s) {
-        const uint32_t o = (uint32_t)s * 256u;
-        mma_tf32(tmem, sdesc(a_lo + o, 128u, sbo), sdesc(b_hi + o, 128u, sbo), id, s > 0 ? 1u : 0u);
-        mma_tf32(tmem, sdesc(a_hi + o, 128u, sbo), sdesc(b_lo + o, 128u, sbo), id, 1u);
-        mma_tf32(tmem, sdesc(a_hi + o, 128u, sbo), sdesc(b_hi + o, 128u, sbo), id, 1u);
-      }
+      bool first = true;
+      for (int order = kSplit - 1; order >= 0; --order)
+        for (int pa = order; pa >= 0; --pa) {
+          const int pb = order - pa;
+          const uint32_t a = smem_u32(sm + d.off_a(pa)), b = smem_u32(sm + boff(pb));
+          for (int s = 0; s < K / 8; ++s) {
+            const uint32_t o = (uint32_t)s * 256u;
+            mma_tf32(tmem, sdesc(a + o, 128u, sbo), sdesc(b + o, 128u, sbo), id, first ? 0u : 1u);
+            first = false;
+          }
+        }
       commit(mbar);
     }
     if (!*fail) {
@@ -233,6 +291,12 @@ struct Engine {
     __syncthreads();
     if (tid == 0) *phase ^= 1u;
     fence_after();
+  }
+  __device__ void gemm_fwd(int K, int N) {
+    gemm(K, N, [&](int p) { return d.off_bf(p); });
+  }
+  __device__ void gemm_inv(int K, int N) {
+    gemm(K, N, [&](int p) { return d.off_bi(p); });
   }
 
   // each warp of the first four per column block reads its lane quarter:
@@ -256,45 +320,36 @@ struct Engine {
   template <typename FFT>
   __device__ void forward_tile(FFT FF, int k0, int nzm) {
     const int n = d.n, L = d.L;
-    float *Ah = ahi(), *Al = alo(), *G = gny();
+    float *G = gny(), *mx = aux0(), *my = aux1();
     // x pass: A[(l, j)][i] = P(i, j, k)
     for (int e = tid; e < 128 * n; e += nt) {
       int r, q;
       cm_coords(e, n, r, q);
       const int l = r / n, j = r % n, k = k0 + l;
-      const float x = k <= nzm ? FF(q + 1, j + 1, k) : 0.f;
-      float hi, lo;
-      split3(x, hi, lo);
-      Ah[e] = hi;
-      Al[e] = lo;
+      put_a(e, k <= nzm ? FF(q + 1, j + 1, k) : 0.f);
     }
     __syncthreads();
-    gemm(n, d.nf, d.off_bfhi(), d.off_bflo());
-    // the x coefficients c < n become the rows of the y pass; c = n (the
-    // Nyquist column) goes to G
+    center_rows(n, mx);
+    gemm_fwd(n, d.nf);
+    // the x coefficients c < n become the rows of the y pass (X_0 with the
+    // row mean added back); c = n (the Nyquist column) goes to G
     read_d(d.nf, [&](int r, int c0, const float *v) {
       const int l = r / n, j = r % n;
       for (int m = 0; m < 16; ++m) {
         const int c = c0 + m;
-        if (c < n) {
-          float hi, lo;
-          split3(v[m], hi, lo);
-          const int e = cm_index(l * n + c, j, n);
-          Ah[e] = hi;
-          Al[e] = lo;
-        } else if (c == n) {
-          G[l * n + j] = v[m];
-        }
+        if (c < n) put_a(cm_index(l * n + c, j, n), c == 0 ? v[m] + mx[r] : v[m]);
+        else if (c == n) G[l * n + j] = v[m];
       }
     });
     __syncthreads();
-    gemm(n, d.nf, d.off_bfhi(), d.off_bflo());
+    center_rows(n, my);
+    gemm_fwd(n, d.nf);
     read_d(d.nf, [&](int r, int c0, const float *v) {
       const int l = r / n, c = r % n, k = k0 + l;
       if (k > nzm) return;
       for (int m = 0; m < 16; ++m) {
         const int jj = c0 + m;
-        if (jj < n + 2) FF(c + 1, jj + 1, k) = v[m];
+        if (jj < n + 2) FF(c + 1, jj + 1, k) = jj == 0 ? v[m] + my[r] : v[m];
       }
     });
     // the Nyquist column's y transform on the CUDA cores
@@ -313,17 +368,16 @@ struct Engine {
   template <typename FFT>
   __device__ void inverse_tile(FFT FF, int k0, int nzm) {
     const int n = d.n, L = d.L, ki = d.ki;
-    float *Ah = ahi(), *Al = alo(), *G = gny();
-    // y pass: A[(l, c)][jj] = F(c + 1, jj + 1, k), c < n; K padded to ki
+    float *G = gny(), *f0 = aux0(), *g0 = aux1();
+    // y pass: A[(l, c)][jj] = F(c + 1, jj + 1, k), c < n, K padded to ki; X_0
+    // (jj = 0) is left out and added to every output
     for (int e = tid; e < 128 * ki; e += nt) {
       int r, q;
       cm_coords(e, ki, r, q);
       const int l = r / n, c = r % n, k = k0 + l;
       const float x = (k <= nzm && q < n + 2) ? FF(c + 1, q + 1, k) : 0.f;
-      float hi, lo;
-      split3(x, hi, lo);
-      Ah[e] = hi;
-      Al[e] = lo;
+      if (q == 0) f0[r] = x;
+      put_a(e, q == 0 ? 0.f : x);
     }
     // the Nyquist column back to grid rows j on the CUDA cores
     for (int e = tid; e < L * n; e += nt) {
@@ -334,38 +388,32 @@ struct Engine {
       G[l * n + j] = s;
     }
     __syncthreads();
-    gemm(ki, n, d.off_bihi(), d.off_bilo());
-    // x pass: A[(l, j)][c] = D[(l, c)][j] for c < n, G for c = n, 0 beyond
+    gemm_inv(ki, n);
+    // x pass: A[(l, j)][c] = D[(l, c)][j] + X_0 for c < n (c = 0 left out and
+    // added to every output), G for c = n, 0 beyond
     read_d(n, [&](int r, int j0, const float *v) {
       const int l = r / n, c = r % n;
       for (int m = 0; m < 16; ++m) {
         const int j = j0 + m;
         if (j < n) {
-          float hi, lo;
-          split3(v[m], hi, lo);
-          const int e = cm_index(l * n + j, c, ki);
-          Ah[e] = hi;
-          Al[e] = lo;
+          const float x = v[m] + f0[r];
+          if (c == 0) g0[l * n + j] = x;
+          put_a(cm_index(l * n + j, c, ki), c == 0 ? 0.f : x);
         }
       }
     });
     for (int e = tid; e < 128 * (ki - n); e += nt) {
       const int r = e / (ki - n), c = n + e % (ki - n);
-      const float x = c == n ? G[(r / n) * n + r % n] : 0.f;
-      float hi, lo;
-      split3(x, hi, lo);
-      const int ee = cm_index(r, c, ki);
-      Ah[ee] = hi;
-      Al[ee] = lo;
+      put_a(cm_index(r, c, ki), c == n ? G[r] : 0.f);
     }
     __syncthreads();
-    gemm(ki, n, d.off_bihi(), d.off_bilo());
+    gemm_inv(ki, n);
     read_d(n, [&](int r, int i0, const float *v) {
       const int l = r / n, j = r % n, k = k0 + l;
       if (k > nzm) return;
       for (int m = 0; m < 16; ++m) {
         const int i = i0 + m;
-        if (i < n) FF(i + 1, j + 1, k) = v[m];
+        if (i < n) FF(i + 1, j + 1, k) = v[m] + g0[r];
       }
     });
     __syncthreads();

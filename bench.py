@@ -354,6 +354,15 @@ def main():
         cfg3.max_ncrms = n3
         cs3 = n3 * int(work3[3].dt_gl / cfg3.crm_dt)
         ctx3, dev3, ms3, kms3 = device_rate(cfg3, args.steps_3d, 1, work3, 'fp32_3d')
+        # the same with the pressure solve's transforms on the tensor cores
+        # (their own kernel instance, one CTA per SM)
+        os.environ['CRM_GB300_TRANSFORM'] = 'tc'
+        try:
+            ctx3t, dev3t, ms3t, _ = device_rate(cfg3, 1, 1, work3, 'fp32_3d_tc', tune=False)
+        finally:
+            os.environ.pop('CRM_GB300_TRANSFORM', None)
+        es3t, eo3t = form_errors(dev3t, dev3, n3)
+        del ctx3t, dev3t
         cfg3d = S.config_3d(precision=T.CRM_FP64)
         cfg3d.max_ncrms = n3
         ctx3d, dev3d, ms3d, _ = device_rate(cfg3d, 1, 1, work3, 'fp64_3d', tune=False)
@@ -366,7 +375,12 @@ def main():
                    'cell_steps_per_s': ws * cs3 * cells3 / (ms3 / 1000.0),
                    'fp64_value': ws * cs3 / (ms3d / 1000.0), 'fp64_ms_per_step': ms3d, 'fp64_steps': 1,
                    'fp32_rel_l2_vs_fp64_state': es3,
-                   'fp32_rel_l2_vs_fp64_tendencies': {n: eo3[n] for n in ('sltend', 'qltend', 'qcltend', 'qiltend')}}
+                   'fp32_rel_l2_vs_fp64_tendencies': {n: eo3[n] for n in ('sltend', 'qltend', 'qcltend', 'qiltend')},
+                   'fp32_tensor_core_transforms': {
+                       'value': ws * cs3 / (ms3t / 1000.0), 'ms_per_step': ms3t, 'steps': 1,
+                       'note': 'x/y transforms of the pressure solve as split-TF32 tcgen05 GEMMs; the kernel '
+                               'instance with tcgen05 code runs one CTA per SM',
+                       'rel_l2_vs_fft_form_tendencies': {n: eo3t[n] for n in ('sltend', 'qltend')}}}
         del ctx3, dev3, ctx3d, dev3d
 
     # ---- serving: Poisson chunks of mixed (nx, nz) at 80 % of the closed-loop peak

@@ -96,16 +96,18 @@ def test_inverse_and_round_trip(gpu_lib, n, nlev):
     assert np.max(np.abs(back[:, :n, :n] - p[:, :n, :n])) < 2e-6 * np.max(np.abs(p))
 
 
-def test_fp32_3d_tensor_core_transforms_against_the_fft(gpu_lib):
-    """The FP32-mixed 3D form with the tensor-core transforms and with the
-    warp FFT (CRM_GB300_TRANSFORM=fft): both within the form's bounds of the
+@pytest.mark.parametrize('n,moist,dt_gl', [(32, True, 300.0), (16, False, 600.0)])
+def test_fp32_3d_tensor_core_transforms_against_the_fft(gpu_lib, n, moist, dt_gl):
+    """The FP32-mixed 3D form with the tensor-core transforms
+    (CRM_GB300_TRANSFORM=tc, its own kernel instance) and with the warp FFT
+    (the default): both within the form's 1e-4 tendency target against the
     FP64 form, and close to each other."""
-    cfg, cin, st, rad, desc = S.workload_3d(ncrms=2, nx=32, ny=32, moist=True)
-    desc.dt_gl = 300.0
+    cfg, cin, st, rad, desc = S.workload_3d(ncrms=2, nx=n, ny=n, moist=moist)
+    desc.dt_gl = dt_gl
     res = {}
     for mode in ('tc', 'fft'):
-        if mode == 'fft':
-            os.environ['CRM_GB300_TRANSFORM'] = 'fft'
+        if mode == 'tc':
+            os.environ['CRM_GB300_TRANSFORM'] = 'tc'
         try:
             c = T.CrmConfig(**{**cfg.__dict__, 'precision': T.CRM_FP32_MIXED, 'max_ncrms': desc.ld})
             ctx = CrmContext(c)
@@ -120,9 +122,10 @@ def test_fp32_3d_tensor_core_transforms_against_the_fft(gpu_lib):
     s64 = st.copy()
     CrmContext(c64).run(desc, cin, s64, rad.copy(), out64, raise_on_error=True)
     for mode, (s2, out) in res.items():
-        e = {n: rel_l2(getattr(out, n), getattr(out64, n)) for n in ('sltend', 'qltend')}
+        e = {k: rel_l2(getattr(out, k), getattr(out64, k)) for k in ('sltend', 'qltend')}
         e['w'] = rel_l2(s2.w_wind, s64.w_wind)
-        print('3D 32x32 FP32-mixed (%s transforms) vs FP64:' % mode, e)
-        assert e['sltend'] <= 1e-4 and e['qltend'] <= 1e-4 and e['w'] <= 5e-3, (mode, e)
+        e['t'] = rel_l2(s2.temperature, s64.temperature)
+        print('3D %dx%d FP32-mixed (%s transforms) vs FP64:' % (n, n, mode), e)
+        assert e['sltend'] <= 1e-4 and e['qltend'] <= 1e-4 and e['w'] <= 5e-3 and e['t'] <= 1e-6, (mode, e)
     d = rel_l2(res['tc'][0].w_wind, res['fft'][0].w_wind)
     assert d <= 5e-3, d
