@@ -53,7 +53,14 @@ for _s in SHAPES_3D:
 # the 3D FP32-mixed form with the tensor-core transforms (one launch shape,
 # crm_kernel.h kTcShape)
 UNITS['crm_fp32_3d_tc'] = ('crm_columns', ['-DCRM_INST_T=float', '-prec-div=false', '-prec-sqrt=false', '-ftz=true',
-                                           '-DCRM_INST_NX=0', '-DCRM_INST_NY=0', '-DCRM_INST_SHAPE=4', '-DCRM_INST_TC=1'])
+                                           '-DCRM_INST_NX=0', '-DCRM_INST_NY=0', '-DCRM_INST_SHAPE=4', '-DCRM_INST_VAR=1'])
+# the FP64 form with multiply-add contraction (CRM_FP64_FMA): one launch
+# shape each (crm_kernel.h kFmaShape2d, kFmaShape3d)
+for _n in NX_BUILT:
+    UNITS['crm_fp64fma_nx%d' % _n] = ('crm_columns', ['-DCRM_INST_T=double', '-DCRM_INST_NX=%d' % _n,
+                                                      '-DCRM_INST_SHAPE=0', '-DCRM_INST_VAR=2'])
+UNITS['crm_fp64fma_3d'] = ('crm_columns', ['-DCRM_INST_T=double', '-DCRM_INST_NX=0', '-DCRM_INST_NY=0',
+                                           '-DCRM_INST_SHAPE=3', '-DCRM_INST_VAR=2'])
 
 
 def _nvcc():

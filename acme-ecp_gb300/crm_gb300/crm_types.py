@@ -31,6 +31,7 @@ CRM_MICRO_SAM1MOM = 0
 CRM_MICRO_M2005 = 1
 CRM_FP64 = 0
 CRM_FP32_MIXED = 1
+CRM_FP64_FMA = 2
 CRM_PER_COLUMN = 0
 CRM_REFERENCE_BATCH = 1
 

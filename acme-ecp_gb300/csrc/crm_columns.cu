@@ -7,7 +7,9 @@
 //       sums and the saturation-adjustment Newton iteration in FP64;
 // -DCRM_INST_NX=n: the compile-time horizontal size (0: generic);
 // -DCRM_INST_NY=m: 1 (default) the 2D CRM, 0 the generic 3D CRM;
-// -DCRM_INST_TC=1: the 3D FP32-mixed form with the tensor-core transforms.
+// -DCRM_INST_VAR=v: 0 the plain forms, 1 the 3D FP32-mixed form with the
+// tensor-core transforms, 2 the FP64 form with multiply-add contraction
+// (compiled without -fmad=false).
 // The build compiles this file once per (precision, nx, launch shape), in
 // parallel.
 #include "crm_kernel.cuh"
@@ -19,12 +21,12 @@
 #ifndef CRM_INST_NY
 #define CRM_INST_NY 1
 #endif
-#ifndef CRM_INST_TC
-#define CRM_INST_TC 0
+#ifndef CRM_INST_VAR
+#define CRM_INST_VAR 0
 #endif
 
 namespace crm {
-template void launch_crm_columns<CRM_INST_T, CRM_INST_NX, CRM_INST_NY, CRM_INST_SHAPE, CRM_INST_TC>(const KParams &, int,
+template void launch_crm_columns<CRM_INST_T, CRM_INST_NX, CRM_INST_NY, CRM_INST_SHAPE, CRM_INST_VAR>(const KParams &, int,
                                                                                                   cudaStream_t, bool);
-template int occupancy_crm_columns<CRM_INST_T, CRM_INST_NX, CRM_INST_NY, CRM_INST_SHAPE, CRM_INST_TC>(int, int, int, int);
+template int occupancy_crm_columns<CRM_INST_T, CRM_INST_NX, CRM_INST_NY, CRM_INST_SHAPE, CRM_INST_VAR>(int, int, int, int);
 }  // namespace crm

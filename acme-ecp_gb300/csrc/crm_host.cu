@@ -80,13 +80,18 @@ void launch_crm_prep(const PrepParams &p, cudaStream_t s);
 int launch_crm_consts(void *dst, const void *src, size_t bytes, cudaStream_t s);
 
 // 3D builds no shapes with shared-memory scratch planes (its planes do not
-// fit): shapes 2 and 5 are never chosen there (occupancy 0)
-template <typename T, int NX, int NY>
+// fit): shapes 2 and 5 are never chosen there (occupancy 0).  The tensor-core
+// and contracted-FP64 instances have one launch shape each.
+template <typename T, int NX, int NY, int VAR>
 static void launch_tn(int shape, const KParams &p, int grid, cudaStream_t s, bool coop) {
+  if constexpr (VAR == kVarFma) {
+    launch_crm_columns<T, NX, NY, (NY != 1 ? kFmaShape3d : kFmaShape2d), kVarFma>(p, grid, s, coop);
+    return;
+  }
   if constexpr (NY != 1) {
     if constexpr (sizeof(T) == 4) {
-      if (p.tc_n) {            // the tensor-core instance has one shape
-        launch_crm_columns<T, NX, NY, kTcShape, 1>(p, grid, s, coop);
+      if (p.tc_n) {
+        launch_crm_columns<T, NX, NY, kTcShape, kVarTc>(p, grid, s, coop);
         return;
       }
     }
@@ -108,12 +113,16 @@ static void launch_tn(int shape, const KParams &p, int grid, cudaStream_t s, boo
   }
 }
 
-template <typename T, int NX, int NY>
+template <typename T, int NX, int NY, int VAR>
 static int occupancy_tn(int shape, int nx, int ny, int nzm, int tc_n) {
+  if constexpr (VAR == kVarFma) {
+    constexpr int fs = NY != 1 ? kFmaShape3d : kFmaShape2d;
+    return shape == fs ? occupancy_crm_columns<T, NX, NY, fs, kVarFma>(nx, ny, nzm, 0) : 0;
+  }
   if constexpr (NY != 1) {
     if (tc_n) {
       if constexpr (sizeof(T) == 4) {
-        if (shape == kTcShape) return occupancy_crm_columns<T, NX, NY, kTcShape, 1>(nx, ny, nzm, tc_n);
+        if (shape == kTcShape) return occupancy_crm_columns<T, NX, NY, kTcShape, kVarTc>(nx, ny, nzm, tc_n);
       }
       return 0;
     }
@@ -136,39 +145,41 @@ static int occupancy_tn(int shape, int nx, int ny, int nzm, int tc_n) {
 }
 
 // 2D: a kernel specialised on nx where one is built; 3D: the generic kernel
-template <typename T>
+template <typename T, int VAR>
 static void launch_t(int shape, const KParams &p, int grid, cudaStream_t s, bool coop) {
   if (p.L.ny > 1) {
-    launch_tn<T, 0, 0>(shape, p, grid, s, coop);
+    launch_tn<T, 0, 0, VAR>(shape, p, grid, s, coop);
     return;
   }
   switch (p.L.nx) {
-    case 32: launch_tn<T, 32, 1>(shape, p, grid, s, coop); break;
-    case 64: launch_tn<T, 64, 1>(shape, p, grid, s, coop); break;
-    case 128: launch_tn<T, 128, 1>(shape, p, grid, s, coop); break;
-    default: launch_tn<T, 0, 1>(shape, p, grid, s, coop); break;
+    case 32: launch_tn<T, 32, 1, VAR>(shape, p, grid, s, coop); break;
+    case 64: launch_tn<T, 64, 1, VAR>(shape, p, grid, s, coop); break;
+    case 128: launch_tn<T, 128, 1, VAR>(shape, p, grid, s, coop); break;
+    default: launch_tn<T, 0, 1, VAR>(shape, p, grid, s, coop); break;
   }
 }
 
-template <typename T>
+template <typename T, int VAR>
 static int occupancy_t(int shape, int nx, int nzm, int ny, int tc_n) {
-  if (ny > 1) return occupancy_tn<T, 0, 0>(shape, nx, ny, nzm, tc_n);
+  if (ny > 1) return occupancy_tn<T, 0, 0, VAR>(shape, nx, ny, nzm, tc_n);
   switch (nx) {
-    case 32: return occupancy_tn<T, 32, 1>(shape, nx, 1, nzm, 0);
-    case 64: return occupancy_tn<T, 64, 1>(shape, nx, 1, nzm, 0);
-    case 128: return occupancy_tn<T, 128, 1>(shape, nx, 1, nzm, 0);
-    default: return occupancy_tn<T, 0, 1>(shape, nx, 1, nzm, 0);
+    case 32: return occupancy_tn<T, 32, 1, VAR>(shape, nx, 1, nzm, 0);
+    case 64: return occupancy_tn<T, 64, 1, VAR>(shape, nx, 1, nzm, 0);
+    case 128: return occupancy_tn<T, 128, 1, VAR>(shape, nx, 1, nzm, 0);
+    default: return occupancy_tn<T, 0, 1, VAR>(shape, nx, 1, nzm, 0);
   }
 }
 
 void launch_columns(int precision, int shape, const KParams &p, int grid, cudaStream_t s, bool coop) {
-  if (precision == CRM_FP64) launch_t<double>(shape, p, grid, s, coop);
-  else launch_t<float>(shape, p, grid, s, coop);
+  if (precision == CRM_FP64) launch_t<double, kVarPlain>(shape, p, grid, s, coop);
+  else if (precision == CRM_FP64_FMA) launch_t<double, kVarFma>(shape, p, grid, s, coop);
+  else launch_t<float, kVarPlain>(shape, p, grid, s, coop);
 }
 
 int occupancy_columns(int precision, int shape, int nx, int nzm, int ny, int tc_n) {
-  return precision == CRM_FP64 ? occupancy_t<double>(shape, nx, nzm, ny, tc_n)
-                               : occupancy_t<float>(shape, nx, nzm, ny, tc_n);
+  if (precision == CRM_FP64) return occupancy_t<double, kVarPlain>(shape, nx, nzm, ny, tc_n);
+  if (precision == CRM_FP64_FMA) return occupancy_t<double, kVarFma>(shape, nx, nzm, ny, tc_n);
+  return occupancy_t<float, kVarPlain>(shape, nx, nzm, ny, tc_n);
 }
 }  // namespace crm
 
@@ -301,7 +312,7 @@ int default_shape(int precision, int nx, int ny = 1) {
     if (v >= 0 && v < crm::kNumShapes) return v;
   }
   // 3D (nx x ny cells per level): 512 threads at 2 CTAs/SM
-  if (ny > 1) return 3;
+  if (ny > 1) return precision == CRM_FP64_FMA ? crm::kFmaShape3d : 3;
   // measured on 1024 columns of nx x 58, 30 steps (column-steps/s):
   //   FP64: 256 threads at 3 CTAs/SM (105K at nx 64; the other shapes are
   //     4-15 % slower);
@@ -311,6 +322,7 @@ int default_shape(int precision, int nx, int ny = 1) {
   //     shared memory for nx >= 128 (291K against 282K without them and
   //     192K at 256 threads).
   if (precision == CRM_FP64) return 0;
+  if (precision == CRM_FP64_FMA) return crm::kFmaShape2d;
   return nx >= 128 ? 5 : 2;
 }
 
@@ -343,7 +355,8 @@ int validate(const crm_config *c) {
   if (c->crm_ny < 1) return CRM_ERR_ARG;
   if (c->microphysics != CRM_MICRO_SAM1MOM) return CRM_ERR_UNSUPPORTED;
   if (c->batch_mode != CRM_PER_COLUMN && c->batch_mode != CRM_REFERENCE_BATCH) return CRM_ERR_ARG;
-  if (c->precision != CRM_FP64 && c->precision != CRM_FP32_MIXED) return CRM_ERR_ARG;
+  if (c->precision != CRM_FP64 && c->precision != CRM_FP32_MIXED && c->precision != CRM_FP64_FMA)
+    return CRM_ERR_ARG;
   if (c->crm_nx < 8 || c->crm_nx % 2 || c->crm_nz < 4 || c->plev < c->crm_nz + 2) return CRM_ERR_ARG;
   if (c->crm_nx_rad < 1 || c->crm_nx % c->crm_nx_rad) return CRM_ERR_ARG;
   if (!(c->crm_dx > 0) || !(c->crm_dt > 0) || 60. < 2 * c->crm_dt) return CRM_ERR_ARG;
@@ -440,7 +453,7 @@ int plan_ctx(crm_ctx *c) {
   const crm_config &g = c->cfg;
   CK(cudaGetDevice(&c->device));
   CK(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, c->device));
-  const size_t esz = g.precision == CRM_FP64 ? sizeof(double) : sizeof(float);
+  const size_t esz = g.precision == CRM_FP32_MIXED ? sizeof(float) : sizeof(double);
   c->L = crm::make_layout(g.crm_nx, g.crm_nz, g.plev, g.crm_nx_rad, (int)esz, g.crm_ny, g.crm_ny_rad);
   c->tc_n = tc_n_of(g);
   c->slab_cap = 0;
@@ -454,6 +467,20 @@ int plan_ctx(crm_ctx *c) {
   c->slab_bytes = c->L.slab * esz;
   c->ld_cap = g.max_ncrms;
   return CRM_OK;
+}
+
+// The handle's default launch shape: the measured default of its precision
+// and size if that shape can run this handle's kernel, else the launchable
+// shape with the most co-resident CTAs (the tensor-core and contracted-FP64
+// instances have one shape each).
+int handle_default_shape(const crm_ctx *c) {
+  const crm_config &g = c->cfg;
+  int s = default_shape(g.precision, g.crm_nx, g.crm_ny);
+  if (c->shape_grid[s] > 0) return s;
+  int best = -1;
+  for (int s2 = 0; s2 < crm::kNumShapes; ++s2)
+    if (c->shape_grid[s2] > 0 && (best < 0 || c->shape_grid[s2] > c->shape_grid[best])) best = s2;
+  return best < 0 ? s : best;
 }
 
 // Device bytes alloc_ctx allocates for a planned handle (the staging
@@ -472,7 +499,7 @@ int alloc_ctx(crm_ctx *c) {
   const crm_config &g = c->cfg;
   int rc = plan_ctx(c);
   if (rc != CRM_OK) return rc;
-  c->shape = default_shape(g.precision, g.crm_nx, g.crm_ny);
+  c->shape = handle_default_shape(c);
   {
     const char *e = getenv("CRM_GB300_SHAPE");
     if (e && *e) c->shape_auto = false;
@@ -661,7 +688,7 @@ int enqueue(crm_ctx *c, const crm_call_desc *d, const crm_input_c *in, crm_state
     for (int s2 = 0; s2 < crm::kNumShapes; ++s2)
       if (c->shape_grid[s2] >= ncrms && (best < 0 || crm::kShapes[s2].threads > crm::kShapes[best].threads))
         best = s2;
-    const int dflt = default_shape(g.precision, g.crm_nx, g.crm_ny);
+    const int dflt = handle_default_shape(c);
     if (best < 0 || c->shape_grid[dflt] >= ncrms && crm::kShapes[dflt].threads >= crm::kShapes[best].threads)
       best = dflt;
     c->shape = best;
@@ -787,7 +814,7 @@ int crm_set_launch_shape(crm_ctx *ctx, int shape) {
   if (!ctx) return CRM_ERR_ARG;
   if (shape == -1) {                       // back to the per-call choice
     ctx->shape_auto = true;
-    ctx->shape = default_shape(ctx->cfg.precision, ctx->cfg.crm_nx, ctx->cfg.crm_ny);
+    ctx->shape = handle_default_shape(ctx);
     ctx->grid_max = ctx->shape_grid[ctx->shape];
     return CRM_OK;
   }
@@ -977,7 +1004,7 @@ struct NoallocPlan {
 // Host arithmetic only: what one call needs and how many slabs fit.
 int noalloc_plan(const crm_config &g, int ncrms, NoallocPlan &q) {
   if (g.crm_nx > CRM_NOALLOC_MAX_NX) return CRM_ERR_TOO_LARGE;
-  q.esz = g.precision == CRM_FP64 ? sizeof(double) : sizeof(float);
+  q.esz = g.precision == CRM_FP32_MIXED ? sizeof(float) : sizeof(double);
   q.L = crm::make_layout(g.crm_nx, g.crm_nz, g.plev, g.crm_nx_rad, (int)q.esz);
   q.ntrigs = 3 * g.crm_nx / 2 + 2 + g.crm_nx;
   q.neign = g.crm_nx + 1;

@@ -3871,8 +3871,11 @@ __host__ __device__ inline size_t crm_smem_bytes3(int nx, int ny, int block, int
   return fft > tcb ? fft : tcb;
 }
 
-template <typename T, int NX, int NY, int NTH, int MINB, int SMP, int TC>
+// VAR: kVarPlain, kVarTc (the tensor-core transforms) or kVarFma (the FP64
+// form compiled with multiply-add contraction); a separate instance each
+template <typename T, int NX, int NY, int NTH, int MINB, int SMP, int VAR>
 __global__ void __launch_bounds__(NTH, MINB) crm_columns_kernel(const __grid_constant__ KParams p) {
+  constexpr int TC = VAR == kVarTc ? 1 : 0;
   __shared__ ColShared S;
   extern __shared__ __align__(16) unsigned char crm_dsm[];
   T *fsh = reinterpret_cast<T *>(crm_dsm);
@@ -3922,18 +3925,18 @@ __global__ void __launch_bounds__(NTH, MINB) crm_columns_kernel(const __grid_con
   }
 }
 
-template <typename T, int NX, int NY, int SHAPE, int TC>
+template <typename T, int NX, int NY, int SHAPE, int VAR>
 size_t crm_launch_smem(int nx, int ny, int nzm, int tc_n) {
   constexpr int nth = kShapes[SHAPE].threads, smp = kShapes[SHAPE].smem_planes;
-  if constexpr (NY != 1) return crm_smem_bytes3<T>(nx, ny, nth, (TC != 0 && sizeof(T) == 4) ? tc_n : 0);
+  if constexpr (NY != 1) return crm_smem_bytes3<T>(nx, ny, nth, (VAR == kVarTc && sizeof(T) == 4) ? tc_n : 0);
   else return crm_smem_bytes<T>(nx, nzm, nth, smp);
 }
 
-template <typename T, int NX, int NY, int SHAPE, int TC>
+template <typename T, int NX, int NY, int SHAPE, int VAR>
 void launch_crm_columns(const KParams &p, int grid, cudaStream_t s, bool cooperative) {
   constexpr int nth = kShapes[SHAPE].threads, minb = kShapes[SHAPE].min_ctas, smp = kShapes[SHAPE].smem_planes;
-  size_t smem = crm_launch_smem<T, NX, NY, SHAPE, TC>(p.L.nx, p.L.ny, p.L.nzm, p.tc_n);
-  auto kern = crm_columns_kernel<T, NX, NY, nth, minb, smp, TC>;
+  size_t smem = crm_launch_smem<T, NX, NY, SHAPE, VAR>(p.L.nx, p.L.ny, p.L.nzm, p.tc_n);
+  auto kern = crm_columns_kernel<T, NX, NY, nth, minb, smp, VAR>;
   cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (cooperative) {
     // every CTA co-resident (the batch-mode grid barrier relies on it); the
@@ -3948,14 +3951,14 @@ void launch_crm_columns(const KParams &p, int grid, cudaStream_t s, bool coopera
 
 // CTAs of the shape resident per SM (0: the shape does not fit); 3D runs
 // without shared-memory scratch planes, so those shapes report 0 there
-template <typename T, int NX, int NY, int SHAPE, int TC>
+template <typename T, int NX, int NY, int SHAPE, int VAR>
 int occupancy_crm_columns(int nx, int ny, int nzm, int tc_n) {
   constexpr int nth = kShapes[SHAPE].threads, minb = kShapes[SHAPE].min_ctas, smp = kShapes[SHAPE].smem_planes;
   if (NY != 1 && smp) return 0;
   int n = 0;
-  size_t smem = crm_launch_smem<T, NX, NY, SHAPE, TC>(nx, ny, nzm, tc_n);
+  size_t smem = crm_launch_smem<T, NX, NY, SHAPE, VAR>(nx, ny, nzm, tc_n);
   if (smem > 227 * 1024) return 0;
-  auto kern = crm_columns_kernel<T, NX, NY, nth, minb, smp, TC>;
+  auto kern = crm_columns_kernel<T, NX, NY, nth, minb, smp, VAR>;
   cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, nth, smem) != cudaSuccess) return 0;
   return n;

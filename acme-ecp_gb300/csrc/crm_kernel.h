@@ -84,16 +84,22 @@ constexpr KShape kShapes[kNumShapes] = {{256, 3, 0}, {256, 4, 0}, {256, 4, 2}, {
 constexpr int kNumNx = 4;
 constexpr int kNxBuilt[kNumNx] = {32, 64, 128, 0};
 
-// One instantiation per (T, NX, NY, shape, TC) lives in its own object
-// (crm_columns.cu); NY = 1 is the 2D CRM, NY = 0 the generic 3D CRM; TC = 1
-// the 3D FP32-mixed form with the tensor-core transforms.
-template <typename T, int NX, int NY, int SHAPE, int TC = 0>
+// Kernel variants, each its own instance: the plain forms; the 3D
+// FP32-mixed form with the tensor-core transforms; the FP64 form compiled
+// with multiply-add contraction (CRM_FP64_FMA).
+constexpr int kVarPlain = 0, kVarTc = 1, kVarFma = 2;
+// One instantiation per (T, NX, NY, shape, variant) lives in its own object
+// (crm_columns.cu); NY = 1 is the 2D CRM, NY = 0 the generic 3D CRM.
+template <typename T, int NX, int NY, int SHAPE, int VAR = kVarPlain>
 void launch_crm_columns(const KParams &p, int grid, cudaStream_t s, bool cooperative);
-template <typename T, int NX, int NY, int SHAPE, int TC = 0>
+template <typename T, int NX, int NY, int SHAPE, int VAR = kVarPlain>
 int occupancy_crm_columns(int nx, int ny, int nzm, int tc_n);
-// the launch shape of the TC = 1 instance (1024 threads, one CTA per SM: a
-// kernel with tcgen05 code is not co-resident with another CTA on GB300)
+// the launch shape of the tensor-core instance (1024 threads, one CTA per SM:
+// a kernel with tcgen05 code is not co-resident with another CTA on GB300)
 constexpr int kTcShape = 4;
+// the launch shapes of the contracted FP64 instances: those of the plain
+// FP64 form's defaults (2D: 256 threads x 3 CTAs/SM, 3D: 512 x 2)
+constexpr int kFmaShape2d = 0, kFmaShape3d = 3;
 
 // Dispatch on (precision, nx, ny, shape) at run time.
 void launch_columns(int precision, int shape, const KParams &p, int grid, cudaStream_t s,

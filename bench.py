@@ -305,6 +305,14 @@ def main():
     cfg64.max_ncrms = NCRMS
     ctx64, dev64, ms64, _ = device_rate(cfg64, args.fp64_steps, 1)
     value64 = ws * colsteps / (ms64 / 1000.0)
+    # the FP64 form with multiply-add contraction (within 1e-10 of the plain
+    # form, not bit-identical)
+    cfgf = S.config_64x58(precision=T.CRM_FP64_FMA)
+    cfgf.max_ncrms = NCRMS
+    ctxf, devf, msf, _ = device_rate(cfgf, args.fp64_steps, 1, tag='fp64_fma', tune=False)
+    valuef = ws * colsteps / (msf / 1000.0)
+    esf, eof = form_errors(devf, dev64)
+    del ctxf, devf
 
     # ---- accuracy of the FP32-mixed form against the FP64 form (same inputs)
     # (the FP64 form equals the oracle bit for bit, so this is the error
@@ -480,6 +488,8 @@ def main():
         'fp64_plain': {'value': value64, 'unit': UNIT, 'ms_per_step': ms64,
                        'ms_per_step_median': medians.get('fp64'), 'steps': args.fp64_steps,
                        'fp64_pipe': fp64_pipe},
+        'fp64_fma': {'value': valuef, 'unit': UNIT, 'ms_per_step': msf, 'steps': args.fp64_steps,
+                     'max_rel_l2_vs_fp64_plain': max(list(esf.values()) + list(eof.values()))},
         'fp32_over_fp64': value / value64,
         'fp32_rel_l2_vs_fp64_state': errs,
         'fp32_rel_l2_vs_fp64_outputs': errs_out,
