@@ -334,14 +334,17 @@ int accel_nstop(const crm_config &g, int nstop) {
   return (int)((double)nstop / (1 + g.crm_accel_factor));
 }
 
-// A transform length the device FFT takes: fax_crm factors 2 and 4 only
-// (vpass_warp), at most 7 of them.
-int check_fft_size(int n) {
+// A transform length the device FFT takes: fax_crm factors 2, 3, 4 and 5
+// (vpass_warp), at most 7 of them; pow2 = true: 2 and 4 only (the 3D CRM
+// decodes a cell index with a shift, so its nx and ny are powers of two).
+int check_fft_size(int n, bool pow2 = false) {
   int f[20];
   fft_factors(f, n);
   if (f[0] < 1) return CRM_ERR_ARG;
-  for (int k = 1; k <= f[0]; ++k)
-    if (f[k] != 2 && f[k] != 4) return CRM_ERR_UNSUPPORTED;
+  for (int k = 1; k <= f[0]; ++k) {
+    if (f[k] != 2 && f[k] != 3 && f[k] != 4 && f[k] != 5) return CRM_ERR_UNSUPPORTED;
+    if (pow2 && f[k] != 2 && f[k] != 4) return CRM_ERR_UNSUPPORTED;
+  }
   if (f[0] > 7) return CRM_ERR_ARG;
   return CRM_OK;
 }
@@ -361,14 +364,14 @@ int validate(const crm_config *c) {
   if (c->crm_nx_rad < 1 || c->crm_nx % c->crm_nx_rad) return CRM_ERR_ARG;
   if (!(c->crm_dx > 0) || !(c->crm_dt > 0) || 60. < 2 * c->crm_dt) return CRM_ERR_ARG;
   if (c->max_ncrms < 1) return CRM_ERR_ARG;
-  int rc = check_fft_size(c->crm_nx);
+  int rc = check_fft_size(c->crm_nx, c->crm_ny > 1);
   if (rc != CRM_OK) return rc;
   if (c->crm_ny == 1) {
     if (c->crm_ny_rad != 1) return CRM_ERR_ARG;
   } else {
     // 3D: ny a transform length of its own; radiation on every CRM column
     if (c->crm_ny < 8) return CRM_ERR_ARG;
-    rc = check_fft_size(c->crm_ny);
+    rc = check_fft_size(c->crm_ny, true);
     if (rc != CRM_OK) return rc;
     if (c->crm_dy < 0) return CRM_ERR_ARG;
     if (c->crm_ny_rad < 1 || c->crm_ny % c->crm_ny_rad) return CRM_ERR_ARG;

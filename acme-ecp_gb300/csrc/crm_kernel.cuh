@@ -1847,6 +1847,58 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
           C[2 * (q + la)] = c1 * (a0 - a1) - s1 * (b0 - b1);
           C[2 * (q + la) + 1] = s1 * (a0 - a1) + c1 * (b0 - b1);
         }
+      } else if (ifac == 3) {
+        // fft.F90 vpassm_crm, radix 3 (REAL*4 sin60)
+        const T sin60 = (T)(double)(float)0.866025403784437;
+        T a2 = A[2 * (pp + 2 * m)], b2 = A[2 * (pp + 2 * m) + 1];
+        T *C0 = C + 2 * q, *C1 = C + 2 * (q + la), *C2 = C + 2 * (q + 2 * la);
+        C0[0] = a0 + (a1 + a2);
+        C0[1] = b0 + (b1 + b2);
+        T xr = a0 - (T)0.5 * (a1 + a2), xi = b0 - (T)0.5 * (b1 + b2);
+        T yr = sin60 * (b1 - b2), yi = sin60 * (a1 - a2);
+        if (g == 0) {
+          C1[0] = xr - yr; C2[0] = xr + yr; C1[1] = xi + yi; C2[1] = xi - yi;
+        } else {
+          T c1 = tw(kb), s1 = tw(kb + 1), c2 = tw(2 * kb), s2 = tw(2 * kb + 1);
+          C1[0] = c1 * (xr - yr) - s1 * (xi + yi);
+          C1[1] = s1 * (xr - yr) + c1 * (xi + yi);
+          C2[0] = c2 * (xr + yr) - s2 * (xi - yi);
+          C2[1] = s2 * (xr + yr) + c2 * (xi - yi);
+        }
+      } else if (ifac == 5) {
+        // fft.F90 vpassm_crm, radix 5 (REAL*4 sin36, cos36, sin72, cos72)
+        const T sin36 = (T)(double)(float)0.587785252292473, cos36 = (T)(double)(float)0.809016994374947;
+        const T sin72 = (T)(double)(float)0.951056516295154, cos72 = (T)(double)(float)0.309016994374947;
+        T a2 = A[2 * (pp + 2 * m)], b2 = A[2 * (pp + 2 * m) + 1];
+        T a3 = A[2 * (pp + 3 * m)], b3 = A[2 * (pp + 3 * m) + 1];
+        T a4 = A[2 * (pp + 4 * m)], b4 = A[2 * (pp + 4 * m) + 1];
+        T *C0 = C + 2 * q, *C1 = C + 2 * (q + la), *C2 = C + 2 * (q + 2 * la), *C3 = C + 2 * (q + 3 * la),
+          *C4 = C + 2 * (q + 4 * la);
+        C0[0] = (a0 + (a1 + a4)) + (a2 + a3);
+        C0[1] = (b0 + (b1 + b4)) + (b2 + b3);
+        T p1r = (a0 + cos72 * (a1 + a4)) - cos36 * (a2 + a3);
+        T q1r = sin72 * (b1 - b4) + sin36 * (b2 - b3);
+        T p1i = (b0 + cos72 * (b1 + b4)) - cos36 * (b2 + b3);
+        T q1i = sin72 * (a1 - a4) + sin36 * (a2 - a3);
+        T p2r = (a0 - cos36 * (a1 + a4)) + cos72 * (a2 + a3);
+        T q2r = sin36 * (b1 - b4) - sin72 * (b2 - b3);
+        T p2i = (b0 - cos36 * (b1 + b4)) + cos72 * (b2 + b3);
+        T q2i = sin36 * (a1 - a4) - sin72 * (a2 - a3);
+        if (g == 0) {
+          C1[0] = p1r - q1r; C4[0] = p1r + q1r; C1[1] = p1i + q1i; C4[1] = p1i - q1i;
+          C2[0] = p2r - q2r; C3[0] = p2r + q2r; C2[1] = p2i + q2i; C3[1] = p2i - q2i;
+        } else {
+          T c1 = tw(kb), s1 = tw(kb + 1), c2 = tw(2 * kb), s2 = tw(2 * kb + 1);
+          T c3 = tw(3 * kb), s3 = tw(3 * kb + 1), c4 = tw(4 * kb), s4 = tw(4 * kb + 1);
+          C1[0] = c1 * (p1r - q1r) - s1 * (p1i + q1i);
+          C1[1] = s1 * (p1r - q1r) + c1 * (p1i + q1i);
+          C4[0] = c4 * (p1r + q1r) - s4 * (p1i - q1i);
+          C4[1] = s4 * (p1r + q1r) + c4 * (p1i - q1i);
+          C2[0] = c2 * (p2r - q2r) - s2 * (p2i + q2i);
+          C2[1] = s2 * (p2r - q2r) + c2 * (p2i + q2i);
+          C3[0] = c3 * (p2r + q2r) - s3 * (p2i - q2i);
+          C3[1] = s3 * (p2r + q2r) + c3 * (p2i - q2i);
+        }
       } else {  // 4
         T a2 = A[2 * (pp + 2 * m)], b2 = A[2 * (pp + 2 * m) + 1];
         T a3 = A[2 * (pp + 3 * m)], b3 = A[2 * (pp + 3 * m) + 1];

@@ -311,8 +311,6 @@ def main():
     cfgf.max_ncrms = NCRMS
     ctxf, devf, msf, _ = device_rate(cfgf, args.fp64_steps, 1, tag='fp64_fma', tune=False)
     valuef = ws * colsteps / (msf / 1000.0)
-    esf, eof = form_errors(devf, dev64)
-    del ctxf, devf
 
     # ---- accuracy of the FP32-mixed form against the FP64 form (same inputs)
     # (the FP64 form equals the oracle bit for bit, so this is the error
@@ -327,6 +325,8 @@ def main():
         return es, eo
 
     errs, errs_out = form_errors(dev32, dev64)
+    esf, eof = form_errors(devf, dev64)
+    del ctxf, devf
     del ctx64, dev64
 
     # ---- the same batch from moist soundings: clouds and rain form, so the

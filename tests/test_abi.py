@@ -66,7 +66,7 @@ def test_create_without_device_fails_loudly(lib):
 
 
 def test_invalid_configurations_are_rejected(lib):
-    for kw in ({'crm_nx': 30}, {'crm_nx': 7}, {'plev': 20}, {'crm_dt': 40.0}, {'crm_ny': 4}):
+    for kw in ({'crm_nx': 14}, {'crm_nx': 7}, {'plev': 20}, {'crm_dt': 40.0}, {'crm_ny': 4}):
         cfg = S.config_32x28()
         cfg.max_ncrms = 4
         for k, v in kw.items():

@@ -288,3 +288,15 @@ def test_fp64_bitexact_random_columns(gpu_lib, seed):
     from test_oracle_properties import _case
     cfg, cin, st, rad, desc, ncol = _case(seed)
     assert mismatches(*run_both(cfg, cin, st, rad, desc)) == []
+
+
+@pytest.mark.parametrize('nx', [48, 80])
+def test_fp64_bitexact_radix_3_and_5_sizes(gpu_lib, nx):
+    """crm_nx with transform factors 3 (48 = 2 x 3 x 8) and 5 (80 = 2 x 5 x 8):
+    the warp FFT's radix-3 and radix-5 passes (fft.F90 vpassm_crm)."""
+    base = S.config_32x28()
+    cfg = T.CrmConfig(**{**base.__dict__, 'crm_nx': nx, 'crm_nx_rad': nx})
+    cin, st, rad, desc = S.make_inputs(cfg, 3, 300.0, 10.0, 100.0, seed=nx, moist=True)
+    desc.dt_gl = 400.0
+    assert mismatches(*run_both(cfg, cin, st, rad, desc)) == []
+
