@@ -77,6 +77,9 @@ static inline double fmax2(double a, double b) { return (b > a) ? b : a; }
 static inline double fmin2(double a, double b) { return (b < a) ? b : a; }
 static inline double fmax3(double a, double b, double c) { return fmax2(fmax2(a, b), c); }
 static inline double fmin3(double a, double b, double c) { return fmin2(fmin2(a, b), c); }
+// gammafff.c (crm/gammafff.c:12): the REAL*4 gamma function of the sam1mom
+// set-up, exp of the C library's lgamma rounded to float
+static float gammafff_r4(float x) { return (float)exp(lgamma((double)x)); }
 
 // ---------------------------------------------------------------- sat.F90
 // Flatau et al. (1992) polynomials; Murphy & Koop (2005) below -80 C.
@@ -2601,7 +2604,7 @@ static int setup_grid_constants(Grid &g, const crm_config *cfg, const crm_call_d
     }
   }
   // gamma functions: gammafff.c returns (float)exp(lgamma(x)) for float x
-  auto gammafff = [](float x) { return (float)exp(lgamma((double)x)); };
+  auto gammafff = [](float x) { return gammafff_r4(x); };
   g.gam3 = gammafff(3.f);
   g.gamr1 = gammafff((float)(3. + b_rain));
   g.gamr2 = gammafff((float)((5. + b_rain) / 2.));
@@ -2998,6 +3001,8 @@ int oracle_crm_run(const crm_config *cfg, const crm_call_desc *desc, const crm_i
 
 // Test hooks for known-answer checks of single routines.
 // RNG_MT: n draws after RNG_MT_set_seed(seed).
+float oracle_gammafff(float x) { return gammafff_r4(x); }
+
 int oracle_rng_mt(int seed, int n, double *out) {
   if (!out || n < 0) return CRM_ERR_ARG;
   RngMT r(seed);

@@ -59,6 +59,8 @@ def load(check=False):
         lib.oracle_sat.restype = C.c_int
         lib.oracle_sat.argtypes = [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int,
                                    C.POINTER(C.c_double)]
+        lib.oracle_gammafff.restype = C.c_float
+        lib.oracle_gammafff.argtypes = [C.c_float]
         lib.oracle_fft991.restype = C.c_int
         lib.oracle_fft991.argtypes = [C.POINTER(C.c_double), C.c_int, C.c_int]
         if check:
@@ -114,3 +116,10 @@ def sat(name, t, p=None):
                            t.size, out.ctypes.data_as(C.POINTER(C.c_double)))
     assert rc == 0
     return out
+
+
+def gammafff(x):
+    """The oracle's gammafff (crm/gammafff.c) for float arguments."""
+    lib = load()
+    return np.array([lib.oracle_gammafff(float(v)) for v in np.atleast_1d(x)], dtype=np.float32)
+

@@ -17,6 +17,10 @@ independent Python restatement:
                    mapping follow RNG_MT_set_seed / RNG_MT_gen_rand, in
                    Python integers with explicit 32-bit wrap-around.
 
+  crm/gammafff.c   compiled from the reference checkout itself
+                   (oracle/build_ref.py) and called: the gamma function of the
+                   sam1mom set-up at its ten arguments and on a sweep.
+
 Run once, with the reference checkout as argument:
 
     python tests/golden/make_kat.py <reference checkout>
@@ -144,6 +148,26 @@ def rng_draws(par, seed, n):
     return out
 
 
+def gamma_values(ref):
+    """gammafff(x) of the reference's compiled gammafff.c: the ten arguments
+    of precip_init.F90 / microphysics.F90 (3 + b, (5 + b) / 2, 4 + b for
+    rain, snow, graupel, and 3) and a sweep of 0.5..12."""
+    import ctypes as C
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))),
+                                    'oracle'))
+    import build_ref
+    lib = C.CDLL(build_ref.build(ref))
+    f = lib.gammafff
+    f.restype = C.c_float
+    f.argtypes = [C.POINTER(C.c_float)]
+    b = {'rain': r4(0.8), 'snow': 0.25, 'grau': 0.5}
+    xs = [3.0]
+    for v in b.values():
+        xs += [3.0 + v, (5.0 + v) / 2.0, 4.0 + v]
+    xs = [float(np.float32(x)) for x in xs] + [float(x) for x in np.linspace(0.5, 12.0, 47, dtype=np.float32)]
+    return {'x': xs, 'value': [float(f(C.byref(C.c_float(x)))) for x in xs]}
+
+
 def main(ref):
     funcs, cold, cold_i = parse_sat(os.path.join(ref, CRM, 'sat.F90'))
     f = sat_functions(funcs, cold, cold_i)
@@ -154,9 +178,10 @@ def main(ref):
     seeds = [1000, 17000, 1024000, 12345000]
     rng = {str(sd): rng_draws(par, sd, 700) for sd in seeds}
     data = {'source': {'sat': 'components/cam/src/physics/crm/sat.F90',
-                       'rng': 'components/cam/src/physics/cam/RNG_MT.F90'},
+                       'rng': 'components/cam/src/physics/cam/RNG_MT.F90',
+                       'gammafff': 'components/cam/src/physics/crm/gammafff.c (compiled, gcc, glibc libm)'},
             'sat_t': temps, 'sat_p': press, 'sat': sat, 'sat_coefficients': funcs,
-            'rng_parameters': par, 'rng': rng}
+            'rng_parameters': par, 'rng': rng, 'gammafff': gamma_values(ref)}
     out = os.path.join(os.path.dirname(os.path.abspath(__file__)), 'kat.json')
     with open(out, 'w') as fh:
         json.dump(data, fh, indent=0)

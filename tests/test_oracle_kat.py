@@ -1,6 +1,8 @@
 """Known-answer checks of single routines of the oracle against values
 computed from the reference's own source text (tests/golden/kat.json,
-generated by tests/golden/make_kat.py from crm/sat.F90 and cam/RNG_MT.F90).
+generated by tests/golden/make_kat.py from crm/sat.F90 and cam/RNG_MT.F90)
+and against the reference's own C code (crm/gammafff.c, compiled by
+oracle/build_ref.py).
 
 These pin the restatement where the reference defines a routine by a
 formula or table that can be evaluated independently:
@@ -54,3 +56,24 @@ def test_kat_constants_are_the_references():
     par = KAT['rng_parameters']
     assert (par['N'], par['M'], par['SEEDMUL']) == (624, 397, 69069)
     assert par['UMASK'] == -1147483648
+
+
+def test_gammafff_equals_the_reference_build():
+    """The oracle's gammafff against values of the reference's own gammafff.c
+    compiled and called (tests/golden/make_kat.py): equal floats at the ten
+    arguments of the sam1mom set-up and on a sweep; and, where the reference
+    checkout is present (oracle/_ref), against the compiled function itself."""
+    g = KAT['gammafff']
+    x = np.array(g['x'], dtype=np.float32)
+    assert np.array_equal(oracle.gammafff(x), np.array(g['value'], dtype=np.float32))
+    import ctypes as C
+    import build_ref
+    path = build_ref.build()
+    if path is None:
+        pytest.skip('no reference checkout here: checked against the committed values only')
+    f = C.CDLL(path).gammafff
+    f.restype = C.c_float
+    f.argtypes = [C.POINTER(C.c_float)]
+    xs = np.linspace(0.3, 20.0, 301, dtype=np.float32)
+    ref = np.array([f(C.byref(C.c_float(float(v)))) for v in xs], dtype=np.float32)
+    assert np.array_equal(oracle.gammafff(xs), ref)
