@@ -249,6 +249,8 @@ def main():
             step_ms.append(dt)
             kms.append(ctx.last_kernel_ms)
         medians[tag] = float(np.median(step_ms))
+        if tag not in tuned:
+            tuned[tag] = {'shape': ctx.launch_shape(), 'ms_per_step_median': round(medians[tag], 2)}
         barrier()
         t = torch.tensor([tot], device='cuda')
         if ws > 1:
