@@ -227,9 +227,15 @@ def main():
         if args.autotune and tune:
             best, times = autotune(ctx, dev, w_st, reps=1, stream=stream)
             tuned[tag] = {'shape': best, 'ms_per_shape': {str(k): round(v, 2) for k, v in times.items()}}
-        for _ in range(warmup):
+        # warm-up: at least `warmup` calls and at least 2 s of device work
+        # (a GPU coming out of idle runs its first seconds slower)
+        t_w = time.perf_counter()
+        nw = 0
+        while nw < warmup or time.perf_counter() - t_w < 2.0:
             dev.reset_state(w_st)
             ctx.run_device(dev, stream)
+            torch.cuda.synchronize()
+            nw += 1
         barrier()
         # each step restarts from the same initial state (igstep 1): the
         # state (213 MB) is re-read from HBM every step, larger than L2

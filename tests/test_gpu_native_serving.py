@@ -135,3 +135,28 @@ def test_native_admission_limits(gpu_lib):
     t = srv.submit(cb, b[0], 4, DT_GL, fields=STEP)
     assert t.poll() == 0
     srv.close()
+
+
+def test_native_3d_step_equals_crm_run(gpu_lib):
+    """The service with a 3D configuration (16 x 16 x 58, FP64): the first
+    step of a chunk equals crm_run of the same columns bit for bit."""
+    from crm_gb300.lib import CrmContext
+    from crm_gb300.native_server import NativeCrmServer
+    cfg, cin, st, rad, desc = S.workload_3d(ncrms=3, nx=16, ny=16, precision=T.CRM_FP64)
+    gcol = list(np.asarray(desc._keep))
+    dt_gl = 100.0
+    srv = NativeCrmServer(cfg, capacity=8, handles=2)
+    c = srv.open_chunk(st, rad, gcol)
+    t = srv.submit(c, cin, 3, dt_gl, rad_means=True)
+    assert t.poll() == 0 and not t.status.any()
+    st_dev, _ = srv.read_state(c, 3)
+    srv.close()
+    c2 = T.CrmConfig(**{**cfg.__dict__, 'max_ncrms': 3})
+    out = T.CrmOutput(3, cfg.crm_nx, cfg.crm_ny, cfg.crm_nz, cfg.plev)
+    st2, rad2 = st.copy(), rad.copy()
+    status = CrmContext(c2).run(T.call_desc(3, 3, dt_gl, 1, gcol), cin, st2, rad2, out)
+    assert not status.any()
+    for n, v in out.arrays().items():
+        assert np.array_equal(v, getattr(t.out, n)), n
+    for n, v in st2.arrays().items():
+        assert np.array_equal(v, getattr(st_dev, n)), n
