@@ -111,6 +111,7 @@ struct ColShared {
   unsigned long long tc_mbar;
   unsigned tc_tmem, tc_phase;
   int tc_fail;
+  int tmin_bits;                    // column minimum of t (FP32 bits)
 };
 
 // The CRM's horizontal size: a compile-time constant for the sizes built
@@ -1261,9 +1262,15 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
       if (k >= max(1, kmin - 2) && k <= kmax) {
         T coef = dtn / (dz * adz[k] * rho[k]);
         T dqi = coef * (fz(i, k) - fz(i, k + 1));
-        qt(i, k) = qt(i, k) + dqi;
         T lat_heat = (T)(C_FAC_COND + C_FAC_FUS) * dqi;
-        t(i, k) = t(i, k) - lat_heat;
+        if constexpr (sizeof(T) == 8) {
+          qt(i, k) = qt(i, k) + dqi;
+          t(i, k) = t(i, k) - lat_heat;
+        } else {
+          // FP32-mixed form: through the carried residues
+          qt(i, k) = add_carry(qt(i, k), dqi, rcq()[e]);
+          t(i, k) = add_carry(t(i, k), -lat_heat, rct()[e]);
+        }
       }
     }
     for (int i = TID + 1; i <= NH(); i += NT) {
@@ -1393,7 +1400,18 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
       T qp_if = (T)0.5 * (qpl(i, kc) + qpi(i, kc) + qpl(i, kb) + qpi(i, kb));
       T bbb = (T)1. + epsv * qtot_if - qp_if;
       T dqtot = qv(i, kc) + qcl(i, kc) + qci(i, kc) - qv(i, kb) - qcl(i, kb) - qci(i, kb);
-      T bs = betdz * (bbb * (t(i, kc) - t(i, kb)) + epsv * tabs_if * dqtot +
+      T dtk = t(i, kc) - t(i, kb);
+      if constexpr (sizeof(T) == 4) {
+        // FP32-mixed form: the vertical differences of t and of the total
+        // water with their carried residues.  In a well-mixed layer the
+        // difference of t is a few FP32 units of ~300 K, and the residues
+        // (up to half a unit each) changed the stability, hence tk and tkh,
+        // by ~1e-3 and the boundary layer's heat flux with them.
+        const size_t oc = (size_t)(i - 1) + (size_t)NH() * (kc - 1), ob = (size_t)(i - 1) + (size_t)NH() * (kb - 1);
+        dtk = dtk + (rct()[oc] - rct()[ob]);
+        dqtot = dqtot + (rcq()[oc] - rcq()[ob]);
+      }
+      T bs = betdz * (bbb * dtk + epsv * tabs_if * dqtot +
                       (bbb * fc - tabs_if) * (qpl(i, kc) - qpl(i, kb)) + (bbb * fs - tabs_if) * (qpi(i, kc) - qpi(i, kb)));
       T ap = (T)-0.5 * (tkh(i, kc) + tkh(i, kb) + (T)R4(0.002)) * bs;
       T qctot = qcl(i, kc) + qci(i, kc) + qcl(i, kb) + qci(i, kb);
@@ -1408,7 +1426,7 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
           T qsatt = omn * qsatw(tif, presi[k + 1]) + ((T)1. - omn) * qsati(tif, presi[k + 1]);
           T b2 = (T)1. + epsv * qsatt + qsatt - qtot_if - qpif + (T)R4(1.61) * tif * dqsat;
           b2 = b2 / ((T)1. + lstarn * dqsat);
-          bs = betdz * (b2 * (t(i, kc) - t(i, kb)) + (b2 * lstarn - ((T)1. + lstarn * dqsat) * tif) * dqtot +
+          bs = betdz * (b2 * dtk + (b2 * lstarn - ((T)1. + lstarn * dqsat) * tif) * dqtot +
                         (b2 * fc - ((T)1. + fc * dqsat) * tabs(i, k)) * (qpl(i, kc) - qpl(i, kb)) +
                         (b2 * fs - ((T)1. + fs * dqsat) * tabs(i, k)) * (qpi(i, kc) - qpi(i, kb)));
           ap = (T)-0.5 * (tkh(i, kc) + tkh(i, kb) + (T)R4(0.002)) * bs;
@@ -2319,6 +2337,50 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
   }
 
   // ---------------------------------------------------------- adams / uvw
+  // FP32-mixed form: t advected as its offset from a column constant c,
+  // an integer 4 K below the column's minimum t (t - c and c + t' are formed
+  // as exact two-sums, the rounding into t's residue).  MPDATA's
+  // antidiffusive fluxes and limiter depend on t only through differences,
+  // and the upwind pass on a divergence-free velocity (discrete divergence D
+  // = 0) advects a constant unchanged, so the offset changes nothing in exact
+  // arithmetic; with D != 0 the result would differ by c D, so the caller
+  // uses this form only where the advecting velocity is the mean of two
+  // projected fields.  In FP32 the upwind fluxes of the lowest levels are
+  // formed from values of a few K instead of ~300 K: the flux rounding behind
+  // the level means of t, hence sltend, drops with them (measured on 64x58
+  // dry columns over 1200 s: sltend 1.3e-4 -> 5.8e-5 relative L2).
+  __device__ void advect_t_offset() {
+    FT t = TT();
+    T *rc = rct();
+    if (TID == 0) S.tmin_bits = 0x7f7fffff;
+    SYNC;
+    float m = 3.0e38f;
+    for (int e = TID; e < NH() * nzm; e += NT) m = fminf(m, (float)t(1 + e % NH(), 1 + e / NH()));
+    for (int o = 16; o > 0; o >>= 1) m = fminf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((TID & 31) == 0) atomicMin(&S.tmin_bits, __float_as_int(m));
+    SYNC;
+    const T c = (T)(floorf(__int_as_float(S.tmin_bits)) - 4.f);
+    // every cell of the plane, halos included (i = -2..nx+3, j = -2..ny+3)
+    const int wx = nx + 6, wy = Y3 ? ny + 6 : 1;
+    auto shift = [&](bool back) {
+      for (int e = TID; e < wx * wy * nzm; e += NT) {
+        const int i = -2 + e % wx, j = Y3 ? -2 + (e / wx) % wy : 1, k = 1 + e / (wx * wy);
+        T &v = Y3 ? t(i, j, k) : t(i, k);
+        if (i >= 1 && i <= nx && j >= 1 && j <= ny) {
+          T er = (T)0.;
+          v = back ? add_carry(c, v, er) : add_carry(v, -c, er);
+          rc[(size_t)(i - 1) + (size_t)nx * (j - 1) + (size_t)nx * ny * (k - 1)] += er;
+        } else {
+          v = back ? v + c : v - c;
+        }
+      }
+      SYNC;
+    };
+    shift(false);
+    if constexpr (Y3) advect_scalar3(t, nullptr, nullptr, rc);
+    else advect_scalar(t, nullptr, nullptr, rc);
+    shift(true);
+  }
   __device__ void adams() {                    // adams.F90:17-38
     FT u = U(), v = V(), w = W();
     FT dua = DU(S.na), dub = DU(S.nb), duc = DU(S.nc);
@@ -2336,9 +2398,40 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
       duc(i, k) = un; dvc(i, k) = vn; dwc(i, k) = wn;
       u(i, k) = (T)0.5 * (u(i, k) + un) * rhox;
       v(i, k) = (T)0.5 * (v(i, k) + vn) * rhoy;
-      w(i, k) = (T)0.5 * (w(i, k) + wn) * rhoz;
+      if constexpr (sizeof(T) == 8) w(i, k) = (T)0.5 * (w(i, k) + wn) * rhoz;
     }
     SYNC;
+    if constexpr (sizeof(T) == 4) {
+      // FP32-mixed form: the projected new w has zero horizontal mean at
+      // every level in exact arithmetic (anelastic continuity, periodic
+      // sides, w = 0 at the surface; the FP64 form's means are ~1e-16 of the
+      // level's rms w).  FP32 rounding in the momentum and pressure phases
+      // leaves a mean of ~1e-6 of the rms, and the upwind scalar fluxes of
+      // the next advection multiply it by the level's mean value (~300 K for
+      // t), which moved the level means of t by ~1e-4 of their change over a
+      // call.  The mean, summed in FP64, is taken out of the new w before it
+      // forms the advecting flux (w = 0.5 (w_old + w_new) rho dt/dz).
+      T *wm = PR(P_TMP0);
+      const int lane = TID & 31, warp = TID >> 5, nw = NT >> 5;
+      const double fxy = 1. / (double)NH();
+      for (int k = 2 + warp; k <= nzm; k += nw) {
+        double sm = 0.;
+        for (int h = 1 + lane; h <= NH(); h += 32) sm = sm + (double)dwc(h, k);
+        for (int o = 16; o > 0; o >>= 1) sm = sm + __shfl_xor_sync(0xffffffffu, sm, o);
+        if (lane == 0) wm[k] = (T)(sm * fxy);
+      }
+      SYNC;
+      for (int e = TID; e < NH() * nzm; e += NT) {
+        const int i = 1 + e % NH(), k = 1 + e / NH();
+        T wn = dwc(i, k);
+        if (k >= 2) {
+          wn = wn - wm[k];
+          dwc(i, k) = wn;
+        }
+        w(i, k) = (T)0.5 * (w(i, k) + wn) * (rhow[k] * dtdz);
+      }
+      SYNC;
+    }
   }
   __device__ void uvw() {                      // uvw.F90
     FT u = U(), v = V(), w = W(), duc = DU(S.nc), dvc = DV(S.nc), dwc = DW(S.nc);
@@ -2899,9 +2992,9 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
         T lf_k = fc + ((T)1. - omk) * ffus;
         const T qpn = qp(i, k) - (fzc - fzk) * ia;
         T lat_heat = -(lf_c * fzc - lf_k * fzk) * ia;
-        const T tn = t(i, k) - lat_heat;
         qp(i, k) = qpn;
-        t(i, k) = tn;
+        if constexpr (sizeof(T) == 8) t(i, k) = t(i, k) - lat_heat;
+        else t(i, k) = add_carry(t(i, k), -lat_heat, rct()[e]);   // FP32-mixed form: carried
         if (k == 1) {
           PS(i) = PS(i) - fzk * (T)1.;
           PSS(i) = PSS(i) - fzk * ((T)1. - omk) * (T)1.;
@@ -3843,14 +3936,18 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
         boundaries(2);
         PHASE_MARK(PH_ADAMS);
         if constexpr (Y3) {
-          advect_scalar3(TT(), nullptr, nullptr, rct());
+          if (sizeof(T) == 4 && (nstep >= 2 || icyc >= 2)) advect_t_offset();
+          else advect_scalar3(TT(), nullptr, nullptr, rct());
           PHASE_MARK(PH_ADV_T);
           advect_scalar3(QT(), PR(P_MKADV0), PR(P_MKWLE0), rcq());
           PHASE_MARK(PH_ADV_QT);
           if (all_pos_zero(QP())) zero_stats(PR(P_MKADV1), PR(P_MKWLE1));
           else advect_scalar3(QP(), PR(P_MKADV1), PR(P_MKWLE1));
         } else {
-          advect_scalar(TT(), nullptr, nullptr, rct());
+          // the offset form needs a divergence-free advecting velocity, the
+          // mean of two projected fields: from the second substep of the call
+          if (sizeof(T) == 4 && (nstep >= 2 || icyc >= 2)) advect_t_offset();
+          else advect_scalar(TT(), nullptr, nullptr, rct());
           PHASE_MARK(PH_ADV_T);
           advect_scalar(QT(), PR(P_MKADV0), PR(P_MKWLE0), rcq());
           PHASE_MARK(PH_ADV_QT);

@@ -2,7 +2,8 @@
 
 The mixed form keeps FP64 only for the pressure tridiagonal solve, the domain
 sums and the saturation-adjustment Newton iteration; t and qt carry per-cell
-FP32 residues of their updates.  After one GCM step (60-120 CRM steps of a
+FP32 residues of their updates, the projected w has its level means taken
+out, and t is advected as an offset from a column constant.  After one GCM step (60-120 CRM steps of a
 convecting boundary layer) rounding differences have been amplified by the
 flow, so the comparison is statistical: relative L2 error per field, with the
 bounds stated below, plus exact agreement of the status codes.
@@ -19,15 +20,15 @@ from conftest import rel_l2
 
 pytestmark = pytest.mark.gpu
 
-# relative L2 bounds after one GCM step: state fields and GCM tendencies
-# (measured 1e-7..9e-4; every other crm() output is held to OUTPUT_BOUND,
-# measured <= 6e-3)
-BOUNDS = {'temperature': 1e-6, 'qt': 2e-5, 'u_wind': 1e-4, 'w_wind': 3e-3, 'qp': 5e-4,
-          'sltend': 5e-4, 'qltend': 5e-4, 'qcltend': 5e-4, 'qiltend': 5e-4}
-OUTPUT_BOUND = 3e-2
-# the tendency target (1e-4 relative L2), met where the GCM step's
-# temperature change is large against FP32 resolution of the static energy
+# the tendency target: every GCM tendency within 1e-4 relative L2
 TENDENCY_TARGET = 1e-4
+# relative L2 bounds after one GCM step: state fields, and the GCM
+# tendencies at the target; every other crm() output is held to
+# OUTPUT_BOUND (measured <= 6e-3)
+BOUNDS = {'temperature': 1e-6, 'qt': 2e-5, 'u_wind': 1e-4, 'w_wind': 3e-3, 'qp': 5e-4,
+          'sltend': TENDENCY_TARGET, 'qltend': TENDENCY_TARGET, 'qcltend': TENDENCY_TARGET,
+          'qiltend': TENDENCY_TARGET}
+OUTPUT_BOUND = 3e-2
 
 
 def _errors(wl, **kw):
@@ -48,8 +49,8 @@ def _errors(wl, **kw):
     return e
 
 
-def _check(e):
-    for n, b in BOUNDS.items():
+def _check(e, **override):
+    for n, b in {**BOUNDS, **override}.items():
         assert e[n] <= b, (n, e[n], b)
     for n, v in e.items():
         assert v <= OUTPUT_BOUND, (n, v, OUTPUT_BOUND)
@@ -60,16 +61,13 @@ def test_fp32_mixed_32x28(gpu_lib, moist):
     e = _errors(S.workload_32x28, ncrms=4, moist=moist)
     print('fp32-mixed rel-L2 vs fp64 oracle (32x28, moist=%s):' % moist, e)
     _check(e)
-    if moist:
-        for n in ('sltend', 'qltend', 'qcltend', 'qiltend'):
-            assert e[n] <= TENDENCY_TARGET, (n, e[n])
 
 
-def test_fp32_mixed_64x58(gpu_lib):
-    e = _errors(S.workload_64x58, ncrms=4)
-    print('fp32-mixed rel-L2 vs fp64 oracle (64x58):', e)
+@pytest.mark.parametrize('moist', [False, True])
+def test_fp32_mixed_64x58(gpu_lib, moist):
+    e = _errors(S.workload_64x58, ncrms=4, moist=moist)
+    print('fp32-mixed rel-L2 vs fp64 oracle (64x58, moist=%s):' % moist, e)
     _check(e)
-    assert e['qltend'] <= TENDENCY_TARGET, e['qltend']
 
 
 def test_fp32_mixed_mean_state_acceleration(gpu_lib):
@@ -79,7 +77,9 @@ def test_fp32_mixed_mean_state_acceleration(gpu_lib):
         return cfg, cin, st, rad, desc
     e = _errors(wl, ncrms=4, moist=True)
     print('fp32-mixed rel-L2 vs fp64 oracle (32x28, accelerated):', e)
-    _check(e)
+    # the acceleration multiplies each level mean's change per step, and its
+    # rounding, by up to 1 + crm_accel_factor = 3: the target scaled by 3
+    _check(e, **{n: 3 * TENDENCY_TARGET for n in ('sltend', 'qltend', 'qcltend', 'qiltend')})
 
 
 def test_fp32_mixed_water_budget(gpu_lib):
@@ -147,5 +147,7 @@ def test_fp32_mixed_reference_batch_mode(gpu_lib):
         return cfg, cin, st, rad, desc
     e = _errors(wl, ncrms=4, moist=True)
     print('fp32-mixed rel-L2 vs fp64 oracle (32x28, reference batch mode):', e)
-    for n in ('temperature', 'qt', 'u_wind', 'sltend', 'qltend'):
-        assert e[n] <= 10 * BOUNDS[n], (n, e[n])
+    # a 40 m/s column drives the batch's ncycle: ten times the field bounds,
+    # 5e-3 on the tendencies
+    for n, b in (('temperature', 1e-5), ('qt', 2e-4), ('u_wind', 1e-3), ('sltend', 5e-3), ('qltend', 5e-3)):
+        assert e[n] <= b, (n, e[n])
