@@ -256,7 +256,7 @@ def main():
             kms.append(ctx.last_kernel_ms)
         medians[tag] = float(np.median(step_ms))
         if tag not in tuned:
-            tuned[tag] = {'shape': ctx.launch_shape(), 'ms_per_step_median': round(medians[tag], 2)}
+            tuned[tag] = {'shape': ctx.launch_shape, 'ms_per_step_median': round(medians[tag], 2)}
         barrier()
         t = torch.tensor([tot], device='cuda')
         if ws > 1:
