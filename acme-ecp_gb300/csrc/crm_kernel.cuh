@@ -111,7 +111,7 @@ struct ColShared {
   unsigned long long tc_mbar;
   unsigned tc_tmem, tc_phase;
   int tc_fail;
-  int tmin_bits;                    // column minimum of t (FP32 bits)
+  float t_off;                      // FP32-mixed form: t's offset in the upwind fluxes
 };
 
 // The CRM's horizontal size: a compile-time constant for the sizes built
@@ -903,6 +903,7 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
             md[(size_t)q[a] * (nz + 2) + k] = m[a];
             PR(ids9(q[a]))[k] = (T)m[a];
           }
+          if (k == 1) S.t_off = rintf((float)m[0]);
         }
       }
       SYNC;
@@ -1091,6 +1092,7 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
     // dt 10 s would be biased by up to ~5 %.  Its t forcing is added after
     // the fixer below, which does not read t.
     T *rc_t = rct(), *rc_q = rcq();
+    int neg_any = 0;
     for (int e = TID; e < NH() * nzm; e += NT) {
       int i = 1 + e % NH(), k = 1 + e / NH();
       if constexpr (sizeof(T) == 8) {
@@ -1099,10 +1101,26 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
       } else {
         qt(i, k) = add_carry(qt(i, k), qtend[k] * dtn, rc_q[e]);
       }
+      neg_any |= qt(i, k) < (T)0.;
       du(i, k) = du(i, k) + utend[k];
       dv(i, k) = dv(i, k) + vtend[k];
     }
-    SYNC;
+    const int qrad_base = 5;
+    const int gx = NH() / NR(), nxr = NR();
+    const T *qrad = base + p.L.rad + (size_t)qrad_base * nxr * nzm;    // (nx_rad, nzm), cached at init
+    if (!__syncthreads_or(neg_any)) {
+      // no negative qt in the column: every level's count is zero and the
+      // fixer below changes nothing (its sums are skipped)
+      for (int e = TID; e < NH() * nzm; e += NT) {
+        int i = 1 + e % NH(), k = 1 + e / NH();
+        int i_rad = (i - 1) / gx + 1;
+        T qr = qrad[(size_t)(k - 1) * nxr + (i_rad - 1)];
+        if constexpr (sizeof(T) == 8) t(i, k) = t(i, k) + qr * dtn;
+        else t(i, k) = add_carry(t(i, k), ttend[k] * dtn + qr * dtn, rc_t[e]);
+      }
+      SYNC;
+      return;
+    }
     // negative-vapour fixer: per-level sums (a cell outside a sum adds an
     // exact zero, which leaves a sum that starts at +0 unchanged)
     T *qneg = PR(P_TMP0), *qpoz = PR(P_TMP1), *nneg = PR(P_TMP2);
@@ -1124,8 +1142,6 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
                [&](int, int) { return 0.; },
                [&](int q, int k, double sv) { (q == 0 ? qneg : q == 1 ? qpoz : nneg)[k] = (T)sv; });
     SYNC;
-    const int gx = NH() / NR(), nxr = NR();
-    const T *qrad = base + p.L.rad + (size_t)5 * nxr * nzm;    // (nx_rad, nzm), cached at init
     for (int e = TID; e < NH() * nzm; e += NT) {
       int i = 1 + e % NH(), k = 1 + e / NH();
       if (nneg[k] > (T)0. && qpoz[k] + qneg[k] > (T)0.) {
@@ -2337,50 +2353,6 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
   }
 
   // ---------------------------------------------------------- adams / uvw
-  // FP32-mixed form: t advected as its offset from a column constant c,
-  // an integer 4 K below the column's minimum t (t - c and c + t' are formed
-  // as exact two-sums, the rounding into t's residue).  MPDATA's
-  // antidiffusive fluxes and limiter depend on t only through differences,
-  // and the upwind pass on a divergence-free velocity (discrete divergence D
-  // = 0) advects a constant unchanged, so the offset changes nothing in exact
-  // arithmetic; with D != 0 the result would differ by c D, so the caller
-  // uses this form only where the advecting velocity is the mean of two
-  // projected fields.  In FP32 the upwind fluxes of the lowest levels are
-  // formed from values of a few K instead of ~300 K: the flux rounding behind
-  // the level means of t, hence sltend, drops with them (measured on 64x58
-  // dry columns over 1200 s: sltend 1.3e-4 -> 5.8e-5 relative L2).
-  __device__ void advect_t_offset() {
-    FT t = TT();
-    T *rc = rct();
-    if (TID == 0) S.tmin_bits = 0x7f7fffff;
-    SYNC;
-    float m = 3.0e38f;
-    for (int e = TID; e < NH() * nzm; e += NT) m = fminf(m, (float)t(1 + e % NH(), 1 + e / NH()));
-    for (int o = 16; o > 0; o >>= 1) m = fminf(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if ((TID & 31) == 0) atomicMin(&S.tmin_bits, __float_as_int(m));
-    SYNC;
-    const T c = (T)(floorf(__int_as_float(S.tmin_bits)) - 4.f);
-    // every cell of the plane, halos included (i = -2..nx+3, j = -2..ny+3)
-    const int wx = nx + 6, wy = Y3 ? ny + 6 : 1;
-    auto shift = [&](bool back) {
-      for (int e = TID; e < wx * wy * nzm; e += NT) {
-        const int i = -2 + e % wx, j = Y3 ? -2 + (e / wx) % wy : 1, k = 1 + e / (wx * wy);
-        T &v = Y3 ? t(i, j, k) : t(i, k);
-        if (i >= 1 && i <= nx && j >= 1 && j <= ny) {
-          T er = (T)0.;
-          v = back ? add_carry(c, v, er) : add_carry(v, -c, er);
-          rc[(size_t)(i - 1) + (size_t)nx * (j - 1) + (size_t)nx * ny * (k - 1)] += er;
-        } else {
-          v = back ? v + c : v - c;
-        }
-      }
-      SYNC;
-    };
-    shift(false);
-    if constexpr (Y3) advect_scalar3(t, nullptr, nullptr, rc);
-    else advect_scalar(t, nullptr, nullptr, rc);
-    shift(true);
-  }
   __device__ void adams() {                    // adams.F90:17-38
     FT u = U(), v = V(), w = W();
     FT dua = DU(S.na), dub = DU(S.nb), duc = DU(S.nc);
@@ -2490,7 +2462,23 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
     SYNC;
   }
 
-  __device__ void advect_scalar(FT f, T *fadv, T *flux, T *rc = nullptr) {
+  // FP32-mixed form: the offset of t in the upwind fluxes.  The upwind pass
+  // forms u+ f(i-1) + u- f(i) (and the w terms) from values of ~300 K, and
+  // their rounding, through the level means of t, was the largest part of
+  // the form's sltend error.  With a column constant c taken out of f in
+  // those products the update changes by c D, D the advecting velocity's
+  // discrete divergence, which is zero in exact arithmetic when that
+  // velocity is the mean of two projected fields: from the second substep
+  // of the call (the first one's old velocity is the input state).  Every
+  // other MPDATA term sees f only through differences, and the update is
+  // applied to t itself through the carried residue.  c: the call's initial
+  // level-1 mean of t, rounded to an integer.  Measured on 64x58 dry columns
+  // over 1200 s: sltend 1.3e-4 -> ~6e-5 relative L2.
+  __device__ __forceinline__ T t_offset(int nstep, int icyc) const {
+    if constexpr (sizeof(T) == 4) return (nstep >= 2 || icyc >= 2) ? (T)S.t_off : (T)0.;
+    return (T)0.;
+  }
+  __device__ void advect_scalar(FT f, T *fadv, T *flux, T *rc = nullptr, T c = (T)0.) {
     FT u = U(), w = W();
     FT mx = SA(), mn = SB(), uuu = SCR(p.L.s_c), www = SCR(p.L.s_d), f0 = SCR(p.L.s_e);
     FT wfl1 = SCR(p.L.s_f);
@@ -2513,8 +2501,8 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
         r.mx = mx2(mx2(mx2(mx2(fb, fc), fkb), fkc), fk);
         r.mn = mn2(mn2(mn2(mn2(fb, fc), fkb), fkc), fk);
         r.fk = fk;
-        r.uuu = mx2((T)0., uk) * fb + mn2((T)0., uk) * fk;
-        r.www = mx2((T)0., wk) * fkb + mn2((T)0., wk) * fk;
+        r.uuu = mx2((T)0., uk) * (fb - c) + mn2((T)0., uk) * (fk - c);
+        r.www = mx2((T)0., wk) * (fkb - c) + mn2((T)0., wk) * (fk - c);
         return r;
       },
       [&](int, const R1 &r) {
@@ -2670,7 +2658,7 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
   // advect_scalar.F90 wrapper's fadv; scratch planes: mx, mn in A, B, the
   // fluxes uuu, vvv, www in C, D, E, the initial field in F, the first-pass
   // vertical flux sum in G
-  __device__ void advect_scalar3(FT f, T *fadv, T *flux, T *rc = nullptr) {
+  __device__ void advect_scalar3(FT f, T *fadv, T *flux, T *rc = nullptr, T c = (T)0.) {
     FT u = U(), v = V(), w = W();
     FT mx = SA(), mn = SB(), uuu = SCR(p.L.s_c), vvv = SCR(p.L.s_d), www = SCR(p.L.s_e), f0 = SCR(p.L.s_f);
     FT wfl1 = SCR(p.L.s_g);
@@ -2693,15 +2681,15 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
         }
         if (j <= ny + 2) {
           const T uk = u(i, j, k);
-          uuu(i, j, k) = mx2((T)0., uk) * f(i - 1, j, k) + mn2((T)0., uk) * f(i, j, k);
+          uuu(i, j, k) = mx2((T)0., uk) * (f(i - 1, j, k) - c) + mn2((T)0., uk) * (f(i, j, k) - c);
         }
         if (i <= nx + 2) {
           const T vk = v(i, j, k);
-          vvv(i, j, k) = mx2((T)0., vk) * f(i, j - 1, k) + mn2((T)0., vk) * f(i, j, k);
+          vvv(i, j, k) = mx2((T)0., vk) * (f(i, j - 1, k) - c) + mn2((T)0., vk) * (f(i, j, k) - c);
         }
         if (i <= nx + 2 && j <= ny + 2) {
           const T wk = w(i, j, k);
-          www(i, j, k) = mx2((T)0., wk) * f(i, j, kb) + mn2((T)0., wk) * f(i, j, k);
+          www(i, j, k) = mx2((T)0., wk) * (f(i, j, kb) - c) + mn2((T)0., wk) * (f(i, j, k) - c);
           if (k == 1) www(i, j, nz) = (T)0.;
         }
         if (fadv && i >= 1 && i <= nx && j >= 1 && j <= ny) f0(i, j, k) = f(i, j, k);
@@ -3936,18 +3924,14 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
         boundaries(2);
         PHASE_MARK(PH_ADAMS);
         if constexpr (Y3) {
-          if (sizeof(T) == 4 && (nstep >= 2 || icyc >= 2)) advect_t_offset();
-          else advect_scalar3(TT(), nullptr, nullptr, rct());
+          advect_scalar3(TT(), nullptr, nullptr, rct(), t_offset(nstep, icyc));
           PHASE_MARK(PH_ADV_T);
           advect_scalar3(QT(), PR(P_MKADV0), PR(P_MKWLE0), rcq());
           PHASE_MARK(PH_ADV_QT);
           if (all_pos_zero(QP())) zero_stats(PR(P_MKADV1), PR(P_MKWLE1));
           else advect_scalar3(QP(), PR(P_MKADV1), PR(P_MKWLE1));
         } else {
-          // the offset form needs a divergence-free advecting velocity, the
-          // mean of two projected fields: from the second substep of the call
-          if (sizeof(T) == 4 && (nstep >= 2 || icyc >= 2)) advect_t_offset();
-          else advect_scalar(TT(), nullptr, nullptr, rct());
+          advect_scalar(TT(), nullptr, nullptr, rct(), t_offset(nstep, icyc));
           PHASE_MARK(PH_ADV_T);
           advect_scalar(QT(), PR(P_MKADV0), PR(P_MKWLE0), rcq());
           PHASE_MARK(PH_ADV_QT);
