@@ -2462,23 +2462,27 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
     SYNC;
   }
 
-  // FP32-mixed form: the offset of t in the upwind fluxes.  The upwind pass
-  // forms u+ f(i-1) + u- f(i) (and the w terms) from values of ~300 K, and
-  // their rounding, through the level means of t, was the largest part of
-  // the form's sltend error.  With a column constant c taken out of f in
-  // those products the update changes by c D, D the advecting velocity's
-  // discrete divergence, which is zero in exact arithmetic when that
-  // velocity is the mean of two projected fields: from the second substep
-  // of the call (the first one's old velocity is the input state).  Every
-  // other MPDATA term sees f only through differences, and the update is
-  // applied to t itself through the carried residue.  c: the call's initial
-  // level-1 mean of t, rounded to an integer.  Measured on 64x58 dry columns
-  // over 1200 s: sltend 1.3e-4 -> ~6e-5 relative L2.
+  // FP32-mixed form: t is advected as its offset from a column constant c
+  // (the call's initial level-1 mean of t, rounded to an integer).  The
+  // upwind pass forms its fluxes u+ f(i-1) + u- f(i) (and the w terms) from
+  // f - c, writes the intermediate field as f - c (with the bounds of the
+  // limiter), and the final update adds c back through an exact two-sum into
+  // the carried residue; the positive-definite clip sees the value itself.
+  // The upwind update changes by c D, D the advecting velocity's discrete
+  // divergence, which is zero in exact arithmetic when that velocity is the
+  // mean of two projected fields: from the second substep of the call (the
+  // first one's old velocity is the input state).  Every other MPDATA term
+  // sees f only through differences.  In FP32 the lowest levels' fluxes and
+  // intermediate values are then a few K instead of ~300 K, and their
+  // rounding, which reached the level means of t and so sltend, drops with
+  // them (64x58 dry columns over 1200 s: sltend 1.3e-4 -> 5.8e-5 relative
+  // L2; over 100 s 7e-5 -> 2.9e-5).  The halos the upwind pass writes keep
+  // the offset; the next exchange before any read of them rewrites them.
   __device__ __forceinline__ T t_offset(int nstep, int icyc) const {
     if constexpr (sizeof(T) == 4) return (nstep >= 2 || icyc >= 2) ? (T)S.t_off : (T)0.;
     return (T)0.;
   }
-  __device__ void advect_scalar(FT f, T *fadv, T *flux, T *rc = nullptr, T c = (T)0.) {
+  __device__ void advect_scalar(FT f, T *fadv, T *flux, T *rc = nullptr, T toff = (T)0.) {
     FT u = U(), w = W();
     FT mx = SA(), mn = SB(), uuu = SCR(p.L.s_c), www = SCR(p.L.s_d), f0 = SCR(p.L.s_e);
     FT wfl1 = SCR(p.L.s_f);
@@ -2501,14 +2505,14 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
         r.mx = mx2(mx2(mx2(mx2(fb, fc), fkb), fkc), fk);
         r.mn = mn2(mn2(mn2(mn2(fb, fc), fkb), fkc), fk);
         r.fk = fk;
-        r.uuu = mx2((T)0., uk) * (fb - c) + mn2((T)0., uk) * (fk - c);
-        r.www = mx2((T)0., wk) * (fkb - c) + mn2((T)0., wk) * (fk - c);
+        r.uuu = mx2((T)0., uk) * (fb - toff) + mn2((T)0., uk) * (fk - toff);
+        r.www = mx2((T)0., wk) * (fkb - toff) + mn2((T)0., wk) * (fk - toff);
         return r;
       },
       [&](int, const R1 &r) {
         const int i = r.i, k = r.k;
         const bool in_w = i <= nx + 2, in_m = i >= 0 && i <= nx + 1;
-        if (in_m) { mx(i, k) = r.mx; mn(i, k) = r.mn; }
+        if (in_m) { mx(i, k) = r.mx - toff; mn(i, k) = r.mn - toff; }
         if (fadv && i >= 1 && i <= nx) f0(i, k) = r.fk;
         uuu(i, k) = r.uuu;
         if (in_w) {
@@ -2531,8 +2535,8 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
         const T iadz = PR(P_IADZ)[k], irho = PR(P_IRHO)[k];
         const T c1 = (uuu(i + 1, k) - uuu(i, k) + (www(i, k + 1) - www(i, k)) * iadz) * irho;
         r.err = (T)0.;
-        if (sizeof(T) == 4 && rc && i >= 1 && i <= nx) r.fn = add_carry(f(i, k), -c1, r.err);
-        else r.fn = f(i, k) - c1;
+        if (sizeof(T) == 4 && rc && i >= 1 && i <= nx) r.fn = add_carry(f(i, k) - toff, -c1, r.err);
+        else r.fn = (f(i, k) - toff) - c1;
         return r;
       },
       [&](int, const R2 &r) {
@@ -2634,10 +2638,15 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
         if (sizeof(T) == 4 && rc) {
           r.r = rc[e];
           r.fn = add_carry(f(i, k), -c2, r.r);
+          if (toff != (T)0.) {
+            T e2 = (T)0.;
+            r.fn = add_carry(toff, r.fn, e2);
+            r.r = r.r + e2;
+          }
           if (!(r.fn > (T)0.)) { r.fn = (T)0.; r.r = (T)0.; }
         } else {
           r.r = (T)0.;
-          r.fn = mx2((T)0., f(i, k) - c2);
+          r.fn = mx2((T)0., (f(i, k) - c2) + toff);
         }
         return r;
       },
@@ -2658,7 +2667,7 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
   // advect_scalar.F90 wrapper's fadv; scratch planes: mx, mn in A, B, the
   // fluxes uuu, vvv, www in C, D, E, the initial field in F, the first-pass
   // vertical flux sum in G
-  __device__ void advect_scalar3(FT f, T *fadv, T *flux, T *rc = nullptr, T c = (T)0.) {
+  __device__ void advect_scalar3(FT f, T *fadv, T *flux, T *rc = nullptr, T toff = (T)0.) {
     FT u = U(), v = V(), w = W();
     FT mx = SA(), mn = SB(), uuu = SCR(p.L.s_c), vvv = SCR(p.L.s_d), www = SCR(p.L.s_e), f0 = SCR(p.L.s_f);
     FT wfl1 = SCR(p.L.s_g);
@@ -2676,20 +2685,20 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
         if (i >= 0 && i <= nx + 1 && j >= 0 && j <= ny + 1) {
           const T a = f(i - 1, j, k), b = f(i + 1, j, k), c = f(i, j - 1, k), d = f(i, j + 1, k);
           const T fb = f(i, j, kb), fc = f(i, j, kc), fk = f(i, j, k);
-          mx(i, j, k) = mx7(a, b, c, d, fb, fc, fk);
-          mn(i, j, k) = mn7(a, b, c, d, fb, fc, fk);
+          mx(i, j, k) = mx7(a, b, c, d, fb, fc, fk) - toff;
+          mn(i, j, k) = mn7(a, b, c, d, fb, fc, fk) - toff;
         }
         if (j <= ny + 2) {
           const T uk = u(i, j, k);
-          uuu(i, j, k) = mx2((T)0., uk) * (f(i - 1, j, k) - c) + mn2((T)0., uk) * (f(i, j, k) - c);
+          uuu(i, j, k) = mx2((T)0., uk) * (f(i - 1, j, k) - toff) + mn2((T)0., uk) * (f(i, j, k) - toff);
         }
         if (i <= nx + 2) {
           const T vk = v(i, j, k);
-          vvv(i, j, k) = mx2((T)0., vk) * (f(i, j - 1, k) - c) + mn2((T)0., vk) * (f(i, j, k) - c);
+          vvv(i, j, k) = mx2((T)0., vk) * (f(i, j - 1, k) - toff) + mn2((T)0., vk) * (f(i, j, k) - toff);
         }
         if (i <= nx + 2 && j <= ny + 2) {
           const T wk = w(i, j, k);
-          www(i, j, k) = mx2((T)0., wk) * (f(i, j, kb) - c) + mn2((T)0., wk) * (f(i, j, k) - c);
+          www(i, j, k) = mx2((T)0., wk) * (f(i, j, kb) - toff) + mn2((T)0., wk) * (f(i, j, k) - toff);
           if (k == 1) www(i, j, nz) = (T)0.;
         }
         if (fadv && i >= 1 && i <= nx && j >= 1 && j <= ny) f0(i, j, k) = f(i, j, k);
@@ -2710,10 +2719,10 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
                       (www(i, j, k + 1) - www(i, j, k)) * iadz) * irho;
         if (sizeof(T) == 4 && rc && i >= 1 && i <= nx && j >= 1 && j <= ny) {
           T err = (T)0.;
-          f(i, j, k) = add_carry(f(i, j, k), -c1, err);
+          f(i, j, k) = add_carry(f(i, j, k) - toff, -c1, err);
           rc[(size_t)(i - 1) + (size_t)nx * (j - 1) + (size_t)nxy * (k - 1)] += err;
         } else {
-          f(i, j, k) = f(i, j, k) - c1;
+          f(i, j, k) = (f(i, j, k) - toff) - c1;
         }
       }
     }
@@ -2819,11 +2828,16 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
       if (sizeof(T) == 4 && rc) {
         T r = rc[e];
         T fn = add_carry(f(i, j, k), -c2, r);
+        if (toff != (T)0.) {
+          T e2 = (T)0.;
+          fn = add_carry(toff, fn, e2);
+          r = r + e2;
+        }
         if (!(fn > (T)0.)) { fn = (T)0.; r = (T)0.; }
         f(i, j, k) = fn;
         rc[e] = r;
       } else {
-        f(i, j, k) = mx2((T)0., f(i, j, k) - c2);
+        f(i, j, k) = mx2((T)0., (f(i, j, k) - c2) + toff);
       }
     }
     SYNC;

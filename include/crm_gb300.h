@@ -53,7 +53,8 @@ enum crm_microphysics { CRM_MICRO_SAM1MOM = 0, CRM_MICRO_M2005 = 1 };
 /* CRM_FP64: every multiply and add separately rounded, bit-identical to the
  * CPU restatement; CRM_FP32_MIXED: FP32 fields and bulk arithmetic, FP64 for
  * the pressure tridiagonal solve, the conservation sums and the saturation
- * Newton iteration; CRM_FP64_FMA: FP64 with multiply-add contraction (within
+ * Newton iteration, every GCM tendency within 1e-4 relative L2 of CRM_FP64
+ * after a GCM step; CRM_FP64_FMA: FP64 with multiply-add contraction (within
  * 1e-11 relative L2 of CRM_FP64 after a GCM step, 12-14 % faster: GB300's FP64
  * pipe is the bound of the FP64 form). */
 enum crm_precision { CRM_FP64 = 0, CRM_FP32_MIXED = 1, CRM_FP64_FMA = 2 };
