@@ -984,24 +984,33 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
     // column whose state stops being finite is caught at the next step.
     bool bad = false;
     FT v = V();
-    level_max(3, 1, nzm,
-              [&](int q, int i, int k) -> T {
-                if (q == 0) { T ww = w(i, k); bad |= !isfinite(ww); return tabs_(ww); }
-                if (q == 1) {
-                  T uu = u(i, k);
-                  bad |= !isfinite(uu);
-                  if constexpr (Y3) {
-                    T vv = v(i, k);
-                    bad |= !isfinite(vv);
-                    return tsqrt(uu * uu + (T)1. * (vv * vv));
-                  }
-                  return tsqrt(uu * uu);
-                }
-                T th = tkh(i, k);
-                bad |= !isfinite(th);
-                return th;
-              },
-              [&](int q, int k, T m) { (q == 0 ? wm : q == 1 ? uhm : tkhm)[k] = m; });
+    // one warp per level takes the three maxima from one pass over the
+    // level's cells (maxima are order-independent, hence exact)
+    {
+      const int lane = TID & 31, warp = TID >> 5, nw = NT >> 5;
+      for (int k = 1 + warp; k <= nzm; k += nw) {
+        T mw = (T)0, mu = (T)0, mt = (T)0;
+        for (int i = 1 + lane; i <= NH(); i += 32) {
+          const T ww = w(i, k), uu = u(i, k), th = tkh(i, k);
+          bad |= !isfinite(ww) || !isfinite(uu) || !isfinite(th);
+          mw = mx2(mw, tabs_(ww));
+          if constexpr (Y3) {
+            const T vv = v(i, k);
+            bad |= !isfinite(vv);
+            mu = mx2(mu, tsqrt(uu * uu + (T)1. * (vv * vv)));
+          } else {
+            mu = mx2(mu, tsqrt(uu * uu));
+          }
+          mt = mx2(mt, th);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+          mw = mx2(mw, __shfl_xor_sync(0xffffffffu, mw, o));
+          mu = mx2(mu, __shfl_xor_sync(0xffffffffu, mu, o));
+          mt = mx2(mt, __shfl_xor_sync(0xffffffffu, mt, o));
+        }
+        if (lane == 0) { wm[k] = mw; uhm[k] = mu; tkhm[k] = mt; }
+      }
+    }
     if (TID == 0) wm[nz] = (T)0.;
     const int nonfinite = __syncthreads_or(bad);
     double cfl = 0.;
@@ -1179,7 +1188,9 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
         tau[k] = (T)1. / tk;
       }
     }
-    level_sums_lo(3, 1, nzm,
+    // the level means only where the sponge acts (each level's sum is
+    // independent of the others); the FP32-mixed form takes t's in FP64 below
+    level_sums_lo(sizeof(T) == 8 ? 3 : 2, max(1, nzm - n_damp), nzm,
                [&](int q, int i, int k) -> T { return (q == 0 ? u(i, k) : q == 1 ? v(i, k) : t(i, k)) / nxy; },
                [&](int, int) { return 0.; },
                [&](int q, int k, double sv) { (q == 0 ? u0l : q == 1 ? v0l : t0l)[k] = (T)sv; });
@@ -2361,19 +2372,19 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
     const T dtdx = (T)(S.dtn / p.dx), dtdz = (T)(S.dtn / S.dz), dtdy = (T)(S.dtn / p.dy);
     const T d3 = (T)S.dt3[S.na - 1], at = (T)S.at, bt = (T)S.bt, ct = (T)S.ct;
     T *rho = PR(P_RHO), *rhow = PR(P_RHOW);
-    for (int e = TID; e < NH() * nzm; e += NT) {
-      int i = 1 + e % NH(), k = 1 + e / NH();
-      T rhox = rho[k] * dtdx, rhoy = rho[k] * dtdy, rhoz = rhow[k] * dtdz;
-      T un = u(i, k) + d3 * (at * dua(i, k) + bt * dub(i, k) + ct * duc(i, k));
-      T vn = v(i, k) + d3 * (at * dva(i, k) + bt * dvb(i, k) + ct * dvc(i, k));
-      T wn = w(i, k) + d3 * (at * dwa(i, k) + bt * dwb(i, k) + ct * dwc(i, k));
-      duc(i, k) = un; dvc(i, k) = vn; dwc(i, k) = wn;
-      u(i, k) = (T)0.5 * (u(i, k) + un) * rhox;
-      v(i, k) = (T)0.5 * (v(i, k) + vn) * rhoy;
-      if constexpr (sizeof(T) == 8) w(i, k) = (T)0.5 * (w(i, k) + wn) * rhoz;
-    }
-    SYNC;
-    if constexpr (sizeof(T) == 4) {
+    if constexpr (sizeof(T) == 8) {
+      for (int e = TID; e < NH() * nzm; e += NT) {
+        int i = 1 + e % NH(), k = 1 + e / NH();
+        T rhox = rho[k] * dtdx, rhoy = rho[k] * dtdy, rhoz = rhow[k] * dtdz;
+        T un = u(i, k) + d3 * (at * dua(i, k) + bt * dub(i, k) + ct * duc(i, k));
+        T vn = v(i, k) + d3 * (at * dva(i, k) + bt * dvb(i, k) + ct * dvc(i, k));
+        T wn = w(i, k) + d3 * (at * dwa(i, k) + bt * dwb(i, k) + ct * dwc(i, k));
+        duc(i, k) = un; dvc(i, k) = vn; dwc(i, k) = wn;
+        u(i, k) = (T)0.5 * (u(i, k) + un) * rhox;
+        v(i, k) = (T)0.5 * (v(i, k) + vn) * rhoy;
+        w(i, k) = (T)0.5 * (w(i, k) + wn) * rhoz;
+      }
+    } else {
       // FP32-mixed form: the projected new w has zero horizontal mean at
       // every level in exact arithmetic (anelastic continuity, periodic
       // sides, w = 0 at the surface; the FP64 form's means are ~1e-16 of the
@@ -2382,28 +2393,36 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
       // the next advection multiply it by the level's mean value (~300 K for
       // t), which moved the level means of t by ~1e-4 of their change over a
       // call.  The mean, summed in FP64, is taken out of the new w before it
-      // forms the advecting flux (w = 0.5 (w_old + w_new) rho dt/dz).
-      T *wm = PR(P_TMP0);
+      // forms the advecting flux (w = 0.5 (w_old + w_new) rho dt/dz).  A warp
+      // per level: the level's sum is reduced by the warp that formed it and
+      // applied by the same threads to the cells they wrote.
       const int lane = TID & 31, warp = TID >> 5, nw = NT >> 5;
       const double fxy = 1. / (double)NH();
-      for (int k = 2 + warp; k <= nzm; k += nw) {
+      for (int k = 1 + warp; k <= nzm; k += nw) {
+        const T rhox = rho[k] * dtdx, rhoy = rho[k] * dtdy, rhoz = rhow[k] * dtdz;
         double sm = 0.;
-        for (int h = 1 + lane; h <= NH(); h += 32) sm = sm + (double)dwc(h, k);
-        for (int o = 16; o > 0; o >>= 1) sm = sm + __shfl_xor_sync(0xffffffffu, sm, o);
-        if (lane == 0) wm[k] = (T)(sm * fxy);
-      }
-      SYNC;
-      for (int e = TID; e < NH() * nzm; e += NT) {
-        const int i = 1 + e % NH(), k = 1 + e / NH();
-        T wn = dwc(i, k);
-        if (k >= 2) {
-          wn = wn - wm[k];
-          dwc(i, k) = wn;
+        for (int h = 1 + lane; h <= NH(); h += 32) {
+          T un = u(h, k) + d3 * (at * dua(h, k) + bt * dub(h, k) + ct * duc(h, k));
+          T vn = v(h, k) + d3 * (at * dva(h, k) + bt * dvb(h, k) + ct * dvc(h, k));
+          T wn = w(h, k) + d3 * (at * dwa(h, k) + bt * dwb(h, k) + ct * dwc(h, k));
+          duc(h, k) = un; dvc(h, k) = vn; dwc(h, k) = wn;
+          u(h, k) = (T)0.5 * (u(h, k) + un) * rhox;
+          v(h, k) = (T)0.5 * (v(h, k) + vn) * rhoy;
+          sm = sm + (double)wn;
         }
-        w(i, k) = (T)0.5 * (w(i, k) + wn) * (rhow[k] * dtdz);
+        for (int o = 16; o > 0; o >>= 1) sm = sm + __shfl_xor_sync(0xffffffffu, sm, o);
+        const T wm = k >= 2 ? (T)(sm * fxy) : (T)0.;
+        for (int h = 1 + lane; h <= NH(); h += 32) {
+          T wn = dwc(h, k);
+          if (k >= 2) {
+            wn = wn - wm;
+            dwc(h, k) = wn;
+          }
+          w(h, k) = (T)0.5 * (w(h, k) + wn) * rhoz;
+        }
       }
-      SYNC;
     }
+    SYNC;
   }
   __device__ void uvw() {                      // uvw.F90
     FT u = U(), v = V(), w = W(), duc = DU(S.nc), dvc = DV(S.nc), dwc = DW(S.nc);
