@@ -447,7 +447,7 @@ def main():
     try:
         with open(os.path.join(REPO, 'profiles', 'crm_columns_fp32_traffic.json')) as f:
             tr = json.load(f)
-        traffic = tr.get('bytes_per_launch_scaled')
+        traffic = tr.get('bytes_per_launch')
     except Exception:
         pass
     # the FP64 form is bound by the FP64 pipe (2 lanes per SM per clock on
