@@ -277,8 +277,31 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
     if constexpr (sizeof(T) == 8) {
       level_sums(nq, k0, k1, term, init, out);
     } else {
-      const int nk = k1 - k0 + 1, npairs = nq * nk;
+      const int nk = k1 - k0 + 1;
       const int lane = TID & 31, warp = TID >> 5, nw = NT >> 5;
+      if (nq <= 4) {
+        // a warp per level takes all nq quantities from one pass over the
+        // level's cells (each quantity summed in the same order as below)
+        for (int kk = warp; kk < nk; kk += nw) {
+          const int k = k0 + kk;
+          T part[4] = {(T)0, (T)0, (T)0, (T)0};
+          for (int i = 1 + lane; i <= NH(); i += 32) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+              if (q < nq) part[q] = part[q] + term(q, i, k);
+          }
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            if (q < nq) {
+              T x = part[q];
+              for (int o = 1; o < 32; o <<= 1) x = x + __shfl_xor_sync(0xffffffffu, x, o);
+              if (lane == 0) out(q, k, (double)((T)init(q, k) + x));
+            }
+          }
+        }
+        return;
+      }
+      const int npairs = nq * nk;
       for (int e = warp; e < npairs; e += nw) {
         int q = e / nk, k = k0 + e % nk;
         T part = (T)0;
