@@ -2916,7 +2916,23 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
     return term;
   }
   // part 1: terminal velocities and the column precipitation CFL number
-  __device__ void precip_fall_1() {
+  __device__ void precip_fall_1(bool qp_zero) {
+    if (qp_zero) {
+      // qp is +0 in every cell: every fall speed is zero (term_vel below
+      // returns 0 at or under the threshold), so the loops below would give
+      // a CFL of 0, no moving cell and one sub-step, and write only planes
+      // that precip_fall_2, then skipped, reads.  The batch maximum is still
+      // taken, as every column of a reference batch must arrive.
+      const double cfl_b = batch_max(0.);
+      if (TID == 0) {
+        S.prec_cfl = 0.;
+        S.prec_any = 0;
+        const double nf = ceil(cfl_b / R4(0.9));
+        S.nprec = (cfl_b > R4(0.9)) ? (nf < 1.0e4 ? (int)nf : 10000) : 1;
+      }
+      SYNC;
+      return;
+    }
     FT tabs = TABS(), qp = QP();
     FT wp = SA(), omega = SB();
     T *rho = PR(P_RHO), *rhow = PR(P_RHOW), *adz = PR(P_ADZ);
@@ -3465,6 +3481,39 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
   __device__ void diagnose() {                 // diagnose.F90:21-85
     FT t = TT(), tabs = TABS(), qcl = QCL(), qci = QCI(), qpl = QPL(), qpi = QPI(), qv = QV(), u = U(), v = V();
     T *gamaz = PR(P_GAMAZ);
+    if constexpr (sizeof(T) == 4) {
+      // FP32-mixed form: one pass, a warp per level: each lane forms tabs of
+      // its cells (the same expression as below) and adds them to the level
+      // sums, and the lane that writes the level's means forms qv0 from the
+      // FP64 means of total and condensed water right after them
+      const double coef = 1. / (double)NH();
+      double q0k = 0.;
+      level_sums_lo_multi<7>(1, nzm,
+                 [&](int, int, int) -> T { return (T)0.; },   // (FP64 form: not used)
+                 [&](int i, int k, T *r) {
+                   const T ql = qcl(i, k), qi = qci(i, k);
+                   const T tb = t(i, k) - gamaz[k] + (T)C_FAC_COND * (ql + qpl(i, k)) + (T)C_FAC_SUB * (qi + qpi(i, k));
+                   tabs(i, k) = tb;
+                   const T c = ql + qi;
+                   r[0] = u(i, k); r[1] = v(i, k); r[2] = t(i, k); r[3] = tb;
+                   r[4] = qv(i, k) + ql + qi; r[5] = c; r[6] = qpl(i, k) + qpi(i, k);
+                 },
+                 [&](int, int) { return 0.; },
+                 [&](int q, int k, double sv) {
+                   sv = sv * coef;
+                   const int ids[7] = {P_U0, P_V0, P_T0, P_TABS0, P_Q0, P_QN0, P_QP0};
+                   PR(ids[q])[k] = (T)sv;
+                   if (q == 4) q0k = sv;
+                   if (q == 5) PR(P_QV0)[k] = (T)(q0k - sv);
+                 });
+      SYNC;
+    } else {
+      diagnose_plain(t, tabs, qcl, qci, qpl, qpi, qv, u, v, gamaz);
+    }
+  }
+  // the FP64 form: tabs, then the means with one thread per (quantity,
+  // level) in the reference's order (level_sums_lo_multi), then qv0
+  __device__ void diagnose_plain(FT t, FT tabs, FT qcl, FT qci, FT qpl, FT qpi, FT qv, FT u, FT v, T *gamaz) {
     for (int e = TID; e < NH() * nzm; e += NT) {
       int i = 1 + e % NH(), k = 1 + e / NH();
       tabs(i, k) = t(i, k) - gamaz[k] + (T)C_FAC_COND * (qcl(i, k) + qpl(i, k)) + (T)C_FAC_SUB * (qci(i, k) + qpi(i, k));
@@ -3979,23 +4028,26 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
         adams();
         boundaries(2);
         PHASE_MARK(PH_ADAMS);
+        bool qp_zero;
         if constexpr (Y3) {
           advect_scalar3(TT(), nullptr, nullptr, rct(), t_offset(nstep, icyc));
           PHASE_MARK(PH_ADV_T);
           advect_scalar3(QT(), PR(P_MKADV0), PR(P_MKWLE0), rcq());
           PHASE_MARK(PH_ADV_QT);
-          if (all_pos_zero(QP())) zero_stats(PR(P_MKADV1), PR(P_MKWLE1));
+          qp_zero = all_pos_zero(QP());
+          if (qp_zero) zero_stats(PR(P_MKADV1), PR(P_MKWLE1));
           else advect_scalar3(QP(), PR(P_MKADV1), PR(P_MKWLE1));
         } else {
           advect_scalar(TT(), nullptr, nullptr, rct(), t_offset(nstep, icyc));
           PHASE_MARK(PH_ADV_T);
           advect_scalar(QT(), PR(P_MKADV0), PR(P_MKWLE0), rcq());
           PHASE_MARK(PH_ADV_QT);
-          if (all_pos_zero(QP())) zero_stats(PR(P_MKADV1), PR(P_MKWLE1));
+          qp_zero = all_pos_zero(QP());
+          if (qp_zero) zero_stats(PR(P_MKADV1), PR(P_MKWLE1));
           else advect_scalar(QP(), PR(P_MKADV1), PR(P_MKWLE1));
         }
         PHASE_MARK(PH_ADV_QP);
-        precip_fall_1();
+        precip_fall_1(qp_zero);
         PHASE_MARK(PH_FALL1);
         if (S.prec_any) precip_fall_2(S.nprec);
         PHASE_MARK(PH_FALL2);
@@ -4006,13 +4058,13 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
           diffuse_scalar3(TT(), nullptr, nullptr, rct());
           PHASE_MARK(PH_DIFF_T);
           diffuse_scalar3(QT(), PR(P_MKDIFF0), PR(P_MKWSB0), rcq());
-          if (all_pos_zero(QP())) zero_stats(PR(P_MKDIFF1), PR(P_MKWSB1));
+          if (qp_zero || all_pos_zero(QP())) zero_stats(PR(P_MKDIFF1), PR(P_MKWSB1));
           else diffuse_scalar3(QP(), PR(P_MKDIFF1), PR(P_MKWSB1));
         } else {
           diffuse_scalar(TT(), nullptr, nullptr, rct());
           PHASE_MARK(PH_DIFF_T);
           diffuse_scalar(QT(), PR(P_MKDIFF0), PR(P_MKWSB0), rcq());
-          if (all_pos_zero(QP())) zero_stats(PR(P_MKDIFF1), PR(P_MKWSB1));
+          if (qp_zero || all_pos_zero(QP())) zero_stats(PR(P_MKDIFF1), PR(P_MKWSB1));
           else diffuse_scalar(QP(), PR(P_MKDIFF1), PR(P_MKWSB1));
         }
         PHASE_MARK(PH_DIFF_Q);
