@@ -151,3 +151,24 @@ def test_fp32_mixed_reference_batch_mode(gpu_lib):
     # 5e-3 on the tendencies
     for n, b in (('temperature', 1e-5), ('qt', 2e-4), ('u_wind', 1e-3), ('sltend', 5e-3), ('qltend', 5e-3)):
         assert e[n] <= b, (n, e[n])
+
+
+@pytest.mark.parametrize('moist', [False, True])
+def test_fp32_mixed_w_has_zero_level_means(gpu_lib, moist):
+    """The projected w has zero horizontal mean at every level in exact
+    arithmetic (anelastic continuity, periodic sides, w = 0 at the surface);
+    the FP32-mixed form takes the FP32 rounding of that mean out of the new
+    w each substep, so the returned state's level means sit at the rounding
+    of the subtraction, not at the ~1e-6 of the rms that the FP32 momentum
+    and pressure phases leave."""
+    cfg, cin, st, rad, desc = S.workload_64x58(ncrms=4, moist=moist)
+    cfg.precision = T.CRM_FP32_MIXED
+    cfg.max_ncrms = desc.ld
+    out = T.CrmOutput(desc.ld, cfg.crm_nx, cfg.crm_ny, cfg.crm_nz, cfg.plev)
+    CrmContext(cfg).run(desc, cin, st, rad, out, raise_on_error=True)
+    w = st.w_wind[:4].reshape(4, cfg.crm_nx, cfg.crm_nz)        # (column, x, level)
+    rms = np.sqrt((w[:, :, 1:] ** 2).mean(axis=1))
+    mean = np.abs(w[:, :, 1:].mean(axis=1))
+    rel = np.where(rms > 0, mean / np.maximum(rms, 1e-30), 0.0)
+    print('FP32-mixed largest |level mean of w| / rms (moist=%s): %.2e' % (moist, rel.max()))
+    assert rel.max() <= 1e-7, rel.max()
