@@ -28,3 +28,21 @@ def test_reference_arm_prints_the_contract_line():
     e2e = line['e2e']
     assert e2e['h2d_bytes_per_step'] == 0 and e2e['d2h_bytes_per_step'] == 0
     assert e2e['value'] == line['value'] and e2e['unit'] == line['unit']
+
+
+def test_profile_records_the_bench_reads():
+    """The roofline inputs bench.py reads from profiles/: the DRAM bytes of
+    the bench launch itself (a one-pass capture of 1024 columns x 120 steps)
+    and the FP64 form's FP64 warp-instructions per column-step."""
+    with open(os.path.join(REPO, 'profiles', 'crm_columns_fp32_traffic.json')) as f:
+        tr = json.load(f)
+    assert tr['passes'] == 1 and tr['column_steps_in_capture'] == 1024 * 120
+    assert tr['bytes_per_launch'] == tr['dram_bytes_read'] + tr['dram_bytes_write']
+    # more than the algorithmic bytes (27 words per cell, 4 B), far below a
+    # re-read of the whole slab every phase
+    assert tr['algorithmic_bytes_per_launch'] == 1024 * 120 * 27 * 64 * 58 * 4
+    assert 1.0 < tr['bytes_per_launch'] / tr['algorithmic_bytes_per_launch'] < 20.0
+    with open(os.path.join(REPO, 'profiles', 'crm_columns_fp64_pipe.json')) as f:
+        fp = json.load(f)
+    assert fp['passes'] == 1
+    assert abs(fp['fp64_warp_inst_per_column_step'] * fp['column_steps_in_capture'] - fp['fp64_warp_instructions']) < 1.0
