@@ -405,21 +405,6 @@ struct ColumnKernel : NxDim<NX>, NyDim<NY> {
     return nullptr;
   }
 
-  // Horizontal maxima (order-independent, hence exact in both forms): one
-  // warp per (q, k) with a shuffle tree.
-  template <typename Term, typename Out>
-  __device__ void level_max(int nq, int k0, int k1, Term term, Out out) {
-    const int nk = k1 - k0 + 1, npairs = nq * nk;
-    const int lane = TID & 31, warp = TID >> 5, nw = NT >> 5;
-    for (int e = warp; e < npairs; e += nw) {
-      int q = e / nk, k = k0 + e % nk;
-      T m = (T)0;
-      for (int i = 1 + lane; i <= NH(); i += 32) m = mx2(m, term(q, i, k));
-      for (int o = 16; o > 0; o >>= 1) m = mx2(m, __shfl_xor_sync(0xffffffffu, m, o));
-      if (lane == 0) out(q, k, m);
-    }
-  }
-
   // ---------------------------------------------------------- batch coupling
   // Reference-batch mode (crm_batch_mode CRM_REFERENCE_BATCH): the column
   // kernel is a cooperative launch with one co-resident CTA per column, and
